@@ -1,0 +1,482 @@
+#!/usr/bin/env python3
+"""Throughput of the batched interval branch-and-bound hot path.
+
+Workload (N=1): the n=32 MIQCQP (4 integers in [0,7], 28 continuous in
+[-5,5], dense Q, 16 quadratic constraints at 20% density), frontier capped
+at 2^20 boxes.  One step is one device-resident batched iteration: the
+2^16 best boxes are selected, each branched into 2^4 children
+(BisectionBudget), every child bounded (fused interval evaluator) and
+sampled, then pruned and compacted into the pool -- 2^20 box evaluations
+per step.  `value` is box evaluations per second of the FP32-screen +
+FP64-certify form; the plain FP64 form, which gives identical certified
+bounds, is reported beside it.
+
+`e2e` is the same metric through the reference-facing role ABI
+(cmn_sample + cmn_bound, the RegionSampler/RegionBounder calls the
+reference's SearchDriver makes) with host buffers: one parent box per step
+split into 2^20 regions, host->device copy of the box and slots and
+device->host copy of the 2^20 verdicts inside the timed region.
+
+--impl reference times the CPU restatement of the reference path (the
+reference has no CPU evaluation backend of its own; its region evaluation
+runs only on the GPU) on all host cores over a bounded sample.
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+E_PARENTS = 1 << 16
+B_BITS = 4
+CAP = 1 << 20
+E2E_B = 20
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-ttg", action="store_true", help="skip the time-to-gap runs")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------- helpers
+class Cudart:
+    def __init__(self):
+        self.lib = None
+        for name in ("libcudart.so.13", "libcudart.so", "/usr/local/cuda/lib64/libcudart.so"):
+            try:
+                self.lib = C.CDLL(name)
+                break
+            except OSError:
+                continue
+        if self.lib is None:
+            raise RuntimeError("libcudart not found")
+
+    def set_device(self, d):
+        assert self.lib.cudaSetDevice(C.c_int(d)) == 0
+
+    def event(self):
+        ev = C.c_void_p()
+        assert self.lib.cudaEventCreate(C.byref(ev)) == 0
+        return ev
+
+    def record(self, ev, stream):
+        assert self.lib.cudaEventRecord(ev, C.c_void_p(stream)) == 0
+
+    def elapsed_ms(self, a, b):
+        assert self.lib.cudaEventSynchronize(b) == 0
+        ms = C.c_float()
+        assert self.lib.cudaEventElapsedTime(C.byref(ms), a, b) == 0
+        return ms.value
+
+    def sync(self):
+        assert self.lib.cudaDeviceSynchronize() == 0
+
+
+class Clocks:
+    """nvidia-smi sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), float(parts[3]), parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i, v in enumerate(r[3]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "power_w_max": max(r[2] for r in rows), "samples": len(rows), "reasons": reasons}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # noqa: F811
+        dist.init_process_group("gloo")
+    return world, rank, local, dist
+
+
+def reduce_max(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def reduce_sum(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+# ------------------------------------------------------------- CPU side
+def cpu_rate(problem, seconds: float, threads: int):
+    """Box evaluations per second of the oracle (CPU restatement of the
+    reference path): sample + bound of one parent's children, the
+    reference's per-iteration work, on `threads` host threads."""
+    import numpy as np
+
+    import oracle as O
+    op = O.OracleProblem(problem)
+    box = problem.root_box()
+    B = 10
+    kinds, vids, widths, _ = O.bisection_choose(box, problem.var_kinds, B)
+    N = int(np.prod(widths))
+    t0 = time.perf_counter()
+    done = 0
+    salt = 1
+    while True:
+        op.sample(box, kinds, vids, widths, N, 1, salt, threads=threads)
+        op.bound(box, kinds, vids, widths, N, threads=threads)
+        done += N
+        salt += 1
+        if time.perf_counter() - t0 >= seconds:
+            break
+    dt = time.perf_counter() - t0
+    return done / dt, {"children_per_step": N, "steps": salt - 1, "seconds": round(dt, 2)}
+
+
+def cpu_info():
+    model = "unknown"
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu model", "hardware")):
+                model = line.split(":", 1)[1].strip()
+                break
+    except OSError:
+        pass
+    return model, os.cpu_count() or 1
+
+
+# ------------------------------------------------------------- GPU side
+def solver_run(dp, rt, precision, steps, warmup):
+    from cuminlp_gb300.solver import Solver
+    s = Solver(dp, bisection_budget=B_BITS, batch_parents=E_PARENTS, frontier_cap=CAP, precision=precision,
+               sample_points=1)
+    # ramp from the root until the pool holds a full batch of parents
+    for _ in range(64):
+        s.step(1)
+        if s.outcome()["frontier_size"] >= E_PARENTS:
+            break
+    for _ in range(warmup):
+        s.step(1)
+    rt.sync()
+    before = s.outcome()["counters"]
+    ev0, ev1 = rt.event(), rt.event()
+    phases = []
+    t0 = time.perf_counter()
+    rt.record(ev0, s.stream)
+    for _ in range(steps):
+        s.step(1)
+        phases.append(phase_ms(s))
+    rt.record(ev1, s.stream)
+    ms = rt.elapsed_ms(ev0, ev1)
+    wall = (time.perf_counter() - t0) * 1e3
+    out = s.outcome()
+    after = out["counters"]
+    kpi = s_kernels(s)
+    s.close()
+    delta = {k: after[k] - before[k] for k in after}
+    return {"ms": ms, "wall_ms": wall, "delta": delta, "phases": phases, "kernels_per_iter": kpi,
+            "outcome": {k: out[k] for k in ("lower_bound", "upper_bound", "frontier_size")}}
+
+
+def phase_ms(s):
+    from cuminlp_gb300._lib import check, lib
+    arr = (C.c_double * 5)()
+    check(lib().cmn_solver_phase_ms(s.handle, arr))
+    return list(arr)
+
+
+def s_kernels(s):
+    from cuminlp_gb300._lib import lib
+    return int(lib().cmn_solver_kernels_per_iteration(s.handle))
+
+
+def fma_peak(precision):
+    from cuminlp_gb300._lib import check, lib
+    v = C.c_double()
+    check(lib().cmn_measure_fma_peak(precision, C.byref(v)))
+    return v.value
+
+
+def e2e_run(dp, problem, steps, warmup):
+    import numpy as np
+
+    import oracle as O
+    from cuminlp_gb300.solver import Bounder, Sampler
+    root = np.array(problem.box_bounds)
+    rng = np.random.default_rng(7)
+    boxes = []
+    for _ in range(steps + warmup):
+        c = rng.uniform(root[:, 0], root[:, 1])
+        w = (root[:, 1] - root[:, 0]) * 0.25
+        lo = np.maximum(c - w, root[:, 0])
+        hi = np.minimum(c + w, root[:, 1])
+        kinds = np.array(problem.var_kinds)
+        lo[kinds != 0] = np.ceil(lo[kinds != 0])
+        hi[kinds != 0] = np.maximum(np.floor(hi[kinds != 0]), lo[kinds != 0])
+        boxes.append(np.stack([lo, hi], 1).reshape(-1))
+    # one composition for all steps: the policy's choice on the first box
+    kinds, vids, widths, _ = O.bisection_choose(boxes[0], problem.var_kinds, E2E_B)
+    N = int(np.prod(widths))
+    bounder = Bounder(dp, kinds, N)
+    sampler = Sampler(dp, kinds, N, sample_points=1)
+    n = problem.n_vars
+    times = []
+    for i, box in enumerate(boxes):
+        t0 = time.perf_counter()
+        sampler.sample(box, vids, widths, salt=i + 1)
+        fe, lb = bounder.bound(box, vids, widths)
+        t = time.perf_counter() - t0
+        if i >= warmup:
+            times.append(t)
+    total = sum(times)
+    h2d = 2 * (16 * n + 64 * 40 + 16)  # box planes + slot table, for each of the two role calls
+    d2h = N * 9 + 24 + 8 * n
+    return {"value": N * len(times) / total, "unit": "boxes/s", "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h, "regions_per_call": N, "ms_per_step": 1e3 * total / len(times)}
+
+
+def time_to_gap(problem, precision, limit_s):
+    from cuminlp_gb300.solver import DeviceProblem, Solver
+    dp = DeviceProblem(problem)
+    s = Solver(dp, bisection_budget=3, batch_parents=1 << 15, frontier_cap=1 << 22, precision=precision,
+               time_limit_ms=int(limit_s * 1000), iter_limit=1 << 62)
+    t0 = time.perf_counter()
+    s.step(0)
+    dt = time.perf_counter() - t0
+    o = s.outcome()
+    s.close()
+    gap = o["upper_bound"] - o["lower_bound"]
+    rel = gap / max(1.0, abs(o["upper_bound"]))
+    return {"seconds": round(dt, 3), "converged": o["stop_reason"] == "converged",
+            "proven_optimal": bool(o["proven_optimal"]), "lower_bound": o["lower_bound"],
+            "upper_bound": o["upper_bound"], "rel_gap": rel, "boxes": o["counters"]["bounded"]}
+
+
+def run_ours(args):
+    world, rank, local, dist = dist_setup(args)
+    from cuminlp_gb300 import generators as G
+    from cuminlp_gb300.solver import DeviceProblem
+    rt = Cudart()
+    rt.set_device(local)
+    problem = G.config2(rank)  # replicas: one independent instance per GPU
+    dp = DeviceProblem(problem)
+    info = dp.info()
+    peak64 = fma_peak(0)
+    peak32 = fma_peak(1)
+
+    barrier(dist)
+    res = {}
+    with Clocks(local) as clk:
+        for prec in ("fp64", "fp32"):
+            barrier(dist)
+            res[prec] = solver_run(dp, rt, prec, args.steps, args.warmup)
+    clocks = clk.summary()
+
+    screen = res["fp32"]
+    plain = res["fp64"]
+    t_max = reduce_max(dist, screen["ms"])
+    boxes = reduce_sum(dist, screen["delta"]["bounded"])
+    value = boxes / (t_max / 1e3)
+    t_plain = reduce_max(dist, plain["ms"])
+    plain_value = reduce_sum(dist, plain["delta"]["bounded"]) / (t_plain / 1e3)
+
+    e2e = e2e_run(dp, problem, args.steps, args.warmup)
+    e2e_all = reduce_sum(dist, e2e["value"])
+
+    if rank != 0:
+        barrier(dist)
+        return
+    # live roofline of the dominant kernel: the FP64 evaluator of the plain
+    # form (phase 1 of the iteration is that kernel plus a tiny count pass)
+    ev_ms = sum(p[1] for p in plain["phases"])
+    nb = plain["delta"]["bounded"]
+    fpb = info["flops_per_box"]
+    achieved = nb * fpb / (ev_ms * 1e-3) / 1e12
+    bpb = info["bytes_per_box"]
+    hbm_gbs = nb * bpb / (ev_ms * 1e-3) / 1e9
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    traffic = None
+    tf = ROOT / "profiles" / "eval_traffic.json"
+    if tf.exists():
+        traffic = json.loads(tf.read_text()).get("dram_bytes_per_box")
+        if traffic is not None:
+            traffic = traffic * nb / max(1, len(plain["phases"]))
+
+    model, cores = cpu_info()
+    cpu_v, cpu_s = cpu_rate(problem, args.cpu_seconds, cores)
+    ttg = None
+    if not args.no_ttg:
+        p1 = G.config1()
+        ttg = {"config": "n=4 QCQP (config 1), gap 1e-6, 20 s cap each",
+               "fp64": time_to_gap(p1, "fp64", 20.0), "fp32_screen_fp64_certify": time_to_gap(p1, "fp32", 20.0)}
+
+    kpi = screen["kernels_per_iter"]
+    line = {
+        "metric": "boxes/s (batched interval B&B box evaluations, FP32 screen + FP64 certify)",
+        "value": value,
+        "unit": "boxes/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": t_max / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64 (certify) + f32 (screen)",
+        "data": "synthetic (seeded generator, config 2 shape)",
+        "config": {
+            "workload": "config2: n=32 MIQCQP (4 int [0,7], 28 cont [-5,5]), m=16 at 20% density, dense Q; "
+                        f"frontier cap 2^20; {E_PARENTS} parents x 2^{B_BITS} children per step",
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+            "l2": "box pool 2 x 512 MiB planes > 129 MB L2 (no flush needed)",
+            "dag_nodes": info["n_nodes"], "reachable_nodes": info["buffer_node_count"],
+            "program_length": info["program_length"], "program_slots": info["program_slots"],
+        },
+        "plain_fp64": {"value": plain_value, "ms_per_step": t_plain / args.steps,
+                       "phases_ms": [round(sum(p[i] for p in plain["phases"]) / len(plain["phases"]), 3)
+                                     for i in range(5)]},
+        "screen_phases_ms": [round(sum(p[i] for p in screen["phases"]) / len(screen["phases"]), 3)
+                             for i in range(5)],
+        "screen_speedup_vs_plain_fp64": value / plain_value,
+        "identical_certified_bounds": plain["outcome"] == screen["outcome"],
+        "screen_certified_fraction": screen["delta"]["certified_fp64"] / max(1, screen["delta"]["screened_fp32"]),
+        "roofline": {
+            "bound": "fp64",
+            "kernel": "eval_children_kernel<double> (fused interval DAG evaluator, plain FP64 form)",
+            "achieved": achieved, "peak": peak64, "unit": "TFLOP/s", "frac": achieved / peak64,
+            "peak_source": "measured by cmn_measure_fma_peak (DFMA loop, all SMs) in this run",
+            "flops_per_box": fpb, "boxes_per_launch": nb / len(plain["phases"]),
+            "traffic": traffic,
+            "hbm": {"achieved": hbm_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": hbm_gbs / hbm_peak,
+                    "bytes_per_box": bpb, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
+            "fp32_fma_peak_tflops": peak32,
+        },
+        "cpu_baseline": {"value": cpu_v, "unit": "boxes/s", "cores": cores, "kind": "port",
+                         "sample": f"oracle sample+bound of {cpu_s['children_per_step']} children of the root, "
+                                   f"{cpu_s['steps']} steps in {cpu_s['seconds']} s", "cpu": model},
+        "e2e": {k: e2e[k] for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step")},
+        "e2e_detail": {"regions_per_call": e2e["regions_per_call"], "ms_per_step": e2e["ms_per_step"],
+                       "all_ranks_value": e2e_all},
+        "gpu_launches": kpi * args.steps,
+        "clocks": clocks,
+        "time_to_gap": ttg,
+    }
+    print(json.dumps(line))
+    barrier(dist)
+
+
+def run_reference(args):
+    world, rank, local, dist = dist_setup(args)
+    if rank != 0:
+        return
+    from cuminlp_gb300 import generators as G
+    problem = G.config2(0)
+    model, cores = cpu_info()
+    per_step = max(2.0, min(20.0, 90.0 / max(1, args.steps + args.warmup)))
+    for _ in range(args.warmup):
+        cpu_rate(problem, per_step / 4, cores)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        v, s = cpu_rate(problem, per_step, cores)
+        vals.append(v)
+    dt = time.perf_counter() - t0
+    value = statistics.mean(vals)
+    line = {
+        "impl": "reference",
+        "metric": "boxes/s (batched interval B&B box evaluations, FP32 screen + FP64 certify)",
+        "value": value, "unit": "boxes/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded generator, config 2 shape)",
+        "config": {"workload": "config2: n=32 MIQCQP, m=16; reference path (sample + bound of one parent's "
+                               "children per iteration) on the host cores"},
+        "cpu_baseline": {"value": value, "unit": "boxes/s", "cores": cores, "kind": "port",
+                         "sample": f"per step: oracle sample+bound of {s['children_per_step']} children for "
+                                   f"~{per_step:.0f} s", "cpu": model},
+        "e2e": {"value": value, "unit": "boxes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,12 @@
+"""GB300-native interval branch-and-bound hot path (CuMINLPSearch)."""
+
+from . import _abi as abi
+from .problem import Expr, InvalidDAG, InvalidProblem, Problem, exp, log, pow, sqr, sqrt
+from .solver import (Bounder, CandidateResult, DeviceProblem, Enumerator, OverBudgetError, Sampler, Solver,
+                     default_options, eval_boxes, eval_boxes_device, solve)
+
+__all__ = [
+    "abi", "Expr", "Problem", "InvalidDAG", "InvalidProblem", "sqr", "sqrt", "exp", "log", "pow",
+    "Bounder", "Sampler", "Enumerator", "CandidateResult", "DeviceProblem", "OverBudgetError", "Solver",
+    "default_options", "eval_boxes", "eval_boxes_device", "solve",
+]

@@ -1,0 +1,1037 @@
+// capi.cu -- the C ABI: problems, region roles, raw batched evaluation and
+// the device-resident batched solver.  No exception leaves this file.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/cuminlp_gb300.h"
+#include "kernels.cuh"
+#include "launch.hpp"
+#include "program.hpp"
+#include "search.hpp"
+
+using namespace cmn;
+
+namespace {
+
+thread_local std::string g_err;
+
+cmn_status fail(cmn_status st, const std::string& msg)
+{
+  g_err = msg;
+  return st;
+}
+
+#define CK(call)                                                                                     \
+  do {                                                                                               \
+    cudaError_t e_ = (call);                                                                         \
+    if (e_ != cudaSuccess) return fail(CMN_CUDA_ERROR, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t n)
+{
+  *p = nullptr;
+  if (n == 0) n = 1;
+  return cudaMalloc(reinterpret_cast<void**>(p), n * sizeof(T));
+}
+
+void dfree(void* p)
+{
+  if (p) cudaFree(p);
+}
+
+int g_attr_device_mask = 0;
+std::mutex g_attr_mu;
+
+}  // namespace
+
+// ----------------------------------------------------------------------
+// device helpers declared in launch.hpp
+// ----------------------------------------------------------------------
+namespace cmn {
+
+int sm_count()
+{
+  int dev = 0, n = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+  return n > 0 ? n : 1;
+}
+
+int max_dynamic_smem()
+{
+  int dev = 0, n = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&n, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  return n;
+}
+
+}  // namespace cmn
+
+// kernel attribute setup lives with the kernels (eval_kernels.cu)
+namespace cmn {
+cudaError_t set_eval_kernel_attributes(int max_smem);
+int eval_kernel_occupancy(int mode, bool fp32, size_t smem, int threads);
+int sample_kernel_occupancy(size_t smem, int threads);
+}  // namespace cmn
+
+static cudaError_t ensure_attributes()
+{
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(g_attr_mu);
+  if (dev < 31 && (g_attr_device_mask & (1 << dev))) return cudaSuccess;
+  e = set_eval_kernel_attributes(max_dynamic_smem());
+  if (e == cudaSuccess && dev < 31) g_attr_device_mask |= (1 << dev);
+  return e;
+}
+
+// ----------------------------------------------------------------------
+// problem
+// ----------------------------------------------------------------------
+struct cmn_problem {
+  HostProblem host;
+  Program prog;
+  int device = 0;
+  Instr* d_prog64 = nullptr;
+  Instr* d_prog32 = nullptr;
+  int32_t* d_kinds = nullptr;
+  double* d_root_lb = nullptr;
+  double* d_root_ub = nullptr;
+
+  ~cmn_problem()
+  {
+    int cur = 0;
+    if (cudaGetDevice(&cur) == cudaSuccess && cur != device) cudaSetDevice(device);
+    dfree(d_prog64);
+    dfree(d_prog32);
+    dfree(d_kinds);
+    dfree(d_root_lb);
+    dfree(d_root_ub);
+    if (cur != device) cudaSetDevice(cur);
+  }
+};
+
+extern "C" const char* cmn_last_error(void) { return g_err.c_str(); }
+
+extern "C" const char* cmn_version(void) { return "cuminlp-gb300 0.1 (sm_103a)"; }
+
+extern "C" cmn_status cmn_problem_create(const cmn_problem_desc* desc, cmn_problem** out)
+{
+  if (out == nullptr) return fail(CMN_INVALID_CONFIGURATION, "null output pointer");
+  *out = nullptr;
+  try {
+    cmn_problem* p = new cmn_problem();
+    std::string err;
+    cmn_status st = build_host_problem(desc, p->host, err);
+    if (st != CMN_OK) {
+      delete p;
+      return fail(st, err);
+    }
+    compile_program(p->host, p->prog);
+    if (cudaGetDevice(&p->device) != cudaSuccess) {
+      delete p;
+      return fail(CMN_CUDA_ERROR, "no CUDA device");
+    }
+    const size_t L = p->prog.code64.size();
+    const int64_t n = p->host.n_vars();
+    cudaError_t e = dalloc(&p->d_prog64, L);
+    if (e == cudaSuccess) e = dalloc(&p->d_prog32, L);
+    if (e == cudaSuccess) e = dalloc(&p->d_kinds, (size_t)n);
+    if (e == cudaSuccess) e = dalloc(&p->d_root_lb, (size_t)n);
+    if (e == cudaSuccess) e = dalloc(&p->d_root_ub, (size_t)n);
+    if (e == cudaSuccess && L) e = cudaMemcpy(p->d_prog64, p->prog.code64.data(), L * sizeof(Instr), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && L) e = cudaMemcpy(p->d_prog32, p->prog.code32.data(), L * sizeof(Instr), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(p->d_kinds, p->host.var_kinds.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(p->d_root_lb, p->host.var_lb.data(), n * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(p->d_root_ub, p->host.var_ub.data(), n * sizeof(double), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      delete p;
+      return fail(CMN_CUDA_ERROR, std::string("uploading the problem: ") + cudaGetErrorString(e));
+    }
+    *out = p;
+    return CMN_OK;
+  } catch (const std::bad_alloc&) {
+    return fail(CMN_INTERNAL, "host allocation failed");
+  } catch (const std::exception& ex) {
+    return fail(CMN_INTERNAL, ex.what());
+  }
+}
+
+extern "C" void cmn_problem_destroy(cmn_problem* p) { delete p; }
+
+extern "C" cmn_status cmn_problem_get_info(const cmn_problem* p, cmn_problem_info* out)
+{
+  if (!p || !out) return fail(CMN_INVALID_CONFIGURATION, "null argument");
+  out->n_vars = p->host.n_vars();
+  out->n_constraints = (int64_t)p->host.constraints.size();
+  out->n_nodes = (int64_t)p->host.nodes.size();
+  out->buffer_node_count = p->host.buffer_node_count;
+  out->program_length = (int64_t)p->prog.code64.size();
+  out->program_slots = p->prog.n_slots;
+  out->flops_per_box = p->prog.flops_per_box;
+  out->point_flops_per_box = p->prog.point_flops_per_box;
+  out->bytes_per_box = 16.0 * (double)p->host.n_vars() + 17.0;
+  return CMN_OK;
+}
+
+static cmn_status check_interval(const cmn_problem* p)
+{
+  if (!p->prog.interval_supported)
+    return fail(CMN_INVALID_CONFIGURATION,
+                "op " + p->prog.unsupported_op + " has no interval implementation in this backend");
+  return CMN_OK;
+}
+
+static cmn_status check_smem(const cmn_problem* p, bool fp32)
+{
+  const size_t need = eval_smem_bytes((int)p->host.n_vars(), p->prog.n_slots, fp32, kEvalThreads);
+  if ((int64_t)need > (int64_t)max_dynamic_smem())
+    return fail(CMN_INVALID_CONFIGURATION, "the problem's variables and program slots need " + std::to_string(need) +
+                                               " B of shared memory per block; the device offers " +
+                                               std::to_string(max_dynamic_smem()));
+  return CMN_OK;
+}
+
+// per-role fixed device bytes: staging of one parent + reduction scratch
+static uint64_t role_fixed_bytes(const cmn_problem* p)
+{
+  return (uint64_t)(16 * p->host.n_vars() + 64 * 48 + 4096 * sizeof(Cand) + 8 * p->host.n_vars());
+}
+
+extern "C" cmn_status cmn_cost_model_get(const cmn_problem* p, cmn_cost_model* out)
+{
+  if (!p || !out) return fail(CMN_INVALID_CONFIGURATION, "null argument");
+  // The fused evaluator keeps every intermediate on chip: per region only
+  // the verdict (feasible byte + FP64 lower bound) reaches device memory,
+  // and the sampler and enumerator keep nothing per element at all.
+  out->sampler_bytes_per_sample = 0;
+  out->bound_bytes_per_region = 9;
+  out->exact_bytes_per_region = 0;
+  out->fixed_bytes = role_fixed_bytes(p);
+  return CMN_OK;
+}
+
+// ----------------------------------------------------------------------
+// roles
+// ----------------------------------------------------------------------
+struct cmn_role {
+  const cmn_problem* p = nullptr;
+  int kind = 0;
+  std::vector<uint8_t> slot_kinds;
+  uint64_t n_regions = 0;
+  uint64_t S = 1;
+  cudaStream_t stream = nullptr;
+  int grid = 1;
+  // one device block: [box lo planes n][box hi planes n][slots][pinfo]
+  unsigned char* d_stage = nullptr;
+  unsigned char* h_stage = nullptr;
+  size_t stage_bytes = 0;
+  uint8_t* d_feas = nullptr;
+  double* d_lb = nullptr;
+  Cand* d_block_best = nullptr;
+  double* d_point = nullptr;
+  uint8_t* h_feas = nullptr;
+  double* h_lb = nullptr;
+  double* h_point = nullptr;
+  Cand* h_cand = nullptr;
+
+  ~cmn_role()
+  {
+    int cur = 0;
+    if (p && cudaGetDevice(&cur) == cudaSuccess && cur != p->device) cudaSetDevice(p->device);
+    if (stream) cudaStreamSynchronize(stream);
+    dfree(d_stage);
+    dfree(d_feas);
+    dfree(d_lb);
+    dfree(d_block_best);
+    dfree(d_point);
+    if (h_stage) cudaFreeHost(h_stage);
+    if (h_feas) cudaFreeHost(h_feas);
+    if (h_lb) cudaFreeHost(h_lb);
+    if (h_point) cudaFreeHost(h_point);
+    if (h_cand) cudaFreeHost(h_cand);
+    if (stream) cudaStreamDestroy(stream);
+    if (p && cur != p->device) cudaSetDevice(cur);
+  }
+};
+
+static bool is_enum_kind(uint8_t k) { return k == CMN_SLOT_INTEGER_ENUMERATE || k == CMN_SLOT_BINARY_ENUMERATE; }
+
+extern "C" cmn_status cmn_role_build(const cmn_problem* p, int32_t role, const uint8_t* slot_kinds,
+                                     int64_t slot_count, uint64_t n_regions, uint64_t budget_bytes,
+                                     uint64_t sample_points, cmn_role** out, cmn_over_budget* facts)
+{
+  if (!p || !out) return fail(CMN_INVALID_CONFIGURATION, "null argument");
+  *out = nullptr;
+  if (role < CMN_ROLE_BOUNDER || role > CMN_ROLE_ENUMERATOR) return fail(CMN_INVALID_CONFIGURATION, "unknown role");
+  if (sample_points < 1)
+    return fail(CMN_INVALID_CONFIGURATION,
+                "sample_points must be at least 1; a point graph that samples nothing can never produce an incumbent");
+  if (slot_count < 0 || slot_count > 64) return fail(CMN_SHAPE_MISMATCH, "slot_count must be within [0, 64]");
+  if (slot_count > 0 && !slot_kinds) return fail(CMN_SHAPE_MISMATCH, "missing slot kinds");
+  for (int64_t j = 0; j < slot_count; ++j)
+    if (slot_kinds[j] > CMN_SLOT_BINARY_ENUMERATE) return fail(CMN_INVALID_CONFIGURATION, "unknown slot kind");
+  if (n_regions < 1) return fail(CMN_INVALID_CONFIGURATION, "n_regions must be at least 1");
+  if (n_regions > (1ULL << 32)) return fail(CMN_INVALID_CONFIGURATION, "n_regions above 2^32");
+  if (role == CMN_ROLE_ENUMERATOR) {
+    for (int64_t j = 0; j < slot_count; ++j)
+      if (!is_enum_kind(slot_kinds[j]))
+        return fail(CMN_INVALID_CONFIGURATION, "an enumerator needs a fully enumerable composition");
+  }
+  cmn_status st = check_interval(p);
+  if (st != CMN_OK && role == CMN_ROLE_BOUNDER) return st;
+  st = check_smem(p, false);
+  if (st != CMN_OK) return st;
+  try {
+    if (cudaSetDevice(p->device) != cudaSuccess) return fail(CMN_CUDA_ERROR, "cudaSetDevice failed");
+    CK(ensure_attributes());
+    cmn_cost_model cm;
+    cmn_cost_model_get(p, &cm);
+    const uint64_t S = role == CMN_ROLE_SAMPLER ? sample_points : 1;
+    uint64_t per = role == CMN_ROLE_BOUNDER ? cm.bound_bytes_per_region
+                   : role == CMN_ROLE_SAMPLER ? cm.sampler_bytes_per_sample * S
+                                              : cm.exact_bytes_per_region;
+    const uint64_t needed = n_regions * per + cm.fixed_bytes;
+    uint64_t budget = budget_bytes;
+    if (budget == 0) {
+      size_t fr = 0, tot = 0;
+      CK(cudaMemGetInfo(&fr, &tot));
+      budget = fr;
+    }
+    if (needed > budget) {
+      if (facts) {
+        facts->needed_bytes = needed;
+        facts->budget_bytes = budget;
+        facts->n_regions = n_regions;
+        facts->elements_per_region = S;
+        facts->bytes_per_element = per;
+      }
+      const char* names[] = {"interval graph", "point graph", "exact graph"};
+      return fail(CMN_OVER_BUDGET, std::string(names[role]) + " needs " + std::to_string(needed) +
+                                       " B of device memory, but only " + std::to_string(budget) + " B is available.");
+    }
+    cmn_role* r = new cmn_role();
+    r->p = p;
+    r->kind = role;
+    r->slot_kinds.assign(slot_kinds, slot_kinds + slot_count);
+    r->n_regions = n_regions;
+    r->S = S;
+    const int64_t n = p->host.n_vars();
+    r->stage_bytes = (size_t)(16 * n) + 64 * sizeof(SlotPlan) + sizeof(ParentInfo);
+    cudaError_t e = cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = dalloc(&r->d_stage, r->stage_bytes);
+    if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&r->h_stage), r->stage_bytes);
+    const int threads = kEvalThreads;
+    const uint64_t blocks_needed = (n_regions + threads - 1) / threads;
+    const int occ = std::max(1, eval_kernel_occupancy(0, false, eval_smem_bytes((int)n, p->prog.n_slots, false, threads), threads));
+    r->grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(blocks_needed, (uint64_t)sm_count() * occ));
+    if (role == CMN_ROLE_BOUNDER) {
+      if (e == cudaSuccess) e = dalloc(&r->d_feas, n_regions);
+      if (e == cudaSuccess) e = dalloc(&r->d_lb, n_regions);
+      if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&r->h_feas), n_regions);
+      if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&r->h_lb), n_regions * sizeof(double));
+    } else {
+      if (e == cudaSuccess) e = dalloc(&r->d_block_best, (size_t)r->grid + 1);
+      if (e == cudaSuccess) e = dalloc(&r->d_point, (size_t)n);
+      if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&r->h_point), n * sizeof(double));
+      if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&r->h_cand), sizeof(Cand));
+    }
+    if (e != cudaSuccess) {
+      delete r;
+      return fail(CMN_CUDA_ERROR, std::string("role allocation: ") + cudaGetErrorString(e));
+    }
+    *out = r;
+    return CMN_OK;
+  } catch (const std::bad_alloc&) {
+    return fail(CMN_INTERNAL, "host allocation failed");
+  }
+}
+
+extern "C" void cmn_role_destroy(cmn_role* r) { delete r; }
+
+extern "C" uint64_t cmn_role_n_regions(const cmn_role* r) { return r ? r->n_regions : 0; }
+
+extern "C" uint64_t cmn_role_n_elements(const cmn_role* r) { return r ? r->n_regions * r->S : 0; }
+
+// Stages the parent box and the per-launch slot data (var_ids, widths)
+// with one host-to-device copy (graph/replay.cuh:610-771 set_domain).
+static cmn_status stage_region(cmn_role* r, const double* box, const uint64_t* var_ids, const uint64_t* widths)
+{
+  const cmn_problem* p = r->p;
+  const int64_t n = p->host.n_vars();
+  const int64_t sc = (int64_t)r->slot_kinds.size();
+  if (!box) return fail(CMN_SHAPE_MISMATCH, "null box");
+  if (sc > 0 && (!var_ids || !widths)) return fail(CMN_SHAPE_MISMATCH, "null var_ids/widths");
+  double* lo = reinterpret_cast<double*>(r->h_stage);
+  double* hi = lo + n;
+  SlotPlan* sp = reinterpret_cast<SlotPlan*>(hi + n);
+  ParentInfo* pi = reinterpret_cast<ParentInfo*>(sp + 64);
+  for (int64_t v = 0; v < n; ++v) {
+    lo[v] = box[2 * v];
+    hi[v] = box[2 * v + 1];
+  }
+  uint64_t running = 1;
+  for (int64_t j = 0; j < sc; ++j) {
+    if (var_ids[j] >= (uint64_t)n) return fail(CMN_SHAPE_MISMATCH, "var_id out of range");
+    if (widths[j] < 1) return fail(CMN_SHAPE_MISMATCH, "slot width must be at least 1");
+    sp[j].width = widths[j];
+    sp[j].prefix = running;
+    sp[j].dom = widths[j];
+    sp[j].vid = (uint32_t)var_ids[j];
+    sp[j].kind = r->slot_kinds[j];
+    if (running > UINT64_MAX / widths[j]) running = UINT64_MAX;
+    else running *= widths[j];
+  }
+  if (running != r->n_regions)
+    return fail(CMN_SHAPE_MISMATCH, "the product of widths (" + std::to_string(running) +
+                                        ") does not equal this role's n_regions (" + std::to_string(r->n_regions) + ")");
+  pi->count = (uint32_t)sc;
+  pi->fathom = 0;
+  pi->nreg = r->n_regions;
+  CK(cudaMemcpyAsync(r->d_stage, r->h_stage, r->stage_bytes, cudaMemcpyHostToDevice, r->stream));
+  return CMN_OK;
+}
+
+static void role_ptrs(const cmn_role* r, const double*& plo, const double*& phi, const SlotPlan*& sp,
+                      const ParentInfo*& pi)
+{
+  const int64_t n = r->p->host.n_vars();
+  plo = reinterpret_cast<const double*>(r->d_stage);
+  phi = plo + n;
+  sp = reinterpret_cast<const SlotPlan*>(phi + n);
+  pi = reinterpret_cast<const ParentInfo*>(sp + 64);
+}
+
+extern "C" cmn_status cmn_bound(cmn_role* r, const double* box, const uint64_t* var_ids, const uint64_t* widths,
+                                const uint8_t** feasible, const double** obj_lb, uint64_t* n_regions)
+{
+  if (!r) return fail(CMN_INVALID_CONFIGURATION, "bound() called on a null role");
+  if (r->kind != CMN_ROLE_BOUNDER) return fail(CMN_INVALID_CONFIGURATION, "bound() called on a role that is not a bounder");
+  CK(cudaSetDevice(r->p->device));
+  cmn_status st = stage_region(r, box, var_ids, widths);
+  if (st != CMN_OK) return st;
+  EvalArgs a = {};
+  const double *plo, *phi;
+  const SlotPlan* sp;
+  const ParentInfo* pi;
+  role_ptrs(r, plo, phi, sp, pi);
+  a.prog = r->p->d_prog64;
+  a.prog_len = (int)r->p->prog.code64.size();
+  a.n_vars = (int)r->p->host.n_vars();
+  a.n_slots = r->p->prog.n_slots;
+  a.log2C = -1;
+  a.plo = plo;
+  a.phi = phi;
+  a.pstride = 1;
+  a.pinfo = pi;
+  a.slots = sp;
+  a.max_slots = 64;
+  a.n_children = r->n_regions;
+  a.out_lb = r->d_lb;
+  a.out_flag = r->d_feas;
+  CK(launch_eval(a, 0, false, r->grid, kEvalThreads, r->stream));
+  CK(cudaMemcpyAsync(r->h_feas, r->d_feas, r->n_regions, cudaMemcpyDeviceToHost, r->stream));
+  CK(cudaMemcpyAsync(r->h_lb, r->d_lb, r->n_regions * sizeof(double), cudaMemcpyDeviceToHost, r->stream));
+  CK(cudaStreamSynchronize(r->stream));
+  if (feasible) *feasible = r->h_feas;
+  if (obj_lb) *obj_lb = r->h_lb;
+  if (n_regions) *n_regions = r->n_regions;
+  return CMN_OK;
+}
+
+static cmn_status candidate_role(cmn_role* r, const double* box, const uint64_t* var_ids, const uint64_t* widths,
+                                 uint64_t salt, int exact, cmn_candidate* out)
+{
+  CK(cudaSetDevice(r->p->device));
+  cmn_status st = stage_region(r, box, var_ids, widths);
+  if (st != CMN_OK) return st;
+  const double *plo, *phi;
+  const SlotPlan* sp;
+  const ParentInfo* pi;
+  role_ptrs(r, plo, phi, sp, pi);
+  SampleArgs a = {};
+  a.prog = r->p->d_prog64;
+  a.prog_len = (int)r->p->prog.code64.size();
+  a.n_vars = (int)r->p->host.n_vars();
+  a.n_slots = r->p->prog.n_slots;
+  a.log2C = -1;
+  a.plo = plo;
+  a.phi = phi;
+  a.pstride = 1;
+  a.pinfo = pi;
+  a.slots = sp;
+  a.max_slots = 64;
+  a.var_kinds = r->p->d_kinds;
+  a.root_lb = r->p->d_root_lb;
+  a.root_ub = r->p->d_root_ub;
+  a.n_children = r->n_regions;
+  a.S = r->S;
+  a.salt = salt;
+  a.exact = exact;
+  a.block_best = r->d_block_best;
+  CK(launch_sample(a, r->grid, kEvalThreads, r->stream));
+  Cand* best = r->d_block_best + r->grid;
+  CK(launch_reduce_cand(r->d_block_best, r->grid, best, r->stream));
+  CK(launch_witness(best, plo, phi, 1, pi, sp, 64, r->p->d_kinds, a.n_vars, r->S, salt, nullptr, exact, nullptr,
+                    r->d_point, r->stream));
+  CK(cudaMemcpyAsync(r->h_cand, best, sizeof(Cand), cudaMemcpyDeviceToHost, r->stream));
+  CK(cudaMemcpyAsync(r->h_point, r->d_point, a.n_vars * sizeof(double), cudaMemcpyDeviceToHost, r->stream));
+  CK(cudaStreamSynchronize(r->stream));
+  const Cand c = *r->h_cand;
+  out->found = c.value < DBL_MAX ? 1 : 0;
+  out->reserved = 0;
+  out->value = c.value;
+  out->point = r->h_point;
+  out->index = out->found ? (int64_t)c.e : -1;
+  return CMN_OK;
+}
+
+extern "C" cmn_status cmn_sample(cmn_role* r, const double* box, const uint64_t* var_ids, const uint64_t* widths,
+                                 uint64_t salt, cmn_candidate* out)
+{
+  if (!r || !out) return fail(CMN_INVALID_CONFIGURATION, "null argument");
+  if (r->kind != CMN_ROLE_SAMPLER) return fail(CMN_INVALID_CONFIGURATION, "sample() called on a role that is not a sampler");
+  return candidate_role(r, box, var_ids, widths, salt, 0, out);
+}
+
+extern "C" cmn_status cmn_enumerate(cmn_role* r, const double* box, const uint64_t* var_ids, const uint64_t* widths,
+                                    cmn_candidate* out)
+{
+  if (!r || !out) return fail(CMN_INVALID_CONFIGURATION, "null argument");
+  if (r->kind != CMN_ROLE_ENUMERATOR)
+    return fail(CMN_INVALID_CONFIGURATION, "enumerate() called on a role that is not an enumerator");
+  return candidate_role(r, box, var_ids, widths, 0, 1, out);
+}
+
+// ----------------------------------------------------------------------
+// raw batched evaluation
+// ----------------------------------------------------------------------
+extern "C" cmn_status cmn_eval_boxes(const cmn_problem* p, int32_t precision, const double* lo, const double* hi,
+                                     uint64_t n_boxes, uint64_t stride, double* obj_lb, double* obj_ub,
+                                     uint8_t* feasible, int32_t device_pointers, void* stream)
+{
+  if (!p) return fail(CMN_INVALID_CONFIGURATION, "null problem");
+  if (precision != CMN_PRECISION_FP64 && precision != CMN_PRECISION_FP32_SCREEN)
+    return fail(CMN_INVALID_CONFIGURATION, "unknown precision");
+  if (n_boxes == 0) return CMN_OK;
+  if (!lo || !hi || !obj_lb || !feasible) return fail(CMN_SHAPE_MISMATCH, "null array");
+  if (stride < n_boxes) return fail(CMN_SHAPE_MISMATCH, "stride below n_boxes");
+  cmn_status st = check_interval(p);
+  if (st != CMN_OK) return st;
+  const bool fp32 = precision == CMN_PRECISION_FP32_SCREEN;
+  st = check_smem(p, fp32);
+  if (st != CMN_OK) return st;
+  CK(cudaSetDevice(p->device));
+  CK(ensure_attributes());
+  const int64_t n = p->host.n_vars();
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const double *dlo = lo, *dhi = hi;
+  double *dlb = obj_lb, *dub = obj_ub;
+  uint8_t* dfe = feasible;
+  double* tmp = nullptr;
+  uint8_t* tmpf = nullptr;
+  uint64_t ps = stride;
+  if (!device_pointers) {
+    ps = n_boxes;
+    const size_t planes = (size_t)n * n_boxes;
+    CK(dalloc(&tmp, 2 * planes + 2 * n_boxes));
+    CK(dalloc(&tmpf, n_boxes));
+    for (int64_t v = 0; v < n; ++v) {
+      CK(cudaMemcpyAsync(tmp + v * n_boxes, lo + v * stride, n_boxes * sizeof(double), cudaMemcpyHostToDevice, s));
+      CK(cudaMemcpyAsync(tmp + planes + v * n_boxes, hi + v * stride, n_boxes * sizeof(double), cudaMemcpyHostToDevice,
+                         s));
+    }
+    dlo = tmp;
+    dhi = tmp + planes;
+    dlb = tmp + 2 * planes;
+    dub = tmp + 2 * planes + n_boxes;
+    dfe = tmpf;
+  }
+  EvalArgs a = {};
+  a.prog = fp32 ? p->d_prog32 : p->d_prog64;
+  a.prog_len = (int)p->prog.code64.size();
+  a.n_vars = (int)n;
+  a.n_slots = p->prog.n_slots;
+  a.log2C = 0;
+  a.plo = dlo;
+  a.phi = dhi;
+  a.pstride = ps;
+  a.pinfo = nullptr;
+  a.n_children = n_boxes;
+  a.out_lb = dlb;
+  a.out_ub = dub;
+  a.out_flag = dfe;
+  const int threads = kEvalThreads;
+  const int occ = std::max(1, eval_kernel_occupancy(0, fp32, eval_smem_bytes((int)n, p->prog.n_slots, fp32, threads), threads));
+  const uint64_t need = (n_boxes + threads - 1) / threads;
+  const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(need, (uint64_t)sm_count() * occ));
+  cudaError_t e = launch_eval(a, 0, fp32, grid, threads, s);
+  if (e != cudaSuccess) {
+    dfree(tmp);
+    dfree(tmpf);
+    return fail(CMN_CUDA_ERROR, std::string("eval launch: ") + cudaGetErrorString(e));
+  }
+  if (!device_pointers) {
+    CK(cudaMemcpyAsync(obj_lb, dlb, n_boxes * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (obj_ub) CK(cudaMemcpyAsync(obj_ub, dub, n_boxes * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(feasible, dfe, n_boxes, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    dfree(tmp);
+    dfree(tmpf);
+  }
+  return CMN_OK;
+}
+
+// ----------------------------------------------------------------------
+// solver
+// ----------------------------------------------------------------------
+extern "C" void cmn_solve_options_default(cmn_solve_options* o)
+{
+  if (!o) return;
+  std::memset(o, 0, sizeof *o);
+  o->iter_limit = 1000000;
+  o->batch_iter_limit = 0;
+  o->tolerance = 1e-6;
+  o->precision = CMN_PRECISION_FP64;
+  o->bisection_budget = 4;
+  o->frontier_cap = 1ull << 20;
+  o->batch_parents = 1ull << 16;
+  o->sample_points = 1;
+  o->sample_all = 0;
+  o->relative_width = 0;
+  o->max_cycle_size = 0;
+  o->enumerate_cap = 0;
+  o->has_known_primal = 0;
+  o->known_primal_bound = 0;
+  o->time_limit_ms = 0;
+}
+
+struct cmn_solver {
+  const cmn_problem* p = nullptr;
+  cmn_solve_options opts{};
+  SolverCfg cfg{};
+  SolverBufs b{};
+  cudaStream_t stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  SolverDev* h_dev = nullptr;  // pinned mirror
+  uint64_t* d_viable = nullptr;
+  uint64_t* h_viable = nullptr;
+  std::vector<void*> allocs;
+  int eval_grid = 1, sample_grid = 1;
+  double elapsed_ms = 0;
+  uint64_t launched = 0;
+  uint64_t kernels_per_iter = 0;
+  cudaEvent_t marks[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+
+  ~cmn_solver()
+  {
+    int cur = 0;
+    if (p && cudaGetDevice(&cur) == cudaSuccess && cur != p->device) cudaSetDevice(p->device);
+    if (stream) cudaStreamSynchronize(stream);
+    for (cudaEvent_t ev : marks)
+      if (ev) cudaEventDestroy(ev);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    for (void* a : allocs) cudaFree(a);
+    if (h_dev) cudaFreeHost(h_dev);
+    if (h_viable) cudaFreeHost(h_viable);
+    if (stream) cudaStreamDestroy(stream);
+    if (p && cur != p->device) cudaSetDevice(cur);
+  }
+
+  template <typename T>
+  cudaError_t alloc(T** ptr, size_t n)
+  {
+    cudaError_t e = dalloc(ptr, n);
+    if (e == cudaSuccess) allocs.push_back(*ptr);
+    return e;
+  }
+};
+
+extern "C" cmn_status cmn_solver_create(const cmn_problem* p, const cmn_solve_options* opts, cmn_solver** out)
+{
+  if (!p || !opts || !out) return fail(CMN_INVALID_CONFIGURATION, "null argument");
+  *out = nullptr;
+  const cmn_solve_options& o = *opts;
+  if (o.bisection_budget < 1 || o.bisection_budget > 20)
+    return fail(CMN_INVALID_CONFIGURATION, "bisection_budget must be within [1, 20] for the batched solver");
+  if (o.sample_points < 1) return fail(CMN_INVALID_CONFIGURATION, "sample_points must be at least 1");
+  if (o.batch_parents < 1) return fail(CMN_INVALID_CONFIGURATION, "batch_parents must be at least 1");
+  if (o.frontier_cap < 1) return fail(CMN_INVALID_CONFIGURATION, "frontier_cap must be at least 1");
+  if (o.max_cycle_size > 64)
+    return fail(CMN_INVALID_CONFIGURATION, "max_cycle_size (" + std::to_string(o.max_cycle_size) +
+                                               ") exceeds kMaxSlots (64)");
+  if (o.precision != CMN_PRECISION_FP64 && o.precision != CMN_PRECISION_FP32_SCREEN)
+    return fail(CMN_INVALID_CONFIGURATION, "unknown precision");
+  const uint64_t C = 1ull << o.bisection_budget;
+  if ((o.batch_parents << o.bisection_budget) > (1ull << 31))
+    return fail(CMN_INVALID_CONFIGURATION, "batch_parents * 2^bisection_budget above 2^31 children per iteration");
+  if (o.frontier_cap > (1ull << 31)) return fail(CMN_INVALID_CONFIGURATION, "frontier_cap above 2^31");
+  cmn_status st = check_interval(p);
+  if (st != CMN_OK) return st;
+  st = check_smem(p, o.precision == CMN_PRECISION_FP32_SCREEN);
+  if (st != CMN_OK) return st;
+  if (sample_smem_bytes((int)p->host.n_vars(), p->prog.n_slots, kEvalThreads) > (size_t)max_dynamic_smem())
+    return fail(CMN_INVALID_CONFIGURATION, "problem too large for the sampler's shared-memory tile");
+  try {
+    CK(cudaSetDevice(p->device));
+    CK(ensure_attributes());
+    cmn_solver* s = new cmn_solver();
+    s->p = p;
+    s->opts = o;
+    SolverCfg& cfg = s->cfg;
+    const int n = (int)p->host.n_vars();
+    cfg.n_vars = n;
+    cfg.n_slots = p->prog.n_slots;
+    cfg.prog_len = (int)p->prog.code64.size();
+    cfg.log2C = o.bisection_budget;
+    cfg.max_slots = o.bisection_budget;
+    cfg.precision = o.precision;
+    cfg.sample_all = o.sample_all;
+    cfg.relative = o.relative_width;
+    cfg.S = o.sample_points;
+    cfg.e_max = o.batch_parents;
+    cfg.cap = o.frontier_cap;
+    cfg.pstride = o.frontier_cap + (o.batch_parents << o.bisection_budget);
+    cfg.iter_limit = o.iter_limit;
+    cfg.batch_iter_limit = o.batch_iter_limit;
+    cfg.max_cycle = (int64_t)o.max_cycle_size;
+    cfg.enumerate_cap = (int64_t)o.enumerate_cap;
+    cfg.tolerance = o.tolerance;
+    const uint64_t maxc = cfg.e_max * C;
+    const int threads = kEvalThreads;
+    const bool fp32 = o.precision == CMN_PRECISION_FP32_SCREEN;
+    const int occ_e = std::max(1, eval_kernel_occupancy(fp32 ? 2 : 1, fp32,
+                                                        eval_smem_bytes(n, p->prog.n_slots, fp32, threads), threads));
+    const int occ_s = std::max(1, sample_kernel_occupancy(sample_smem_bytes(n, p->prog.n_slots, threads), threads));
+    const uint64_t need = (maxc + threads - 1) / threads;
+    s->eval_grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(need, (uint64_t)sm_count() * occ_e));
+    s->sample_grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(need, (uint64_t)sm_count() * occ_s));
+
+    SolverBufs& b = s->b;
+    cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    auto A = [&](auto** ptr, size_t count) {
+      if (e == cudaSuccess) e = s->alloc(ptr, count);
+    };
+    A(&b.dev, 1);
+    A(&b.radix, 1);
+    for (int q = 0; q < 2; ++q) {
+      A(&b.lo[q], (size_t)n * cfg.pstride);
+      A(&b.hi[q], (size_t)n * cfg.pstride);
+      A(&b.lb[q], cfg.pstride);
+      A(&b.depth[q], cfg.pstride);
+    }
+    A(&b.sel, cfg.pstride);
+    A(&b.plo, (size_t)n * cfg.e_max);
+    A(&b.phi, (size_t)n * cfg.e_max);
+    A(&b.pdepth, cfg.e_max);
+    A(&b.pinfo, cfg.e_max);
+    A(&b.slots, cfg.e_max * (size_t)cfg.max_slots);
+    unsigned char* es = nullptr;
+    unsigned char* bs = nullptr;
+    A(&es, cfg.e_max * (size_t)n * 32);
+    A(&bs, cfg.e_max * (size_t)n * 40);
+    b.enum_scratch = es;
+    b.bis_scratch = bs;
+    A(&b.heap_scratch, cfg.e_max * (size_t)n);
+    A(&b.clb, maxc);
+    A(&b.cstate, maxc);
+    A(&b.list, maxc);
+    const size_t nblk = (std::max<uint64_t>(cfg.pstride, maxc) + kScanBlock - 1) / kScanBlock + 1;
+    A(&b.block_counts, nblk);
+    A(&b.block_offsets, nblk);
+    b.n_block_best = s->sample_grid + 1;
+    A(&b.block_best, (size_t)b.n_block_best);
+    A(&b.best_point, (size_t)n);
+    A(&s->d_viable, 1);
+    if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&s->h_dev), sizeof(SolverDev));
+    if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&s->h_viable), sizeof(uint64_t));
+    if (e != cudaSuccess) {
+      delete s;
+      if (e == cudaErrorMemoryAllocation)
+        return fail(CMN_OVER_BUDGET, "the solver's pools do not fit in device memory (frontier_cap / batch_parents)");
+      return fail(CMN_CUDA_ERROR, std::string("solver allocation: ") + cudaGetErrorString(e));
+    }
+    b.prog64 = p->d_prog64;
+    b.prog32 = p->d_prog32;
+    b.kinds = p->d_kinds;
+    b.root_lb = p->d_root_lb;
+    b.root_ub = p->d_root_ub;
+    const double gub0 = o.has_known_primal ? o.known_primal_bound : DBL_MAX;
+    e = solver_init(cfg, b, p->d_root_lb, p->d_root_ub, gub0, s->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b.best_point, 0xff, (size_t)n * sizeof(double), s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    for (int i = 0; i < 5 && e == cudaSuccess; ++i) e = cudaEventCreate(&s->marks[i]);
+    // capture one iteration
+    if (e == cudaSuccess) e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      cudaError_t e2 = solver_iteration(cfg, b, s->eval_grid, s->sample_grid, s->stream, s->marks);
+      e = cudaStreamEndCapture(s->stream, &s->graph);
+      if (e2 != cudaSuccess) e = e2;
+    }
+    if (e == cudaSuccess) {
+      size_t nn = 0;
+      e = cudaGraphGetNodes(s->graph, nullptr, &nn);
+      std::vector<cudaGraphNode_t> nodes(nn);
+      if (e == cudaSuccess && nn) e = cudaGraphGetNodes(s->graph, nodes.data(), &nn);
+      for (size_t i = 0; i < nn && e == cudaSuccess; ++i) {
+        cudaGraphNodeType t;
+        e = cudaGraphNodeGetType(nodes[i], &t);
+        if (t == cudaGraphNodeTypeKernel) ++s->kernels_per_iter;
+      }
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&s->exec, s->graph, 0);
+    if (e != cudaSuccess) {
+      delete s;
+      return fail(CMN_CUDA_ERROR, std::string("solver setup: ") + cudaGetErrorString(e));
+    }
+    *out = s;
+    return CMN_OK;
+  } catch (const std::bad_alloc&) {
+    return fail(CMN_INTERNAL, "host allocation failed");
+  }
+}
+
+extern "C" void cmn_solver_destroy(cmn_solver* s) { delete s; }
+
+extern "C" void* cmn_solver_stream(cmn_solver* s) { return s ? reinterpret_cast<void*>(s->stream) : nullptr; }
+
+static cmn_status pull_state(cmn_solver* s)
+{
+  CK(cudaMemcpyAsync(s->h_dev, s->b.dev, sizeof(SolverDev), cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return CMN_OK;
+}
+
+extern "C" cmn_status cmn_solver_step(cmn_solver* s, uint64_t max_iterations)
+{
+  if (!s) return fail(CMN_INVALID_CONFIGURATION, "null solver");
+  CK(cudaSetDevice(s->p->device));
+  const auto t0 = std::chrono::steady_clock::now();
+  cmn_status st = pull_state(s);
+  if (st != CMN_OK) return st;
+  uint64_t done_iters = 0;
+  uint64_t burst = 1;
+  while (!s->h_dev->done && (max_iterations == 0 || done_iters < max_iterations)) {
+    uint64_t k = burst;
+    if (max_iterations) k = std::min<uint64_t>(k, max_iterations - done_iters);
+    for (uint64_t i = 0; i < k; ++i) CK(cudaGraphLaunch(s->exec, s->stream));
+    done_iters += k;
+    s->launched += k;
+    st = pull_state(s);
+    if (st != CMN_OK) return st;
+    if (s->h_dev->error) return fail(CMN_INTERNAL, "device-side error flag set");
+    const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (s->opts.time_limit_ms && s->elapsed_ms + ms >= (double)s->opts.time_limit_ms) break;
+    if (ms < 50.0 && burst < 64) burst *= 2;
+  }
+  s->elapsed_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return CMN_OK;
+}
+
+extern "C" cmn_status cmn_query_bounds(const cmn_solver* s, double* lower_bound, double* upper_bound)
+{
+  if (!s) return fail(CMN_INVALID_CONFIGURATION, "null solver");
+  cmn_status st = pull_state(const_cast<cmn_solver*>(s));
+  if (st != CMN_OK) return st;
+  if (lower_bound) *lower_bound = s->h_dev->glb;
+  if (upper_bound) *upper_bound = s->h_dev->gub;
+  return CMN_OK;
+}
+
+extern "C" cmn_status cmn_query_gap(const cmn_solver* s, double* gap)
+{
+  double lb, ub;
+  cmn_status st = cmn_query_bounds(s, &lb, &ub);
+  if (st != CMN_OK) return st;
+  if (gap) *gap = ub - lb;
+  return CMN_OK;
+}
+
+extern "C" cmn_status cmn_query_incumbent(const cmn_solver* s, double* point, int32_t* found)
+{
+  if (!s) return fail(CMN_INVALID_CONFIGURATION, "null solver");
+  cmn_solver* m = const_cast<cmn_solver*>(s);
+  cmn_status st = pull_state(m);
+  if (st != CMN_OK) return st;
+  const bool f = s->h_dev->have_best && s->h_dev->gub < DBL_MAX;
+  if (found) *found = f ? 1 : 0;
+  if (point) {
+    CK(cudaMemcpyAsync(point, s->b.best_point, s->p->host.n_vars() * sizeof(double), cudaMemcpyDeviceToHost,
+                       m->stream));
+    CK(cudaStreamSynchronize(m->stream));
+    if (!f)
+      for (int64_t v = 0; v < s->p->host.n_vars(); ++v) point[v] = NAN;
+  }
+  return CMN_OK;
+}
+
+extern "C" cmn_status cmn_solver_frontier(cmn_solver* s, double* boxes, double* lower_bounds, uint32_t* depths,
+                                          uint64_t room, uint64_t* count)
+{
+  if (!s) return fail(CMN_INVALID_CONFIGURATION, "null solver");
+  CK(cudaSetDevice(s->p->device));
+  cmn_status st = pull_state(s);
+  if (st != CMN_OK) return st;
+  const uint64_t L = s->h_dev->pool_size;
+  if (count) *count = L;
+  const uint64_t m = std::min(L, room);
+  if (m == 0) return CMN_OK;
+  const uint32_t q = s->h_dev->parity;
+  const int64_t n = s->p->host.n_vars();
+  if (boxes) {
+    std::vector<double> plane(m);
+    for (int64_t v = 0; v < n; ++v) {
+      for (int side = 0; side < 2; ++side) {
+        const double* src = (side == 0 ? s->b.lo[q] : s->b.hi[q]) + (uint64_t)v * s->cfg.pstride;
+        CK(cudaMemcpyAsync(plane.data(), src, m * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        for (uint64_t i = 0; i < m; ++i) boxes[i * 2 * n + 2 * v + side] = plane[i];
+      }
+    }
+  }
+  if (lower_bounds) CK(cudaMemcpyAsync(lower_bounds, s->b.lb[q], m * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  if (depths) CK(cudaMemcpyAsync(depths, s->b.depth[q], m * sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return CMN_OK;
+}
+
+static bool gap_closed_host(double gub, double bound, double tol)
+{
+  return gub - bound <= tol * std::max(1.0, std::fabs(gub));
+}
+
+extern "C" cmn_status cmn_solver_outcome(cmn_solver* s, cmn_outcome* out)
+{
+  if (!s || !out) return fail(CMN_INVALID_CONFIGURATION, "null argument");
+  CK(cudaSetDevice(s->p->device));
+  CK(solver_pool_stats(s->cfg, s->b, s->d_viable, s->stream));
+  CK(cudaMemcpyAsync(s->h_viable, s->d_viable, sizeof(uint64_t), cudaMemcpyDeviceToHost, s->stream));
+  cmn_status st = pull_state(s);
+  if (st != CMN_OK) return st;
+  const SolverDev& d = *s->h_dev;
+  const double tol = s->opts.tolerance;
+  const bool pending_empty = d.pool_size == 0;
+  const double frontier_min = pending_empty ? DBL_MAX : [&] {
+    const uint64_t k = d.pool_min_key;
+    const uint64_t u = (k >> 63) ? (k & 0x7fffffffffffffffULL) : ~k;
+    double x;
+    std::memcpy(&x, &u, 8);
+    return x;
+  }();
+  const bool found = d.gub < DBL_MAX;
+  const uint64_t viable = *s->h_viable;
+  std::memset(out, 0, sizeof *out);
+  // finalise_bounds (search/epilogue.hpp:89-127)
+  const double dropped_min = d.dropped_lb_min;
+  const bool lost_nothing = d.counters.dropped_viable == 0;
+  out->proven_optimal =
+      found && (d.converged || pending_empty || viable == 0) && gap_closed_host(d.gub, dropped_min, tol);
+  if (out->proven_optimal) {
+    out->lower_bound = d.gub;
+  } else if (pending_empty && lost_nothing) {
+    out->infeasible = 1;
+    out->lower_bound = d.glb;
+  } else {
+    double g = std::min(pending_empty ? DBL_MAX : frontier_min, dropped_min);
+    if (found) g = std::min(g, d.gub);
+    out->lower_bound = g;
+  }
+  out->upper_bound = d.gub;
+  if (!d.done) {
+    out->stop_reason = CMN_STOP_RUNNING;
+  } else if (d.converged) {
+    out->stop_reason = CMN_STOP_CONVERGED;
+  } else {
+    out->stop_reason = pending_empty ? CMN_STOP_EXHAUSTED
+                       : gap_closed_host(d.gub, d.glb, tol) ? CMN_STOP_CONVERGED
+                                                            : CMN_STOP_ITERATION_LIMIT;
+  }
+  out->found_incumbent = found ? 1 : 0;
+  out->frontier_size = d.pool_size;
+  out->viable = viable;
+  out->dropped_lb_min = dropped_min;
+  out->elapsed_ms = s->elapsed_ms;
+  out->counters = d.counters;
+  out->counters.iterations = d.iterations;
+  out->counters.expansions = d.expansions;
+  return CMN_OK;
+}
+
+extern "C" cmn_status cmn_solver_phase_ms(cmn_solver* s, double* ms5)
+{
+  if (!s || !ms5) return fail(CMN_INVALID_CONFIGURATION, "null argument");
+  CK(cudaEventSynchronize(s->marks[4]));
+  float t = 0;
+  for (int i = 0; i < 4; ++i) {
+    CK(cudaEventElapsedTime(&t, s->marks[i], s->marks[i + 1]));
+    ms5[i] = t;
+  }
+  CK(cudaEventElapsedTime(&t, s->marks[0], s->marks[4]));
+  ms5[4] = t;
+  return CMN_OK;
+}
+
+extern "C" uint64_t cmn_solver_kernels_per_iteration(const cmn_solver* s) { return s ? s->kernels_per_iter : 0; }
+
+namespace cmn {
+cudaError_t launch_fma_peak(int precision, int grid, int threads, int iters, void* sink, cudaStream_t s);
+}
+
+extern "C" cmn_status cmn_measure_fma_peak(int32_t precision, double* tflops)
+{
+  if (!tflops) return fail(CMN_INVALID_CONFIGURATION, "null argument");
+  const int threads = 256, iters = 4096;
+  const int grid = sm_count() * 8;
+  void* sink = nullptr;
+  CK(cudaMalloc(&sink, (size_t)grid * threads * sizeof(double)));
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  CK(launch_fma_peak(precision, grid, threads, iters, sink, nullptr));  // warm-up
+  CK(cudaEventRecord(a, nullptr));
+  const int reps = 5;
+  for (int r = 0; r < reps; ++r) CK(launch_fma_peak(precision, grid, threads, iters, sink, nullptr));
+  CK(cudaEventRecord(b, nullptr));
+  CK(cudaEventSynchronize(b));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(sink);
+  // 8 independent FMA chains per thread per iteration, 2 flops each
+  const double flops = 2.0 * 8.0 * iters * (double)grid * threads * reps;
+  *tflops = flops / (ms * 1e-3) / 1e12;
+  return CMN_OK;
+}
+
+extern "C" cmn_status cmn_solve(const cmn_problem* p, const cmn_solve_options* opts, cmn_outcome* outcome,
+                                double* best_point)
+{
+  cmn_solver* s = nullptr;
+  cmn_status st = cmn_solver_create(p, opts, &s);
+  if (st != CMN_OK) return st;
+  st = cmn_solver_step(s, 0);
+  if (st == CMN_OK && outcome) st = cmn_solver_outcome(s, outcome);
+  if (st == CMN_OK && best_point) {
+    int32_t found = 0;
+    st = cmn_query_incumbent(s, best_point, &found);
+  }
+  cmn_solver_destroy(s);
+  return st;
+}

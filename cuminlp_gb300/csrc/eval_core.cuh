@@ -1,0 +1,565 @@
+// eval_core.cuh -- device arithmetic and the fused DAG interpreter.
+//
+// Interval operators return the tightest enclosure under IEEE-754 directed
+// rounding (the semantics of the reference's interval library for the
+// operator set of graph/ops.cuh:24-355).  They use the CUDA directed
+// rounding intrinsics only (__dadd_rd, __dmul_ru, __fmul_rd, ...), never
+// plain expressions, so no FMA contraction can change a bound.
+//
+// The multiplication picks the extreme corner products from the operand
+// sign classes (two products; four only when both operands straddle zero),
+// instead of forming all eight directed products.  Sign classes come from
+// the sign bits (integer pipe), leaving the FP64 pipe to the products.
+#pragma once
+
+#include <cstdint>
+
+#include "program.h"
+
+namespace cmn {
+
+template <typename T>
+struct Iv {
+  T lo, hi;
+};
+
+template <typename T>
+struct Arith;
+
+template <>
+struct Arith<double> {
+  static __device__ __forceinline__ double add_rd(double a, double b) { return __dadd_rd(a, b); }
+  static __device__ __forceinline__ double add_ru(double a, double b) { return __dadd_ru(a, b); }
+  static __device__ __forceinline__ double sub_rd(double a, double b) { return __dsub_rd(a, b); }
+  static __device__ __forceinline__ double sub_ru(double a, double b) { return __dsub_ru(a, b); }
+  static __device__ __forceinline__ double mul_rd(double a, double b) { return __dmul_rd(a, b); }
+  static __device__ __forceinline__ double mul_ru(double a, double b) { return __dmul_ru(a, b); }
+  static __device__ __forceinline__ double div_rd(double a, double b) { return __ddiv_rd(a, b); }
+  static __device__ __forceinline__ double div_ru(double a, double b) { return __ddiv_ru(a, b); }
+  static __device__ __forceinline__ double sqrt_rd(double a) { return __dsqrt_rd(a); }
+  static __device__ __forceinline__ double sqrt_ru(double a) { return __dsqrt_ru(a); }
+  static __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+  static __device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+  static __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+  static __device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
+  static __device__ __forceinline__ double sqrt_rn(double a) { return __dsqrt_rn(a); }
+  // sign bit set (negative, -0 or negative NaN)
+  static __device__ __forceinline__ bool sgn(double x) { return __double2hiint(x) < 0; }
+  static __device__ __forceinline__ bool is_zero(double x)
+  {
+    return ((__double2hiint(x) & 0x7fffffff) | __double2loint(x)) == 0;
+  }
+  // a > b for two non-negative values (sign bit clear), on the integer pipe
+  static __device__ __forceinline__ bool gt_nonneg(double a, double b)
+  {
+    return __double_as_longlong(a) > __double_as_longlong(b);
+  }
+  static __device__ __forceinline__ double inf() { return __longlong_as_double(0x7ff0000000000000LL); }
+  static __device__ __forceinline__ double nan() { return __longlong_as_double(0x7ff8000000000000LL); }
+};
+
+template <>
+struct Arith<float> {
+  static __device__ __forceinline__ float add_rd(float a, float b) { return __fadd_rd(a, b); }
+  static __device__ __forceinline__ float add_ru(float a, float b) { return __fadd_ru(a, b); }
+  static __device__ __forceinline__ float sub_rd(float a, float b) { return __fsub_rd(a, b); }
+  static __device__ __forceinline__ float sub_ru(float a, float b) { return __fsub_ru(a, b); }
+  static __device__ __forceinline__ float mul_rd(float a, float b) { return __fmul_rd(a, b); }
+  static __device__ __forceinline__ float mul_ru(float a, float b) { return __fmul_ru(a, b); }
+  static __device__ __forceinline__ float div_rd(float a, float b) { return __fdiv_rd(a, b); }
+  static __device__ __forceinline__ float div_ru(float a, float b) { return __fdiv_ru(a, b); }
+  static __device__ __forceinline__ float sqrt_rd(float a) { return __fsqrt_rd(a); }
+  static __device__ __forceinline__ float sqrt_ru(float a) { return __fsqrt_ru(a); }
+  static __device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+  static __device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+  static __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+  static __device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, b); }
+  static __device__ __forceinline__ float sqrt_rn(float a) { return __fsqrt_rn(a); }
+  static __device__ __forceinline__ bool sgn(float x) { return __float_as_int(x) < 0; }
+  static __device__ __forceinline__ bool is_zero(float x) { return (__float_as_int(x) & 0x7fffffff) == 0; }
+  static __device__ __forceinline__ bool gt_nonneg(float a, float b)
+  {
+    return __float_as_int(a) > __float_as_int(b);
+  }
+  static __device__ __forceinline__ float inf() { return __int_as_float(0x7f800000); }
+  static __device__ __forceinline__ float nan() { return __int_as_float(0x7fc00000); }
+};
+
+// x*y for interval endpoints: a zero factor gives +0 even against an
+// infinite bound (IEEE 1788), never NaN.
+template <typename T>
+__device__ __forceinline__ T emul_rd(T x, T y)
+{
+  using A = Arith<T>;
+  return (A::is_zero(x) | A::is_zero(y)) ? T(0) : A::mul_rd(x, y);
+}
+template <typename T>
+__device__ __forceinline__ T emul_ru(T x, T y)
+{
+  using A = Arith<T>;
+  return (A::is_zero(x) | A::is_zero(y)) ? T(0) : A::mul_ru(x, y);
+}
+
+template <typename T>
+__device__ __forceinline__ Iv<T> iv_add(Iv<T> a, Iv<T> b)
+{
+  return {Arith<T>::add_rd(a.lo, b.lo), Arith<T>::add_ru(a.hi, b.hi)};
+}
+
+template <typename T>
+__device__ __forceinline__ Iv<T> iv_sub(Iv<T> a, Iv<T> b)
+{
+  return {Arith<T>::sub_rd(a.lo, b.hi), Arith<T>::sub_ru(a.hi, b.lo)};
+}
+
+template <typename T>
+__device__ __forceinline__ Iv<T> iv_neg(Iv<T> a)
+{
+  return {-a.hi, -a.lo};
+}
+
+// Tightest product.  Sign classes: pos (lo has no sign bit), neg (hi has
+// the sign bit), mixed otherwise.  A zero endpoint may land in either
+// class; the chosen corner products then differ only in the sign of a zero.
+template <typename T>
+__device__ __forceinline__ Iv<T> iv_mul(Iv<T> a, Iv<T> b)
+{
+  using A = Arith<T>;
+  const bool ap = !A::sgn(a.lo), an = A::sgn(a.hi);
+  const bool bp = !A::sgn(b.lo), bn = A::sgn(b.hi);
+  const bool am = !ap && !an, bm = !bp && !bn;
+  const T la = ap ? (bp ? a.lo : a.hi) : (an ? (bn ? a.hi : a.lo) : (bn ? a.hi : a.lo));
+  const T lb = ap ? b.lo : (an ? b.hi : (bn ? b.lo : b.hi));
+  const T ua = ap ? (bn ? a.lo : a.hi) : (an ? (bp ? a.hi : a.lo) : (bn ? a.lo : a.hi));
+  const T ub = ap ? b.hi : (an ? b.lo : (bn ? b.lo : b.hi));
+  Iv<T> r = {emul_rd(la, lb), emul_ru(ua, ub)};
+  const bool mm = am && bm;
+  if (__any_sync(__activemask(), mm)) {
+    const T l2 = emul_rd(a.hi, b.lo);
+    const T u2 = emul_ru(a.lo, b.lo);
+    if (mm) {
+      r.lo = l2 < r.lo ? l2 : r.lo;
+      r.hi = u2 > r.hi ? u2 : r.hi;
+    }
+  }
+  return r;
+}
+
+template <typename T>
+__device__ __forceinline__ Iv<T> iv_sqr(Iv<T> a)
+{
+  using A = Arith<T>;
+  const bool p = !A::sgn(a.lo), n = A::sgn(a.hi);
+  const T mlo = -a.lo;
+  const T mag = A::gt_nonneg(mlo, a.hi) ? mlo : a.hi;  // mixed: both >= 0
+  const T lo_op = p ? a.lo : (n ? a.hi : T(0));
+  const T hi_op = p ? a.hi : (n ? a.lo : mag);
+  return {emul_rd(lo_op, lo_op), emul_ru(hi_op, hi_op)};
+}
+
+template <typename T>
+__device__ __forceinline__ T tmin(T a, T b) { return a < b ? a : b; }
+template <typename T>
+__device__ __forceinline__ T tmax(T a, T b) { return a > b ? a : b; }
+
+template <typename T>
+__device__ Iv<T> iv_div(Iv<T> a, Iv<T> b)
+{
+  using A = Arith<T>;
+  Iv<T> r;
+  if (b.lo > T(0) || b.hi < T(0)) {
+    const T l1 = A::div_rd(a.lo, b.lo), l2 = A::div_rd(a.lo, b.hi);
+    const T l3 = A::div_rd(a.hi, b.lo), l4 = A::div_rd(a.hi, b.hi);
+    const T u1 = A::div_ru(a.lo, b.lo), u2 = A::div_ru(a.lo, b.hi);
+    const T u3 = A::div_ru(a.hi, b.lo), u4 = A::div_ru(a.hi, b.hi);
+    r.lo = tmin(tmin(l1, l2), tmin(l3, l4));
+    r.hi = tmax(tmax(u1, u2), tmax(u3, u4));
+    return r;
+  }
+  if (b.lo == T(0) && b.hi == T(0)) return {A::nan(), A::nan()};
+  if (b.lo == T(0)) {
+    if (a.lo >= T(0)) return {A::div_rd(a.lo, b.hi), A::inf()};
+    if (a.hi <= T(0)) return {-A::inf(), A::div_ru(a.hi, b.hi)};
+  } else if (b.hi == T(0)) {
+    if (a.lo >= T(0)) return {-A::inf(), A::div_ru(a.lo, b.lo)};
+    if (a.hi <= T(0)) return {A::div_rd(a.hi, b.lo), A::inf()};
+  }
+  return {-A::inf(), A::inf()};
+}
+
+template <typename T>
+__device__ __forceinline__ Iv<T> iv_sqrt(Iv<T> a)
+{
+  using A = Arith<T>;
+  if (a.hi < T(0)) return {A::nan(), A::nan()};
+  return {a.lo > T(0) ? A::sqrt_rd(a.lo) : T(0), A::sqrt_ru(a.hi)};
+}
+
+template <typename T>
+__device__ __forceinline__ Iv<T> iv_abs(Iv<T> a)
+{
+  if (a.lo >= T(0)) return a;
+  if (a.hi <= T(0)) return {-a.hi, -a.lo};
+  return {T(0), tmax(-a.lo, a.hi)};
+}
+
+template <typename T>
+__device__ __forceinline__ T powu_rd(T a, int k)
+{
+  T r = T(1), base = a;
+  while (k > 0) {
+    if (k & 1) r = emul_rd(r, base);
+    k >>= 1;
+    if (k > 0) base = emul_rd(base, base);
+  }
+  return r;
+}
+
+template <typename T>
+__device__ __forceinline__ T powu_ru(T a, int k)
+{
+  T r = T(1), base = a;
+  while (k > 0) {
+    if (k & 1) r = emul_ru(r, base);
+    k >>= 1;
+    if (k > 0) base = emul_ru(base, base);
+  }
+  return r;
+}
+
+template <typename T>
+__device__ Iv<T> iv_pown(Iv<T> a, int k)
+{
+  if (k == 0) return {T(1), T(1)};
+  if (k == 1) return a;
+  if (k == 2) {
+    // same classes as the oracle's sqr for pown(x, 2)
+    return iv_sqr(a);
+  }
+  if (k < 0) {
+    Iv<T> one = {T(1), T(1)};
+    return iv_div(one, iv_pown(a, -k));
+  }
+  if ((k & 1) == 0) {
+    const T mig = a.lo > T(0) ? a.lo : (a.hi < T(0) ? -a.hi : T(0));
+    const T mag = tmax(a.lo < T(0) ? -a.lo : a.lo, a.hi < T(0) ? -a.hi : a.hi);
+    return {powu_rd(mig, k), powu_ru(mag, k)};
+  }
+  return {a.lo >= T(0) ? powu_rd(a.lo, k) : -powu_ru(-a.lo, k),
+          a.hi >= T(0) ? powu_ru(a.hi, k) : -powu_rd(-a.hi, k)};
+}
+
+template <typename T>
+__device__ __forceinline__ Iv<T> iv_generic(uint8_t op, Iv<T> a, Iv<T> b, int k)
+{
+  switch (op) {
+    case kGAdd: return iv_add(a, b);
+    case kGSub: return iv_sub(a, b);
+    case kGMul: return iv_mul(a, b);
+    case kGDiv: return iv_div(a, b);
+    case kGSqr: return iv_sqr(a);
+    case kGNeg: return iv_neg(a);
+    case kGSqrt: return iv_sqrt(a);
+    case kGPowN: return iv_pown(a, k);
+    case kGAbs: return iv_abs(a);
+    case kGMin: return {tmin(a.lo, b.lo), tmin(a.hi, b.hi)};
+    case kGMax: return {tmax(a.lo, b.lo), tmax(a.hi, b.hi)};
+    default: return {Arith<T>::nan(), Arith<T>::nan()};
+  }
+}
+
+// Point arithmetic: one round-to-nearest operation per DAG node
+// (graph/ops.cuh point overloads).
+__device__ __forceinline__ double pt_generic(uint8_t op, double a, double b, int k)
+{
+  using A = Arith<double>;
+  switch (op) {
+    case kGAdd: return A::add_rn(a, b);
+    case kGSub: return A::sub_rn(a, b);
+    case kGMul: return A::mul_rn(a, b);
+    case kGDiv: return A::div_rn(a, b);
+    case kGSqr: return A::mul_rn(a, a);
+    case kGNeg: return -a;
+    case kGSqrt: return A::sqrt_rn(a);
+    case kGPowN: return k == 2 ? A::mul_rn(a, a) : pow(a, (double)k);
+    case kGAbs: return fabs(a);
+    case kGMin: return fmin(a, b);
+    case kGMax: return fmax(a, b);
+    default: return A::nan();
+  }
+}
+
+// The value of one variable / slot for this thread: shared-memory planes,
+// plane-major with `stride` entries per plane, this thread at `tid`.
+template <typename T>
+struct Tile {
+  T* lo;  // n_vars planes
+  T* hi;
+  T* slo;  // program slots
+  T* shi;
+  int stride;
+  int tid;
+  __device__ __forceinline__ Iv<T> var(int v) const { return {lo[v * stride + tid], hi[v * stride + tid]}; }
+  __device__ __forceinline__ Iv<T> slot(int s) const { return {slo[s * stride + tid], shi[s * stride + tid]}; }
+  __device__ __forceinline__ void set_slot(int s, Iv<T> x) const
+  {
+    slo[s * stride + tid] = x.lo;
+    shi[s * stride + tid] = x.hi;
+  }
+};
+
+__device__ __forceinline__ Instr load_instr(const Instr* prog, int pc)
+{
+  int4 raw = __ldg(reinterpret_cast<const int4*>(prog) + pc);
+  Instr ins;
+  memcpy(&ins, &raw, sizeof(Instr));
+  return ins;
+}
+
+// Operand of an interval program.  FP64 constants are point intervals; FP32
+// constants carry their outward-rounded pair.
+template <typename T>
+__device__ __forceinline__ Iv<T> const_of(const Instr& ins);
+template <>
+__device__ __forceinline__ Iv<double> const_of<double>(const Instr& ins)
+{
+  return {ins.c, ins.c};
+}
+template <>
+__device__ __forceinline__ Iv<float> const_of<float>(const Instr& ins)
+{
+  return {ins.c32.clo, ins.c32.chi};
+}
+
+template <typename T>
+__device__ __forceinline__ Iv<T> fetch(const Tile<T>& t, const Iv<T>& acc, const Instr& ins, int mode, int idx)
+{
+  switch (mode) {
+    case kModeSlot: return t.slot(idx);
+    case kModeVar: return t.var(idx);
+    case kModeAcc: return acc;
+    default: return const_of<T>(ins);
+  }
+}
+
+// Result of interpreting the program on one box.
+template <typename T>
+struct Verdict {
+  Iv<T> obj;
+  bool feasible;    // FP64: reference predicate (NaN lb -> infeasible)
+  bool excluded;    // a constraint is proven violated (NaN never excludes)
+};
+
+// Interval interpretation of `prog` for this thread's box.
+template <typename T>
+__device__ Verdict<T> run_interval(const Instr* __restrict__ prog, int len, const Tile<T>& t)
+{
+  using A = Arith<T>;
+  Iv<T> acc = {T(0), T(0)};
+  Verdict<T> out;
+  out.obj = {A::nan(), A::nan()};
+  out.feasible = true;
+  out.excluded = false;
+  Instr ins = len > 0 ? load_instr(prog, 0) : Instr{};
+  for (int pc = 0; pc < len; ++pc) {
+    const Instr cur = ins;
+    if (pc + 1 < len) ins = load_instr(prog, pc + 1);  // software prefetch
+    const int code = cur.head & 7;
+    const int sub = cur.head >> 3;
+    switch (code) {
+      case kOpTerm: {
+        Iv<T> p;
+        const int pk = sub & kTermPMask;
+        if (pk == kTermProd) {
+          p = iv_mul(t.var(cur.a), t.var(cur.b));
+        } else if (pk == kTermSqr) {
+          p = iv_sqr(t.var(cur.a));
+        } else {
+          p = t.var(cur.a);
+        }
+        if (sub & kTermHasC) p = iv_mul(const_of<T>(cur), p);
+        if (sub & kTermInit) acc = p;
+        else if (sub & kTermSub) acc = iv_sub(acc, p);
+        else acc = iv_add(acc, p);
+        break;
+      }
+      case kOpGeneric: {
+        const Iv<T> a = fetch(t, acc, cur, cur.modes & 3, cur.a);
+        const Iv<T> b = fetch(t, acc, cur, (cur.modes >> 2) & 3, cur.b);
+        t.set_slot(cur.dst, iv_generic<T>((uint8_t)sub, a, b, (int)(int16_t)cur.b));
+        break;
+      }
+      case kOpStoreAcc:
+        t.set_slot(cur.dst, acc);
+        break;
+      case kOpLoadAcc:
+        acc = fetch(t, acc, cur, cur.modes & 3, cur.a);
+        break;
+      case kOpConstToSlot:
+        t.set_slot(cur.dst, const_of<T>(cur));
+        break;
+      case kOpCheck: {
+        const Iv<T> v = fetch(t, acc, cur, cur.modes & 3, cur.a);
+        // rhs is kept in FP64 for both precisions; compare in FP64 exactly
+        const double rhs = cur.c;
+        const double lo = (double)v.lo, hi = (double)v.hi;
+        if (sub == 0) {
+          out.feasible = out.feasible && (lo <= rhs);
+          out.excluded = out.excluded || (lo > rhs);
+        } else {
+          out.feasible = out.feasible && (lo <= rhs && rhs <= hi);
+          out.excluded = out.excluded || (lo > rhs || hi < rhs);
+        }
+        break;
+      }
+      case kOpObjective:
+        out.obj = fetch(t, acc, cur, cur.modes & 3, cur.a);
+        break;
+      default:
+        break;
+    }
+  }
+  return out;
+}
+
+// Point interpretation (FP64 round-to-nearest) for this thread's point,
+// held in t.lo; slots use t.slo.  Feasibility follows the point predicates
+// of graph/kernels.cuh:283-320 (LE exact; EQ abs 1e-8 / rel 1e-6).
+__device__ __forceinline__ bool almost_equal(double a, double b)
+{
+  const double diff = fabs(__dsub_rn(a, b));
+  if (diff <= 1e-8) return true;
+  return diff <= __dmul_rn(1e-6, fmax(fabs(a), fabs(b)));
+}
+
+struct PointVerdict {
+  double obj;
+  bool feasible;
+};
+
+__device__ __forceinline__ double pfetch(const Tile<double>& t, double acc, const Instr& ins, int mode, int idx)
+{
+  switch (mode) {
+    case kModeSlot: return t.slo[idx * t.stride + t.tid];
+    case kModeVar: return t.lo[idx * t.stride + t.tid];
+    case kModeAcc: return acc;
+    default: return ins.c;
+  }
+}
+
+__device__ inline PointVerdict run_point(const Instr* __restrict__ prog, int len, const Tile<double>& t)
+{
+  using A = Arith<double>;
+  double acc = 0.0;
+  PointVerdict out;
+  out.obj = A::nan();
+  out.feasible = true;
+  Instr ins = len > 0 ? load_instr(prog, 0) : Instr{};
+  for (int pc = 0; pc < len; ++pc) {
+    const Instr cur = ins;
+    if (pc + 1 < len) ins = load_instr(prog, pc + 1);
+    const int code = cur.head & 7;
+    const int sub = cur.head >> 3;
+    switch (code) {
+      case kOpTerm: {
+        double p;
+        const int pk = sub & kTermPMask;
+        const double xa = t.lo[cur.a * t.stride + t.tid];
+        if (pk == kTermProd) {
+          p = A::mul_rn(xa, t.lo[cur.b * t.stride + t.tid]);
+        } else if (pk == kTermSqr) {
+          p = A::mul_rn(xa, xa);
+        } else {
+          p = xa;
+        }
+        if (sub & kTermHasC) p = A::mul_rn(cur.c, p);
+        if (sub & kTermInit) acc = p;
+        else if (sub & kTermSub) acc = A::sub_rn(acc, p);
+        else acc = A::add_rn(acc, p);
+        break;
+      }
+      case kOpGeneric: {
+        const double a = pfetch(t, acc, cur, cur.modes & 3, cur.a);
+        const double b = pfetch(t, acc, cur, (cur.modes >> 2) & 3, cur.b);
+        t.slo[cur.dst * t.stride + t.tid] = pt_generic((uint8_t)sub, a, b, (int)(int16_t)cur.b);
+        break;
+      }
+      case kOpStoreAcc:
+        t.slo[cur.dst * t.stride + t.tid] = acc;
+        break;
+      case kOpLoadAcc:
+        acc = pfetch(t, acc, cur, cur.modes & 3, cur.a);
+        break;
+      case kOpConstToSlot:
+        t.slo[cur.dst * t.stride + t.tid] = cur.c;
+        break;
+      case kOpCheck: {
+        const double v = pfetch(t, acc, cur, cur.modes & 3, cur.a);
+        const bool ok = (sub == 0) ? (v <= cur.c) : almost_equal(v, cur.c);
+        out.feasible = out.feasible && ok;
+        break;
+      }
+      case kOpObjective:
+        out.obj = pfetch(t, acc, cur, cur.modes & 3, cur.a);
+        break;
+      default:
+        break;
+    }
+  }
+  return out;
+}
+
+// ---- region decode (region/decode.hpp:44-71), FMA form as compiled on
+// the device, and the sampler (graph/subregion_sampler.cuh:53-120) ----
+__device__ __forceinline__ void slot_bounds(int kind, double plo, double phi, uint64_t part, uint64_t fan,
+                                            double& lo, double& hi)
+{
+  if (kind == 2 || kind == 3) {  // IntegerEnumerate / BinaryEnumerate
+    double value = __dadd_rn(ceil(plo), (double)part);
+    if (value > phi) value = phi;
+    lo = value;
+    hi = value;
+    return;
+  }
+  const double width = __ddiv_rn(__dsub_rn(phi, plo), (double)fan);
+  lo = __fma_rn(width, (double)part, plo);
+  hi = (part + 1 == fan) ? phi : __fma_rn(width, (double)(part + 1), plo);
+}
+
+__device__ __forceinline__ uint64_t sample_hash(uint64_t vid, uint64_t i, uint64_t region, uint64_t salt)
+{
+  uint64_t x = vid * 0x9e3779b97f4a7c15ULL;
+  x ^= i * 0xbf58476d1ce4e5b9ULL;
+  x ^= region * 0x94d049bb133111ebULL;
+  x ^= salt * 0xd6e8feb86659fd93ULL;
+  x += 0x9e3779b97f4a7c15ULL;
+  x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ULL;
+  x = (x ^ (x >> 27)) * 0x94d049bb133111ebULL;
+  x ^= x >> 31;
+  return x;
+}
+
+__device__ __forceinline__ double sample_value(bool discrete, double lb, double ub, uint64_t vid, uint64_t i,
+                                               uint64_t region, uint64_t salt)
+{
+  const uint64_t x = sample_hash(vid, i, region, salt);
+  if (!discrete) {
+    const double u = __dmul_rn(__ull2double_rn(x >> 11), 1.0 / 9007199254740992.0);
+    return __fma_rn(u, __dsub_rn(ub, lb), lb);
+  }
+  const double lo = ceil(lb), hi = floor(ub);
+  if (hi < lo) return lo;
+  const uint64_t count = (uint64_t)__double2ull_rz(__dsub_rn(hi, lo)) + 1;
+  const uint64_t idx = x % count;
+  return __dadd_rn(lo, __ull2double_rn(idx));
+}
+
+// Total order on doubles for selection keys (NaN last).
+__device__ __forceinline__ uint64_t lb_key(double x)
+{
+  const uint64_t u = (uint64_t)__double_as_longlong(x);
+  if (x != x) return ~0ULL;
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ULL);
+}
+
+}  // namespace cmn

@@ -1,0 +1,429 @@
+// eval_kernels.cu -- the fused interval evaluator (a), the point sampler
+// (b) and the incumbent ArgMin, over children decoded from parent boxes.
+//
+// One thread owns one child box.  Its variable intervals and program slots
+// live in shared memory laid out plane-major ([plane][thread]), so every
+// access of a warp is one conflict-free row.  Nothing is shared between
+// threads, so the kernels need no barriers and a thread whose child is
+// invalid simply skips the program.
+//
+// Replaces graph/kernels.cuh:76-461 (broadcast/apply root kernels, one op
+// kernel per DAG node, feasibility, extract, mask, gather) and the CUB
+// ArgMin of graph/replay.cuh:439-474.
+#include <cfloat>
+#include <cstdint>
+
+#include "eval_core.cuh"
+#include "kernels.cuh"
+#include "launch.hpp"
+
+namespace cmn {
+
+template <typename T>
+__device__ __forceinline__ T conv_lo(double x);
+template <typename T>
+__device__ __forceinline__ T conv_hi(double x);
+template <>
+__device__ __forceinline__ double conv_lo<double>(double x) { return x; }
+template <>
+__device__ __forceinline__ double conv_hi<double>(double x) { return x; }
+template <>
+__device__ __forceinline__ float conv_lo<float>(double x) { return __double2float_rd(x); }
+template <>
+__device__ __forceinline__ float conv_hi<float>(double x) { return __double2float_ru(x); }
+
+__device__ __forceinline__ void child_of(int log2C, uint64_t g, uint64_t& k, uint64_t& r)
+{
+  if (log2C < 0) {
+    k = 0;
+    r = g;
+  } else {
+    k = g >> log2C;
+    r = g & ((1ULL << log2C) - 1ULL);
+  }
+}
+
+// Decodes child (k, r) into this thread's tile column; returns false when
+// the child is a duplicate (a slot digit at or past its domain size).
+template <typename T>
+__device__ __forceinline__ bool load_child(const EvalArgs& a, const Tile<T>& t, uint64_t k, uint64_t r)
+{
+  for (int v = 0; v < a.n_vars; ++v) {
+    const double lo = a.plo[(uint64_t)v * a.pstride + k];
+    const double hi = a.phi[(uint64_t)v * a.pstride + k];
+    t.lo[v * t.stride + t.tid] = conv_lo<T>(lo);
+    t.hi[v * t.stride + t.tid] = conv_hi<T>(hi);
+  }
+  bool dup = false;
+  if (a.pinfo != nullptr) {
+    const uint32_t count = a.pinfo[k].count;
+    const SlotPlan* sp = a.slots + k * (uint64_t)a.max_slots;
+    for (uint32_t j = 0; j < count; ++j) {
+      const SlotPlan s = sp[j];
+      const uint64_t part = (r / s.prefix) % s.width;
+      if (part >= s.dom) dup = true;
+      const double plo = a.plo[(uint64_t)s.vid * a.pstride + k];
+      const double phi = a.phi[(uint64_t)s.vid * a.pstride + k];
+      double lo, hi;
+      slot_bounds((int)s.kind, plo, phi, part, s.width, lo, hi);
+      t.lo[s.vid * t.stride + t.tid] = conv_lo<T>(lo);
+      t.hi[s.vid * t.stride + t.tid] = conv_hi<T>(hi);
+    }
+  }
+  return !dup;
+}
+
+// kMode 0: role / raw boxes -> out_lb, out_ub, out_flag = feasible
+// kMode 1: solver FP64 -> out_lb, out_flag = ChildState
+// kMode 2: solver FP32 screen -> out_lb (FP32 bound), out_flag = ChildState
+// kMode 3: solver FP64 certify of a child list
+template <typename T, int kMode>
+__global__ void __launch_bounds__(kEvalThreads) eval_children_kernel(const EvalArgs a)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* base = reinterpret_cast<T*>(smem_raw);
+  const int B = blockDim.x;
+  Tile<T> t;
+  t.lo = base;
+  t.hi = base + (size_t)a.n_vars * B;
+  t.slo = base + (size_t)2 * a.n_vars * B;
+  t.shi = base + (size_t)(2 * a.n_vars + a.n_slots) * B;
+  t.stride = B;
+  t.tid = threadIdx.x;
+
+  if (a.done != nullptr && *a.done) return;
+  uint64_t total;
+  if (kMode == 3) total = *a.list_count;
+  else total = a.n_children_dev ? *a.n_children_dev : a.n_children;
+  const double gub = a.gub ? *a.gub : DBL_MAX;
+
+  for (uint64_t idx = (uint64_t)blockIdx.x * B + threadIdx.x; idx < total; idx += (uint64_t)gridDim.x * B) {
+    const uint64_t g = (kMode == 3) ? (uint64_t)a.list[idx] : idx;
+    uint64_t k, r;
+    child_of(a.log2C, g, k, r);
+    if (kMode != 0 && a.pinfo != nullptr) {
+      const ParentInfo pi = a.pinfo[k];
+      if (pi.fathom || r >= pi.nreg) {
+        if (kMode != 3) a.out_flag[g] = kChildNone;
+        continue;
+      }
+    }
+    const bool unique = load_child<T>(a, t, k, r);
+    if (kMode != 0 && !unique) {
+      a.out_flag[g] = kChildDuplicate;
+      continue;
+    }
+    const Verdict<T> v = run_interval<T>(a.prog, a.prog_len, t);
+    const double lb = (double)v.obj.lo;
+    if (kMode == 0) {
+      a.out_lb[g] = lb;
+      if (a.out_ub) a.out_ub[g] = (double)v.obj.hi;
+      // FP64: the reference predicate; FP32: not proven violated
+      a.out_flag[g] = (uint8_t)(sizeof(T) == 8 ? v.feasible : !v.excluded);
+    } else if (kMode == 2) {
+      a.out_lb[g] = lb;
+      a.out_flag[g] = v.excluded ? kChildInfeasible : (lb > gub ? kChildDominated : kChildScreened);
+    } else {
+      a.out_lb[g] = lb;
+      a.out_flag[g] = !v.feasible ? kChildInfeasible : (lb > gub ? kChildDominated : kChildEligible);
+    }
+  }
+}
+
+__device__ __forceinline__ void warp_min_cand(Cand& c)
+{
+  for (int off = 16; off > 0; off >>= 1) {
+    Cand o;
+    o.value = __shfl_down_sync(0xffffffffu, c.value, off);
+    o.k = __shfl_down_sync(0xffffffffu, c.k, off);
+    o.e = __shfl_down_sync(0xffffffffu, c.e, off);
+    o.pad = 0;
+    if (cand_less(o, c)) c = o;
+  }
+}
+
+// Block-wide min of one Cand per thread; result valid in thread 0.
+__device__ __forceinline__ Cand block_min_cand(Cand c)
+{
+  __shared__ Cand warp_best[32];
+  warp_min_cand(c);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) warp_best[wid] = c;
+  __syncthreads();
+  const int nw = (blockDim.x + 31) >> 5;
+  if (wid == 0) {
+    Cand x = lane < nw ? warp_best[lane] : Cand{INFINITY, 0xffffffffu, 0, ~0ULL};
+    warp_min_cand(x);
+    c = x;
+  }
+  __syncthreads();
+  return c;
+}
+
+__device__ __forceinline__ bool admissible(const SampleArgs& a, const Tile<double>& t)
+{
+  for (int v = 0; v < a.n_vars; ++v) {
+    const double x = t.lo[v * t.stride + t.tid];
+    if (!(x >= a.root_lb[v]) || !(x <= a.root_ub[v])) return false;
+    if (a.var_kinds[v] != 0) {
+      const double nearest = rint(x);
+      if (fabs(__dsub_rn(x, nearest)) > 1e-6) return false;
+    }
+  }
+  return true;
+}
+
+// Point sampling (graph/subregion_sampler.cuh:133-199) and exact points
+// (graph/kernels.cuh:131-172), point program, feasibility mask and the
+// ArgMin over (value, parent, element) -- element = region * S + sample.
+__global__ void __launch_bounds__(kEvalThreads) sample_children_kernel(const SampleArgs a)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* base = reinterpret_cast<double*>(smem_raw);
+  const int B = blockDim.x;
+  Tile<double> t;
+  t.lo = base;
+  t.hi = base;  // unused by the point program
+  t.slo = base + (size_t)a.n_vars * B;
+  t.shi = t.slo;
+  t.stride = B;
+  t.tid = threadIdx.x;
+
+  if (a.done != nullptr && *a.done) {
+    if (threadIdx.x == 0) a.block_best[blockIdx.x] = Cand{INFINITY, 0xffffffffu, 0, ~0ULL};
+    return;
+  }
+  const uint64_t total = a.n_children_dev ? *a.n_children_dev : a.n_children;
+  const uint64_t salt_base = a.salt_base_dev ? *a.salt_base_dev : 0;
+  const double gub = a.gub ? *a.gub : DBL_MAX;
+  Cand best = {INFINITY, 0xffffffffu, 0, ~0ULL};
+  unsigned long long rejected = 0;
+
+  for (uint64_t g = (uint64_t)blockIdx.x * B + threadIdx.x; g < total; g += (uint64_t)gridDim.x * B) {
+    uint64_t k, r;
+    child_of(a.log2C, g, k, r);
+    bool fathom = a.exact != 0;
+    uint64_t nreg = ~0ULL;
+    if (a.pinfo != nullptr) {
+      const ParentInfo pi = a.pinfo[k];
+      nreg = pi.nreg;
+      fathom = fathom || pi.fathom;
+    }
+    if (r >= nreg) continue;
+    if (a.state != nullptr && !fathom) {
+      const uint8_t st = a.state[g];
+      const bool take = a.sample_all ? (st != kChildNone) : (st == kChildEligible);
+      if (!take) continue;
+    }
+    // child bounds per variable: parent bound, narrowed by its slot
+    const SlotPlan* sp = a.pinfo ? a.slots + k * (uint64_t)a.max_slots : nullptr;
+    const uint32_t count = a.pinfo ? a.pinfo[k].count : 0;
+    const uint64_t salt = a.salt_base_dev ? salt_base + k + 1 : a.salt;
+    const uint64_t S = fathom ? 1 : a.S;
+    for (uint64_t i = 0; i < S; ++i) {
+      // stage the point in the tile: every variable from its region bound
+      for (int v = 0; v < a.n_vars; ++v) {
+        double lo = a.plo[(uint64_t)v * a.pstride + k];
+        double hi = a.phi[(uint64_t)v * a.pstride + k];
+        for (uint32_t j = 0; j < count; ++j) {
+          if (sp[j].vid == (uint32_t)v) {
+            const uint64_t part = (r / sp[j].prefix) % sp[j].width;
+            slot_bounds((int)sp[j].kind, lo, hi, part, sp[j].width, lo, hi);
+            break;
+          }
+        }
+        t.lo[v * B + t.tid] =
+            fathom ? lo : sample_value(a.var_kinds[v] != 0, lo, hi, (uint64_t)v, i, r, salt);
+      }
+      const PointVerdict pv = run_point(a.prog, a.prog_len, t);
+      double value = (pv.feasible && !(pv.obj != pv.obj)) ? pv.obj : INFINITY;
+      if (fathom && a.state != nullptr && value < INFINITY && !admissible(a, t)) {
+        if (value < gub) ++rejected;
+        value = INFINITY;
+      }
+      const Cand c = {value, (uint32_t)k, 0, r * S + i};
+      if (value < INFINITY && cand_less(c, best)) best = c;
+    }
+  }
+  best = block_min_cand(best);
+  if (threadIdx.x == 0) a.block_best[blockIdx.x] = best;
+  if (a.rejected != nullptr) {
+    for (int off = 16; off > 0; off >>= 1) rejected += __shfl_down_sync(0xffffffffu, rejected, off);
+    if ((threadIdx.x & 31) == 0 && rejected) atomicAdd(a.rejected, rejected);
+  }
+}
+
+// Final ArgMin over the per-block candidates (one block).
+__global__ void reduce_cand_kernel(const Cand* __restrict__ block_best, int n, Cand* __restrict__ out)
+{
+  Cand best = {INFINITY, 0xffffffffu, 0, ~0ULL};
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const Cand c = block_best[i];
+    if (cand_less(c, best)) best = c;
+  }
+  best = block_min_cand(best);
+  if (threadIdx.x == 0) *out = best;
+}
+
+// Witness of a candidate: the point the sampler (or the exact grid) drew
+// for (parent k, element e).  One thread per variable.
+__global__ void witness_kernel(const Cand* __restrict__ cand, const double* __restrict__ plo,
+                               const double* __restrict__ phi, uint64_t pstride, const ParentInfo* __restrict__ pinfo,
+                               const SlotPlan* __restrict__ slots, int max_slots, const int32_t* __restrict__ kinds,
+                               int n_vars, uint64_t S, uint64_t salt, const uint64_t* __restrict__ salt_base_dev,
+                               int exact, const uint32_t* __restrict__ write_flag, double* __restrict__ out)
+{
+  if (write_flag != nullptr && *write_flag == 0) return;
+  const Cand c = *cand;
+  const bool found = c.value < DBL_MAX;
+  const uint64_t k = c.k;
+  bool fathom = exact != 0;
+  if (pinfo && found) fathom = fathom || pinfo[k].fathom;
+  const uint64_t SS = fathom ? 1 : S;
+  const uint64_t r = found ? c.e / SS : 0, i = found ? c.e % SS : 0;
+  const uint64_t sl = salt_base_dev ? *salt_base_dev + k + 1 : salt;
+  for (int v = threadIdx.x + blockIdx.x * blockDim.x; v < n_vars; v += blockDim.x * gridDim.x) {
+    if (!found) {
+      out[v] = __longlong_as_double(0x7ff8000000000000LL);
+      continue;
+    }
+    double lo = plo[(uint64_t)v * pstride + k];
+    double hi = phi[(uint64_t)v * pstride + k];
+    if (pinfo) {
+      const SlotPlan* sp = slots + k * (uint64_t)max_slots;
+      const uint32_t count = pinfo[k].count;
+      for (uint32_t j = 0; j < count; ++j) {
+        if (sp[j].vid == (uint32_t)v) {
+          const uint64_t part = (r / sp[j].prefix) % sp[j].width;
+          slot_bounds((int)sp[j].kind, lo, hi, part, sp[j].width, lo, hi);
+          break;
+        }
+      }
+    }
+    out[v] = fathom ? lo : sample_value(kinds[v] != 0, lo, hi, (uint64_t)v, i, r, sl);
+  }
+}
+
+// FMA throughput probe: 8 independent FMA chains per thread.
+template <typename T>
+__global__ void fma_peak_kernel(int iters, T* sink)
+{
+  T a0 = T(threadIdx.x) * T(1e-7), a1 = a0 + T(1), a2 = a0 + T(2), a3 = a0 + T(3);
+  T a4 = a0 + T(4), a5 = a0 + T(5), a6 = a0 + T(6), a7 = a0 + T(7);
+  const T m = T(0.999999), c = T(1e-9);
+  for (int i = 0; i < iters; ++i) {
+    a0 = fma(a0, m, c);
+    a1 = fma(a1, m, c);
+    a2 = fma(a2, m, c);
+    a3 = fma(a3, m, c);
+    a4 = fma(a4, m, c);
+    a5 = fma(a5, m, c);
+    a6 = fma(a6, m, c);
+    a7 = fma(a7, m, c);
+  }
+  sink[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+}
+
+cudaError_t launch_fma_peak(int precision, int grid, int threads, int iters, void* sink, cudaStream_t s)
+{
+  if (precision == 0) fma_peak_kernel<double><<<grid, threads, 0, s>>>(iters, static_cast<double*>(sink));
+  else fma_peak_kernel<float><<<grid, threads, 0, s>>>(iters, static_cast<float*>(sink));
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------
+// host launchers
+// ---------------------------------------------------------------------
+size_t eval_smem_bytes(int n_vars, int n_slots, bool fp32, int threads)
+{
+  const size_t es = fp32 ? 4 : 8;
+  return es * (size_t)(2 * n_vars + 2 * n_slots) * threads;
+}
+
+size_t sample_smem_bytes(int n_vars, int n_slots, int threads)
+{
+  return 8 * (size_t)(n_vars + n_slots) * threads;
+}
+
+// Kernel attributes are set once per device, before any launch, so that
+// launches stay legal inside stream capture.
+cudaError_t set_eval_kernel_attributes(int max_smem)
+{
+  const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
+  cudaError_t e = cudaFuncSetAttribute(eval_children_kernel<double, 0>, at, max_smem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(eval_children_kernel<double, 1>, at, max_smem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(eval_children_kernel<double, 3>, at, max_smem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(eval_children_kernel<float, 0>, at, max_smem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(eval_children_kernel<float, 2>, at, max_smem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(sample_children_kernel, at, max_smem);
+  return e;
+}
+
+int eval_kernel_occupancy(int mode, bool fp32, size_t smem, int threads)
+{
+  int blocks = 0;
+  cudaError_t e;
+  if (fp32) {
+    e = mode == 0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, eval_children_kernel<float, 0>, threads, smem)
+                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, eval_children_kernel<float, 2>, threads, smem);
+  } else {
+    e = mode == 0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, eval_children_kernel<double, 0>, threads, smem)
+        : mode == 1
+            ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, eval_children_kernel<double, 1>, threads, smem)
+            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, eval_children_kernel<double, 3>, threads, smem);
+  }
+  return e == cudaSuccess ? blocks : 1;
+}
+
+int sample_kernel_occupancy(size_t smem, int threads)
+{
+  int blocks = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sample_children_kernel, threads, smem);
+  return e == cudaSuccess ? blocks : 1;
+}
+
+template <typename T, int kMode>
+static cudaError_t launch_eval_t(const EvalArgs& a, int grid, int threads, cudaStream_t s)
+{
+  const size_t smem = eval_smem_bytes(a.n_vars, a.n_slots, sizeof(T) == 4, threads);
+  eval_children_kernel<T, kMode><<<grid, threads, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_eval(const EvalArgs& a, int mode, bool fp32, int grid, int threads, cudaStream_t s)
+{
+  if (fp32) {
+    if (mode == 0) return launch_eval_t<float, 0>(a, grid, threads, s);
+    return launch_eval_t<float, 2>(a, grid, threads, s);
+  }
+  if (mode == 0) return launch_eval_t<double, 0>(a, grid, threads, s);
+  if (mode == 1) return launch_eval_t<double, 1>(a, grid, threads, s);
+  return launch_eval_t<double, 3>(a, grid, threads, s);
+}
+
+cudaError_t launch_sample(const SampleArgs& a, int grid, int threads, cudaStream_t s)
+{
+  const size_t smem = sample_smem_bytes(a.n_vars, a.n_slots, threads);
+  sample_children_kernel<<<grid, threads, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_reduce_cand(const Cand* block_best, int n, Cand* out, cudaStream_t s)
+{
+  reduce_cand_kernel<<<1, 1024, 0, s>>>(block_best, n, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_witness(const Cand* cand, const double* plo, const double* phi, uint64_t pstride,
+                           const ParentInfo* pinfo, const SlotPlan* slots, int max_slots, const int32_t* kinds,
+                           int n_vars, uint64_t S, uint64_t salt, const uint64_t* salt_base_dev, int exact,
+                           const uint32_t* write_flag, double* out, cudaStream_t s)
+{
+  const int threads = 128;
+  const int grid = (n_vars + threads - 1) / threads;
+  witness_kernel<<<grid, threads, 0, s>>>(cand, plo, phi, pstride, pinfo, slots, max_slots, kinds, n_vars, S, salt,
+                                          salt_base_dev, exact, write_flag, out);
+  return cudaGetLastError();
+}
+
+}  // namespace cmn

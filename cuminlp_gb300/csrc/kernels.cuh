@@ -1,0 +1,107 @@
+// kernels.cuh -- device data structures shared by the kernels and the host
+// code that launches them.
+#pragma once
+
+#include <cstdint>
+
+#include "program.h"
+
+namespace cmn {
+
+// One slot of one parent box: which variable it narrows and how
+// (region/composition.hpp:50-56 SlotAssignment, flattened per slot).
+struct SlotPlan {
+  uint64_t width;   // fan-out of the slot
+  uint64_t prefix;  // product of the previous slots' widths
+  uint64_t dom;     // true domain size; parts >= dom are duplicates
+  uint32_t vid;
+  uint32_t kind;    // cmn_slot_kind
+};
+
+struct ParentInfo {
+  uint32_t count;   // slots in use
+  uint32_t fathom;  // every live variable enumerated: exact points only
+  uint64_t nreg;    // children the composition produces
+};
+
+// child verdict codes of the solver's evaluation
+enum ChildState : uint8_t {
+  kChildNone = 0,        // no child here (beyond nreg, or a fathomed parent)
+  kChildDuplicate = 1,   // region::is_duplicate_child
+  kChildInfeasible = 2,  // a constraint excludes the box
+  kChildDominated = 3,   // obj lb above the incumbent
+  kChildEligible = 4,    // survives (so far)
+  kChildScreened = 5,    // FP32 screen left it open: certify in FP64
+};
+
+// Candidate of the incumbent reduction: smallest (value, parent, element).
+struct Cand {
+  double value;
+  uint32_t k;
+  uint32_t pad;
+  uint64_t e;
+};
+
+__host__ __device__ inline bool cand_less(const Cand& a, const Cand& b)
+{
+  if (a.value < b.value) return true;
+  if (b.value < a.value) return false;
+  if (a.k != b.k) return a.k < b.k;
+  return a.e < b.e;
+}
+
+// Arguments of the child evaluation kernels.
+struct EvalArgs {
+  const Instr* prog;
+  int prog_len;
+  int n_vars;
+  int n_slots;
+  int log2C;             // children per parent = 2^log2C; -1: all children belong to parent 0
+  const double* plo;     // parent planes: variable v of parent k at [v * pstride + k]
+  const double* phi;
+  uint64_t pstride;
+  const ParentInfo* pinfo;  // null: every parent has no slots, one child
+  const SlotPlan* slots;    // [k * max_slots + j]
+  int max_slots;
+  uint64_t n_children;            // used when n_children_dev is null
+  const uint64_t* n_children_dev;
+  const uint32_t* list;           // optional: evaluate only these children
+  const uint64_t* list_count;
+  const double* gub;              // incumbent at the start of the iteration
+  const uint32_t* done;           // solver: nonzero once the search stopped
+  // outputs
+  double* out_lb;
+  double* out_ub;
+  uint8_t* out_flag;  // role/raw: feasible; solver: ChildState
+};
+
+struct SampleArgs {
+  const Instr* prog;
+  int prog_len;
+  int n_vars;
+  int n_slots;
+  int log2C;
+  const double* plo;
+  const double* phi;
+  uint64_t pstride;
+  const ParentInfo* pinfo;
+  const SlotPlan* slots;
+  int max_slots;
+  const int32_t* var_kinds;
+  const double* root_lb;
+  const double* root_ub;
+  uint64_t n_children;
+  const uint64_t* n_children_dev;
+  uint64_t S;                // samples per child
+  uint64_t salt;             // role: the salt; solver: salt of parent k is salt_base + k + 1
+  const uint64_t* salt_base_dev;
+  int exact;                 // role enumerator: exact points
+  int sample_all;            // solver: sample every valid child, else only eligible ones
+  const uint8_t* state;      // solver child states (null for roles)
+  const double* gub;         // for the inadmissible-witness count
+  const uint32_t* done;      // solver: nonzero once the search stopped
+  Cand* block_best;          // [gridDim.x]
+  unsigned long long* rejected;  // inadmissible feasible exact points below gub
+};
+
+}  // namespace cmn

@@ -1,0 +1,32 @@
+// launch.hpp -- host-side launch wrappers of the device kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+#include "kernels.cuh"
+
+namespace cmn {
+
+constexpr int kEvalThreads = 128;
+
+size_t eval_smem_bytes(int n_vars, int n_slots, bool fp32, int threads);
+size_t sample_smem_bytes(int n_vars, int n_slots, int threads);
+
+// mode 0: role / raw boxes; 1: solver FP64; 2: solver FP32 screen (fp32
+// must be true); 3: solver FP64 certify over EvalArgs::list
+cudaError_t launch_eval(const EvalArgs& a, int mode, bool fp32, int grid, int threads, cudaStream_t s);
+cudaError_t launch_sample(const SampleArgs& a, int grid, int threads, cudaStream_t s);
+cudaError_t launch_reduce_cand(const Cand* block_best, int n, Cand* out, cudaStream_t s);
+cudaError_t launch_witness(const Cand* cand, const double* plo, const double* phi, uint64_t pstride,
+                           const ParentInfo* pinfo, const SlotPlan* slots, int max_slots, const int32_t* kinds,
+                           int n_vars, uint64_t S, uint64_t salt, const uint64_t* salt_base_dev, int exact,
+                           const uint32_t* write_flag, double* out, cudaStream_t s);
+
+// Largest dynamic shared memory a block may use on this device.
+int max_dynamic_smem();
+int sm_count();
+
+}  // namespace cmn

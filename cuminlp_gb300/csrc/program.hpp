@@ -1,0 +1,51 @@
+// program.hpp -- host-side problem model and the DAG -> program compiler.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/cuminlp_gb300.h"
+#include "program.h"
+
+namespace cmn {
+
+// A validated, flattened model::Problem<double> (model/problem.hpp:195-358).
+struct HostProblem {
+  std::vector<cmn_node> nodes;
+  std::vector<double> var_lb, var_ub;
+  std::vector<int32_t> var_kinds;
+  int64_t objective_root = -1;
+  std::vector<cmn_constraint> constraints;
+  std::vector<uint8_t> reach;  // reachable from a root
+  int64_t buffer_node_count = 0;
+
+  int64_t n_vars() const { return (int64_t)var_lb.size(); }
+};
+
+// Builds a HostProblem from the C description, applying the checks of
+// Problem::validate() (model/problem.hpp:282-355) plus the structural
+// checks the reference's GraphBuilder makes at build time
+// (graph/builder.cuh:266-271, 466-470, 497-501).  Returns a cmn_status and
+// fills `err` on failure.
+cmn_status build_host_problem(const cmn_problem_desc* desc, HostProblem& out, std::string& err);
+
+struct Program {
+  std::vector<Instr> code64;  // FP64 interval / point program
+  std::vector<Instr> code32;  // FP32 outward-rounded screen program
+  int n_slots = 0;
+  bool interval_supported = true;  // every reachable op has an interval form
+  std::string unsupported_op;
+  double flops_per_box = 0;        // algorithmic FP64 ops, interval eval
+  double point_flops_per_box = 0;  // algorithmic FP64 ops, point eval
+  int64_t n_terms = 0;             // fused sum-chain terms
+};
+
+// Compiles the reachable DAG into the fused straight-line program.
+void compile_program(const HostProblem& p, Program& out);
+
+// Outward conversion of an FP64 constant to an FP32 pair.
+float d2f_rd(double x);
+float d2f_ru(double x);
+
+}  // namespace cmn

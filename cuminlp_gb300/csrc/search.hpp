@@ -1,0 +1,127 @@
+// search.hpp -- device-resident state of the batched branch-and-bound and
+// the launchers of its kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "../../include/cuminlp_gb300.h"
+#include "kernels.cuh"
+
+namespace cmn {
+
+constexpr int kRadixBits = 11;
+constexpr int kRadixBins = 1 << kRadixBits;
+constexpr int kScanBlock = 512;  // items per block of the compaction kernels
+
+// k-th smallest key search (radix select over lb keys).
+struct RadixState {
+  uint64_t prefix;
+  uint64_t mask;
+  uint64_t k;      // rank still to find inside the current prefix
+  uint64_t less;   // entries with key below the prefix bucket so far
+  uint32_t active; // 0: take everything (k >= n)
+  uint32_t pad;
+  uint32_t hist[kRadixBins];
+};
+
+// Everything the iteration kernels read and write, in device memory.
+struct SolverDev {
+  double gub;
+  double glb;
+  double dropped_lb_min;
+  uint64_t pool_min_key;   // min lb key of the current pool
+  uint64_t pool_size;      // L
+  uint64_t n_parents;      // E of this iteration
+  uint64_t n_children;     // E << log2C
+  uint64_t salt_base;      // expansions before this iteration
+  uint64_t expansions;
+  uint64_t iterations;
+  uint64_t remaining;      // unselected pool entries kept
+  uint64_t kept;           // children kept
+  uint64_t new_size;
+  uint64_t certify_count;
+  uint64_t evict;          // 1 when the rebuilt pool exceeds the cap
+  uint64_t dropped_min_key;
+  uint32_t parity;         // pool buffer holding the current pool
+  uint32_t done;
+  uint32_t converged;
+  uint32_t have_best;
+  uint32_t improved;
+  uint32_t error;
+  Cand best;
+  cmn_counters counters;
+};
+
+// Static configuration baked into the captured iteration.
+struct SolverCfg {
+  int n_vars;
+  int n_slots;
+  int prog_len;
+  int log2C;        // B
+  int max_slots;    // = B
+  int precision;
+  int sample_all;
+  int relative;
+  uint64_t S;
+  uint64_t e_max;   // parents per iteration
+  uint64_t cap;     // pool capacity (entries kept after an iteration)
+  uint64_t pstride; // pool plane stride (cap + e_max << B)
+  uint64_t iter_limit;
+  uint64_t batch_iter_limit;
+  int64_t max_cycle;
+  int64_t enumerate_cap;
+  double tolerance;
+};
+
+struct SolverBufs {
+  SolverDev* dev;
+  RadixState* radix;
+  // pools (two parities): planes [v * pstride + i]
+  double* lo[2];
+  double* hi[2];
+  double* lb[2];
+  uint32_t* depth[2];
+  uint8_t* sel;          // selection / keep marks over a pool
+  // staging of this iteration's parents: planes [v * e_max + k]
+  double* plo;
+  double* phi;
+  uint32_t* pdepth;
+  ParentInfo* pinfo;
+  SlotPlan* slots;
+  // policy scratch [k * n_vars + i]
+  void* enum_scratch;
+  void* bis_scratch;
+  uint64_t* heap_scratch;
+  // children
+  double* clb;
+  uint8_t* cstate;
+  uint32_t* list;        // certify list
+  // compaction scratch
+  uint32_t* block_counts;
+  uint32_t* block_offsets;
+  Cand* block_best;
+  int n_block_best;
+  // problem
+  const Instr* prog64;
+  const Instr* prog32;
+  const int32_t* kinds;
+  const double* root_lb;
+  const double* root_ub;
+  double* best_point;
+};
+
+// Initialises the device state: the root box as the only pool entry.
+cudaError_t solver_init(const SolverCfg& cfg, const SolverBufs& b, const double* root_lb_host,
+                        const double* root_ub_host, double gub0, cudaStream_t s);
+// Enqueues one batched iteration (all kernels) on `s`; capturable.
+// `marks` (5 events or null) are recorded as event nodes at the phase
+// boundaries: start, after branching, after bounding, after sampling, end.
+cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval_grid, int sample_grid,
+                             cudaStream_t s, const cudaEvent_t* marks);
+// Fills min key / viable count of the current pool (after the run).
+cudaError_t solver_pool_stats(const SolverCfg& cfg, const SolverBufs& b, uint64_t* viable_dev, cudaStream_t s);
+
+
+}  // namespace cmn

@@ -1,0 +1,989 @@
+// search_kernels.cu -- the device half of the batched branch-and-bound:
+// parent selection, the branching policy, prune + compaction (c) and the
+// box pool with eviction (d).  Every kernel reads the iteration's sizes
+// from SolverDev, so one captured graph replays any iteration.
+//
+// The reference keeps its frontier on the host: a binary heap of 40-byte
+// nodes and a refcounted box history (search/frontier.hpp:152-338,
+// search/history.hpp:20-137), pruned by an O(N) host loop after every
+// launch (search/driver.hpp:303-352).  Here the frontier is a pool of SoA
+// boxes in HBM; selection is a radix select on the lower-bound keys, and
+// every compaction is a stable, deterministic block scan.
+#include <cfloat>
+#include <cstdint>
+
+#include "eval_core.cuh"
+#include "launch.hpp"
+#include "search.hpp"
+
+namespace cmn {
+
+__device__ __forceinline__ bool gap_closed_dev(double gub, double bound, double tol)
+{
+  return __dsub_rn(gub, bound) <= __dmul_rn(tol, fmax(1.0, fabs(gub)));
+}
+
+__device__ __forceinline__ double key_to_lb(uint64_t k)
+{
+  const uint64_t u = (k >> 63) ? (k & 0x7fffffffffffffffULL) : ~k;
+  return __longlong_as_double((long long)u);
+}
+
+// ---------------------------------------------------------------------
+// init / begin / finish
+// ---------------------------------------------------------------------
+__global__ void init_kernel(const SolverCfg cfg, const SolverBufs b, const double* __restrict__ root_lb,
+                            const double* __restrict__ root_ub, double gub0)
+{
+  const int t = threadIdx.x + blockIdx.x * blockDim.x;
+  for (int v = t; v < cfg.n_vars; v += blockDim.x * gridDim.x) {
+    b.lo[0][(uint64_t)v * cfg.pstride] = root_lb[v];
+    b.hi[0][(uint64_t)v * cfg.pstride] = root_ub[v];
+  }
+  if (t == 0) {
+    SolverDev* d = b.dev;
+    memset(d, 0, sizeof(SolverDev));
+    d->gub = gub0;
+    d->glb = -DBL_MAX;
+    d->dropped_lb_min = INFINITY;
+    d->dropped_min_key = ~0ULL;
+    b.lb[0][0] = -DBL_MAX;
+    b.depth[0][0] = 0;
+    d->pool_size = 1;
+    d->pool_min_key = lb_key(-DBL_MAX);
+    d->parity = 0;
+    d->counters.peak_frontier = 1;
+  }
+}
+
+// Top of the loop of search/driver.hpp:221-233: convergence of the least
+// pending lower bound, the expansion budget, and this iteration's size.
+__global__ void begin_kernel(const SolverCfg cfg, const SolverBufs b)
+{
+  SolverDev* d = b.dev;
+  if (d->done) return;
+  const uint64_t L = d->pool_size;
+  if (L == 0) {
+    d->done = 1;
+    return;
+  }
+  const double m = key_to_lb(d->pool_min_key);
+  if (gap_closed_dev(d->gub, m, cfg.tolerance)) {
+    d->converged = 1;
+    d->done = 1;
+    return;
+  }
+  d->glb = m;
+  if (d->expansions >= cfg.iter_limit || (cfg.batch_iter_limit && d->iterations >= cfg.batch_iter_limit)) {
+    d->done = 1;
+    return;
+  }
+  uint64_t E = L < cfg.e_max ? L : cfg.e_max;
+  const uint64_t left = cfg.iter_limit - d->expansions;
+  if (E > left) E = left;
+  d->iterations += 1;
+  d->n_parents = E;
+  d->n_children = E << cfg.log2C;
+  d->salt_base = d->expansions;
+  d->expansions += E;
+  d->certify_count = 0;
+  d->remaining = 0;
+  d->kept = 0;
+  d->new_size = 0;
+  d->evict = 0;
+  d->improved = 0;
+  d->counters.iterations = d->iterations;
+  d->counters.expansions = d->expansions;
+}
+
+// ---------------------------------------------------------------------
+// radix select of the k-th smallest lower-bound key
+// ---------------------------------------------------------------------
+// which = 0: the current pool (n = pool_size, k = n_parents)
+// which = 1: the rebuilt pool (n = new_size, k = cap) when evicting
+__device__ __forceinline__ const double* pick_lb(const SolverBufs& b, int which)
+{
+  const uint32_t p = b.dev->parity;
+  return which == 0 ? b.lb[p] : b.lb[1 - p];
+}
+
+__device__ __forceinline__ uint64_t rs_n(const SolverCfg& cfg, const SolverDev* d, int which)
+{
+  (void)cfg;
+  return which == 0 ? d->pool_size : d->new_size;
+}
+
+__global__ void radix_init_kernel(const SolverCfg cfg, const SolverBufs b, int which)
+{
+  SolverDev* d = b.dev;
+  RadixState* rs = b.radix;
+  const uint64_t n = rs_n(cfg, d, which);
+  const uint64_t k = which == 0 ? d->n_parents : cfg.cap;
+  bool active;
+  if (d->done) active = false;
+  else if (which == 1) active = d->evict && k < n;
+  else active = k < n;
+  for (int i = threadIdx.x; i < kRadixBins; i += blockDim.x) rs->hist[i] = 0;
+  if (threadIdx.x == 0) {
+    rs->prefix = 0;
+    rs->mask = 0;
+    rs->k = k;
+    rs->less = 0;
+    rs->active = active ? 1u : 0u;
+  }
+}
+
+__global__ void radix_hist_kernel(const SolverCfg cfg, const SolverBufs b, int which, int shift, int bits)
+{
+  __shared__ uint32_t h[kRadixBins];
+  RadixState* rs = b.radix;
+  if (!rs->active) return;
+  const uint64_t n = rs_n(cfg, b.dev, which);
+  if ((uint64_t)blockIdx.x * blockDim.x >= n) return;
+  const int nb = 1 << bits;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) h[i] = 0;
+  __syncthreads();
+  const double* lb = pick_lb(b, which);
+  const uint64_t prefix = rs->prefix, mask = rs->mask;
+  const uint64_t dmask = (uint64_t)(nb - 1);
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t key = lb_key(lb[i]);
+    if ((key & mask) == prefix) atomicAdd(&h[(key >> shift) & dmask], 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nb; i += blockDim.x)
+    if (h[i]) atomicAdd(&rs->hist[i], h[i]);
+}
+
+__global__ void radix_pick_kernel(const SolverBufs b, int shift, int bits)
+{
+  RadixState* rs = b.radix;
+  if (!rs->active) return;
+  if (threadIdx.x != 0) return;
+  const int nb = 1 << bits;
+  uint64_t cum = 0;
+  int d = nb - 1;
+  for (int i = 0; i < nb; ++i) {
+    const uint64_t c = rs->hist[i];
+    if (cum + c >= rs->k) {
+      d = i;
+      break;
+    }
+    cum += c;
+  }
+  rs->less += cum;
+  rs->k -= cum;
+  rs->prefix |= (uint64_t)d << shift;
+  rs->mask |= ((uint64_t)(nb - 1)) << shift;
+  for (int i = 0; i < nb; ++i) rs->hist[i] = 0;
+}
+
+// ---------------------------------------------------------------------
+// stable compaction: count -> scan -> scatter, one item per thread
+// ---------------------------------------------------------------------
+__device__ __forceinline__ int block_excl_rank(bool f, int& total)
+{
+  __shared__ int warp_tot[kScanBlock / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const unsigned ball = __ballot_sync(0xffffffffu, f);
+  const int in_warp = __popc(ball & ((1u << lane) - 1u));
+  if (lane == 0) warp_tot[wid] = __popc(ball);
+  __syncthreads();
+  int before = 0;
+  total = 0;
+  for (int w = 0; w < kScanBlock / 32; ++w) {
+    if (w < wid) before += warp_tot[w];
+    total += warp_tot[w];
+  }
+  __syncthreads();
+  return before + in_warp;
+}
+
+// Exclusive scan of `nblocks` block counts (one block of 1024 threads);
+// writes the total to *total_out (plus `total_bias`).
+__global__ void scan_kernel(const uint32_t* __restrict__ counts, uint32_t* __restrict__ offsets,
+                            const uint64_t* __restrict__ n_items, uint64_t* __restrict__ total_out,
+                            const uint32_t* __restrict__ active, const uint32_t* __restrict__ done)
+{
+  __shared__ uint32_t warp_sum[32];
+  __shared__ uint64_t carry_s;
+  if (*done) return;
+  if (active && !*active) {
+    if (threadIdx.x == 0 && total_out) *total_out = 0;
+    return;
+  }
+  const uint64_t n = *n_items;
+  const uint64_t nblocks = (n + kScanBlock - 1) / kScanBlock;
+  if (threadIdx.x == 0) carry_s = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (uint64_t base = 0; base < nblocks; base += blockDim.x) {
+    const uint64_t i = base + threadIdx.x;
+    const uint32_t v = i < nblocks ? counts[i] : 0;
+    uint32_t x = v;
+    for (int off = 1; off < 32; off <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+      if (lane >= off) x += y;
+    }
+    if (lane == 31) warp_sum[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+      uint32_t s = lane < (int)(blockDim.x / 32) ? warp_sum[lane] : 0;
+      for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, s, off);
+        if (lane >= off) s += y;
+      }
+      warp_sum[lane] = s;  // inclusive
+    }
+    __syncthreads();
+    const uint64_t carry = carry_s;
+    const uint32_t warp_before = wid > 0 ? warp_sum[wid - 1] : 0;
+    if (i < nblocks) offsets[i] = (uint32_t)(carry + warp_before + x - v);
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry_s = carry + warp_sum[blockDim.x / 32 - 1];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && total_out) *total_out = carry_s;
+}
+
+// ---- predicates / operations -----------------------------------------
+struct SelPool {  // marked entries of the current (which=0) or rebuilt pool
+  SolverBufs b;
+  int which;
+  bool want;  // true: marked entries; false: unmarked entries
+  __device__ uint64_t size() const { return which == 0 ? b.dev->pool_size : b.dev->new_size; }
+  __device__ bool operator()(uint64_t i) const { return (b.sel[i] != 0) == want; }
+  __device__ bool skip() const { return b.dev->done != 0 || (which == 1 && !b.dev->evict); }
+};
+
+struct KeptChild {
+  SolverBufs b;
+  __device__ uint64_t size() const { return b.dev->n_children; }
+  __device__ bool operator()(uint64_t g) const { return b.cstate[g] == kChildEligible && !(b.clb[g] > b.dev->gub); }
+  __device__ bool skip() const { return b.dev->done != 0; }
+};
+
+struct ScreenedChild {
+  SolverBufs b;
+  __device__ uint64_t size() const { return b.dev->n_children; }
+  __device__ bool operator()(uint64_t g) const { return b.cstate[g] == kChildScreened; }
+  __device__ bool skip() const { return b.dev->done != 0; }
+};
+
+struct EqKey {  // entries whose key equals the radix threshold
+  SolverBufs b;
+  int which;
+  __device__ uint64_t size() const { return which == 0 ? b.dev->pool_size : b.dev->new_size; }
+  __device__ bool operator()(uint64_t i) const
+  {
+    const double* lb = which == 0 ? b.lb[b.dev->parity] : b.lb[1 - b.dev->parity];
+    return lb_key(lb[i]) == b.radix->prefix;
+  }
+  __device__ bool skip() const { return b.dev->done != 0 || !b.radix->active; }
+};
+
+template <class P>
+__global__ void __launch_bounds__(kScanBlock) count_kernel(const P pred, uint32_t* __restrict__ counts)
+{
+  if (pred.skip()) return;
+  const uint64_t n = pred.size();
+  const uint64_t i = (uint64_t)blockIdx.x * kScanBlock + threadIdx.x;
+  if ((uint64_t)blockIdx.x * kScanBlock >= n) return;
+  const bool f = i < n && pred(i);
+  const int c = __syncthreads_count(f);
+  if (threadIdx.x == 0) counts[blockIdx.x] = (uint32_t)c;
+}
+
+// Marks the k smallest (key, position) entries: all keys below the
+// threshold, and the first `k` entries equal to it in position order.
+__global__ void __launch_bounds__(kScanBlock) mark_kernel(const SolverCfg cfg, const SolverBufs b, int which,
+                                                          const uint32_t* __restrict__ eq_offsets)
+{
+  const SolverDev* d = b.dev;
+  if (d->done) return;
+  if (which == 1 && !d->evict) return;
+  const uint64_t n = which == 0 ? d->pool_size : d->new_size;
+  if ((uint64_t)blockIdx.x * kScanBlock >= n) return;
+  const uint64_t i = (uint64_t)blockIdx.x * kScanBlock + threadIdx.x;
+  const RadixState* rs = b.radix;
+  const bool active = rs->active != 0;
+  const double* lb = which == 0 ? b.lb[d->parity] : b.lb[1 - d->parity];
+  const uint64_t key = i < n ? lb_key(lb[i]) : ~0ULL;
+  const bool eq = active && i < n && key == rs->prefix;
+  int total;
+  const int rank = block_excl_rank(eq, total);
+  if (i >= n) return;
+  bool mark;
+  if (!active) mark = true;
+  else if (key < rs->prefix) mark = true;
+  else if (eq) mark = (uint64_t)eq_offsets[blockIdx.x] + (uint64_t)rank < rs->k;
+  else mark = false;
+  b.sel[i] = mark ? 1 : 0;
+  (void)cfg;
+}
+
+// gather the selected parents into the staging planes
+struct GatherParents {
+  SolverCfg cfg;
+  SolverBufs b;
+  __device__ void operator()(uint64_t i, uint64_t pos) const
+  {
+    const uint32_t p = b.dev->parity;
+    for (int v = 0; v < cfg.n_vars; ++v) {
+      b.plo[(uint64_t)v * cfg.e_max + pos] = b.lo[p][(uint64_t)v * cfg.pstride + i];
+      b.phi[(uint64_t)v * cfg.e_max + pos] = b.hi[p][(uint64_t)v * cfg.pstride + i];
+    }
+    b.pdepth[pos] = b.depth[p][i];
+  }
+};
+
+// copy an unselected pool entry into the rebuilt pool
+struct CopyRemaining {
+  SolverCfg cfg;
+  SolverBufs b;
+  __device__ void operator()(uint64_t i, uint64_t pos) const
+  {
+    const uint32_t p = b.dev->parity, q = 1 - p;
+    for (int v = 0; v < cfg.n_vars; ++v) {
+      b.lo[q][(uint64_t)v * cfg.pstride + pos] = b.lo[p][(uint64_t)v * cfg.pstride + i];
+      b.hi[q][(uint64_t)v * cfg.pstride + pos] = b.hi[p][(uint64_t)v * cfg.pstride + i];
+    }
+    b.lb[q][pos] = b.lb[p][i];
+    b.depth[q][pos] = b.depth[p][i];
+  }
+};
+
+// decode a kept child from its parent and append it to the rebuilt pool
+struct AppendChild {
+  SolverCfg cfg;
+  SolverBufs b;
+  __device__ void operator()(uint64_t g, uint64_t pos) const
+  {
+    const uint32_t q = 1 - b.dev->parity;
+    const uint64_t at = b.dev->remaining + pos;
+    const uint64_t k = g >> cfg.log2C, r = g & ((1ULL << cfg.log2C) - 1ULL);
+    for (int v = 0; v < cfg.n_vars; ++v) {
+      b.lo[q][(uint64_t)v * cfg.pstride + at] = b.plo[(uint64_t)v * cfg.e_max + k];
+      b.hi[q][(uint64_t)v * cfg.pstride + at] = b.phi[(uint64_t)v * cfg.e_max + k];
+    }
+    const ParentInfo pi = b.pinfo[k];
+    const SlotPlan* sp = b.slots + k * (uint64_t)cfg.max_slots;
+    for (uint32_t j = 0; j < pi.count; ++j) {
+      const SlotPlan s = sp[j];
+      const uint64_t part = (r / s.prefix) % s.width;
+      double lo, hi;
+      slot_bounds((int)s.kind, b.plo[(uint64_t)s.vid * cfg.e_max + k], b.phi[(uint64_t)s.vid * cfg.e_max + k], part,
+                  s.width, lo, hi);
+      b.lo[q][(uint64_t)s.vid * cfg.pstride + at] = lo;
+      b.hi[q][(uint64_t)s.vid * cfg.pstride + at] = hi;
+    }
+    b.lb[q][at] = b.clb[g];
+    b.depth[q][at] = b.pdepth[k] + 1;
+  }
+};
+
+// move a surviving entry of the rebuilt (over-cap) pool back to the
+// current buffer
+struct CopyEvictKeep {
+  SolverCfg cfg;
+  SolverBufs b;
+  __device__ void operator()(uint64_t i, uint64_t pos) const
+  {
+    const uint32_t p = b.dev->parity, q = 1 - p;
+    for (int v = 0; v < cfg.n_vars; ++v) {
+      b.lo[p][(uint64_t)v * cfg.pstride + pos] = b.lo[q][(uint64_t)v * cfg.pstride + i];
+      b.hi[p][(uint64_t)v * cfg.pstride + pos] = b.hi[q][(uint64_t)v * cfg.pstride + i];
+    }
+    b.lb[p][pos] = b.lb[q][i];
+    b.depth[p][pos] = b.depth[q][i];
+  }
+};
+
+struct ListChild {
+  SolverBufs b;
+  __device__ void operator()(uint64_t g, uint64_t pos) const { b.list[pos] = (uint32_t)g; }
+};
+
+template <class P, class Op>
+__global__ void __launch_bounds__(kScanBlock) scatter_kernel(const P pred, const Op op,
+                                                             const uint32_t* __restrict__ offsets)
+{
+  if (pred.skip()) return;
+  const uint64_t n = pred.size();
+  if ((uint64_t)blockIdx.x * kScanBlock >= n) return;
+  const uint64_t i = (uint64_t)blockIdx.x * kScanBlock + threadIdx.x;
+  const bool f = i < n && pred(i);
+  int total;
+  const int rank = block_excl_rank(f, total);
+  if (f) op(i, (uint64_t)offsets[blockIdx.x] + (uint64_t)rank);
+}
+
+// ---------------------------------------------------------------------
+// branching: BisectionBudgetCompositionPolicy::choose per parent
+// (policy/bisection_budget.hpp:81-262), with the C++ library's heap order
+// for equally wide candidates
+// ---------------------------------------------------------------------
+struct EnumCand {
+  uint64_t vid, domain, bits;
+  uint32_t kind, pad;
+};
+struct BisCand {
+  uint64_t vid, bis;
+  double live, orig;
+  uint32_t kind, pad;
+};
+
+struct HeapCtx {
+  const BisCand* c;
+  int relative;
+  __device__ double key(uint64_t i) const { return relative ? __ddiv_rn(c[i].live, c[i].orig) : c[i].live; }
+  __device__ bool less(uint64_t a, uint64_t b) const { return key(a) < key(b); }
+};
+
+__device__ void hp_push_hole(uint64_t* f, int64_t hole, int64_t top, uint64_t value, const HeapCtx& h)
+{
+  int64_t parent = (hole - 1) / 2;
+  while (hole > top && h.less(f[parent], value)) {
+    f[hole] = f[parent];
+    hole = parent;
+    parent = (hole - 1) / 2;
+  }
+  f[hole] = value;
+}
+
+__device__ void hp_adjust(uint64_t* f, int64_t hole, int64_t len, uint64_t value, const HeapCtx& h)
+{
+  const int64_t top = hole;
+  int64_t second = hole;
+  while (second < (len - 1) / 2) {
+    second = 2 * (second + 1);
+    if (h.less(f[second], f[second - 1])) second--;
+    f[hole] = f[second];
+    hole = second;
+  }
+  if ((len & 1) == 0 && second == (len - 2) / 2) {
+    second = 2 * (second + 1);
+    f[hole] = f[second - 1];
+    hole = second - 1;
+  }
+  hp_push_hole(f, hole, top, value, h);
+}
+
+__device__ void hp_make(uint64_t* f, int64_t len, const HeapCtx& h)
+{
+  if (len < 2) return;
+  int64_t parent = (len - 2) / 2;
+  for (;;) {
+    const uint64_t v = f[parent];
+    hp_adjust(f, parent, len, v, h);
+    if (parent == 0) return;
+    parent--;
+  }
+}
+
+__device__ __forceinline__ uint64_t int_domain(double lb, double ub)
+{
+  const double lo = ceil(lb), hi = floor(ub);
+  if (hi < lo) return 0;
+  return (uint64_t)__double2ull_rz(__dsub_rn(hi, lo)) + 1;
+}
+
+__device__ __forceinline__ uint64_t bits_for(uint64_t d)
+{
+  const uint64_t eff = d == 0 ? 1 : d;
+  uint64_t bits = 0, cap = 1;
+  while (cap < eff) {
+    cap <<= 1;
+    ++bits;
+  }
+  return bits > 1 ? bits : 1;
+}
+
+__global__ void branch_kernel(const SolverCfg cfg, const SolverBufs b)
+{
+  const SolverDev* d = b.dev;
+  if (d->done) return;
+  const uint64_t E = d->n_parents;
+  const int n = cfg.n_vars;
+  uint64_t fathomed = 0, fathomed_points = 0, bounded = 0;
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < E; k += (uint64_t)gridDim.x * blockDim.x) {
+    EnumCand* ec = reinterpret_cast<EnumCand*>(b.enum_scratch) + k * (uint64_t)n;
+    BisCand* bc = reinterpret_cast<BisCand*>(b.bis_scratch) + k * (uint64_t)n;
+    uint64_t* heap = b.heap_scratch + k * (uint64_t)n;
+    const int64_t cap = cfg.max_cycle == 0 ? 64 : cfg.max_cycle;
+    int64_t ne = 0, nb = 0, live = 0;
+    for (int v = 0; v < n; ++v) {
+      const double lb = b.plo[(uint64_t)v * cfg.e_max + k], ub = b.phi[(uint64_t)v * cfg.e_max + k];
+      if (ub > lb) ++live;
+    }
+    for (int v = 0; v < n && ne + nb < cap; ++v) {
+      const double lb = b.plo[(uint64_t)v * cfg.e_max + k], ub = b.phi[(uint64_t)v * cfg.e_max + k];
+      if (!(ub > lb)) continue;
+      const double w = __dsub_rn(ub, lb);
+      const int vk = b.kinds[v];
+      if (vk == CMN_VAR_BINARY) {
+        ec[ne] = {(uint64_t)v, 2, bits_for(2), (uint32_t)CMN_SLOT_BINARY_ENUMERATE, 0};
+        ++ne;
+      } else if (vk == CMN_VAR_INTEGER) {
+        const uint64_t dd = int_domain(lb, ub);
+        const uint64_t dm = dd > 1 ? dd : 1;
+        if (cfg.enumerate_cap == 0 || dm <= (uint64_t)cfg.enumerate_cap) {
+          ec[ne] = {(uint64_t)v, dd, bits_for(dd), (uint32_t)CMN_SLOT_INTEGER_ENUMERATE, 0};
+          ++ne;
+        } else {
+          bc[nb] = {(uint64_t)v, 0, w, w, (uint32_t)CMN_SLOT_INTEGER_PARTITION, 0};
+          ++nb;
+        }
+      } else {
+        bc[nb] = {(uint64_t)v, 0, w, w, (uint32_t)CMN_SLOT_CONTINUOUS, 0};
+        ++nb;
+      }
+    }
+    ParentInfo pi;
+    SlotPlan* sp = b.slots + k * (uint64_t)cfg.max_slots;
+    if (ne + nb == 0) {
+      pi.count = 0;
+      pi.nreg = 1;
+      pi.fathom = 1;
+    } else {
+      for (int64_t i = 1; i < ne; ++i) {  // stable insertion sort by cost
+        const EnumCand x = ec[i];
+        int64_t j = i - 1;
+        while (j >= 0 && x.bits < ec[j].bits) {
+          ec[j + 1] = ec[j];
+          --j;
+        }
+        ec[j + 1] = x;
+      }
+      uint64_t remaining = (uint64_t)cfg.log2C;
+      int64_t taken = 0;
+      for (; taken < ne; ++taken) {
+        if (ec[taken].bits > remaining) break;
+        remaining -= ec[taken].bits;
+      }
+      for (int64_t i = taken; i < ne; ++i) {
+        if (ec[i].kind == CMN_SLOT_INTEGER_ENUMERATE) {
+          const uint64_t v = ec[i].vid;
+          const double w = __dsub_rn(b.phi[v * cfg.e_max + k], b.plo[v * cfg.e_max + k]);
+          bc[nb] = {v, 0, w, w, (uint32_t)CMN_SLOT_INTEGER_PARTITION, 0};
+          ++nb;
+        }
+      }
+      for (int64_t i = 0; i < nb; ++i) heap[i] = (uint64_t)i;
+      const HeapCtx h = {bc, cfg.relative};
+      hp_make(heap, nb, h);
+      uint64_t spent = 0;
+      for (; spent < remaining && nb > 0; ++spent) {
+        // pop_heap, halve the top, push_heap
+        if (nb > 1) {
+          const uint64_t v = heap[nb - 1];
+          heap[nb - 1] = heap[0];
+          hp_adjust(heap, 0, nb - 1, v, h);
+        }
+        BisCand* c = &bc[heap[nb - 1]];
+        c->live = __ddiv_rn(c->live, 2.0);
+        ++c->bis;
+        hp_push_hole(heap, nb - 1, 0, heap[nb - 1], h);
+      }
+      for (uint64_t q = spent; q < remaining; ++q) {
+        int64_t widest = 0;
+        for (int64_t i = 1; i < taken; ++i)
+          if (ec[i].bits > ec[widest].bits) widest = i;
+        ++ec[widest].bits;
+      }
+      uint32_t count = 0;
+      bool all_enum = true;
+      for (int64_t i = 0; i < taken; ++i) {
+        sp[count] = {1ULL << ec[i].bits, 0, ec[i].domain, (uint32_t)ec[i].vid, ec[i].kind};
+        ++count;
+      }
+      for (int64_t i = 0; i < nb; ++i) {
+        if (bc[i].bis == 0) continue;
+        const uint64_t w = 1ULL << bc[i].bis;
+        sp[count] = {w, 0, w, (uint32_t)bc[i].vid, bc[i].kind};
+        all_enum = false;
+        ++count;
+      }
+      uint64_t running = 1;
+      for (uint32_t j = 0; j < count; ++j) {
+        sp[j].prefix = running;
+        running *= sp[j].width;
+      }
+      pi.count = count;
+      pi.nreg = running;
+      pi.fathom = (live <= (int64_t)count && all_enum) ? 1 : 0;
+    }
+    b.pinfo[k] = pi;
+    if (pi.fathom) {
+      ++fathomed;
+      fathomed_points += pi.nreg;
+    } else {
+      bounded += pi.nreg;
+    }
+  }
+  if (fathomed) atomicAdd((unsigned long long*)&b.dev->counters.fathomed, (unsigned long long)fathomed);
+  if (fathomed_points)
+    atomicAdd((unsigned long long*)&b.dev->counters.fathomed_points, (unsigned long long)fathomed_points);
+  if (bounded) atomicAdd((unsigned long long*)&b.dev->counters.bounded, (unsigned long long)bounded);
+}
+
+// ---------------------------------------------------------------------
+// incumbent, prune accounting, pool finish
+// ---------------------------------------------------------------------
+__global__ void incumbent_kernel(const SolverBufs b, const Cand* __restrict__ best)
+{
+  SolverDev* d = b.dev;
+  if (d->done) return;
+  const Cand c = *best;
+  d->improved = 0;
+  if (c.value < DBL_MAX && c.value < d->gub) {
+    d->gub = c.value;
+    d->best = c;
+    d->have_best = 1;
+    d->improved = 1;
+  }
+}
+
+// counts of this iteration's child verdicts (search/driver.hpp:319-350)
+__global__ void prune_count_kernel(const SolverCfg cfg, const SolverBufs b)
+{
+  SolverDev* d = b.dev;
+  if (d->done) return;
+  const uint64_t n = d->n_children;
+  const double gub = d->gub;
+  unsigned long long dup = 0, inf = 0, dom = 0, kept = 0, sampled = 0;
+  for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n; g += (uint64_t)gridDim.x * blockDim.x) {
+    const uint8_t s = b.cstate[g];
+    if (s == kChildNone) continue;
+    if (cfg.sample_all || s == kChildEligible) ++sampled;
+    if (s == kChildDuplicate) ++dup;
+    else if (s == kChildInfeasible) ++inf;
+    else if (s == kChildDominated || b.clb[g] > gub) ++dom;
+    else ++kept;
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    dup += __shfl_down_sync(0xffffffffu, dup, off);
+    inf += __shfl_down_sync(0xffffffffu, inf, off);
+    dom += __shfl_down_sync(0xffffffffu, dom, off);
+    kept += __shfl_down_sync(0xffffffffu, kept, off);
+    sampled += __shfl_down_sync(0xffffffffu, sampled, off);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (dup) atomicAdd((unsigned long long*)&d->counters.pruned_duplicate, dup);
+    if (inf) atomicAdd((unsigned long long*)&d->counters.pruned_infeasible, inf);
+    if (dom) atomicAdd((unsigned long long*)&d->counters.pruned_dominated, dom);
+    if (kept) atomicAdd((unsigned long long*)&d->counters.enqueued, kept);
+    if (sampled) atomicAdd((unsigned long long*)&d->counters.sampled, sampled * cfg.S);
+  }
+}
+
+// FP64 evaluations of this iteration: every non-duplicate child in FP64
+// mode, the certify list in the screened mode.
+__global__ void eval_count_kernel(const SolverCfg cfg, const SolverBufs b)
+{
+  SolverDev* d = b.dev;
+  if (d->done) return;
+  const uint64_t n = d->n_children;
+  unsigned long long screened = 0, certified = 0;
+  for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n; g += (uint64_t)gridDim.x * blockDim.x) {
+    const uint8_t s = b.cstate[g];
+    if (s == kChildNone || s == kChildDuplicate) continue;
+    if (cfg.precision == CMN_PRECISION_FP32_SCREEN) ++screened;
+    else ++certified;
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    screened += __shfl_down_sync(0xffffffffu, screened, off);
+    certified += __shfl_down_sync(0xffffffffu, certified, off);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (screened) atomicAdd((unsigned long long*)&d->counters.screened_fp32, screened);
+    if (certified) atomicAdd((unsigned long long*)&d->counters.certified_fp64, certified);
+  }
+}
+
+__global__ void certify_count_kernel(const SolverBufs b)
+{
+  SolverDev* d = b.dev;
+  if (d->done) return;
+  d->counters.certified_fp64 += d->certify_count;
+}
+
+__global__ void size_kernel(const SolverCfg cfg, const SolverBufs b)
+{
+  SolverDev* d = b.dev;
+  if (d->done) return;
+  d->new_size = d->remaining + d->kept;
+  d->evict = d->new_size > cfg.cap ? 1 : 0;
+}
+
+// fold evicted entries into the dropped floor (search/budget.hpp:190-209)
+__global__ void evict_account_kernel(const SolverBufs b)
+{
+  SolverDev* d = b.dev;
+  if (d->done || !d->evict) return;
+  const uint64_t n = d->new_size;
+  const double gub = d->gub;
+  const double* lb = b.lb[1 - d->parity];
+  unsigned long long viable = 0, dominated = 0;
+  uint64_t mkey = ~0ULL;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    if (b.sel[i]) continue;
+    const double x = lb[i];
+    if (x <= gub) {
+      ++viable;
+      const uint64_t k = lb_key(x);
+      mkey = k < mkey ? k : mkey;
+    } else {
+      ++dominated;
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    viable += __shfl_down_sync(0xffffffffu, viable, off);
+    dominated += __shfl_down_sync(0xffffffffu, dominated, off);
+    const uint64_t o = __shfl_down_sync(0xffffffffu, mkey, off);
+    mkey = o < mkey ? o : mkey;
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (viable) atomicAdd((unsigned long long*)&d->counters.dropped_viable, viable);
+    if (dominated) atomicAdd((unsigned long long*)&d->counters.dropped_dominated, dominated);
+    if (mkey != ~0ULL) atomicMin((unsigned long long*)&d->dropped_min_key, (unsigned long long)mkey);
+  }
+}
+
+__global__ void finish_kernel(const SolverCfg cfg, const SolverBufs b)
+{
+  SolverDev* d = b.dev;
+  if (d->done) return;
+  if (d->evict) {
+    d->pool_size = cfg.cap;  // survivors were moved back into the current buffer
+  } else {
+    d->pool_size = d->new_size;
+    d->parity = 1 - d->parity;
+  }
+  if (d->dropped_min_key != ~0ULL) d->dropped_lb_min = key_to_lb(d->dropped_min_key);
+  if (d->pool_size > d->counters.peak_frontier) d->counters.peak_frontier = d->pool_size;
+  d->pool_min_key = ~0ULL;
+}
+
+__global__ void pool_min_kernel(const SolverBufs b, uint64_t* viable_out)
+{
+  SolverDev* d = b.dev;
+  const uint64_t n = d->pool_size;
+  const double* lb = b.lb[d->parity];
+  const double gub = d->gub;
+  uint64_t mkey = ~0ULL;
+  unsigned long long viable = 0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t k = lb_key(lb[i]);
+    mkey = k < mkey ? k : mkey;
+    if (lb[i] <= gub) ++viable;
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    const uint64_t o = __shfl_down_sync(0xffffffffu, mkey, off);
+    mkey = o < mkey ? o : mkey;
+    viable += __shfl_down_sync(0xffffffffu, viable, off);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (mkey != ~0ULL) atomicMin((unsigned long long*)&d->pool_min_key, (unsigned long long)mkey);
+    if (viable_out && viable) atomicAdd((unsigned long long*)viable_out, viable);
+  }
+}
+
+__global__ void pool_min_reset_kernel(const SolverBufs b, uint64_t* viable_out)
+{
+  b.dev->pool_min_key = ~0ULL;
+  if (viable_out) *viable_out = 0;
+}
+
+// ---------------------------------------------------------------------
+// host: enqueue one iteration
+// ---------------------------------------------------------------------
+template <class P>
+static cudaError_t compact(const P& pred, uint64_t max_items, const uint64_t* n_items_dev, uint64_t* total_dev,
+                           const SolverBufs& b, const uint32_t* active, cudaStream_t s)
+{
+  const int grid = (int)((max_items + kScanBlock - 1) / kScanBlock);
+  count_kernel<P><<<grid, kScanBlock, 0, s>>>(pred, b.block_counts);
+  scan_kernel<<<1, 1024, 0, s>>>(b.block_counts, b.block_offsets, n_items_dev, total_dev, active, &b.dev->done);
+  return cudaGetLastError();
+}
+
+template <class P, class Op>
+static cudaError_t scatter(const P& pred, const Op& op, uint64_t max_items, cudaStream_t s, const SolverBufs& b)
+{
+  const int grid = (int)((max_items + kScanBlock - 1) / kScanBlock);
+  scatter_kernel<P, Op><<<grid, kScanBlock, 0, s>>>(pred, op, b.block_offsets);
+  return cudaGetLastError();
+}
+
+static void radix_select(const SolverCfg& cfg, const SolverBufs& b, int which, uint64_t max_items, cudaStream_t s)
+{
+  radix_init_kernel<<<1, 256, 0, s>>>(cfg, b, which);
+  const int grid = (int)std::min<uint64_t>((max_items + 255) / 256, 4096);
+  // digits from the most significant: 6 x 11 bits minus the 2 top bits
+  const int shifts[6] = {53, 42, 31, 20, 9, 0};
+  const int bits[6] = {11, 11, 11, 11, 11, 9};
+  for (int p = 0; p < 6; ++p) {
+    radix_hist_kernel<<<grid, 256, 0, s>>>(cfg, b, which, shifts[p], bits[p]);
+    radix_pick_kernel<<<1, 32, 0, s>>>(b, shifts[p], bits[p]);
+  }
+  // ranks among entries equal to the threshold, then the marks
+  const uint64_t* n_dev = which == 0 ? &b.dev->pool_size : &b.dev->new_size;
+  EqKey eq{b, which};
+  compact(eq, max_items, n_dev, nullptr, b, &b.radix->active, s);
+  const int mgrid = (int)((max_items + kScanBlock - 1) / kScanBlock);
+  mark_kernel<<<mgrid, kScanBlock, 0, s>>>(cfg, b, which, b.block_offsets);
+}
+
+static void mark(const cudaEvent_t* marks, int i, cudaStream_t s)
+{
+  if (marks) cudaEventRecordWithFlags(marks[i], s, cudaEventRecordExternal);
+}
+
+cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval_grid, int sample_grid,
+                             cudaStream_t s, const cudaEvent_t* marks)
+{
+  const uint64_t max_children = cfg.e_max << cfg.log2C;
+  const uint64_t max_pool = cfg.pstride;
+  mark(marks, 0, s);
+  begin_kernel<<<1, 1, 0, s>>>(cfg, b);
+
+  // (1) select the E best parents and stage them
+  radix_select(cfg, b, 0, cfg.cap, s);
+  SelPool selected{b, 0, true};
+  compact(selected, cfg.cap, &b.dev->pool_size, nullptr, b, nullptr, s);
+  scatter(selected, GatherParents{cfg, b}, cfg.cap, s, b);
+
+  // (2) branch
+  {
+    const int grid = (int)std::min<uint64_t>((cfg.e_max + 127) / 128, 2048);
+    branch_kernel<<<grid, 128, 0, s>>>(cfg, b);
+  }
+  mark(marks, 1, s);
+
+  // (3) bound every child: FP64, or FP32 screen + FP64 certify
+  EvalArgs ea = {};
+  ea.n_vars = cfg.n_vars;
+  ea.n_slots = cfg.n_slots;
+  ea.log2C = cfg.log2C;
+  ea.plo = b.plo;
+  ea.phi = b.phi;
+  ea.pstride = cfg.e_max;
+  ea.pinfo = b.pinfo;
+  ea.slots = b.slots;
+  ea.max_slots = cfg.max_slots;
+  ea.n_children_dev = &b.dev->n_children;
+  ea.gub = &b.dev->gub;
+  ea.done = &b.dev->done;
+  ea.out_lb = b.clb;
+  ea.out_flag = b.cstate;
+  ea.prog_len = cfg.prog_len;
+  cudaError_t e;
+  if (cfg.precision == CMN_PRECISION_FP32_SCREEN) {
+    ea.prog = b.prog32;
+    e = launch_eval(ea, 2, true, eval_grid, kEvalThreads, s);
+    if (e != cudaSuccess) return e;
+    ScreenedChild sc{b};
+    compact(sc, max_children, &b.dev->n_children, &b.dev->certify_count, b, nullptr, s);
+    scatter(sc, ListChild{b}, max_children, s, b);
+    EvalArgs ca = ea;
+    ca.prog = b.prog64;
+    ca.list = b.list;
+    ca.list_count = &b.dev->certify_count;
+    e = launch_eval(ca, 3, false, eval_grid, kEvalThreads, s);
+    if (e != cudaSuccess) return e;
+  } else {
+    ea.prog = b.prog64;
+    e = launch_eval(ea, 1, false, eval_grid, kEvalThreads, s);
+    if (e != cudaSuccess) return e;
+  }
+  {
+    const int grid = (int)std::min<uint64_t>((max_children + 255) / 256, 4096);
+    eval_count_kernel<<<grid, 256, 0, s>>>(cfg, b);
+    if (cfg.precision == CMN_PRECISION_FP32_SCREEN) certify_count_kernel<<<1, 1, 0, s>>>(b);
+  }
+  mark(marks, 2, s);
+
+  // (4) sample, ArgMin, incumbent update and witness
+  SampleArgs sa = {};
+  sa.prog = b.prog64;
+  sa.prog_len = cfg.prog_len;
+  sa.n_vars = cfg.n_vars;
+  sa.n_slots = cfg.n_slots;
+  sa.log2C = cfg.log2C;
+  sa.plo = b.plo;
+  sa.phi = b.phi;
+  sa.pstride = cfg.e_max;
+  sa.pinfo = b.pinfo;
+  sa.slots = b.slots;
+  sa.max_slots = cfg.max_slots;
+  sa.var_kinds = b.kinds;
+  sa.root_lb = b.root_lb;
+  sa.root_ub = b.root_ub;
+  sa.n_children_dev = &b.dev->n_children;
+  sa.S = cfg.S;
+  sa.salt_base_dev = &b.dev->salt_base;
+  sa.sample_all = cfg.sample_all;
+  sa.state = b.cstate;
+  sa.gub = &b.dev->gub;
+  sa.done = &b.dev->done;
+  sa.block_best = b.block_best;
+  sa.rejected = (unsigned long long*)&b.dev->counters.witness_rejected;
+  e = launch_sample(sa, sample_grid, kEvalThreads, s);
+  if (e != cudaSuccess) return e;
+  Cand* best = b.block_best + b.n_block_best - 1;  // last entry holds the result
+  e = launch_reduce_cand(b.block_best, sample_grid, best, s);
+  if (e != cudaSuccess) return e;
+  incumbent_kernel<<<1, 1, 0, s>>>(b, best);
+  e = launch_witness(best, b.plo, b.phi, cfg.e_max, b.pinfo, b.slots, cfg.max_slots, b.kinds, cfg.n_vars, cfg.S, 0,
+                     &b.dev->salt_base, 0, &b.dev->improved, b.best_point, s);
+  if (e != cudaSuccess) return e;
+  mark(marks, 3, s);
+
+  // (5) prune with the new incumbent and rebuild the pool
+  {
+    const int grid = (int)std::min<uint64_t>((max_children + 255) / 256, 4096);
+    prune_count_kernel<<<grid, 256, 0, s>>>(cfg, b);
+  }
+  SelPool unselected{b, 0, false};
+  compact(unselected, cfg.cap, &b.dev->pool_size, &b.dev->remaining, b, nullptr, s);
+  scatter(unselected, CopyRemaining{cfg, b}, cfg.cap, s, b);
+  KeptChild kept{b};
+  compact(kept, max_children, &b.dev->n_children, &b.dev->kept, b, nullptr, s);
+  scatter(kept, AppendChild{cfg, b}, max_children, s, b);
+  size_kernel<<<1, 1, 0, s>>>(cfg, b);
+
+  // (6) over the cap: keep the `cap` best, fold the rest into the floor
+  radix_select(cfg, b, 1, max_pool, s);
+  {
+    const int grid = (int)std::min<uint64_t>((max_pool + 255) / 256, 4096);
+    evict_account_kernel<<<grid, 256, 0, s>>>(b);
+  }
+  SelPool keep{b, 1, true};
+  compact(keep, max_pool, &b.dev->new_size, nullptr, b, nullptr, s);
+  scatter(keep, CopyEvictKeep{cfg, b}, max_pool, s, b);
+  finish_kernel<<<1, 1, 0, s>>>(cfg, b);
+  {
+    const int grid = (int)std::min<uint64_t>((max_pool + 255) / 256, 4096);
+    pool_min_kernel<<<grid, 256, 0, s>>>(b, nullptr);
+  }
+  mark(marks, 4, s);
+  return cudaGetLastError();
+}
+
+cudaError_t solver_init(const SolverCfg& cfg, const SolverBufs& b, const double* root_lb_dev,
+                        const double* root_ub_dev, double gub0, cudaStream_t s)
+{
+  init_kernel<<<1, 256, 0, s>>>(cfg, b, root_lb_dev, root_ub_dev, gub0);
+  return cudaGetLastError();
+}
+
+cudaError_t solver_pool_stats(const SolverCfg& cfg, const SolverBufs& b, uint64_t* viable_dev, cudaStream_t s)
+{
+  pool_min_reset_kernel<<<1, 1, 0, s>>>(b, viable_dev);
+  const int grid = (int)std::min<uint64_t>((cfg.pstride + 255) / 256, 4096);
+  pool_min_kernel<<<grid, 256, 0, s>>>(b, viable_dev);
+  return cudaGetLastError();
+}
+
+}  // namespace cmn

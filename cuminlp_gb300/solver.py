@@ -1,0 +1,261 @@
+"""Python face of the C ABI: region roles, batched evaluation and the
+device-resident solver.
+
+Role objects mirror the reference's plugin boundary
+(backend/backend.hpp:81-219): ``Bounder.bound(box, var_ids, widths)``
+returns per-region ``feasible`` and ``obj_lb`` views valid until the next
+call; ``Sampler.sample(..., salt)`` and ``Enumerator.enumerate(...)``
+return a candidate (found, value, point, index).  ``solve()`` mirrors
+``SearchDriver::solve`` (search/driver.hpp:137-537) and returns the
+``SolveOutcome`` fields.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _abi as A
+from ._lib import check, lib
+from .problem import Problem
+
+
+class DeviceProblem:
+    """A Problem compiled and resident on the current CUDA device."""
+
+    def __init__(self, problem: Problem):
+        self.problem = problem
+        desc, self._keep = problem.desc()
+        h = C.c_void_p()
+        check(lib().cmn_problem_create(C.byref(desc), C.byref(h)))
+        self.handle = h
+        self.n_vars = problem.n_vars
+
+    def info(self) -> dict:
+        inf = A.ProblemInfo()
+        check(lib().cmn_problem_get_info(self.handle, C.byref(inf)))
+        return {f: getattr(inf, f) for f, _ in A.ProblemInfo._fields_}
+
+    def cost_model(self) -> dict:
+        cm = A.CostModel()
+        check(lib().cmn_cost_model_get(self.handle, C.byref(cm)))
+        return {f: int(getattr(cm, f)) for f, _ in A.CostModel._fields_}
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().cmn_problem_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class OverBudgetError(RuntimeError):
+    def __init__(self, message, facts: dict):
+        super().__init__(message)
+        self.facts = facts
+
+
+@dataclass
+class CandidateResult:
+    found: bool
+    value: float
+    point: np.ndarray
+    index: int
+
+
+class _Role:
+    kind = -1
+
+    def __init__(self, dp: DeviceProblem, slot_kinds, n_regions: int, budget_bytes: int = 0,
+                 sample_points: int = 1):
+        self.dp = dp
+        self.slot_kinds = np.ascontiguousarray(slot_kinds, dtype=np.uint8)
+        h = C.c_void_p()
+        facts = A.OverBudget()
+        st = lib().cmn_role_build(dp.handle, self.kind, A.ptr(self.slot_kinds) if len(self.slot_kinds) else None,
+                                  len(self.slot_kinds), int(n_regions), int(budget_bytes), int(sample_points),
+                                  C.byref(h), C.byref(facts))
+        if st == 5:  # OVER_BUDGET
+            msg = lib().cmn_last_error().decode()
+            raise OverBudgetError(msg, {f: int(getattr(facts, f)) for f, _ in A.OverBudget._fields_})
+        check(st)
+        self.handle = h
+
+    @property
+    def n_regions(self) -> int:
+        return int(lib().cmn_role_n_regions(self.handle))
+
+    @property
+    def n_elements(self) -> int:
+        return int(lib().cmn_role_n_elements(self.handle))
+
+    def _args(self, box, var_ids, widths):
+        box = np.ascontiguousarray(box, dtype=np.float64)
+        vids = np.ascontiguousarray(var_ids, dtype=np.uint64)
+        w = np.ascontiguousarray(widths, dtype=np.uint64)
+        self._keep = (box, vids, w)
+        return A.ptr(box), A.ptr(vids) if len(vids) else None, A.ptr(w) if len(w) else None
+
+    def _candidate(self, cand: A.Candidate) -> CandidateResult:
+        n = self.dp.n_vars
+        pt = np.ctypeslib.as_array(cand.point, shape=(n,)).copy()
+        return CandidateResult(bool(cand.found), float(cand.value), pt, int(cand.index))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().cmn_role_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Bounder(_Role):
+    kind = A.ROLE_BOUNDER
+
+    def bound(self, box, var_ids, widths):
+        fp = C.POINTER(C.c_uint8)()
+        lp = C.POINTER(C.c_double)()
+        n = C.c_uint64()
+        check(lib().cmn_bound(self.handle, *self._args(box, var_ids, widths), C.byref(fp), C.byref(lp), C.byref(n)))
+        nr = n.value
+        return (np.ctypeslib.as_array(fp, shape=(nr,)), np.ctypeslib.as_array(lp, shape=(nr,)))
+
+
+class Sampler(_Role):
+    kind = A.ROLE_SAMPLER
+
+    def sample(self, box, var_ids, widths, salt: int) -> CandidateResult:
+        cand = A.Candidate()
+        check(lib().cmn_sample(self.handle, *self._args(box, var_ids, widths), int(salt), C.byref(cand)))
+        return self._candidate(cand)
+
+
+class Enumerator(_Role):
+    kind = A.ROLE_ENUMERATOR
+
+    def enumerate(self, box, var_ids, widths) -> CandidateResult:
+        cand = A.Candidate()
+        check(lib().cmn_enumerate(self.handle, *self._args(box, var_ids, widths), C.byref(cand)))
+        return self._candidate(cand)
+
+
+def eval_boxes(dp: DeviceProblem, lo: np.ndarray, hi: np.ndarray, precision: int = A.PRECISION_FP64):
+    """Fused evaluation of host boxes given as (n_vars, n_boxes) planes."""
+    lo = np.ascontiguousarray(lo, dtype=np.float64)
+    hi = np.ascontiguousarray(hi, dtype=np.float64)
+    nb = lo.shape[1]
+    lb = np.empty(nb)
+    ub = np.empty(nb)
+    fe = np.empty(nb, dtype=np.uint8)
+    check(lib().cmn_eval_boxes(dp.handle, precision, A.ptr(lo), A.ptr(hi), nb, nb, A.ptr(lb), A.ptr(ub), A.ptr(fe),
+                               0, None))
+    return lb, ub, fe
+
+
+def eval_boxes_device(dp: DeviceProblem, lo_ptr: int, hi_ptr: int, n_boxes: int, stride: int, lb_ptr: int,
+                      ub_ptr: int, feas_ptr: int, precision: int = A.PRECISION_FP64, stream: int = 0):
+    """Asynchronous fused evaluation of device-resident planes."""
+    check(lib().cmn_eval_boxes(dp.handle, precision, lo_ptr, hi_ptr, n_boxes, stride, lb_ptr, ub_ptr, feas_ptr, 1,
+                               stream or None))
+
+
+def default_options(**kw) -> A.SolveOptions:
+    o = A.SolveOptions()
+    lib().cmn_solve_options_default(C.byref(o))
+    for k, v in kw.items():
+        if k == "precision" and isinstance(v, str):
+            v = A.PRECISION_FP32_SCREEN if v.lower().startswith("fp32") else A.PRECISION_FP64
+        if k == "known_primal_bound" and v is not None:
+            o.has_known_primal = 1
+        if v is None:
+            continue
+        if not hasattr(o, k):
+            raise TypeError(f"unknown solve option {k}")
+        setattr(o, k, v)
+    return o
+
+
+class Solver:
+    """Incremental handle over the batched device solver."""
+
+    def __init__(self, dp: DeviceProblem, **options):
+        self.dp = dp
+        self.options = default_options(**options)
+        h = C.c_void_p()
+        check(lib().cmn_solver_create(dp.handle, C.byref(self.options), C.byref(h)))
+        self.handle = h
+
+    def step(self, max_iterations: int = 0) -> None:
+        check(lib().cmn_solver_step(self.handle, int(max_iterations)))
+
+    def bounds(self):
+        lb, ub = C.c_double(), C.c_double()
+        check(lib().cmn_query_bounds(self.handle, C.byref(lb), C.byref(ub)))
+        return lb.value, ub.value
+
+    def gap(self) -> float:
+        g = C.c_double()
+        check(lib().cmn_query_gap(self.handle, C.byref(g)))
+        return g.value
+
+    def incumbent(self):
+        pt = np.empty(self.dp.n_vars)
+        f = C.c_int32()
+        check(lib().cmn_query_incumbent(self.handle, A.ptr(pt), C.byref(f)))
+        return bool(f.value), pt
+
+    def outcome(self) -> dict:
+        o = A.Outcome()
+        check(lib().cmn_solver_outcome(self.handle, C.byref(o)))
+        d = A.outcome_dict(o)
+        found, pt = self.incumbent()
+        d["best_point"] = pt if found else np.array([])
+        return d
+
+    def frontier(self, room: int = 1 << 20):
+        """(boxes [count, 2n] interleaved, lower bounds, depths) in pool order."""
+        n = self.dp.n_vars
+        cnt = C.c_uint64()
+        check(lib().cmn_solver_frontier(self.handle, None, None, None, 0, C.byref(cnt)))
+        m = min(cnt.value, room)
+        boxes = np.empty((m, 2 * n))
+        lb = np.empty(m)
+        depth = np.empty(m, dtype=np.uint32)
+        if m:
+            check(lib().cmn_solver_frontier(self.handle, A.ptr(boxes), A.ptr(lb), A.ptr(depth), m, C.byref(cnt)))
+        return boxes, lb, depth
+
+    @property
+    def stream(self) -> int:
+        return lib().cmn_solver_stream(self.handle) or 0
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().cmn_solver_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def solve(problem: Problem | DeviceProblem, **options) -> dict:
+    dp = problem if isinstance(problem, DeviceProblem) else DeviceProblem(problem)
+    s = Solver(dp, **options)
+    try:
+        s.step(0)
+        return s.outcome()
+    finally:
+        s.close()

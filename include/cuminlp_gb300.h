@@ -1,0 +1,390 @@
+/*
+ * cuminlp_gb300.h -- C ABI of the GB300-native interval branch-and-bound
+ * hot path.
+ *
+ * Everything crosses this boundary as plain pointers, sizes and POD structs;
+ * no exception, no C++ type and no torch type leaves the library.  Every
+ * entry point returns a cmn_status; on failure cmn_last_error() holds a
+ * human-readable message for the calling thread.
+ *
+ * Each declaration names the interface of the reference (CuMINLPSearch,
+ * include/cuminlp/...) that it replaces, as file:line.
+ *
+ * Conventions
+ *   - A box is n_vars (lb, ub) pairs of doubles, interleaved: the exact
+ *     memory layout of `cu::interval<double>[n_vars]`
+ *     (backend/backend.hpp:39-44, Region::box).
+ *   - Pointers returned by a role call are views into storage the role
+ *     owns, valid until the next call on that role
+ *     (backend/backend.hpp:52-54, 66-67).
+ *   - One handle is never used from two threads at once.
+ */
+#ifndef CUMINLP_GB300_H
+#define CUMINLP_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------------
+ * Status codes.  Mirror the reference's exception hierarchy
+ * (errors.hpp:11-57: InvalidDAG, InvalidProblem, ShapeMismatch,
+ * InvalidConfiguration, ResourceExhausted), CUDAError
+ * (cuda_utils.cuh:22-35) and OverBudgetError (backend/backend.hpp:236-287).
+ * ------------------------------------------------------------------- */
+typedef enum cmn_status {
+  CMN_OK = 0,
+  CMN_INVALID_DAG = 1,
+  CMN_INVALID_PROBLEM = 2,
+  CMN_SHAPE_MISMATCH = 3,
+  CMN_INVALID_CONFIGURATION = 4,
+  CMN_OVER_BUDGET = 5,
+  CMN_CUDA_ERROR = 6,
+  CMN_TIMEOUT = 7,
+  CMN_INTERNAL = 8
+} cmn_status;
+
+/* Operators, in the order of model::Op (model/dag.hpp:12-33). */
+typedef enum cmn_op {
+  CMN_OP_VAR = 0,
+  CMN_OP_CONST = 1,
+  CMN_OP_ADD = 2,
+  CMN_OP_SUB = 3,
+  CMN_OP_MUL = 4,
+  CMN_OP_DIV = 5,
+  CMN_OP_SQR = 6,
+  CMN_OP_NEG = 7,
+  CMN_OP_EXP = 8,
+  CMN_OP_LOG = 9,
+  CMN_OP_SQRT = 10,
+  CMN_OP_SIN = 11,
+  CMN_OP_COS = 12,
+  CMN_OP_TANH = 13,
+  CMN_OP_POWN = 14,
+  CMN_OP_POW = 15,
+  CMN_OP_ABS = 16,
+  CMN_OP_MIN = 17,
+  CMN_OP_MAX = 18
+} cmn_op;
+
+/* model::VarKind (model/problem.hpp:16-21). */
+typedef enum cmn_var_kind {
+  CMN_VAR_CONTINUOUS = 0,
+  CMN_VAR_INTEGER = 1,
+  CMN_VAR_BINARY = 2
+} cmn_var_kind;
+
+/* model::Cmp (model/problem.hpp:22-26). */
+typedef enum cmn_cmp { CMN_CMP_LE = 0, CMN_CMP_EQ = 1 } cmn_cmp;
+
+/* region::SlotKind (region/slot.hpp:12-18). */
+typedef enum cmn_slot_kind {
+  CMN_SLOT_CONTINUOUS = 0,
+  CMN_SLOT_INTEGER_PARTITION = 1,
+  CMN_SLOT_INTEGER_ENUMERATE = 2,
+  CMN_SLOT_BINARY_ENUMERATE = 3
+} cmn_slot_kind;
+
+/* One model::DAGNode (model/dag.hpp:58-68), flattened.  `in0`/`in1` are
+ * operand node ids (-1 when absent); `n_in` says how many are used.  The
+ * payload union of the reference becomes three plain fields, of which the
+ * one matching `op` is read: `constant` (Const), `var_index` (Var),
+ * `int_exp` (PowN). */
+typedef struct cmn_node {
+  int32_t op;
+  int32_t n_in;
+  int64_t in0;
+  int64_t in1;
+  int64_t var_index;
+  double constant;
+  int32_t int_exp;
+  int32_t reserved;
+} cmn_node;
+
+/* model::ConstraintRef (model/problem.hpp:34-40). */
+typedef struct cmn_constraint {
+  int64_t root;
+  int32_t cmp;
+  int32_t reserved;
+  double rhs;
+} cmn_constraint;
+
+/* The flattened model::Problem<double> (model/problem.hpp:195-358). */
+typedef struct cmn_problem_desc {
+  const cmn_node* nodes;
+  int64_t n_nodes;
+  const double* var_lb;
+  const double* var_ub;
+  const int32_t* var_kinds;
+  int64_t n_vars;
+  int64_t objective_root;
+  const cmn_constraint* constraints;
+  int64_t n_constraints;
+} cmn_problem_desc;
+
+typedef struct cmn_problem cmn_problem; /* opaque, owns device copies */
+
+/* What the library derived from a problem when it was created. */
+typedef struct cmn_problem_info {
+  int64_t n_vars;
+  int64_t n_constraints;
+  int64_t n_nodes;
+  int64_t buffer_node_count;  /* backend/graph/cost.hpp:38-68 */
+  int64_t program_length;     /* fused-evaluator instructions */
+  int64_t program_slots;      /* shared-memory value slots per box */
+  double flops_per_box;       /* algorithmic FP64 ops of one interval eval */
+  double point_flops_per_box; /* algorithmic FP64 ops of one point eval */
+  double bytes_per_box;       /* algorithmic HBM bytes of one box eval */
+} cmn_problem_info;
+
+/* Thread-local message describing the last failure on this thread. */
+const char* cmn_last_error(void);
+
+/* Library version string. */
+const char* cmn_version(void);
+
+/* Builds a problem from a flattened DAG and validates it exactly as
+ * Problem::validate() does (model/problem.hpp:282-355), then uploads the
+ * compiled evaluation program to the current CUDA device. */
+cmn_status cmn_problem_create(const cmn_problem_desc* desc,
+                              cmn_problem** out);
+void cmn_problem_destroy(cmn_problem* problem);
+cmn_status cmn_problem_get_info(const cmn_problem* problem,
+                                cmn_problem_info* out);
+
+/* backend::RegionCostModel (backend/cost_model.hpp:26-76) of the fused
+ * backend: device bytes per sample / region and a fixed per-role part. */
+typedef struct cmn_cost_model {
+  uint64_t sampler_bytes_per_sample;
+  uint64_t bound_bytes_per_region;
+  uint64_t exact_bytes_per_region;
+  uint64_t fixed_bytes;
+} cmn_cost_model;
+/* Replaces RegionBackendFactory::cost_model (backend/backend.hpp:200-201)
+ * and graph::cost_model_for (backend/graph/cost.hpp:83-99). */
+cmn_status cmn_cost_model_get(const cmn_problem* problem, cmn_cost_model* out);
+
+/* ---------------------------------------------------------------------
+ * Region roles: the plugin boundary of the reference
+ * (backend/backend.hpp:81-219).  A role is built once per Composition
+ * (its slot kinds) and launched per box with per-launch var_ids/widths.
+ * ------------------------------------------------------------------- */
+typedef enum cmn_role_kind {
+  CMN_ROLE_BOUNDER = 0,    /* RegionBounder     backend/backend.hpp:93-101 */
+  CMN_ROLE_SAMPLER = 1,    /* RegionSampler     backend/backend.hpp:81-90  */
+  CMN_ROLE_ENUMERATOR = 2  /* RegionEnumerator  backend/backend.hpp:108-116 */
+} cmn_role_kind;
+
+typedef struct cmn_role cmn_role; /* opaque */
+
+/* backend::OverBudget facts (backend/backend.hpp:236-260). */
+typedef struct cmn_over_budget {
+  uint64_t needed_bytes;
+  uint64_t budget_bytes;
+  uint64_t n_regions;
+  uint64_t elements_per_region;
+  uint64_t bytes_per_element;
+} cmn_over_budget;
+
+/* backend::CandidateResult (backend/backend.hpp:57-64).  `point` is all-NaN
+ * when `found` is 0; `value` is +inf then. */
+typedef struct cmn_candidate {
+  int32_t found;
+  int32_t reserved;
+  double value;
+  const double* point;
+  int64_t index;
+} cmn_candidate;
+
+/* Replaces RegionBackendFactory::build_subdivision for one role
+ * (backend/backend.hpp:215-219; graph/replay.cuh:264-521 GraphReplay::build).
+ * `budget_bytes` 0 means "what the device has free".  On CMN_OVER_BUDGET
+ * `facts` (if non-null) is filled and nothing is allocated.  Building an
+ * enumerator for a composition that is not fully enumerable returns
+ * CMN_INVALID_CONFIGURATION. */
+cmn_status cmn_role_build(const cmn_problem* problem, int32_t role,
+                          const uint8_t* slot_kinds, int64_t slot_count,
+                          uint64_t n_regions, uint64_t budget_bytes,
+                          uint64_t sample_points, cmn_role** out,
+                          cmn_over_budget* facts);
+void cmn_role_destroy(cmn_role* role);
+uint64_t cmn_role_n_regions(const cmn_role* role);
+/* n_samples() / n_points() of the reference roles. */
+uint64_t cmn_role_n_elements(const cmn_role* role);
+
+/* RegionBounder::bound (backend/backend.hpp:99; graph/replay.cuh:823-828).
+ * `feasible`/`obj_lb` receive pointers to n_regions entries each. */
+cmn_status cmn_bound(cmn_role* role, const double* box,
+                     const uint64_t* var_ids, const uint64_t* widths,
+                     const uint8_t** feasible, const double** obj_lb,
+                     uint64_t* n_regions);
+
+/* RegionSampler::sample (backend/backend.hpp:87-88; graph/replay.cuh:830-836). */
+cmn_status cmn_sample(cmn_role* role, const double* box,
+                      const uint64_t* var_ids, const uint64_t* widths,
+                      uint64_t salt, cmn_candidate* out);
+
+/* RegionEnumerator::enumerate (backend/backend.hpp:114; replay.cuh:838-843). */
+cmn_status cmn_enumerate(cmn_role* role, const double* box,
+                         const uint64_t* var_ids, const uint64_t* widths,
+                         cmn_candidate* out);
+
+/* ---------------------------------------------------------------------
+ * Raw batched evaluation: the fused evaluator (a) over a frontier of boxes
+ * stored SoA as lo/hi planes (plane v holds variable v of every box).
+ * Replaces the per-node kernel chain of graph/kernels.cuh:177-419 for a
+ * batch of already-materialised boxes.
+ * ------------------------------------------------------------------- */
+typedef enum cmn_precision {
+  CMN_PRECISION_FP64 = 0,            /* plain FP64 directed rounding */
+  CMN_PRECISION_FP32_SCREEN = 1      /* FP32 outward screen, FP64 certify */
+} cmn_precision;
+
+/* `lo`/`hi` point at n_vars planes of `stride` doubles; outputs have
+ * n_boxes entries.  `device_pointers` 1 means every array is device memory
+ * and the call is asynchronous on `stream` (a cudaStream_t, or NULL for the
+ * legacy default stream); 0 means host memory and the call blocks.
+ * precision FP32_SCREEN evaluates in FP32 with outward-rounded inputs and
+ * writes the (sound, wider) FP32 enclosure widened to double. */
+cmn_status cmn_eval_boxes(const cmn_problem* problem, int32_t precision,
+                          const double* lo, const double* hi,
+                          uint64_t n_boxes, uint64_t stride,
+                          double* obj_lb, double* obj_ub, uint8_t* feasible,
+                          int32_t device_pointers, void* stream);
+
+/* ---------------------------------------------------------------------
+ * Device-resident batched branch-and-bound: the solver API
+ * (search/driver.hpp:36-54 SolveOutcome, :97-134 SearchDriver constructor,
+ * :137-537 solve()).  The frontier (box pool) lives in HBM; one iteration
+ * selects the best parents, branches them (BisectionBudget policy,
+ * policy/bisection_budget.hpp:81-262), bounds and samples every child,
+ * prunes and compacts -- all as one captured CUDA graph.
+ * ------------------------------------------------------------------- */
+
+/* search::StopReason (search/budget.hpp:21-29), plus FrontierCap. */
+typedef enum cmn_stop_reason {
+  CMN_STOP_CONVERGED = 0,
+  CMN_STOP_EXHAUSTED = 1,
+  CMN_STOP_ITERATION_LIMIT = 2,
+  CMN_STOP_HOST_MEMORY = 3,
+  CMN_STOP_ALLOCATION_FAILURE = 4,
+  CMN_STOP_DEVICE_MEMORY = 5,
+  CMN_STOP_RUNNING = 6
+} cmn_stop_reason;
+
+typedef struct cmn_solve_options {
+  uint64_t iter_limit;        /* max boxes expanded (SearchDriver iter_limit) */
+  uint64_t batch_iter_limit;  /* max batched iterations, 0 = unlimited */
+  double tolerance;           /* gap_closed tolerance, default 1e-6 */
+  int32_t precision;          /* cmn_precision */
+  int32_t bisection_budget;   /* B: each expanded box gets 2^B children */
+  uint64_t frontier_cap;      /* pool capacity in boxes */
+  uint64_t batch_parents;     /* max boxes expanded per iteration */
+  uint64_t sample_points;     /* samples per child */
+  int32_t sample_all;         /* 1: sample every child (reference order) */
+  int32_t relative_width;     /* RelativeBisectionBudget heap key */
+  uint64_t max_cycle_size;    /* slot cap (SearchCalibration) 0 = 64 */
+  uint64_t enumerate_cap;     /* SearchCalibration::enumerate_cap */
+  int32_t has_known_primal;   /* seeds GUB (known_primal_bound) */
+  int32_t reserved;
+  double known_primal_bound;
+  uint64_t time_limit_ms;     /* 0 = none */
+} cmn_solve_options;
+
+/* report::RunTelemetry (report/telemetry.hpp:23-87) plus the batched and
+ * precision counters. */
+typedef struct cmn_counters {
+  uint64_t iterations;         /* batched iterations */
+  uint64_t expansions;         /* boxes expanded (reference iterations) */
+  uint64_t fathomed;
+  uint64_t fathomed_points;
+  uint64_t bounded;            /* child boxes evaluated */
+  uint64_t sampled;
+  uint64_t enqueued;
+  uint64_t witness_rejected;
+  uint64_t pruned_duplicate;
+  uint64_t pruned_infeasible;
+  uint64_t pruned_dominated;
+  uint64_t dropped_viable;
+  uint64_t dropped_dominated;
+  uint64_t screened_fp32;      /* children evaluated by the FP32 screen */
+  uint64_t certified_fp64;     /* children evaluated in FP64 */
+  uint64_t peak_frontier;
+} cmn_counters;
+
+typedef struct cmn_outcome {
+  double lower_bound;
+  double upper_bound;
+  int32_t stop_reason;
+  int32_t proven_optimal;
+  int32_t infeasible;
+  int32_t found_incumbent;
+  uint64_t frontier_size;
+  uint64_t viable;
+  double dropped_lb_min;
+  double elapsed_ms;
+  cmn_counters counters;
+} cmn_outcome;
+
+/* Fills `opts` with the defaults (SearchDriver defaults where they exist:
+ * driver.hpp:97-109). */
+void cmn_solve_options_default(cmn_solve_options* opts);
+
+typedef struct cmn_solver cmn_solver; /* opaque */
+
+cmn_status cmn_solver_create(const cmn_problem* problem,
+                             const cmn_solve_options* opts,
+                             cmn_solver** out);
+void cmn_solver_destroy(cmn_solver* solver);
+/* Runs up to `max_iterations` batched iterations (0 = until a stop
+ * condition).  Returns CMN_OK while running or stopped normally. */
+cmn_status cmn_solver_step(cmn_solver* solver, uint64_t max_iterations);
+/* Live queries: bounds, incumbent and gap (GUB - GLB). */
+cmn_status cmn_query_bounds(const cmn_solver* solver, double* lower_bound,
+                            double* upper_bound);
+/* Copies the incumbent into `point` (n_vars doubles); returns 0 in
+ * `found` when there is none. */
+cmn_status cmn_query_incumbent(const cmn_solver* solver, double* point,
+                               int32_t* found);
+cmn_status cmn_query_gap(const cmn_solver* solver, double* gap);
+/* Final (or current) outcome after finalise_bounds
+ * (search/epilogue.hpp:89-127). */
+cmn_status cmn_solver_outcome(cmn_solver* solver, cmn_outcome* out);
+/* The CUDA stream the solver's iteration runs on (a cudaStream_t). */
+void* cmn_solver_stream(cmn_solver* solver);
+/* Copies the current frontier (pool order) to the host: up to `room`
+ * boxes as interleaved (lb, ub) pairs, their lower bounds and depths.
+ * `count` receives the frontier size.  The reference keeps this state in
+ * IntervalPQueue + IntervalHistory (search/frontier.hpp:152-338,
+ * search/history.hpp:20-137); any pointer may be NULL. */
+cmn_status cmn_solver_frontier(cmn_solver* solver, double* boxes,
+                               double* lower_bounds, uint32_t* depths,
+                               uint64_t room, uint64_t* count);
+
+/* Phase timings of the most recent iteration, from CUDA events recorded
+ * inside the captured iteration: [0] select+branch, [1] bound (FP64
+ * evaluation, or FP32 screen + FP64 certify), [2] sample + incumbent,
+ * [3] prune + pool rebuild, [4] whole iteration; milliseconds. */
+cmn_status cmn_solver_phase_ms(cmn_solver* solver, double* ms5);
+/* Kernel nodes one captured iteration launches. */
+uint64_t cmn_solver_kernels_per_iteration(const cmn_solver* solver);
+
+/* Measures the device's FP64 (precision 0) or FP32 (precision 1) FMA
+ * throughput with a dependent-chain-free FMA loop on every SM; writes
+ * TFLOP/s (2 flops per FMA).  A roofline denominator, not part of the
+ * search path. */
+cmn_status cmn_measure_fma_peak(int32_t precision, double* tflops);
+
+/* One-call solve: create, run to a stop condition, report, destroy. */
+cmn_status cmn_solve(const cmn_problem* problem,
+                     const cmn_solve_options* opts, cmn_outcome* outcome,
+                     double* best_point);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CUMINLP_GB300_H */

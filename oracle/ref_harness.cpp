@@ -1,0 +1,336 @@
+// ref_harness.cpp -- runs the reference's own host code on given inputs.
+//
+// TEST INFRASTRUCTURE ONLY.  Compiled (by oracle/build_ref.sh) straight
+// from the reference sources where they lie, with the one-struct
+// cuinterval shim in oracle/ref_shim; the binary lands in oracle/_ref/ and
+// is used only to generate golden fixtures under tests/golden/.
+//
+// Region evaluation comes from the CPU oracle (liboracle), plugged in
+// behind the reference's RegionBackendFactory interface
+// (backend/backend.hpp:193-219), so the driver, policies, frontier heap,
+// history and epilogue that run here are the reference's code.
+//
+// Commands (all numbers read and written as C99 hex floats / integers):
+//   decode  <in> <out>   lines "kind plo phi part fan" -> "lo hi"
+//   policy  <in> <out>   BisectionBudget / GreedyEnum choose() cases
+//   driver  <in> <out>   SearchDriver::solve on a problem file
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <iostream>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "cuminlp/backend/backend.hpp"
+#include "cuminlp/model/problem.hpp"
+#include "cuminlp/policy/bisection_budget.hpp"
+#include "cuminlp/policy/greedy_enum.hpp"
+#include "cuminlp/region/decode.hpp"
+#include "cuminlp/search/driver.hpp"
+
+extern "C" {
+#include "oracle.h"
+}
+
+using namespace cuminlp;
+
+static double rd(std::istream& in)
+{
+  std::string s;
+  in >> s;
+  return std::strtod(s.c_str(), nullptr);
+}
+
+static std::string hx(double x)
+{
+  char buf[64];
+  std::snprintf(buf, sizeof buf, "%a", x);
+  return buf;
+}
+
+// ---- problem file: the flattened DAG, rebuilt with ExprDAG::emit ------
+struct Loaded {
+  model::Problem<double> problem;
+  std::vector<cmn_node> nodes;
+  std::vector<double> lb, ub;
+  std::vector<int32_t> kinds;
+  std::vector<cmn_constraint> cons;
+  orc_problem* orc = nullptr;
+};
+
+static void load_problem(std::istream& in, Loaded& L)
+{
+  size_t n_nodes;
+  in >> n_nodes;
+  for (size_t i = 0; i < n_nodes; ++i) {
+    cmn_node nd{};
+    in >> nd.op >> nd.n_in >> nd.in0 >> nd.in1 >> nd.var_index;
+    nd.constant = rd(in);
+    in >> nd.int_exp;
+    L.nodes.push_back(nd);
+    model::DAGNodePayload<double> p{};
+    if (nd.op == CMN_OP_CONST) p.constant = nd.constant;
+    if (nd.op == CMN_OP_VAR) p.var_index = (size_t)nd.var_index;
+    if (nd.op == CMN_OP_POWN) p.int_exp = nd.int_exp;
+    auto op = static_cast<model::Op>(nd.op);
+    if (nd.n_in == 0) L.problem.graph.emit(op, {}, p);
+    else if (nd.n_in == 1) L.problem.graph.emit(op, {(size_t)nd.in0}, p);
+    else L.problem.graph.emit(op, {(size_t)nd.in0, (size_t)nd.in1}, p);
+  }
+  size_t n_vars;
+  in >> n_vars;
+  for (size_t v = 0; v < n_vars; ++v) {
+    double lo = rd(in), hi = rd(in);
+    int k;
+    in >> k;
+    L.lb.push_back(lo);
+    L.ub.push_back(hi);
+    L.kinds.push_back(k);
+    L.problem.box_bounds.push_back({lo, hi});
+    L.problem.var_kinds.push_back(static_cast<model::VarKind>(k));
+  }
+  in >> L.problem.objective_root;
+  size_t m;
+  in >> m;
+  for (size_t c = 0; c < m; ++c) {
+    cmn_constraint cc{};
+    in >> cc.root >> cc.cmp;
+    cc.rhs = rd(in);
+    L.cons.push_back(cc);
+    L.problem.constraints.push_back({(size_t)cc.root, static_cast<model::Cmp>(cc.cmp), cc.rhs});
+  }
+  L.problem.validate();
+  cmn_problem_desc d{};
+  d.nodes = L.nodes.data();
+  d.n_nodes = (int64_t)L.nodes.size();
+  d.var_lb = L.lb.data();
+  d.var_ub = L.ub.data();
+  d.var_kinds = L.kinds.data();
+  d.n_vars = (int64_t)L.lb.size();
+  d.objective_root = (int64_t)L.problem.objective_root;
+  d.constraints = L.cons.data();
+  d.n_constraints = (int64_t)L.cons.size();
+  L.orc = orc_problem_create(&d);
+  if (!L.orc) throw std::runtime_error(orc_last_error());
+}
+
+// ---- the oracle behind the reference's role interface -------------------
+struct OracleRoles {
+  const orc_problem* p;
+  std::vector<uint8_t> kinds;
+  std::size_t n_regions;
+  std::size_t samples;
+  std::vector<uint8_t> feas;
+  std::vector<double> lb;
+  std::vector<double> point;
+
+  void args(const backend::Region<double>& r, std::vector<uint64_t>& vids, std::vector<uint64_t>& widths)
+  {
+    vids.assign(r.assignment.var_ids.begin(), r.assignment.var_ids.end());
+    widths.assign(r.assignment.widths.begin(), r.assignment.widths.end());
+  }
+};
+
+class OBounder : public backend::RegionBounder<double> {
+ public:
+  explicit OBounder(OracleRoles r) : r_(std::move(r)) {}
+  backend::BoundResult<double> bound(const backend::Region<double>& region) override
+  {
+    std::vector<uint64_t> v, w;
+    r_.args(region, v, w);
+    r_.feas.resize(r_.n_regions);
+    r_.lb.resize(r_.n_regions);
+    if (orc_bound(r_.p, reinterpret_cast<const double*>(region.box.data()), r_.kinds.data(), v.data(), w.data(),
+                  (int64_t)r_.kinds.size(), r_.n_regions, r_.feas.data(), r_.lb.data(), 1))
+      throw std::runtime_error(orc_last_error());
+    return {r_.feas, r_.lb, r_.n_regions};
+  }
+  std::size_t n_regions() const override { return r_.n_regions; }
+
+ private:
+  OracleRoles r_;
+};
+
+class OSampler : public backend::RegionSampler<double> {
+ public:
+  explicit OSampler(OracleRoles r) : r_(std::move(r)) {}
+  backend::CandidateResult<double> sample(const backend::Region<double>& region, std::uint64_t salt) override
+  {
+    std::vector<uint64_t> v, w;
+    r_.args(region, v, w);
+    r_.point.resize(region.box.size());
+    int32_t found;
+    double value;
+    int64_t index;
+    if (orc_sample(r_.p, reinterpret_cast<const double*>(region.box.data()), r_.kinds.data(), v.data(), w.data(),
+                   (int64_t)r_.kinds.size(), r_.n_regions, r_.samples, salt, &found, &value, &index, r_.point.data(),
+                   1))
+      throw std::runtime_error(orc_last_error());
+    return {found != 0, value, r_.point, index};
+  }
+  std::size_t n_samples() const override { return r_.n_regions * r_.samples; }
+
+ private:
+  OracleRoles r_;
+};
+
+class OEnumerator : public backend::RegionEnumerator<double> {
+ public:
+  explicit OEnumerator(OracleRoles r) : r_(std::move(r)) {}
+  backend::CandidateResult<double> enumerate(const backend::Region<double>& region) override
+  {
+    std::vector<uint64_t> v, w;
+    r_.args(region, v, w);
+    r_.point.resize(region.box.size());
+    int32_t found;
+    double value;
+    int64_t index;
+    if (orc_enumerate(r_.p, reinterpret_cast<const double*>(region.box.data()), r_.kinds.data(), v.data(), w.data(),
+                      (int64_t)r_.kinds.size(), r_.n_regions, &found, &value, &index, r_.point.data(), 1))
+      throw std::runtime_error(orc_last_error());
+    return {found != 0, value, r_.point, index};
+  }
+  std::size_t n_points() const override { return r_.n_regions; }
+
+ private:
+  OracleRoles r_;
+};
+
+class OracleFactory : public backend::RegionBackendFactory<double> {
+ public:
+  explicit OracleFactory(const orc_problem* p) : p_(p) {}
+  backend::BackendCapabilities capabilities() const override { return {}; }
+  backend::RegionCostModel cost_model(const model::Problem<double>&) const override
+  {
+    backend::RegionCostModel c;
+    c.bound_bytes_per_region = 9;
+    c.fixed_bytes = 1;
+    return c;
+  }
+  backend::SubdivisionBundle<double> build_subdivision(const model::Problem<double>&,
+                                                       const region::Composition& composition, std::size_t n_regions,
+                                                       const backend::BuildBudget& budget,
+                                                       backend::RoleRequest roles) const override
+  {
+    OracleRoles r{p_, {}, n_regions, budget.samples_per_region, {}, {}, {}};
+    for (auto k : composition) r.kinds.push_back(static_cast<uint8_t>(k));
+    backend::SubdivisionBundle<double> b;
+    if (roles.sampler) b.sampler = std::make_unique<OSampler>(r);
+    if (roles.bounder) b.bounder = std::make_unique<OBounder>(r);
+    if (roles.enumerator && region::is_fully_enumerable(composition)) b.enumerator = std::make_unique<OEnumerator>(r);
+    return b;
+  }
+
+ private:
+  const orc_problem* p_;
+};
+
+// ---- commands ----------------------------------------------------------
+static int cmd_decode(std::istream& in, std::ostream& out)
+{
+  int kind;
+  while (in >> kind) {
+    double plo = rd(in), phi = rd(in);
+    size_t part, fan;
+    in >> part >> fan;
+    cu::interval<double> parent{plo, phi}, child{};
+    region::decode::slot_bounds<double>(static_cast<region::SlotKind>(kind), parent, part, fan, child);
+    out << hx(child.lb) << ' ' << hx(child.ub) << '\n';
+  }
+  return 0;
+}
+
+// per case: "B <B> <max_cycle> <enum_cap> <relative> <n>" or
+// "G <partition_num> <enumerate_cap> <max_cycle> <n>", then n kinds, then
+// n (lb ub) pairs.  Output: "<count> (kind vid width dom)*"
+static int cmd_policy(std::istream& in, std::ostream& out)
+{
+  std::string tag;
+  while (in >> tag) {
+    size_t B = 0, max_cycle = 0, enum_cap = 0, rel = 0, pn = 0, ecap = 0, n = 0;
+    if (tag == "B") in >> B >> max_cycle >> enum_cap >> rel >> n;
+    else in >> pn >> ecap >> max_cycle >> n;
+    std::vector<model::VarKind> kinds(n);
+    for (auto& k : kinds) {
+      int x;
+      in >> x;
+      k = static_cast<model::VarKind>(x);
+    }
+    std::vector<cu::interval<double>> box(n);
+    for (auto& b : box) {
+      b.lb = rd(in);
+      b.ub = rd(in);
+    }
+    config::SearchCalibration cal{};
+    cal.max_cycle_size = max_cycle;
+    cal.enumerate_cap = enum_cap;
+    region::SlotAssignment a;
+    if (tag == "B") {
+      policy::BisectionBudgetCompositionPolicy<double> pol(B, cal, rel != 0);
+      a = pol.choose(box, kinds);
+    } else {
+      policy::GreedyEnumCompositionPolicy<double> pol(region::FanOutSpec(pn, ecap), cal);
+      a = pol.choose(box, kinds);
+    }
+    out << a.size();
+    for (size_t j = 0; j < a.size(); ++j) {
+      size_t dom = a.domain_sizes.empty() ? a.widths[j] : a.domain_sizes[j];
+      out << ' ' << (int)a.composition[j] << ' ' << a.var_ids[j] << ' ' << a.widths[j] << ' ' << dom;
+    }
+    out << '\n';
+  }
+  return 0;
+}
+
+// "<iter_limit> <B> <samples> <tolerance>" then the problem
+static int cmd_driver(std::istream& in, std::ostream& out)
+{
+  uint32_t iter_limit;
+  size_t B, samples;
+  in >> iter_limit >> B >> samples;
+  double tol = rd(in);
+  Loaded L;
+  load_problem(in, L);
+  auto pol = std::make_shared<policy::BisectionBudgetCompositionPolicy<double>>(B);
+  auto fac = std::make_shared<OracleFactory>(L.orc);
+  search::SearchDriver<double> drv(pol, fac, iter_limit, tol, samples);
+  std::streambuf* prev = std::cout.rdbuf();
+  std::ostringstream sink;
+  std::cout.rdbuf(sink.rdbuf());
+  auto o = drv.solve(L.problem);
+  std::cout.rdbuf(prev);
+  const auto& t = o.counters;
+  out << hx(o.lower_bound) << ' ' << hx(o.upper_bound) << ' ' << search::to_string(o.stop_reason) << ' '
+      << o.proven_optimal << ' ' << o.infeasible << '\n';
+  out << t.iterations << ' ' << t.fathomed << ' ' << t.fathomed_points << ' ' << t.bounded << ' ' << t.sampled << ' '
+      << t.enqueued << ' ' << t.witness_rejected << ' ' << t.pruned_duplicate << ' ' << t.pruned_infeasible << ' '
+      << t.pruned_dominated << ' ' << t.pending << ' ' << t.viable << '\n';
+  out << o.best_point.size();
+  for (double x : o.best_point) out << ' ' << hx(x);
+  out << '\n';
+  orc_problem_destroy(L.orc);
+  return 0;
+}
+
+int main(int argc, char** argv)
+{
+  if (argc < 4) {
+    std::cerr << "usage: ref_harness decode|policy|driver <in> <out>\n";
+    return 2;
+  }
+  std::ifstream in(argv[2]);
+  std::ofstream out(argv[3]);
+  std::string cmd = argv[1];
+  try {
+    if (cmd == "decode") return cmd_decode(in, out);
+    if (cmd == "policy") return cmd_policy(in, out);
+    if (cmd == "driver") return cmd_driver(in, out);
+  } catch (const std::exception& e) {
+    std::cerr << "error: " << e.what() << '\n';
+    return 1;
+  }
+  std::cerr << "unknown command\n";
+  return 2;
+}

@@ -1,0 +1,110 @@
+"""The device-resident batched solver against its CPU restatement in the
+oracle: identical frontiers (boxes, bounds, depths) after fixed numbers of
+iterations, identical incumbents, bounds and counters; and the FP32 screen
+with FP64 certification reproducing the plain FP64 search exactly."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle as O
+from cuminlp_gb300 import generators as G
+from cuminlp_gb300.solver import DeviceProblem, Solver
+from tests.conftest import bits_equal
+from tests.test_oracle_pins import contract_model, fixture_problems
+
+pytestmark = pytest.mark.gpu
+
+COUNTERS = ["iterations", "expansions", "fathomed", "fathomed_points", "bounded", "sampled", "enqueued",
+            "witness_rejected", "pruned_duplicate", "pruned_infeasible", "pruned_dominated", "dropped_viable",
+            "dropped_dominated", "screened_fp32", "certified_fp64", "peak_frontier"]
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    from cuminlp_gb300 import build
+    build.build_library()
+
+
+def problems():
+    fx = fixture_problems()
+    return {
+        "square_le5": fx["square_le5"], "infeasible": fx["infeasible"], "aggregate": fx["aggregate_fixture"],
+        "contract": contract_model(), "int_eq": fx["int_eq"], "miqcqp_n6": fx["miqcqp_n6"],
+        "cfg1": G.config1(), "cfg1b": G.config1(1),
+    }
+
+
+def compare(p, iterations, **opts):
+    dp = DeviceProblem(p)
+    s = Solver(dp, batch_iter_limit=iterations, **opts)
+    s.step(0)
+    g = s.outcome()
+    gbox, glb, gdepth = s.frontier()
+    obox, olb, odepth, o = O.OracleProblem(p).batched_frontier(iterations, room=1 << 20, **opts)
+    assert len(glb) == len(olb)
+    assert bits_equal(glb, olb)
+    assert np.array_equal(gdepth, odepth)
+    assert bits_equal(gbox, obox)
+    for k in ("lower_bound", "upper_bound", "stop_reason", "proven_optimal", "infeasible", "frontier_size",
+              "viable"):
+        if isinstance(g[k], float):
+            assert bits_equal(np.float64(g[k]), np.float64(o[k])), k
+        else:
+            assert g[k] == o[k], k
+    for k in COUNTERS:
+        assert g["counters"][k] == o["counters"][k], k
+    if o["upper_bound"] < np.finfo(np.float64).max:
+        assert bits_equal(g["best_point"], o["best_point"])
+    s.close()
+    return g
+
+
+@pytest.mark.parametrize("name", ["square_le5", "infeasible", "aggregate", "contract", "int_eq", "miqcqp_n6",
+                                  "cfg1"])
+def test_solver_matches_oracle(name):
+    p = problems()[name]
+    compare(p, 12, bisection_budget=2, batch_parents=64, sample_points=2)
+    compare(p, 5, bisection_budget=3, batch_parents=1, sample_points=1, sample_all=1)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_solver_matches_oracle_larger(precision):
+    compare(G.config1(), 30, bisection_budget=3, batch_parents=512, precision=precision)
+    compare(G.config1(2), 20, bisection_budget=4, batch_parents=256, precision=precision, relative_width=1)
+
+
+def test_eviction_matches_oracle():
+    g = compare(G.config1(1), 25, bisection_budget=3, batch_parents=128, frontier_cap=300)
+    assert g["counters"]["dropped_viable"] + g["counters"]["dropped_dominated"] > 0
+
+
+def test_fp32_screen_identical_certified_bounds():
+    p = G.config1()
+    dp = DeviceProblem(p)
+    out = {}
+    for prec in ("fp64", "fp32"):
+        s = Solver(dp, batch_iter_limit=60, bisection_budget=3, batch_parents=1024, precision=prec)
+        s.step(0)
+        out[prec] = (s.outcome(), s.frontier())
+        s.close()
+    a, fa = out["fp64"]
+    b, fb = out["fp32"]
+    assert a["lower_bound"] == b["lower_bound"] and a["upper_bound"] == b["upper_bound"]
+    assert np.array_equal(a["best_point"], b["best_point"])
+    assert bits_equal(fa[1], fb[1]) and bits_equal(fa[0], fb[0])
+    assert b["counters"]["certified_fp64"] < a["counters"]["certified_fp64"]
+
+
+def test_solver_converges_on_small_problem():
+    p = problems()["aggregate"]
+    dp = DeviceProblem(p)
+    s = Solver(dp, bisection_budget=2, batch_parents=256)
+    s.step(0)
+    g = s.outcome()
+    ref = O.OracleProblem(p).solve_reference(iter_limit=200000, bisection_budget=2, sample_points=1)
+    assert g["stop_reason"] == "converged" and g["proven_optimal"] == 1
+    tol = 1e-6 * max(1.0, abs(ref["upper_bound"]))
+    assert abs(g["upper_bound"] - ref["upper_bound"]) <= tol
+    assert abs(g["lower_bound"] - ref["lower_bound"]) <= tol

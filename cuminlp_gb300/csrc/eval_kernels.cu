@@ -347,15 +347,26 @@ size_t sample_smem_bytes(int n_vars, int n_slots, int threads)
 
 // Kernel attributes are set once per device, before any launch, so that
 // launches stay legal inside stream capture.
+// The dynamic allowance is the opt-in maximum less the kernel's own static
+// shared memory (the reduction scratch of the sampler).
+template <typename K>
+static cudaError_t allow_dynamic_smem(K kernel, int max_smem)
+{
+  cudaFuncAttributes fa;
+  cudaError_t e = cudaFuncGetAttributes(&fa, kernel);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              max_smem - (int)fa.sharedSizeBytes);
+}
+
 cudaError_t set_eval_kernel_attributes(int max_smem)
 {
-  const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
-  cudaError_t e = cudaFuncSetAttribute(eval_children_kernel<double, 0>, at, max_smem);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(eval_children_kernel<double, 1>, at, max_smem);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(eval_children_kernel<double, 3>, at, max_smem);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(eval_children_kernel<float, 0>, at, max_smem);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(eval_children_kernel<float, 2>, at, max_smem);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(sample_children_kernel, at, max_smem);
+  cudaError_t e = allow_dynamic_smem(eval_children_kernel<double, 0>, max_smem);
+  if (e == cudaSuccess) e = allow_dynamic_smem(eval_children_kernel<double, 1>, max_smem);
+  if (e == cudaSuccess) e = allow_dynamic_smem(eval_children_kernel<double, 3>, max_smem);
+  if (e == cudaSuccess) e = allow_dynamic_smem(eval_children_kernel<float, 0>, max_smem);
+  if (e == cudaSuccess) e = allow_dynamic_smem(eval_children_kernel<float, 2>, max_smem);
+  if (e == cudaSuccess) e = allow_dynamic_smem(sample_children_kernel, max_smem);
   return e;
 }
 

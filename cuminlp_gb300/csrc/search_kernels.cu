@@ -61,6 +61,7 @@ __global__ void init_kernel(const SolverCfg cfg, const SolverBufs b, const doubl
 __global__ void begin_kernel(const SolverCfg cfg, const SolverBufs b)
 {
   SolverDev* d = b.dev;
+  d->improved = 0;  // an iteration after the stop must not rewrite the witness
   if (d->done) return;
   const uint64_t L = d->pool_size;
   if (L == 0) {
@@ -329,6 +330,10 @@ struct GatherParents {
   __device__ void operator()(uint64_t i, uint64_t pos) const
   {
     const uint32_t p = b.dev->parity;
+    if (pos >= cfg.e_max) {  // more marks than parents: never written, flagged
+      b.dev->error = 1;
+      return;
+    }
     for (int v = 0; v < cfg.n_vars; ++v) {
       b.plo[(uint64_t)v * cfg.e_max + pos] = b.lo[p][(uint64_t)v * cfg.pstride + i];
       b.phi[(uint64_t)v * cfg.e_max + pos] = b.hi[p][(uint64_t)v * cfg.pstride + i];

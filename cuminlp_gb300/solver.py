@@ -119,16 +119,25 @@ class _Role:
             pass
 
 
+def _view(ptr, ctype, n: int, owner, dtype):
+    """numpy view of role-owned memory that keeps the role alive."""
+    buf = (ctype * n).from_address(C.cast(ptr, C.c_void_p).value)
+    buf.owner = owner
+    return np.frombuffer(buf, dtype=dtype)
+
+
 class Bounder(_Role):
     kind = A.ROLE_BOUNDER
 
     def bound(self, box, var_ids, widths):
+        """(feasible, obj_lb) per region: views of role-owned storage, valid
+        until the next call on this role (backend/backend.hpp:66-67)."""
         fp = C.POINTER(C.c_uint8)()
         lp = C.POINTER(C.c_double)()
         n = C.c_uint64()
         check(lib().cmn_bound(self.handle, *self._args(box, var_ids, widths), C.byref(fp), C.byref(lp), C.byref(n)))
         nr = n.value
-        return (np.ctypeslib.as_array(fp, shape=(nr,)), np.ctypeslib.as_array(lp, shape=(nr,)))
+        return _view(fp, C.c_uint8, nr, self, np.uint8), _view(lp, C.c_double, nr, self, np.float64)
 
 
 class Sampler(_Role):

@@ -97,14 +97,35 @@ def test_fp32_screen_identical_certified_bounds():
     assert b["counters"]["certified_fp64"] < a["counters"]["certified_fp64"]
 
 
-def test_solver_converges_on_small_problem():
-    p = problems()["aggregate"]
-    dp = DeviceProblem(p)
-    s = Solver(dp, bisection_budget=2, batch_parents=256)
-    s.step(0)
-    g = s.outcome()
-    ref = O.OracleProblem(p).solve_reference(iter_limit=200000, bisection_budget=2, sample_points=1)
-    assert g["stop_reason"] == "converged" and g["proven_optimal"] == 1
-    tol = 1e-6 * max(1.0, abs(ref["upper_bound"]))
-    assert abs(g["upper_bound"] - ref["upper_bound"]) <= tol
-    assert abs(g["lower_bound"] - ref["lower_bound"]) <= tol
+def test_one_parent_per_iteration_reproduces_reference_driver():
+    # with one parent per iteration and every child sampled, the device
+    # search expands boxes in the reference SearchDriver's order: its bounds
+    # after a fixed expansion budget equal the driver restatement's (which
+    # the golden fixtures pin to the reference's own code)
+    for name, iters in (("aggregate", 4000), ("miqcqp_n6", 1500), ("cfg1", 1500)):
+        p = problems()[name]
+        s = Solver(DeviceProblem(p), bisection_budget=2, batch_parents=1, sample_all=1, iter_limit=iters)
+        s.step(0)
+        g = s.outcome()
+        s.close()
+        ref = O.OracleProblem(p).solve_reference(iter_limit=iters, bisection_budget=2, sample_points=1, threads=1)
+        assert g["lower_bound"] == ref["lower_bound"] and g["upper_bound"] == ref["upper_bound"], name
+        assert g["frontier_size"] == ref["frontier_size"] and g["viable"] == ref["viable"], name
+
+
+def test_batched_solver_certifies_the_reference_optimum():
+    # config-1 instance 1: the reference driver proves optimality (golden
+    # fixture); the batched search must certify the same optimum within the
+    # solver's gap
+    p = G.config1(1)
+    ref = O.OracleProblem(p).solve_reference(iter_limit=20000, bisection_budget=3, sample_points=2, threads=1)
+    assert ref["proven_optimal"] == 1
+    for prec in ("fp64", "fp32"):
+        s = Solver(DeviceProblem(p), bisection_budget=3, batch_parents=256, sample_points=2, precision=prec)
+        s.step(0)
+        g = s.outcome()
+        s.close()
+        assert g["stop_reason"] == "converged" and g["proven_optimal"] == 1
+        tol = 1e-6 * max(1.0, abs(ref["upper_bound"]))
+        assert abs(g["upper_bound"] - ref["upper_bound"]) <= tol
+        assert abs(g["lower_bound"] - ref["lower_bound"]) <= tol

@@ -36,6 +36,7 @@ SIGNATURES = {
     "cmn_bound": (I32, [P, P, P, P, C.POINTER(C.POINTER(C.c_uint8)), C.POINTER(C.POINTER(D)), C.POINTER(U64)]),
     "cmn_sample": (I32, [P, P, P, P, U64, C.POINTER(A.Candidate)]),
     "cmn_enumerate": (I32, [P, P, P, P, C.POINTER(A.Candidate)]),
+    "cmn_sample_noalloc": (I32, [P, P, I64, U64, U64, P, P, P, U64, C.POINTER(A.Candidate), P, P]),
     "cmn_eval_boxes": (I32, [P, I32, P, P, U64, U64, P, P, P, I32, P]),
     "cmn_solve_options_default": (None, [C.POINTER(A.SolveOptions)]),
     "cmn_solver_create": (I32, [P, C.POINTER(A.SolveOptions), PP]),

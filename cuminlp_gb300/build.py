@@ -29,7 +29,7 @@ NVCC_FLAGS = [
     "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
     "--expt-relaxed-constexpr", "-DNDEBUG",
 ]
-SOURCES = ["program.cpp", "eval_kernels.cu", "search_kernels.cu", "capi.cu"]
+SOURCES = ["program.cpp", "eval_kernels.cu", "search_kernels.cu", "capi.cu", "noalloc.cu"]
 
 
 def _nvcc() -> str:

@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "../../include/cuminlp_gb300.h"
+#include "handles.hpp"
 #include "kernels.cuh"
 #include "launch.hpp"
 #include "program.hpp"
@@ -99,28 +100,22 @@ static cudaError_t ensure_attributes()
 // ----------------------------------------------------------------------
 // problem
 // ----------------------------------------------------------------------
-struct cmn_problem {
-  HostProblem host;
-  Program prog;
-  int device = 0;
-  Instr* d_prog64 = nullptr;
-  Instr* d_prog32 = nullptr;
-  int32_t* d_kinds = nullptr;
-  double* d_root_lb = nullptr;
-  double* d_root_ub = nullptr;
+cmn_problem::~cmn_problem()
+{
+  int cur = 0;
+  if (cudaGetDevice(&cur) == cudaSuccess && cur != device) cudaSetDevice(device);
+  dfree(d_prog64);
+  dfree(d_prog32);
+  dfree(d_kinds);
+  dfree(d_root_lb);
+  dfree(d_root_ub);
+  if (cur != device) cudaSetDevice(cur);
+}
 
-  ~cmn_problem()
-  {
-    int cur = 0;
-    if (cudaGetDevice(&cur) == cudaSuccess && cur != device) cudaSetDevice(device);
-    dfree(d_prog64);
-    dfree(d_prog32);
-    dfree(d_kinds);
-    dfree(d_root_lb);
-    dfree(d_root_ub);
-    if (cur != device) cudaSetDevice(cur);
-  }
-};
+namespace cmn {
+cmn_status set_error(cmn_status st, const std::string& msg) { return fail(st, msg); }
+cudaError_t ensure_kernel_attributes() { return ensure_attributes(); }
+}  // namespace cmn
 
 extern "C" const char* cmn_last_error(void) { return g_err.c_str(); }
 

@@ -1,0 +1,33 @@
+// handles.hpp -- definitions shared by the C ABI translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "../../include/cuminlp_gb300.h"
+#include "program.hpp"
+
+// A compiled problem resident on one device.
+struct cmn_problem {
+  cmn::HostProblem host;
+  cmn::Program prog;
+  int device = 0;
+  cmn::Instr* d_prog64 = nullptr;
+  cmn::Instr* d_prog32 = nullptr;
+  int32_t* d_kinds = nullptr;
+  double* d_root_lb = nullptr;
+  double* d_root_ub = nullptr;
+
+  ~cmn_problem();
+};
+
+namespace cmn {
+
+// Records `msg` as this thread's cmn_last_error() and returns `st`.
+cmn_status set_error(cmn_status st, const std::string& msg);
+
+// Sets the kernels' dynamic shared-memory allowance once per device.
+cudaError_t ensure_kernel_attributes();
+
+}  // namespace cmn

@@ -27,6 +27,8 @@ cudaError_t launch_witness(const Cand* cand, const double* plo, const double* ph
 
 // Largest dynamic shared memory a block may use on this device.
 int max_dynamic_smem();
+// Resident blocks per SM of the sampler at this shared-memory size.
+int sample_kernel_occupancy(size_t smem, int threads);
 int sm_count();
 
 }  // namespace cmn

@@ -232,6 +232,31 @@ cmn_status cmn_enumerate(cmn_role* role, const double* box,
                          const uint64_t* var_ids, const uint64_t* widths,
                          cmn_candidate* out);
 
+/* Allocation-free sampler.  No counterpart in the reference: it exists for
+ * callers that cannot call cudaMalloc -- processes whose device memory is
+ * owned by a pool they do not control (a serving framework's caching
+ * allocator, a fixed arena on a shared GPU) or code that must not grow its
+ * device footprint after start-up.  It does what a sampler role built by
+ * cmn_role_build(slot_kinds, n_regions, sample_points) then cmn_sample(box,
+ * var_ids, widths, salt) does, with the same results, but allocates no
+ * device memory: its scratch is one 512 KiB device array per GPU, held by
+ * the library until the process exits.  Host inputs and outputs; `point`
+ * receives n_vars doubles and out->point points at it.  Limits: at most
+ * 8192 variables (larger problems get CMN_INVALID_CONFIGURATION).  The
+ * first call on a device looks up the array's address on that device, so
+ * make it before any stream capture.  All calls share the array and it
+ * keeps the last call's contents; calls that overlap on the GPU (several
+ * streams or threads at once) race on it and must be serialised by the
+ * caller.  `stream` is a cudaStream_t or NULL; the call returns after the
+ * results are on the host. */
+cmn_status cmn_sample_noalloc(const cmn_problem* problem,
+                              const uint8_t* slot_kinds, int64_t slot_count,
+                              uint64_t n_regions, uint64_t sample_points,
+                              const double* box, const uint64_t* var_ids,
+                              const uint64_t* widths, uint64_t salt,
+                              cmn_candidate* out, double* point,
+                              void* stream);
+
 /* ---------------------------------------------------------------------
  * Raw batched evaluation: the fused evaluator (a) over a frontier of boxes
  * stored SoA as lo/hi planes (plane v holds variable v of every box).

@@ -51,6 +51,8 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-ttg", action="store_true", help="skip the time-to-gap runs")
+    ap.add_argument("--quick", action="store_true",
+                    help="solver steps only (no e2e, CPU baseline or time-to-gap): the profiling command")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     return ap.parse_args()
 
@@ -309,7 +311,7 @@ def e2e_run(dp, problem, steps, warmup):
 def time_to_gap(problem, precision, limit_s):
     from cuminlp_gb300.solver import DeviceProblem, Solver
     dp = DeviceProblem(problem)
-    s = Solver(dp, bisection_budget=3, batch_parents=1 << 15, frontier_cap=1 << 22, precision=precision,
+    s = Solver(dp, bisection_budget=3, batch_parents=1 << 15, frontier_cap=1 << 24, precision=precision,
                time_limit_ms=int(limit_s * 1000), iter_limit=1 << 62)
     t0 = time.perf_counter()
     s.step(0)
@@ -351,6 +353,9 @@ def run_ours(args):
     t_plain = reduce_max(dist, plain["ms"])
     plain_value = reduce_sum(dist, plain["delta"]["bounded"]) / (t_plain / 1e3)
 
+    if args.quick:
+        print(json.dumps({"quick": True, "fp64_ms": plain["ms"], "fp32_ms": screen["ms"], "boxes/s": value}))
+        return
     e2e = e2e_run(dp, problem, args.steps, args.warmup)
     e2e_all = reduce_sum(dist, e2e["value"])
 
@@ -411,7 +416,10 @@ def run_ours(args):
                              for i in range(5)],
         "screen_speedup_vs_plain_fp64": value / plain_value,
         "identical_certified_bounds": plain["outcome"] == screen["outcome"],
-        "screen_certified_fraction": screen["delta"]["certified_fp64"] / max(1, screen["delta"]["screened_fp32"]),
+        # the adaptive screen: share of boxes the FP32 pass saw, and share of
+        # boxes that needed FP64 certification
+        "screen_active_fraction": screen["delta"]["screened_fp32"] / max(1, screen["delta"]["bounded"]),
+        "screen_certified_fraction": screen["delta"]["certified_fp64"] / max(1, screen["delta"]["bounded"]),
         "roofline": {
             "bound": "fp64",
             "kernel": "eval_children_kernel<double> (fused interval DAG evaluator, plain FP64 form)",

@@ -96,6 +96,9 @@ __global__ void __launch_bounds__(kEvalThreads) eval_children_kernel(const EvalA
   if (kMode == 3) total = *a.list_count;
   else total = a.n_children_dev ? *a.n_children_dev : a.n_children;
   const double gub = a.gub ? *a.gub : DBL_MAX;
+  // screen switched off for this iteration: every child goes to the FP64
+  // certify pass unevaluated (duplicates and empty slots still classified)
+  const bool pass_through = kMode == 2 && a.use_screen != nullptr && *a.use_screen == 0;
 
   for (uint64_t idx = (uint64_t)blockIdx.x * B + threadIdx.x; idx < total; idx += (uint64_t)gridDim.x * B) {
     const uint64_t g = (kMode == 3) ? (uint64_t)a.list[idx] : idx;
@@ -107,6 +110,14 @@ __global__ void __launch_bounds__(kEvalThreads) eval_children_kernel(const EvalA
         if (kMode != 3) a.out_flag[g] = kChildNone;
         continue;
       }
+    }
+    if (pass_through) {
+      bool dup = false;
+      const uint32_t count = a.pinfo[k].count;
+      const SlotPlan* sp = a.slots + k * (uint64_t)a.max_slots;
+      for (uint32_t j = 0; j < count; ++j) dup = dup || ((r / sp[j].prefix) % sp[j].width >= sp[j].dom);
+      a.out_flag[g] = dup ? kChildDuplicate : kChildScreened;
+      continue;
     }
     const bool unique = load_child<T>(a, t, k, r);
     if (kMode != 0 && !unique) {

@@ -69,6 +69,7 @@ struct EvalArgs {
   const uint64_t* list_count;
   const double* gub;              // incumbent at the start of the iteration
   const uint32_t* done;           // solver: nonzero once the search stopped
+  const uint32_t* use_screen;     // FP32 screen: zero passes every child to the certify pass
   // outputs
   double* out_lb;
   double* out_ub;

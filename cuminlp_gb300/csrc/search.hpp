@@ -44,6 +44,10 @@ struct SolverDev {
   uint64_t certify_count;
   uint64_t evict;          // 1 when the rebuilt pool exceeds the cap
   uint64_t dropped_min_key;
+  uint64_t iter_valid;     // children bounded this iteration (not duplicates)
+  uint64_t iter_excluded;  // of those, excluded by the FP64 verdict
+  uint32_t use_screen;     // FP32 screen on for this iteration
+  uint32_t pad_;
   uint32_t parity;         // pool buffer holding the current pool
   uint32_t done;
   uint32_t converged;

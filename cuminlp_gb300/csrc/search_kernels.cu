@@ -52,6 +52,7 @@ __global__ void init_kernel(const SolverCfg cfg, const SolverBufs b, const doubl
     d->pool_size = 1;
     d->pool_min_key = lb_key(-DBL_MAX);
     d->parity = 0;
+    d->use_screen = 1;
     d->counters.peak_frontier = 1;
   }
 }
@@ -88,6 +89,8 @@ __global__ void begin_kernel(const SolverCfg cfg, const SolverBufs b)
   d->salt_base = d->expansions;
   d->expansions += E;
   d->certify_count = 0;
+  d->iter_valid = 0;
+  d->iter_excluded = 0;
   d->remaining = 0;
   d->kept = 0;
   d->new_size = 0;
@@ -689,21 +692,37 @@ __global__ void eval_count_kernel(const SolverCfg cfg, const SolverBufs b)
   SolverDev* d = b.dev;
   if (d->done) return;
   const uint64_t n = d->n_children;
-  unsigned long long screened = 0, certified = 0;
+  const bool fp32 = cfg.precision == CMN_PRECISION_FP32_SCREEN;
+  unsigned long long valid = 0, excluded = 0;
   for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n; g += (uint64_t)gridDim.x * blockDim.x) {
     const uint8_t s = b.cstate[g];
     if (s == kChildNone || s == kChildDuplicate) continue;
-    if (cfg.precision == CMN_PRECISION_FP32_SCREEN) ++screened;
-    else ++certified;
+    ++valid;
+    if (s == kChildInfeasible || s == kChildDominated) ++excluded;
   }
   for (int off = 16; off > 0; off >>= 1) {
-    screened += __shfl_down_sync(0xffffffffu, screened, off);
-    certified += __shfl_down_sync(0xffffffffu, certified, off);
+    valid += __shfl_down_sync(0xffffffffu, valid, off);
+    excluded += __shfl_down_sync(0xffffffffu, excluded, off);
   }
   if ((threadIdx.x & 31) == 0) {
-    if (screened) atomicAdd((unsigned long long*)&d->counters.screened_fp32, screened);
-    if (certified) atomicAdd((unsigned long long*)&d->counters.certified_fp64, certified);
+    if (valid) atomicAdd((unsigned long long*)&d->iter_valid, valid);
+    if (excluded) atomicAdd((unsigned long long*)&d->iter_excluded, excluded);
+    if (valid && fp32 && d->use_screen)
+      atomicAdd((unsigned long long*)&d->counters.screened_fp32, valid);
+    if (valid && !fp32) atomicAdd((unsigned long long*)&d->counters.certified_fp64, valid);
   }
+}
+
+// The screen stays on while it excludes at least a quarter of the children
+// it sees, and comes back on once the FP64 verdicts would have excluded a
+// quarter: it never changes a decision, only whether the work is done.
+__global__ void screen_policy_kernel(const SolverCfg cfg, const SolverBufs b)
+{
+  SolverDev* d = b.dev;
+  if (d->done || cfg.precision != CMN_PRECISION_FP32_SCREEN) return;
+  const uint64_t v = d->iter_valid;
+  const uint64_t x = d->use_screen ? v - d->certify_count : d->iter_excluded;
+  if (v > 0) d->use_screen = (x * 4 >= v) ? 1 : 0;
 }
 
 __global__ void certify_count_kernel(const SolverBufs b)
@@ -886,6 +905,7 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
   cudaError_t e;
   if (cfg.precision == CMN_PRECISION_FP32_SCREEN) {
     ea.prog = b.prog32;
+    ea.use_screen = &b.dev->use_screen;
     e = launch_eval(ea, 2, true, eval_grid, kEvalThreads, s);
     if (e != cudaSuccess) return e;
     ScreenedChild sc{b};
@@ -905,7 +925,10 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
   {
     const int grid = (int)std::min<uint64_t>((max_children + 255) / 256, 4096);
     eval_count_kernel<<<grid, 256, 0, s>>>(cfg, b);
-    if (cfg.precision == CMN_PRECISION_FP32_SCREEN) certify_count_kernel<<<1, 1, 0, s>>>(b);
+    if (cfg.precision == CMN_PRECISION_FP32_SCREEN) {
+      certify_count_kernel<<<1, 1, 0, s>>>(b);
+      screen_policy_kernel<<<1, 1, 0, s>>>(cfg, b);
+    }
   }
   mark(marks, 2, s);
 

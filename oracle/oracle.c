@@ -1932,6 +1932,7 @@ typedef struct {
   uint64_t E;
   double gub_old;
   uint64_t salt0;
+  int use_screen; /* FP32 screen switched on for this iteration */
   /* outputs per child slot (E*C) */
   double* lb;
   uint8_t* state; /* 0 invalid, 1 dup, 2 infeasible, 3 dominated(old), 4 eligible */
@@ -1989,7 +1990,7 @@ static void batch_range(void* vc, int64_t g0, int64_t g1, int tid)
     } else {
       double lb, ub;
       int f, screened_out = 0;
-      if (c->o->precision == CMN_PRECISION_FP32_SCREEN) {
+      if (c->o->precision == CMN_PRECISION_FP32_SCREEN && c->use_screen) {
         if (eval_all_f(p, cb, v32)) c->failed = 1;
         f = verdict_f(p, v32, &lb, &ub);
         if (!f) {
@@ -2038,6 +2039,7 @@ typedef struct {
   drop_acc dropped;
   uint64_t expansions, iterations;
   int converged, stopped_early, stop;
+  int use_screen; /* FP32 screen on for the next iteration */
 } bstate;
 
 /* Runs the batched search for at most `max_iter` iterations (0 = no cap
@@ -2131,6 +2133,7 @@ static int batched_run(const orc_problem* p, const cmn_solve_options* o,
     c.E = E;
     c.gub_old = st->GUB;
     c.salt0 = salt0;
+    c.use_screen = st->use_screen;
     c.lb = (double*)malloc(sizeof(double) * G);
     c.state = (uint8_t*)malloc(G);
     c.screened = (uint8_t*)malloc(G);
@@ -2144,6 +2147,7 @@ static int batched_run(const orc_problem* p, const cmn_solve_options* o,
 
     /* incumbent: argmin over (value, parent, element) of admissible
      * feasible candidates */
+    uint64_t iter_valid = 0, iter_excluded = 0, iter_certified = 0;
     double best = INFINITY;
     uint64_t best_k = 0;
     int64_t best_e = -1;
@@ -2160,11 +2164,17 @@ static int batched_run(const orc_problem* p, const cmn_solve_options* o,
         if (r >= pl->nreg) continue;
         if (!pl->fathom) {
           if (c.state[g] != 1) { /* duplicates are never evaluated */
-            if (o->precision == CMN_PRECISION_FP32_SCREEN) {
+            ++iter_valid;
+            if (c.state[g] == 2 || c.state[g] == 3) ++iter_excluded;
+            if (o->precision == CMN_PRECISION_FP32_SCREEN && st->use_screen) {
               ++ct->screened_fp32;
-              if (!c.screened[g]) ++ct->certified_fp64;
+              if (!c.screened[g]) {
+                ++ct->certified_fp64;
+                ++iter_certified;
+              }
             } else {
               ++ct->certified_fp64;
+              ++iter_certified;
             }
           }
           if (o->sample_all || c.state[g] == 4) ct->sampled += S;
@@ -2198,6 +2208,12 @@ static int batched_run(const orc_problem* p, const cmn_solve_options* o,
       st->GUB = best;
       memcpy(best_point, x, sizeof(double) * (size_t)n);
       st->have_best = 1;
+    }
+    /* the screen stays on while it excludes >= 1/4 of the children it sees
+     * and comes back once the FP64 verdicts would have excluded 1/4 */
+    if (o->precision == CMN_PRECISION_FP32_SCREEN && iter_valid > 0) {
+      uint64_t x = st->use_screen ? iter_valid - iter_certified : iter_excluded;
+      st->use_screen = x * 4 >= iter_valid;
     }
     double gub = st->GUB;
 
@@ -2298,6 +2314,7 @@ static void batched_init(const orc_problem* p, const cmn_solve_options* o,
   st->GLB = -DBL_MAX;
   st->dropped.lb_min = INFINITY;
   st->stop = CMN_STOP_ITERATION_LIMIT;
+  st->use_screen = 1;
 }
 
 static void batched_finish(const orc_problem* p, const cmn_solve_options* o,

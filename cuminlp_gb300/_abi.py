@@ -85,6 +85,11 @@ class SolveOptions(C.Structure):
     ]
 
 
+class BatchConfig(C.Structure):
+    _fields_ = [("slots", C.c_uint64), ("max_vars", C.c_int32), ("max_program_slots", C.c_int32),
+                ("device", C.c_int32), ("reserved", C.c_int32), ("shared", SolveOptions)]
+
+
 COUNTER_NAMES = ["iterations", "expansions", "fathomed", "fathomed_points", "bounded", "sampled", "enqueued",
                  "witness_rejected", "pruned_duplicate", "pruned_infeasible", "pruned_dominated",
                  "dropped_viable", "dropped_dominated", "screened_fp32", "certified_fp64", "peak_frontier"]

@@ -52,6 +52,17 @@ SIGNATURES = {
     "cmn_solver_kernels_per_iteration": (U64, [P]),
     "cmn_measure_fma_peak": (I32, [I32, C.POINTER(D)]),
     "cmn_solve": (I32, [P, C.POINTER(A.SolveOptions), C.POINTER(A.Outcome), P]),
+    "cmn_batch_create": (I32, [C.POINTER(A.BatchConfig), PP]),
+    "cmn_batch_destroy": (None, [P]),
+    "cmn_batch_add": (I32, [P, P, C.POINTER(A.SolveOptions), C.POINTER(U64)]),
+    "cmn_batch_step": (I32, [P, U64, C.POINTER(U64)]),
+    "cmn_batch_poll": (I32, [P, U64, C.POINTER(I32)]),
+    "cmn_batch_outcome": (I32, [P, U64, C.POINTER(A.Outcome), P]),
+    "cmn_batch_frontier": (I32, [P, U64, P, P, P, U64, C.POINTER(U64)]),
+    "cmn_batch_release": (I32, [P, U64]),
+    "cmn_batch_stream": (P, [P]),
+    "cmn_batch_kernels_per_iteration": (U64, [P]),
+    "cmn_batch_solve": (I32, [C.POINTER(A.BatchConfig), P, P, U64, P, P, U64]),
 }
 
 

@@ -29,7 +29,8 @@ NVCC_FLAGS = [
     "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
     "--expt-relaxed-constexpr", "-DNDEBUG",
 ]
-SOURCES = ["program.cpp", "eval_kernels.cu", "search_kernels.cu", "capi.cu", "noalloc.cu"]
+SOURCES = ["program.cpp", "eval_kernels.cu", "search_kernels.cu", "batch_kernels.cu", "capi.cu", "batch.cu",
+           "noalloc.cu"]
 
 
 def _nvcc() -> str:

@@ -1,0 +1,116 @@
+// batch.hpp -- many independent instances of uneven sizes advanced together:
+// each iteration is one captured graph in which the evaluator and the
+// sampler are single launches over the children of every instance, and the
+// per-instance steps (selection, incumbent, prune, pool rebuild, eviction)
+// run as one thread block per instance in shared memory.
+//
+// Every instance follows the batched algorithm of the single-instance
+// solver step for step (same selection order, salts, pool order, eviction
+// and adaptive screen), so an instance's result does not depend on which
+// other instances share the launches.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "../../include/cuminlp_gb300.h"
+#include "kernels.cuh"
+
+namespace cmn {
+
+constexpr int kMiThreads = 1024;   // threads of a per-instance block
+constexpr int kMiSortMax = 8192;   // largest pool a block sorts in shared memory
+
+struct BatchCfg {
+  int n_max;        // variables per instance, at most
+  int slots_max;    // program slots per instance, at most
+  int log2C;        // B: children per parent = 2^B
+  int max_slots;    // = B
+  int precision;
+  int sample_all;
+  int relative;
+  uint64_t S;
+  uint64_t e_max;         // parents per instance per iteration
+  uint64_t cap;           // pool capacity per instance
+  uint64_t P;             // pool stride: cap + e_max << B
+  uint64_t K;             // instance slots
+  uint64_t child_stride;  // child slots per instance: e_max << B
+  int64_t max_cycle;
+  int64_t enumerate_cap;
+};
+
+struct InstDesc {
+  const Instr* prog64;
+  const Instr* prog32;
+  const int32_t* kinds;
+  const double* root_lb;
+  const double* root_ub;
+  int32_t prog_len;
+  int32_t n_vars;
+  int32_t n_slots;
+  int32_t active;
+  uint64_t iter_limit;
+  uint64_t batch_iter_limit;
+  double tolerance;
+};
+
+struct InstState {
+  double gub;
+  double glb;
+  double dropped_lb_min;
+  uint64_t pool_min_key;
+  uint64_t pool_size;
+  uint64_t n_parents;
+  uint64_t salt_base;
+  uint64_t expansions;
+  uint64_t iterations;
+  uint64_t remaining;
+  uint64_t viable;
+  uint64_t dropped_min_key;
+  uint32_t done;
+  uint32_t converged;
+  uint32_t have_best;
+  uint32_t use_screen;
+  Cand best;
+  cmn_counters counters;
+};
+
+struct BatchBufs {
+  InstDesc* desc;
+  InstState* st;
+  double* lo;  // [K][n_max][P]
+  double* hi;
+  double* lb;  // [K][P]
+  uint32_t* depth;
+  double* plo;  // [K][n_max][e_max]
+  double* phi;
+  uint32_t* pdepth;  // [K][e_max]
+  ParentInfo* pinfo;
+  SlotPlan* slots;  // [K][e_max][B]
+  void* enum_scratch;  // [K][e_max][n_max]
+  void* bis_scratch;
+  uint64_t* heap_scratch;
+  double* clb;  // [K][child_stride]
+  uint8_t* cstate;
+  double* cval;
+  uint64_t* ce;
+  uint32_t* list;  // certify list
+  uint64_t* list_count;
+  uint32_t* block_counts;
+  uint32_t* block_offsets;
+  double* best_point;  // [K][n_max]
+};
+
+// Puts `slot`'s root box in its pool and resets its state.
+cudaError_t batch_init_slot(const BatchCfg& cfg, const BatchBufs& b, uint64_t slot, double gub0, cudaStream_t s);
+// Enqueues one iteration over every active instance (capturable).
+cudaError_t batch_iteration(const BatchCfg& cfg, const BatchBufs& b, int eval_grid, cudaStream_t s);
+size_t batch_eval_smem(const BatchCfg& cfg, bool fp32);
+size_t batch_sample_smem(const BatchCfg& cfg);
+// resident blocks per SM of the bound (fp32: screen) and sample kernels
+int batch_eval_occupancy(const BatchCfg& cfg, bool fp32);
+int batch_sample_occupancy(const BatchCfg& cfg);
+cudaError_t set_batch_kernel_attributes(int max_smem);
+
+}  // namespace cmn

@@ -1,0 +1,832 @@
+// batch_kernels.cu -- the multi-instance iteration (see batch.hpp).
+//
+// Per iteration: begin (thread per instance) -> select + gather + in-place
+// compaction (block per instance, pool sorted in shared memory) -> branch
+// (thread per parent) -> bound (one launch over all instances' children;
+// FP64, or FP32 screen + FP64 certify) -> sample (one launch) -> finish
+// (block per instance: ArgMin, incumbent and witness, prune, append kept
+// children, evict above the cap, pool minimum, adaptive screen).
+#include <cfloat>
+#include <cstdint>
+
+#include "batch.hpp"
+#include "eval_core.cuh"
+#include "launch.hpp"
+#include "policy.cuh"
+
+namespace cmn {
+
+namespace {
+
+constexpr uint8_t kCertifiedBit = 0x80;  // set by the FP64 certify pass
+constexpr int kMaxPerThread = kMiSortMax / kMiThreads;
+
+__device__ __forceinline__ bool gap_closed_b(double gub, double bound, double tol)
+{
+  return __dsub_rn(gub, bound) <= __dmul_rn(tol, fmax(1.0, fabs(gub)));
+}
+
+__device__ __forceinline__ double key_to_lb_b(uint64_t k)
+{
+  const uint64_t u = (k >> 63) ? (k & 0x7fffffffffffffffULL) : ~k;
+  return __longlong_as_double((long long)u);
+}
+
+__device__ __forceinline__ uint64_t next_pow2(uint64_t x)
+{
+  uint64_t p = 1;
+  while (p < x) p <<= 1;
+  return p;
+}
+
+// exclusive rank of `f` among the block's threads (1024 threads)
+__device__ __forceinline__ int block_rank(bool f, int& total)
+{
+  __shared__ int warp_tot[kMiThreads / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const unsigned ball = __ballot_sync(0xffffffffu, f);
+  if (lane == 0) warp_tot[wid] = __popc(ball);
+  __syncthreads();
+  int before = 0;
+  total = 0;
+  for (int w = 0; w < kMiThreads / 32; ++w) {
+    if (w < wid) before += warp_tot[w];
+    total += warp_tot[w];
+  }
+  __syncthreads();
+  return before + __popc(ball & ((1u << lane) - 1u));
+}
+
+// ascending bitonic sort of (key, pos) pairs, n a power of two
+__device__ void bitonic_sort(uint64_t* keys, uint32_t* pos, uint32_t n)
+{
+  for (uint32_t k = 2; k <= n; k <<= 1) {
+    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+      for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const uint32_t ixj = i ^ j;
+        if (ixj > i) {
+          const bool asc = (i & k) == 0;
+          const uint64_t ka = keys[i], kb = keys[ixj];
+          const uint32_t pa = pos[i], pb = pos[ixj];
+          const bool b_less = kb < ka || (kb == ka && pb < pa);
+          if (asc ? b_less : !b_less) {
+            keys[i] = kb;
+            keys[ixj] = ka;
+            pos[i] = pb;
+            pos[ixj] = pa;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+__device__ __forceinline__ size_t plane(const BatchCfg& c, uint64_t slot, int v)
+{
+  return ((size_t)slot * c.n_max + v) * c.P;
+}
+
+__device__ __forceinline__ size_t splane(const BatchCfg& c, uint64_t slot, int v)
+{
+  return ((size_t)slot * c.n_max + v) * c.e_max;
+}
+
+// Stable in-place compaction of the marked entries among the first `n` of
+// `slot`'s pool (marks in `keep`, new positions built in `newpos`).
+__device__ void compact_pool(const BatchCfg& c, const BatchBufs& b, uint64_t slot, uint32_t n, int n_vars,
+                             const uint8_t* keep, uint32_t* newpos, uint32_t* running)
+{
+  if (threadIdx.x == 0) *running = 0;
+  __syncthreads();
+  for (uint32_t base = 0; base < n; base += kMiThreads) {
+    const uint32_t i = base + threadIdx.x;
+    const bool f = i < n && keep[i];
+    int total;
+    const int r = block_rank(f, total);
+    if (f) newpos[i] = *running + (uint32_t)r;
+    __syncthreads();
+    if (threadIdx.x == 0) *running += (uint32_t)total;
+    __syncthreads();
+  }
+  double val[kMaxPerThread];
+  for (int v = -1; v < 2 * n_vars; ++v) {
+    // v = -1: lower bounds; then lo / hi planes
+    double* arr = v < 0 ? b.lb + (size_t)slot * c.P : (v & 1 ? b.hi : b.lo) + plane(c, slot, v >> 1);
+#pragma unroll
+    for (int j = 0; j < kMaxPerThread; ++j) {
+      const uint32_t i = threadIdx.x + j * kMiThreads;
+      if (i < n && keep[i]) val[j] = arr[i];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kMaxPerThread; ++j) {
+      const uint32_t i = threadIdx.x + j * kMiThreads;
+      if (i < n && keep[i]) arr[newpos[i]] = val[j];
+    }
+    __syncthreads();
+  }
+  uint32_t dv[kMaxPerThread];
+  uint32_t* dep = b.depth + (size_t)slot * c.P;
+#pragma unroll
+  for (int j = 0; j < kMaxPerThread; ++j) {
+    const uint32_t i = threadIdx.x + j * kMiThreads;
+    if (i < n && keep[i]) dv[j] = dep[i];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < kMaxPerThread; ++j) {
+    const uint32_t i = threadIdx.x + j * kMiThreads;
+    if (i < n && keep[i]) dep[newpos[i]] = dv[j];
+  }
+  __syncthreads();
+}
+
+struct SortSmem {
+  uint64_t* keys;
+  uint32_t* pos;
+  uint8_t* flag;
+};
+
+__device__ __forceinline__ SortSmem sort_smem(unsigned char* raw)
+{
+  SortSmem s;
+  s.keys = reinterpret_cast<uint64_t*>(raw);
+  s.pos = reinterpret_cast<uint32_t*>(s.keys + kMiSortMax);
+  s.flag = reinterpret_cast<uint8_t*>(s.pos + kMiSortMax);
+  return s;
+}
+
+// Marks the `k` smallest (key, position) entries among the first `n`.
+__device__ void mark_smallest(const double* lb, uint32_t n, uint32_t k, const SortSmem& s)
+{
+  if (k >= n) {
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) s.flag[i] = 1;
+    __syncthreads();
+    return;
+  }
+  const uint32_t n2 = (uint32_t)next_pow2(n);
+  for (uint32_t i = threadIdx.x; i < n2; i += blockDim.x) {
+    s.keys[i] = i < n ? lb_key(lb[i]) : ~0ULL;
+    s.pos[i] = i < n ? i : 0xffffffffu;
+    if (i < n) s.flag[i] = 0;
+  }
+  __syncthreads();
+  bitonic_sort(s.keys, s.pos, n2);
+  for (uint32_t i = threadIdx.x; i < k; i += blockDim.x) s.flag[s.pos[i]] = 1;
+  __syncthreads();
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------
+__global__ void batch_init_slot_kernel(const BatchCfg c, const BatchBufs b, uint64_t slot, double gub0)
+{
+  const InstDesc d = b.desc[slot];
+  for (int v = threadIdx.x; v < c.n_max; v += blockDim.x) {
+    if (v < d.n_vars) {
+      b.lo[plane(c, slot, v)] = d.root_lb[v];
+      b.hi[plane(c, slot, v)] = d.root_ub[v];
+    }
+    b.best_point[slot * c.n_max + v] = __longlong_as_double(0x7ff8000000000000LL);
+  }
+  if (threadIdx.x == 0) {
+    InstState* s = &b.st[slot];
+    memset(s, 0, sizeof(InstState));
+    s->gub = gub0;
+    s->glb = -DBL_MAX;
+    s->dropped_lb_min = INFINITY;
+    s->dropped_min_key = ~0ULL;
+    s->pool_size = 1;
+    s->viable = (-DBL_MAX <= gub0) ? 1 : 0;
+    s->pool_min_key = lb_key(-DBL_MAX);
+    s->use_screen = 1;
+    s->counters.peak_frontier = 1;
+    b.lb[slot * c.P] = -DBL_MAX;
+    b.depth[slot * c.P] = 0;
+  }
+}
+
+__global__ void batch_begin_kernel(const BatchCfg c, const BatchBufs b)
+{
+  const uint64_t slot = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= c.K) return;
+  InstState& s = b.st[slot];
+  const InstDesc& d = b.desc[slot];
+  s.n_parents = 0;
+  if (!d.active || s.done) return;
+  const uint64_t L = s.pool_size;
+  if (L == 0) {
+    s.done = 1;
+    return;
+  }
+  const double m = key_to_lb_b(s.pool_min_key);
+  if (gap_closed_b(s.gub, m, d.tolerance)) {
+    s.converged = 1;
+    s.done = 1;
+    return;
+  }
+  s.glb = m;
+  if (s.expansions >= d.iter_limit || (d.batch_iter_limit && s.iterations >= d.batch_iter_limit)) {
+    s.done = 1;
+    return;
+  }
+  uint64_t E = L < c.e_max ? L : c.e_max;
+  const uint64_t left = d.iter_limit - s.expansions;
+  if (E > left) E = left;
+  s.iterations += 1;
+  s.n_parents = E;
+  s.salt_base = s.expansions;
+  s.expansions += E;
+  s.counters.iterations = s.iterations;
+  s.counters.expansions = s.expansions;
+}
+
+// select the E best parents, stage them, compact the rest in place
+__global__ void __launch_bounds__(kMiThreads) batch_select_kernel(const BatchCfg c, const BatchBufs b)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ uint32_t running;
+  const uint64_t slot = blockIdx.x;
+  InstState* st = &b.st[slot];
+  const uint32_t E = (uint32_t)st->n_parents;
+  if (E == 0) return;
+  const uint32_t L = (uint32_t)st->pool_size;
+  const int n = b.desc[slot].n_vars;
+  const SortSmem s = sort_smem(smem_raw);
+  mark_smallest(b.lb + (size_t)slot * c.P, L, E, s);
+  // gather the selected parents in pool order
+  if (threadIdx.x == 0) running = 0;
+  __syncthreads();
+  for (uint32_t base = 0; base < L; base += kMiThreads) {
+    const uint32_t i = base + threadIdx.x;
+    const bool f = i < L && s.flag[i];
+    int total;
+    const int r = block_rank(f, total);
+    if (f) {
+      const uint32_t k = running + (uint32_t)r;
+      for (int v = 0; v < n; ++v) {
+        b.plo[splane(c, slot, v) + k] = b.lo[plane(c, slot, v) + i];
+        b.phi[splane(c, slot, v) + k] = b.hi[plane(c, slot, v) + i];
+      }
+      b.pdepth[slot * c.e_max + k] = b.depth[(size_t)slot * c.P + i];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) running += (uint32_t)total;
+    __syncthreads();
+  }
+  // the unselected entries keep their order at the front of the pool
+  for (uint32_t i = threadIdx.x; i < L; i += blockDim.x) s.flag[i] = !s.flag[i];
+  __syncthreads();
+  compact_pool(c, b, slot, L, n, s.flag, s.pos, &running);
+  if (threadIdx.x == 0) {
+    st->remaining = L - E;
+    st->pool_size = L - E;
+  }
+}
+
+__global__ void batch_branch_kernel(const BatchCfg c, const BatchBufs b)
+{
+  const uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= c.K * c.e_max) return;
+  const uint64_t slot = idx / c.e_max, k = idx % c.e_max;
+  InstState* st = &b.st[slot];
+  if (k >= st->n_parents) return;
+  const InstDesc d = b.desc[slot];
+  const size_t pk = slot * c.e_max + k;
+  EnumCand* ec = reinterpret_cast<EnumCand*>(b.enum_scratch) + pk * c.n_max;
+  BisCand* bc = reinterpret_cast<BisCand*>(b.bis_scratch) + pk * c.n_max;
+  uint64_t* heap = b.heap_scratch + pk * c.n_max;
+  SlotPlan* sp = b.slots + pk * c.max_slots;
+  const PolicyParams pp = {c.log2C, c.max_cycle, c.enumerate_cap, c.relative};
+  const ParentInfo pi =
+      bisection_policy(b.plo + splane(c, slot, 0) + k, b.phi + splane(c, slot, 0) + k, c.e_max, d.n_vars, d.kinds,
+                       pp, ec, bc, heap, sp);
+  b.pinfo[pk] = pi;
+  if (pi.fathom) {
+    atomicAdd((unsigned long long*)&st->counters.fathomed, 1ULL);
+    atomicAdd((unsigned long long*)&st->counters.fathomed_points, (unsigned long long)pi.nreg);
+  } else {
+    atomicAdd((unsigned long long*)&st->counters.bounded, (unsigned long long)pi.nreg);
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ T bconv_lo(double x);
+template <typename T>
+__device__ __forceinline__ T bconv_hi(double x);
+template <>
+__device__ __forceinline__ double bconv_lo<double>(double x) { return x; }
+template <>
+__device__ __forceinline__ double bconv_hi<double>(double x) { return x; }
+template <>
+__device__ __forceinline__ float bconv_lo<float>(double x) { return __double2float_rd(x); }
+template <>
+__device__ __forceinline__ float bconv_hi<float>(double x) { return __double2float_ru(x); }
+
+// kMode 1: FP64 bound; 2: FP32 screen; 3: FP64 certify of the listed children
+template <typename T, int kMode>
+__global__ void __launch_bounds__(kEvalThreads) batch_eval_kernel(const BatchCfg c, const BatchBufs b)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* base = reinterpret_cast<T*>(smem_raw);
+  const int B = blockDim.x;
+  Tile<T> t;
+  t.lo = base;
+  t.hi = base + (size_t)c.n_max * B;
+  t.slo = base + (size_t)2 * c.n_max * B;
+  t.shi = base + (size_t)(2 * c.n_max + c.slots_max) * B;
+  t.stride = B;
+  t.tid = threadIdx.x;
+  const uint64_t total = kMode == 3 ? *b.list_count : c.K * c.child_stride;
+  for (uint64_t idx = (uint64_t)blockIdx.x * B + threadIdx.x; idx < total; idx += (uint64_t)gridDim.x * B) {
+    const uint64_t g = kMode == 3 ? (uint64_t)b.list[idx] : idx;
+    const uint64_t slot = g / c.child_stride, local = g % c.child_stride;
+    const uint64_t k = local >> c.log2C, r = local & ((1ULL << c.log2C) - 1ULL);
+    const InstState* st = &b.st[slot];
+    if (k >= st->n_parents) continue;
+    const size_t pk = slot * c.e_max + k;
+    const ParentInfo pi = b.pinfo[pk];
+    if (pi.fathom || r >= pi.nreg) {
+      if (kMode != 3) b.cstate[g] = kChildNone;
+      continue;
+    }
+    const SlotPlan* sp = b.slots + pk * c.max_slots;
+    if (kMode == 2 && !st->use_screen) {
+      bool dup = false;
+      for (uint32_t j = 0; j < pi.count; ++j) dup = dup || ((r / sp[j].prefix) % sp[j].width >= sp[j].dom);
+      b.cstate[g] = dup ? kChildDuplicate : kChildScreened;
+      continue;
+    }
+    const InstDesc& d = b.desc[slot];
+    const int n = d.n_vars;
+    for (int v = 0; v < n; ++v) {
+      t.lo[v * B + t.tid] = bconv_lo<T>(b.plo[splane(c, slot, v) + k]);
+      t.hi[v * B + t.tid] = bconv_hi<T>(b.phi[splane(c, slot, v) + k]);
+    }
+    bool dup = false;
+    for (uint32_t j = 0; j < pi.count; ++j) {
+      const SlotPlan s = sp[j];
+      const uint64_t part = (r / s.prefix) % s.width;
+      if (part >= s.dom) dup = true;
+      double lo, hi;
+      slot_bounds((int)s.kind, b.plo[splane(c, slot, s.vid) + k], b.phi[splane(c, slot, s.vid) + k], part, s.width,
+                  lo, hi);
+      t.lo[s.vid * B + t.tid] = bconv_lo<T>(lo);
+      t.hi[s.vid * B + t.tid] = bconv_hi<T>(hi);
+    }
+    if (dup) {
+      b.cstate[g] = kChildDuplicate;
+      continue;
+    }
+    const Instr* prog = sizeof(T) == 4 ? d.prog32 : d.prog64;
+    const Verdict<T> v = run_interval<T>(prog, d.prog_len, t);
+    const double lb = (double)v.obj.lo;
+    const double gub = st->gub;
+    b.clb[g] = lb;
+    if (kMode == 2) {
+      b.cstate[g] = v.excluded ? kChildInfeasible : (lb > gub ? kChildDominated : kChildScreened);
+    } else {
+      const uint8_t sv = !v.feasible ? kChildInfeasible : (lb > gub ? kChildDominated : kChildEligible);
+      b.cstate[g] = kMode == 3 ? (uint8_t)(sv | kCertifiedBit) : sv;
+    }
+  }
+}
+
+__device__ __forceinline__ double child_bound(const BatchCfg& c, const BatchBufs& b, uint64_t slot, uint64_t k,
+                                              uint64_t r, int v, const SlotPlan* sp, uint32_t count, double& hi)
+{
+  double lo = b.plo[splane(c, slot, v) + k];
+  hi = b.phi[splane(c, slot, v) + k];
+  for (uint32_t j = 0; j < count; ++j) {
+    if (sp[j].vid == (uint32_t)v) {
+      const uint64_t part = (r / sp[j].prefix) % sp[j].width;
+      slot_bounds((int)sp[j].kind, lo, hi, part, sp[j].width, lo, hi);
+      break;
+    }
+  }
+  return lo;
+}
+
+// samples (or exact points of fathomed parents) of every child: the best
+// (value, element) per child
+__global__ void __launch_bounds__(kEvalThreads) batch_sample_kernel(const BatchCfg c, const BatchBufs b)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* base = reinterpret_cast<double*>(smem_raw);
+  const int B = blockDim.x;
+  Tile<double> t;
+  t.lo = base;
+  t.hi = base;
+  t.slo = base + (size_t)c.n_max * B;
+  t.shi = t.slo;
+  t.stride = B;
+  t.tid = threadIdx.x;
+  const uint64_t total = c.K * c.child_stride;
+  for (uint64_t g = (uint64_t)blockIdx.x * B + threadIdx.x; g < total; g += (uint64_t)gridDim.x * B) {
+    const uint64_t slot = g / c.child_stride, local = g % c.child_stride;
+    const uint64_t k = local >> c.log2C, r = local & ((1ULL << c.log2C) - 1ULL);
+    InstState* st = &b.st[slot];
+    if (k >= st->n_parents) continue;
+    b.cval[g] = INFINITY;
+    const size_t pk = slot * c.e_max + k;
+    const ParentInfo pi = b.pinfo[pk];
+    if (r >= pi.nreg) continue;
+    const bool fathom = pi.fathom != 0;
+    if (!fathom) {
+      const uint8_t s8 = b.cstate[g] & 0x7f;
+      const bool take = c.sample_all ? (s8 != kChildNone) : (s8 == kChildEligible);
+      if (!take) continue;
+    }
+    const InstDesc& d = b.desc[slot];
+    const int n = d.n_vars;
+    const SlotPlan* sp = b.slots + pk * c.max_slots;
+    const uint64_t salt = st->salt_base + k + 1;
+    const uint64_t S = fathom ? 1 : c.S;
+    double best = INFINITY;
+    uint64_t best_e = 0;
+    for (uint64_t i = 0; i < S; ++i) {
+      for (int v = 0; v < n; ++v) {
+        double hi;
+        const double lo = child_bound(c, b, slot, k, r, v, sp, pi.count, hi);
+        t.lo[v * B + t.tid] = fathom ? lo : sample_value(d.kinds[v] != 0, lo, hi, (uint64_t)v, i, r, salt);
+      }
+      const PointVerdict pv = run_point(d.prog64, d.prog_len, t);
+      double value = (pv.feasible && !(pv.obj != pv.obj)) ? pv.obj : INFINITY;
+      if (fathom && value < INFINITY) {
+        bool ok = true;
+        for (int v = 0; v < n && ok; ++v) {
+          const double x = t.lo[v * B + t.tid];
+          if (!(x >= d.root_lb[v]) || !(x <= d.root_ub[v])) ok = false;
+          else if (d.kinds[v] != 0 && fabs(__dsub_rn(x, rint(x))) > 1e-6) ok = false;
+        }
+        if (!ok) {
+          if (value < st->gub) atomicAdd((unsigned long long*)&st->counters.witness_rejected, 1ULL);
+          value = INFINITY;
+        }
+      }
+      if (value < best) {
+        best = value;
+        best_e = r * S + i;
+      }
+    }
+    b.cval[g] = best;
+    b.ce[g] = best_e;
+  }
+}
+
+// per instance: incumbent, prune, append kept children, evict, statistics
+__global__ void __launch_bounds__(kMiThreads) batch_finish_kernel(const BatchCfg c, const BatchBufs b)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ uint32_t running;
+  __shared__ Cand best_s;
+  __shared__ unsigned long long cnt[10];
+  __shared__ unsigned long long min_key_s;
+  const uint64_t slot = blockIdx.x;
+  InstState* st = &b.st[slot];
+  const uint32_t E = (uint32_t)st->n_parents;
+  if (E == 0) return;
+  const InstDesc d = b.desc[slot];
+  const int n = d.n_vars;
+  const uint32_t nch = E << c.log2C;
+  const uint64_t cbase = slot * c.child_stride;
+  const double gub_old = st->gub;
+  if (threadIdx.x < 10) cnt[threadIdx.x] = 0;
+  if (threadIdx.x == 0) min_key_s = ~0ULL;
+
+  // (1) ArgMin over (value, parent, element)
+  Cand mine = {INFINITY, 0xffffffffu, 0, ~0ULL};
+  for (uint32_t local = threadIdx.x; local < nch; local += blockDim.x) {
+    const double v = b.cval[cbase + local];
+    if (v < INFINITY) {
+      const Cand cc = {v, local >> c.log2C, 0, b.ce[cbase + local]};
+      if (cand_less(cc, mine)) mine = cc;
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    Cand o;
+    o.value = __shfl_down_sync(0xffffffffu, mine.value, off);
+    o.k = __shfl_down_sync(0xffffffffu, mine.k, off);
+    o.e = __shfl_down_sync(0xffffffffu, mine.e, off);
+    o.pad = 0;
+    if (cand_less(o, mine)) mine = o;
+  }
+  {
+    __shared__ Cand wb[kMiThreads / 32];
+    if ((threadIdx.x & 31) == 0) wb[threadIdx.x >> 5] = mine;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      Cand bst = wb[0];
+      for (int w = 1; w < kMiThreads / 32; ++w)
+        if (cand_less(wb[w], bst)) bst = wb[w];
+      best_s = bst;
+    }
+    __syncthreads();
+  }
+  const Cand best = best_s;
+  const bool improved = best.value < gub_old;
+  if (improved) {
+    const uint64_t k = best.k;
+    const size_t pk = slot * c.e_max + k;
+    const ParentInfo pi = b.pinfo[pk];
+    const SlotPlan* sp = b.slots + pk * c.max_slots;
+    const bool fathom = pi.fathom != 0;
+    const uint64_t S = fathom ? 1 : c.S;
+    const uint64_t r = best.e / S, i = best.e % S;
+    for (int v = threadIdx.x; v < n; v += blockDim.x) {
+      double hi;
+      const double lo = child_bound(c, b, slot, k, r, v, sp, pi.count, hi);
+      b.best_point[slot * c.n_max + v] =
+          fathom ? lo : sample_value(d.kinds[v] != 0, lo, hi, (uint64_t)v, i, r, st->salt_base + k + 1);
+    }
+    if (threadIdx.x == 0) {
+      st->gub = best.value;
+      st->best = best;
+      st->have_best = 1;
+    }
+  }
+  __syncthreads();
+  const double gub = st->gub;
+
+  // (2) verdict counts and (3) append kept children after the remaining pool
+  const uint32_t remaining = (uint32_t)st->remaining;
+  if (threadIdx.x == 0) running = 0;
+  __syncthreads();
+  unsigned long long l_dup = 0, l_inf = 0, l_dom = 0, l_kept = 0, l_smp = 0, l_valid = 0, l_excl = 0, l_cert = 0;
+  for (uint32_t cb = 0; cb < nch; cb += kMiThreads) {
+    const uint32_t local = cb + threadIdx.x;
+    bool keep = false;
+    if (local < nch) {
+      const uint8_t raw = b.cstate[cbase + local];
+      const uint64_t k = local >> c.log2C, r = local & ((1ULL << c.log2C) - 1ULL);
+      const ParentInfo pi = b.pinfo[slot * c.e_max + k];
+      if (!pi.fathom && r < pi.nreg) {
+        const uint8_t s8 = raw & 0x7f;
+        if (s8 != kChildNone) {
+          if (c.sample_all || s8 == kChildEligible) ++l_smp;
+          if (s8 != kChildDuplicate) {
+            ++l_valid;
+            if (s8 == kChildInfeasible || s8 == kChildDominated) ++l_excl;
+            if (raw & kCertifiedBit) ++l_cert;
+          }
+          if (s8 == kChildDuplicate) ++l_dup;
+          else if (s8 == kChildInfeasible) ++l_inf;
+          else if (s8 == kChildDominated || s8 == kChildScreened || b.clb[cbase + local] > gub) ++l_dom;
+          else {
+            ++l_kept;
+            keep = true;
+          }
+        }
+      }
+    }
+    int total;
+    const int rank = block_rank(keep, total);
+    if (keep) {
+      const uint32_t at = remaining + running + (uint32_t)rank;
+      const uint64_t k = local >> c.log2C, r = local & ((1ULL << c.log2C) - 1ULL);
+      const size_t pk = slot * c.e_max + k;
+      const ParentInfo pi = b.pinfo[pk];
+      const SlotPlan* sp = b.slots + pk * c.max_slots;
+      for (int v = 0; v < n; ++v) {
+        double hi;
+        const double lo = child_bound(c, b, slot, k, r, v, sp, pi.count, hi);
+        b.lo[plane(c, slot, v) + at] = lo;
+        b.hi[plane(c, slot, v) + at] = hi;
+      }
+      b.lb[(size_t)slot * c.P + at] = b.clb[cbase + local];
+      b.depth[(size_t)slot * c.P + at] = b.pdepth[pk] + 1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) running += (uint32_t)total;
+    __syncthreads();
+  }
+  atomicAdd(&cnt[0], l_dup);
+  atomicAdd(&cnt[1], l_inf);
+  atomicAdd(&cnt[2], l_dom);
+  atomicAdd(&cnt[3], l_kept);
+  atomicAdd(&cnt[4], l_smp);
+  atomicAdd(&cnt[5], l_valid);
+  atomicAdd(&cnt[6], l_excl);
+  atomicAdd(&cnt[7], l_cert);
+  __syncthreads();
+  const uint32_t new_size = remaining + (uint32_t)cnt[3];
+
+  // (4) above the cap: keep the `cap` best, fold the rest into the floor
+  uint32_t final_size = new_size;
+  if (new_size > c.cap) {
+    const SortSmem s = sort_smem(smem_raw);
+    const double* lbp = b.lb + (size_t)slot * c.P;
+    mark_smallest(lbp, new_size, (uint32_t)c.cap, s);
+    unsigned long long via = 0, dom = 0;
+    uint64_t mk = ~0ULL;
+    for (uint32_t i = threadIdx.x; i < new_size; i += blockDim.x) {
+      if (s.flag[i]) continue;
+      const double x = lbp[i];
+      if (x <= gub) {
+        ++via;
+        const uint64_t kk = lb_key(x);
+        mk = kk < mk ? kk : mk;
+      } else {
+        ++dom;
+      }
+    }
+    atomicAdd(&cnt[8], via);
+    atomicAdd(&cnt[9], dom);
+    if (mk != ~0ULL) atomicMin(&min_key_s, (unsigned long long)mk);
+    __syncthreads();
+    compact_pool(c, b, slot, new_size, n, s.flag, s.pos, &running);
+    final_size = (uint32_t)c.cap;
+  }
+
+  // (5) pool minimum and viable count
+  uint64_t mk = ~0ULL;
+  unsigned long long viable = 0;
+  const double* lbp = b.lb + (size_t)slot * c.P;
+  for (uint32_t i = threadIdx.x; i < final_size; i += blockDim.x) {
+    const uint64_t kk = lb_key(lbp[i]);
+    mk = kk < mk ? kk : mk;
+    if (lbp[i] <= gub) ++viable;
+  }
+  __shared__ unsigned long long pool_min_s, viable_s;
+  if (threadIdx.x == 0) {
+    pool_min_s = ~0ULL;
+    viable_s = 0;
+  }
+  __syncthreads();
+  atomicMin(&pool_min_s, (unsigned long long)mk);
+  atomicAdd(&viable_s, viable);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    cmn_counters& ct = st->counters;
+    ct.pruned_duplicate += cnt[0];
+    ct.pruned_infeasible += cnt[1];
+    ct.pruned_dominated += cnt[2];
+    ct.enqueued += cnt[3];
+    ct.sampled += cnt[4] * c.S;
+    if (c.precision == CMN_PRECISION_FP32_SCREEN) {
+      if (st->use_screen) ct.screened_fp32 += cnt[5];
+      ct.certified_fp64 += cnt[7];
+      if (cnt[5] > 0) {
+        const unsigned long long x = st->use_screen ? cnt[5] - cnt[7] : cnt[6];
+        st->use_screen = (x * 4 >= cnt[5]) ? 1 : 0;
+      }
+    } else {
+      ct.certified_fp64 += cnt[5];
+    }
+    ct.dropped_viable += cnt[8];
+    ct.dropped_dominated += cnt[9];
+    if (min_key_s < st->dropped_min_key) st->dropped_min_key = min_key_s;
+    if (st->dropped_min_key != ~0ULL) st->dropped_lb_min = key_to_lb_b(st->dropped_min_key);
+    st->pool_size = final_size;
+    st->pool_min_key = pool_min_s;
+    st->viable = viable_s;
+    if (final_size > ct.peak_frontier) ct.peak_frontier = final_size;
+  }
+}
+
+// ---------------------------------------------------------------------
+// certify list (children the screen left open), stable over (slot, child)
+// ---------------------------------------------------------------------
+__global__ void __launch_bounds__(512) batch_list_count_kernel(const BatchCfg c, const BatchBufs b)
+{
+  const uint64_t total = c.K * c.child_stride;
+  const uint64_t i = (uint64_t)blockIdx.x * 512 + threadIdx.x;
+  bool f = false;
+  if (i < total) {
+    const uint64_t slot = i / c.child_stride, k = (i % c.child_stride) >> c.log2C;
+    f = k < b.st[slot].n_parents && b.cstate[i] == kChildScreened;
+  }
+  const int cnt = __syncthreads_count(f);
+  if (threadIdx.x == 0) b.block_counts[blockIdx.x] = (uint32_t)cnt;
+}
+
+__global__ void batch_list_scan_kernel(const BatchCfg c, const BatchBufs b)
+{
+  __shared__ uint64_t carry;
+  __shared__ uint32_t wsum[32];
+  const uint64_t nblocks = (c.K * c.child_stride + 511) / 512;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (uint64_t base = 0; base < nblocks; base += blockDim.x) {
+    const uint64_t i = base + threadIdx.x;
+    const uint32_t v = i < nblocks ? b.block_counts[i] : 0;
+    uint32_t x = v;
+    for (int off = 1; off < 32; off <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+      if (lane >= off) x += y;
+    }
+    if (lane == 31) wsum[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+      uint32_t sw = lane < (int)(blockDim.x / 32) ? wsum[lane] : 0;
+      for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, sw, off);
+        if (lane >= off) sw += y;
+      }
+      wsum[lane] = sw;
+    }
+    __syncthreads();
+    const uint64_t cy = carry;
+    if (i < nblocks) b.block_offsets[i] = (uint32_t)(cy + (wid > 0 ? wsum[wid - 1] : 0) + x - v);
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry = cy + wsum[blockDim.x / 32 - 1];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *b.list_count = carry;
+}
+
+__global__ void __launch_bounds__(512) batch_list_scatter_kernel(const BatchCfg c, const BatchBufs b)
+{
+  __shared__ int wt[16];
+  const uint64_t total = c.K * c.child_stride;
+  const uint64_t i = (uint64_t)blockIdx.x * 512 + threadIdx.x;
+  bool f = false;
+  if (i < total) {
+    const uint64_t slot = i / c.child_stride, k = (i % c.child_stride) >> c.log2C;
+    f = k < b.st[slot].n_parents && b.cstate[i] == kChildScreened;
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const unsigned ball = __ballot_sync(0xffffffffu, f);
+  if (lane == 0) wt[wid] = __popc(ball);
+  __syncthreads();
+  int before = 0;
+  for (int w = 0; w < wid; ++w) before += wt[w];
+  if (f) b.list[b.block_offsets[blockIdx.x] + before + __popc(ball & ((1u << lane) - 1u))] = (uint32_t)i;
+}
+
+// ---------------------------------------------------------------------
+size_t batch_eval_smem(const BatchCfg& c, bool fp32)
+{
+  return (fp32 ? 4 : 8) * (size_t)(2 * c.n_max + 2 * c.slots_max) * kEvalThreads;
+}
+
+size_t batch_sample_smem(const BatchCfg& c) { return 8 * (size_t)(c.n_max + c.slots_max) * kEvalThreads; }
+
+int batch_eval_occupancy(const BatchCfg& c, bool fp32)
+{
+  int n = 0;
+  if (fp32)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_eval_kernel<float, 2>, kEvalThreads,
+                                                  batch_eval_smem(c, true));
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_eval_kernel<double, 1>, kEvalThreads,
+                                                  batch_eval_smem(c, false));
+  return n;
+}
+
+int batch_sample_occupancy(const BatchCfg& c)
+{
+  int n = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_sample_kernel, kEvalThreads, batch_sample_smem(c));
+  return n;
+}
+
+static size_t sort_smem_bytes() { return (size_t)kMiSortMax * (8 + 4 + 1); }
+
+cudaError_t set_batch_kernel_attributes(int max_smem)
+{
+  const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
+  cudaFuncAttributes fa;
+  cudaError_t e = cudaFuncGetAttributes(&fa, batch_select_kernel);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_select_kernel, at, max_smem - (int)fa.sharedSizeBytes);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, batch_finish_kernel);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_finish_kernel, at, max_smem - (int)fa.sharedSizeBytes);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_eval_kernel<double, 1>, at, max_smem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_eval_kernel<float, 2>, at, max_smem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_eval_kernel<double, 3>, at, max_smem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_sample_kernel, at, max_smem);
+  return e;
+}
+
+cudaError_t batch_init_slot(const BatchCfg& c, const BatchBufs& b, uint64_t slot, double gub0, cudaStream_t s)
+{
+  batch_init_slot_kernel<<<1, 128, 0, s>>>(c, b, slot, gub0);
+  return cudaGetLastError();
+}
+
+cudaError_t batch_iteration(const BatchCfg& c, const BatchBufs& b, int eval_grid, cudaStream_t s)
+{
+  const int kb = (int)((c.K + 255) / 256);
+  batch_begin_kernel<<<kb, 256, 0, s>>>(c, b);
+  batch_select_kernel<<<(int)c.K, kMiThreads, sort_smem_bytes(), s>>>(c, b);
+  const uint64_t np = c.K * c.e_max;
+  batch_branch_kernel<<<(int)((np + 127) / 128), 128, 0, s>>>(c, b);
+  const bool fp32 = c.precision == CMN_PRECISION_FP32_SCREEN;
+  if (fp32) {
+    batch_eval_kernel<float, 2><<<eval_grid, kEvalThreads, batch_eval_smem(c, true), s>>>(c, b);
+    const int lg = (int)((c.K * c.child_stride + 511) / 512);
+    batch_list_count_kernel<<<lg, 512, 0, s>>>(c, b);
+    batch_list_scan_kernel<<<1, 1024, 0, s>>>(c, b);
+    batch_list_scatter_kernel<<<lg, 512, 0, s>>>(c, b);
+    batch_eval_kernel<double, 3><<<eval_grid, kEvalThreads, batch_eval_smem(c, false), s>>>(c, b);
+  } else {
+    batch_eval_kernel<double, 1><<<eval_grid, kEvalThreads, batch_eval_smem(c, false), s>>>(c, b);
+  }
+  batch_sample_kernel<<<eval_grid, kEvalThreads, batch_sample_smem(c), s>>>(c, b);
+  batch_finish_kernel<<<(int)c.K, kMiThreads, sort_smem_bytes(), s>>>(c, b);
+  return cudaGetLastError();
+}
+
+}  // namespace cmn

@@ -15,6 +15,7 @@
 #include "../../include/cuminlp_gb300.h"
 #include "handles.hpp"
 #include "kernels.cuh"
+#include "batch.hpp"
 #include "launch.hpp"
 #include "program.hpp"
 #include "search.hpp"
@@ -93,6 +94,7 @@ static cudaError_t ensure_attributes()
   std::lock_guard<std::mutex> lock(g_attr_mu);
   if (dev < 31 && (g_attr_device_mask & (1 << dev))) return cudaSuccess;
   e = set_eval_kernel_attributes(max_dynamic_smem());
+  if (e == cudaSuccess) e = set_batch_kernel_attributes(max_dynamic_smem());
   if (e == cudaSuccess && dev < 31) g_attr_device_mask |= (1 << dev);
   return e;
 }

@@ -14,6 +14,7 @@
 
 #include "eval_core.cuh"
 #include "launch.hpp"
+#include "policy.cuh"
 #include "search.hpp"
 
 namespace cmn {
@@ -428,199 +429,21 @@ __global__ void __launch_bounds__(kScanBlock) scatter_kernel(const P pred, const
 
 // ---------------------------------------------------------------------
 // branching: BisectionBudgetCompositionPolicy::choose per parent
-// (policy/bisection_budget.hpp:81-262), with the C++ library's heap order
-// for equally wide candidates
 // ---------------------------------------------------------------------
-struct EnumCand {
-  uint64_t vid, domain, bits;
-  uint32_t kind, pad;
-};
-struct BisCand {
-  uint64_t vid, bis;
-  double live, orig;
-  uint32_t kind, pad;
-};
-
-struct HeapCtx {
-  const BisCand* c;
-  int relative;
-  __device__ double key(uint64_t i) const { return relative ? __ddiv_rn(c[i].live, c[i].orig) : c[i].live; }
-  __device__ bool less(uint64_t a, uint64_t b) const { return key(a) < key(b); }
-};
-
-__device__ void hp_push_hole(uint64_t* f, int64_t hole, int64_t top, uint64_t value, const HeapCtx& h)
-{
-  int64_t parent = (hole - 1) / 2;
-  while (hole > top && h.less(f[parent], value)) {
-    f[hole] = f[parent];
-    hole = parent;
-    parent = (hole - 1) / 2;
-  }
-  f[hole] = value;
-}
-
-__device__ void hp_adjust(uint64_t* f, int64_t hole, int64_t len, uint64_t value, const HeapCtx& h)
-{
-  const int64_t top = hole;
-  int64_t second = hole;
-  while (second < (len - 1) / 2) {
-    second = 2 * (second + 1);
-    if (h.less(f[second], f[second - 1])) second--;
-    f[hole] = f[second];
-    hole = second;
-  }
-  if ((len & 1) == 0 && second == (len - 2) / 2) {
-    second = 2 * (second + 1);
-    f[hole] = f[second - 1];
-    hole = second - 1;
-  }
-  hp_push_hole(f, hole, top, value, h);
-}
-
-__device__ void hp_make(uint64_t* f, int64_t len, const HeapCtx& h)
-{
-  if (len < 2) return;
-  int64_t parent = (len - 2) / 2;
-  for (;;) {
-    const uint64_t v = f[parent];
-    hp_adjust(f, parent, len, v, h);
-    if (parent == 0) return;
-    parent--;
-  }
-}
-
-__device__ __forceinline__ uint64_t int_domain(double lb, double ub)
-{
-  const double lo = ceil(lb), hi = floor(ub);
-  if (hi < lo) return 0;
-  return (uint64_t)__double2ull_rz(__dsub_rn(hi, lo)) + 1;
-}
-
-__device__ __forceinline__ uint64_t bits_for(uint64_t d)
-{
-  const uint64_t eff = d == 0 ? 1 : d;
-  uint64_t bits = 0, cap = 1;
-  while (cap < eff) {
-    cap <<= 1;
-    ++bits;
-  }
-  return bits > 1 ? bits : 1;
-}
-
 __global__ void branch_kernel(const SolverCfg cfg, const SolverBufs b)
 {
   const SolverDev* d = b.dev;
   if (d->done) return;
   const uint64_t E = d->n_parents;
   const int n = cfg.n_vars;
+  const PolicyParams pp = {cfg.log2C, cfg.max_cycle, cfg.enumerate_cap, cfg.relative};
   uint64_t fathomed = 0, fathomed_points = 0, bounded = 0;
   for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < E; k += (uint64_t)gridDim.x * blockDim.x) {
     EnumCand* ec = reinterpret_cast<EnumCand*>(b.enum_scratch) + k * (uint64_t)n;
     BisCand* bc = reinterpret_cast<BisCand*>(b.bis_scratch) + k * (uint64_t)n;
     uint64_t* heap = b.heap_scratch + k * (uint64_t)n;
-    const int64_t cap = cfg.max_cycle == 0 ? 64 : cfg.max_cycle;
-    int64_t ne = 0, nb = 0, live = 0;
-    for (int v = 0; v < n; ++v) {
-      const double lb = b.plo[(uint64_t)v * cfg.e_max + k], ub = b.phi[(uint64_t)v * cfg.e_max + k];
-      if (ub > lb) ++live;
-    }
-    for (int v = 0; v < n && ne + nb < cap; ++v) {
-      const double lb = b.plo[(uint64_t)v * cfg.e_max + k], ub = b.phi[(uint64_t)v * cfg.e_max + k];
-      if (!(ub > lb)) continue;
-      const double w = __dsub_rn(ub, lb);
-      const int vk = b.kinds[v];
-      if (vk == CMN_VAR_BINARY) {
-        ec[ne] = {(uint64_t)v, 2, bits_for(2), (uint32_t)CMN_SLOT_BINARY_ENUMERATE, 0};
-        ++ne;
-      } else if (vk == CMN_VAR_INTEGER) {
-        const uint64_t dd = int_domain(lb, ub);
-        const uint64_t dm = dd > 1 ? dd : 1;
-        if (cfg.enumerate_cap == 0 || dm <= (uint64_t)cfg.enumerate_cap) {
-          ec[ne] = {(uint64_t)v, dd, bits_for(dd), (uint32_t)CMN_SLOT_INTEGER_ENUMERATE, 0};
-          ++ne;
-        } else {
-          bc[nb] = {(uint64_t)v, 0, w, w, (uint32_t)CMN_SLOT_INTEGER_PARTITION, 0};
-          ++nb;
-        }
-      } else {
-        bc[nb] = {(uint64_t)v, 0, w, w, (uint32_t)CMN_SLOT_CONTINUOUS, 0};
-        ++nb;
-      }
-    }
-    ParentInfo pi;
     SlotPlan* sp = b.slots + k * (uint64_t)cfg.max_slots;
-    if (ne + nb == 0) {
-      pi.count = 0;
-      pi.nreg = 1;
-      pi.fathom = 1;
-    } else {
-      for (int64_t i = 1; i < ne; ++i) {  // stable insertion sort by cost
-        const EnumCand x = ec[i];
-        int64_t j = i - 1;
-        while (j >= 0 && x.bits < ec[j].bits) {
-          ec[j + 1] = ec[j];
-          --j;
-        }
-        ec[j + 1] = x;
-      }
-      uint64_t remaining = (uint64_t)cfg.log2C;
-      int64_t taken = 0;
-      for (; taken < ne; ++taken) {
-        if (ec[taken].bits > remaining) break;
-        remaining -= ec[taken].bits;
-      }
-      for (int64_t i = taken; i < ne; ++i) {
-        if (ec[i].kind == CMN_SLOT_INTEGER_ENUMERATE) {
-          const uint64_t v = ec[i].vid;
-          const double w = __dsub_rn(b.phi[v * cfg.e_max + k], b.plo[v * cfg.e_max + k]);
-          bc[nb] = {v, 0, w, w, (uint32_t)CMN_SLOT_INTEGER_PARTITION, 0};
-          ++nb;
-        }
-      }
-      for (int64_t i = 0; i < nb; ++i) heap[i] = (uint64_t)i;
-      const HeapCtx h = {bc, cfg.relative};
-      hp_make(heap, nb, h);
-      uint64_t spent = 0;
-      for (; spent < remaining && nb > 0; ++spent) {
-        // pop_heap, halve the top, push_heap
-        if (nb > 1) {
-          const uint64_t v = heap[nb - 1];
-          heap[nb - 1] = heap[0];
-          hp_adjust(heap, 0, nb - 1, v, h);
-        }
-        BisCand* c = &bc[heap[nb - 1]];
-        c->live = __ddiv_rn(c->live, 2.0);
-        ++c->bis;
-        hp_push_hole(heap, nb - 1, 0, heap[nb - 1], h);
-      }
-      for (uint64_t q = spent; q < remaining; ++q) {
-        int64_t widest = 0;
-        for (int64_t i = 1; i < taken; ++i)
-          if (ec[i].bits > ec[widest].bits) widest = i;
-        ++ec[widest].bits;
-      }
-      uint32_t count = 0;
-      bool all_enum = true;
-      for (int64_t i = 0; i < taken; ++i) {
-        sp[count] = {1ULL << ec[i].bits, 0, ec[i].domain, (uint32_t)ec[i].vid, ec[i].kind};
-        ++count;
-      }
-      for (int64_t i = 0; i < nb; ++i) {
-        if (bc[i].bis == 0) continue;
-        const uint64_t w = 1ULL << bc[i].bis;
-        sp[count] = {w, 0, w, (uint32_t)bc[i].vid, bc[i].kind};
-        all_enum = false;
-        ++count;
-      }
-      uint64_t running = 1;
-      for (uint32_t j = 0; j < count; ++j) {
-        sp[j].prefix = running;
-        running *= sp[j].width;
-      }
-      pi.count = count;
-      pi.nreg = running;
-      pi.fathom = (live <= (int64_t)count && all_enum) ? 1 : 0;
-    }
+    const ParentInfo pi = bisection_policy(b.plo + k, b.phi + k, cfg.e_max, n, b.kinds, pp, ec, bc, heap, sp);
     b.pinfo[k] = pi;
     if (pi.fathom) {
       ++fathomed;

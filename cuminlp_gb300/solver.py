@@ -268,3 +268,149 @@ def solve(problem: Problem | DeviceProblem, **options) -> dict:
         return s.outcome()
     finally:
         s.close()
+
+
+# the options a batch fixes for all of its instances
+SHARED_OPTIONS = ("precision", "bisection_budget", "batch_parents", "frontier_cap", "sample_points", "sample_all",
+                  "relative_width", "max_cycle_size", "enumerate_cap")
+
+
+def batch_options(**kw) -> A.SolveOptions:
+    """Options for a batch: per-instance pools are small (frontier_cap +
+    batch_parents * 2^bisection_budget <= 8192), so the defaults differ
+    from the single-instance solver's."""
+    kw.setdefault("batch_parents", 256)
+    kw.setdefault("frontier_cap", 4096)
+    return default_options(**kw)
+
+
+class Batch:
+    """Many problems of uneven sizes resident in slots and advanced together
+    (cmn_batch_*)."""
+
+    def __init__(self, slots: int, max_vars: int, max_program_slots: int = -1, device: int = 0, **shared):
+        self.options = batch_options(**shared)
+        cfg = A.BatchConfig()
+        cfg.slots = slots
+        cfg.max_vars = max_vars
+        cfg.max_program_slots = max_program_slots
+        cfg.device = device
+        cfg.shared = self.options
+        h = C.c_void_p()
+        check(lib().cmn_batch_create(C.byref(cfg), C.byref(h)))
+        self.handle = h
+        self.slots: dict[int, DeviceProblem] = {}
+
+    def instance_options(self, **kw) -> A.SolveOptions:
+        o = A.SolveOptions()
+        C.memmove(C.byref(o), C.byref(self.options), C.sizeof(o))
+        for k, v in kw.items():
+            if k in SHARED_OPTIONS:
+                raise TypeError(f"{k} is fixed by the batch")
+            if k == "known_primal_bound" and v is not None:
+                o.has_known_primal = 1
+            if v is None:
+                continue
+            if not hasattr(o, k):
+                raise TypeError(f"unknown solve option {k}")
+            setattr(o, k, v)
+        return o
+
+    def add(self, dp: DeviceProblem, **options) -> int:
+        o = self.instance_options(**options)
+        slot = C.c_uint64()
+        check(lib().cmn_batch_add(self.handle, dp.handle, C.byref(o), C.byref(slot)))
+        self.slots[slot.value] = dp
+        return slot.value
+
+    def step(self, max_iterations: int = 0) -> int:
+        running = C.c_uint64()
+        check(lib().cmn_batch_step(self.handle, int(max_iterations), C.byref(running)))
+        return running.value
+
+    def done(self, slot: int) -> bool:
+        d = C.c_int32()
+        check(lib().cmn_batch_poll(self.handle, slot, C.byref(d)))
+        return bool(d.value)
+
+    def outcome(self, slot: int) -> dict:
+        o = A.Outcome()
+        pt = np.empty(self.slots[slot].n_vars)
+        check(lib().cmn_batch_outcome(self.handle, slot, C.byref(o), A.ptr(pt)))
+        d = A.outcome_dict(o)
+        d["best_point"] = pt if o.found_incumbent else np.array([])
+        return d
+
+    def frontier(self, slot: int, room: int = 1 << 16):
+        """(boxes [count, 2n] interleaved, lower bounds, depths) of `slot`."""
+        n = self.slots[slot].n_vars
+        cnt = C.c_uint64()
+        check(lib().cmn_batch_frontier(self.handle, slot, None, None, None, 0, C.byref(cnt)))
+        m = min(cnt.value, room)
+        boxes = np.empty((m, 2 * n))
+        lb = np.empty(m)
+        depth = np.empty(m, dtype=np.uint32)
+        if m:
+            check(lib().cmn_batch_frontier(self.handle, slot, A.ptr(boxes), A.ptr(lb), A.ptr(depth), m,
+                                           C.byref(cnt)))
+        return boxes, lb, depth
+
+    def release(self, slot: int) -> None:
+        check(lib().cmn_batch_release(self.handle, slot))
+        self.slots.pop(slot, None)
+
+    @property
+    def kernels_per_iteration(self) -> int:
+        return int(lib().cmn_batch_kernels_per_iteration(self.handle))
+
+    @property
+    def stream(self) -> int:
+        return lib().cmn_batch_stream(self.handle) or 0
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().cmn_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def batch_solve(problems, slots: int | None = None, per_instance: list[dict] | None = None, **shared) -> list[dict]:
+    """Solves every problem through cmn_batch_solve with up to `slots`
+    resident at once; returns one outcome dict per problem."""
+    dps = [p if isinstance(p, DeviceProblem) else DeviceProblem(p) for p in problems]
+    count = len(dps)
+    base = batch_options(**{k: v for k, v in shared.items() if k in SHARED_OPTIONS})
+    rest = {k: v for k, v in shared.items() if k not in SHARED_OPTIONS}
+    cfg = A.BatchConfig()
+    cfg.slots = slots or max(1, count)
+    cfg.max_vars = max(dp.n_vars for dp in dps) if dps else 1
+    cfg.max_program_slots = max(int(dp.info()["program_slots"]) for dp in dps) if dps else 0
+    cfg.device = 0
+    cfg.shared = base
+    opts = (A.SolveOptions * max(1, count))()
+    for i in range(count):
+        C.memmove(C.byref(opts[i]), C.byref(base), C.sizeof(base))
+        kw = dict(rest)
+        if per_instance is not None:
+            kw.update(per_instance[i])
+        for k, v in kw.items():
+            if k == "known_primal_bound" and v is not None:
+                opts[i].has_known_primal = 1
+            if v is not None:
+                setattr(opts[i], k, v)
+    handles = (C.c_void_p * max(1, count))(*[dp.handle.value for dp in dps])
+    outs = (A.Outcome * max(1, count))()
+    stride = cfg.max_vars
+    pts = np.full(max(1, count) * stride, np.nan)
+    check(lib().cmn_batch_solve(C.byref(cfg), handles, opts, count, outs, A.ptr(pts), stride))
+    res = []
+    for i, dp in enumerate(dps):
+        d = A.outcome_dict(outs[i])
+        d["best_point"] = pts[i * stride:i * stride + dp.n_vars].copy() if outs[i].found_incumbent else np.array([])
+        res.append(d)
+    return res

@@ -408,6 +408,72 @@ cmn_status cmn_solve(const cmn_problem* problem,
                      const cmn_solve_options* opts, cmn_outcome* outcome,
                      double* best_point);
 
+/* ------------------------------------------------------------------------
+ * Multi-instance batch: many independent problems of uneven sizes advanced
+ * together, one captured graph per iteration over every occupied slot.
+ * No reference counterpart (the reference solves one problem per
+ * SearchDriver, search/driver.hpp:137-537); every instance follows the
+ * batched algorithm of cmn_solver step for step, so its outcome, incumbent
+ * and counters are those cmn_solver gives it with the same options.
+ *
+ * The batch fixes the shared options when it is created: precision,
+ * bisection_budget, batch_parents (parents per instance per iteration),
+ * frontier_cap (pool per instance), sample_points, sample_all,
+ * relative_width, max_cycle_size and enumerate_cap.  Per instance:
+ * iter_limit, batch_iter_limit, tolerance and the known primal bound.
+ * Limits: frontier_cap + batch_parents * 2^bisection_budget <= 8192.
+ * ---------------------------------------------------------------------- */
+typedef struct cmn_batch cmn_batch; /* opaque */
+
+typedef struct {
+  uint64_t slots;            /* instances resident at once */
+  int32_t max_vars;          /* largest n_vars an instance may have */
+  int32_t max_program_slots; /* largest program slot count; -1: as many as
+                                fit (smaller tiles give more resident blocks) */
+  int32_t device;            /* CUDA device of the batch and its problems */
+  int32_t reserved;
+  cmn_solve_options shared;  /* the shared options listed above */
+} cmn_batch_config;
+
+cmn_status cmn_batch_create(const cmn_batch_config* config, cmn_batch** out);
+void cmn_batch_destroy(cmn_batch* batch);
+/* Puts `problem` into a free slot (written to `slot`) with its root box.
+ * `opts` gives the per-instance options; its shared options must equal
+ * the batch's.  CMN_OVER_BUDGET when no slot is free.  The problem must
+ * outlive its slot. */
+cmn_status cmn_batch_add(cmn_batch* batch, const cmn_problem* problem,
+                         const cmn_solve_options* opts, uint64_t* slot);
+/* Runs up to `max_iterations` iterations (0 = until every occupied slot
+ * has stopped); `running` receives the occupied slots still searching. */
+cmn_status cmn_batch_step(cmn_batch* batch, uint64_t max_iterations,
+                          uint64_t* running);
+/* State of `slot` as of the last step: 1 in `done` once it stopped. */
+cmn_status cmn_batch_poll(const cmn_batch* batch, uint64_t slot,
+                          int32_t* done);
+/* Outcome (finalise_bounds, search/epilogue.hpp:89-127) and incumbent of
+ * `slot` (`best_point`: n_vars doubles, NaN when none; may be NULL). */
+cmn_status cmn_batch_outcome(cmn_batch* batch, uint64_t slot,
+                             cmn_outcome* out, double* best_point);
+/* Copies `slot`'s frontier (pool order) as cmn_solver_frontier does. */
+cmn_status cmn_batch_frontier(cmn_batch* batch, uint64_t slot, double* boxes,
+                              double* lower_bounds, uint32_t* depths,
+                              uint64_t room, uint64_t* count);
+/* Frees `slot` for another problem. */
+cmn_status cmn_batch_release(cmn_batch* batch, uint64_t slot);
+/* The CUDA stream the batch runs on (a cudaStream_t). */
+void* cmn_batch_stream(cmn_batch* batch);
+/* Kernel nodes one captured batch iteration launches. */
+uint64_t cmn_batch_kernels_per_iteration(const cmn_batch* batch);
+/* Solves `count` problems with up to `config->slots` resident at once,
+ * refilling slots as instances stop; opts[i] are problem i's options.
+ * outcomes[i] and best_points + i * point_stride (n_vars of problem i;
+ * NULL to skip) receive the results. */
+cmn_status cmn_batch_solve(const cmn_batch_config* config,
+                           const cmn_problem* const* problems,
+                           const cmn_solve_options* opts, uint64_t count,
+                           cmn_outcome* outcomes, double* best_points,
+                           uint64_t point_stride);
+
 #ifdef __cplusplus
 }
 #endif

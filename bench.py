@@ -54,6 +54,11 @@ def parse_args():
     ap.add_argument("--quick", action="store_true",
                     help="solver steps only (no e2e, CPU baseline or time-to-gap): the profiling command")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-batch", action="store_true", help="skip the 1024-instance batch (config 4)")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving stream (config 5)")
+    ap.add_argument("--only", choices=["batch", "serve"], help="run one of the extra workloads alone")
+    ap.add_argument("--instances", type=int, default=1024, help="--only batch: instances in the batch")
+    ap.add_argument("--precision", choices=["fp64", "fp32"], help="--only batch: one form only")
     return ap.parse_args()
 
 
@@ -325,12 +330,90 @@ def time_to_gap(problem, precision, limit_s):
             "upper_bound": o["upper_bound"], "rel_gap": rel, "boxes": o["counters"]["bounded"]}
 
 
+BATCH_OPTS = dict(bisection_budget=4, batch_parents=256, frontier_cap=4096, sample_points=1)
+
+
+def batch_run(rt, precision, steps, warmup, n_inst=1024):
+    """1024 uneven QCQPs (n ~ U{4..48}) in one batch: boxes/s over `steps`
+    iterations, each iteration one captured graph over every instance."""
+    from cuminlp_gb300 import generators as G
+    from cuminlp_gb300.solver import Batch, DeviceProblem
+    dps = [DeviceProblem(G.config4_instance(i)) for i in range(n_inst)]
+    n_max = max(dp.n_vars for dp in dps)
+    slots = max(dp.info()["program_slots"] for dp in dps)
+    b = Batch(n_inst, n_max, slots, precision=precision, **BATCH_OPTS)
+    for dp in dps:
+        b.add(dp, iter_limit=1 << 62)
+    b.launch(warmup)
+    b.sync()
+    c0, _ = b.totals()
+    phases = []
+    for _ in range(steps):  # device time of each captured iteration, from its own phase events
+        b.launch(1)
+        phases.append(b.phase_ms())
+    ms = sum(p[4] for p in phases)
+    c1, running = b.totals()
+    kpi = b.kernels_per_iteration
+    b.close()
+    d = {k: c1[k] - c0[k] for k in c1}
+    return {"ms": ms, "boxes": d["bounded"], "value": d["bounded"] / (ms * 1e-3), "running_after": running,
+            "certified_fp64": d["certified_fp64"], "screened_fp32": d["screened_fp32"], "kernels_per_iter": kpi,
+            "n_max": n_max, "instances": n_inst,
+            "phases_ms": [round(sum(p[i] for p in phases) / len(phases), 3) for i in range(5)]}
+
+
+SERVE_CLASSES = [(8, 512), (16, 512), (32, 256), (64, 128)]
+SERVE_OPTS = dict(bisection_budget=4, batch_parents=256, frontier_cap=4096, sample_points=1,
+                  precision="fp32")
+SERVE_BUDGET = 120 * (1 << 30)
+
+
+def serving_run(rate, n_requests, dps, seed=11, iter_limit=256 * 40):
+    """Poisson arrivals at `rate` per second of the n in {8,16,32,64} mix;
+    requests cycle through the pre-built problems `dps`."""
+    import numpy as np
+    from cuminlp_gb300.solver import Server
+    slots = max(dp.info()["program_slots"] for dp in dps)
+    srv = Server([(v, k, slots) for v, k in SERVE_CLASSES], pool_budget_bytes=SERVE_BUDGET,
+                 iterations_per_round=2, **SERVE_OPTS)
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n_requests))
+    ids = []
+    t0 = time.perf_counter()
+    for i in range(n_requests):
+        now = time.perf_counter() - t0
+        if arrivals[i] > now:
+            time.sleep(arrivals[i] - now)
+        ids.append(srv.submit(dps[i % len(dps)], iter_limit=iter_limit, tolerance=1e-6))
+    outs = [srv.wait(r, timeout_ms=600000) for r in ids]
+    st = srv.stats()
+    srv.close()
+    conv = [o["elapsed_ms"] for o in outs if o["stop_reason"] == "converged"]
+    conv.sort()
+    pick = (lambda q: conv[min(len(conv) - 1, max(0, int(np.ceil(q * len(conv))) - 1))]) if conv else (lambda q: None)
+    return {"rate_per_s": rate, "requests": n_requests, "latency_p50_ms": st["latency_p50_ms"],
+            "latency_p99_ms": st["latency_p99_ms"], "latency_max_ms": st["latency_max_ms"],
+            "queue_p99_ms": st["queue_p99_ms"], "converged": st["converged"],
+            "time_to_gap_p50_ms": pick(0.5), "time_to_gap_p99_ms": pick(0.99),
+            "boxes_per_s": st["boxes_per_s"], "wall_ms": st["wall_ms"],
+            "pool_bytes_peak": st["pool_bytes_peak"], "rounds": st["rounds"]}
+
+
 def run_ours(args):
     world, rank, local, dist = dist_setup(args)
     from cuminlp_gb300 import generators as G
     from cuminlp_gb300.solver import DeviceProblem
     rt = Cudart()
     rt.set_device(local)
+    if args.only == "batch":
+        precs = ("fp64", "fp32") if args.precision is None else (args.precision,)
+        print(json.dumps({p: batch_run(rt, p, args.steps, args.warmup, args.instances) for p in precs}))
+        return
+    if args.only == "serve":
+        from cuminlp_gb300.solver import DeviceProblem
+        dps = [DeviceProblem(G.config5_request(i)) for i in range(400)]
+        print(json.dumps([serving_run(r, n, dps) for r, n in ((100, 300), (1000, 1500), (10000, 6000))]))
+        return
     problem = G.config2(rank)  # replicas: one independent instance per GPU
     dp = DeviceProblem(problem)
     info = dp.info()
@@ -387,6 +470,23 @@ def run_ours(args):
         ttg = {"config": "n=4 QCQP (config 1), gap 1e-6, 20 s cap each",
                "fp64": time_to_gap(p1, "fp64", 20.0), "fp32_screen_fp64_certify": time_to_gap(p1, "fp32", 20.0)}
 
+    batch = None
+    if not args.no_batch:
+        bres = {p: batch_run(rt, p, args.steps * 4, args.warmup) for p in ("fp64", "fp32")}
+        batch = {"workload": "config4: 1024 uneven QCQPs, n ~ U{4..48}, m ~ U{0..24}, 0-25% integers; "
+                             "256 parents x 2^4 children per instance per step; pool cap 4096 per instance",
+                 "fp32_screen": bres["fp32"], "plain_fp64": bres["fp64"],
+                 "screen_speedup_vs_plain_fp64": bres["fp32"]["value"] / bres["fp64"]["value"]}
+    serving = None
+    if not args.no_serve:
+        from cuminlp_gb300 import generators as G
+        from cuminlp_gb300.solver import DeviceProblem
+        dps = [DeviceProblem(G.config5_request(i)) for i in range(400)]
+        serving = {"workload": "config5: Poisson arrivals, n in {8,16,32,64} (0.4/0.3/0.2/0.1), m = n/2, "
+                               "10% integers; FP32 screen + FP64 certify; per-request limit 256*40 expansions, "
+                               "gap 1e-6; size classes " + str(SERVE_CLASSES) + "; 120 GiB box-pool admission cap",
+                   "runs": [serving_run(r, n, dps) for r, n in ((100, 300), (1000, 1500), (10000, 6000))]}
+
     kpi = screen["kernels_per_iter"]
     line = {
         "metric": "boxes/s (batched interval B&B box evaluations, FP32 screen + FP64 certify)",
@@ -440,6 +540,8 @@ def run_ours(args):
         "gpu_launches": kpi * args.steps,
         "clocks": clocks,
         "time_to_gap": ttg,
+        "batch_uneven": batch,
+        "serving": serving,
     }
     print(json.dumps(line))
     barrier(dist)

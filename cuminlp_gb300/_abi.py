@@ -90,6 +90,25 @@ class BatchConfig(C.Structure):
                 ("device", C.c_int32), ("reserved", C.c_int32), ("shared", SolveOptions)]
 
 
+SERVER_MAX_CLASSES = 8
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("shared", SolveOptions), ("device", C.c_int32), ("n_classes", C.c_int32),
+                ("class_max_vars", C.c_int32 * SERVER_MAX_CLASSES),
+                ("class_max_program_slots", C.c_int32 * SERVER_MAX_CLASSES),
+                ("class_slots", C.c_uint64 * SERVER_MAX_CLASSES), ("pool_budget_bytes", C.c_uint64),
+                ("iterations_per_round", C.c_uint64)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in ("submitted", "admitted", "completed", "queued", "running", "converged",
+                                          "boxes", "rounds", "pool_bytes_in_use", "pool_bytes_peak",
+                                          "pool_budget_bytes")] + \
+               [(n, C.c_double) for n in ("latency_p50_ms", "latency_p99_ms", "latency_mean_ms", "latency_max_ms",
+                                          "queue_p50_ms", "queue_p99_ms", "wall_ms", "boxes_per_s")]
+
+
 COUNTER_NAMES = ["iterations", "expansions", "fathomed", "fathomed_points", "bounded", "sampled", "enqueued",
                  "witness_rejected", "pruned_duplicate", "pruned_infeasible", "pruned_dominated",
                  "dropped_viable", "dropped_dominated", "screened_fp32", "certified_fp64", "peak_frontier"]

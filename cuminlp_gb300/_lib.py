@@ -63,6 +63,17 @@ SIGNATURES = {
     "cmn_batch_stream": (P, [P]),
     "cmn_batch_kernels_per_iteration": (U64, [P]),
     "cmn_batch_solve": (I32, [C.POINTER(A.BatchConfig), P, P, U64, P, P, U64]),
+    "cmn_batch_launch": (I32, [P, U64]),
+    "cmn_batch_sync": (I32, [P, C.POINTER(U64)]),
+    "cmn_batch_slot_bytes": (U64, [P]),
+    "cmn_batch_phase_ms": (I32, [P, C.POINTER(D)]),
+    "cmn_batch_totals": (I32, [P, C.POINTER(A.Counters), C.POINTER(U64)]),
+    "cmn_server_create": (I32, [C.POINTER(A.ServerConfig), PP]),
+    "cmn_server_destroy": (None, [P]),
+    "cmn_server_submit": (I32, [P, P, C.POINTER(A.SolveOptions), C.POINTER(U64)]),
+    "cmn_server_poll": (I32, [P, U64, C.POINTER(I32), C.POINTER(A.Outcome), P]),
+    "cmn_server_wait": (I32, [P, U64, U64, C.POINTER(A.Outcome), P]),
+    "cmn_server_stats_get": (I32, [P, C.POINTER(A.ServerStats)]),
 }
 
 

@@ -30,7 +30,7 @@ NVCC_FLAGS = [
     "--expt-relaxed-constexpr", "-DNDEBUG",
 ]
 SOURCES = ["program.cpp", "eval_kernels.cu", "search_kernels.cu", "batch_kernels.cu", "capi.cu", "batch.cu",
-           "noalloc.cu"]
+           "server.cpp", "noalloc.cu"]
 
 
 def _nvcc() -> str:
@@ -71,7 +71,7 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
         for fut in [ex.submit(_run, j) for j in jobs]:
             fut.result()
     if force or jobs or _stale(LIB, objs):
-        _run([nvcc, ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart"])
+        _run([nvcc, ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart", "-lpthread"])
     if verbose:
         print(f"built {LIB}")
     return LIB

@@ -73,14 +73,19 @@ struct cmn_batch {
   std::vector<Clock::time_point> t_add;
   std::vector<double> elapsed_ms;  // add -> first step that saw it stopped
   std::vector<void*> allocs;
+  uint64_t alloc_bytes = 0;
+  bool fresh = false;  // h_st matches the device: nothing enqueued since pull()
   int eval_grid = 1;
   uint64_t kernels_per_iter = 0;
+  cudaEvent_t marks[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
 
   ~cmn_batch()
   {
     int cur = 0;
     if (cudaGetDevice(&cur) == cudaSuccess && cur != device) cudaSetDevice(device);
     if (stream) cudaStreamSynchronize(stream);
+    for (cudaEvent_t ev : marks)
+      if (ev) cudaEventDestroy(ev);
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
     for (void* a : allocs) cudaFree(a);
@@ -93,8 +98,12 @@ struct cmn_batch {
   cudaError_t alloc(T** ptr, size_t n)
   {
     *ptr = nullptr;
-    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(ptr), std::max<size_t>(n, 1) * sizeof(T));
-    if (e == cudaSuccess) allocs.push_back(*ptr);
+    const size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(ptr), bytes);
+    if (e == cudaSuccess) {
+      allocs.push_back(*ptr);
+      alloc_bytes += bytes;
+    }
     return e;
   }
 
@@ -106,6 +115,7 @@ struct cmn_batch {
     for (uint64_t i = 0; i < cfg.K; ++i)
       if (busy[i] && h_st[i].done && elapsed_ms[i] < 0)
         elapsed_ms[i] = std::chrono::duration<double, std::milli>(now - t_add[i]).count();
+    fresh = true;
     return CMN_OK;
   }
 
@@ -233,9 +243,10 @@ extern "C" cmn_status cmn_batch_create(const cmn_batch_config* config, cmn_batch
     const int occ = std::max(1, std::min(batch_eval_occupancy(c, fp32), batch_sample_occupancy(c)));
     const uint64_t need = (G + kEvalThreads - 1) / kEvalThreads;
     s->eval_grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(need, (uint64_t)sm_count() * occ));
+    for (int i = 0; i < 5 && e == cudaSuccess; ++i) e = cudaEventCreate(&s->marks[i]);
     if (e == cudaSuccess) e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-      cudaError_t e2 = batch_iteration(c, b, s->eval_grid, s->stream);
+      cudaError_t e2 = batch_iteration(c, b, s->eval_grid, s->stream, s->marks);
       e = cudaStreamEndCapture(s->stream, &s->graph);
       if (e2 != cudaSuccess) e = e2;
     }
@@ -306,6 +317,7 @@ extern "C" cmn_status cmn_batch_add(cmn_batch* s, const cmn_problem* p, const cm
   s->opts[k] = *opts;
   s->busy[k] = 1;
   s->h_st[k].done = 0;
+  s->fresh = false;
   s->t_add[k] = Clock::now();
   s->elapsed_ms[k] = -1.0;
   *slot = k;
@@ -323,6 +335,7 @@ extern "C" cmn_status cmn_batch_step(cmn_batch* s, uint64_t max_iterations, uint
   while (s->running() > 0 && (max_iterations == 0 || done_iters < max_iterations)) {
     uint64_t k = burst;
     if (max_iterations) k = std::min<uint64_t>(k, max_iterations - done_iters);
+    s->fresh = false;
     for (uint64_t i = 0; i < k; ++i) BCK(cudaGraphLaunch(s->exec, s->stream));
     done_iters += k;
     st = s->pull();
@@ -332,6 +345,67 @@ extern "C" cmn_status cmn_batch_step(cmn_batch* s, uint64_t max_iterations, uint
   }
   if (running) *running = s->running();
   return CMN_OK;
+}
+
+extern "C" cmn_status cmn_batch_launch(cmn_batch* s, uint64_t iterations)
+{
+  if (!s) return fail(CMN_INVALID_CONFIGURATION, "null batch");
+  BCK(cudaSetDevice(s->device));
+  s->fresh = false;
+  for (uint64_t i = 0; i < iterations; ++i) BCK(cudaGraphLaunch(s->exec, s->stream));
+  return CMN_OK;
+}
+
+extern "C" cmn_status cmn_batch_sync(cmn_batch* s, uint64_t* running)
+{
+  if (!s) return fail(CMN_INVALID_CONFIGURATION, "null batch");
+  BCK(cudaSetDevice(s->device));
+  cmn_status st = s->pull();
+  if (st != CMN_OK) return st;
+  if (running) *running = s->running();
+  return CMN_OK;
+}
+
+extern "C" cmn_status cmn_batch_totals(cmn_batch* s, cmn_counters* sum, uint64_t* running)
+{
+  if (!s || !sum) return fail(CMN_INVALID_CONFIGURATION, "null argument");
+  BCK(cudaSetDevice(s->device));
+  cmn_status st = s->fresh ? CMN_OK : s->pull();
+  if (st != CMN_OK) return st;
+  uint64_t acc[16] = {0};
+  static_assert(sizeof(cmn_counters) == sizeof(acc), "cmn_counters is 16 uint64");
+  for (uint64_t k = 0; k < s->cfg.K; ++k) {
+    if (!s->busy[k]) continue;
+    cmn_counters c = s->h_st[k].counters;
+    c.iterations = s->h_st[k].iterations;
+    c.expansions = s->h_st[k].expansions;
+    uint64_t v[16];
+    std::memcpy(v, &c, sizeof v);
+    for (int i = 0; i < 16; ++i) acc[i] += v[i];
+  }
+  std::memcpy(sum, acc, sizeof acc);
+  if (running) *running = s->running();
+  return CMN_OK;
+}
+
+extern "C" cmn_status cmn_batch_phase_ms(cmn_batch* s, double* ms5)
+{
+  if (!s || !ms5) return fail(CMN_INVALID_CONFIGURATION, "null argument");
+  BCK(cudaSetDevice(s->device));
+  BCK(cudaEventSynchronize(s->marks[4]));
+  float t = 0;
+  for (int i = 0; i < 4; ++i) {
+    BCK(cudaEventElapsedTime(&t, s->marks[i], s->marks[i + 1]));
+    ms5[i] = t;
+  }
+  BCK(cudaEventElapsedTime(&t, s->marks[0], s->marks[4]));
+  ms5[4] = t;
+  return CMN_OK;
+}
+
+extern "C" uint64_t cmn_batch_slot_bytes(const cmn_batch* s)
+{
+  return s && s->cfg.K ? (s->alloc_bytes + s->cfg.K - 1) / s->cfg.K : 0;
 }
 
 extern "C" cmn_status cmn_batch_poll(const cmn_batch* s, uint64_t slot, int32_t* done)
@@ -347,7 +421,7 @@ extern "C" cmn_status cmn_batch_outcome(cmn_batch* s, uint64_t slot, cmn_outcome
   if (!s || !out) return fail(CMN_INVALID_CONFIGURATION, "null argument");
   if (slot >= s->cfg.K || !s->busy[slot]) return fail(CMN_INVALID_CONFIGURATION, "slot not occupied");
   BCK(cudaSetDevice(s->device));
-  cmn_status st = s->pull();
+  cmn_status st = s->fresh ? CMN_OK : s->pull();
   if (st != CMN_OK) return st;
   const InstState& d = s->h_st[slot];
   const double tol = s->opts[slot].tolerance;
@@ -405,7 +479,7 @@ extern "C" cmn_status cmn_batch_frontier(cmn_batch* s, uint64_t slot, double* bo
   if (!s || !count) return fail(CMN_INVALID_CONFIGURATION, "null argument");
   if (slot >= s->cfg.K || !s->busy[slot]) return fail(CMN_INVALID_CONFIGURATION, "slot not occupied");
   BCK(cudaSetDevice(s->device));
-  cmn_status st = s->pull();
+  cmn_status st = s->fresh ? CMN_OK : s->pull();
   if (st != CMN_OK) return st;
   const uint64_t L = s->h_st[slot].pool_size;
   *count = L;

@@ -105,7 +105,10 @@ struct BatchBufs {
 // Puts `slot`'s root box in its pool and resets its state.
 cudaError_t batch_init_slot(const BatchCfg& cfg, const BatchBufs& b, uint64_t slot, double gub0, cudaStream_t s);
 // Enqueues one iteration over every active instance (capturable).
-cudaError_t batch_iteration(const BatchCfg& cfg, const BatchBufs& b, int eval_grid, cudaStream_t s);
+// `marks` (5 events or null) are recorded at the phase boundaries: start,
+// after select + branch, after bound, after sample, after finish.
+cudaError_t batch_iteration(const BatchCfg& cfg, const BatchBufs& b, int eval_grid, cudaStream_t s,
+                            const cudaEvent_t* marks);
 size_t batch_eval_smem(const BatchCfg& cfg, bool fp32);
 size_t batch_sample_smem(const BatchCfg& cfg);
 // resident blocks per SM of the bound (fp32: screen) and sample kernels

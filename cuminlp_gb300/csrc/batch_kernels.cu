@@ -806,13 +806,21 @@ cudaError_t batch_init_slot(const BatchCfg& c, const BatchBufs& b, uint64_t slot
   return cudaGetLastError();
 }
 
-cudaError_t batch_iteration(const BatchCfg& c, const BatchBufs& b, int eval_grid, cudaStream_t s)
+static void mark(const cudaEvent_t* marks, int i, cudaStream_t s)
 {
+  if (marks) cudaEventRecordWithFlags(marks[i], s, cudaEventRecordExternal);
+}
+
+cudaError_t batch_iteration(const BatchCfg& c, const BatchBufs& b, int eval_grid, cudaStream_t s,
+                            const cudaEvent_t* marks)
+{
+  mark(marks, 0, s);
   const int kb = (int)((c.K + 255) / 256);
   batch_begin_kernel<<<kb, 256, 0, s>>>(c, b);
   batch_select_kernel<<<(int)c.K, kMiThreads, sort_smem_bytes(), s>>>(c, b);
   const uint64_t np = c.K * c.e_max;
   batch_branch_kernel<<<(int)((np + 127) / 128), 128, 0, s>>>(c, b);
+  mark(marks, 1, s);
   const bool fp32 = c.precision == CMN_PRECISION_FP32_SCREEN;
   if (fp32) {
     batch_eval_kernel<float, 2><<<eval_grid, kEvalThreads, batch_eval_smem(c, true), s>>>(c, b);
@@ -824,8 +832,11 @@ cudaError_t batch_iteration(const BatchCfg& c, const BatchBufs& b, int eval_grid
   } else {
     batch_eval_kernel<double, 1><<<eval_grid, kEvalThreads, batch_eval_smem(c, false), s>>>(c, b);
   }
+  mark(marks, 2, s);
   batch_sample_kernel<<<eval_grid, kEvalThreads, batch_sample_smem(c), s>>>(c, b);
+  mark(marks, 3, s);
   batch_finish_kernel<<<(int)c.K, kMiThreads, sort_smem_bytes(), s>>>(c, b);
+  mark(marks, 4, s);
   return cudaGetLastError();
 }
 

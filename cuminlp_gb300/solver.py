@@ -328,6 +328,28 @@ class Batch:
         check(lib().cmn_batch_step(self.handle, int(max_iterations), C.byref(running)))
         return running.value
 
+    def launch(self, iterations: int) -> None:
+        """Enqueues iterations without waiting (see sync)."""
+        check(lib().cmn_batch_launch(self.handle, int(iterations)))
+
+    def sync(self) -> int:
+        running = C.c_uint64()
+        check(lib().cmn_batch_sync(self.handle, C.byref(running)))
+        return running.value
+
+    def phase_ms(self) -> list[float]:
+        """[select+branch, bound, sample, finish, whole] of the last iteration."""
+        ms = (C.c_double * 5)()
+        check(lib().cmn_batch_phase_ms(self.handle, ms))
+        return list(ms)
+
+    def totals(self) -> tuple[dict, int]:
+        """(counters summed over the occupied slots, slots still searching)."""
+        c = A.Counters()
+        running = C.c_uint64()
+        check(lib().cmn_batch_totals(self.handle, C.byref(c), C.byref(running)))
+        return {n: int(getattr(c, n)) for n in A.COUNTER_NAMES}, running.value
+
     def done(self, slot: int) -> bool:
         d = C.c_int32()
         check(lib().cmn_batch_poll(self.handle, slot, C.byref(d)))
@@ -414,3 +436,80 @@ def batch_solve(problems, slots: int | None = None, per_instance: list[dict] | N
         d["best_point"] = pts[i * stride:i * stride + dp.n_vars].copy() if outs[i].found_incumbent else np.array([])
         res.append(d)
     return res
+
+
+class Server:
+    """Continuous-batching request loop (cmn_server_*): one batch per size
+    class, requests admitted into free slots within a box-pool memory cap."""
+
+    def __init__(self, classes, pool_budget_bytes: int = 0, iterations_per_round: int = 4, device: int = 0,
+                 **shared):
+        """`classes`: [(max_vars, slots)] or [(max_vars, slots, max_program_slots)], ascending in max_vars."""
+        self.options = batch_options(**shared)
+        cfg = A.ServerConfig()
+        cfg.shared = self.options
+        cfg.device = device
+        cfg.n_classes = len(classes)
+        for i, c in enumerate(classes):
+            cfg.class_max_vars[i] = c[0]
+            cfg.class_slots[i] = c[1]
+            cfg.class_max_program_slots[i] = c[2] if len(c) > 2 else 0
+        cfg.pool_budget_bytes = pool_budget_bytes
+        cfg.iterations_per_round = iterations_per_round
+        h = C.c_void_p()
+        check(lib().cmn_server_create(C.byref(cfg), C.byref(h)))
+        self.handle = h
+        self._n = {}
+        self._keep = {}
+
+    def submit(self, dp: DeviceProblem, **options) -> int:
+        o = A.SolveOptions()
+        C.memmove(C.byref(o), C.byref(self.options), C.sizeof(o))
+        for k, v in options.items():
+            if k in SHARED_OPTIONS:
+                raise TypeError(f"{k} is fixed by the server")
+            if k == "known_primal_bound" and v is not None:
+                o.has_known_primal = 1
+            if v is not None:
+                setattr(o, k, v)
+        rid = C.c_uint64()
+        check(lib().cmn_server_submit(self.handle, dp.handle, C.byref(o), C.byref(rid)))
+        self._n[rid.value] = dp.n_vars
+        self._keep[rid.value] = dp
+        return rid.value
+
+    def _result(self, rid, o, pt):
+        d = A.outcome_dict(o)
+        d["best_point"] = pt if o.found_incumbent else np.array([])
+        self._keep.pop(rid, None)
+        return d
+
+    def poll(self, rid: int):
+        """The outcome dict once the request finished, else None."""
+        o = A.Outcome()
+        pt = np.empty(self._n[rid])
+        done = C.c_int32()
+        check(lib().cmn_server_poll(self.handle, rid, C.byref(done), C.byref(o), A.ptr(pt)))
+        return self._result(rid, o, pt) if done.value else None
+
+    def wait(self, rid: int, timeout_ms: int = 0) -> dict:
+        o = A.Outcome()
+        pt = np.empty(self._n[rid])
+        check(lib().cmn_server_wait(self.handle, rid, timeout_ms, C.byref(o), A.ptr(pt)))
+        return self._result(rid, o, pt)
+
+    def stats(self) -> dict:
+        s = A.ServerStats()
+        check(lib().cmn_server_stats_get(self.handle, C.byref(s)))
+        return {f: getattr(s, f) for f, _ in A.ServerStats._fields_}
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().cmn_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -447,6 +447,20 @@ cmn_status cmn_batch_add(cmn_batch* batch, const cmn_problem* problem,
  * has stopped); `running` receives the occupied slots still searching. */
 cmn_status cmn_batch_step(cmn_batch* batch, uint64_t max_iterations,
                           uint64_t* running);
+/* The two halves of cmn_batch_step, for callers that overlap several
+ * batches: enqueue `iterations` iterations without waiting, then wait for
+ * them and refresh the per-slot state (`running` as in cmn_batch_step). */
+cmn_status cmn_batch_launch(cmn_batch* batch, uint64_t iterations);
+cmn_status cmn_batch_sync(cmn_batch* batch, uint64_t* running);
+/* Sum of the counters of every occupied slot (as of the device's current
+ * state) and the number of occupied slots still searching. */
+cmn_status cmn_batch_totals(cmn_batch* batch, cmn_counters* sum,
+                            uint64_t* running);
+/* Phase timings of the most recent batch iteration, as
+ * cmn_solver_phase_ms reports them. */
+cmn_status cmn_batch_phase_ms(cmn_batch* batch, double* ms5);
+/* Device bytes one slot's box pool and work buffers take. */
+uint64_t cmn_batch_slot_bytes(const cmn_batch* batch);
 /* State of `slot` as of the last step: 1 in `done` once it stopped. */
 cmn_status cmn_batch_poll(const cmn_batch* batch, uint64_t slot,
                           int32_t* done);
@@ -473,6 +487,68 @@ cmn_status cmn_batch_solve(const cmn_batch_config* config,
                            const cmn_solve_options* opts, uint64_t count,
                            cmn_outcome* outcomes, double* best_points,
                            uint64_t point_stride);
+
+/* ------------------------------------------------------------------------
+ * Serving: a request loop with continuous batching.  No reference
+ * counterpart.  A worker thread owns one cmn_batch per size class (each
+ * on its own stream, so the classes' iterations overlap on the device);
+ * between rounds of `iterations_per_round` iterations it admits queued
+ * requests into free slots of the smallest class that holds them, while the
+ * resident box pools stay within `pool_budget_bytes`, and retires the
+ * requests that stopped.  A request's result does not depend on the other
+ * requests or on its class: it is what cmn_batch (and cmn_solver) give
+ * it alone with the same options.
+ * ---------------------------------------------------------------------- */
+typedef struct cmn_server cmn_server; /* opaque */
+
+#define CMN_SERVER_MAX_CLASSES 8
+
+typedef struct {
+  cmn_solve_options shared;  /* as cmn_batch_config.shared */
+  int32_t device;
+  int32_t n_classes;                                /* 1..8 */
+  int32_t class_max_vars[CMN_SERVER_MAX_CLASSES];   /* ascending */
+  int32_t class_max_program_slots[CMN_SERVER_MAX_CLASSES];
+  uint64_t class_slots[CMN_SERVER_MAX_CLASSES];
+  uint64_t pool_budget_bytes;     /* cap on admitted slots' bytes; 0: none */
+  uint64_t iterations_per_round;  /* iterations between admissions; 0: 4 */
+} cmn_server_config;
+
+typedef struct {
+  uint64_t submitted, admitted, completed, queued, running;
+  uint64_t converged;          /* completed requests that closed the gap */
+  uint64_t boxes;              /* child boxes bounded for completed requests */
+  uint64_t rounds;             /* admission rounds of the worker */
+  uint64_t pool_bytes_in_use, pool_bytes_peak, pool_budget_bytes;
+  double latency_p50_ms, latency_p99_ms, latency_mean_ms, latency_max_ms;
+  double queue_p50_ms, queue_p99_ms;  /* submit -> admission */
+  double wall_ms;              /* first submit -> last completion */
+  double boxes_per_s;          /* boxes / wall_ms */
+} cmn_server_stats;
+
+cmn_status cmn_server_create(const cmn_server_config* config,
+                             cmn_server** out);
+/* Stops the worker (running requests are abandoned) and frees everything. */
+void cmn_server_destroy(cmn_server* server);
+/* Queues a solve of `problem` (which must outlive the request).  `opts`
+ * shared options must equal the server's; CMN_INVALID_CONFIGURATION when
+ * no class takes the problem. */
+cmn_status cmn_server_submit(cmn_server* server, const cmn_problem* problem,
+                             const cmn_solve_options* opts,
+                             uint64_t* request_id);
+/* Non-blocking: `done` is 1 once the request finished; then `out` (its
+ * elapsed_ms is submit -> completion) and `best_point` (may be NULL) are
+ * filled. */
+cmn_status cmn_server_poll(cmn_server* server, uint64_t request_id,
+                           int32_t* done, cmn_outcome* out,
+                           double* best_point);
+/* Blocks until the request finished or `timeout_ms` passed (0: no limit;
+ * CMN_TIMEOUT then). */
+cmn_status cmn_server_wait(cmn_server* server, uint64_t request_id,
+                           uint64_t timeout_ms, cmn_outcome* out,
+                           double* best_point);
+/* Latency percentiles and throughput over the completed requests. */
+cmn_status cmn_server_stats_get(cmn_server* server, cmn_server_stats* out);
 
 #ifdef __cplusplus
 }

@@ -158,9 +158,10 @@ extern "C" cmn_status cmn_batch_create(const cmn_batch_config* config, cmn_batch
     const int max_smem = max_dynamic_smem();
     const bool fp32 = o.precision == CMN_PRECISION_FP32_SCREEN;
     const int64_t n_max = cf.max_vars;
-    // program slots that fit beside n_max variables in the FP64 bound tile
-    // (the certify pass of the FP32 form is FP64 too) and the sample tile
-    const int64_t fit_eval = (int64_t)max_smem / (8 * 2 * kEvalThreads) - n_max;
+    // program slots that fit beside the split variables in the FP64 bound
+    // tile (the certify pass of the FP32 form is FP64 too) and beside
+    // n_max variables in the sample tile
+    const int64_t fit_eval = ((int64_t)max_smem / kEvalThreads - 20 * (int64_t)o.bisection_budget) / 16;
     const int64_t fit_smp = (int64_t)max_smem / (8 * kEvalThreads) - n_max;
     const int64_t fit = std::min(fit_eval, fit_smp);
     if (fit < 0) return fail(CMN_INVALID_CONFIGURATION, "max_vars too large for the evaluator's shared-memory tile");
@@ -203,6 +204,10 @@ extern "C" cmn_status cmn_batch_create(const cmn_batch_config* config, cmn_batch
     A(&b.depth, K * c.P);
     A(&b.plo, K * nm * c.e_max);
     A(&b.phi, K * nm * c.e_max);
+    if (fp32) {
+      A(&b.plo32, K * nm * c.e_max);
+      A(&b.phi32, K * nm * c.e_max);
+    }
     A(&b.pdepth, K * c.e_max);
     A(&b.pinfo, K * c.e_max);
     A(&b.slots, K * c.e_max * (uint64_t)c.max_slots);

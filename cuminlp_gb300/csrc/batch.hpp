@@ -85,6 +85,8 @@ struct BatchBufs {
   uint32_t* depth;
   double* plo;  // [K][n_max][e_max]
   double* phi;
+  float* plo32;  // FP32 screen only: the same planes rounded outward
+  float* phi32;
   uint32_t* pdepth;  // [K][e_max]
   ParentInfo* pinfo;
   SlotPlan* slots;  // [K][e_max][B]

@@ -266,8 +266,13 @@ __global__ void __launch_bounds__(kMiThreads) batch_select_kernel(const BatchCfg
     if (f) {
       const uint32_t k = running + (uint32_t)r;
       for (int v = 0; v < n; ++v) {
-        b.plo[splane(c, slot, v) + k] = b.lo[plane(c, slot, v) + i];
-        b.phi[splane(c, slot, v) + k] = b.hi[plane(c, slot, v) + i];
+        const double lo = b.lo[plane(c, slot, v) + i], hi = b.hi[plane(c, slot, v) + i];
+        b.plo[splane(c, slot, v) + k] = lo;
+        b.phi[splane(c, slot, v) + k] = hi;
+        if (b.plo32 != nullptr) {
+          b.plo32[splane(c, slot, v) + k] = __double2float_rd(lo);
+          b.phi32[splane(c, slot, v) + k] = __double2float_ru(hi);
+        }
       }
       b.pdepth[slot * c.e_max + k] = b.depth[(size_t)slot * c.P + i];
     }
@@ -311,33 +316,35 @@ __global__ void batch_branch_kernel(const BatchCfg c, const BatchBufs b)
   }
 }
 
-template <typename T>
-__device__ __forceinline__ T bconv_lo(double x);
-template <typename T>
-__device__ __forceinline__ T bconv_hi(double x);
-template <>
-__device__ __forceinline__ double bconv_lo<double>(double x) { return x; }
-template <>
-__device__ __forceinline__ double bconv_hi<double>(double x) { return x; }
-template <>
-__device__ __forceinline__ float bconv_lo<float>(double x) { return __double2float_rd(x); }
-template <>
-__device__ __forceinline__ float bconv_hi<float>(double x) { return __double2float_ru(x); }
-
-// kMode 1: FP64 bound; 2: FP32 screen; 3: FP64 certify of the listed children
+// kMode 1: FP64 bound; 2: FP32 screen; 3: FP64 certify of the listed children.
+// Variables come from the parent planes (FP32 copies for the screen) with
+// the child's split variables in this thread's shared-memory column.
 template <typename T, int kMode>
 __global__ void __launch_bounds__(kEvalThreads) batch_eval_kernel(const BatchCfg c, const BatchBufs b)
 {
+  using S = T;  // the screen reads the FP32 planes, the FP64 passes the FP64 planes
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* base = reinterpret_cast<T*>(smem_raw);
   const int B = blockDim.x;
-  Tile<T> t;
-  t.lo = base;
-  t.hi = base + (size_t)c.n_max * B;
-  t.slo = base + (size_t)2 * c.n_max * B;
-  t.shi = base + (size_t)(2 * c.n_max + c.slots_max) * B;
+  Tile<T> t;  // program slots only
+  t.lo = nullptr;
+  t.hi = nullptr;
+  t.slo = base;
+  t.shi = base + (size_t)c.slots_max * B;
   t.stride = B;
   t.tid = threadIdx.x;
+  T* olo = base + (size_t)2 * c.slots_max * B + threadIdx.x;
+  T* ohi = olo + (size_t)c.max_slots * B;
+  int32_t* ovid = reinterpret_cast<int32_t*>(base + (size_t)2 * (c.slots_max + c.max_slots) * B) + threadIdx.x;
+  const S* planes_lo;
+  const S* planes_hi;
+  if constexpr (sizeof(T) == 4) {
+    planes_lo = b.plo32;
+    planes_hi = b.phi32;
+  } else {
+    planes_lo = b.plo;
+    planes_hi = b.phi;
+  }
   const uint64_t total = kMode == 3 ? *b.list_count : c.K * c.child_stride;
   for (uint64_t idx = (uint64_t)blockIdx.x * B + threadIdx.x; idx < total; idx += (uint64_t)gridDim.x * B) {
     const uint64_t g = kMode == 3 ? (uint64_t)b.list[idx] : idx;
@@ -358,12 +365,16 @@ __global__ void __launch_bounds__(kEvalThreads) batch_eval_kernel(const BatchCfg
       b.cstate[g] = dup ? kChildDuplicate : kChildScreened;
       continue;
     }
-    const InstDesc& d = b.desc[slot];
-    const int n = d.n_vars;
-    for (int v = 0; v < n; ++v) {
-      t.lo[v * B + t.tid] = bconv_lo<T>(b.plo[splane(c, slot, v) + k]);
-      t.hi[v * B + t.tid] = bconv_hi<T>(b.phi[splane(c, slot, v) + k]);
-    }
+    ChildVars<T, S> cv;
+    cv.plo = planes_lo + splane(c, slot, 0) + k;
+    cv.phi = planes_hi + splane(c, slot, 0) + k;
+    cv.pstride = c.e_max;
+    cv.mask = 0;
+    cv.olo = olo;
+    cv.ohi = ohi;
+    cv.ovid = ovid;
+    cv.count = (int)pi.count;
+    cv.stride = B;
     bool dup = false;
     for (uint32_t j = 0; j < pi.count; ++j) {
       const SlotPlan s = sp[j];
@@ -372,15 +383,18 @@ __global__ void __launch_bounds__(kEvalThreads) batch_eval_kernel(const BatchCfg
       double lo, hi;
       slot_bounds((int)s.kind, b.plo[splane(c, slot, s.vid) + k], b.phi[splane(c, slot, s.vid) + k], part, s.width,
                   lo, hi);
-      t.lo[s.vid * B + t.tid] = bconv_lo<T>(lo);
-      t.hi[s.vid * B + t.tid] = bconv_hi<T>(hi);
+      olo[j * B] = Widen<T, double>::lo(lo);
+      ohi[j * B] = Widen<T, double>::hi(hi);
+      ovid[j * B] = (int32_t)s.vid;
+      cv.mask |= 1ULL << (s.vid & 63);
     }
     if (dup) {
       b.cstate[g] = kChildDuplicate;
       continue;
     }
+    const InstDesc& d = b.desc[slot];
     const Instr* prog = sizeof(T) == 4 ? d.prog32 : d.prog64;
-    const Verdict<T> v = run_interval<T>(prog, d.prog_len, t);
+    const Verdict<T> v = run_interval<T, ChildVars<T, S>>(prog, d.prog_len, cv, t);
     const double lb = (double)v.obj.lo;
     const double gub = st->gub;
     b.clb[g] = lb;
@@ -759,7 +773,7 @@ __global__ void __launch_bounds__(512) batch_list_scatter_kernel(const BatchCfg 
 // ---------------------------------------------------------------------
 size_t batch_eval_smem(const BatchCfg& c, bool fp32)
 {
-  return (fp32 ? 4 : 8) * (size_t)(2 * c.n_max + 2 * c.slots_max) * kEvalThreads;
+  return ((fp32 ? 8 : 16) * (size_t)(c.slots_max + c.max_slots) + 4 * (size_t)c.max_slots) * kEvalThreads;
 }
 
 size_t batch_sample_smem(const BatchCfg& c) { return 8 * (size_t)(c.n_max + c.slots_max) * kEvalThreads; }

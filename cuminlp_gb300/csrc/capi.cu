@@ -193,11 +193,12 @@ static cmn_status check_interval(const cmn_problem* p)
   return CMN_OK;
 }
 
-static cmn_status check_smem(const cmn_problem* p, bool fp32)
+static cmn_status check_smem(const cmn_problem* p, bool fp32, int max_slots)
 {
-  const size_t need = eval_smem_bytes((int)p->host.n_vars(), p->prog.n_slots, fp32, kEvalThreads);
+  const size_t need = eval_smem_bytes(p->prog.n_slots, max_slots, fp32, kEvalThreads);
   if ((int64_t)need > (int64_t)max_dynamic_smem())
-    return fail(CMN_INVALID_CONFIGURATION, "the problem's variables and program slots need " + std::to_string(need) +
+    return fail(CMN_INVALID_CONFIGURATION, "the problem's program slots and split variables need " +
+                                               std::to_string(need) +
                                                " B of shared memory per block; the device offers " +
                                                std::to_string(max_dynamic_smem()));
   return CMN_OK;
@@ -291,7 +292,7 @@ extern "C" cmn_status cmn_role_build(const cmn_problem* p, int32_t role, const u
   }
   cmn_status st = check_interval(p);
   if (st != CMN_OK && role == CMN_ROLE_BOUNDER) return st;
-  st = check_smem(p, false);
+  st = check_smem(p, false, (int)slot_count);
   if (st != CMN_OK) return st;
   try {
     if (cudaSetDevice(p->device) != cudaSuccess) return fail(CMN_CUDA_ERROR, "cudaSetDevice failed");
@@ -334,7 +335,8 @@ extern "C" cmn_status cmn_role_build(const cmn_problem* p, int32_t role, const u
     if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&r->h_stage), r->stage_bytes);
     const int threads = kEvalThreads;
     const uint64_t blocks_needed = (n_regions + threads - 1) / threads;
-    const int occ = std::max(1, eval_kernel_occupancy(0, false, eval_smem_bytes((int)n, p->prog.n_slots, false, threads), threads));
+    const int occ = std::max(
+        1, eval_kernel_occupancy(0, false, eval_smem_bytes(p->prog.n_slots, (int)slot_count, false, threads), threads));
     r->grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(blocks_needed, (uint64_t)sm_count() * occ));
     if (role == CMN_ROLE_BOUNDER) {
       if (e == cudaSuccess) e = dalloc(&r->d_feas, n_regions);
@@ -436,7 +438,7 @@ extern "C" cmn_status cmn_bound(cmn_role* r, const double* box, const uint64_t* 
   a.pstride = 1;
   a.pinfo = pi;
   a.slots = sp;
-  a.max_slots = 64;
+  a.max_slots = (int)r->slot_kinds.size();  // one parent: the stride of the slot table is unused
   a.n_children = r->n_regions;
   a.out_lb = r->d_lb;
   a.out_flag = r->d_feas;
@@ -530,7 +532,7 @@ extern "C" cmn_status cmn_eval_boxes(const cmn_problem* p, int32_t precision, co
   cmn_status st = check_interval(p);
   if (st != CMN_OK) return st;
   const bool fp32 = precision == CMN_PRECISION_FP32_SCREEN;
-  st = check_smem(p, fp32);
+  st = check_smem(p, fp32, 0);
   if (st != CMN_OK) return st;
   CK(cudaSetDevice(p->device));
   CK(ensure_attributes());
@@ -573,7 +575,8 @@ extern "C" cmn_status cmn_eval_boxes(const cmn_problem* p, int32_t precision, co
   a.out_ub = dub;
   a.out_flag = dfe;
   const int threads = kEvalThreads;
-  const int occ = std::max(1, eval_kernel_occupancy(0, fp32, eval_smem_bytes((int)n, p->prog.n_slots, fp32, threads), threads));
+  const int occ =
+      std::max(1, eval_kernel_occupancy(0, fp32, eval_smem_bytes(p->prog.n_slots, 0, fp32, threads), threads));
   const uint64_t need = (n_boxes + threads - 1) / threads;
   const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(need, (uint64_t)sm_count() * occ));
   cudaError_t e = launch_eval(a, 0, fp32, grid, threads, s);
@@ -681,7 +684,7 @@ extern "C" cmn_status cmn_solver_create(const cmn_problem* p, const cmn_solve_op
   if (o.frontier_cap > (1ull << 31)) return fail(CMN_INVALID_CONFIGURATION, "frontier_cap above 2^31");
   cmn_status st = check_interval(p);
   if (st != CMN_OK) return st;
-  st = check_smem(p, o.precision == CMN_PRECISION_FP32_SCREEN);
+  st = check_smem(p, o.precision == CMN_PRECISION_FP32_SCREEN, o.bisection_budget);
   if (st != CMN_OK) return st;
   if (sample_smem_bytes((int)p->host.n_vars(), p->prog.n_slots, kEvalThreads) > (size_t)max_dynamic_smem())
     return fail(CMN_INVALID_CONFIGURATION, "problem too large for the sampler's shared-memory tile");
@@ -714,7 +717,7 @@ extern "C" cmn_status cmn_solver_create(const cmn_problem* p, const cmn_solve_op
     const int threads = kEvalThreads;
     const bool fp32 = o.precision == CMN_PRECISION_FP32_SCREEN;
     const int occ_e = std::max(1, eval_kernel_occupancy(fp32 ? 2 : 1, fp32,
-                                                        eval_smem_bytes(n, p->prog.n_slots, fp32, threads), threads));
+                                                        eval_smem_bytes(p->prog.n_slots, cfg.max_slots, fp32, threads), threads));
     const int occ_s = std::max(1, sample_kernel_occupancy(sample_smem_bytes(n, p->prog.n_slots, threads), threads));
     const uint64_t need = (maxc + threads - 1) / threads;
     s->eval_grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(need, (uint64_t)sm_count() * occ_e));
@@ -736,6 +739,10 @@ extern "C" cmn_status cmn_solver_create(const cmn_problem* p, const cmn_solve_op
     A(&b.sel, cfg.pstride);
     A(&b.plo, (size_t)n * cfg.e_max);
     A(&b.phi, (size_t)n * cfg.e_max);
+    if (fp32) {
+      A(&b.plo32, (size_t)n * cfg.e_max);
+      A(&b.phi32, (size_t)n * cfg.e_max);
+    }
     A(&b.pdepth, cfg.e_max);
     A(&b.pinfo, cfg.e_max);
     A(&b.slots, cfg.e_max * (size_t)cfg.max_slots);

@@ -308,6 +308,47 @@ struct Tile {
   }
 };
 
+// Bound of storage type S as an interval endpoint of type T: identity, or
+// FP64 -> FP32 rounded outward.
+template <typename T, typename S>
+struct Widen {
+  __device__ static __forceinline__ T lo(S x) { return x; }
+  __device__ static __forceinline__ T hi(S x) { return x; }
+};
+template <>
+struct Widen<float, double> {
+  __device__ static __forceinline__ float lo(double x) { return __double2float_rd(x); }
+  __device__ static __forceinline__ float hi(double x) { return __double2float_ru(x); }
+};
+
+// The variables of one child box without a per-thread copy of the box: a
+// variable is read from the parent's planes in global memory (siblings read
+// the same addresses, so the loads hit L1), unless it is one of the child's
+// split variables, whose narrowed bounds sit in this thread's shared-memory
+// column.  `mask` has bit (v & 63) set for every split variable v, so an
+// unsplit variable costs one test.
+template <typename T, typename S>
+struct ChildVars {
+  const S* plo;  // the parent's bound of variable v at plo[v * pstride]
+  const S* phi;
+  uint64_t pstride;
+  uint64_t mask;
+  const T* olo;  // split slot j of this thread at olo[j * stride]
+  const T* ohi;
+  const int32_t* ovid;
+  int count;
+  int stride;
+  __device__ __forceinline__ Iv<T> var(int v) const
+  {
+    if ((mask >> (v & 63)) & 1ULL) {
+      for (int j = 0; j < count; ++j)
+        if (ovid[j * stride] == v) return {olo[j * stride], ohi[j * stride]};
+    }
+    const uint64_t off = (uint64_t)v * pstride;
+    return {Widen<T, S>::lo(__ldg(plo + off)), Widen<T, S>::hi(__ldg(phi + off))};
+  }
+};
+
 __device__ __forceinline__ Instr load_instr(const Instr* prog, int pc)
 {
   int4 raw = __ldg(reinterpret_cast<const int4*>(prog) + pc);
@@ -331,12 +372,13 @@ __device__ __forceinline__ Iv<float> const_of<float>(const Instr& ins)
   return {ins.c32.clo, ins.c32.chi};
 }
 
-template <typename T>
-__device__ __forceinline__ Iv<T> fetch(const Tile<T>& t, const Iv<T>& acc, const Instr& ins, int mode, int idx)
+template <typename T, typename V>
+__device__ __forceinline__ Iv<T> fetch(const V& vars, const Tile<T>& t, const Iv<T>& acc, const Instr& ins, int mode,
+                                       int idx)
 {
   switch (mode) {
     case kModeSlot: return t.slot(idx);
-    case kModeVar: return t.var(idx);
+    case kModeVar: return vars.var(idx);
     case kModeAcc: return acc;
     default: return const_of<T>(ins);
   }
@@ -350,9 +392,10 @@ struct Verdict {
   bool excluded;    // a constraint is proven violated (NaN never excludes)
 };
 
-// Interval interpretation of `prog` for this thread's box.
-template <typename T>
-__device__ Verdict<T> run_interval(const Instr* __restrict__ prog, int len, const Tile<T>& t)
+// Interval interpretation of `prog` for this thread's box: variables from
+// `vars` (anything with var(v) -> Iv<T>), program slots in `t`.
+template <typename T, typename V>
+__device__ Verdict<T> run_interval(const Instr* __restrict__ prog, int len, const V& vars, const Tile<T>& t)
 {
   using A = Arith<T>;
   Iv<T> acc = {T(0), T(0)};
@@ -371,11 +414,11 @@ __device__ Verdict<T> run_interval(const Instr* __restrict__ prog, int len, cons
         Iv<T> p;
         const int pk = sub & kTermPMask;
         if (pk == kTermProd) {
-          p = iv_mul(t.var(cur.a), t.var(cur.b));
+          p = iv_mul(vars.var(cur.a), vars.var(cur.b));
         } else if (pk == kTermSqr) {
-          p = iv_sqr(t.var(cur.a));
+          p = iv_sqr(vars.var(cur.a));
         } else {
-          p = t.var(cur.a);
+          p = vars.var(cur.a);
         }
         if (sub & kTermHasC) p = iv_mul(const_of<T>(cur), p);
         if (sub & kTermInit) acc = p;
@@ -384,8 +427,8 @@ __device__ Verdict<T> run_interval(const Instr* __restrict__ prog, int len, cons
         break;
       }
       case kOpGeneric: {
-        const Iv<T> a = fetch(t, acc, cur, cur.modes & 3, cur.a);
-        const Iv<T> b = fetch(t, acc, cur, (cur.modes >> 2) & 3, cur.b);
+        const Iv<T> a = fetch(vars, t, acc, cur, cur.modes & 3, cur.a);
+        const Iv<T> b = fetch(vars, t, acc, cur, (cur.modes >> 2) & 3, cur.b);
         t.set_slot(cur.dst, iv_generic<T>((uint8_t)sub, a, b, (int)(int16_t)cur.b));
         break;
       }
@@ -393,13 +436,13 @@ __device__ Verdict<T> run_interval(const Instr* __restrict__ prog, int len, cons
         t.set_slot(cur.dst, acc);
         break;
       case kOpLoadAcc:
-        acc = fetch(t, acc, cur, cur.modes & 3, cur.a);
+        acc = fetch(vars, t, acc, cur, cur.modes & 3, cur.a);
         break;
       case kOpConstToSlot:
         t.set_slot(cur.dst, const_of<T>(cur));
         break;
       case kOpCheck: {
-        const Iv<T> v = fetch(t, acc, cur, cur.modes & 3, cur.a);
+        const Iv<T> v = fetch(vars, t, acc, cur, cur.modes & 3, cur.a);
         // rhs is kept in FP64 for both precisions; compare in FP64 exactly
         const double rhs = cur.c;
         const double lo = (double)v.lo, hi = (double)v.hi;
@@ -413,13 +456,20 @@ __device__ Verdict<T> run_interval(const Instr* __restrict__ prog, int len, cons
         break;
       }
       case kOpObjective:
-        out.obj = fetch(t, acc, cur, cur.modes & 3, cur.a);
+        out.obj = fetch(vars, t, acc, cur, cur.modes & 3, cur.a);
         break;
       default:
         break;
     }
   }
   return out;
+}
+
+// Variables held in the tile's own planes.
+template <typename T>
+__device__ Verdict<T> run_interval(const Instr* __restrict__ prog, int len, const Tile<T>& t)
+{
+  return run_interval<T, Tile<T>>(prog, len, t, t);
 }
 
 // Point interpretation (FP64 round-to-nearest) for this thread's point,

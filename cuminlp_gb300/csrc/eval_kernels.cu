@@ -1,11 +1,16 @@
 // eval_kernels.cu -- the fused interval evaluator (a), the point sampler
 // (b) and the incumbent ArgMin, over children decoded from parent boxes.
 //
-// One thread owns one child box.  Its variable intervals and program slots
-// live in shared memory laid out plane-major ([plane][thread]), so every
-// access of a warp is one conflict-free row.  Nothing is shared between
-// threads, so the kernels need no barriers and a thread whose child is
-// invalid simply skips the program.
+// One thread owns one child box.  The interval kernels keep no copy of the
+// box: a variable is read from the parent's planes (the siblings of a
+// parent read the same addresses, so those loads hit L1), except the
+// child's few split variables, which sit in the thread's shared-memory
+// column beside its program slots.  Shared memory per thread is then
+// independent of the number of variables, which keeps enough warps resident
+// to saturate the FP64 pipe.  The sampler stages each point in shared
+// memory, plane-major ([plane][thread]) so every warp access is one
+// conflict-free row.  Nothing is shared between threads, so the kernels
+// need no barriers and a thread whose child is invalid simply skips it.
 //
 // Replaces graph/kernels.cuh:76-461 (broadcast/apply root kernels, one op
 // kernel per DAG node, feasibility, extract, mask, gather) and the CUB
@@ -19,19 +24,6 @@
 
 namespace cmn {
 
-template <typename T>
-__device__ __forceinline__ T conv_lo(double x);
-template <typename T>
-__device__ __forceinline__ T conv_hi(double x);
-template <>
-__device__ __forceinline__ double conv_lo<double>(double x) { return x; }
-template <>
-__device__ __forceinline__ double conv_hi<double>(double x) { return x; }
-template <>
-__device__ __forceinline__ float conv_lo<float>(double x) { return __double2float_rd(x); }
-template <>
-__device__ __forceinline__ float conv_hi<float>(double x) { return __double2float_ru(x); }
-
 __device__ __forceinline__ void child_of(int log2C, uint64_t g, uint64_t& k, uint64_t& r)
 {
   if (log2C < 0) {
@@ -43,18 +35,27 @@ __device__ __forceinline__ void child_of(int log2C, uint64_t g, uint64_t& k, uin
   }
 }
 
-// Decodes child (k, r) into this thread's tile column; returns false when
-// the child is a duplicate (a slot digit at or past its domain size).
-template <typename T>
-__device__ __forceinline__ bool load_child(const EvalArgs& a, const Tile<T>& t, uint64_t k, uint64_t r)
+// The variable source of child (k, r): the parent's planes `plo`/`phi`
+// (FP64, or FP32 rounded outward) plus the child's split variables, decoded
+// from the parent's FP64 bounds into this thread's columns olo/ohi/ovid.
+// `dup` is set when a slot digit is at or past its domain size
+// (region::is_duplicate_child).
+template <typename T, typename S>
+__device__ __forceinline__ ChildVars<T, S> child_vars(const EvalArgs& a, const S* plo, const S* phi, uint64_t k,
+                                                      uint64_t r, T* olo, T* ohi, int32_t* ovid, int stride,
+                                                      bool& dup)
 {
-  for (int v = 0; v < a.n_vars; ++v) {
-    const double lo = a.plo[(uint64_t)v * a.pstride + k];
-    const double hi = a.phi[(uint64_t)v * a.pstride + k];
-    t.lo[v * t.stride + t.tid] = conv_lo<T>(lo);
-    t.hi[v * t.stride + t.tid] = conv_hi<T>(hi);
-  }
-  bool dup = false;
+  ChildVars<T, S> cv;
+  cv.plo = plo + k;
+  cv.phi = phi + k;
+  cv.pstride = a.pstride;
+  cv.mask = 0;
+  cv.olo = olo;
+  cv.ohi = ohi;
+  cv.ovid = ovid;
+  cv.count = 0;
+  cv.stride = stride;
+  dup = false;
   if (a.pinfo != nullptr) {
     const uint32_t count = a.pinfo[k].count;
     const SlotPlan* sp = a.slots + k * (uint64_t)a.max_slots;
@@ -62,34 +63,48 @@ __device__ __forceinline__ bool load_child(const EvalArgs& a, const Tile<T>& t, 
       const SlotPlan s = sp[j];
       const uint64_t part = (r / s.prefix) % s.width;
       if (part >= s.dom) dup = true;
-      const double plo = a.plo[(uint64_t)s.vid * a.pstride + k];
-      const double phi = a.phi[(uint64_t)s.vid * a.pstride + k];
       double lo, hi;
-      slot_bounds((int)s.kind, plo, phi, part, s.width, lo, hi);
-      t.lo[s.vid * t.stride + t.tid] = conv_lo<T>(lo);
-      t.hi[s.vid * t.stride + t.tid] = conv_hi<T>(hi);
+      slot_bounds((int)s.kind, a.plo[(uint64_t)s.vid * a.pstride + k], a.phi[(uint64_t)s.vid * a.pstride + k], part,
+                  s.width, lo, hi);
+      olo[j * stride] = Widen<T, double>::lo(lo);
+      ohi[j * stride] = Widen<T, double>::hi(hi);
+      ovid[j * stride] = (int32_t)s.vid;
+      cv.mask |= 1ULL << (s.vid & 63);
     }
+    cv.count = (int)count;
   }
-  return !dup;
+  return cv;
+}
+
+// Shared memory of the interval kernels, per thread: the program slots
+// (lo, hi) and up to `max_slots` split variables (lo, hi, id).
+size_t eval_smem_bytes(int n_slots, int max_slots, bool fp32, int threads)
+{
+  const size_t t = fp32 ? 4 : 8;
+  return ((2 * t) * (size_t)(n_slots + max_slots) + 4 * (size_t)max_slots) * (size_t)threads;
 }
 
 // kMode 0: role / raw boxes -> out_lb, out_ub, out_flag = feasible
 // kMode 1: solver FP64 -> out_lb, out_flag = ChildState
 // kMode 2: solver FP32 screen -> out_lb (FP32 bound), out_flag = ChildState
 // kMode 3: solver FP64 certify of a child list
-template <typename T, int kMode>
-__global__ void __launch_bounds__(kEvalThreads) eval_children_kernel(const EvalArgs a)
+template <typename T, int kMode, typename S>
+__device__ __forceinline__ void eval_children(const EvalArgs& a, const S* plo, const S* phi)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* base = reinterpret_cast<T*>(smem_raw);
   const int B = blockDim.x;
-  Tile<T> t;
-  t.lo = base;
-  t.hi = base + (size_t)a.n_vars * B;
-  t.slo = base + (size_t)2 * a.n_vars * B;
-  t.shi = base + (size_t)(2 * a.n_vars + a.n_slots) * B;
+  const int ms = a.pinfo != nullptr ? a.max_slots : 0;
+  Tile<T> t;  // program slots only
+  t.lo = nullptr;
+  t.hi = nullptr;
+  t.slo = base;
+  t.shi = base + (size_t)a.n_slots * B;
   t.stride = B;
   t.tid = threadIdx.x;
+  T* olo = base + (size_t)2 * a.n_slots * B + threadIdx.x;
+  T* ohi = olo + (size_t)ms * B;
+  int32_t* ovid = reinterpret_cast<int32_t*>(base + (size_t)2 * (a.n_slots + ms) * B) + threadIdx.x;
 
   if (a.done != nullptr && *a.done) return;
   uint64_t total;
@@ -119,12 +134,13 @@ __global__ void __launch_bounds__(kEvalThreads) eval_children_kernel(const EvalA
       a.out_flag[g] = dup ? kChildDuplicate : kChildScreened;
       continue;
     }
-    const bool unique = load_child<T>(a, t, k, r);
-    if (kMode != 0 && !unique) {
+    bool dup;
+    const ChildVars<T, S> cv = child_vars<T, S>(a, plo, phi, k, r, olo, ohi, ovid, B, dup);
+    if (kMode != 0 && dup) {
       a.out_flag[g] = kChildDuplicate;
       continue;
     }
-    const Verdict<T> v = run_interval<T>(a.prog, a.prog_len, t);
+    const Verdict<T> v = run_interval<T, ChildVars<T, S>>(a.prog, a.prog_len, cv, t);
     const double lb = (double)v.obj.lo;
     if (kMode == 0) {
       a.out_lb[g] = lb;
@@ -139,6 +155,18 @@ __global__ void __launch_bounds__(kEvalThreads) eval_children_kernel(const EvalA
       a.out_flag[g] = !v.feasible ? kChildInfeasible : (lb > gub ? kChildDominated : kChildEligible);
     }
   }
+}
+
+template <typename T, int kMode>
+__global__ void __launch_bounds__(kEvalThreads) eval_children_kernel(const EvalArgs a)
+{
+  if constexpr (sizeof(T) == 4) {
+    if (a.plo32 != nullptr) {
+      eval_children<T, kMode, float>(a, a.plo32, a.phi32);
+      return;
+    }
+  }
+  eval_children<T, kMode, double>(a, a.plo, a.phi);
 }
 
 __device__ __forceinline__ void warp_min_cand(Cand& c)
@@ -345,11 +373,6 @@ cudaError_t launch_fma_peak(int precision, int grid, int threads, int iters, voi
 // ---------------------------------------------------------------------
 // host launchers
 // ---------------------------------------------------------------------
-size_t eval_smem_bytes(int n_vars, int n_slots, bool fp32, int threads)
-{
-  const size_t es = fp32 ? 4 : 8;
-  return es * (size_t)(2 * n_vars + 2 * n_slots) * threads;
-}
 
 size_t sample_smem_bytes(int n_vars, int n_slots, int threads)
 {
@@ -407,7 +430,7 @@ int sample_kernel_occupancy(size_t smem, int threads)
 template <typename T, int kMode>
 static cudaError_t launch_eval_t(const EvalArgs& a, int grid, int threads, cudaStream_t s)
 {
-  const size_t smem = eval_smem_bytes(a.n_vars, a.n_slots, sizeof(T) == 4, threads);
+  const size_t smem = eval_smem_bytes(a.n_slots, a.pinfo != nullptr ? a.max_slots : 0, sizeof(T) == 4, threads);
   eval_children_kernel<T, kMode><<<grid, threads, smem, s>>>(a);
   return cudaGetLastError();
 }

@@ -59,6 +59,8 @@ struct EvalArgs {
   int log2C;             // children per parent = 2^log2C; -1: all children belong to parent 0
   const double* plo;     // parent planes: variable v of parent k at [v * pstride + k]
   const double* phi;
+  const float* plo32;    // optional FP32 copies (rounded outward) read by the FP32 screen
+  const float* phi32;
   uint64_t pstride;
   const ParentInfo* pinfo;  // null: every parent has no slots, one child
   const SlotPlan* slots;    // [k * max_slots + j]

@@ -12,7 +12,8 @@ namespace cmn {
 
 constexpr int kEvalThreads = 128;
 
-size_t eval_smem_bytes(int n_vars, int n_slots, bool fp32, int threads);
+// interval kernels: program slots plus `max_slots` split variables per thread
+size_t eval_smem_bytes(int n_slots, int max_slots, bool fp32, int threads);
 size_t sample_smem_bytes(int n_vars, int n_slots, int threads);
 
 // mode 0: role / raw boxes; 1: solver FP64; 2: solver FP32 screen (fp32

@@ -91,6 +91,8 @@ struct SolverBufs {
   // staging of this iteration's parents: planes [v * e_max + k]
   double* plo;
   double* phi;
+  float* plo32;  // FP32 screen only: the same planes rounded outward
+  float* phi32;
   uint32_t* pdepth;
   ParentInfo* pinfo;
   SlotPlan* slots;

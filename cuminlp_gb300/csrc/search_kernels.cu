@@ -339,8 +339,14 @@ struct GatherParents {
       return;
     }
     for (int v = 0; v < cfg.n_vars; ++v) {
-      b.plo[(uint64_t)v * cfg.e_max + pos] = b.lo[p][(uint64_t)v * cfg.pstride + i];
-      b.phi[(uint64_t)v * cfg.e_max + pos] = b.hi[p][(uint64_t)v * cfg.pstride + i];
+      const double lo = b.lo[p][(uint64_t)v * cfg.pstride + i];
+      const double hi = b.hi[p][(uint64_t)v * cfg.pstride + i];
+      b.plo[(uint64_t)v * cfg.e_max + pos] = lo;
+      b.phi[(uint64_t)v * cfg.e_max + pos] = hi;
+      if (b.plo32 != nullptr) {
+        b.plo32[(uint64_t)v * cfg.e_max + pos] = __double2float_rd(lo);
+        b.phi32[(uint64_t)v * cfg.e_max + pos] = __double2float_ru(hi);
+      }
     }
     b.pdepth[pos] = b.depth[p][i];
   }
@@ -728,6 +734,8 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
   cudaError_t e;
   if (cfg.precision == CMN_PRECISION_FP32_SCREEN) {
     ea.prog = b.prog32;
+    ea.plo32 = b.plo32;
+    ea.phi32 = b.phi32;
     ea.use_screen = &b.dev->use_screen;
     e = launch_eval(ea, 2, true, eval_grid, kEvalThreads, s);
     if (e != cudaSuccess) return e;
@@ -736,6 +744,8 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
     scatter(sc, ListChild{b}, max_children, s, b);
     EvalArgs ca = ea;
     ca.prog = b.prog64;
+    ca.plo32 = nullptr;
+    ca.phi32 = nullptr;
     ca.list = b.list;
     ca.list_count = &b.dev->certify_count;
     e = launch_eval(ca, 3, false, eval_grid, kEvalThreads, s);

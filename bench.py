@@ -362,13 +362,22 @@ def batch_run(rt, precision, steps, warmup, n_inst=1024):
             "phases_ms": [round(sum(p[i] for p in phases) / len(phases), 3) for i in range(5)]}
 
 
-SERVE_CLASSES = [(8, 512), (16, 512), (32, 256), (64, 128)]
-SERVE_OPTS = dict(bisection_budget=4, batch_parents=256, frontier_cap=4096, sample_points=1,
+SERVE_CLASSES = [(8, 1024), (16, 1024), (32, 512), (64, 256)]
+SERVE_OPTS = dict(bisection_budget=4, batch_parents=64, frontier_cap=2048, sample_points=1,
                   precision="fp32")
 SERVE_BUDGET = 120 * (1 << 30)
+SERVE_ITER_LIMIT = 64 * 32  # expansions per request: at most 32 full iterations
+SERVE_RUNS = ((100, 300), (1000, 1500), (10000, 6000))  # (arrivals per second, requests)
 
 
-def serving_run(rate, n_requests, dps, seed=11, iter_limit=256 * 40):
+def serving_workload() -> str:
+    return ("config5: Poisson arrivals, n in {8,16,32,64} (0.4/0.3/0.2/0.1), m = n/2, 10% integers; FP32 screen + "
+            f"FP64 certify; 64 parents x 2^4 children per request per iteration, per-request limit "
+            f"{SERVE_ITER_LIMIT} expansions, gap 1e-6; size classes (max_vars, slots) {SERVE_CLASSES}; "
+            "120 GiB box-pool admission cap; requests cycle through 400 pre-built problems")
+
+
+def serving_run(rate, n_requests, dps, seed=11, iter_limit=SERVE_ITER_LIMIT):
     """Poisson arrivals at `rate` per second of the n in {8,16,32,64} mix;
     requests cycle through the pre-built problems `dps`."""
     import numpy as np
@@ -412,7 +421,7 @@ def run_ours(args):
     if args.only == "serve":
         from cuminlp_gb300.solver import DeviceProblem
         dps = [DeviceProblem(G.config5_request(i)) for i in range(400)]
-        print(json.dumps([serving_run(r, n, dps) for r, n in ((100, 300), (1000, 1500), (10000, 6000))]))
+        print(json.dumps({"workload": serving_workload(), "runs": [serving_run(r, n, dps) for r, n in SERVE_RUNS]}))
         return
     problem = G.config2(rank)  # replicas: one independent instance per GPU
     dp = DeviceProblem(problem)
@@ -482,10 +491,7 @@ def run_ours(args):
         from cuminlp_gb300 import generators as G
         from cuminlp_gb300.solver import DeviceProblem
         dps = [DeviceProblem(G.config5_request(i)) for i in range(400)]
-        serving = {"workload": "config5: Poisson arrivals, n in {8,16,32,64} (0.4/0.3/0.2/0.1), m = n/2, "
-                               "10% integers; FP32 screen + FP64 certify; per-request limit 256*40 expansions, "
-                               "gap 1e-6; size classes " + str(SERVE_CLASSES) + "; 120 GiB box-pool admission cap",
-                   "runs": [serving_run(r, n, dps) for r, n in ((100, 300), (1000, 1500), (10000, 6000))]}
+        serving = {"workload": serving_workload(), "runs": [serving_run(r, n, dps) for r, n in SERVE_RUNS]}
 
     kpi = screen["kernels_per_iter"]
     line = {

@@ -65,6 +65,7 @@ SIGNATURES = {
     "cmn_batch_solve": (I32, [C.POINTER(A.BatchConfig), P, P, U64, P, P, U64]),
     "cmn_batch_launch": (I32, [P, U64]),
     "cmn_batch_sync": (I32, [P, C.POINTER(U64)]),
+    "cmn_batch_query": (I32, [P, C.POINTER(I32)]),
     "cmn_batch_slot_bytes": (U64, [P]),
     "cmn_batch_phase_ms": (I32, [P, C.POINTER(D)]),
     "cmn_batch_totals": (I32, [P, C.POINTER(A.Counters), C.POINTER(U64)]),

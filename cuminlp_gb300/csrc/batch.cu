@@ -361,6 +361,20 @@ extern "C" cmn_status cmn_batch_launch(cmn_batch* s, uint64_t iterations)
   return CMN_OK;
 }
 
+extern "C" cmn_status cmn_batch_query(cmn_batch* s, int32_t* idle)
+{
+  if (!s || !idle) return fail(CMN_INVALID_CONFIGURATION, "null argument");
+  BCK(cudaSetDevice(s->device));
+  const cudaError_t e = cudaStreamQuery(s->stream);
+  if (e == cudaErrorNotReady) {
+    *idle = 0;
+    return CMN_OK;
+  }
+  BCK(e);
+  *idle = 1;
+  return CMN_OK;
+}
+
 extern "C" cmn_status cmn_batch_sync(cmn_batch* s, uint64_t* running)
 {
   if (!s) return fail(CMN_INVALID_CONFIGURATION, "null batch");

@@ -1,6 +1,7 @@
 // server.cpp -- cmn_server_*: continuous batching of solve requests over
-// one cmn_batch per size class.  The worker thread is the only user of the
-// batches; submitters touch the request table under the mutex only.
+// one cmn_batch per size class, each class on its own stream and cadence.
+// The worker thread is the only user of the batches; submitters touch the
+// request table under the mutex only.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -166,68 +167,84 @@ struct cmn_server {
     }
   }
 
-  void retire_locked()
+  // Retires the stopped requests of class c (its state freshly pulled).
+  void retire_class_locked(int c)
   {
-    for (int c = 0; c < conf.n_classes; ++c) {
-      if (!occupied[c]) continue;
-      for (uint64_t k = 0; k < owner[c].size(); ++k) {
-        const uint64_t id = owner[c][k];
-        if (id == ~0ULL) continue;
-        int32_t done = 0;
-        if (cmn_batch_poll(batches[c], k, &done) != CMN_OK || !done) continue;
-        Request& r = reqs[id];
-        r.point.assign((size_t)r.n_vars, 0.0);
-        cmn_status st = cmn_batch_outcome(batches[c], k, &r.out, r.point.data());
-        if (st == CMN_OK) st = cmn_batch_release(batches[c], k);
-        if (st != CMN_OK) {
-          set_fatal(st, "retiring a request");
-          return;
-        }
-        r.t_done = Clock::now();
-        r.out.elapsed_ms = ms_between(r.t_submit, r.t_done);
-        r.state = kDone;
-        owner[c][k] = ~0ULL;
-        --occupied[c];
-        in_use -= slot_bytes[c];
-        ++completed;
-        if (r.out.stop_reason == CMN_STOP_CONVERGED) ++converged;
-        boxes += r.out.counters.bounded;
-        latencies.push_back(r.out.elapsed_ms);
-        t_last_done = r.t_done;
+    for (uint64_t k = 0; k < owner[c].size() && occupied[c]; ++k) {
+      const uint64_t id = owner[c][k];
+      if (id == ~0ULL) continue;
+      int32_t done = 0;
+      if (cmn_batch_poll(batches[c], k, &done) != CMN_OK || !done) continue;
+      Request& r = reqs[id];
+      r.point.assign((size_t)r.n_vars, 0.0);
+      cmn_status st = cmn_batch_outcome(batches[c], k, &r.out, r.point.data());
+      if (st == CMN_OK) st = cmn_batch_release(batches[c], k);
+      if (st != CMN_OK) {
+        set_fatal(st, "retiring a request");
+        return;
       }
+      r.t_done = Clock::now();
+      r.out.elapsed_ms = ms_between(r.t_submit, r.t_done);
+      r.state = kDone;
+      owner[c][k] = ~0ULL;
+      --occupied[c];
+      in_use -= slot_bytes[c];
+      ++completed;
+      if (r.out.stop_reason == CMN_STOP_CONVERGED) ++converged;
+      boxes += r.out.counters.bounded;
+      latencies.push_back(r.out.elapsed_ms);
+      t_last_done = r.t_done;
     }
     cv_done.notify_all();
   }
 
+  // Each class runs on its own: as soon as a class's iterations finish, its
+  // stopped requests retire, queued requests are admitted and the class
+  // launches again, without waiting for the other classes.
   void run()
   {
     const uint64_t ipr = conf.iterations_per_round ? conf.iterations_per_round : 4;
-    std::vector<int> active(conf.n_classes, 0);
+    std::vector<int> inflight(conf.n_classes, 0);
     for (;;) {
       {
         std::unique_lock<std::mutex> lk(mu);
         if (stop || fatal != CMN_OK) return;
         admit_locked();
-        if (running_total() == 0) {
+        bool busy = false;
+        for (int c = 0; c < conf.n_classes; ++c) busy = busy || inflight[c] || occupied[c] > 0;
+        if (!busy) {
           cv_work.wait_for(lk, std::chrono::milliseconds(2), [&] { return stop || !queue.empty(); });
           continue;
         }
-        for (int c = 0; c < conf.n_classes; ++c) active[c] = occupied[c] > 0;
       }
-      // every class with work launches, then every class waits: the
-      // classes' streams overlap on the device
+      // only the worker changes `occupied`, so it reads it without the lock
       cmn_status st = CMN_OK;
-      for (int c = 0; c < conf.n_classes && st == CMN_OK; ++c)
-        if (active[c]) st = cmn_batch_launch(batches[c], ipr);
-      for (int c = 0; c < conf.n_classes && st == CMN_OK; ++c)
-        if (active[c]) st = cmn_batch_sync(batches[c], nullptr);
-      std::lock_guard<std::mutex> lk(mu);
+      for (int c = 0; c < conf.n_classes && st == CMN_OK; ++c) {
+        if (inflight[c] || occupied[c] == 0) continue;
+        st = cmn_batch_launch(batches[c], ipr);
+        inflight[c] = 1;
+      }
+      bool progressed = false;
+      for (int c = 0; c < conf.n_classes && st == CMN_OK; ++c) {
+        if (!inflight[c]) continue;
+        int32_t idle = 0;
+        st = cmn_batch_query(batches[c], &idle);
+        if (st != CMN_OK || !idle) continue;
+        st = cmn_batch_sync(batches[c], nullptr);
+        if (st != CMN_OK) break;
+        inflight[c] = 0;
+        progressed = true;
+        std::lock_guard<std::mutex> lk(mu);
+        ++rounds;
+        retire_class_locked(c);
+        if (fatal != CMN_OK) return;
+      }
       if (st != CMN_OK) {
-        set_fatal(st, "running a round");
+        std::lock_guard<std::mutex> lk(mu);
+        set_fatal(st, "running the classes");
         return;
       }
-      ++rounds;
-      retire_locked();
+      if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(50));
     }
   }
 };

@@ -452,6 +452,8 @@ cmn_status cmn_batch_step(cmn_batch* batch, uint64_t max_iterations,
  * them and refresh the per-slot state (`running` as in cmn_batch_step). */
 cmn_status cmn_batch_launch(cmn_batch* batch, uint64_t iterations);
 cmn_status cmn_batch_sync(cmn_batch* batch, uint64_t* running);
+/* Non-blocking: 1 in `idle` when every launched iteration has finished. */
+cmn_status cmn_batch_query(cmn_batch* batch, int32_t* idle);
 /* Sum of the counters of every occupied slot (as of the device's current
  * state) and the number of occupied slots still searching. */
 cmn_status cmn_batch_totals(cmn_batch* batch, cmn_counters* sum,

@@ -56,6 +56,7 @@ class ProblemInfo(C.Structure):
         ("n_vars", C.c_int64), ("n_constraints", C.c_int64), ("n_nodes", C.c_int64),
         ("buffer_node_count", C.c_int64), ("program_length", C.c_int64), ("program_slots", C.c_int64),
         ("flops_per_box", C.c_double), ("point_flops_per_box", C.c_double), ("bytes_per_box", C.c_double),
+        ("program_segments", C.c_int64), ("lanes_per_box_max", C.c_int64),
     ]
 
 

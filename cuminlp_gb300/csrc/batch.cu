@@ -226,6 +226,7 @@ extern "C" cmn_status cmn_batch_create(const cmn_batch_config* config, cmn_batch
     A(&b.list_count, 1);
     A(&b.block_counts, (G + 511) / 512);
     A(&b.block_offsets, (G + 511) / 512);
+    A(&b.child_base, K + 2);
     A(&b.best_point, K * nm);
     if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&s->h_st), sizeof(InstState) * K);
     if (e != cudaSuccess) {
@@ -246,8 +247,11 @@ extern "C" cmn_status cmn_batch_create(const cmn_batch_config* config, cmn_batch
     if (e == cudaSuccess) e = cudaMemcpyAsync(b.st, s->h_st, sizeof(InstState) * K, cudaMemcpyHostToDevice, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     const int occ = std::max(1, std::min(batch_eval_occupancy(c, fp32), batch_sample_occupancy(c)));
-    const uint64_t need = (G + kEvalThreads - 1) / kEvalThreads;
+    const uint64_t need = (G * 32 + kEvalThreads - 1) / kEvalThreads;  // room for 32 lanes per child
     s->eval_grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(need, (uint64_t)sm_count() * occ));
+    c.g_max = 32;
+    c.eval_capacity = (uint64_t)s->eval_grid * kEvalThreads;
+    c.sample_capacity = c.eval_capacity;
     for (int i = 0; i < 5 && e == cudaSuccess; ++i) e = cudaEventCreate(&s->marks[i]);
     if (e == cudaSuccess) e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
@@ -309,6 +313,8 @@ extern "C" cmn_status cmn_batch_add(cmn_batch* s, const cmn_problem* p, const cm
   d.prog_len = (int32_t)p->prog.code64.size();
   d.n_vars = (int32_t)n;
   d.n_slots = p->prog.n_slots;
+  d.sched = p->d_sched;
+  d.g_max = p->d_sched ? p->prog.group_max : 1;
   d.active = 1;
   d.iter_limit = opts->iter_limit;
   d.batch_iter_limit = opts->batch_iter_limit;

@@ -38,6 +38,9 @@ struct BatchCfg {
   uint64_t child_stride;  // child slots per instance: e_max << B
   int64_t max_cycle;
   int64_t enumerate_cap;
+  int g_max;                 // lanes per child at most (1: one lane per child)
+  uint64_t eval_capacity;    // threads the bound launches keep resident
+  uint64_t sample_capacity;  // threads the sample launch keeps resident
 };
 
 struct InstDesc {
@@ -46,10 +49,13 @@ struct InstDesc {
   const int32_t* kinds;
   const double* root_lb;
   const double* root_ub;
+  const int32_t* sched;  // lane schedules of the program (null: none)
   int32_t prog_len;
   int32_t n_vars;
   int32_t n_slots;
   int32_t active;
+  int32_t g_max;        // lanes that may share one of its boxes
+  int32_t pad_;
   uint64_t iter_limit;
   uint64_t batch_iter_limit;
   double tolerance;
@@ -101,6 +107,7 @@ struct BatchBufs {
   uint64_t* list_count;
   uint32_t* block_counts;
   uint32_t* block_offsets;
+  uint64_t* child_base;  // [K + 2]: exclusive prefix of live children per slot, then the lane cap
   double* best_point;  // [K][n_max]
 };
 

@@ -316,11 +316,91 @@ __global__ void batch_branch_kernel(const BatchCfg c, const BatchBufs b)
   }
 }
 
+// Exclusive prefix of the live children per slot (n_parents << B) into
+// child_base[0..K]; child_base[K] is this iteration's live child count and
+// child_base[K + 1] the most lanes any live instance can use per child.
+__global__ void __launch_bounds__(1024) batch_live_kernel(const BatchCfg c, const BatchBufs b)
+{
+  __shared__ uint64_t wsum[32];
+  __shared__ uint64_t carry;
+  __shared__ int gmax;
+  if (threadIdx.x == 0) {
+    carry = 0;
+    gmax = 1;
+  }
+  __syncthreads();
+  int my_gmax = 1;
+  for (uint64_t i = threadIdx.x; i < c.K; i += 1024)
+    if (b.st[i].n_parents > 0 && b.desc[i].g_max > my_gmax) my_gmax = b.desc[i].g_max;
+  atomicMax(&gmax, my_gmax);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (uint64_t base = 0; base < c.K; base += 1024) {
+    const uint64_t i = base + threadIdx.x;
+    const uint64_t v = i < c.K ? (b.st[i].n_parents << c.log2C) : 0;
+    uint64_t x = v;
+    for (int off = 1; off < 32; off <<= 1) {
+      const uint64_t y = __shfl_up_sync(0xffffffffu, x, off);
+      if (lane >= off) x += y;
+    }
+    if (lane == 31) wsum[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+      uint64_t w = wsum[lane];
+      for (int off = 1; off < 32; off <<= 1) {
+        const uint64_t y = __shfl_up_sync(0xffffffffu, w, off);
+        if (lane >= off) w += y;
+      }
+      wsum[lane] = w;
+    }
+    __syncthreads();
+    const uint64_t cy = carry;
+    if (i < c.K) b.child_base[i] = cy + (wid > 0 ? wsum[wid - 1] : 0) + x - v;
+    __syncthreads();
+    if (threadIdx.x == 0) carry = cy + wsum[31];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    b.child_base[c.K] = carry;
+    b.child_base[c.K + 1] = (uint64_t)min(gmax, c.g_max);
+  }
+}
+
+// Live child i -> its global index slot * child_stride + local.
+__device__ __forceinline__ uint64_t live_child(const BatchCfg& c, const BatchBufs& b, uint64_t i)
+{
+  uint64_t lo = 0, hi = c.K;  // largest slot with child_base[slot] <= i
+  while (hi - lo > 1) {
+    const uint64_t mid = (lo + hi) >> 1;
+    if (__ldg(b.child_base + mid) <= i) lo = mid;
+    else hi = mid;
+  }
+  return lo * c.child_stride + (i - __ldg(b.child_base + lo));
+}
+
+// Lanes of a group of 2^lg that run instance d's program on one box: all of
+// them over the instance's lane schedule, or lane 0 alone over the whole
+// program when the instance has none (or takes fewer lanes).
+template <typename T, typename V>
+__device__ __forceinline__ Verdict<T> batch_lane_verdict(const InstDesc& d, const Instr* prog, int lg, int lane,
+                                                         const V& vars, const Tile<T>& t)
+{
+  int li = 0;
+  while (li < lg && (2 << li) <= d.g_max) ++li;
+  if (d.sched == nullptr || li == 0) {
+    if (lane == 0) return run_interval<T, V>(prog, d.prog_len, vars, t);
+    return verdict_init<T>();
+  }
+  if (lane < (1 << li)) return run_interval_lane<T, V>(prog, d.sched, li, lane, vars, t);
+  return verdict_init<T>();
+}
+
 // kMode 1: FP64 bound; 2: FP32 screen; 3: FP64 certify of the listed children.
 // Variables come from the parent planes (FP32 copies for the screen) with
-// the child's split variables in this thread's shared-memory column.
+// the child's split variables in this thread's shared-memory column.  The
+// launch walks only live children (child_base), with 2^lg lanes per child
+// when there are few of them.
 template <typename T, int kMode>
-__global__ void __launch_bounds__(kEvalThreads) batch_eval_kernel(const BatchCfg c, const BatchBufs b)
+__global__ void __launch_bounds__(kEvalThreads, 4) batch_eval_kernel(const BatchCfg c, const BatchBufs b)
 {
   using S = T;  // the screen reads the FP32 planes, the FP64 passes the FP64 planes
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -345,64 +425,82 @@ __global__ void __launch_bounds__(kEvalThreads) batch_eval_kernel(const BatchCfg
     planes_lo = b.plo;
     planes_hi = b.phi;
   }
-  const uint64_t total = kMode == 3 ? *b.list_count : c.K * c.child_stride;
-  for (uint64_t idx = (uint64_t)blockIdx.x * B + threadIdx.x; idx < total; idx += (uint64_t)gridDim.x * B) {
-    const uint64_t g = kMode == 3 ? (uint64_t)b.list[idx] : idx;
-    const uint64_t slot = g / c.child_stride, local = g % c.child_stride;
-    const uint64_t k = local >> c.log2C, r = local & ((1ULL << c.log2C) - 1ULL);
-    const InstState* st = &b.st[slot];
-    if (k >= st->n_parents) continue;
-    const size_t pk = slot * c.e_max + k;
-    const ParentInfo pi = b.pinfo[pk];
-    if (pi.fathom || r >= pi.nreg) {
-      if (kMode != 3) b.cstate[g] = kChildNone;
-      continue;
+  const uint64_t total = kMode == 3 ? *b.list_count : b.child_base[c.K];
+  const int lg = lanes_per_box(total, c.eval_capacity, (int)b.child_base[c.K + 1]);
+  const int G = 1 << lg;
+  const int lane = threadIdx.x & (G - 1);
+  const uint64_t per_block = (uint64_t)(B >> lg);
+  for (uint64_t bb = (uint64_t)blockIdx.x * per_block; bb < total; bb += (uint64_t)gridDim.x * per_block) {
+    const uint64_t idx = bb + (threadIdx.x >> lg);
+    bool live = idx < total;
+    uint64_t g = 0, slot = 0, k = 0, r = 0;
+    ParentInfo pi = {0, 1, 0};
+    const InstState* st = nullptr;
+    if (live) {
+      g = kMode == 3 ? (uint64_t)b.list[idx] : live_child(c, b, idx);
+      slot = g / c.child_stride;
+      const uint64_t local = g % c.child_stride;
+      k = local >> c.log2C;
+      r = local & ((1ULL << c.log2C) - 1ULL);
+      st = &b.st[slot];
+      pi = b.pinfo[slot * c.e_max + k];
+      if (pi.fathom || r >= pi.nreg) {
+        if (kMode != 3 && lane == 0) b.cstate[g] = kChildNone;
+        live = false;
+      }
     }
-    const SlotPlan* sp = b.slots + pk * c.max_slots;
-    if (kMode == 2 && !st->use_screen) {
+    const SlotPlan* sp = b.slots + (slot * c.e_max + k) * c.max_slots;
+    if (live && kMode == 2 && !st->use_screen) {
       bool dup = false;
       for (uint32_t j = 0; j < pi.count; ++j) dup = dup || ((r / sp[j].prefix) % sp[j].width >= sp[j].dom);
-      b.cstate[g] = dup ? kChildDuplicate : kChildScreened;
-      continue;
+      if (lane == 0) b.cstate[g] = dup ? kChildDuplicate : kChildScreened;
+      live = false;
     }
-    ChildVars<T, S> cv;
-    cv.plo = planes_lo + splane(c, slot, 0) + k;
-    cv.phi = planes_hi + splane(c, slot, 0) + k;
-    cv.pstride = c.e_max;
-    cv.mask = 0;
-    cv.olo = olo;
-    cv.ohi = ohi;
-    cv.ovid = ovid;
-    cv.count = (int)pi.count;
-    cv.stride = B;
-    bool dup = false;
-    for (uint32_t j = 0; j < pi.count; ++j) {
-      const SlotPlan s = sp[j];
-      const uint64_t part = (r / s.prefix) % s.width;
-      if (part >= s.dom) dup = true;
-      double lo, hi;
-      slot_bounds((int)s.kind, b.plo[splane(c, slot, s.vid) + k], b.phi[splane(c, slot, s.vid) + k], part, s.width,
-                  lo, hi);
-      olo[j * B] = Widen<T, double>::lo(lo);
-      ohi[j * B] = Widen<T, double>::hi(hi);
-      ovid[j * B] = (int32_t)s.vid;
-      cv.mask |= 1ULL << (s.vid & 63);
+    Verdict<T> v = verdict_init<T>();
+    if (live) {
+      ChildVars<T, S> cv;
+      cv.plo = planes_lo + splane(c, slot, 0) + k;
+      cv.phi = planes_hi + splane(c, slot, 0) + k;
+      cv.pstride = c.e_max;
+      cv.mask = 0;
+      cv.olo = olo;
+      cv.ohi = ohi;
+      cv.ovid = ovid;
+      cv.count = (int)pi.count;
+      cv.stride = B;
+      bool dup = false;
+      for (uint32_t j = 0; j < pi.count; ++j) {
+        const SlotPlan sj = sp[j];
+        const uint64_t part = (r / sj.prefix) % sj.width;
+        if (part >= sj.dom) dup = true;
+        double lo, hi;
+        slot_bounds((int)sj.kind, b.plo[splane(c, slot, sj.vid) + k], b.phi[splane(c, slot, sj.vid) + k], part,
+                    sj.width, lo, hi);
+        olo[j * B] = Widen<T, double>::lo(lo);
+        ohi[j * B] = Widen<T, double>::hi(hi);
+        ovid[j * B] = (int32_t)sj.vid;
+        cv.mask |= 1ULL << (sj.vid & 63);
+      }
+      if (dup) {
+        if (lane == 0) b.cstate[g] = kChildDuplicate;
+        live = false;
+      } else {
+        const InstDesc& d = b.desc[slot];
+        const Instr* prog = sizeof(T) == 4 ? d.prog32 : d.prog64;
+        v = batch_lane_verdict<T, ChildVars<T, S>>(d, prog, lg, lane, cv, t);
+      }
     }
-    if (dup) {
-      b.cstate[g] = kChildDuplicate;
-      continue;
-    }
-    const InstDesc& d = b.desc[slot];
-    const Instr* prog = sizeof(T) == 4 ? d.prog32 : d.prog64;
-    const Verdict<T> v = run_interval<T, ChildVars<T, S>>(prog, d.prog_len, cv, t);
-    const double lb = (double)v.obj.lo;
-    const double gub = st->gub;
-    b.clb[g] = lb;
-    if (kMode == 2) {
-      b.cstate[g] = v.excluded ? kChildInfeasible : (lb > gub ? kChildDominated : kChildScreened);
-    } else {
-      const uint8_t sv = !v.feasible ? kChildInfeasible : (lb > gub ? kChildDominated : kChildEligible);
-      b.cstate[g] = kMode == 3 ? (uint8_t)(sv | kCertifiedBit) : sv;
+    if (lg > 0) v = group_verdict<T>(v, G);
+    if (live && lane == 0) {
+      const double lb = (double)v.obj.lo;
+      const double gub = st->gub;
+      b.clb[g] = lb;
+      if (kMode == 2) {
+        b.cstate[g] = v.excluded ? kChildInfeasible : (lb > gub ? kChildDominated : kChildScreened);
+      } else {
+        const uint8_t sv = !v.feasible ? kChildInfeasible : (lb > gub ? kChildDominated : kChildEligible);
+        b.cstate[g] = kMode == 3 ? (uint8_t)(sv | kCertifiedBit) : sv;
+      }
     }
   }
 }
@@ -422,8 +520,9 @@ __device__ __forceinline__ double child_bound(const BatchCfg& c, const BatchBufs
   return lo;
 }
 
-// samples (or exact points of fathomed parents) of every child: the best
-// (value, element) per child
+// samples (or exact points of fathomed parents) of every live child: the
+// best (value, element) per child.  With 2^lg lanes per child every lane
+// stages the point in its own column and runs its share of the program.
 __global__ void __launch_bounds__(kEvalThreads) batch_sample_kernel(const BatchCfg c, const BatchBufs b)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -436,56 +535,85 @@ __global__ void __launch_bounds__(kEvalThreads) batch_sample_kernel(const BatchC
   t.shi = t.slo;
   t.stride = B;
   t.tid = threadIdx.x;
-  const uint64_t total = c.K * c.child_stride;
-  for (uint64_t g = (uint64_t)blockIdx.x * B + threadIdx.x; g < total; g += (uint64_t)gridDim.x * B) {
-    const uint64_t slot = g / c.child_stride, local = g % c.child_stride;
-    const uint64_t k = local >> c.log2C, r = local & ((1ULL << c.log2C) - 1ULL);
-    InstState* st = &b.st[slot];
-    if (k >= st->n_parents) continue;
-    b.cval[g] = INFINITY;
-    const size_t pk = slot * c.e_max + k;
-    const ParentInfo pi = b.pinfo[pk];
-    if (r >= pi.nreg) continue;
-    const bool fathom = pi.fathom != 0;
-    if (!fathom) {
-      const uint8_t s8 = b.cstate[g] & 0x7f;
-      const bool take = c.sample_all ? (s8 != kChildNone) : (s8 == kChildEligible);
-      if (!take) continue;
+  const uint64_t total = b.child_base[c.K];
+  const int lg = lanes_per_box(total, c.sample_capacity, (int)b.child_base[c.K + 1]);
+  const int G = 1 << lg;
+  const int lane = threadIdx.x & (G - 1);
+  const uint64_t per_block = (uint64_t)(B >> lg);
+  for (uint64_t bb = (uint64_t)blockIdx.x * per_block; bb < total; bb += (uint64_t)gridDim.x * per_block) {
+    const uint64_t idx = bb + (threadIdx.x >> lg);
+    bool live = idx < total;
+    uint64_t g = 0, slot = 0, k = 0, r = 0;
+    ParentInfo pi = {0, 0, 0};
+    InstState* st = nullptr;
+    bool fathom = false;
+    if (live) {
+      g = live_child(c, b, idx);
+      slot = g / c.child_stride;
+      const uint64_t local = g % c.child_stride;
+      k = local >> c.log2C;
+      r = local & ((1ULL << c.log2C) - 1ULL);
+      st = &b.st[slot];
+      if (lane == 0) b.cval[g] = INFINITY;
+      pi = b.pinfo[slot * c.e_max + k];
+      fathom = pi.fathom != 0;
+      if (r >= pi.nreg) live = false;
+      if (live && !fathom) {
+        const uint8_t s8 = b.cstate[g] & 0x7f;
+        live = c.sample_all ? (s8 != kChildNone) : (s8 == kChildEligible);
+      }
     }
-    const InstDesc& d = b.desc[slot];
-    const int n = d.n_vars;
-    const SlotPlan* sp = b.slots + pk * c.max_slots;
-    const uint64_t salt = st->salt_base + k + 1;
+    const SlotPlan* sp = b.slots + (slot * c.e_max + k) * c.max_slots;
     const uint64_t S = fathom ? 1 : c.S;
     double best = INFINITY;
     uint64_t best_e = 0;
-    for (uint64_t i = 0; i < S; ++i) {
-      for (int v = 0; v < n; ++v) {
-        double hi;
-        const double lo = child_bound(c, b, slot, k, r, v, sp, pi.count, hi);
-        t.lo[v * B + t.tid] = fathom ? lo : sample_value(d.kinds[v] != 0, lo, hi, (uint64_t)v, i, r, salt);
-      }
-      const PointVerdict pv = run_point(d.prog64, d.prog_len, t);
-      double value = (pv.feasible && !(pv.obj != pv.obj)) ? pv.obj : INFINITY;
-      if (fathom && value < INFINITY) {
-        bool ok = true;
-        for (int v = 0; v < n && ok; ++v) {
-          const double x = t.lo[v * B + t.tid];
-          if (!(x >= d.root_lb[v]) || !(x <= d.root_ub[v])) ok = false;
-          else if (d.kinds[v] != 0 && fabs(__dsub_rn(x, rint(x))) > 1e-6) ok = false;
+    for (uint64_t i = 0; i < c.S; ++i) {  // c.S bounds every box's S: the shuffles see every lane
+      const bool act = live && i < S;
+      PointVerdict pv;
+      pv.obj = INFINITY;
+      pv.feasible = true;
+      pv.has_obj = false;
+      const InstDesc* d = act ? &b.desc[slot] : nullptr;
+      if (act) {
+        const uint64_t salt = st->salt_base + k + 1;
+        for (int v = 0; v < d->n_vars; ++v) {
+          double hi;
+          const double lo = child_bound(c, b, slot, k, r, v, sp, pi.count, hi);
+          t.lo[v * B + t.tid] = fathom ? lo : sample_value(d->kinds[v] != 0, lo, hi, (uint64_t)v, i, r, salt);
         }
-        if (!ok) {
-          if (value < st->gub) atomicAdd((unsigned long long*)&st->counters.witness_rejected, 1ULL);
-          value = INFINITY;
+        int li = 0;
+        while (li < lg && (2 << li) <= d->g_max) ++li;
+        if (d->sched == nullptr || li == 0) {
+          if (lane == 0) pv = run_point(d->prog64, d->prog_len, t);
+        } else if (lane < (1 << li)) {
+          pv = run_point_lane(d->prog64, d->sched, li, lane, t);
         }
       }
-      if (value < best) {
-        best = value;
-        best_e = r * S + i;
+      if (lg > 0) pv = group_point_verdict(pv, G);
+      if (act && lane == 0) {
+        double value = (pv.feasible && !(pv.obj != pv.obj)) ? pv.obj : INFINITY;
+        if (fathom && value < INFINITY) {
+          bool ok = true;
+          for (int v = 0; v < d->n_vars && ok; ++v) {
+            const double x = t.lo[v * B + t.tid];
+            if (!(x >= d->root_lb[v]) || !(x <= d->root_ub[v])) ok = false;
+            else if (d->kinds[v] != 0 && fabs(__dsub_rn(x, rint(x))) > 1e-6) ok = false;
+          }
+          if (!ok) {
+            if (value < st->gub) atomicAdd((unsigned long long*)&st->counters.witness_rejected, 1ULL);
+            value = INFINITY;
+          }
+        }
+        if (value < best) {
+          best = value;
+          best_e = r * S + i;
+        }
       }
     }
-    b.cval[g] = best;
-    b.ce[g] = best_e;
+    if (live && lane == 0) {
+      b.cval[g] = best;
+      b.ce[g] = best_e;
+    }
   }
 }
 
@@ -834,6 +962,7 @@ cudaError_t batch_iteration(const BatchCfg& c, const BatchBufs& b, int eval_grid
   batch_select_kernel<<<(int)c.K, kMiThreads, sort_smem_bytes(), s>>>(c, b);
   const uint64_t np = c.K * c.e_max;
   batch_branch_kernel<<<(int)((np + 127) / 128), 128, 0, s>>>(c, b);
+  batch_live_kernel<<<1, 1024, 0, s>>>(c, b);
   mark(marks, 1, s);
   const bool fp32 = c.precision == CMN_PRECISION_FP32_SCREEN;
   if (fp32) {

@@ -111,6 +111,7 @@ cmn_problem::~cmn_problem()
   dfree(d_kinds);
   dfree(d_root_lb);
   dfree(d_root_ub);
+  dfree(d_sched);
   if (cur != device) cudaSetDevice(cur);
 }
 
@@ -155,6 +156,12 @@ extern "C" cmn_status cmn_problem_create(const cmn_problem_desc* desc, cmn_probl
       e = cudaMemcpy(p->d_root_lb, p->host.var_lb.data(), n * sizeof(double), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
       e = cudaMemcpy(p->d_root_ub, p->host.var_ub.data(), n * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !p->prog.sched.empty()) {
+      e = dalloc(&p->d_sched, p->prog.sched.size());
+      if (e == cudaSuccess)
+        e = cudaMemcpy(p->d_sched, p->prog.sched.data(), p->prog.sched.size() * sizeof(int32_t),
+                       cudaMemcpyHostToDevice);
+    }
     if (e != cudaSuccess) {
       delete p;
       return fail(CMN_CUDA_ERROR, std::string("uploading the problem: ") + cudaGetErrorString(e));
@@ -182,6 +189,8 @@ extern "C" cmn_status cmn_problem_get_info(const cmn_problem* p, cmn_problem_inf
   out->flops_per_box = p->prog.flops_per_box;
   out->point_flops_per_box = p->prog.point_flops_per_box;
   out->bytes_per_box = 16.0 * (double)p->host.n_vars() + 17.0;
+  out->program_segments = p->prog.n_segments;
+  out->lanes_per_box_max = p->prog.group_max;
   return CMN_OK;
 }
 
@@ -334,7 +343,7 @@ extern "C" cmn_status cmn_role_build(const cmn_problem* p, int32_t role, const u
     if (e == cudaSuccess) e = dalloc(&r->d_stage, r->stage_bytes);
     if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&r->h_stage), r->stage_bytes);
     const int threads = kEvalThreads;
-    const uint64_t blocks_needed = (n_regions + threads - 1) / threads;
+    const uint64_t blocks_needed = (n_regions * (uint64_t)p->prog.group_max + threads - 1) / threads;
     const int occ = std::max(
         1, eval_kernel_occupancy(0, false, eval_smem_bytes(p->prog.n_slots, (int)slot_count, false, threads), threads));
     r->grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(blocks_needed, (uint64_t)sm_count() * occ));
@@ -442,6 +451,9 @@ extern "C" cmn_status cmn_bound(cmn_role* r, const double* box, const uint64_t* 
   a.n_children = r->n_regions;
   a.out_lb = r->d_lb;
   a.out_flag = r->d_feas;
+  a.sched = r->p->d_sched;
+  a.g_max = r->p->prog.group_max;
+  a.capacity = (uint64_t)r->grid * kEvalThreads;
   CK(launch_eval(a, 0, false, r->grid, kEvalThreads, r->stream));
   CK(cudaMemcpyAsync(r->h_feas, r->d_feas, r->n_regions, cudaMemcpyDeviceToHost, r->stream));
   CK(cudaMemcpyAsync(r->h_lb, r->d_lb, r->n_regions * sizeof(double), cudaMemcpyDeviceToHost, r->stream));
@@ -482,6 +494,9 @@ static cmn_status candidate_role(cmn_role* r, const double* box, const uint64_t*
   a.salt = salt;
   a.exact = exact;
   a.block_best = r->d_block_best;
+  a.sched = r->p->d_sched;
+  a.g_max = r->p->prog.group_max;
+  a.capacity = (uint64_t)r->grid * kEvalThreads;
   CK(launch_sample(a, r->grid, kEvalThreads, r->stream));
   Cand* best = r->d_block_best + r->grid;
   CK(launch_reduce_cand(r->d_block_best, r->grid, best, r->stream));
@@ -577,8 +592,11 @@ extern "C" cmn_status cmn_eval_boxes(const cmn_problem* p, int32_t precision, co
   const int threads = kEvalThreads;
   const int occ =
       std::max(1, eval_kernel_occupancy(0, fp32, eval_smem_bytes(p->prog.n_slots, 0, fp32, threads), threads));
-  const uint64_t need = (n_boxes + threads - 1) / threads;
+  const uint64_t need = (n_boxes * (uint64_t)p->prog.group_max + threads - 1) / threads;
   const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(need, (uint64_t)sm_count() * occ));
+  a.sched = p->d_sched;
+  a.g_max = p->prog.group_max;
+  a.capacity = (uint64_t)sm_count() * occ * threads;
   cudaError_t e = launch_eval(a, 0, fp32, grid, threads, s);
   if (e != cudaSuccess) {
     dfree(tmp);
@@ -719,9 +737,12 @@ extern "C" cmn_status cmn_solver_create(const cmn_problem* p, const cmn_solve_op
     const int occ_e = std::max(1, eval_kernel_occupancy(fp32 ? 2 : 1, fp32,
                                                         eval_smem_bytes(p->prog.n_slots, cfg.max_slots, fp32, threads), threads));
     const int occ_s = std::max(1, sample_kernel_occupancy(sample_smem_bytes(n, p->prog.n_slots, threads), threads));
-    const uint64_t need = (maxc + threads - 1) / threads;
+    const uint64_t need = (maxc * (uint64_t)p->prog.group_max + threads - 1) / threads;
     s->eval_grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(need, (uint64_t)sm_count() * occ_e));
     s->sample_grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(need, (uint64_t)sm_count() * occ_s));
+    cfg.g_max = p->d_sched ? p->prog.group_max : 1;
+    cfg.eval_capacity = (uint64_t)s->eval_grid * threads;
+    cfg.sample_capacity = (uint64_t)s->sample_grid * threads;
 
     SolverBufs& b = s->b;
     cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
@@ -773,6 +794,7 @@ extern "C" cmn_status cmn_solver_create(const cmn_problem* p, const cmn_solve_op
     }
     b.prog64 = p->d_prog64;
     b.prog32 = p->d_prog32;
+    b.sched = p->d_sched;
     b.kinds = p->d_kinds;
     b.root_lb = p->d_root_lb;
     b.root_ub = p->d_root_ub;

@@ -390,23 +390,33 @@ struct Verdict {
   Iv<T> obj;
   bool feasible;    // FP64: reference predicate (NaN lb -> infeasible)
   bool excluded;    // a constraint is proven violated (NaN never excludes)
+  bool has_obj;     // this lane executed the objective (segmented runs)
 };
 
-// Interval interpretation of `prog` for this thread's box: variables from
-// `vars` (anything with var(v) -> Iv<T>), program slots in `t`.
-template <typename T, typename V>
-__device__ Verdict<T> run_interval(const Instr* __restrict__ prog, int len, const V& vars, const Tile<T>& t)
+template <typename T>
+__device__ __forceinline__ Verdict<T> verdict_init()
 {
-  using A = Arith<T>;
-  Iv<T> acc = {T(0), T(0)};
   Verdict<T> out;
-  out.obj = {A::nan(), A::nan()};
+  out.obj = {Arith<T>::nan(), Arith<T>::nan()};
   out.feasible = true;
   out.excluded = false;
-  Instr ins = len > 0 ? load_instr(prog, 0) : Instr{};
-  for (int pc = 0; pc < len; ++pc) {
+  out.has_obj = false;
+  return out;
+}
+
+// Interval interpretation of instructions [pc0, pc1) for this thread's box,
+// starting from a zero accumulator: variables from `vars` (anything with
+// var(v) -> Iv<T>), program slots in `t`.  Checks fold into `out` with AND /
+// OR, so ranges may run in any order.
+template <typename T, typename V>
+__device__ __forceinline__ void interval_range(const Instr* __restrict__ prog, int pc0, int pc1, const V& vars,
+                                               const Tile<T>& t, Verdict<T>& out)
+{
+  Iv<T> acc = {T(0), T(0)};
+  Instr ins = pc0 < pc1 ? load_instr(prog, pc0) : Instr{};
+  for (int pc = pc0; pc < pc1; ++pc) {
     const Instr cur = ins;
-    if (pc + 1 < len) ins = load_instr(prog, pc + 1);  // software prefetch
+    if (pc + 1 < pc1) ins = load_instr(prog, pc + 1);  // software prefetch
     const int code = cur.head & 7;
     const int sub = cur.head >> 3;
     switch (code) {
@@ -457,12 +467,85 @@ __device__ Verdict<T> run_interval(const Instr* __restrict__ prog, int len, cons
       }
       case kOpObjective:
         out.obj = fetch(vars, t, acc, cur, cur.modes & 3, cur.a);
+        out.has_obj = true;
         break;
       default:
         break;
     }
   }
+}
+
+template <typename T, typename V>
+__device__ Verdict<T> run_interval(const Instr* __restrict__ prog, int len, const V& vars, const Tile<T>& t)
+{
+  Verdict<T> out = verdict_init<T>();
+  interval_range<T, V>(prog, 0, len, vars, t, out);
   return out;
+}
+
+// Segments of `lane` in a group of 2^l lanes: [b, e) indexes the (pc0, pc1)
+// pairs of the level's block of the lane schedule (Program::sched).
+struct LaneSegs {
+  const int32_t* pairs;
+  int b, e;
+};
+__device__ __forceinline__ LaneSegs lane_segments(const int32_t* __restrict__ sched, int l, int lane)
+{
+  const int32_t* L = sched + __ldg(sched + l);
+  LaneSegs s;
+  s.b = __ldg(L + lane);
+  s.e = __ldg(L + lane + 1);
+  s.pairs = L + (1 << l) + 1;
+  return s;
+}
+
+// One lane of a group of 2^l lanes that share a box: it runs its share of
+// the program's segments (independent sum chains, each starting with an
+// accumulator reset).  Every instruction performs the same roundings as in
+// the whole-program run, so the group's combined verdict (group_verdict) is
+// bit-identical to run_interval's.
+template <typename T, typename V>
+__device__ Verdict<T> run_interval_lane(const Instr* __restrict__ prog, const int32_t* __restrict__ sched, int l,
+                                        int lane, const V& vars, const Tile<T>& t)
+{
+  Verdict<T> out = verdict_init<T>();
+  const LaneSegs ls = lane_segments(sched, l, lane);
+  for (int j = ls.b; j < ls.e; ++j)
+    interval_range<T, V>(prog, __ldg(ls.pairs + 2 * j), __ldg(ls.pairs + 2 * j + 1), vars, t, out);
+  return out;
+}
+
+// Combines the verdicts of a group of G consecutive lanes (G a power of two
+// up to 32); every lane of the warp must call it with the same G.
+template <typename T>
+__device__ __forceinline__ Verdict<T> group_verdict(Verdict<T> v, int G)
+{
+  for (int off = 1; off < G; off <<= 1) {
+    const int f = __shfl_xor_sync(0xffffffffu, (int)v.feasible, off);
+    const int e = __shfl_xor_sync(0xffffffffu, (int)v.excluded, off);
+    const int h = __shfl_xor_sync(0xffffffffu, (int)v.has_obj, off);
+    const T lo = __shfl_xor_sync(0xffffffffu, v.obj.lo, off);
+    const T hi = __shfl_xor_sync(0xffffffffu, v.obj.hi, off);
+    v.feasible = v.feasible && f;
+    v.excluded = v.excluded || e;
+    if (!v.has_obj && h) {
+      v.obj = {lo, hi};
+      v.has_obj = true;
+    }
+  }
+  return v;
+}
+
+// Lanes per box for `n` boxes: the largest power of two G <= g_max with
+// n * G <= capacity (the threads the launch keeps resident), so a small
+// frontier spreads each box over several lanes and a large one keeps one
+// lane per box.
+// Returns log2 of the group size.
+__device__ __forceinline__ int lanes_per_box(uint64_t n, uint64_t capacity, int g_max)
+{
+  int l = 0;
+  while ((1 << l) < g_max && n * (uint64_t)(2 << l) <= capacity) ++l;
+  return l;
 }
 
 // Variables held in the tile's own planes.
@@ -485,6 +568,7 @@ __device__ __forceinline__ bool almost_equal(double a, double b)
 struct PointVerdict {
   double obj;
   bool feasible;
+  bool has_obj;
 };
 
 __device__ __forceinline__ double pfetch(const Tile<double>& t, double acc, const Instr& ins, int mode, int idx)
@@ -497,17 +581,15 @@ __device__ __forceinline__ double pfetch(const Tile<double>& t, double acc, cons
   }
 }
 
-__device__ inline PointVerdict run_point(const Instr* __restrict__ prog, int len, const Tile<double>& t)
+__device__ __forceinline__ void point_range(const Instr* __restrict__ prog, int pc0, int pc1, const Tile<double>& t,
+                                            PointVerdict& out)
 {
   using A = Arith<double>;
   double acc = 0.0;
-  PointVerdict out;
-  out.obj = A::nan();
-  out.feasible = true;
-  Instr ins = len > 0 ? load_instr(prog, 0) : Instr{};
-  for (int pc = 0; pc < len; ++pc) {
+  Instr ins = pc0 < pc1 ? load_instr(prog, pc0) : Instr{};
+  for (int pc = pc0; pc < pc1; ++pc) {
     const Instr cur = ins;
-    if (pc + 1 < len) ins = load_instr(prog, pc + 1);
+    if (pc + 1 < pc1) ins = load_instr(prog, pc + 1);
     const int code = cur.head & 7;
     const int sub = cur.head >> 3;
     switch (code) {
@@ -551,12 +633,50 @@ __device__ inline PointVerdict run_point(const Instr* __restrict__ prog, int len
       }
       case kOpObjective:
         out.obj = pfetch(t, acc, cur, cur.modes & 3, cur.a);
+        out.has_obj = true;
         break;
       default:
         break;
     }
   }
+}
+
+__device__ inline PointVerdict run_point(const Instr* __restrict__ prog, int len, const Tile<double>& t)
+{
+  PointVerdict out;
+  out.obj = Arith<double>::nan();
+  out.feasible = true;
+  out.has_obj = false;
+  point_range(prog, 0, len, t, out);
   return out;
+}
+
+// One lane of a group sharing a point (see run_interval_lane).
+__device__ inline PointVerdict run_point_lane(const Instr* __restrict__ prog, const int32_t* __restrict__ sched, int l,
+                                              int lane, const Tile<double>& t)
+{
+  PointVerdict out;
+  out.obj = Arith<double>::nan();
+  out.feasible = true;
+  out.has_obj = false;
+  const LaneSegs ls = lane_segments(sched, l, lane);
+  for (int j = ls.b; j < ls.e; ++j) point_range(prog, __ldg(ls.pairs + 2 * j), __ldg(ls.pairs + 2 * j + 1), t, out);
+  return out;
+}
+
+__device__ __forceinline__ PointVerdict group_point_verdict(PointVerdict v, int G)
+{
+  for (int off = 1; off < G; off <<= 1) {
+    const int f = __shfl_xor_sync(0xffffffffu, (int)v.feasible, off);
+    const int h = __shfl_xor_sync(0xffffffffu, (int)v.has_obj, off);
+    const double o = __shfl_xor_sync(0xffffffffu, v.obj, off);
+    v.feasible = v.feasible && f;
+    if (!v.has_obj && h) {
+      v.obj = o;
+      v.has_obj = true;
+    }
+  }
+  return v;
 }
 
 // ---- region decode (region/decode.hpp:44-71), FMA form as compiled on

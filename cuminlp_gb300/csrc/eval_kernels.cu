@@ -84,6 +84,75 @@ size_t eval_smem_bytes(int n_slots, int max_slots, bool fp32, int threads)
   return ((2 * t) * (size_t)(n_slots + max_slots) + 4 * (size_t)max_slots) * (size_t)threads;
 }
 
+// Writes the verdict of child g (kModes as in eval_children).
+template <typename T, int kMode>
+__device__ __forceinline__ void write_verdict(const EvalArgs& a, uint64_t g, const Verdict<T>& v, double gub)
+{
+  const double lb = (double)v.obj.lo;
+  if (kMode == 0) {
+    a.out_lb[g] = lb;
+    if (a.out_ub) a.out_ub[g] = (double)v.obj.hi;
+    // FP64: the reference predicate; FP32: not proven violated
+    a.out_flag[g] = (uint8_t)(sizeof(T) == 8 ? v.feasible : !v.excluded);
+  } else if (kMode == 2) {
+    a.out_lb[g] = lb;
+    a.out_flag[g] = v.excluded ? kChildInfeasible : (lb > gub ? kChildDominated : kChildScreened);
+  } else {
+    a.out_lb[g] = lb;
+    a.out_flag[g] = !v.feasible ? kChildInfeasible : (lb > gub ? kChildDominated : kChildEligible);
+  }
+}
+
+// Groups of 2^lg consecutive lanes share one child: each lane runs its
+// segments of the program and the group combines the verdicts.  The loop
+// bound is per block, so every lane of a warp reaches the shuffles.
+template <typename T, int kMode, typename S>
+__device__ void eval_children_grouped(const EvalArgs& a, const S* plo, const S* phi, uint64_t total, double gub,
+                                      bool pass_through, int lg, const Tile<T>& t, T* olo, T* ohi, int32_t* ovid)
+{
+  const int B = blockDim.x;
+  const int G = 1 << lg;
+  const int lane = threadIdx.x & (G - 1);
+  const uint64_t per_block = (uint64_t)(B >> lg);
+  for (uint64_t base = (uint64_t)blockIdx.x * per_block; base < total; base += (uint64_t)gridDim.x * per_block) {
+    const uint64_t idx = base + (threadIdx.x >> lg);
+    bool live = idx < total;
+    uint64_t g = 0, k = 0, r = 0;
+    if (live) {
+      g = (kMode == 3) ? (uint64_t)a.list[idx] : idx;
+      child_of(a.log2C, g, k, r);
+      if (kMode != 0 && a.pinfo != nullptr) {
+        const ParentInfo pi = a.pinfo[k];
+        if (pi.fathom || r >= pi.nreg) {
+          if (kMode != 3 && lane == 0) a.out_flag[g] = kChildNone;
+          live = false;
+        }
+      }
+    }
+    if (live && pass_through) {
+      bool dup = false;
+      const uint32_t count = a.pinfo[k].count;
+      const SlotPlan* sp = a.slots + k * (uint64_t)a.max_slots;
+      for (uint32_t j = 0; j < count; ++j) dup = dup || ((r / sp[j].prefix) % sp[j].width >= sp[j].dom);
+      if (lane == 0) a.out_flag[g] = dup ? kChildDuplicate : kChildScreened;
+      live = false;
+    }
+    Verdict<T> v = verdict_init<T>();
+    if (live) {
+      bool dup;
+      const ChildVars<T, S> cv = child_vars<T, S>(a, plo, phi, k, r, olo, ohi, ovid, B, dup);
+      if (kMode != 0 && dup) {
+        if (lane == 0) a.out_flag[g] = kChildDuplicate;
+        live = false;
+      } else {
+        v = run_interval_lane<T, ChildVars<T, S>>(a.prog, a.sched, lg, lane, cv, t);
+      }
+    }
+    v = group_verdict<T>(v, G);
+    if (live && lane == 0) write_verdict<T, kMode>(a, g, v, gub);
+  }
+}
+
 // kMode 0: role / raw boxes -> out_lb, out_ub, out_flag = feasible
 // kMode 1: solver FP64 -> out_lb, out_flag = ChildState
 // kMode 2: solver FP32 screen -> out_lb (FP32 bound), out_flag = ChildState
@@ -115,6 +184,11 @@ __device__ __forceinline__ void eval_children(const EvalArgs& a, const S* plo, c
   // certify pass unevaluated (duplicates and empty slots still classified)
   const bool pass_through = kMode == 2 && a.use_screen != nullptr && *a.use_screen == 0;
 
+  const int lg = a.sched != nullptr ? lanes_per_box(total, a.capacity, a.g_max) : 0;
+  if (lg > 0) {
+    eval_children_grouped<T, kMode, S>(a, plo, phi, total, gub, pass_through, lg, t, olo, ohi, ovid);
+    return;
+  }
   for (uint64_t idx = (uint64_t)blockIdx.x * B + threadIdx.x; idx < total; idx += (uint64_t)gridDim.x * B) {
     const uint64_t g = (kMode == 3) ? (uint64_t)a.list[idx] : idx;
     uint64_t k, r;
@@ -158,7 +232,7 @@ __device__ __forceinline__ void eval_children(const EvalArgs& a, const S* plo, c
 }
 
 template <typename T, int kMode>
-__global__ void __launch_bounds__(kEvalThreads) eval_children_kernel(const EvalArgs a)
+__global__ void __launch_bounds__(kEvalThreads, 4) eval_children_kernel(const EvalArgs a)
 {
   if constexpr (sizeof(T) == 4) {
     if (a.plo32 != nullptr) {
@@ -212,6 +286,84 @@ __device__ __forceinline__ bool admissible(const SampleArgs& a, const Tile<doubl
   return true;
 }
 
+// The point of sample i of child (k, r), staged in this thread's column:
+// every variable from its region bound (the parent's, narrowed by its slot).
+__device__ __forceinline__ void stage_point(const SampleArgs& a, const Tile<double>& t, uint64_t k, uint64_t r,
+                                            uint64_t i, uint64_t salt, bool fathom)
+{
+  const SlotPlan* sp = a.pinfo ? a.slots + k * (uint64_t)a.max_slots : nullptr;
+  const uint32_t count = a.pinfo ? a.pinfo[k].count : 0;
+  for (int v = 0; v < a.n_vars; ++v) {
+    double lo = a.plo[(uint64_t)v * a.pstride + k];
+    double hi = a.phi[(uint64_t)v * a.pstride + k];
+    for (uint32_t j = 0; j < count; ++j) {
+      if (sp[j].vid == (uint32_t)v) {
+        const uint64_t part = (r / sp[j].prefix) % sp[j].width;
+        slot_bounds((int)sp[j].kind, lo, hi, part, sp[j].width, lo, hi);
+        break;
+      }
+    }
+    t.lo[v * t.stride + t.tid] = fathom ? lo : sample_value(a.var_kinds[v] != 0, lo, hi, (uint64_t)v, i, r, salt);
+  }
+}
+
+// Sampling with groups of 2^lg lanes per child (see eval_children_grouped):
+// every lane stages the whole point in its own column, runs its segments
+// of the point program, and lane 0 of the group scores the combined result.
+__device__ void sample_children_grouped(const SampleArgs& a, const Tile<double>& t, uint64_t total,
+                                        uint64_t salt_base, double gub, int lg, Cand& best,
+                                        unsigned long long& rejected)
+{
+  const int B = blockDim.x;
+  const int G = 1 << lg;
+  const int lane = threadIdx.x & (G - 1);
+  const uint64_t per_block = (uint64_t)(B >> lg);
+  const uint64_t S_loop = a.exact ? 1 : a.S;
+  for (uint64_t base = (uint64_t)blockIdx.x * per_block; base < total; base += (uint64_t)gridDim.x * per_block) {
+    const uint64_t g = base + (threadIdx.x >> lg);
+    bool live = g < total;
+    uint64_t k = 0, r = 0;
+    bool fathom = a.exact != 0;
+    if (live) {
+      child_of(a.log2C, g, k, r);
+      uint64_t nreg = ~0ULL;
+      if (a.pinfo != nullptr) {
+        const ParentInfo pi = a.pinfo[k];
+        nreg = pi.nreg;
+        fathom = fathom || pi.fathom;
+      }
+      if (r >= nreg) live = false;
+      if (live && a.state != nullptr && !fathom) {
+        const uint8_t st = a.state[g];
+        live = a.sample_all ? (st != kChildNone) : (st == kChildEligible);
+      }
+    }
+    const uint64_t salt = a.salt_base_dev ? salt_base + k + 1 : a.salt;
+    const uint64_t S = fathom ? 1 : a.S;
+    for (uint64_t i = 0; i < S_loop; ++i) {
+      const bool act = live && i < S;
+      PointVerdict pv;
+      pv.obj = INFINITY;
+      pv.feasible = true;
+      pv.has_obj = false;
+      if (act) {
+        stage_point(a, t, k, r, i, salt, fathom);
+        pv = run_point_lane(a.prog, a.sched, lg, lane, t);
+      }
+      pv = group_point_verdict(pv, G);
+      if (act && lane == 0) {
+        double value = (pv.feasible && !(pv.obj != pv.obj)) ? pv.obj : INFINITY;
+        if (fathom && a.state != nullptr && value < INFINITY && !admissible(a, t)) {
+          if (value < gub) ++rejected;
+          value = INFINITY;
+        }
+        const Cand c = {value, (uint32_t)k, 0, r * S + i};
+        if (value < INFINITY && cand_less(c, best)) best = c;
+      }
+    }
+  }
+}
+
 // Point sampling (graph/subregion_sampler.cuh:133-199) and exact points
 // (graph/kernels.cuh:131-172), point program, feasibility mask and the
 // ArgMin over (value, parent, element) -- element = region * S + sample.
@@ -238,7 +390,9 @@ __global__ void __launch_bounds__(kEvalThreads) sample_children_kernel(const Sam
   Cand best = {INFINITY, 0xffffffffu, 0, ~0ULL};
   unsigned long long rejected = 0;
 
-  for (uint64_t g = (uint64_t)blockIdx.x * B + threadIdx.x; g < total; g += (uint64_t)gridDim.x * B) {
+  const int lg = a.sched != nullptr ? lanes_per_box(total, a.capacity, a.g_max) : 0;
+  if (lg > 0) sample_children_grouped(a, t, total, salt_base, gub, lg, best, rejected);
+  for (uint64_t g = (uint64_t)blockIdx.x * B + threadIdx.x; lg == 0 && g < total; g += (uint64_t)gridDim.x * B) {
     uint64_t k, r;
     child_of(a.log2C, g, k, r);
     bool fathom = a.exact != 0;

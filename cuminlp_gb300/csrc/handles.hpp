@@ -18,6 +18,7 @@ struct cmn_problem {
   int32_t* d_kinds = nullptr;
   double* d_root_lb = nullptr;
   double* d_root_ub = nullptr;
+  int32_t* d_sched = nullptr;  // lane schedules (Program::sched), null when none
 
   ~cmn_problem();
 };

@@ -72,6 +72,10 @@ struct EvalArgs {
   const double* gub;              // incumbent at the start of the iteration
   const uint32_t* done;           // solver: nonzero once the search stopped
   const uint32_t* use_screen;     // FP32 screen: zero passes every child to the certify pass
+  // lane groups (null sched: one lane per box); see Program::sched
+  const int32_t* sched;
+  int g_max;
+  uint64_t capacity;  // threads the launch keeps resident
   // outputs
   double* out_lb;
   double* out_ub;
@@ -105,6 +109,9 @@ struct SampleArgs {
   const uint32_t* done;      // solver: nonzero once the search stopped
   Cand* block_best;          // [gridDim.x]
   unsigned long long* rejected;  // inadmissible feasible exact points below gub
+  const int32_t* sched;      // lane groups, as EvalArgs
+  int g_max;
+  uint64_t capacity;
 };
 
 }  // namespace cmn

@@ -270,6 +270,7 @@ class Compiler {
     classify_terms();
     emit_all();
     out_.n_slots = max_slots_;
+    build_schedule();
     out_.code32 = out_.code64;
     for (size_t k = 0; k < out_.code64.size(); ++k) {
       Instr& s = out_.code32[k];
@@ -289,6 +290,67 @@ class Compiler {
   }
 
  private:
+  // Splits a slot-free program at every accumulator reset (a chain's first
+  // TERM, or LoadAcc) into independent segments, then assigns them to the
+  // lanes of groups of 2..32 lanes, longest first, each to the lane with
+  // the least work so far.
+  void build_schedule()
+  {
+    const int len = (int)out_.code64.size();
+    if (out_.n_slots != 0 || len == 0) return;
+    std::vector<std::pair<int, int>> segs;
+    int start = 0;
+    for (int pc = 1; pc < len; ++pc) {
+      const Instr& in = out_.code64[pc];
+      const int code = in.head & 7, sub = in.head >> 3;
+      if ((code == kOpTerm && (sub & kTermInit)) || code == kOpLoadAcc) {
+        segs.push_back({start, pc});
+        start = pc;
+      }
+    }
+    segs.push_back({start, len});
+    std::stable_sort(segs.begin(), segs.end(), [](const std::pair<int, int>& a, const std::pair<int, int>& b) {
+      return (a.second - a.first) > (b.second - b.first);
+    });
+    const int ns = (int)segs.size();
+    out_.n_segments = ns;
+    out_.sched.assign(6, 0);
+    out_.makespan.assign(6, 0);
+    out_.makespan[0] = len;
+    for (int l = 1; l <= 5; ++l) {
+      const int G = 1 << l;
+      std::vector<std::vector<int>> lanes(G);
+      std::vector<int64_t> load(G, 0);
+      for (int j = 0; j < ns; ++j) {
+        int best = 0;
+        for (int q = 1; q < G; ++q)
+          if (load[q] < load[best]) best = q;
+        lanes[best].push_back(j);
+        load[best] += segs[j].second - segs[j].first;
+      }
+      out_.makespan[l] = *std::max_element(load.begin(), load.end());
+      out_.sched[l] = (int32_t)out_.sched.size();
+      int32_t acc = 0;
+      out_.sched.push_back(0);
+      for (int q = 0; q < G; ++q) {
+        acc += (int32_t)lanes[q].size();
+        out_.sched.push_back(acc);
+      }
+      for (int q = 0; q < G; ++q)
+        for (int j : lanes[q]) {
+          out_.sched.push_back(segs[j].first);
+          out_.sched.push_back(segs[j].second);
+        }
+    }
+    // more lanes per box only while they cut the busiest lane's work by a
+    // fifth or more
+    out_.group_max = 1;
+    for (int l = 1; l <= 5; ++l) {
+      if (out_.makespan[l] * 5 > out_.makespan[l - 1] * 4) break;
+      out_.group_max = 1 << l;
+    }
+  }
+
   bool is_var(int64_t id) const { return p_.nodes[id].op == CMN_OP_VAR; }
   bool is_const(int64_t id) const { return p_.nodes[id].op == CMN_OP_CONST; }
 

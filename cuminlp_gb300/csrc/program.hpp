@@ -39,6 +39,16 @@ struct Program {
   double flops_per_box = 0;        // algorithmic FP64 ops, interval eval
   double point_flops_per_box = 0;  // algorithmic FP64 ops, point eval
   int64_t n_terms = 0;             // fused sum-chain terms
+  // Lane schedules for boxes shared by a group of G = 2^l lanes (l = 1..5),
+  // built only for programs without slots, whose segments (independent sum
+  // chains) can run in any order.  Layout: sched[l] is the offset of level
+  // l's block: G + 1 per-lane offsets into the pair list that follows, then
+  // (pc0, pc1) pairs in lane order.  Lanes get segments by longest-first
+  // greedy assignment (LPT).
+  int n_segments = 0;
+  int group_max = 1;               // largest G that still shortens a box's critical path
+  std::vector<int32_t> sched;
+  std::vector<int64_t> makespan;   // instructions on the busiest lane, per level
 };
 
 // Compiles the reachable DAG into the fused straight-line program.

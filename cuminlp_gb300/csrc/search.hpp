@@ -77,6 +77,9 @@ struct SolverCfg {
   int64_t max_cycle;
   int64_t enumerate_cap;
   double tolerance;
+  int g_max;                 // lanes per child at most (1: one lane per child)
+  uint64_t eval_capacity;    // resident threads of the bound kernels
+  uint64_t sample_capacity;  // resident threads of the sampler
 };
 
 struct SolverBufs {
@@ -112,6 +115,7 @@ struct SolverBufs {
   // problem
   const Instr* prog64;
   const Instr* prog32;
+  const int32_t* sched;  // lane schedules of the program (null: none)
   const int32_t* kinds;
   const double* root_lb;
   const double* root_ub;

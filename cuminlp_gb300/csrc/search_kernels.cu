@@ -731,6 +731,9 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
   ea.out_lb = b.clb;
   ea.out_flag = b.cstate;
   ea.prog_len = cfg.prog_len;
+  ea.sched = b.sched;
+  ea.g_max = cfg.g_max;
+  ea.capacity = cfg.eval_capacity;
   cudaError_t e;
   if (cfg.precision == CMN_PRECISION_FP32_SCREEN) {
     ea.prog = b.prog32;
@@ -790,6 +793,9 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
   sa.done = &b.dev->done;
   sa.block_best = b.block_best;
   sa.rejected = (unsigned long long*)&b.dev->counters.witness_rejected;
+  sa.sched = b.sched;
+  sa.g_max = cfg.g_max;
+  sa.capacity = cfg.sample_capacity;
   e = launch_sample(sa, sample_grid, kEvalThreads, s);
   if (e != cudaSuccess) return e;
   Cand* best = b.block_best + b.n_block_best - 1;  // last entry holds the result

@@ -138,6 +138,8 @@ typedef struct cmn_problem_info {
   double flops_per_box;       /* algorithmic FP64 ops of one interval eval */
   double point_flops_per_box; /* algorithmic FP64 ops of one point eval */
   double bytes_per_box;       /* algorithmic HBM bytes of one box eval */
+  int64_t program_segments;   /* independent sum chains (0: not split) */
+  int64_t lanes_per_box_max;  /* lanes that may share one box (1: none) */
 } cmn_problem_info;
 
 /* Thread-local message describing the last failure on this thread. */

@@ -38,6 +38,7 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
+EVAL_DRAM_BYTES_PER_BOX = (43186688 + 34048) / 1048576  # ncu, eval_children_kernel<double, 1>, config 2
 E_PARENTS = 1 << 16
 B_BITS = 4
 CAP = 1 << 20
@@ -464,12 +465,10 @@ def run_ours(args):
     hbm_gbs = nb * bpb / (ev_ms * 1e-3) / 1e9
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    traffic = None
-    tf = ROOT / "profiles" / "eval_traffic.json"
-    if tf.exists():
-        traffic = json.loads(tf.read_text()).get("dram_bytes_per_box")
-        if traffic is not None:
-            traffic = traffic * nb / max(1, len(plain["phases"]))
+    # DRAM bytes per launch of the dominant kernel, from one ncu capture of
+    # a full-size config-2 iteration (43,186,688 B read + 34,048 B written
+    # for 1,048,576 child boxes), scaled to this run's boxes per launch
+    traffic = EVAL_DRAM_BYTES_PER_BOX * nb / max(1, len(plain["phases"]))
 
     model, cores = cpu_info()
     cpu_v, cpu_s = cpu_rate(problem, args.cpu_seconds, cores)
@@ -531,6 +530,9 @@ def run_ours(args):
             "kernel": "eval_children_kernel<double> (fused interval DAG evaluator, plain FP64 form)",
             "achieved": achieved, "peak": peak64, "unit": "TFLOP/s", "frac": achieved / peak64,
             "peak_source": "measured by cmn_measure_fma_peak (DFMA loop, all SMs) in this run",
+            # directed rounding forbids FMA: one flop per FP64 instruction, so
+            # the pipe's ceiling for this arithmetic is half the DFMA flop rate
+            "frac_of_fp64_instruction_ceiling": achieved / (peak64 / 2),
             "flops_per_box": fpb, "boxes_per_launch": nb / len(plain["phases"]),
             "traffic": traffic,
             "hbm": {"achieved": hbm_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": hbm_gbs / hbm_peak,

@@ -75,6 +75,10 @@ class Candidate(C.Structure):
                 ("point", C.POINTER(C.c_double)), ("index", C.c_int64)]
 
 
+class AggregateBound(C.Structure):
+    _fields_ = [("lb", C.c_double), ("hull_ub", C.c_double), ("feasible", C.c_int32), ("reserved", C.c_int32)]
+
+
 class SolveOptions(C.Structure):
     _fields_ = [
         ("iter_limit", C.c_uint64), ("batch_iter_limit", C.c_uint64), ("tolerance", C.c_double),

@@ -35,6 +35,7 @@ SIGNATURES = {
     "cmn_role_n_elements": (U64, [P]),
     "cmn_bound": (I32, [P, P, P, P, C.POINTER(C.POINTER(C.c_uint8)), C.POINTER(C.POINTER(D)), C.POINTER(U64)]),
     "cmn_sample": (I32, [P, P, P, P, U64, C.POINTER(A.Candidate)]),
+    "cmn_bound_children": (I32, [P, P, P, P, U64, C.POINTER(C.POINTER(A.AggregateBound))]),
     "cmn_enumerate": (I32, [P, P, P, P, C.POINTER(A.Candidate)]),
     "cmn_sample_noalloc": (I32, [P, P, I64, U64, U64, P, P, P, U64, C.POINTER(A.Candidate), P, P]),
     "cmn_eval_boxes": (I32, [P, I32, P, P, U64, U64, P, P, P, I32, P]),

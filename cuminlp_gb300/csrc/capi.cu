@@ -255,12 +255,20 @@ struct cmn_role {
   double* h_lb = nullptr;
   double* h_point = nullptr;
   Cand* h_cand = nullptr;
+  // aggregate bounds: 2k fold keys on the device and host, k results
+  unsigned long long* d_agg = nullptr;
+  unsigned long long* h_agg = nullptr;
+  cmn_aggregate_bound* h_agg_out = nullptr;
+  uint64_t agg_cap = 0;
 
   ~cmn_role()
   {
     int cur = 0;
     if (p && cudaGetDevice(&cur) == cudaSuccess && cur != p->device) cudaSetDevice(p->device);
     if (stream) cudaStreamSynchronize(stream);
+    dfree(d_agg);
+    if (h_agg) cudaFreeHost(h_agg);
+    if (h_agg_out) cudaFreeHost(h_agg_out);
     dfree(d_stage);
     dfree(d_feas);
     dfree(d_lb);
@@ -461,6 +469,96 @@ extern "C" cmn_status cmn_bound(cmn_role* r, const double* box, const uint64_t* 
   if (feasible) *feasible = r->h_feas;
   if (obj_lb) *obj_lb = r->h_lb;
   if (n_regions) *n_regions = r->n_regions;
+  return CMN_OK;
+}
+
+// total order of doubles used by the aggregate fold (NaN above +inf)
+static uint64_t host_key(double x)
+{
+  uint64_t u;
+  std::memcpy(&u, &x, 8);
+  if (x != x) return ~0ULL;
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ULL);
+}
+
+static double host_unkey(uint64_t k)
+{
+  const uint64_t u = (k >> 63) ? (k & 0x7fffffffffffffffULL) : ~k;
+  double x;
+  std::memcpy(&x, &u, 8);
+  return x;
+}
+
+extern "C" cmn_status cmn_bound_children(cmn_role* r, const double* box, const uint64_t* var_ids,
+                                          const uint64_t* widths, uint64_t k, const cmn_aggregate_bound** out)
+{
+  if (!r || !out) return fail(CMN_INVALID_CONFIGURATION, "null argument");
+  if (r->kind != CMN_ROLE_BOUNDER)
+    return fail(CMN_INVALID_CONFIGURATION, "aggregate bounds need a role built as a bounder");
+  if (k == 0 || r->n_regions % k != 0)
+    return fail(CMN_SHAPE_MISMATCH, "k (" + std::to_string(k) + ") must divide the role's n_regions (" +
+                                        std::to_string(r->n_regions) + ")");
+  CK(cudaSetDevice(r->p->device));
+  cmn_status st = stage_region(r, box, var_ids, widths);
+  if (st != CMN_OK) return st;
+  if (k > r->agg_cap) {
+    dfree(r->d_agg);
+    if (r->h_agg) cudaFreeHost(r->h_agg);
+    if (r->h_agg_out) cudaFreeHost(r->h_agg_out);
+    r->d_agg = nullptr;
+    r->h_agg = nullptr;
+    r->h_agg_out = nullptr;
+    r->agg_cap = 0;
+    CK(dalloc(&r->d_agg, 2 * k));
+    CK(cudaMallocHost(reinterpret_cast<void**>(&r->h_agg), 2 * k * sizeof(unsigned long long)));
+    CK(cudaMallocHost(reinterpret_cast<void**>(&r->h_agg_out), k * sizeof(cmn_aggregate_bound)));
+    r->agg_cap = k;
+  }
+  // identities: every region excluded leaves (+inf, -inf)
+  for (uint64_t c = 0; c < k; ++c) {
+    r->h_agg[c] = host_key(INFINITY);
+    r->h_agg[k + c] = host_key(-INFINITY);
+  }
+  CK(cudaMemcpyAsync(r->d_agg, r->h_agg, 2 * k * sizeof(unsigned long long), cudaMemcpyHostToDevice, r->stream));
+  EvalArgs a = {};
+  const double *plo, *phi;
+  const SlotPlan* sp;
+  const ParentInfo* pi;
+  role_ptrs(r, plo, phi, sp, pi);
+  a.prog = r->p->d_prog64;
+  a.prog_len = (int)r->p->prog.code64.size();
+  a.n_vars = (int)r->p->host.n_vars();
+  a.n_slots = r->p->prog.n_slots;
+  a.log2C = -1;
+  a.plo = plo;
+  a.phi = phi;
+  a.pstride = 1;
+  a.pinfo = pi;
+  a.slots = sp;
+  a.max_slots = (int)r->slot_kinds.size();
+  a.n_children = r->n_regions;
+  a.sched = r->p->d_sched;
+  a.g_max = r->p->prog.group_max;
+  a.capacity = (uint64_t)r->grid * kEvalThreads;
+  a.agg_keys = r->d_agg;
+  a.agg_m = r->n_regions / k;
+  a.agg_k = k;
+  CK(launch_eval(a, 4, false, r->grid, kEvalThreads, r->stream));
+  CK(cudaMemcpyAsync(r->h_agg, r->d_agg, 2 * k * sizeof(unsigned long long), cudaMemcpyDeviceToHost, r->stream));
+  CK(cudaStreamSynchronize(r->stream));
+  for (uint64_t c = 0; c < k; ++c) {
+    const double lb = host_unkey(r->h_agg[c]);
+    const double ub = host_unkey(r->h_agg[k + c]);
+    // replay.cuh:343-361: a child whose Max is still -inf had every region
+    // excluded; it is normalised to (+inf, +inf, infeasible)
+    const bool feasible = ub > -INFINITY;
+    cmn_aggregate_bound& o = r->h_agg_out[c];
+    o.lb = feasible ? lb : INFINITY;
+    o.hull_ub = feasible ? ub : INFINITY;
+    o.feasible = feasible ? 1 : 0;
+    o.reserved = 0;
+  }
+  *out = r->h_agg_out;
   return CMN_OK;
 }
 

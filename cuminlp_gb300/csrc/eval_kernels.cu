@@ -103,6 +103,38 @@ __device__ __forceinline__ void write_verdict(const EvalArgs& a, uint64_t g, con
   }
 }
 
+// Aggregate bounder (backend/aggregate/kernels.cuh:32-47 mask and the
+// replay's per-child Min/Max, replay.cuh:497-556), fused: region r belongs
+// to child r / agg_m; infeasible regions count as lb = +inf, ub = -inf.
+// Minimum and maximum follow the total order of lb_key.  A warp whose
+// active lanes share one child combines them before one pair of atomics.
+// Every lane of the warp calls this.
+__device__ __forceinline__ void aggregate_fold(const EvalArgs& a, bool active, uint64_t r, const Verdict<double>& v)
+{
+  const unsigned c = active ? (unsigned)(r / a.agg_m) : 0xffffffffu;
+  unsigned long long kmin = lb_key(active && v.feasible ? v.obj.lo : INFINITY);
+  unsigned long long kmax = lb_key(active && v.feasible ? v.obj.hi : -INFINITY);
+  const unsigned any = __ballot_sync(0xffffffffu, active);
+  if (any == 0) return;
+  const unsigned cmin = __reduce_min_sync(0xffffffffu, c);
+  const unsigned cmax = __reduce_max_sync(0xffffffffu, active ? c : 0u);
+  if (cmin == cmax) {
+    for (int off = 16; off > 0; off >>= 1) {
+      const unsigned long long a1 = __shfl_xor_sync(0xffffffffu, kmin, off);
+      const unsigned long long b1 = __shfl_xor_sync(0xffffffffu, kmax, off);
+      kmin = a1 < kmin ? a1 : kmin;
+      kmax = b1 > kmax ? b1 : kmax;
+    }
+    if ((threadIdx.x & 31) == (unsigned)(__ffs(any) - 1)) {
+      atomicMin(a.agg_keys + cmin, kmin);
+      atomicMax(a.agg_keys + a.agg_k + cmin, kmax);
+    }
+  } else if (active) {
+    atomicMin(a.agg_keys + c, kmin);
+    atomicMax(a.agg_keys + a.agg_k + c, kmax);
+  }
+}
+
 // Groups of 2^lg consecutive lanes share one child: each lane runs its
 // segments of the program and the group combines the verdicts.  The loop
 // bound is per block, so every lane of a warp reaches the shuffles.
@@ -121,7 +153,7 @@ __device__ void eval_children_grouped(const EvalArgs& a, const S* plo, const S* 
     if (live) {
       g = (kMode == 3) ? (uint64_t)a.list[idx] : idx;
       child_of(a.log2C, g, k, r);
-      if (kMode != 0 && a.pinfo != nullptr) {
+      if (kMode != 0 && kMode != 4 && a.pinfo != nullptr) {
         const ParentInfo pi = a.pinfo[k];
         if (pi.fathom || r >= pi.nreg) {
           if (kMode != 3 && lane == 0) a.out_flag[g] = kChildNone;
@@ -141,15 +173,21 @@ __device__ void eval_children_grouped(const EvalArgs& a, const S* plo, const S* 
     if (live) {
       bool dup;
       const ChildVars<T, S> cv = child_vars<T, S>(a, plo, phi, k, r, olo, ohi, ovid, B, dup);
-      if (kMode != 0 && dup) {
+      if (kMode != 0 && kMode != 4 && dup) {
         if (lane == 0) a.out_flag[g] = kChildDuplicate;
         live = false;
-      } else {
+      } else if (lg > 0) {
         v = run_interval_lane<T, ChildVars<T, S>>(a.prog, a.sched, lg, lane, cv, t);
+      } else {  // one lane per box (the aggregate fold's loop): the whole program
+        v = run_interval<T, ChildVars<T, S>>(a.prog, a.prog_len, cv, t);
       }
     }
     v = group_verdict<T>(v, G);
-    if (live && lane == 0) write_verdict<T, kMode>(a, g, v, gub);
+    if constexpr (kMode == 4) {
+      aggregate_fold(a, live && lane == 0, r, v);
+    } else {
+      if (live && lane == 0) write_verdict<T, kMode>(a, g, v, gub);
+    }
   }
 }
 
@@ -185,7 +223,7 @@ __device__ __forceinline__ void eval_children(const EvalArgs& a, const S* plo, c
   const bool pass_through = kMode == 2 && a.use_screen != nullptr && *a.use_screen == 0;
 
   const int lg = a.sched != nullptr ? lanes_per_box(total, a.capacity, a.g_max) : 0;
-  if (lg > 0) {
+  if (lg > 0 || kMode == 4) {  // the aggregate fold needs whole warps: the grouped loop, even at one lane
     eval_children_grouped<T, kMode, S>(a, plo, phi, total, gub, pass_through, lg, t, olo, ohi, ovid);
     return;
   }
@@ -552,6 +590,7 @@ cudaError_t set_eval_kernel_attributes(int max_smem)
   cudaError_t e = allow_dynamic_smem(eval_children_kernel<double, 0>, max_smem);
   if (e == cudaSuccess) e = allow_dynamic_smem(eval_children_kernel<double, 1>, max_smem);
   if (e == cudaSuccess) e = allow_dynamic_smem(eval_children_kernel<double, 3>, max_smem);
+  if (e == cudaSuccess) e = allow_dynamic_smem(eval_children_kernel<double, 4>, max_smem);
   if (e == cudaSuccess) e = allow_dynamic_smem(eval_children_kernel<float, 0>, max_smem);
   if (e == cudaSuccess) e = allow_dynamic_smem(eval_children_kernel<float, 2>, max_smem);
   if (e == cudaSuccess) e = allow_dynamic_smem(sample_children_kernel, max_smem);
@@ -597,6 +636,7 @@ cudaError_t launch_eval(const EvalArgs& a, int mode, bool fp32, int grid, int th
   }
   if (mode == 0) return launch_eval_t<double, 0>(a, grid, threads, s);
   if (mode == 1) return launch_eval_t<double, 1>(a, grid, threads, s);
+  if (mode == 4) return launch_eval_t<double, 4>(a, grid, threads, s);
   return launch_eval_t<double, 3>(a, grid, threads, s);
 }
 

@@ -80,6 +80,11 @@ struct EvalArgs {
   double* out_lb;
   double* out_ub;
   uint8_t* out_flag;  // role/raw: feasible; solver: ChildState
+  // aggregate bounder: child c = r / agg_m folds into agg_keys[c] (min lb
+  // key) and agg_keys[agg_k + c] (max ub key)
+  unsigned long long* agg_keys;
+  uint64_t agg_m;
+  uint64_t agg_k;
 };
 
 struct SampleArgs {

@@ -17,7 +17,8 @@ size_t eval_smem_bytes(int n_slots, int max_slots, bool fp32, int threads);
 size_t sample_smem_bytes(int n_vars, int n_slots, int threads);
 
 // mode 0: role / raw boxes; 1: solver FP64; 2: solver FP32 screen (fp32
-// must be true); 3: solver FP64 certify over EvalArgs::list
+// must be true); 3: solver FP64 certify over EvalArgs::list; 4: aggregate
+// bounder (FP64, per-child fold into EvalArgs::agg_keys)
 cudaError_t launch_eval(const EvalArgs& a, int mode, bool fp32, int grid, int threads, cudaStream_t s);
 cudaError_t launch_sample(const SampleArgs& a, int grid, int threads, cudaStream_t s);
 cudaError_t launch_reduce_cand(const Cand* block_best, int n, Cand* out, cudaStream_t s);

@@ -139,6 +139,17 @@ class Bounder(_Role):
         nr = n.value
         return _view(fp, C.c_uint8, nr, self, np.uint8), _view(lp, C.c_double, nr, self, np.float64)
 
+    def bound_children(self, box, var_ids, widths, k: int):
+        """(lb, hull_ub, feasible) of the k children of this region: region r
+        belongs to child r // (n_regions // k) (AggregateBounder::bound_children)."""
+        out = C.POINTER(A.AggregateBound)()
+        check(lib().cmn_bound_children(self.handle, *self._args(box, var_ids, widths), int(k), C.byref(out)))
+        arr = (A.AggregateBound * int(k)).from_address(C.cast(out, C.c_void_p).value)
+        lb = np.array([arr[i].lb for i in range(k)])
+        ub = np.array([arr[i].hull_ub for i in range(k)])
+        fe = np.array([arr[i].feasible for i in range(k)], dtype=np.int32)
+        return lb, ub, fe
+
 
 class Sampler(_Role):
     kind = A.ROLE_SAMPLER

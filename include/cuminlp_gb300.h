@@ -356,6 +356,31 @@ typedef struct cmn_outcome {
   cmn_counters counters;
 } cmn_outcome;
 
+/* aggregate::AggregateBound (aggregate/bound.hpp:40-59).  `hull_ub` is
+ * not an incumbent: it bounds the objective over the child's unexcluded
+ * part, at no known point. */
+typedef struct cmn_aggregate_bound {
+  double lb;       /* min objective lb over the child's feasible regions */
+  double hull_ub;  /* max objective ub over them */
+  int32_t feasible;
+  int32_t reserved;
+} cmn_aggregate_bound;
+
+/* Replaces AggregateBounder::bound_children (aggregate/bound.hpp:84-105;
+ * the AggregateBounderReplay launch and fold, backend/aggregate/
+ * replay.cuh:320-361, 497-556, with mask_bounds_kernel,
+ * backend/aggregate/kernels.cuh:32-47) for one region.  `role` is a bounder
+ * of N regions; region r belongs to child r / (N / k), which is how the
+ * reference lays out a partition's launch slots (refine slots first, branch
+ * slots last: aggregate/partition.hpp).  The per-region verdicts are folded
+ * on the device and only k results cross to the host.  Minimum and maximum
+ * follow IEEE total order on equal magnitudes (-0 below +0).  A child whose
+ * regions are all excluded is (+inf, +inf, feasible = 0).  `out` is a view
+ * of k entries, valid until the next call on the role. */
+cmn_status cmn_bound_children(cmn_role* role, const double* box,
+                              const uint64_t* var_ids, const uint64_t* widths,
+                              uint64_t k, const cmn_aggregate_bound** out);
+
 /* Fills `opts` with the defaults (SearchDriver defaults where they exist:
  * driver.hpp:97-109). */
 void cmn_solve_options_default(cmn_solve_options* opts);

@@ -49,6 +49,7 @@ _SIG = {
     "orc_sample_continuous_f32": (F, [F, F, U64, U64, U64, U64]),
     "orc_sample_discrete_f32": (F, [F, F, U64, U64, U64, U64]),
     "orc_bound": (I32, [P, P, P, P, P, I64, U64, P, P, I32]),
+    "orc_aggregate_bound": (I32, [P, P, P, P, P, I64, U64, U64, P, P, P, I32]),
     "orc_sample": (I32, [P, P, P, P, P, I64, U64, U64, U64, C.POINTER(I32), C.POINTER(D), C.POINTER(I64), P, I32]),
     "orc_enumerate": (I32, [P, P, P, P, P, I64, U64, C.POINTER(I32), C.POINTER(D), C.POINTER(I64), P, I32]),
     "orc_bisection_choose": (I64, [P, P, I64, I64, I64, I64, I32, P, P, P, P]),
@@ -165,6 +166,18 @@ class OracleProblem:
                            threads or threads_default()):
             raise ValueError(lib().orc_last_error().decode())
         return fe, lb
+
+    def aggregate_bound(self, box, kinds, var_ids, widths, n_regions, k, threads=None):
+        """(lb, hull_ub, feasible) per child: k children of n_regions / k regions."""
+        box = np.ascontiguousarray(box, dtype=np.float64)
+        kk, v, w = self._slots(kinds, var_ids, widths)
+        lb = np.empty(k)
+        ub = np.empty(k)
+        fe = np.empty(k, dtype=np.int32)
+        if lib().orc_aggregate_bound(self.h, A.ptr(box), A.ptr(kk), A.ptr(v), A.ptr(w), len(kk), n_regions, k,
+                                     A.ptr(lb), A.ptr(ub), A.ptr(fe), threads or threads_default()):
+            raise ValueError(lib().orc_last_error().decode())
+        return lb, ub, fe
 
     def sample(self, box, kinds, var_ids, widths, n_regions, sample_points, salt, threads=None):
         box = np.ascontiguousarray(box, dtype=np.float64)

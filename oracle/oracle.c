@@ -1051,6 +1051,7 @@ typedef struct {
   const slots_t* s;
   uint8_t* feas;
   double* obj_lb;
+  double* obj_ub; /* optional */
   int failed;
   /* sampling / enumerate */
   uint64_t S, salt;
@@ -1072,6 +1073,7 @@ static void bound_range(void* vc, int64_t r0, int64_t r1, int tid)
     double lb, ub;
     c->feas[r] = (uint8_t)verdict_d(p, val, &lb, &ub);
     c->obj_lb[r] = lb;
+    if (c->obj_ub) c->obj_ub[r] = ub;
   }
   free(cb);
   free(val);
@@ -1117,6 +1119,86 @@ int orc_bound(const orc_problem* p, const double* box,
     return -1;
   }
   return 0;
+}
+
+/* Aggregate bounder (backend/aggregate/kernels.cuh:32-47 mask,
+ * backend/aggregate/replay.cuh:343-361 fold, :497-556 reductions):
+ * region r belongs to child r / M (M = n_regions / k); a child's lb is the
+ * minimum objective lower bound over its feasible regions (+inf when none),
+ * its hull_ub the maximum upper bound (-inf when none); a child with
+ * hull_ub == -inf is infeasible and normalised to (+inf, +inf).  Minimum and
+ * maximum follow the total order of lb_key (-0 below +0, NaN above +inf),
+ * which fixes the one choice CUB's Min/Max leave to reduction order. */
+static inline uint64_t agg_key(double x)
+{
+  uint64_t u = dbits(x);
+  if (x != x) return UINT64_MAX;
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ULL);
+}
+
+static inline double agg_unkey(uint64_t k)
+{
+  uint64_t u = (k >> 63) ? (k & 0x7fffffffffffffffULL) : ~k;
+  return bitsd(u);
+}
+
+int orc_aggregate_bound(const orc_problem* p, const double* box,
+                        const uint8_t* slot_kinds, const uint64_t* var_ids,
+                        const uint64_t* widths, int64_t slot_count,
+                        uint64_t n_regions, uint64_t k, double* child_lb,
+                        double* child_hull_ub, int32_t* child_feasible,
+                        int threads)
+{
+  if (k == 0 || n_regions % k != 0) {
+    set_err("k must divide n_regions");
+    return -1;
+  }
+  slots_t s;
+  if (slot_count > 64) {
+    set_err("slot count above 64");
+    return -1;
+  }
+  slots_init(&s, slot_kinds, var_ids, widths, slot_count);
+  if (check_widths(&s, n_regions)) {
+    set_err("widths do not multiply out to n_regions");
+    return -1;
+  }
+  uint8_t* feas = (uint8_t*)malloc(n_regions);
+  double* lb = (double*)malloc(sizeof(double) * n_regions);
+  double* ub = (double*)malloc(sizeof(double) * n_regions);
+  role_ctx c;
+  memset(&c, 0, sizeof c);
+  c.p = p;
+  c.box = box;
+  c.s = &s;
+  c.feas = feas;
+  c.obj_lb = lb;
+  c.obj_ub = ub;
+  parallel_for((int64_t)n_regions, threads, bound_range, &c);
+  int rc = 0;
+  if (c.failed) {
+    set_err("op without an interval implementation");
+    rc = -1;
+  }
+  const uint64_t M = n_regions / k;
+  for (uint64_t ch = 0; ch < k && rc == 0; ++ch) {
+    uint64_t kmin = agg_key(INFINITY), kmax = agg_key(-INFINITY);
+    for (uint64_t r = ch * M; r < (ch + 1) * M; ++r) {
+      const uint64_t a = agg_key(feas[r] ? lb[r] : INFINITY);
+      const uint64_t b = agg_key(feas[r] ? ub[r] : -INFINITY);
+      if (a < kmin) kmin = a;
+      if (b > kmax) kmax = b;
+    }
+    const double clb = agg_unkey(kmin), cub = agg_unkey(kmax);
+    const int f = cub > -INFINITY;
+    child_lb[ch] = f ? clb : INFINITY;
+    child_hull_ub[ch] = f ? cub : INFINITY;
+    child_feasible[ch] = f;
+  }
+  free(feas);
+  free(lb);
+  free(ub);
+  return rc;
 }
 
 /* Sampled point of (region r, sample i): every variable is drawn from its

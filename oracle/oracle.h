@@ -91,6 +91,14 @@ int orc_bound(const orc_problem* p, const double* box,
               const uint8_t* slot_kinds, const uint64_t* var_ids,
               const uint64_t* widths, int64_t slot_count, uint64_t n_regions,
               uint8_t* feasible, double* obj_lb, int threads);
+/* AggregateBounder::bound_children for one region: k children of
+ * n_regions / k contiguous regions each. */
+int orc_aggregate_bound(const orc_problem* p, const double* box,
+                        const uint8_t* slot_kinds, const uint64_t* var_ids,
+                        const uint64_t* widths, int64_t slot_count,
+                        uint64_t n_regions, uint64_t k, double* child_lb,
+                        double* child_hull_ub, int32_t* child_feasible,
+                        int threads);
 int orc_sample(const orc_problem* p, const double* box,
                const uint8_t* slot_kinds, const uint64_t* var_ids,
                const uint64_t* widths, int64_t slot_count,

@@ -10,6 +10,7 @@ import pytest
 
 import oracle as O
 from cuminlp_gb300 import generators as G
+from cuminlp_gb300 import report
 from cuminlp_gb300.solver import DeviceProblem, Solver
 from tests.conftest import bits_equal
 from tests.test_oracle_pins import contract_model, fixture_problems
@@ -57,6 +58,7 @@ def compare(p, iterations, **opts):
         assert g["counters"][k] == o["counters"][k], k
     if o["upper_bound"] < np.finfo(np.float64).max:
         assert bits_equal(g["best_point"], o["best_point"])
+    assert report.balances(g)  # RunTelemetry::balances on the device's counters
     s.close()
     return g
 

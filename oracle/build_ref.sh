@@ -17,4 +17,8 @@ CXX=${CXX:-g++}
 "$CC" -O2 -std=c11 -ffp-contract=off -fPIC -c "$HERE/oracle.c" -o "$OUT/oracle.o"
 "$CXX" -O2 -std=c++20 -mfma -ffp-contract=fast -I"$HERE/ref_shim" -I"$REF/include" -I"$HERE" \
   "$HERE/ref_harness.cpp" "$OUT/oracle.o" -o "$OUT/ref_harness" -lm -lpthread
-echo "$OUT/ref_harness"
+# the reference's GAMS frontend, without contraction (its constant folding is
+# plain IEEE arithmetic on the host)
+"$CXX" -O2 -std=c++20 -ffp-contract=off -I"$HERE/ref_shim" -I"$REF/include" -I"$REF/source/gams" \
+  "$REF/source/gams/frontend.cpp" "$HERE/ref_gams.cpp" -o "$OUT/ref_gams" -lm
+echo "$OUT/ref_harness $OUT/ref_gams"

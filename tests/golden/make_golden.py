@@ -201,12 +201,24 @@ def driver_cases(problems):
     return res
 
 
+def gams_cases():
+    """The reference frontend's lowering of this repository's own .gms
+    models (tests/data/gams), as oracle/_ref/ref_gams prints it."""
+    out = {}
+    for f in sorted((ROOT / "tests" / "data" / "gams").glob("*.gms")):
+        res = subprocess.run([str(ROOT / "oracle" / "_ref" / "ref_gams"), str(f)], capture_output=True, text=True,
+                             check=True)
+        out[f.name] = res.stdout.splitlines()
+    return out
+
+
 def main():
     if not HARNESS.exists():
         raise SystemExit("oracle/_ref/ref_harness missing: run oracle/build_ref.sh first")
     (HERE / "decode.json").write_text(json.dumps(decode_cases(), indent=0))
     (HERE / "policy.json").write_text(json.dumps(policy_cases(), indent=0))
     (HERE / "driver.json").write_text(json.dumps(driver_cases(fixture_problems()), indent=1))
+    (HERE / "gams.json").write_text(json.dumps(gams_cases(), indent=1))
     print("golden fixtures written")
 
 

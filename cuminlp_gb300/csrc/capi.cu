@@ -17,6 +17,7 @@
 #include "kernels.cuh"
 #include "batch.hpp"
 #include "launch.hpp"
+#include "policy.cuh"
 #include "program.hpp"
 #include "search.hpp"
 
@@ -217,6 +218,61 @@ static cmn_status check_smem(const cmn_problem* p, bool fp32, int max_slots)
 static uint64_t role_fixed_bytes(const cmn_problem* p)
 {
   return (uint64_t)(16 * p->host.n_vars() + 64 * 48 + 4096 * sizeof(Cand) + 8 * p->host.n_vars());
+}
+
+// ----------------------------------------------------------------------
+// host-side policy and decode, for drivers that run on the host
+// ----------------------------------------------------------------------
+extern "C" cmn_status cmn_bisection_choose(const double* box, const int32_t* var_kinds, int64_t n_vars,
+                                           int32_t budget_bits, uint64_t max_cycle_size, uint64_t enumerate_cap,
+                                           int32_t relative_width, uint8_t* slot_kinds, uint64_t* var_ids,
+                                           uint64_t* widths, uint64_t* domain_sizes, int64_t* slot_count,
+                                           int32_t* fathom)
+{
+  if (n_vars < 0 || (n_vars > 0 && (!box || !var_kinds)) || !slot_kinds || !var_ids || !widths || !domain_sizes ||
+      !slot_count)
+    return fail(CMN_INVALID_CONFIGURATION, "null argument");
+  if (budget_bits < 1 || budget_bits > 62)
+    return fail(CMN_INVALID_CONFIGURATION, "bisection budget must be within [1, 62]");
+  if (max_cycle_size > 64) return fail(CMN_INVALID_CONFIGURATION, "max_cycle_size exceeds kMaxSlots (64)");
+  try {
+    std::vector<EnumCand> ec((size_t)std::max<int64_t>(n_vars, 1));
+    std::vector<BisCand> bc((size_t)std::max<int64_t>(n_vars, 1));
+    std::vector<uint64_t> heap((size_t)std::max<int64_t>(n_vars, 1));
+    std::vector<SlotPlan> sp((size_t)budget_bits);
+    const PolicyParams pp = {budget_bits, (int64_t)max_cycle_size, (int64_t)enumerate_cap, relative_width};
+    // the interleaved box read as two planes of stride 2
+    const ParentInfo pi = bisection_policy(box, box + 1, 2, (int)n_vars, var_kinds, pp, ec.data(), bc.data(),
+                                           heap.data(), sp.data());
+    for (uint32_t j = 0; j < pi.count; ++j) {
+      slot_kinds[j] = (uint8_t)sp[j].kind;
+      var_ids[j] = sp[j].vid;
+      widths[j] = sp[j].width;
+      domain_sizes[j] = sp[j].dom;
+    }
+    *slot_count = pi.count;
+    if (fathom) *fathom = (int32_t)pi.fathom;
+    return CMN_OK;
+  } catch (const std::bad_alloc&) {
+    return fail(CMN_INTERNAL, "host allocation failed");
+  }
+}
+
+extern "C" void cmn_slot_bounds(int32_t kind, double plo, double phi, uint64_t part, uint64_t fan_out, double* lo,
+                                double* hi)
+{
+  if (!lo || !hi) return;
+  if (kind == CMN_SLOT_INTEGER_ENUMERATE || kind == CMN_SLOT_BINARY_ENUMERATE) {
+    double value = std::ceil(plo) + (double)part;
+    if (value > phi) value = phi;
+    *lo = value;
+    *hi = value;
+    return;
+  }
+  // the device's FMA form (region/decode.hpp:44-71 as nvcc compiles it)
+  const double width = (phi - plo) / (double)fan_out;
+  *lo = std::fma(width, (double)part, plo);
+  *hi = (part + 1 == fan_out) ? phi : std::fma(width, (double)(part + 1), plo);
 }
 
 extern "C" cmn_status cmn_cost_model_get(const cmn_problem* p, cmn_cost_model* out)

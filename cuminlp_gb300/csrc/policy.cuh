@@ -16,6 +16,19 @@
 
 namespace cmn {
 
+// The policy runs on the device (one thread per parent) and on the host
+// (cmn_bisection_choose, for host-side drivers): the same source, with the
+// round-to-nearest FP64 operations spelled once for both.
+#ifdef __CUDA_ARCH__
+#define CMN_POLICY_SUB(a, b) __dsub_rn((a), (b))
+#define CMN_POLICY_DIV(a, b) __ddiv_rn((a), (b))
+#define CMN_POLICY_D2U(x) __double2ull_rz(x)
+#else
+#define CMN_POLICY_SUB(a, b) ((a) - (b))
+#define CMN_POLICY_DIV(a, b) ((a) / (b))
+#define CMN_POLICY_D2U(x) ((unsigned long long)(x))
+#endif
+
 struct EnumCand {
   uint64_t vid, domain, bits;
   uint32_t kind, pad;
@@ -29,11 +42,11 @@ struct BisCand {
 struct HeapCtx {
   const BisCand* c;
   int relative;
-  __device__ double key(uint64_t i) const { return relative ? __ddiv_rn(c[i].live, c[i].orig) : c[i].live; }
-  __device__ bool less(uint64_t a, uint64_t b) const { return key(a) < key(b); }
+  __host__ __device__ double key(uint64_t i) const { return relative ? CMN_POLICY_DIV(c[i].live, c[i].orig) : c[i].live; }
+  __host__ __device__ bool less(uint64_t a, uint64_t b) const { return key(a) < key(b); }
 };
 
-__device__ inline void hp_push_hole(uint64_t* f, int64_t hole, int64_t top, uint64_t value, const HeapCtx& h)
+__host__ __device__ inline void hp_push_hole(uint64_t* f, int64_t hole, int64_t top, uint64_t value, const HeapCtx& h)
 {
   int64_t parent = (hole - 1) / 2;
   while (hole > top && h.less(f[parent], value)) {
@@ -44,7 +57,7 @@ __device__ inline void hp_push_hole(uint64_t* f, int64_t hole, int64_t top, uint
   f[hole] = value;
 }
 
-__device__ inline void hp_adjust(uint64_t* f, int64_t hole, int64_t len, uint64_t value, const HeapCtx& h)
+__host__ __device__ inline void hp_adjust(uint64_t* f, int64_t hole, int64_t len, uint64_t value, const HeapCtx& h)
 {
   const int64_t top = hole;
   int64_t second = hole;
@@ -62,7 +75,7 @@ __device__ inline void hp_adjust(uint64_t* f, int64_t hole, int64_t len, uint64_
   hp_push_hole(f, hole, top, value, h);
 }
 
-__device__ inline void hp_make(uint64_t* f, int64_t len, const HeapCtx& h)
+__host__ __device__ inline void hp_make(uint64_t* f, int64_t len, const HeapCtx& h)
 {
   if (len < 2) return;
   int64_t parent = (len - 2) / 2;
@@ -74,14 +87,14 @@ __device__ inline void hp_make(uint64_t* f, int64_t len, const HeapCtx& h)
   }
 }
 
-__device__ __forceinline__ uint64_t int_domain(double lb, double ub)
+__host__ __device__ inline uint64_t int_domain(double lb, double ub)
 {
   const double lo = ceil(lb), hi = floor(ub);
   if (hi < lo) return 0;
-  return (uint64_t)__double2ull_rz(__dsub_rn(hi, lo)) + 1;
+  return (uint64_t)CMN_POLICY_D2U(CMN_POLICY_SUB(hi, lo)) + 1;
 }
 
-__device__ __forceinline__ uint64_t bits_for(uint64_t d)
+__host__ __device__ inline uint64_t bits_for(uint64_t d)
 {
   const uint64_t eff = d == 0 ? 1 : d;
   uint64_t bits = 0, cap = 1;
@@ -101,7 +114,7 @@ struct PolicyParams {
 
 // Variable v of the parent box is (plo[v * stride], phi[v * stride]).
 // `ec`, `bc`, `heap` are scratch of n entries; `sp` receives the slots.
-__device__ inline ParentInfo bisection_policy(const double* __restrict__ plo, const double* __restrict__ phi,
+__host__ __device__ inline ParentInfo bisection_policy(const double* __restrict__ plo, const double* __restrict__ phi,
                                               uint64_t stride, int n, const int32_t* __restrict__ kinds,
                                               const PolicyParams& pp, EnumCand* ec, BisCand* bc, uint64_t* heap,
                                               SlotPlan* sp)
@@ -113,7 +126,7 @@ __device__ inline ParentInfo bisection_policy(const double* __restrict__ plo, co
   for (int v = 0; v < n && ne + nb < cap; ++v) {
     const double lb = plo[(uint64_t)v * stride], ub = phi[(uint64_t)v * stride];
     if (!(ub > lb)) continue;
-    const double w = __dsub_rn(ub, lb);
+    const double w = CMN_POLICY_SUB(ub, lb);
     const int vk = kinds[v];
     if (vk == CMN_VAR_BINARY) {
       ec[ne] = {(uint64_t)v, 2, bits_for(2), (uint32_t)CMN_SLOT_BINARY_ENUMERATE, 0};
@@ -158,7 +171,7 @@ __device__ inline ParentInfo bisection_policy(const double* __restrict__ plo, co
   for (int64_t i = taken; i < ne; ++i) {
     if (ec[i].kind == CMN_SLOT_INTEGER_ENUMERATE) {
       const uint64_t v = ec[i].vid;
-      const double w = __dsub_rn(phi[v * stride], plo[v * stride]);
+      const double w = CMN_POLICY_SUB(phi[v * stride], plo[v * stride]);
       bc[nb] = {v, 0, w, w, (uint32_t)CMN_SLOT_INTEGER_PARTITION, 0};
       ++nb;
     }
@@ -175,7 +188,7 @@ __device__ inline ParentInfo bisection_policy(const double* __restrict__ plo, co
       hp_adjust(heap, 0, nb - 1, v, h);
     }
     BisCand* c = &bc[heap[nb - 1]];
-    c->live = __ddiv_rn(c->live, 2.0);
+    c->live = CMN_POLICY_DIV(c->live, 2.0);
     ++c->bis;
     hp_push_hole(heap, nb - 1, 0, heap[nb - 1], h);
   }

@@ -169,6 +169,26 @@ typedef struct cmn_cost_model {
  * and graph::cost_model_for (backend/graph/cost.hpp:83-99). */
 cmn_status cmn_cost_model_get(const cmn_problem* problem, cmn_cost_model* out);
 
+/* Host-side policy and decode, for drivers that run on the host.
+ *
+ * Replaces BisectionBudgetCompositionPolicy::choose
+ * (policy/bisection_budget.hpp:81-262) on one box (interleaved (lb, ub),
+ * n_vars pairs): writes up to 64 slots (kinds, var_ids, widths, domain
+ * sizes) and their count; `fathom` (may be NULL) is 1 when every live
+ * variable is enumerated.  Ties resolve in the reference's heap order, as
+ * the device policy does. */
+cmn_status cmn_bisection_choose(const double* box, const int32_t* var_kinds,
+                                int64_t n_vars, int32_t budget_bits,
+                                uint64_t max_cycle_size, uint64_t enumerate_cap,
+                                int32_t relative_width, uint8_t* slot_kinds,
+                                uint64_t* var_ids, uint64_t* widths,
+                                uint64_t* domain_sizes, int64_t* slot_count,
+                                int32_t* fathom);
+/* region::decode::slot_bounds (region/decode.hpp:44-71) in the FMA form the
+ * device evaluates. */
+void cmn_slot_bounds(int32_t kind, double plo, double phi, uint64_t part,
+                     uint64_t fan_out, double* lo, double* hi);
+
 /* ---------------------------------------------------------------------
  * Region roles: the plugin boundary of the reference
  * (backend/backend.hpp:81-219).  A role is built once per Composition

@@ -14,6 +14,8 @@
 //   decode  <in> <out>   lines "kind plo phi part fan" -> "lo hi"
 //   policy  <in> <out>   BisectionBudget / GreedyEnum choose() cases
 //   driver  <in> <out>   SearchDriver::solve on a problem file
+//   aggdriver <in> <out> AggregateDriver::solve (WidestBranchPolicy) on a
+//                        problem file, the oracle behind its roles
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
@@ -23,6 +25,7 @@
 #include <string>
 #include <vector>
 
+#include "cuminlp/aggregate/driver.hpp"
 #include "cuminlp/backend/backend.hpp"
 #include "cuminlp/model/problem.hpp"
 #include "cuminlp/policy/bisection_budget.hpp"
@@ -314,6 +317,106 @@ static int cmd_driver(std::istream& in, std::ostream& out)
   return 0;
 }
 
+// ---- aggregate roles over the oracle ---------------------------------------
+class OAggBounder : public aggregate::AggregateBounder<double> {
+ public:
+  OAggBounder(const orc_problem* p, std::size_t n, std::size_t k) : p_(p), n_(n), k_(k), out_(k) {}
+  std::span<const aggregate::AggregateBound<double>> bound_children(
+      std::span<const aggregate::AggregateRegion<double>> regions) override
+  {
+    const auto& launch = regions[0].partition.launch;
+    std::vector<uint8_t> kinds;
+    for (std::size_t j = 0; j < launch.size(); ++j) kinds.push_back(static_cast<uint8_t>(launch.composition[j]));
+    std::vector<uint64_t> v(launch.var_ids.begin(), launch.var_ids.end()), w(launch.widths.begin(), launch.widths.end());
+    std::vector<double> lb(k_), ub(k_);
+    std::vector<int32_t> fe(k_);
+    if (orc_aggregate_bound(p_, reinterpret_cast<const double*>(regions[0].box.data()), kinds.data(), v.data(),
+                            w.data(), (int64_t)kinds.size(), n_, k_, lb.data(), ub.data(), fe.data(), 1))
+      throw std::runtime_error(orc_last_error());
+    for (std::size_t c = 0; c < k_; ++c) out_[c] = aggregate::AggregateBound<double>{lb[c], ub[c], fe[c] != 0};
+    return out_;
+  }
+  std::size_t n_subregions() const override { return n_; }
+
+ private:
+  const orc_problem* p_;
+  std::size_t n_, k_;
+  std::vector<aggregate::AggregateBound<double>> out_;
+};
+
+class OAggSampler : public aggregate::AggregateSampler<double> {
+ public:
+  OAggSampler(const orc_problem* p, std::size_t n, std::size_t s) : p_(p), n_(n), s_(s) {}
+  backend::CandidateResult<double> sample(std::span<const aggregate::AggregateRegion<double>> regions,
+                                          std::uint64_t salt) override
+  {
+    const auto& launch = regions[0].partition.launch;
+    std::vector<uint8_t> kinds;
+    for (std::size_t j = 0; j < launch.size(); ++j) kinds.push_back(static_cast<uint8_t>(launch.composition[j]));
+    std::vector<uint64_t> v(launch.var_ids.begin(), launch.var_ids.end()), w(launch.widths.begin(), launch.widths.end());
+    point_.resize(regions[0].box.size());
+    int32_t found;
+    double value;
+    int64_t index;
+    if (orc_sample(p_, reinterpret_cast<const double*>(regions[0].box.data()), kinds.data(), v.data(), w.data(),
+                   (int64_t)kinds.size(), n_, s_, salt, &found, &value, &index, point_.data(), 1))
+      throw std::runtime_error(orc_last_error());
+    return {found != 0, value, point_, index};
+  }
+  std::size_t n_samples() const override { return n_ * s_; }
+
+ private:
+  const orc_problem* p_;
+  std::size_t n_, s_;
+  std::vector<double> point_;
+};
+
+class OAggCache : public aggregate::AggregateRoleCache<double> {
+ public:
+  OAggCache(const orc_problem* p, std::size_t n, std::size_t ns, std::size_t k, std::size_t s)
+      : bounder_(p, n, k), sampler_(p, ns, s) {}
+  aggregate::AggregateBounder<double>& bounder(const region::Composition&) override { return bounder_; }
+  aggregate::AggregateSampler<double>& sampler(const region::Composition&) override { return sampler_; }
+  std::size_t graphs_built() const override { return 0; }
+  std::size_t graphs_rebuilt() const override { return 0; }
+
+ private:
+  OAggBounder bounder_;
+  OAggSampler sampler_;
+};
+
+// "<iter_limit> <k> <N> <Ns> <samples> <rule> <tolerance>" then the problem
+static int cmd_aggdriver(std::istream& in, std::ostream& out)
+{
+  uint32_t iter_limit;
+  size_t k, N, Ns, samples;
+  std::string rule_name;
+  in >> iter_limit >> k >> N >> Ns >> samples >> rule_name;
+  double tol = rd(in);
+  Loaded L;
+  load_problem(in, L);
+  auto rule = aggregate::parse_selection_rule(rule_name);
+  if (!rule) throw std::runtime_error("unknown selection rule");
+  auto pol = std::make_shared<aggregate::WidestBranchPolicy<double>>(k, N);
+  auto spol = std::make_shared<aggregate::WidestBranchPolicy<double>>(k, Ns);
+  auto cache = std::make_shared<OAggCache>(L.orc, N, Ns, k, samples);
+  auto obs = std::make_shared<report::SearchObserver>();
+  aggregate::AggregateDriver<double> drv(pol, spol, cache, *rule, iter_limit, tol, 0, obs);
+  auto o = drv.solve(L.problem);
+  const auto& t = o.counters;
+  out << hx(o.lower_bound) << ' ' << hx(o.upper_bound) << ' ' << search::to_string(o.stop_reason) << ' '
+      << o.proven_optimal << ' ' << o.infeasible << ' ' << o.selection_rule_engaged << '\n';
+  out << t.iterations << ' ' << t.fathomed << ' ' << t.fathomed_points << ' ' << t.bounded << ' ' << t.sampled << ' '
+      << t.enqueued << ' ' << t.witness_rejected << ' ' << t.pruned_duplicate << ' ' << t.pruned_infeasible << ' '
+      << t.pruned_dominated << ' ' << t.pending << ' ' << t.viable << ' ' << t.history_freed << ' '
+      << t.history_peak_live << '\n';
+  out << o.best_point.size();
+  for (double x : o.best_point) out << ' ' << hx(x);
+  out << '\n';
+  orc_problem_destroy(L.orc);
+  return 0;
+}
+
 int main(int argc, char** argv)
 {
   if (argc < 4) {
@@ -327,6 +430,7 @@ int main(int argc, char** argv)
     if (cmd == "decode") return cmd_decode(in, out);
     if (cmd == "policy") return cmd_policy(in, out);
     if (cmd == "driver") return cmd_driver(in, out);
+    if (cmd == "aggdriver") return cmd_aggdriver(in, out);
   } catch (const std::exception& e) {
     std::cerr << "error: " << e.what() << '\n';
     return 1;

@@ -201,6 +201,26 @@ def driver_cases(problems):
     return res
 
 
+AGG_CASES = (("square_le5", 300), ("infeasible", 50), ("aggregate_fixture", 400), ("int_eq", 100),
+             ("miqcqp_n6", 300), ("qcqp_n4_1", 600))
+
+
+def aggdriver_cases(problems):
+    """The reference AggregateDriver (WidestBranchPolicy k=2, N=16, sampler
+    N=8 with 2 points) with the oracle behind its roles, per selection rule."""
+    res = []
+    for name, iters in AGG_CASES:
+        for rule in ("least-lower-bound", "reject-index", "reject-index-stale"):
+            head = f"{iters} 2 16 8 2 {rule} {hx(1e-6)}\n"
+            out = run("aggdriver", head + problem_text(problems[name]))
+            f0 = out[0].split()
+            res.append({"problem": name, "iter_limit": iters, "k": 2, "N": 16, "Ns": 8, "samples": 2, "rule": rule,
+                        "lower_bound": f0[0], "upper_bound": f0[1], "stop_reason": f0[2], "proven_optimal": int(f0[3]),
+                        "infeasible": int(f0[4]), "selection_rule_engaged": int(f0[5]),
+                        "counters": [int(x) for x in out[1].split()], "best_point": out[2].split()[1:]})
+    return res
+
+
 def gams_cases():
     """The reference frontend's lowering of this repository's own .gms
     models (tests/data/gams), as oracle/_ref/ref_gams prints it."""
@@ -219,6 +239,7 @@ def main():
     (HERE / "policy.json").write_text(json.dumps(policy_cases(), indent=0))
     (HERE / "driver.json").write_text(json.dumps(driver_cases(fixture_problems()), indent=1))
     (HERE / "gams.json").write_text(json.dumps(gams_cases(), indent=1))
+    (HERE / "aggdriver.json").write_text(json.dumps(aggdriver_cases(fixture_problems()), indent=1))
     print("golden fixtures written")
 
 

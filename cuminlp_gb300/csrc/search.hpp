@@ -14,14 +14,23 @@ namespace cmn {
 constexpr int kRadixBits = 11;
 constexpr int kRadixBins = 1 << kRadixBits;
 constexpr int kScanBlock = 512;  // items per block of the compaction kernels
+constexpr int kPickThreads = kRadixBins / 2;  // two bins per thread
 
-// k-th smallest key search (radix select over lb keys).
+constexpr uint8_t kSelAlive = 0;
+constexpr uint8_t kSelParent = 1;
+constexpr uint8_t kSelEvicted = 2;
+
+// k-th smallest key search (radix select over lb keys). The threshold is
+// the bucket `prefix` under `mask` (the digits fixed so far); entries below
+// it are taken, and the first `k` entries inside it in position order.
 struct RadixState {
   uint64_t prefix;
   uint64_t mask;
-  uint64_t k;      // rank still to find inside the current prefix
-  uint64_t less;   // entries with key below the prefix bucket so far
-  uint32_t active; // 0: take everything (k >= n)
+  uint64_t k;        // rank still to find inside the current prefix
+  uint64_t less;     // entries with key below the prefix bucket so far
+  uint32_t active;   // 0: take everything (k >= n)
+  uint32_t settled;  // 1: the bucket is taken whole; no further digits
+  uint32_t rank;     // 1: entries inside the bucket need position ranks
   uint32_t pad;
   uint32_t hist[kRadixBins];
 };
@@ -40,7 +49,9 @@ struct SolverDev {
   uint64_t iterations;
   uint64_t remaining;      // unselected pool entries kept
   uint64_t kept;           // children kept
-  uint64_t new_size;
+  uint64_t new_size;       // remaining + kept: the rebuilt pool before eviction
+  uint64_t extent;         // pool_size + kept: entries of the current buffer
+  uint64_t survivors;      // entries moved to the other buffer
   uint64_t certify_count;
   uint64_t evict;          // 1 when the rebuilt pool exceeds the cap
   uint64_t dropped_min_key;
@@ -90,7 +101,9 @@ struct SolverBufs {
   double* hi[2];
   double* lb[2];
   uint32_t* depth[2];
-  uint8_t* sel;          // selection / keep marks over a pool
+  // marks over the current buffer: kSelAlive, kSelParent (expanded this
+  // iteration: a hole), kSelEvicted (dropped by the cap)
+  uint8_t* sel;
   // staging of this iteration's parents: planes [v * e_max + k]
   double* plo;
   double* phi;

@@ -95,6 +95,8 @@ __global__ void begin_kernel(const SolverCfg cfg, const SolverBufs b)
   d->remaining = 0;
   d->kept = 0;
   d->new_size = 0;
+  d->extent = 0;
+  d->survivors = 0;
   d->evict = 0;
   d->improved = 0;
   d->counters.iterations = d->iterations;
@@ -105,29 +107,24 @@ __global__ void begin_kernel(const SolverCfg cfg, const SolverBufs b)
 // radix select of the k-th smallest lower-bound key
 // ---------------------------------------------------------------------
 // which = 0: the current pool (n = pool_size, k = n_parents)
-// which = 1: the rebuilt pool (n = new_size, k = cap) when evicting
-__device__ __forceinline__ const double* pick_lb(const SolverBufs& b, int which)
-{
-  const uint32_t p = b.dev->parity;
-  return which == 0 ? b.lb[p] : b.lb[1 - p];
-}
+// which = 1: the current buffer after the children were appended behind
+//            the pool (n = extent, k = cap), alive entries only, when evicting
+__device__ __forceinline__ const double* pool_lb(const SolverBufs& b) { return b.lb[b.dev->parity]; }
 
-__device__ __forceinline__ uint64_t rs_n(const SolverCfg& cfg, const SolverDev* d, int which)
+__device__ __forceinline__ uint64_t rs_n(const SolverDev* d, int which)
 {
-  (void)cfg;
-  return which == 0 ? d->pool_size : d->new_size;
+  return which == 0 ? d->pool_size : d->extent;
 }
 
 __global__ void radix_init_kernel(const SolverCfg cfg, const SolverBufs b, int which)
 {
   SolverDev* d = b.dev;
   RadixState* rs = b.radix;
-  const uint64_t n = rs_n(cfg, d, which);
   const uint64_t k = which == 0 ? d->n_parents : cfg.cap;
   bool active;
   if (d->done) active = false;
-  else if (which == 1) active = d->evict && k < n;
-  else active = k < n;
+  else if (which == 1) active = d->evict && k < d->new_size;
+  else active = k < d->pool_size;
   for (int i = threadIdx.x; i < kRadixBins; i += blockDim.x) rs->hist[i] = 0;
   if (threadIdx.x == 0) {
     rs->prefix = 0;
@@ -135,52 +132,118 @@ __global__ void radix_init_kernel(const SolverCfg cfg, const SolverBufs b, int w
     rs->k = k;
     rs->less = 0;
     rs->active = active ? 1u : 0u;
+    rs->settled = 0;
+    rs->rank = active ? 1u : 0u;
   }
 }
 
+// One digit's histogram over the entries inside the current bucket. Lanes
+// of a warp that hit the same bin add once (match + popc), which keeps the
+// first digits, where nearly every key shares one bin, off a single
+// shared-memory address.
 __global__ void radix_hist_kernel(const SolverCfg cfg, const SolverBufs b, int which, int shift, int bits)
 {
   __shared__ uint32_t h[kRadixBins];
   RadixState* rs = b.radix;
-  if (!rs->active) return;
-  const uint64_t n = rs_n(cfg, b.dev, which);
+  if (!rs->active || rs->settled) return;
+  const uint64_t n = rs_n(b.dev, which);
   if ((uint64_t)blockIdx.x * blockDim.x >= n) return;
   const int nb = 1 << bits;
   for (int i = threadIdx.x; i < nb; i += blockDim.x) h[i] = 0;
   __syncthreads();
-  const double* lb = pick_lb(b, which);
+  const double* __restrict__ lb = pool_lb(b);
+  const uint8_t* __restrict__ sel = which == 1 ? b.sel : nullptr;
   const uint64_t prefix = rs->prefix, mask = rs->mask;
-  const uint64_t dmask = (uint64_t)(nb - 1);
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t key = lb_key(lb[i]);
-    if ((key & mask) == prefix) atomicAdd(&h[(key >> shift) & dmask], 1u);
+  const uint32_t dmask = (uint32_t)(nb - 1);
+  const int lane = threadIdx.x & 31;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  // warp-uniform trip count: `base` is the same for the 32 lanes
+  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
+    const uint64_t i = base + lane;
+    bool ok = false;
+    uint32_t bin = 0xffffffffu;
+    if (i < n && (sel == nullptr || sel[i] == kSelAlive)) {
+      const uint64_t key = lb_key(lb[i]);
+      if ((key & mask) == prefix) {
+        ok = true;
+        bin = (uint32_t)(key >> shift) & dmask;
+      }
+    }
+    if (__any_sync(0xffffffffu, ok)) {
+      const unsigned peers = __match_any_sync(0xffffffffu, bin);
+      if (ok && __ffs(peers) - 1 == lane) atomicAdd(&h[bin], (uint32_t)__popc(peers));
+    }
   }
   __syncthreads();
   for (int i = threadIdx.x; i < nb; i += blockDim.x)
     if (h[i]) atomicAdd(&rs->hist[i], h[i]);
+  (void)cfg;
 }
 
-__global__ void radix_pick_kernel(const SolverBufs b, int shift, int bits)
+// Picks the digit whose bin holds the k-th entry: a block scan over the
+// bins (two per thread). When the entries up to and including that bin
+// are exactly k, the bin is taken whole and the search stops.
+__global__ void __launch_bounds__(kPickThreads) radix_pick_kernel(const SolverBufs b, int shift, int bits)
 {
+  __shared__ uint64_t warp_sum[kPickThreads / 32];
+  __shared__ int pick_d;
+  __shared__ uint64_t pick_cum, pick_cnt;
   RadixState* rs = b.radix;
-  if (!rs->active) return;
-  if (threadIdx.x != 0) return;
+  if (!rs->active || rs->settled) return;
   const int nb = 1 << bits;
-  uint64_t cum = 0;
-  int d = nb - 1;
-  for (int i = 0; i < nb; ++i) {
-    const uint64_t c = rs->hist[i];
-    if (cum + c >= rs->k) {
-      d = i;
-      break;
-    }
-    cum += c;
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  const int b0 = 2 * t;
+  const uint32_t c0 = b0 < nb ? rs->hist[b0] : 0u;
+  const uint32_t c1 = b0 + 1 < nb ? rs->hist[b0 + 1] : 0u;
+  if (t == 0) pick_d = -1;
+  uint64_t x = (uint64_t)c0 + c1;
+  for (int off = 1; off < 32; off <<= 1) {
+    const uint64_t y = __shfl_up_sync(0xffffffffu, x, off);
+    if (lane >= off) x += y;
   }
-  rs->less += cum;
-  rs->k -= cum;
-  rs->prefix |= (uint64_t)d << shift;
+  if (lane == 31) warp_sum[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    uint64_t s = lane < kPickThreads / 32 ? warp_sum[lane] : 0;
+    for (int off = 1; off < 32; off <<= 1) {
+      const uint64_t y = __shfl_up_sync(0xffffffffu, s, off);
+      if (lane >= off) s += y;
+    }
+    if (lane < kPickThreads / 32) warp_sum[lane] = s;  // inclusive
+  }
+  __syncthreads();
+  const uint64_t incl = x + (wid > 0 ? warp_sum[wid - 1] : 0);
+  const uint64_t excl = incl - c0 - c1;
+  const uint64_t k = rs->k;
+  if (excl < k && k <= incl) {  // exactly one thread holds the k-th entry
+    if (excl + c0 >= k) {
+      pick_d = b0;
+      pick_cum = excl;
+      pick_cnt = c0;
+    } else {
+      pick_d = b0 + 1;
+      pick_cum = excl + c0;
+      pick_cnt = c1;
+    }
+  }
+  __syncthreads();
+  if (b0 < nb) rs->hist[b0] = 0;
+  if (b0 + 1 < nb) rs->hist[b0 + 1] = 0;
+  if (t != 0) return;
+  if (pick_d < 0) {  // fewer entries in the bucket than its rank: never expected
+    b.dev->error = 1;
+    rs->settled = 1;
+    rs->rank = 0;
+    return;
+  }
+  rs->less += pick_cum;
+  rs->k = k - pick_cum;
+  rs->prefix |= (uint64_t)pick_d << shift;
   rs->mask |= ((uint64_t)(nb - 1)) << shift;
-  for (int i = 0; i < nb; ++i) rs->hist[i] = 0;
+  if (pick_cum + pick_cnt == k) {
+    rs->settled = 1;
+    rs->rank = 0;
+  }
 }
 
 // ---------------------------------------------------------------------
@@ -252,13 +315,18 @@ __global__ void scan_kernel(const uint32_t* __restrict__ counts, uint32_t* __res
 }
 
 // ---- predicates / operations -----------------------------------------
-struct SelPool {  // marked entries of the current (which=0) or rebuilt pool
+struct SelParents {  // entries of the current pool marked as this iteration's parents
   SolverBufs b;
-  int which;
-  bool want;  // true: marked entries; false: unmarked entries
-  __device__ uint64_t size() const { return which == 0 ? b.dev->pool_size : b.dev->new_size; }
-  __device__ bool operator()(uint64_t i) const { return (b.sel[i] != 0) == want; }
-  __device__ bool skip() const { return b.dev->done != 0 || (which == 1 && !b.dev->evict); }
+  __device__ uint64_t size() const { return b.dev->pool_size; }
+  __device__ bool operator()(uint64_t i) const { return b.sel[i] == kSelParent; }
+  __device__ bool skip() const { return b.dev->done != 0; }
+};
+
+struct AliveEntry {  // entries of the current buffer that stay in the pool
+  SolverBufs b;
+  __device__ uint64_t size() const { return b.dev->extent; }
+  __device__ bool operator()(uint64_t i) const { return b.sel[i] == kSelAlive; }
+  __device__ bool skip() const { return b.dev->done != 0; }
 };
 
 struct KeptChild {
@@ -275,16 +343,16 @@ struct ScreenedChild {
   __device__ bool skip() const { return b.dev->done != 0; }
 };
 
-struct EqKey {  // entries whose key equals the radix threshold
+struct EqKey {  // alive entries inside the radix threshold bucket
   SolverBufs b;
   int which;
-  __device__ uint64_t size() const { return which == 0 ? b.dev->pool_size : b.dev->new_size; }
+  __device__ uint64_t size() const { return rs_n(b.dev, which); }
   __device__ bool operator()(uint64_t i) const
   {
-    const double* lb = which == 0 ? b.lb[b.dev->parity] : b.lb[1 - b.dev->parity];
-    return lb_key(lb[i]) == b.radix->prefix;
+    if (which == 1 && b.sel[i] != kSelAlive) return false;
+    return (lb_key(pool_lb(b)[i]) & b.radix->mask) == b.radix->prefix;
   }
-  __device__ bool skip() const { return b.dev->done != 0 || !b.radix->active; }
+  __device__ bool skip() const { return b.dev->done != 0 || !b.radix->rank; }
 };
 
 template <class P>
@@ -300,30 +368,34 @@ __global__ void __launch_bounds__(kScanBlock) count_kernel(const P pred, uint32_
 }
 
 // Marks the k smallest (key, position) entries: all keys below the
-// threshold, and the first `k` entries equal to it in position order.
+// threshold bucket, and the first `k` entries inside it in position order
+// (all of them once the bucket is settled). which = 0 writes kSelParent /
+// kSelAlive over the pool; which = 1 marks alive entries kSelEvicted when
+// they fall outside the cap and leaves the parents' holes as they are.
 __global__ void __launch_bounds__(kScanBlock) mark_kernel(const SolverCfg cfg, const SolverBufs b, int which,
                                                           const uint32_t* __restrict__ eq_offsets)
 {
   const SolverDev* d = b.dev;
   if (d->done) return;
   if (which == 1 && !d->evict) return;
-  const uint64_t n = which == 0 ? d->pool_size : d->new_size;
+  const uint64_t n = rs_n(d, which);
   if ((uint64_t)blockIdx.x * kScanBlock >= n) return;
   const uint64_t i = (uint64_t)blockIdx.x * kScanBlock + threadIdx.x;
   const RadixState* rs = b.radix;
   const bool active = rs->active != 0;
-  const double* lb = which == 0 ? b.lb[d->parity] : b.lb[1 - d->parity];
-  const uint64_t key = i < n ? lb_key(lb[i]) : ~0ULL;
-  const bool eq = active && i < n && key == rs->prefix;
+  const bool alive = i < n && (which == 0 || b.sel[i] == kSelAlive);
+  const uint64_t key = alive ? (lb_key(pool_lb(b)[i]) & rs->mask) : ~0ULL;
+  const bool eq = active && alive && key == rs->prefix;
   int total;
   const int rank = block_excl_rank(eq, total);
-  if (i >= n) return;
+  if (!alive) return;
   bool mark;
   if (!active) mark = true;
   else if (key < rs->prefix) mark = true;
-  else if (eq) mark = (uint64_t)eq_offsets[blockIdx.x] + (uint64_t)rank < rs->k;
+  else if (eq) mark = rs->settled || (uint64_t)eq_offsets[blockIdx.x] + (uint64_t)rank < rs->k;
   else mark = false;
-  b.sel[i] = mark ? 1 : 0;
+  if (which == 0) b.sel[i] = mark ? kSelParent : kSelAlive;
+  else if (!mark) b.sel[i] = kSelEvicted;
   (void)cfg;
 }
 
@@ -352,34 +424,19 @@ struct GatherParents {
   }
 };
 
-// copy an unselected pool entry into the rebuilt pool
-struct CopyRemaining {
-  SolverCfg cfg;
-  SolverBufs b;
-  __device__ void operator()(uint64_t i, uint64_t pos) const
-  {
-    const uint32_t p = b.dev->parity, q = 1 - p;
-    for (int v = 0; v < cfg.n_vars; ++v) {
-      b.lo[q][(uint64_t)v * cfg.pstride + pos] = b.lo[p][(uint64_t)v * cfg.pstride + i];
-      b.hi[q][(uint64_t)v * cfg.pstride + pos] = b.hi[p][(uint64_t)v * cfg.pstride + i];
-    }
-    b.lb[q][pos] = b.lb[p][i];
-    b.depth[q][pos] = b.depth[p][i];
-  }
-};
-
-// decode a kept child from its parent and append it to the rebuilt pool
+// decode a kept child from its parent and append it behind the pool in
+// the current buffer (positions pool_size + pos)
 struct AppendChild {
   SolverCfg cfg;
   SolverBufs b;
   __device__ void operator()(uint64_t g, uint64_t pos) const
   {
-    const uint32_t q = 1 - b.dev->parity;
-    const uint64_t at = b.dev->remaining + pos;
+    const uint32_t p = b.dev->parity;
+    const uint64_t at = b.dev->pool_size + pos;
     const uint64_t k = g >> cfg.log2C, r = g & ((1ULL << cfg.log2C) - 1ULL);
     for (int v = 0; v < cfg.n_vars; ++v) {
-      b.lo[q][(uint64_t)v * cfg.pstride + at] = b.plo[(uint64_t)v * cfg.e_max + k];
-      b.hi[q][(uint64_t)v * cfg.pstride + at] = b.phi[(uint64_t)v * cfg.e_max + k];
+      b.lo[p][(uint64_t)v * cfg.pstride + at] = b.plo[(uint64_t)v * cfg.e_max + k];
+      b.hi[p][(uint64_t)v * cfg.pstride + at] = b.phi[(uint64_t)v * cfg.e_max + k];
     }
     const ParentInfo pi = b.pinfo[k];
     const SlotPlan* sp = b.slots + k * (uint64_t)cfg.max_slots;
@@ -389,28 +446,49 @@ struct AppendChild {
       double lo, hi;
       slot_bounds((int)s.kind, b.plo[(uint64_t)s.vid * cfg.e_max + k], b.phi[(uint64_t)s.vid * cfg.e_max + k], part,
                   s.width, lo, hi);
-      b.lo[q][(uint64_t)s.vid * cfg.pstride + at] = lo;
-      b.hi[q][(uint64_t)s.vid * cfg.pstride + at] = hi;
+      b.lo[p][(uint64_t)s.vid * cfg.pstride + at] = lo;
+      b.hi[p][(uint64_t)s.vid * cfg.pstride + at] = hi;
     }
-    b.lb[q][at] = b.clb[g];
-    b.depth[q][at] = b.pdepth[k] + 1;
+    b.lb[p][at] = b.clb[g];
+    b.depth[p][at] = b.pdepth[k] + 1;
+    b.sel[at] = kSelAlive;
   }
 };
 
-// move a surviving entry of the rebuilt (over-cap) pool back to the
-// current buffer
-struct CopyEvictKeep {
+// move an alive entry of the current buffer to position `pos` of the other
+// buffer. Loads of a group of planes are issued before its stores so that
+// each thread keeps several reads in flight.
+struct CopyPool {
   SolverCfg cfg;
   SolverBufs b;
   __device__ void operator()(uint64_t i, uint64_t pos) const
   {
+    constexpr int kGroup = 4;
     const uint32_t p = b.dev->parity, q = 1 - p;
-    for (int v = 0; v < cfg.n_vars; ++v) {
-      b.lo[p][(uint64_t)v * cfg.pstride + pos] = b.lo[q][(uint64_t)v * cfg.pstride + i];
-      b.hi[p][(uint64_t)v * cfg.pstride + pos] = b.hi[q][(uint64_t)v * cfg.pstride + i];
+    const double* __restrict__ slo = b.lo[p];
+    const double* __restrict__ shi = b.hi[p];
+    double* __restrict__ dlo = b.lo[q];
+    double* __restrict__ dhi = b.hi[q];
+    const uint64_t ps = cfg.pstride;
+    const double lbv = b.lb[p][i];
+    const uint32_t dep = b.depth[p][i];
+    for (int v0 = 0; v0 < cfg.n_vars; v0 += kGroup) {
+      double l[kGroup], h[kGroup];
+#pragma unroll
+      for (int u = 0; u < kGroup; ++u)
+        if (v0 + u < cfg.n_vars) {
+          l[u] = slo[(uint64_t)(v0 + u) * ps + i];
+          h[u] = shi[(uint64_t)(v0 + u) * ps + i];
+        }
+#pragma unroll
+      for (int u = 0; u < kGroup; ++u)
+        if (v0 + u < cfg.n_vars) {
+          dlo[(uint64_t)(v0 + u) * ps + pos] = l[u];
+          dhi[(uint64_t)(v0 + u) * ps + pos] = h[u];
+        }
     }
-    b.lb[p][pos] = b.lb[q][i];
-    b.depth[p][pos] = b.depth[q][i];
+    b.lb[q][pos] = lbv;
+    b.depth[q][pos] = dep;
   }
 };
 
@@ -565,7 +643,9 @@ __global__ void size_kernel(const SolverCfg cfg, const SolverBufs b)
 {
   SolverDev* d = b.dev;
   if (d->done) return;
+  d->remaining = d->pool_size - d->n_parents;
   d->new_size = d->remaining + d->kept;
+  d->extent = d->pool_size + d->kept;
   d->evict = d->new_size > cfg.cap ? 1 : 0;
 }
 
@@ -574,13 +654,13 @@ __global__ void evict_account_kernel(const SolverBufs b)
 {
   SolverDev* d = b.dev;
   if (d->done || !d->evict) return;
-  const uint64_t n = d->new_size;
+  const uint64_t n = d->extent;
   const double gub = d->gub;
-  const double* lb = b.lb[1 - d->parity];
+  const double* lb = b.lb[d->parity];
   unsigned long long viable = 0, dominated = 0;
   uint64_t mkey = ~0ULL;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-    if (b.sel[i]) continue;
+    if (b.sel[i] != kSelEvicted) continue;
     const double x = lb[i];
     if (x <= gub) {
       ++viable;
@@ -607,12 +687,12 @@ __global__ void finish_kernel(const SolverCfg cfg, const SolverBufs b)
 {
   SolverDev* d = b.dev;
   if (d->done) return;
-  if (d->evict) {
-    d->pool_size = cfg.cap;  // survivors were moved back into the current buffer
-  } else {
-    d->pool_size = d->new_size;
-    d->parity = 1 - d->parity;
-  }
+  // the survivors were moved to the other buffer: exactly the cap when
+  // evicting, otherwise every alive entry
+  const uint64_t expect = d->evict ? cfg.cap : d->new_size;
+  if (d->survivors != expect) d->error = 1;
+  d->pool_size = d->survivors;
+  d->parity = 1 - d->parity;
   if (d->dropped_min_key != ~0ULL) d->dropped_lb_min = key_to_lb(d->dropped_min_key);
   if (d->pool_size > d->counters.peak_frontier) d->counters.peak_frontier = d->pool_size;
   d->pool_min_key = ~0ULL;
@@ -673,17 +753,18 @@ static void radix_select(const SolverCfg& cfg, const SolverBufs& b, int which, u
 {
   radix_init_kernel<<<1, 256, 0, s>>>(cfg, b, which);
   const int grid = (int)std::min<uint64_t>((max_items + 255) / 256, 4096);
-  // digits from the most significant: 6 x 11 bits minus the 2 top bits
+  // digits from the most significant: 6 x 11 bits minus the 2 top bits;
+  // the passes after the bucket settles return at once
   const int shifts[6] = {53, 42, 31, 20, 9, 0};
   const int bits[6] = {11, 11, 11, 11, 11, 9};
   for (int p = 0; p < 6; ++p) {
     radix_hist_kernel<<<grid, 256, 0, s>>>(cfg, b, which, shifts[p], bits[p]);
-    radix_pick_kernel<<<1, 32, 0, s>>>(b, shifts[p], bits[p]);
+    radix_pick_kernel<<<1, kPickThreads, 0, s>>>(b, shifts[p], bits[p]);
   }
-  // ranks among entries equal to the threshold, then the marks
-  const uint64_t* n_dev = which == 0 ? &b.dev->pool_size : &b.dev->new_size;
+  // ranks among entries inside the threshold bucket, then the marks
+  const uint64_t* n_dev = which == 0 ? &b.dev->pool_size : &b.dev->extent;
   EqKey eq{b, which};
-  compact(eq, max_items, n_dev, nullptr, b, &b.radix->active, s);
+  compact(eq, max_items, n_dev, nullptr, b, &b.radix->rank, s);
   const int mgrid = (int)((max_items + kScanBlock - 1) / kScanBlock);
   mark_kernel<<<mgrid, kScanBlock, 0, s>>>(cfg, b, which, b.block_offsets);
 }
@@ -703,7 +784,7 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
 
   // (1) select the E best parents and stage them
   radix_select(cfg, b, 0, cfg.cap, s);
-  SelPool selected{b, 0, true};
+  SelParents selected{b};
   compact(selected, cfg.cap, &b.dev->pool_size, nullptr, b, nullptr, s);
   scatter(selected, GatherParents{cfg, b}, cfg.cap, s, b);
 
@@ -812,23 +893,23 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
     const int grid = (int)std::min<uint64_t>((max_children + 255) / 256, 4096);
     prune_count_kernel<<<grid, 256, 0, s>>>(cfg, b);
   }
-  SelPool unselected{b, 0, false};
-  compact(unselected, cfg.cap, &b.dev->pool_size, &b.dev->remaining, b, nullptr, s);
-  scatter(unselected, CopyRemaining{cfg, b}, cfg.cap, s, b);
+  // the kept children go behind the pool in the current buffer; the
+  // parents stay there as holes until the one compaction below
   KeptChild kept{b};
   compact(kept, max_children, &b.dev->n_children, &b.dev->kept, b, nullptr, s);
   scatter(kept, AppendChild{cfg, b}, max_children, s, b);
   size_kernel<<<1, 1, 0, s>>>(cfg, b);
 
-  // (6) over the cap: keep the `cap` best, fold the rest into the floor
+  // (6) over the cap: keep the `cap` best alive entries, fold the rest into
+  // the floor; then move every alive entry to the other buffer in order
   radix_select(cfg, b, 1, max_pool, s);
   {
     const int grid = (int)std::min<uint64_t>((max_pool + 255) / 256, 4096);
     evict_account_kernel<<<grid, 256, 0, s>>>(b);
   }
-  SelPool keep{b, 1, true};
-  compact(keep, max_pool, &b.dev->new_size, nullptr, b, nullptr, s);
-  scatter(keep, CopyEvictKeep{cfg, b}, max_pool, s, b);
+  AliveEntry alive{b};
+  compact(alive, max_pool, &b.dev->extent, &b.dev->survivors, b, nullptr, s);
+  scatter(alive, CopyPool{cfg, b}, max_pool, s, b);
   finish_kernel<<<1, 1, 0, s>>>(cfg, b);
   {
     const int grid = (int)std::min<uint64_t>((max_pool + 255) / 256, 4096);

@@ -474,8 +474,7 @@ __global__ void __launch_bounds__(kEvalThreads, 4) batch_eval_kernel(const Batch
         const uint64_t part = (r / sj.prefix) % sj.width;
         if (part >= sj.dom) dup = true;
         double lo, hi;
-        slot_bounds((int)sj.kind, b.plo[splane(c, slot, sj.vid) + k], b.phi[splane(c, slot, sj.vid) + k], part,
-                    sj.width, lo, hi);
+        slot_bounds(sj, b.plo[splane(c, slot, sj.vid) + k], b.phi[splane(c, slot, sj.vid) + k], part, lo, hi);
         olo[j * B] = Widen<T, double>::lo(lo);
         ohi[j * B] = Widen<T, double>::hi(hi);
         ovid[j * B] = (int32_t)sj.vid;
@@ -513,7 +512,7 @@ __device__ __forceinline__ double child_bound(const BatchCfg& c, const BatchBufs
   for (uint32_t j = 0; j < count; ++j) {
     if (sp[j].vid == (uint32_t)v) {
       const uint64_t part = (r / sp[j].prefix) % sp[j].width;
-      slot_bounds((int)sp[j].kind, lo, hi, part, sp[j].width, lo, hi);
+      slot_bounds(sp[j], lo, hi, part, lo, hi);
       break;
     }
   }

@@ -465,6 +465,7 @@ static cmn_status stage_region(cmn_role* r, const double* box, const uint64_t* v
     sp[j].dom = widths[j];
     sp[j].vid = (uint32_t)var_ids[j];
     sp[j].kind = r->slot_kinds[j];
+    sp[j].step = slot_step(sp[j].kind, lo[var_ids[j]], hi[var_ids[j]], widths[j]);
     if (running > UINT64_MAX / widths[j]) running = UINT64_MAX;
     else running *= widths[j];
   }
@@ -931,7 +932,7 @@ extern "C" cmn_status cmn_solver_create(const cmn_problem* p, const cmn_solve_op
     A(&b.clb, maxc);
     A(&b.cstate, maxc);
     A(&b.list, maxc);
-    const size_t nblk = (std::max<uint64_t>(cfg.pstride, maxc) + kScanBlock - 1) / kScanBlock + 1;
+    const size_t nblk = (std::max<uint64_t>(cfg.pstride, maxc) + kScanTile - 1) / kScanTile + 1;
     A(&b.block_counts, nblk);
     A(&b.block_offsets, nblk);
     b.n_block_best = s->sample_grid + 1;

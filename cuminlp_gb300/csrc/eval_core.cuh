@@ -14,6 +14,7 @@
 
 #include <cstdint>
 
+#include "kernels.cuh"
 #include "program.h"
 
 namespace cmn {
@@ -681,19 +682,19 @@ __device__ __forceinline__ PointVerdict group_point_verdict(PointVerdict v, int 
 
 // ---- region decode (region/decode.hpp:44-71), FMA form as compiled on
 // the device, and the sampler (graph/subregion_sampler.cuh:53-120) ----
-__device__ __forceinline__ void slot_bounds(int kind, double plo, double phi, uint64_t part, uint64_t fan,
-                                            double& lo, double& hi)
+// bounds of part `part` of slot `s` over the parent's [plo, phi]
+__device__ __forceinline__ void slot_bounds(const SlotPlan& s, double plo, double phi, uint64_t part, double& lo,
+                                            double& hi)
 {
-  if (kind == 2 || kind == 3) {  // IntegerEnumerate / BinaryEnumerate
-    double value = __dadd_rn(ceil(plo), (double)part);
+  if (s.kind == 2 || s.kind == 3) {  // IntegerEnumerate / BinaryEnumerate
+    double value = __dadd_rn(s.step, (double)part);  // step = ceil(plo)
     if (value > phi) value = phi;
     lo = value;
     hi = value;
     return;
   }
-  const double width = __ddiv_rn(__dsub_rn(phi, plo), (double)fan);
-  lo = __fma_rn(width, (double)part, plo);
-  hi = (part + 1 == fan) ? phi : __fma_rn(width, (double)(part + 1), plo);
+  lo = __fma_rn(s.step, (double)part, plo);
+  hi = (part + 1 == s.width) ? phi : __fma_rn(s.step, (double)(part + 1), plo);
 }
 
 __device__ __forceinline__ uint64_t sample_hash(uint64_t vid, uint64_t i, uint64_t region, uint64_t salt)
@@ -727,8 +728,10 @@ __device__ __forceinline__ double sample_value(bool discrete, double lb, double 
 // Total order on doubles for selection keys (NaN last).
 __device__ __forceinline__ uint64_t lb_key(double x)
 {
+  // integer NaN test: an FP64 compare would run on the FP64 pipe, which
+  // bounds the pool passes on this part
   const uint64_t u = (uint64_t)__double_as_longlong(x);
-  if (x != x) return ~0ULL;
+  if ((u & 0x7fffffffffffffffULL) > 0x7ff0000000000000ULL) return ~0ULL;
   return (u >> 63) ? ~u : (u | 0x8000000000000000ULL);
 }
 

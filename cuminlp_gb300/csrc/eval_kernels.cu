@@ -64,8 +64,7 @@ __device__ __forceinline__ ChildVars<T, S> child_vars(const EvalArgs& a, const S
       const uint64_t part = (r / s.prefix) % s.width;
       if (part >= s.dom) dup = true;
       double lo, hi;
-      slot_bounds((int)s.kind, a.plo[(uint64_t)s.vid * a.pstride + k], a.phi[(uint64_t)s.vid * a.pstride + k], part,
-                  s.width, lo, hi);
+      slot_bounds(s, a.plo[(uint64_t)s.vid * a.pstride + k], a.phi[(uint64_t)s.vid * a.pstride + k], part, lo, hi);
       olo[j * stride] = Widen<T, double>::lo(lo);
       ohi[j * stride] = Widen<T, double>::hi(hi);
       ovid[j * stride] = (int32_t)s.vid;
@@ -337,7 +336,7 @@ __device__ __forceinline__ void stage_point(const SampleArgs& a, const Tile<doub
     for (uint32_t j = 0; j < count; ++j) {
       if (sp[j].vid == (uint32_t)v) {
         const uint64_t part = (r / sp[j].prefix) % sp[j].width;
-        slot_bounds((int)sp[j].kind, lo, hi, part, sp[j].width, lo, hi);
+        slot_bounds(sp[j], lo, hi, part, lo, hi);
         break;
       }
     }
@@ -459,7 +458,7 @@ __global__ void __launch_bounds__(kEvalThreads) sample_children_kernel(const Sam
         for (uint32_t j = 0; j < count; ++j) {
           if (sp[j].vid == (uint32_t)v) {
             const uint64_t part = (r / sp[j].prefix) % sp[j].width;
-            slot_bounds((int)sp[j].kind, lo, hi, part, sp[j].width, lo, hi);
+            slot_bounds(sp[j], lo, hi, part, lo, hi);
             break;
           }
         }
@@ -526,7 +525,7 @@ __global__ void witness_kernel(const Cand* __restrict__ cand, const double* __re
       for (uint32_t j = 0; j < count; ++j) {
         if (sp[j].vid == (uint32_t)v) {
           const uint64_t part = (r / sp[j].prefix) % sp[j].width;
-          slot_bounds((int)sp[j].kind, lo, hi, part, sp[j].width, lo, hi);
+          slot_bounds(sp[j], lo, hi, part, lo, hi);
           break;
         }
       }

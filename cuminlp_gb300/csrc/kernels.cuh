@@ -2,6 +2,7 @@
 // code that launches them.
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 
 #include "program.h"
@@ -16,7 +17,27 @@ struct SlotPlan {
   uint64_t dom;     // true domain size; parts >= dom are duplicates
   uint32_t vid;
   uint32_t kind;    // cmn_slot_kind
+  // from the parent box: the width of one part (partition kinds) or the
+  // ceiling of the lower bound (enumeration kinds), so that a child's
+  // bounds cost one fused multiply-add instead of a division
+  double step;
 };
+
+// SlotPlan::step of a slot over [plo, phi] (region/decode.hpp:44-71); the
+// host and the device round the same IEEE operations the same way.
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+inline double slot_step(uint32_t kind, double plo, double phi, uint64_t fan)
+{
+#ifdef __CUDA_ARCH__
+  if (kind == 2 || kind == 3) return ceil(plo);
+  return __ddiv_rn(__dsub_rn(phi, plo), (double)fan);
+#else
+  if (kind == 2 || kind == 3) return std::ceil(plo);
+  return (phi - plo) / (double)fan;
+#endif
+}
 
 struct ParentInfo {
   uint32_t count;   // slots in use

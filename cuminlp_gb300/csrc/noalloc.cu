@@ -97,7 +97,8 @@ extern "C" cmn_status cmn_sample_noalloc(const cmn_problem* p, const uint8_t* sl
     if (slot_kinds[j] > CMN_SLOT_BINARY_ENUMERATE) return set_error(CMN_INVALID_CONFIGURATION, "unknown slot kind");
     if (var_ids[j] >= (uint64_t)n) return set_error(CMN_SHAPE_MISMATCH, "var_id out of range");
     if (widths[j] < 1) return set_error(CMN_SHAPE_MISMATCH, "slot width must be at least 1");
-    staged.slots[j] = SlotPlan{widths[j], running, widths[j], (uint32_t)var_ids[j], slot_kinds[j]};
+    staged.slots[j] = SlotPlan{widths[j], running, widths[j], (uint32_t)var_ids[j], slot_kinds[j],
+                               slot_step(slot_kinds[j], box[2 * var_ids[j]], box[2 * var_ids[j] + 1], widths[j])};
     running = running > UINT64_MAX / widths[j] ? UINT64_MAX : running * widths[j];
   }
   if (running != n_regions) return set_error(CMN_SHAPE_MISMATCH, "the product of widths does not equal n_regions");

@@ -215,6 +215,7 @@ __host__ __device__ inline ParentInfo bisection_policy(const double* __restrict_
   for (uint32_t j = 0; j < count; ++j) {
     sp[j].prefix = running;
     running *= sp[j].width;
+    sp[j].step = slot_step(sp[j].kind, plo[(uint64_t)sp[j].vid * stride], phi[(uint64_t)sp[j].vid * stride], sp[j].width);
   }
   pi.count = count;
   pi.nreg = running;

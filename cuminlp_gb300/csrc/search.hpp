@@ -13,7 +13,10 @@ namespace cmn {
 
 constexpr int kRadixBits = 11;
 constexpr int kRadixBins = 1 << kRadixBits;
-constexpr int kScanBlock = 512;  // items per block of the compaction kernels
+constexpr int kScanBlock = 512;  // threads per block of the compaction kernels
+constexpr int kScanItems = 8;    // items per thread
+constexpr int kScanTile = kScanBlock * kScanItems;
+constexpr int kHistUnroll = 8;   // entries per lane in flight in the radix histogram
 constexpr int kPickThreads = kRadixBins / 2;  // two bins per thread
 
 constexpr uint8_t kSelAlive = 0;

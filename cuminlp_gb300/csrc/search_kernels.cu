@@ -109,7 +109,15 @@ __global__ void begin_kernel(const SolverCfg cfg, const SolverBufs b)
 // which = 0: the current pool (n = pool_size, k = n_parents)
 // which = 1: the current buffer after the children were appended behind
 //            the pool (n = extent, k = cap), alive entries only, when evicting
-__device__ __forceinline__ const double* pool_lb(const SolverBufs& b) { return b.lb[b.dev->parity]; }
+// one of the two pool buffers without indexing the parameter arrays by a
+// runtime value (which would copy them to local memory)
+template <class T>
+__device__ __forceinline__ T* parity_buf(T* const (&a)[2], uint32_t p)
+{
+  return p ? a[1] : a[0];
+}
+
+__device__ __forceinline__ const double* pool_lb(const SolverBufs& b) { return parity_buf(b.lb, b.dev->parity); }
 
 __device__ __forceinline__ uint64_t rs_n(const SolverDev* d, int which)
 {
@@ -137,10 +145,11 @@ __global__ void radix_init_kernel(const SolverCfg cfg, const SolverBufs b, int w
   }
 }
 
-// One digit's histogram over the entries inside the current bucket. Lanes
-// of a warp that hit the same bin add once (match + popc), which keeps the
-// first digits, where nearly every key shares one bin, off a single
-// shared-memory address.
+// One digit's histogram over the entries inside the current bucket. Each
+// thread counts a run of equal bins in registers and adds it to the block's
+// shared histogram only when the bin changes: converging lower bounds share
+// most leading digits, so a pass makes few shared-memory atomics instead of
+// one per entry on a single address.
 __global__ void radix_hist_kernel(const SolverCfg cfg, const SolverBufs b, int which, int shift, int bits)
 {
   __shared__ uint32_t h[kRadixBins];
@@ -156,24 +165,35 @@ __global__ void radix_hist_kernel(const SolverCfg cfg, const SolverBufs b, int w
   const uint64_t prefix = rs->prefix, mask = rs->mask;
   const uint32_t dmask = (uint32_t)(nb - 1);
   const int lane = threadIdx.x & 31;
-  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  // warp-uniform trip count: `base` is the same for the 32 lanes
-  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
-    const uint64_t i = base + lane;
-    bool ok = false;
-    uint32_t bin = 0xffffffffu;
-    if (i < n && (sel == nullptr || sel[i] == kSelAlive)) {
-      const uint64_t key = lb_key(lb[i]);
-      if ((key & mask) == prefix) {
-        ok = true;
-        bin = (uint32_t)(key >> shift) & dmask;
-      }
+  // each warp takes chunks of 32 x kHistUnroll consecutive entries and
+  // issues all their loads before it bins them
+  constexpr int kChunk = 32 * kHistUnroll;
+  const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x / 32);
+  uint32_t run_bin = 0, run = 0;
+  for (uint64_t c = (uint64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); c * kChunk < n; c += warps) {
+    double x[kHistUnroll];
+    bool in[kHistUnroll];
+#pragma unroll
+    for (int u = 0; u < kHistUnroll; ++u) {
+      const uint64_t i = c * kChunk + (uint64_t)u * 32 + lane;
+      in[u] = i < n;
+      x[u] = in[u] ? lb[i] : 0.0;
+      if (sel != nullptr && in[u]) in[u] = sel[i] == kSelAlive;
     }
-    if (__any_sync(0xffffffffu, ok)) {
-      const unsigned peers = __match_any_sync(0xffffffffu, bin);
-      if (ok && __ffs(peers) - 1 == lane) atomicAdd(&h[bin], (uint32_t)__popc(peers));
+#pragma unroll
+    for (int u = 0; u < kHistUnroll; ++u) {
+      const uint64_t key = lb_key(x[u]);
+      if (!in[u] || (key & mask) != prefix) continue;
+      const uint32_t bin = (uint32_t)(key >> shift) & dmask;
+      if (bin != run_bin) {
+        if (run) atomicAdd(&h[run_bin], run);
+        run_bin = bin;
+        run = 0;
+      }
+      ++run;
     }
   }
+  if (run) atomicAdd(&h[run_bin], run);
   __syncthreads();
   for (int i = threadIdx.x; i < nb; i += blockDim.x)
     if (h[i]) atomicAdd(&rs->hist[i], h[i]);
@@ -247,24 +267,105 @@ __global__ void __launch_bounds__(kPickThreads) radix_pick_kernel(const SolverBu
 }
 
 // ---------------------------------------------------------------------
-// stable compaction: count -> scan -> scatter, one item per thread
+// stable compaction: count -> scan -> scatter over tiles of kScanTile
+// items; item j of thread t in tile T is T * kScanTile + j * kScanBlock + t,
+// so every pass reads whole cache lines and keeps kScanItems loads in flight
+// per thread.
 // ---------------------------------------------------------------------
-__device__ __forceinline__ int block_excl_rank(bool f, int& total)
+__device__ __forceinline__ uint64_t tile_item(int j)
 {
-  __shared__ int warp_tot[kScanBlock / 32];
+  return (uint64_t)blockIdx.x * kScanTile + (uint64_t)j * kScanBlock + threadIdx.x;
+}
+
+// Ranks of the flagged items of this block's tile in item order; returns
+// the tile's flagged count. One call per kernel.
+__device__ __forceinline__ int tile_ranks(const bool (&f)[kScanItems], int (&rank)[kScanItems])
+{
+  constexpr int kWarps = kScanBlock / 32;
+  constexpr int kPer = kScanItems * kWarps / 32;  // table entries per lane of warp 0
+  __shared__ int tab[kScanItems * kWarps];
+  __shared__ int tile_total;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const unsigned ball = __ballot_sync(0xffffffffu, f);
-  const int in_warp = __popc(ball & ((1u << lane) - 1u));
-  if (lane == 0) warp_tot[wid] = __popc(ball);
-  __syncthreads();
-  int before = 0;
-  total = 0;
-  for (int w = 0; w < kScanBlock / 32; ++w) {
-    if (w < wid) before += warp_tot[w];
-    total += warp_tot[w];
+  unsigned ball[kScanItems];
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    ball[j] = __ballot_sync(0xffffffffu, f[j]);
+    if (lane == 0) tab[j * kWarps + wid] = __popc(ball[j]);
   }
   __syncthreads();
-  return before + in_warp;
+  if (wid == 0) {
+    int v[kPer], sum = 0;
+#pragma unroll
+    for (int e = 0; e < kPer; ++e) {
+      v[e] = tab[lane * kPer + e];
+      sum += v[e];
+    }
+    int x = sum;
+    for (int off = 1; off < 32; off <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, off);
+      if (lane >= off) x += y;
+    }
+    int run = x - sum;
+#pragma unroll
+    for (int e = 0; e < kPer; ++e) {
+      tab[lane * kPer + e] = run;
+      run += v[e];
+    }
+    if (lane == 31) tile_total = x;
+  }
+  __syncthreads();
+  const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) rank[j] = tab[j * kWarps + wid] + __popc(ball[j] & lt);
+  return tile_total;
+}
+
+// Sum of `c` over the block.
+__device__ __forceinline__ int tile_count(int c)
+{
+  __shared__ int tot;
+  if (threadIdx.x == 0) tot = 0;
+  __syncthreads();
+  const int w = __reduce_add_sync(0xffffffffu, c);
+  if ((threadIdx.x & 31) == 0 && w) atomicAdd(&tot, w);
+  __syncthreads();
+  return tot;
+}
+
+// Block totals of per-thread counters, for thread 0 (one global atomic per
+// block instead of one per warp: same-address atomics serialise in L2).
+// Every thread of the block calls it.
+template <int N>
+__device__ __forceinline__ void block_sum(unsigned long long (&v)[N])
+{
+  __shared__ unsigned long long acc[N];
+  if (threadIdx.x < N) acc[threadIdx.x] = 0;
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    unsigned long long x = v[k];
+    for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+    if ((threadIdx.x & 31) == 0 && x) atomicAdd(&acc[k], x);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int k = 0; k < N; ++k) v[k] = acc[k];
+}
+
+// Block minimum of `m`, for thread 0. Every thread of the block calls it.
+__device__ __forceinline__ uint64_t block_min(uint64_t m)
+{
+  __shared__ unsigned long long acc;
+  if (threadIdx.x == 0) acc = ~0ULL;
+  __syncthreads();
+  for (int off = 16; off > 0; off >>= 1) {
+    const uint64_t o = __shfl_down_sync(0xffffffffu, m, off);
+    m = o < m ? o : m;
+  }
+  if ((threadIdx.x & 31) == 0 && m != ~0ULL) atomicMin(&acc, (unsigned long long)m);
+  __syncthreads();
+  return acc;
 }
 
 // Exclusive scan of `nblocks` block counts (one block of 1024 threads);
@@ -281,7 +382,7 @@ __global__ void scan_kernel(const uint32_t* __restrict__ counts, uint32_t* __res
     return;
   }
   const uint64_t n = *n_items;
-  const uint64_t nblocks = (n + kScanBlock - 1) / kScanBlock;
+  const uint64_t nblocks = (n + kScanTile - 1) / kScanTile;
   if (threadIdx.x == 0) carry_s = 0;
   __syncthreads();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -322,13 +423,6 @@ struct SelParents {  // entries of the current pool marked as this iteration's p
   __device__ bool skip() const { return b.dev->done != 0; }
 };
 
-struct AliveEntry {  // entries of the current buffer that stay in the pool
-  SolverBufs b;
-  __device__ uint64_t size() const { return b.dev->extent; }
-  __device__ bool operator()(uint64_t i) const { return b.sel[i] == kSelAlive; }
-  __device__ bool skip() const { return b.dev->done != 0; }
-};
-
 struct KeptChild {
   SolverBufs b;
   __device__ uint64_t size() const { return b.dev->n_children; }
@@ -360,42 +454,100 @@ __global__ void __launch_bounds__(kScanBlock) count_kernel(const P pred, uint32_
 {
   if (pred.skip()) return;
   const uint64_t n = pred.size();
-  const uint64_t i = (uint64_t)blockIdx.x * kScanBlock + threadIdx.x;
-  if ((uint64_t)blockIdx.x * kScanBlock >= n) return;
-  const bool f = i < n && pred(i);
-  const int c = __syncthreads_count(f);
+  if ((uint64_t)blockIdx.x * kScanTile >= n) return;
+  bool f[kScanItems];
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    const uint64_t i = tile_item(j);
+    f[j] = i < n && pred(i);
+  }
+  int c = 0;
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) c += f[j] ? 1 : 0;
+  c = tile_count(c);
   if (threadIdx.x == 0) counts[blockIdx.x] = (uint32_t)c;
 }
 
 // Marks the k smallest (key, position) entries: all keys below the
 // threshold bucket, and the first `k` entries inside it in position order
-// (all of them once the bucket is settled). which = 0 writes kSelParent /
-// kSelAlive over the pool; which = 1 marks alive entries kSelEvicted when
-// they fall outside the cap and leaves the parents' holes as they are.
-__global__ void __launch_bounds__(kScanBlock) mark_kernel(const SolverCfg cfg, const SolverBufs b, int which,
-                                                          const uint32_t* __restrict__ eq_offsets)
+// (all of them once the bucket is settled).
+//   which = 0: writes kSelParent / kSelAlive over the pool and the tile
+//              counts of the parents;
+//   which = 1: marks alive entries outside the cap kSelEvicted (leaving the
+//              parents' holes as they are), folds them into the dropped
+//              floor (search/budget.hpp:190-209) and writes the tile counts
+//              of the entries that stay.
+__global__ void __launch_bounds__(kScanBlock, 2) mark_kernel(const SolverCfg cfg, const SolverBufs b, int which,
+                                                          const uint32_t* __restrict__ eq_offsets,
+                                                          uint32_t* __restrict__ out_counts)
 {
-  const SolverDev* d = b.dev;
+  SolverDev* d = b.dev;
   if (d->done) return;
-  if (which == 1 && !d->evict) return;
   const uint64_t n = rs_n(d, which);
-  if ((uint64_t)blockIdx.x * kScanBlock >= n) return;
-  const uint64_t i = (uint64_t)blockIdx.x * kScanBlock + threadIdx.x;
+  if ((uint64_t)blockIdx.x * kScanTile >= n) return;
   const RadixState* rs = b.radix;
   const bool active = rs->active != 0;
-  const bool alive = i < n && (which == 0 || b.sel[i] == kSelAlive);
-  const uint64_t key = alive ? (lb_key(pool_lb(b)[i]) & rs->mask) : ~0ULL;
-  const bool eq = active && alive && key == rs->prefix;
-  int total;
-  const int rank = block_excl_rank(eq, total);
-  if (!alive) return;
-  bool mark;
-  if (!active) mark = true;
-  else if (key < rs->prefix) mark = true;
-  else if (eq) mark = rs->settled || (uint64_t)eq_offsets[blockIdx.x] + (uint64_t)rank < rs->k;
-  else mark = false;
-  if (which == 0) b.sel[i] = mark ? kSelParent : kSelAlive;
-  else if (!mark) b.sel[i] = kSelEvicted;
+  const uint64_t prefix = rs->prefix, mask = rs->mask;
+  const double* __restrict__ lb = pool_lb(b);
+  bool alive[kScanItems], eq[kScanItems];
+  uint64_t key[kScanItems];
+  double x[kScanItems];
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    const uint64_t i = tile_item(j);
+    alive[j] = i < n && (which == 0 || b.sel[i] == kSelAlive);
+    x[j] = alive[j] ? lb[i] : 0.0;
+  }
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    key[j] = alive[j] ? (lb_key(x[j]) & mask) : ~0ULL;
+    eq[j] = active && alive[j] && key[j] == prefix;
+  }
+  int rank[kScanItems] = {};
+  uint64_t eq_base = 0;
+  if (rs->rank) {  // the same for the whole grid
+    tile_ranks(eq, rank);
+    eq_base = eq_offsets[blockIdx.x];
+  }
+  const double gub = d->gub;
+  int out = 0;
+  uint32_t viable = 0, dominated = 0;
+  uint64_t mkey = ~0ULL;
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    if (!alive[j]) continue;
+    bool mark;
+    if (!active) mark = true;
+    else if (key[j] < prefix) mark = true;
+    else if (eq[j]) mark = rs->settled || eq_base + (uint64_t)rank[j] < rs->k;
+    else mark = false;
+    const uint64_t i = tile_item(j);
+    if (which == 0) {
+      b.sel[i] = mark ? kSelParent : kSelAlive;
+    } else if (!mark) {
+      b.sel[i] = kSelEvicted;
+      if (x[j] <= gub) {
+        ++viable;
+        const uint64_t k = lb_key(x[j]);
+        mkey = k < mkey ? k : mkey;
+      } else {
+        ++dominated;
+      }
+    }
+    out += mark ? 1 : 0;
+  }
+  out = tile_count(out);
+  if (threadIdx.x == 0) out_counts[blockIdx.x] = (uint32_t)out;
+  if (which == 1 && active) {
+    unsigned long long c[2] = {viable, dominated};
+    block_sum(c);
+    mkey = block_min(mkey);
+    if (threadIdx.x == 0) {
+      if (c[0]) atomicAdd((unsigned long long*)&d->counters.dropped_viable, c[0]);
+      if (c[1]) atomicAdd((unsigned long long*)&d->counters.dropped_dominated, c[1]);
+      if (mkey != ~0ULL) atomicMin((unsigned long long*)&d->dropped_min_key, (unsigned long long)mkey);
+    }
+  }
   (void)cfg;
 }
 
@@ -411,8 +563,8 @@ struct GatherParents {
       return;
     }
     for (int v = 0; v < cfg.n_vars; ++v) {
-      const double lo = b.lo[p][(uint64_t)v * cfg.pstride + i];
-      const double hi = b.hi[p][(uint64_t)v * cfg.pstride + i];
+      const double lo = parity_buf(b.lo, p)[(uint64_t)v * cfg.pstride + i];
+      const double hi = parity_buf(b.hi, p)[(uint64_t)v * cfg.pstride + i];
       b.plo[(uint64_t)v * cfg.e_max + pos] = lo;
       b.phi[(uint64_t)v * cfg.e_max + pos] = hi;
       if (b.plo32 != nullptr) {
@@ -420,7 +572,7 @@ struct GatherParents {
         b.phi32[(uint64_t)v * cfg.e_max + pos] = __double2float_ru(hi);
       }
     }
-    b.pdepth[pos] = b.depth[p][i];
+    b.pdepth[pos] = parity_buf(b.depth, p)[i];
   }
 };
 
@@ -435,8 +587,8 @@ struct AppendChild {
     const uint64_t at = b.dev->pool_size + pos;
     const uint64_t k = g >> cfg.log2C, r = g & ((1ULL << cfg.log2C) - 1ULL);
     for (int v = 0; v < cfg.n_vars; ++v) {
-      b.lo[p][(uint64_t)v * cfg.pstride + at] = b.plo[(uint64_t)v * cfg.e_max + k];
-      b.hi[p][(uint64_t)v * cfg.pstride + at] = b.phi[(uint64_t)v * cfg.e_max + k];
+      parity_buf(b.lo, p)[(uint64_t)v * cfg.pstride + at] = b.plo[(uint64_t)v * cfg.e_max + k];
+      parity_buf(b.hi, p)[(uint64_t)v * cfg.pstride + at] = b.phi[(uint64_t)v * cfg.e_max + k];
     }
     const ParentInfo pi = b.pinfo[k];
     const SlotPlan* sp = b.slots + k * (uint64_t)cfg.max_slots;
@@ -444,34 +596,33 @@ struct AppendChild {
       const SlotPlan s = sp[j];
       const uint64_t part = (r / s.prefix) % s.width;
       double lo, hi;
-      slot_bounds((int)s.kind, b.plo[(uint64_t)s.vid * cfg.e_max + k], b.phi[(uint64_t)s.vid * cfg.e_max + k], part,
-                  s.width, lo, hi);
-      b.lo[p][(uint64_t)s.vid * cfg.pstride + at] = lo;
-      b.hi[p][(uint64_t)s.vid * cfg.pstride + at] = hi;
+      slot_bounds(s, b.plo[(uint64_t)s.vid * cfg.e_max + k], b.phi[(uint64_t)s.vid * cfg.e_max + k], part, lo, hi);
+      parity_buf(b.lo, p)[(uint64_t)s.vid * cfg.pstride + at] = lo;
+      parity_buf(b.hi, p)[(uint64_t)s.vid * cfg.pstride + at] = hi;
     }
-    b.lb[p][at] = b.clb[g];
-    b.depth[p][at] = b.pdepth[k] + 1;
+    parity_buf(b.lb, p)[at] = b.clb[g];
+    parity_buf(b.depth, p)[at] = b.pdepth[k] + 1;
     b.sel[at] = kSelAlive;
   }
 };
 
 // move an alive entry of the current buffer to position `pos` of the other
-// buffer. Loads of a group of planes are issued before its stores so that
-// each thread keeps several reads in flight.
+// buffer and return its lb key. Loads of a group of planes are issued
+// before its stores so that each thread keeps several reads in flight.
 struct CopyPool {
   SolverCfg cfg;
   SolverBufs b;
-  __device__ void operator()(uint64_t i, uint64_t pos) const
+  __device__ uint64_t operator()(uint64_t i, uint64_t pos) const
   {
     constexpr int kGroup = 4;
     const uint32_t p = b.dev->parity, q = 1 - p;
-    const double* __restrict__ slo = b.lo[p];
-    const double* __restrict__ shi = b.hi[p];
-    double* __restrict__ dlo = b.lo[q];
-    double* __restrict__ dhi = b.hi[q];
+    const double* __restrict__ slo = parity_buf(b.lo, p);
+    const double* __restrict__ shi = parity_buf(b.hi, p);
+    double* __restrict__ dlo = parity_buf(b.lo, q);
+    double* __restrict__ dhi = parity_buf(b.hi, q);
     const uint64_t ps = cfg.pstride;
-    const double lbv = b.lb[p][i];
-    const uint32_t dep = b.depth[p][i];
+    const double lbv = parity_buf(b.lb, p)[i];
+    const uint32_t dep = parity_buf(b.depth, p)[i];
     for (int v0 = 0; v0 < cfg.n_vars; v0 += kGroup) {
       double l[kGroup], h[kGroup];
 #pragma unroll
@@ -487,8 +638,9 @@ struct CopyPool {
           dhi[(uint64_t)(v0 + u) * ps + pos] = h[u];
         }
     }
-    b.lb[q][pos] = lbv;
-    b.depth[q][pos] = dep;
+    parity_buf(b.lb, q)[pos] = lbv;
+    parity_buf(b.depth, q)[pos] = dep;
+    return lb_key(lbv);
   }
 };
 
@@ -503,12 +655,49 @@ __global__ void __launch_bounds__(kScanBlock) scatter_kernel(const P pred, const
 {
   if (pred.skip()) return;
   const uint64_t n = pred.size();
-  if ((uint64_t)blockIdx.x * kScanBlock >= n) return;
-  const uint64_t i = (uint64_t)blockIdx.x * kScanBlock + threadIdx.x;
-  const bool f = i < n && pred(i);
-  int total;
-  const int rank = block_excl_rank(f, total);
-  if (f) op(i, (uint64_t)offsets[blockIdx.x] + (uint64_t)rank);
+  if ((uint64_t)blockIdx.x * kScanTile >= n) return;
+  bool f[kScanItems];
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    const uint64_t i = tile_item(j);
+    f[j] = i < n && pred(i);
+  }
+  int rank[kScanItems];
+  tile_ranks(f, rank);
+  const uint64_t base = offsets[blockIdx.x];
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j)
+    if (f[j]) op(tile_item(j), base + (uint64_t)rank[j]);
+}
+
+// Moves the alive entries of the current buffer, in order, to the other
+// buffer, and folds their lower bounds into the pool minimum.
+__global__ void __launch_bounds__(kScanBlock, 2) copy_pool_kernel(const SolverCfg cfg, const SolverBufs b,
+                                                               const uint32_t* __restrict__ offsets)
+{
+  SolverDev* d = b.dev;
+  if (d->done) return;
+  const uint64_t n = d->extent;
+  if ((uint64_t)blockIdx.x * kScanTile >= n) return;
+  bool f[kScanItems];
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    const uint64_t i = tile_item(j);
+    f[j] = i < n && b.sel[i] == kSelAlive;
+  }
+  int rank[kScanItems];
+  tile_ranks(f, rank);
+  const uint64_t base = offsets[blockIdx.x];
+  const CopyPool op{cfg, b};
+  uint64_t mkey = ~0ULL;
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j)
+    if (f[j]) {
+      const uint64_t k = op(tile_item(j), base + (uint64_t)rank[j]);
+      mkey = k < mkey ? k : mkey;
+    }
+  mkey = block_min(mkey);
+  if (threadIdx.x == 0 && mkey != ~0ULL) atomicMin((unsigned long long*)&d->pool_min_key, (unsigned long long)mkey);
 }
 
 // ---------------------------------------------------------------------
@@ -536,10 +725,13 @@ __global__ void branch_kernel(const SolverCfg cfg, const SolverBufs b)
       bounded += pi.nreg;
     }
   }
-  if (fathomed) atomicAdd((unsigned long long*)&b.dev->counters.fathomed, (unsigned long long)fathomed);
-  if (fathomed_points)
-    atomicAdd((unsigned long long*)&b.dev->counters.fathomed_points, (unsigned long long)fathomed_points);
-  if (bounded) atomicAdd((unsigned long long*)&b.dev->counters.bounded, (unsigned long long)bounded);
+  unsigned long long c[3] = {fathomed, fathomed_points, bounded};
+  block_sum(c);
+  if (threadIdx.x == 0) {
+    if (c[0]) atomicAdd((unsigned long long*)&b.dev->counters.fathomed, c[0]);
+    if (c[1]) atomicAdd((unsigned long long*)&b.dev->counters.fathomed_points, c[1]);
+    if (c[2]) atomicAdd((unsigned long long*)&b.dev->counters.bounded, c[2]);
+  }
 }
 
 // ---------------------------------------------------------------------
@@ -576,19 +768,14 @@ __global__ void prune_count_kernel(const SolverCfg cfg, const SolverBufs b)
     else if (s == kChildDominated || b.clb[g] > gub) ++dom;
     else ++kept;
   }
-  for (int off = 16; off > 0; off >>= 1) {
-    dup += __shfl_down_sync(0xffffffffu, dup, off);
-    inf += __shfl_down_sync(0xffffffffu, inf, off);
-    dom += __shfl_down_sync(0xffffffffu, dom, off);
-    kept += __shfl_down_sync(0xffffffffu, kept, off);
-    sampled += __shfl_down_sync(0xffffffffu, sampled, off);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    if (dup) atomicAdd((unsigned long long*)&d->counters.pruned_duplicate, dup);
-    if (inf) atomicAdd((unsigned long long*)&d->counters.pruned_infeasible, inf);
-    if (dom) atomicAdd((unsigned long long*)&d->counters.pruned_dominated, dom);
-    if (kept) atomicAdd((unsigned long long*)&d->counters.enqueued, kept);
-    if (sampled) atomicAdd((unsigned long long*)&d->counters.sampled, sampled * cfg.S);
+  unsigned long long c[5] = {dup, inf, dom, kept, sampled};
+  block_sum(c);
+  if (threadIdx.x == 0) {
+    if (c[0]) atomicAdd((unsigned long long*)&d->counters.pruned_duplicate, c[0]);
+    if (c[1]) atomicAdd((unsigned long long*)&d->counters.pruned_infeasible, c[1]);
+    if (c[2]) atomicAdd((unsigned long long*)&d->counters.pruned_dominated, c[2]);
+    if (c[3]) atomicAdd((unsigned long long*)&d->counters.enqueued, c[3]);
+    if (c[4]) atomicAdd((unsigned long long*)&d->counters.sampled, c[4] * cfg.S);
   }
 }
 
@@ -607,16 +794,13 @@ __global__ void eval_count_kernel(const SolverCfg cfg, const SolverBufs b)
     ++valid;
     if (s == kChildInfeasible || s == kChildDominated) ++excluded;
   }
-  for (int off = 16; off > 0; off >>= 1) {
-    valid += __shfl_down_sync(0xffffffffu, valid, off);
-    excluded += __shfl_down_sync(0xffffffffu, excluded, off);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    if (valid) atomicAdd((unsigned long long*)&d->iter_valid, valid);
-    if (excluded) atomicAdd((unsigned long long*)&d->iter_excluded, excluded);
-    if (valid && fp32 && d->use_screen)
-      atomicAdd((unsigned long long*)&d->counters.screened_fp32, valid);
-    if (valid && !fp32) atomicAdd((unsigned long long*)&d->counters.certified_fp64, valid);
+  unsigned long long c[2] = {valid, excluded};
+  block_sum(c);
+  if (threadIdx.x == 0) {
+    if (c[0]) atomicAdd((unsigned long long*)&d->iter_valid, c[0]);
+    if (c[1]) atomicAdd((unsigned long long*)&d->iter_excluded, c[1]);
+    if (c[0] && fp32 && d->use_screen) atomicAdd((unsigned long long*)&d->counters.screened_fp32, c[0]);
+    if (c[0] && !fp32) atomicAdd((unsigned long long*)&d->counters.certified_fp64, c[0]);
   }
 }
 
@@ -647,40 +831,7 @@ __global__ void size_kernel(const SolverCfg cfg, const SolverBufs b)
   d->new_size = d->remaining + d->kept;
   d->extent = d->pool_size + d->kept;
   d->evict = d->new_size > cfg.cap ? 1 : 0;
-}
-
-// fold evicted entries into the dropped floor (search/budget.hpp:190-209)
-__global__ void evict_account_kernel(const SolverBufs b)
-{
-  SolverDev* d = b.dev;
-  if (d->done || !d->evict) return;
-  const uint64_t n = d->extent;
-  const double gub = d->gub;
-  const double* lb = b.lb[d->parity];
-  unsigned long long viable = 0, dominated = 0;
-  uint64_t mkey = ~0ULL;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-    if (b.sel[i] != kSelEvicted) continue;
-    const double x = lb[i];
-    if (x <= gub) {
-      ++viable;
-      const uint64_t k = lb_key(x);
-      mkey = k < mkey ? k : mkey;
-    } else {
-      ++dominated;
-    }
-  }
-  for (int off = 16; off > 0; off >>= 1) {
-    viable += __shfl_down_sync(0xffffffffu, viable, off);
-    dominated += __shfl_down_sync(0xffffffffu, dominated, off);
-    const uint64_t o = __shfl_down_sync(0xffffffffu, mkey, off);
-    mkey = o < mkey ? o : mkey;
-  }
-  if ((threadIdx.x & 31) == 0) {
-    if (viable) atomicAdd((unsigned long long*)&d->counters.dropped_viable, viable);
-    if (dominated) atomicAdd((unsigned long long*)&d->counters.dropped_dominated, dominated);
-    if (mkey != ~0ULL) atomicMin((unsigned long long*)&d->dropped_min_key, (unsigned long long)mkey);
-  }
+  d->pool_min_key = ~0ULL;  // refilled by the move to the other buffer
 }
 
 __global__ void finish_kernel(const SolverCfg cfg, const SolverBufs b)
@@ -695,14 +846,13 @@ __global__ void finish_kernel(const SolverCfg cfg, const SolverBufs b)
   d->parity = 1 - d->parity;
   if (d->dropped_min_key != ~0ULL) d->dropped_lb_min = key_to_lb(d->dropped_min_key);
   if (d->pool_size > d->counters.peak_frontier) d->counters.peak_frontier = d->pool_size;
-  d->pool_min_key = ~0ULL;
 }
 
 __global__ void pool_min_kernel(const SolverBufs b, uint64_t* viable_out)
 {
   SolverDev* d = b.dev;
   const uint64_t n = d->pool_size;
-  const double* lb = b.lb[d->parity];
+  const double* lb = parity_buf(b.lb, d->parity);
   const double gub = d->gub;
   uint64_t mkey = ~0ULL;
   unsigned long long viable = 0;
@@ -711,14 +861,12 @@ __global__ void pool_min_kernel(const SolverBufs b, uint64_t* viable_out)
     mkey = k < mkey ? k : mkey;
     if (lb[i] <= gub) ++viable;
   }
-  for (int off = 16; off > 0; off >>= 1) {
-    const uint64_t o = __shfl_down_sync(0xffffffffu, mkey, off);
-    mkey = o < mkey ? o : mkey;
-    viable += __shfl_down_sync(0xffffffffu, viable, off);
-  }
-  if ((threadIdx.x & 31) == 0) {
+  unsigned long long c[1] = {viable};
+  block_sum(c);
+  mkey = block_min(mkey);
+  if (threadIdx.x == 0) {
     if (mkey != ~0ULL) atomicMin((unsigned long long*)&d->pool_min_key, (unsigned long long)mkey);
-    if (viable_out && viable) atomicAdd((unsigned long long*)viable_out, viable);
+    if (viable_out && c[0]) atomicAdd((unsigned long long*)viable_out, c[0]);
   }
 }
 
@@ -731,22 +879,26 @@ __global__ void pool_min_reset_kernel(const SolverBufs b, uint64_t* viable_out)
 // ---------------------------------------------------------------------
 // host: enqueue one iteration
 // ---------------------------------------------------------------------
-template <class P>
-static cudaError_t compact(const P& pred, uint64_t max_items, const uint64_t* n_items_dev, uint64_t* total_dev,
-                           const SolverBufs& b, const uint32_t* active, cudaStream_t s)
+static int tiles(uint64_t max_items) { return (int)((max_items + kScanTile - 1) / kScanTile); }
+
+static void scan(const SolverBufs& b, const uint64_t* n_items_dev, uint64_t* total_dev, const uint32_t* active,
+                 cudaStream_t s)
 {
-  const int grid = (int)((max_items + kScanBlock - 1) / kScanBlock);
-  count_kernel<P><<<grid, kScanBlock, 0, s>>>(pred, b.block_counts);
   scan_kernel<<<1, 1024, 0, s>>>(b.block_counts, b.block_offsets, n_items_dev, total_dev, active, &b.dev->done);
-  return cudaGetLastError();
+}
+
+template <class P>
+static void compact(const P& pred, uint64_t max_items, const uint64_t* n_items_dev, uint64_t* total_dev,
+                    const SolverBufs& b, const uint32_t* active, cudaStream_t s)
+{
+  count_kernel<P><<<tiles(max_items), kScanBlock, 0, s>>>(pred, b.block_counts);
+  scan(b, n_items_dev, total_dev, active, s);
 }
 
 template <class P, class Op>
-static cudaError_t scatter(const P& pred, const Op& op, uint64_t max_items, cudaStream_t s, const SolverBufs& b)
+static void scatter(const P& pred, const Op& op, uint64_t max_items, cudaStream_t s, const SolverBufs& b)
 {
-  const int grid = (int)((max_items + kScanBlock - 1) / kScanBlock);
-  scatter_kernel<P, Op><<<grid, kScanBlock, 0, s>>>(pred, op, b.block_offsets);
-  return cudaGetLastError();
+  scatter_kernel<P, Op><<<tiles(max_items), kScanBlock, 0, s>>>(pred, op, b.block_offsets);
 }
 
 static void radix_select(const SolverCfg& cfg, const SolverBufs& b, int which, uint64_t max_items, cudaStream_t s)
@@ -761,12 +913,13 @@ static void radix_select(const SolverCfg& cfg, const SolverBufs& b, int which, u
     radix_hist_kernel<<<grid, 256, 0, s>>>(cfg, b, which, shifts[p], bits[p]);
     radix_pick_kernel<<<1, kPickThreads, 0, s>>>(b, shifts[p], bits[p]);
   }
-  // ranks among entries inside the threshold bucket, then the marks
+  // ranks among entries inside the threshold bucket, then the marks with
+  // the tile counts of the entries the next compaction moves
   const uint64_t* n_dev = which == 0 ? &b.dev->pool_size : &b.dev->extent;
   EqKey eq{b, which};
   compact(eq, max_items, n_dev, nullptr, b, &b.radix->rank, s);
-  const int mgrid = (int)((max_items + kScanBlock - 1) / kScanBlock);
-  mark_kernel<<<mgrid, kScanBlock, 0, s>>>(cfg, b, which, b.block_offsets);
+  mark_kernel<<<tiles(max_items), kScanBlock, 0, s>>>(cfg, b, which, b.block_offsets, b.block_counts);
+  scan(b, n_dev, which == 0 ? nullptr : &b.dev->survivors, nullptr, s);
 }
 
 static void mark(const cudaEvent_t* marks, int i, cudaStream_t s)
@@ -784,9 +937,7 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
 
   // (1) select the E best parents and stage them
   radix_select(cfg, b, 0, cfg.cap, s);
-  SelParents selected{b};
-  compact(selected, cfg.cap, &b.dev->pool_size, nullptr, b, nullptr, s);
-  scatter(selected, GatherParents{cfg, b}, cfg.cap, s, b);
+  scatter(SelParents{b}, GatherParents{cfg, b}, cfg.cap, s, b);
 
   // (2) branch
   {
@@ -840,7 +991,7 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
     if (e != cudaSuccess) return e;
   }
   {
-    const int grid = (int)std::min<uint64_t>((max_children + 255) / 256, 4096);
+    const int grid = (int)std::min<uint64_t>((max_children + 255) / 256, 1024);
     eval_count_kernel<<<grid, 256, 0, s>>>(cfg, b);
     if (cfg.precision == CMN_PRECISION_FP32_SCREEN) {
       certify_count_kernel<<<1, 1, 0, s>>>(b);
@@ -890,7 +1041,7 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
 
   // (5) prune with the new incumbent and rebuild the pool
   {
-    const int grid = (int)std::min<uint64_t>((max_children + 255) / 256, 4096);
+    const int grid = (int)std::min<uint64_t>((max_children + 255) / 256, 1024);
     prune_count_kernel<<<grid, 256, 0, s>>>(cfg, b);
   }
   // the kept children go behind the pool in the current buffer; the
@@ -903,18 +1054,8 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
   // (6) over the cap: keep the `cap` best alive entries, fold the rest into
   // the floor; then move every alive entry to the other buffer in order
   radix_select(cfg, b, 1, max_pool, s);
-  {
-    const int grid = (int)std::min<uint64_t>((max_pool + 255) / 256, 4096);
-    evict_account_kernel<<<grid, 256, 0, s>>>(b);
-  }
-  AliveEntry alive{b};
-  compact(alive, max_pool, &b.dev->extent, &b.dev->survivors, b, nullptr, s);
-  scatter(alive, CopyPool{cfg, b}, max_pool, s, b);
+  copy_pool_kernel<<<tiles(max_pool), kScanBlock, 0, s>>>(cfg, b, b.block_offsets);
   finish_kernel<<<1, 1, 0, s>>>(cfg, b);
-  {
-    const int grid = (int)std::min<uint64_t>((max_pool + 255) / 256, 4096);
-    pool_min_kernel<<<grid, 256, 0, s>>>(b, nullptr);
-  }
   mark(marks, 4, s);
   return cudaGetLastError();
 }

@@ -907,11 +907,13 @@ extern "C" cmn_status cmn_solver_create(const cmn_problem* p, const cmn_solve_op
     A(&b.dev, 1);
     A(&b.radix, 1);
     for (int q = 0; q < 2; ++q) {
-      A(&b.lo[q], (size_t)n * cfg.pstride);
-      A(&b.hi[q], (size_t)n * cfg.pstride);
       A(&b.lb[q], cfg.pstride);
-      A(&b.depth[q], cfg.pstride);
+      A(&b.slot[q], cfg.pstride);
     }
+    A(&b.lo, (size_t)n * cfg.pstride);
+    A(&b.hi, (size_t)n * cfg.pstride);
+    A(&b.depth, cfg.pstride);
+    A(&b.free_slots, cfg.pstride);
     A(&b.sel, cfg.pstride);
     A(&b.plo, (size_t)n * cfg.e_max);
     A(&b.phi, (size_t)n * cfg.e_max);
@@ -1075,19 +1077,30 @@ extern "C" cmn_status cmn_solver_frontier(cmn_solver* s, double* boxes, double* 
   if (m == 0) return CMN_OK;
   const uint32_t q = s->h_dev->parity;
   const int64_t n = s->p->host.n_vars();
-  if (boxes) {
-    std::vector<double> plane(m);
-    for (int64_t v = 0; v < n; ++v) {
-      for (int side = 0; side < 2; ++side) {
-        const double* src = (side == 0 ? s->b.lo[q] : s->b.hi[q]) + (uint64_t)v * s->cfg.pstride;
-        CK(cudaMemcpyAsync(plane.data(), src, m * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
-        CK(cudaStreamSynchronize(s->stream));
-        for (uint64_t i = 0; i < m; ++i) boxes[i * 2 * n + 2 * v + side] = plane[i];
-      }
-    }
-  }
   if (lower_bounds) CK(cudaMemcpyAsync(lower_bounds, s->b.lb[q], m * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
-  if (depths) CK(cudaMemcpyAsync(depths, s->b.depth[q], m * sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream));
+  if (boxes || depths) {
+    // unpack the boxes from the store in chunks of about 64 MB
+    const uint64_t per = (uint64_t)(2 * n) * sizeof(double) + sizeof(uint32_t);
+    const uint64_t chunk = std::max<uint64_t>(1, std::min<uint64_t>(m, (64ULL << 20) / per));
+    double* d_boxes = nullptr;
+    uint32_t* d_depths = nullptr;
+    CK(cudaMalloc(&d_boxes, chunk * 2 * (uint64_t)n * sizeof(double) + 16));
+    cudaError_t e = cudaMalloc(&d_depths, chunk * sizeof(uint32_t));
+    for (uint64_t start = 0; e == cudaSuccess && start < m; start += chunk) {
+      const uint64_t c = std::min(chunk, m - start);
+      e = solver_frontier_gather(s->cfg, s->b, start, c, boxes ? d_boxes : nullptr, depths ? d_depths : nullptr,
+                                 s->stream);
+      if (e == cudaSuccess && boxes)
+        e = cudaMemcpyAsync(boxes + start * 2 * n, d_boxes, c * 2 * n * sizeof(double), cudaMemcpyDeviceToHost,
+                            s->stream);
+      if (e == cudaSuccess && depths)
+        e = cudaMemcpyAsync(depths + start, d_depths, c * sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    }
+    cudaFree(d_depths);
+    cudaFree(d_boxes);
+    CK(e);
+  }
   CK(cudaStreamSynchronize(s->stream));
   return CMN_OK;
 }

@@ -725,14 +725,34 @@ __device__ __forceinline__ double sample_value(bool discrete, double lb, double 
   return __dadd_rn(lo, __ull2double_rn(idx));
 }
 
-// Total order on doubles for selection keys (NaN last).
-__device__ __forceinline__ uint64_t lb_key(double x)
+// Total order on doubles for selection keys (NaN last), from the raw bits.
+// The pool passes stay on the integer pipe: FP64 instructions, even
+// compares, issue at a small fraction of the integer rate on this part.
+__device__ __forceinline__ uint64_t bits_key(uint64_t u)
 {
-  // integer NaN test: an FP64 compare would run on the FP64 pipe, which
-  // bounds the pool passes on this part
-  const uint64_t u = (uint64_t)__double_as_longlong(x);
   if ((u & 0x7fffffffffffffffULL) > 0x7ff0000000000000ULL) return ~0ULL;
   return (u >> 63) ? ~u : (u | 0x8000000000000000ULL);
 }
+
+__device__ __forceinline__ uint64_t lb_key(double x) { return bits_key((uint64_t)__double_as_longlong(x)); }
+
+// IEEE `a <= b` on the raw bits of two doubles (false if either is NaN;
+// -0 equals +0), on the integer pipe.
+__device__ __forceinline__ bool bits_le(uint64_t a, uint64_t b)
+{
+  const uint64_t am = a & 0x7fffffffffffffffULL, bm = b & 0x7fffffffffffffffULL;
+  if (am > 0x7ff0000000000000ULL || bm > 0x7ff0000000000000ULL) return false;
+  return bits_key(am == 0 ? 0 : a) <= bits_key(bm == 0 ? 0 : b);
+}
+
+// IEEE `a < b` on the raw bits, as bits_le.
+__device__ __forceinline__ bool bits_lt(uint64_t a, uint64_t b)
+{
+  const uint64_t am = a & 0x7fffffffffffffffULL, bm = b & 0x7fffffffffffffffULL;
+  if (am > 0x7ff0000000000000ULL || bm > 0x7ff0000000000000ULL) return false;
+  return bits_key(am == 0 ? 0 : a) < bits_key(bm == 0 ? 0 : b);
+}
+
+__device__ __forceinline__ uint64_t dbits(double x) { return (uint64_t)__double_as_longlong(x); }
 
 }  // namespace cmn

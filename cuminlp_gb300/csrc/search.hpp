@@ -55,6 +55,7 @@ struct SolverDev {
   uint64_t new_size;       // remaining + kept: the rebuilt pool before eviction
   uint64_t extent;         // pool_size + kept: entries of the current buffer
   uint64_t survivors;      // entries moved to the other buffer
+  uint64_t free_top;       // free box-store slots (height of the free stack)
   uint64_t certify_count;
   uint64_t evict;          // 1 when the rebuilt pool exceeds the cap
   uint64_t dropped_min_key;
@@ -99,11 +100,16 @@ struct SolverCfg {
 struct SolverBufs {
   SolverDev* dev;
   RadixState* radix;
-  // pools (two parities): planes [v * pstride + i]
-  double* lo[2];
-  double* hi[2];
+  // the pool in position order (two parities): lower bound and box slot
   double* lb[2];
-  uint32_t* depth[2];
+  uint32_t* slot[2];
+  // box store: planes [v * pstride + slot] and depth [slot]. A box keeps its
+  // slot from its append until it is expanded or evicted, so rebuilding the
+  // pool moves 12 bytes per entry instead of the whole box.
+  double* lo;
+  double* hi;
+  uint32_t* depth;
+  uint32_t* free_slots;  // stack of free store slots (free_top entries)
   // marks over the current buffer: kSelAlive, kSelParent (expanded this
   // iteration: a hole), kSelEvicted (dropped by the cap)
   uint8_t* sel;
@@ -148,6 +154,10 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
                              cudaStream_t s, const cudaEvent_t* marks);
 // Fills min key / viable count of the current pool (after the run).
 cudaError_t solver_pool_stats(const SolverCfg& cfg, const SolverBufs& b, uint64_t* viable_dev, cudaStream_t s);
+// Copies pool entries [start, start + count) in position order: boxes as
+// [i][v] (lo, hi) pairs and depths (either may be null).
+cudaError_t solver_frontier_gather(const SolverCfg& cfg, const SolverBufs& b, uint64_t start, uint64_t count,
+                                   double* boxes, uint32_t* depths, cudaStream_t s);
 
 
 }  // namespace cmn

@@ -37,9 +37,9 @@ __global__ void init_kernel(const SolverCfg cfg, const SolverBufs b, const doubl
                             const double* __restrict__ root_ub, double gub0)
 {
   const int t = threadIdx.x + blockIdx.x * blockDim.x;
-  for (int v = t; v < cfg.n_vars; v += blockDim.x * gridDim.x) {
-    b.lo[0][(uint64_t)v * cfg.pstride] = root_lb[v];
-    b.hi[0][(uint64_t)v * cfg.pstride] = root_ub[v];
+  for (int v = t; v < cfg.n_vars; v += blockDim.x * gridDim.x) {  // the root box in store slot 0
+    b.lo[(uint64_t)v * cfg.pstride] = root_lb[v];
+    b.hi[(uint64_t)v * cfg.pstride] = root_ub[v];
   }
   if (t == 0) {
     SolverDev* d = b.dev;
@@ -49,13 +49,23 @@ __global__ void init_kernel(const SolverCfg cfg, const SolverBufs b, const doubl
     d->dropped_lb_min = INFINITY;
     d->dropped_min_key = ~0ULL;
     b.lb[0][0] = -DBL_MAX;
-    b.depth[0][0] = 0;
+    b.slot[0][0] = 0;
+    b.depth[0] = 0;
+    d->free_top = cfg.pstride - 1;
     d->pool_size = 1;
     d->pool_min_key = lb_key(-DBL_MAX);
     d->parity = 0;
     d->use_screen = 1;
     d->counters.peak_frontier = 1;
   }
+}
+
+// every store slot but the root's is free; pops take the low slots first
+__global__ void free_init_kernel(const SolverCfg cfg, const SolverBufs b)
+{
+  const uint64_t n = cfg.pstride - 1;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    b.free_slots[i] = (uint32_t)(cfg.pstride - 1 - i);
 }
 
 // Top of the loop of search/driver.hpp:221-233: convergence of the least
@@ -160,7 +170,7 @@ __global__ void radix_hist_kernel(const SolverCfg cfg, const SolverBufs b, int w
   const int nb = 1 << bits;
   for (int i = threadIdx.x; i < nb; i += blockDim.x) h[i] = 0;
   __syncthreads();
-  const double* __restrict__ lb = pool_lb(b);
+  const uint64_t* __restrict__ lb = reinterpret_cast<const uint64_t*>(pool_lb(b));
   const uint8_t* __restrict__ sel = which == 1 ? b.sel : nullptr;
   const uint64_t prefix = rs->prefix, mask = rs->mask;
   const uint32_t dmask = (uint32_t)(nb - 1);
@@ -171,18 +181,18 @@ __global__ void radix_hist_kernel(const SolverCfg cfg, const SolverBufs b, int w
   const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x / 32);
   uint32_t run_bin = 0, run = 0;
   for (uint64_t c = (uint64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); c * kChunk < n; c += warps) {
-    double x[kHistUnroll];
+    uint64_t x[kHistUnroll];
     bool in[kHistUnroll];
 #pragma unroll
     for (int u = 0; u < kHistUnroll; ++u) {
       const uint64_t i = c * kChunk + (uint64_t)u * 32 + lane;
       in[u] = i < n;
-      x[u] = in[u] ? lb[i] : 0.0;
+      x[u] = in[u] ? lb[i] : 0;
       if (sel != nullptr && in[u]) in[u] = sel[i] == kSelAlive;
     }
 #pragma unroll
     for (int u = 0; u < kHistUnroll; ++u) {
-      const uint64_t key = lb_key(x[u]);
+      const uint64_t key = bits_key(x[u]);
       if (!in[u] || (key & mask) != prefix) continue;
       const uint32_t bin = (uint32_t)(key >> shift) & dmask;
       if (bin != run_bin) {
@@ -272,10 +282,11 @@ __global__ void __launch_bounds__(kPickThreads) radix_pick_kernel(const SolverBu
 // so every pass reads whole cache lines and keeps kScanItems loads in flight
 // per thread.
 // ---------------------------------------------------------------------
-__device__ __forceinline__ uint64_t tile_item(int j)
-{
-  return (uint64_t)blockIdx.x * kScanTile + (uint64_t)j * kScanBlock + threadIdx.x;
-}
+// first item of this thread in its block's tile, read once per kernel (the
+// special registers are slow to re-read)
+__device__ __forceinline__ uint64_t tile_first() { return (uint64_t)blockIdx.x * kScanTile + threadIdx.x; }
+
+__device__ __forceinline__ uint64_t tile_item(uint64_t t0, int j) { return t0 + (uint64_t)j * kScanBlock; }
 
 // Ranks of the flagged items of this block's tile in item order; returns
 // the tile's flagged count. One call per kernel.
@@ -416,17 +427,13 @@ __global__ void scan_kernel(const uint32_t* __restrict__ counts, uint32_t* __res
 }
 
 // ---- predicates / operations -----------------------------------------
-struct SelParents {  // entries of the current pool marked as this iteration's parents
-  SolverBufs b;
-  __device__ uint64_t size() const { return b.dev->pool_size; }
-  __device__ bool operator()(uint64_t i) const { return b.sel[i] == kSelParent; }
-  __device__ bool skip() const { return b.dev->done != 0; }
-};
-
 struct KeptChild {
   SolverBufs b;
   __device__ uint64_t size() const { return b.dev->n_children; }
-  __device__ bool operator()(uint64_t g) const { return b.cstate[g] == kChildEligible && !(b.clb[g] > b.dev->gub); }
+  __device__ bool operator()(uint64_t g) const
+  {
+    return b.cstate[g] == kChildEligible && !bits_lt(dbits(b.dev->gub), dbits(b.clb[g]));
+  }
   __device__ bool skip() const { return b.dev->done != 0; }
 };
 
@@ -452,13 +459,14 @@ struct EqKey {  // alive entries inside the radix threshold bucket
 template <class P>
 __global__ void __launch_bounds__(kScanBlock) count_kernel(const P pred, uint32_t* __restrict__ counts)
 {
+  const uint64_t t0 = tile_first();
   if (pred.skip()) return;
   const uint64_t n = pred.size();
   if ((uint64_t)blockIdx.x * kScanTile >= n) return;
   bool f[kScanItems];
 #pragma unroll
   for (int j = 0; j < kScanItems; ++j) {
-    const uint64_t i = tile_item(j);
+    const uint64_t i = tile_item(t0, j);
     f[j] = i < n && pred(i);
   }
   int c = 0;
@@ -471,8 +479,8 @@ __global__ void __launch_bounds__(kScanBlock) count_kernel(const P pred, uint32_
 // Marks the k smallest (key, position) entries: all keys below the
 // threshold bucket, and the first `k` entries inside it in position order
 // (all of them once the bucket is settled).
-//   which = 0: writes kSelParent / kSelAlive over the pool and the tile
-//              counts of the parents;
+//   which = 0: marks the parents kSelParent (every entry of the pool is
+//              kSelAlive before) and writes the tile counts of the parents;
 //   which = 1: marks alive entries outside the cap kSelEvicted (leaving the
 //              parents' holes as they are), folds them into the dropped
 //              floor (search/budget.hpp:190-209) and writes the tile counts
@@ -481,55 +489,58 @@ __global__ void __launch_bounds__(kScanBlock, 2) mark_kernel(const SolverCfg cfg
                                                           const uint32_t* __restrict__ eq_offsets,
                                                           uint32_t* __restrict__ out_counts)
 {
+  const uint64_t t0 = tile_first();
   SolverDev* d = b.dev;
-  if (d->done) return;
+  // the control words and the tile's entries are loaded together: a tile is
+  // short, so a chain of dependent loads would set its duration
+  const uint32_t done = d->done;
   const uint64_t n = rs_n(d, which);
+  const uint64_t* __restrict__ lb = reinterpret_cast<const uint64_t*>(pool_lb(b));
+  uint64_t x[kScanItems];  // raw bits of the lower bounds
+  uint8_t sv[kScanItems];
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    const uint64_t i = tile_item(t0, j);
+    const bool inb = i < cfg.pstride;
+    x[j] = inb ? lb[i] : 0;
+    sv[j] = (which == 1 && inb) ? b.sel[i] : kSelAlive;
+  }
+  if (done) return;
   if ((uint64_t)blockIdx.x * kScanTile >= n) return;
   const RadixState* rs = b.radix;
-  const bool active = rs->active != 0;
-  const uint64_t prefix = rs->prefix, mask = rs->mask;
-  const double* __restrict__ lb = pool_lb(b);
+  const bool active = rs->active != 0, settled = rs->settled != 0, ranked = rs->rank != 0;
+  const uint64_t prefix = rs->prefix, mask = rs->mask, kth = rs->k;
+  const uint64_t gub = (uint64_t)__double_as_longlong(d->gub);
   bool alive[kScanItems], eq[kScanItems];
-  uint64_t key[kScanItems];
-  double x[kScanItems];
 #pragma unroll
-  for (int j = 0; j < kScanItems; ++j) {
-    const uint64_t i = tile_item(j);
-    alive[j] = i < n && (which == 0 || b.sel[i] == kSelAlive);
-    x[j] = alive[j] ? lb[i] : 0.0;
-  }
+  for (int j = 0; j < kScanItems; ++j) alive[j] = tile_item(t0, j) < n && sv[j] == kSelAlive;
 #pragma unroll
-  for (int j = 0; j < kScanItems; ++j) {
-    key[j] = alive[j] ? (lb_key(x[j]) & mask) : ~0ULL;
-    eq[j] = active && alive[j] && key[j] == prefix;
-  }
+  for (int j = 0; j < kScanItems; ++j) eq[j] = active && alive[j] && (bits_key(x[j]) & mask) == prefix;
   int rank[kScanItems] = {};
   uint64_t eq_base = 0;
-  if (rs->rank) {  // the same for the whole grid
+  if (ranked) {  // the same for the whole grid
     tile_ranks(eq, rank);
     eq_base = eq_offsets[blockIdx.x];
   }
-  const double gub = d->gub;
   int out = 0;
   uint32_t viable = 0, dominated = 0;
   uint64_t mkey = ~0ULL;
 #pragma unroll
   for (int j = 0; j < kScanItems; ++j) {
     if (!alive[j]) continue;
+    const uint64_t key = bits_key(x[j]);
     bool mark;
     if (!active) mark = true;
-    else if (key[j] < prefix) mark = true;
-    else if (eq[j]) mark = rs->settled || eq_base + (uint64_t)rank[j] < rs->k;
-    else mark = false;
-    const uint64_t i = tile_item(j);
+    else if (eq[j]) mark = settled || eq_base + (uint64_t)rank[j] < kth;
+    else mark = (key & mask) < prefix;
+    const uint64_t i = tile_item(t0, j);
     if (which == 0) {
-      b.sel[i] = mark ? kSelParent : kSelAlive;
+      if (mark) b.sel[i] = kSelParent;  // the others are kSelAlive already
     } else if (!mark) {
       b.sel[i] = kSelEvicted;
-      if (x[j] <= gub) {
+      if (bits_le(x[j], gub)) {
         ++viable;
-        const uint64_t k = lb_key(x[j]);
-        mkey = k < mkey ? k : mkey;
+        mkey = key < mkey ? key : mkey;
       } else {
         ++dominated;
       }
@@ -557,14 +568,14 @@ struct GatherParents {
   SolverBufs b;
   __device__ void operator()(uint64_t i, uint64_t pos) const
   {
-    const uint32_t p = b.dev->parity;
+    const uint64_t s = parity_buf(b.slot, b.dev->parity)[i];
     if (pos >= cfg.e_max) {  // more marks than parents: never written, flagged
       b.dev->error = 1;
       return;
     }
     for (int v = 0; v < cfg.n_vars; ++v) {
-      const double lo = parity_buf(b.lo, p)[(uint64_t)v * cfg.pstride + i];
-      const double hi = parity_buf(b.hi, p)[(uint64_t)v * cfg.pstride + i];
+      const double lo = b.lo[(uint64_t)v * cfg.pstride + s];
+      const double hi = b.hi[(uint64_t)v * cfg.pstride + s];
       b.plo[(uint64_t)v * cfg.e_max + pos] = lo;
       b.phi[(uint64_t)v * cfg.e_max + pos] = hi;
       if (b.plo32 != nullptr) {
@@ -572,75 +583,44 @@ struct GatherParents {
         b.phi32[(uint64_t)v * cfg.e_max + pos] = __double2float_ru(hi);
       }
     }
-    b.pdepth[pos] = parity_buf(b.depth, p)[i];
+    b.pdepth[pos] = b.depth[s];
   }
 };
 
-// decode a kept child from its parent and append it behind the pool in
-// the current buffer (positions pool_size + pos)
+// decode a kept child from its parent into a free store slot and append it
+// behind the pool in the current buffer (position pool_size + pos)
 struct AppendChild {
   SolverCfg cfg;
   SolverBufs b;
   __device__ void operator()(uint64_t g, uint64_t pos) const
   {
-    const uint32_t p = b.dev->parity;
-    const uint64_t at = b.dev->pool_size + pos;
+    const SolverDev* d = b.dev;
+    if (pos >= d->free_top) {  // more children than free slots: never expected
+      b.dev->error = 1;
+      return;
+    }
+    const uint64_t s = b.free_slots[d->free_top - 1 - pos];
+    const uint64_t at = d->pool_size + pos;
     const uint64_t k = g >> cfg.log2C, r = g & ((1ULL << cfg.log2C) - 1ULL);
     for (int v = 0; v < cfg.n_vars; ++v) {
-      parity_buf(b.lo, p)[(uint64_t)v * cfg.pstride + at] = b.plo[(uint64_t)v * cfg.e_max + k];
-      parity_buf(b.hi, p)[(uint64_t)v * cfg.pstride + at] = b.phi[(uint64_t)v * cfg.e_max + k];
+      b.lo[(uint64_t)v * cfg.pstride + s] = b.plo[(uint64_t)v * cfg.e_max + k];
+      b.hi[(uint64_t)v * cfg.pstride + s] = b.phi[(uint64_t)v * cfg.e_max + k];
     }
     const ParentInfo pi = b.pinfo[k];
     const SlotPlan* sp = b.slots + k * (uint64_t)cfg.max_slots;
     for (uint32_t j = 0; j < pi.count; ++j) {
-      const SlotPlan s = sp[j];
-      const uint64_t part = (r / s.prefix) % s.width;
+      const SlotPlan sj = sp[j];
+      const uint64_t part = (r / sj.prefix) % sj.width;
       double lo, hi;
-      slot_bounds(s, b.plo[(uint64_t)s.vid * cfg.e_max + k], b.phi[(uint64_t)s.vid * cfg.e_max + k], part, lo, hi);
-      parity_buf(b.lo, p)[(uint64_t)s.vid * cfg.pstride + at] = lo;
-      parity_buf(b.hi, p)[(uint64_t)s.vid * cfg.pstride + at] = hi;
+      slot_bounds(sj, b.plo[(uint64_t)sj.vid * cfg.e_max + k], b.phi[(uint64_t)sj.vid * cfg.e_max + k], part, lo, hi);
+      b.lo[(uint64_t)sj.vid * cfg.pstride + s] = lo;
+      b.hi[(uint64_t)sj.vid * cfg.pstride + s] = hi;
     }
+    b.depth[s] = b.pdepth[k] + 1;
+    const uint32_t p = d->parity;
     parity_buf(b.lb, p)[at] = b.clb[g];
-    parity_buf(b.depth, p)[at] = b.pdepth[k] + 1;
+    parity_buf(b.slot, p)[at] = (uint32_t)s;
     b.sel[at] = kSelAlive;
-  }
-};
-
-// move an alive entry of the current buffer to position `pos` of the other
-// buffer and return its lb key. Loads of a group of planes are issued
-// before its stores so that each thread keeps several reads in flight.
-struct CopyPool {
-  SolverCfg cfg;
-  SolverBufs b;
-  __device__ uint64_t operator()(uint64_t i, uint64_t pos) const
-  {
-    constexpr int kGroup = 4;
-    const uint32_t p = b.dev->parity, q = 1 - p;
-    const double* __restrict__ slo = parity_buf(b.lo, p);
-    const double* __restrict__ shi = parity_buf(b.hi, p);
-    double* __restrict__ dlo = parity_buf(b.lo, q);
-    double* __restrict__ dhi = parity_buf(b.hi, q);
-    const uint64_t ps = cfg.pstride;
-    const double lbv = parity_buf(b.lb, p)[i];
-    const uint32_t dep = parity_buf(b.depth, p)[i];
-    for (int v0 = 0; v0 < cfg.n_vars; v0 += kGroup) {
-      double l[kGroup], h[kGroup];
-#pragma unroll
-      for (int u = 0; u < kGroup; ++u)
-        if (v0 + u < cfg.n_vars) {
-          l[u] = slo[(uint64_t)(v0 + u) * ps + i];
-          h[u] = shi[(uint64_t)(v0 + u) * ps + i];
-        }
-#pragma unroll
-      for (int u = 0; u < kGroup; ++u)
-        if (v0 + u < cfg.n_vars) {
-          dlo[(uint64_t)(v0 + u) * ps + pos] = l[u];
-          dhi[(uint64_t)(v0 + u) * ps + pos] = h[u];
-        }
-    }
-    parity_buf(b.lb, q)[pos] = lbv;
-    parity_buf(b.depth, q)[pos] = dep;
-    return lb_key(lbv);
   }
 };
 
@@ -653,13 +633,14 @@ template <class P, class Op>
 __global__ void __launch_bounds__(kScanBlock) scatter_kernel(const P pred, const Op op,
                                                              const uint32_t* __restrict__ offsets)
 {
+  const uint64_t t0 = tile_first();
   if (pred.skip()) return;
   const uint64_t n = pred.size();
   if ((uint64_t)blockIdx.x * kScanTile >= n) return;
   bool f[kScanItems];
 #pragma unroll
   for (int j = 0; j < kScanItems; ++j) {
-    const uint64_t i = tile_item(j);
+    const uint64_t i = tile_item(t0, j);
     f[j] = i < n && pred(i);
   }
   int rank[kScanItems];
@@ -667,37 +648,115 @@ __global__ void __launch_bounds__(kScanBlock) scatter_kernel(const P pred, const
   const uint64_t base = offsets[blockIdx.x];
 #pragma unroll
   for (int j = 0; j < kScanItems; ++j)
-    if (f[j]) op(tile_item(j), base + (uint64_t)rank[j]);
+    if (f[j]) op(tile_item(t0, j), base + (uint64_t)rank[j]);
 }
 
-// Moves the alive entries of the current buffer, in order, to the other
-// buffer, and folds their lower bounds into the pool minimum.
-__global__ void __launch_bounds__(kScanBlock, 2) copy_pool_kernel(const SolverCfg cfg, const SolverBufs b,
-                                                               const uint32_t* __restrict__ offsets)
+// Stages this iteration's parents (kSelParent entries of the pool, in
+// position order) from the store into the parent planes.
+__global__ void __launch_bounds__(kScanBlock) gather_parents_kernel(const SolverCfg cfg, const SolverBufs b,
+                                                                    const uint32_t* __restrict__ offsets)
 {
-  SolverDev* d = b.dev;
-  if (d->done) return;
-  const uint64_t n = d->extent;
+  const uint64_t t0 = tile_first();
+  const SolverDev* d = b.dev;
+  const uint32_t done = d->done;
+  const uint64_t n = d->pool_size;
+  const uint64_t base = offsets[blockIdx.x];
+  uint8_t sv[kScanItems];
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    const uint64_t i = tile_item(t0, j);
+    sv[j] = i < cfg.pstride ? b.sel[i] : kSelAlive;
+  }
+  if (done) return;
   if ((uint64_t)blockIdx.x * kScanTile >= n) return;
   bool f[kScanItems];
 #pragma unroll
-  for (int j = 0; j < kScanItems; ++j) {
-    const uint64_t i = tile_item(j);
-    f[j] = i < n && b.sel[i] == kSelAlive;
-  }
+  for (int j = 0; j < kScanItems; ++j) f[j] = tile_item(t0, j) < n && sv[j] == kSelParent;
   int rank[kScanItems];
   tile_ranks(f, rank);
-  const uint64_t base = offsets[blockIdx.x];
-  const CopyPool op{cfg, b};
-  uint64_t mkey = ~0ULL;
+  const GatherParents op{cfg, b};
 #pragma unroll
   for (int j = 0; j < kScanItems; ++j)
+    if (f[j]) op(tile_item(t0, j), base + (uint64_t)rank[j]);
+}
+
+// Moves the alive entries of the current buffer, in order, to the other
+// buffer (lower bound and store slot), folds their lower bounds into the
+// pool minimum, and pushes the store slots of the others (this iteration's
+// parents and the evicted) onto the free stack in position order.
+__global__ void __launch_bounds__(kScanBlock, 2) copy_pool_kernel(const SolverCfg cfg, const SolverBufs b,
+                                                                  const uint32_t* __restrict__ offsets)
+{
+  const uint64_t t0 = tile_first();
+  SolverDev* d = b.dev;
+  // control words, the tile's entries and its offset are loaded together
+  const uint32_t done = d->done;
+  const uint64_t n = d->extent;
+  const uint64_t free_base = d->free_top;
+  const uint32_t p = d->parity, q = 1 - p;
+  const uint64_t* __restrict__ slb = reinterpret_cast<const uint64_t*>(parity_buf(b.lb, p));
+  const uint32_t* __restrict__ sslot = parity_buf(b.slot, p);
+  uint64_t* __restrict__ dlb = reinterpret_cast<uint64_t*>(parity_buf(b.lb, q));
+  uint32_t* __restrict__ dslot = parity_buf(b.slot, q);
+  const uint64_t base = offsets[blockIdx.x];
+  bool f[kScanItems], in[kScanItems];
+  uint64_t x[kScanItems];  // raw bits of the lower bounds
+  uint32_t sl[kScanItems];
+  uint8_t sv[kScanItems];
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    const uint64_t i = tile_item(t0, j);
+    const bool inb = i < cfg.pstride;
+    sv[j] = inb ? b.sel[i] : kSelParent;
+    x[j] = inb ? slb[i] : 0;
+    sl[j] = inb ? sslot[i] : 0u;
+  }
+  if (done) return;
+  if ((uint64_t)blockIdx.x * kScanTile >= n) return;
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    in[j] = tile_item(t0, j) < n;
+    f[j] = in[j] && sv[j] == kSelAlive;
+  }
+  int rank[kScanItems];  // alive entries before each item of the tile
+  tile_ranks(f, rank);
+  uint64_t mkey = ~0ULL;
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    if (!in[j]) continue;
+    const uint64_t i = tile_item(t0, j);
+    const uint64_t alive_before = base + (uint64_t)rank[j];
     if (f[j]) {
-      const uint64_t k = op(tile_item(j), base + (uint64_t)rank[j]);
+      dlb[alive_before] = x[j];
+      dslot[alive_before] = sl[j];
+      const uint64_t k = bits_key(x[j]);
       mkey = k < mkey ? k : mkey;
+    } else {
+      b.free_slots[free_base + (i - alive_before)] = sl[j];
     }
+  }
   mkey = block_min(mkey);
   if (threadIdx.x == 0 && mkey != ~0ULL) atomicMin((unsigned long long*)&d->pool_min_key, (unsigned long long)mkey);
+  (void)cfg;
+}
+
+// pool entries [start, start + count) in position order, unpacked from the
+// store
+__global__ void frontier_gather_kernel(const SolverCfg cfg, const SolverBufs b, uint64_t start, uint64_t count,
+                                       double* __restrict__ boxes, uint32_t* __restrict__ depths)
+{
+  const uint32_t p = b.dev->parity;
+  const uint32_t* slot = parity_buf(b.slot, p);
+  const int n = cfg.n_vars;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t s = slot[start + i];
+    if (boxes)
+      for (int v = 0; v < n; ++v) {
+        boxes[(i * n + v) * 2] = b.lo[(uint64_t)v * cfg.pstride + s];
+        boxes[(i * n + v) * 2 + 1] = b.hi[(uint64_t)v * cfg.pstride + s];
+      }
+    if (depths) depths[i] = b.depth[s];
+  }
 }
 
 // ---------------------------------------------------------------------
@@ -765,7 +824,7 @@ __global__ void prune_count_kernel(const SolverCfg cfg, const SolverBufs b)
     if (cfg.sample_all || s == kChildEligible) ++sampled;
     if (s == kChildDuplicate) ++dup;
     else if (s == kChildInfeasible) ++inf;
-    else if (s == kChildDominated || b.clb[g] > gub) ++dom;
+    else if (s == kChildDominated || bits_lt(dbits(gub), dbits(b.clb[g]))) ++dom;
     else ++kept;
   }
   unsigned long long c[5] = {dup, inf, dom, kept, sampled};
@@ -830,6 +889,7 @@ __global__ void size_kernel(const SolverCfg cfg, const SolverBufs b)
   d->remaining = d->pool_size - d->n_parents;
   d->new_size = d->remaining + d->kept;
   d->extent = d->pool_size + d->kept;
+  d->free_top -= d->kept;  // taken by the appended children
   d->evict = d->new_size > cfg.cap ? 1 : 0;
   d->pool_min_key = ~0ULL;  // refilled by the move to the other buffer
 }
@@ -842,6 +902,8 @@ __global__ void finish_kernel(const SolverCfg cfg, const SolverBufs b)
   // evicting, otherwise every alive entry
   const uint64_t expect = d->evict ? cfg.cap : d->new_size;
   if (d->survivors != expect) d->error = 1;
+  d->free_top += d->extent - d->survivors;  // the parents' and the evicted slots
+  if (d->free_top + d->survivors != cfg.pstride) d->error = 1;
   d->pool_size = d->survivors;
   d->parity = 1 - d->parity;
   if (d->dropped_min_key != ~0ULL) d->dropped_lb_min = key_to_lb(d->dropped_min_key);
@@ -937,7 +999,7 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
 
   // (1) select the E best parents and stage them
   radix_select(cfg, b, 0, cfg.cap, s);
-  scatter(SelParents{b}, GatherParents{cfg, b}, cfg.cap, s, b);
+  gather_parents_kernel<<<tiles(cfg.cap), kScanBlock, 0, s>>>(cfg, b, b.block_offsets);
 
   // (2) branch
   {
@@ -1055,6 +1117,8 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
   // the floor; then move every alive entry to the other buffer in order
   radix_select(cfg, b, 1, max_pool, s);
   copy_pool_kernel<<<tiles(max_pool), kScanBlock, 0, s>>>(cfg, b, b.block_offsets);
+  // every entry of the next pool starts alive
+  cudaMemsetAsync(b.sel, kSelAlive, cfg.pstride, s);
   finish_kernel<<<1, 1, 0, s>>>(cfg, b);
   mark(marks, 4, s);
   return cudaGetLastError();
@@ -1064,6 +1128,18 @@ cudaError_t solver_init(const SolverCfg& cfg, const SolverBufs& b, const double*
                         const double* root_ub_dev, double gub0, cudaStream_t s)
 {
   init_kernel<<<1, 256, 0, s>>>(cfg, b, root_lb_dev, root_ub_dev, gub0);
+  const int grid = (int)std::min<uint64_t>((cfg.pstride + 255) / 256, 4096);
+  free_init_kernel<<<grid, 256, 0, s>>>(cfg, b);
+  cudaMemsetAsync(b.sel, kSelAlive, cfg.pstride, s);
+  return cudaGetLastError();
+}
+
+cudaError_t solver_frontier_gather(const SolverCfg& cfg, const SolverBufs& b, uint64_t start, uint64_t count,
+                                   double* boxes, uint32_t* depths, cudaStream_t s)
+{
+  if (count == 0) return cudaSuccess;
+  const int grid = (int)std::min<uint64_t>((count + 255) / 256, 4096);
+  frontier_gather_kernel<<<grid, 256, 0, s>>>(cfg, b, start, count, boxes, depths);
   return cudaGetLastError();
 }
 

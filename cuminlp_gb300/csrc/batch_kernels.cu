@@ -452,7 +452,7 @@ __global__ void __launch_bounds__(kEvalThreads, 4) batch_eval_kernel(const Batch
     const SlotPlan* sp = b.slots + (slot * c.e_max + k) * c.max_slots;
     if (live && kMode == 2 && !st->use_screen) {
       bool dup = false;
-      for (uint32_t j = 0; j < pi.count; ++j) dup = dup || ((r / sp[j].prefix) % sp[j].width >= sp[j].dom);
+      for (uint32_t j = 0; j < pi.count; ++j) dup = dup || (slot_part(r, sp[j]) >= sp[j].dom);
       if (lane == 0) b.cstate[g] = dup ? kChildDuplicate : kChildScreened;
       live = false;
     }
@@ -471,7 +471,7 @@ __global__ void __launch_bounds__(kEvalThreads, 4) batch_eval_kernel(const Batch
       bool dup = false;
       for (uint32_t j = 0; j < pi.count; ++j) {
         const SlotPlan sj = sp[j];
-        const uint64_t part = (r / sj.prefix) % sj.width;
+        const uint64_t part = slot_part(r, sj);
         if (part >= sj.dom) dup = true;
         double lo, hi;
         slot_bounds(sj, b.plo[splane(c, slot, sj.vid) + k], b.phi[splane(c, slot, sj.vid) + k], part, lo, hi);
@@ -511,7 +511,7 @@ __device__ __forceinline__ double child_bound(const BatchCfg& c, const BatchBufs
   hi = b.phi[splane(c, slot, v) + k];
   for (uint32_t j = 0; j < count; ++j) {
     if (sp[j].vid == (uint32_t)v) {
-      const uint64_t part = (r / sp[j].prefix) % sp[j].width;
+      const uint64_t part = slot_part(r, sp[j]);
       slot_bounds(sp[j], lo, hi, part, lo, hi);
       break;
     }

@@ -926,8 +926,8 @@ extern "C" cmn_status cmn_solver_create(const cmn_problem* p, const cmn_solve_op
     A(&b.slots, cfg.e_max * (size_t)cfg.max_slots);
     unsigned char* es = nullptr;
     unsigned char* bs = nullptr;
-    A(&es, cfg.e_max * (size_t)n * 32);
-    A(&bs, cfg.e_max * (size_t)n * 40);
+    A(&es, cfg.e_max * (size_t)n * sizeof(EnumCand));
+    A(&bs, cfg.e_max * (size_t)n * sizeof(BisCand));
     b.enum_scratch = es;
     b.bis_scratch = bs;
     A(&b.heap_scratch, cfg.e_max * (size_t)n);

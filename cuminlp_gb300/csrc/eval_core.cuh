@@ -682,6 +682,16 @@ __device__ __forceinline__ PointVerdict group_point_verdict(PointVerdict v, int 
 
 // ---- region decode (region/decode.hpp:44-71), FMA form as compiled on
 // the device, and the sampler (graph/subregion_sampler.cuh:53-120) ----
+// The part of slot `s` that child `r` of a parent takes: (r / prefix) %
+// width. The branching policy's plans have power-of-two widths, which take
+// a shift and a mask instead of a 64-bit division.
+__device__ __forceinline__ uint64_t slot_part(uint64_t r, const SlotPlan& s)
+{
+  if (((s.prefix & (s.prefix - 1)) | (s.width & (s.width - 1))) == 0)
+    return (r >> (__ffsll((long long)s.prefix) - 1)) & (s.width - 1);
+  return (r / s.prefix) % s.width;
+}
+
 // bounds of part `part` of slot `s` over the parent's [plo, phi]
 __device__ __forceinline__ void slot_bounds(const SlotPlan& s, double plo, double phi, uint64_t part, double& lo,
                                             double& hi)

@@ -61,7 +61,7 @@ __device__ __forceinline__ ChildVars<T, S> child_vars(const EvalArgs& a, const S
     const SlotPlan* sp = a.slots + k * (uint64_t)a.max_slots;
     for (uint32_t j = 0; j < count; ++j) {
       const SlotPlan s = sp[j];
-      const uint64_t part = (r / s.prefix) % s.width;
+      const uint64_t part = slot_part(r, s);
       if (part >= s.dom) dup = true;
       double lo, hi;
       slot_bounds(s, a.plo[(uint64_t)s.vid * a.pstride + k], a.phi[(uint64_t)s.vid * a.pstride + k], part, lo, hi);
@@ -164,7 +164,7 @@ __device__ void eval_children_grouped(const EvalArgs& a, const S* plo, const S* 
       bool dup = false;
       const uint32_t count = a.pinfo[k].count;
       const SlotPlan* sp = a.slots + k * (uint64_t)a.max_slots;
-      for (uint32_t j = 0; j < count; ++j) dup = dup || ((r / sp[j].prefix) % sp[j].width >= sp[j].dom);
+      for (uint32_t j = 0; j < count; ++j) dup = dup || (slot_part(r, sp[j]) >= sp[j].dom);
       if (lane == 0) a.out_flag[g] = dup ? kChildDuplicate : kChildScreened;
       live = false;
     }
@@ -241,7 +241,7 @@ __device__ __forceinline__ void eval_children(const EvalArgs& a, const S* plo, c
       bool dup = false;
       const uint32_t count = a.pinfo[k].count;
       const SlotPlan* sp = a.slots + k * (uint64_t)a.max_slots;
-      for (uint32_t j = 0; j < count; ++j) dup = dup || ((r / sp[j].prefix) % sp[j].width >= sp[j].dom);
+      for (uint32_t j = 0; j < count; ++j) dup = dup || (slot_part(r, sp[j]) >= sp[j].dom);
       a.out_flag[g] = dup ? kChildDuplicate : kChildScreened;
       continue;
     }
@@ -335,7 +335,7 @@ __device__ __forceinline__ void stage_point(const SampleArgs& a, const Tile<doub
     double hi = a.phi[(uint64_t)v * a.pstride + k];
     for (uint32_t j = 0; j < count; ++j) {
       if (sp[j].vid == (uint32_t)v) {
-        const uint64_t part = (r / sp[j].prefix) % sp[j].width;
+        const uint64_t part = slot_part(r, sp[j]);
         slot_bounds(sp[j], lo, hi, part, lo, hi);
         break;
       }
@@ -457,7 +457,7 @@ __global__ void __launch_bounds__(kEvalThreads) sample_children_kernel(const Sam
         double hi = a.phi[(uint64_t)v * a.pstride + k];
         for (uint32_t j = 0; j < count; ++j) {
           if (sp[j].vid == (uint32_t)v) {
-            const uint64_t part = (r / sp[j].prefix) % sp[j].width;
+            const uint64_t part = slot_part(r, sp[j]);
             slot_bounds(sp[j], lo, hi, part, lo, hi);
             break;
           }
@@ -524,7 +524,7 @@ __global__ void witness_kernel(const Cand* __restrict__ cand, const double* __re
       const uint32_t count = pinfo[k].count;
       for (uint32_t j = 0; j < count; ++j) {
         if (sp[j].vid == (uint32_t)v) {
-          const uint64_t part = (r / sp[j].prefix) % sp[j].width;
+          const uint64_t part = slot_part(r, sp[j]);
           slot_bounds(sp[j], lo, hi, part, lo, hi);
           break;
         }

@@ -610,7 +610,7 @@ struct AppendChild {
     const SlotPlan* sp = b.slots + k * (uint64_t)cfg.max_slots;
     for (uint32_t j = 0; j < pi.count; ++j) {
       const SlotPlan sj = sp[j];
-      const uint64_t part = (r / sj.prefix) % sj.width;
+      const uint64_t part = slot_part(r, sj);
       double lo, hi;
       slot_bounds(sj, b.plo[(uint64_t)sj.vid * cfg.e_max + k], b.phi[(uint64_t)sj.vid * cfg.e_max + k], part, lo, hi);
       b.lo[(uint64_t)sj.vid * cfg.pstride + s] = lo;

@@ -26,15 +26,17 @@ constexpr uint8_t kSelEvicted = 2;
 // k-th smallest key search (radix select over lb keys). The threshold is
 // the bucket `prefix` under `mask` (the digits fixed so far); entries below
 // it are taken, and the first `k` entries inside it in position order.
+// The search starts below the leading bits that the smallest and largest
+// keys share, which every key of the set shares too.
 struct RadixState {
   uint64_t prefix;
   uint64_t mask;
-  uint64_t k;        // rank still to find inside the current prefix
-  uint64_t less;     // entries with key below the prefix bucket so far
-  uint32_t active;   // 0: take everything (k >= n)
-  uint32_t settled;  // 1: the bucket is taken whole; no further digits
-  uint32_t rank;     // 1: entries inside the bucket need position ranks
-  uint32_t pad;
+  uint64_t k;         // rank still to find inside the current prefix
+  uint64_t less;      // entries with key below the prefix bucket so far
+  uint32_t active;    // 0: take everything (k >= n)
+  uint32_t settled;   // 1: the bucket is taken whole; no further digits
+  uint32_t rank;      // 1: entries inside the bucket need position ranks
+  uint32_t bits_left; // key bits below the mask
   uint32_t hist[kRadixBins];
 };
 
@@ -44,6 +46,11 @@ struct SolverDev {
   double glb;
   double dropped_lb_min;
   uint64_t pool_min_key;   // min lb key of the current pool
+  uint64_t pool_max_key;   // max lb key of the current pool
+  uint64_t child_min_key;  // min / max lb key of this iteration's kept children
+  uint64_t child_max_key;
+  uint64_t evict_lo_key;   // key range of the rebuilt pool (before eviction)
+  uint64_t evict_hi_key;
   uint64_t pool_size;      // L
   uint64_t n_parents;      // E of this iteration
   uint64_t n_children;     // E << log2C

@@ -54,6 +54,7 @@ __global__ void init_kernel(const SolverCfg cfg, const SolverBufs b, const doubl
     d->free_top = cfg.pstride - 1;
     d->pool_size = 1;
     d->pool_min_key = lb_key(-DBL_MAX);
+    d->pool_max_key = lb_key(-DBL_MAX);
     d->parity = 0;
     d->use_screen = 1;
     d->counters.peak_frontier = 1;
@@ -105,6 +106,8 @@ __global__ void begin_kernel(const SolverCfg cfg, const SolverBufs b)
   d->remaining = 0;
   d->kept = 0;
   d->new_size = 0;
+  d->child_min_key = ~0ULL;
+  d->child_max_key = 0;
   d->extent = 0;
   d->survivors = 0;
   d->evict = 0;
@@ -145,13 +148,18 @@ __global__ void radix_init_kernel(const SolverCfg cfg, const SolverBufs b, int w
   else active = k < d->pool_size;
   for (int i = threadIdx.x; i < kRadixBins; i += blockDim.x) rs->hist[i] = 0;
   if (threadIdx.x == 0) {
-    rs->prefix = 0;
-    rs->mask = 0;
+    const uint64_t lo = which == 0 ? d->pool_min_key : d->evict_lo_key;
+    const uint64_t hi = which == 0 ? d->pool_max_key : d->evict_hi_key;
+    const int common = lo <= hi ? ((lo ^ hi) == 0 ? 64 : __clzll((long long)(lo ^ hi))) : 0;
+    const uint64_t top = common == 0 ? 0 : (~0ULL << (64 - common));
+    rs->prefix = lo & top;
+    rs->mask = top;
     rs->k = k;
     rs->less = 0;
     rs->active = active ? 1u : 0u;
     rs->settled = 0;
     rs->rank = active ? 1u : 0u;
+    rs->bits_left = (uint32_t)(64 - common);
   }
 }
 
@@ -160,11 +168,13 @@ __global__ void radix_init_kernel(const SolverCfg cfg, const SolverBufs b, int w
 // shared histogram only when the bin changes: converging lower bounds share
 // most leading digits, so a pass makes few shared-memory atomics instead of
 // one per entry on a single address.
-__global__ void radix_hist_kernel(const SolverCfg cfg, const SolverBufs b, int which, int shift, int bits)
+__global__ void radix_hist_kernel(const SolverCfg cfg, const SolverBufs b, int which)
 {
   __shared__ uint32_t h[kRadixBins];
   RadixState* rs = b.radix;
-  if (!rs->active || rs->settled) return;
+  if (!rs->active || rs->settled || rs->bits_left == 0) return;
+  const int bits = rs->bits_left < (uint32_t)kRadixBits ? (int)rs->bits_left : kRadixBits;
+  const int shift = (int)rs->bits_left - bits;
   const uint64_t n = rs_n(b.dev, which);
   if ((uint64_t)blockIdx.x * blockDim.x >= n) return;
   const int nb = 1 << bits;
@@ -213,13 +223,15 @@ __global__ void radix_hist_kernel(const SolverCfg cfg, const SolverBufs b, int w
 // Picks the digit whose bin holds the k-th entry: a block scan over the
 // bins (two per thread). When the entries up to and including that bin
 // are exactly k, the bin is taken whole and the search stops.
-__global__ void __launch_bounds__(kPickThreads) radix_pick_kernel(const SolverBufs b, int shift, int bits)
+__global__ void __launch_bounds__(kPickThreads) radix_pick_kernel(const SolverBufs b)
 {
   __shared__ uint64_t warp_sum[kPickThreads / 32];
   __shared__ int pick_d;
   __shared__ uint64_t pick_cum, pick_cnt;
   RadixState* rs = b.radix;
-  if (!rs->active || rs->settled) return;
+  if (!rs->active || rs->settled || rs->bits_left == 0) return;
+  const int bits = rs->bits_left < (uint32_t)kRadixBits ? (int)rs->bits_left : kRadixBits;
+  const int shift = (int)rs->bits_left - bits;
   const int nb = 1 << bits;
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
   const int b0 = 2 * t;
@@ -270,6 +282,7 @@ __global__ void __launch_bounds__(kPickThreads) radix_pick_kernel(const SolverBu
   rs->k = k - pick_cum;
   rs->prefix |= (uint64_t)pick_d << shift;
   rs->mask |= ((uint64_t)(nb - 1)) << shift;
+  rs->bits_left = (uint32_t)shift;
   if (pick_cum + pick_cnt == k) {
     rs->settled = 1;
     rs->rank = 0;
@@ -362,6 +375,21 @@ __device__ __forceinline__ void block_sum(unsigned long long (&v)[N])
   if (threadIdx.x == 0)
 #pragma unroll
     for (int k = 0; k < N; ++k) v[k] = acc[k];
+}
+
+// Block maximum of `m`, for thread 0. Every thread of the block calls it.
+__device__ __forceinline__ uint64_t block_max(uint64_t m)
+{
+  __shared__ unsigned long long acc;
+  if (threadIdx.x == 0) acc = 0;
+  __syncthreads();
+  for (int off = 16; off > 0; off >>= 1) {
+    const uint64_t o = __shfl_down_sync(0xffffffffu, m, off);
+    m = o > m ? o : m;
+  }
+  if ((threadIdx.x & 31) == 0 && m != 0) atomicMax(&acc, (unsigned long long)m);
+  __syncthreads();
+  return acc;
 }
 
 // Block minimum of `m`, for thread 0. Every thread of the block calls it.
@@ -720,7 +748,7 @@ __global__ void __launch_bounds__(kScanBlock, 2) copy_pool_kernel(const SolverCf
   }
   int rank[kScanItems];  // alive entries before each item of the tile
   tile_ranks(f, rank);
-  uint64_t mkey = ~0ULL;
+  uint64_t mkey = ~0ULL, xkey = 0;
 #pragma unroll
   for (int j = 0; j < kScanItems; ++j) {
     if (!in[j]) continue;
@@ -731,12 +759,17 @@ __global__ void __launch_bounds__(kScanBlock, 2) copy_pool_kernel(const SolverCf
       dslot[alive_before] = sl[j];
       const uint64_t k = bits_key(x[j]);
       mkey = k < mkey ? k : mkey;
+      xkey = k > xkey ? k : xkey;
     } else {
       b.free_slots[free_base + (i - alive_before)] = sl[j];
     }
   }
   mkey = block_min(mkey);
-  if (threadIdx.x == 0 && mkey != ~0ULL) atomicMin((unsigned long long*)&d->pool_min_key, (unsigned long long)mkey);
+  xkey = block_max(xkey);
+  if (threadIdx.x == 0) {
+    if (mkey != ~0ULL) atomicMin((unsigned long long*)&d->pool_min_key, (unsigned long long)mkey);
+    if (xkey != 0) atomicMax((unsigned long long*)&d->pool_max_key, (unsigned long long)xkey);
+  }
   (void)cfg;
 }
 
@@ -818,6 +851,7 @@ __global__ void prune_count_kernel(const SolverCfg cfg, const SolverBufs b)
   const uint64_t n = d->n_children;
   const double gub = d->gub;
   unsigned long long dup = 0, inf = 0, dom = 0, kept = 0, sampled = 0;
+  uint64_t mkey = ~0ULL, xkey = 0;  // key range of the children the pool takes
   for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n; g += (uint64_t)gridDim.x * blockDim.x) {
     const uint8_t s = b.cstate[g];
     if (s == kChildNone) continue;
@@ -826,10 +860,19 @@ __global__ void prune_count_kernel(const SolverCfg cfg, const SolverBufs b)
     else if (s == kChildInfeasible) ++inf;
     else if (s == kChildDominated || bits_lt(dbits(gub), dbits(b.clb[g]))) ++dom;
     else ++kept;
+    if (s == kChildEligible) {  // a superset of the kept children
+      const uint64_t k = lb_key(b.clb[g]);
+      mkey = k < mkey ? k : mkey;
+      xkey = k > xkey ? k : xkey;
+    }
   }
   unsigned long long c[5] = {dup, inf, dom, kept, sampled};
   block_sum(c);
+  mkey = block_min(mkey);
+  xkey = block_max(xkey);
   if (threadIdx.x == 0) {
+    if (mkey != ~0ULL) atomicMin((unsigned long long*)&d->child_min_key, (unsigned long long)mkey);
+    if (xkey != 0) atomicMax((unsigned long long*)&d->child_max_key, (unsigned long long)xkey);
     if (c[0]) atomicAdd((unsigned long long*)&d->counters.pruned_duplicate, c[0]);
     if (c[1]) atomicAdd((unsigned long long*)&d->counters.pruned_infeasible, c[1]);
     if (c[2]) atomicAdd((unsigned long long*)&d->counters.pruned_dominated, c[2]);
@@ -891,7 +934,10 @@ __global__ void size_kernel(const SolverCfg cfg, const SolverBufs b)
   d->extent = d->pool_size + d->kept;
   d->free_top -= d->kept;  // taken by the appended children
   d->evict = d->new_size > cfg.cap ? 1 : 0;
+  d->evict_lo_key = d->pool_min_key < d->child_min_key ? d->pool_min_key : d->child_min_key;
+  d->evict_hi_key = d->pool_max_key > d->child_max_key ? d->pool_max_key : d->child_max_key;
   d->pool_min_key = ~0ULL;  // refilled by the move to the other buffer
+  d->pool_max_key = 0;
 }
 
 __global__ void finish_kernel(const SolverCfg cfg, const SolverBufs b)
@@ -967,13 +1013,11 @@ static void radix_select(const SolverCfg& cfg, const SolverBufs& b, int which, u
 {
   radix_init_kernel<<<1, 256, 0, s>>>(cfg, b, which);
   const int grid = (int)std::min<uint64_t>((max_items + 255) / 256, 4096);
-  // digits from the most significant: 6 x 11 bits minus the 2 top bits;
-  // the passes after the bucket settles return at once
-  const int shifts[6] = {53, 42, 31, 20, 9, 0};
-  const int bits[6] = {11, 11, 11, 11, 11, 9};
-  for (int p = 0; p < 6; ++p) {
-    radix_hist_kernel<<<grid, 256, 0, s>>>(cfg, b, which, shifts[p], bits[p]);
-    radix_pick_kernel<<<1, kPickThreads, 0, s>>>(b, shifts[p], bits[p]);
+  // digits of up to 11 bits from below the keys' common leading bits;
+  // the passes after the bucket settles or the bits run out return at once
+  for (int p = 0; p < (64 + kRadixBits - 1) / kRadixBits; ++p) {
+    radix_hist_kernel<<<grid, 256, 0, s>>>(cfg, b, which);
+    radix_pick_kernel<<<1, kPickThreads, 0, s>>>(b);
   }
   // ranks among entries inside the threshold bucket, then the marks with
   // the tile counts of the entries the next compaction moves

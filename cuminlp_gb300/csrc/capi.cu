@@ -905,7 +905,7 @@ extern "C" cmn_status cmn_solver_create(const cmn_problem* p, const cmn_solve_op
       if (e == cudaSuccess) e = s->alloc(ptr, count);
     };
     A(&b.dev, 1);
-    A(&b.radix, 1);
+    A(&b.radix, 2);
     for (int q = 0; q < 2; ++q) {
       A(&b.lb[q], cfg.pstride);
       A(&b.slot[q], cfg.pstride);
@@ -914,7 +914,8 @@ extern "C" cmn_status cmn_solver_create(const cmn_problem* p, const cmn_solve_op
     A(&b.hi, (size_t)n * cfg.pstride);
     A(&b.depth, cfg.pstride);
     A(&b.free_slots, cfg.pstride);
-    A(&b.sel, cfg.pstride);
+    A(&b.sel[0], cfg.pstride);
+    A(&b.sel[1], cfg.pstride);
     A(&b.plo, (size_t)n * cfg.e_max);
     A(&b.phi, (size_t)n * cfg.e_max);
     if (fp32) {
@@ -922,6 +923,7 @@ extern "C" cmn_status cmn_solver_create(const cmn_problem* p, const cmn_solve_op
       A(&b.phi32, (size_t)n * cfg.e_max);
     }
     A(&b.pdepth, cfg.e_max);
+    A(&b.pslot, cfg.e_max);
     A(&b.pinfo, cfg.e_max);
     A(&b.slots, cfg.e_max * (size_t)cfg.max_slots);
     unsigned char* es = nullptr;
@@ -937,6 +939,8 @@ extern "C" cmn_status cmn_solver_create(const cmn_problem* p, const cmn_solve_op
     const size_t nblk = (std::max<uint64_t>(cfg.pstride, maxc) + kScanTile - 1) / kScanTile + 1;
     A(&b.block_counts, nblk);
     A(&b.block_offsets, nblk);
+    A(&b.block_counts2, nblk);
+    A(&b.block_offsets2, nblk);
     b.n_block_best = s->sample_grid + 1;
     A(&b.block_best, (size_t)b.n_block_best);
     A(&b.best_point, (size_t)n);

@@ -22,6 +22,7 @@ constexpr int kPickThreads = kRadixBins / 2;  // two bins per thread
 constexpr uint8_t kSelAlive = 0;
 constexpr uint8_t kSelParent = 1;
 constexpr uint8_t kSelEvicted = 2;
+constexpr uint8_t kSelNextParent = 3;
 
 // k-th smallest key search (radix select over lb keys). The threshold is
 // the bucket `prefix` under `mask` (the digits fixed so far); entries below
@@ -63,6 +64,12 @@ struct SolverDev {
   uint64_t extent;         // pool_size + kept: entries of the current buffer
   uint64_t survivors;      // entries moved to the other buffer
   uint64_t free_top;       // free box-store slots (height of the free stack)
+  // the next iteration's parents, selected while this iteration rebuilds the
+  // pool: how many were asked for and how many were marked and staged
+  uint64_t pre_k;
+  uint64_t pre_count;
+  uint32_t pre_valid;      // the staged parents are the next iteration's
+  uint32_t skip_select;    // this iteration's parents were staged already
   uint64_t certify_count;
   uint64_t evict;          // 1 when the rebuilt pool exceeds the cap
   uint64_t dropped_min_key;
@@ -106,7 +113,7 @@ struct SolverCfg {
 
 struct SolverBufs {
   SolverDev* dev;
-  RadixState* radix;
+  RadixState* radix;  // two select targets
   // the pool in position order (two parities): lower bound and box slot
   double* lb[2];
   uint32_t* slot[2];
@@ -117,15 +124,17 @@ struct SolverBufs {
   double* hi;
   uint32_t* depth;
   uint32_t* free_slots;  // stack of free store slots (free_top entries)
-  // marks over the current buffer: kSelAlive, kSelParent (expanded this
-  // iteration: a hole), kSelEvicted (dropped by the cap)
-  uint8_t* sel;
+  // marks over the pool buffers (two parities): kSelAlive, kSelParent
+  // (expanded this iteration: a hole), kSelEvicted (dropped by the cap),
+  // kSelNextParent (stays, and is expanded next iteration)
+  uint8_t* sel[2];
   // staging of this iteration's parents: planes [v * e_max + k]
   double* plo;
   double* phi;
   float* plo32;  // FP32 screen only: the same planes rounded outward
   float* phi32;
   uint32_t* pdepth;
+  uint32_t* pslot;       // store slots of the next iteration's parents, in order
   ParentInfo* pinfo;
   SlotPlan* slots;
   // policy scratch [k * n_vars + i]
@@ -139,6 +148,8 @@ struct SolverBufs {
   // compaction scratch
   uint32_t* block_counts;
   uint32_t* block_offsets;
+  uint32_t* block_counts2;   // the second select target's
+  uint32_t* block_offsets2;
   Cand* block_best;
   int n_block_best;
   // problem

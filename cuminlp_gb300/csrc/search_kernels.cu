@@ -95,6 +95,11 @@ __global__ void begin_kernel(const SolverCfg cfg, const SolverBufs b)
   uint64_t E = L < cfg.e_max ? L : cfg.e_max;
   const uint64_t left = cfg.iter_limit - d->expansions;
   if (E > left) E = left;
+  // the previous iteration staged the E best entries of this pool already
+  d->skip_select = (d->pre_valid && d->pre_k == E) ? 1u : 0u;
+  d->pre_valid = 0;
+  d->pre_k = 0;
+  d->pre_count = 0;
   d->iterations += 1;
   d->n_parents = E;
   d->n_children = E << cfg.log2C;
@@ -131,65 +136,94 @@ __device__ __forceinline__ T* parity_buf(T* const (&a)[2], uint32_t p)
 }
 
 __device__ __forceinline__ const double* pool_lb(const SolverBufs& b) { return parity_buf(b.lb, b.dev->parity); }
+__device__ __forceinline__ uint8_t* pool_sel(const SolverBufs& b) { return parity_buf(b.sel, b.dev->parity); }
 
 __device__ __forceinline__ uint64_t rs_n(const SolverDev* d, int which)
 {
   return which == 0 ? d->pool_size : d->extent;
 }
 
+// Number of select targets of a pass: which = 0 selects this iteration's
+// parents; which = 1 selects the entries that stay under the cap (target 0)
+// and, among them, the next iteration's parents (target 1).
+__device__ __forceinline__ int n_targets(int which) { return which == 0 ? 1 : 2; }
+
+__device__ __forceinline__ bool target_live(const RadixState& r)
+{
+  return r.active && !r.settled && r.bits_left != 0;
+}
+
 __global__ void radix_init_kernel(const SolverCfg cfg, const SolverBufs b, int which)
 {
   SolverDev* d = b.dev;
-  RadixState* rs = b.radix;
-  const uint64_t k = which == 0 ? d->n_parents : cfg.cap;
-  bool active;
-  if (d->done) active = false;
-  else if (which == 1) active = d->evict && k < d->new_size;
-  else active = k < d->pool_size;
-  for (int i = threadIdx.x; i < kRadixBins; i += blockDim.x) rs->hist[i] = 0;
-  if (threadIdx.x == 0) {
-    const uint64_t lo = which == 0 ? d->pool_min_key : d->evict_lo_key;
-    const uint64_t hi = which == 0 ? d->pool_max_key : d->evict_hi_key;
-    const int common = lo <= hi ? ((lo ^ hi) == 0 ? 64 : __clzll((long long)(lo ^ hi))) : 0;
-    const uint64_t top = common == 0 ? 0 : (~0ULL << (64 - common));
-    rs->prefix = lo & top;
-    rs->mask = top;
-    rs->k = k;
-    rs->less = 0;
-    rs->active = active ? 1u : 0u;
-    rs->settled = 0;
-    rs->rank = active ? 1u : 0u;
-    rs->bits_left = (uint32_t)(64 - common);
+  for (int t = 0; t < n_targets(which); ++t) {
+    RadixState* rs = b.radix + t;
+    uint64_t k;
+    bool active;
+    if (which == 0) {
+      k = d->n_parents;
+      active = !d->done && !d->skip_select && k < d->pool_size;
+    } else if (t == 0) {
+      k = cfg.cap;
+      active = !d->done && d->evict && k < d->new_size;
+    } else {
+      k = d->pre_k;
+      active = !d->done && k > 0 && k < d->new_size;
+    }
+    for (int i = threadIdx.x; i < kRadixBins; i += blockDim.x) rs->hist[i] = 0;
+    if (threadIdx.x == 0) {
+      const uint64_t lo = which == 0 ? d->pool_min_key : d->evict_lo_key;
+      const uint64_t hi = which == 0 ? d->pool_max_key : d->evict_hi_key;
+      const int common = lo <= hi ? ((lo ^ hi) == 0 ? 64 : __clzll((long long)(lo ^ hi))) : 0;
+      const uint64_t top = common == 0 ? 0 : (~0ULL << (64 - common));
+      rs->prefix = lo & top;
+      rs->mask = top;
+      rs->k = k;
+      rs->less = 0;
+      rs->active = active ? 1u : 0u;
+      rs->settled = 0;
+      rs->rank = active ? 1u : 0u;
+      rs->bits_left = (uint32_t)(64 - common);
+    }
   }
 }
 
-// One digit's histogram over the entries inside the current bucket. Each
-// thread counts a run of equal bins in registers and adds it to the block's
-// shared histogram only when the bin changes: converging lower bounds share
-// most leading digits, so a pass makes few shared-memory atomics instead of
-// one per entry on a single address.
+// One digit's histogram per live target over the entries inside its
+// bucket, in one read of the keys. Each thread counts a run of equal bins
+// in registers and adds it to the block's shared histogram only when the
+// bin changes: converging lower bounds share most leading digits, so a pass
+// makes few shared-memory atomics instead of one per entry on one address.
 __global__ void radix_hist_kernel(const SolverCfg cfg, const SolverBufs b, int which)
 {
-  __shared__ uint32_t h[kRadixBins];
-  RadixState* rs = b.radix;
-  if (!rs->active || rs->settled || rs->bits_left == 0) return;
-  const int bits = rs->bits_left < (uint32_t)kRadixBits ? (int)rs->bits_left : kRadixBits;
-  const int shift = (int)rs->bits_left - bits;
+  __shared__ uint32_t h[2][kRadixBins];
+  const int T = n_targets(which);
+  bool go[2] = {false, false};
+  int shift[2] = {0, 0}, nb[2] = {1, 1};
+  uint64_t prefix[2] = {0, 0}, mask[2] = {0, 0};
+  for (int t = 0; t < T; ++t) {
+    const RadixState& r = b.radix[t];
+    go[t] = target_live(r);
+    if (!go[t]) continue;
+    const int bits = r.bits_left < (uint32_t)kRadixBits ? (int)r.bits_left : kRadixBits;
+    shift[t] = (int)r.bits_left - bits;
+    nb[t] = 1 << bits;
+    prefix[t] = r.prefix;
+    mask[t] = r.mask;
+  }
+  if (!go[0] && !go[1]) return;
   const uint64_t n = rs_n(b.dev, which);
   if ((uint64_t)blockIdx.x * blockDim.x >= n) return;
-  const int nb = 1 << bits;
-  for (int i = threadIdx.x; i < nb; i += blockDim.x) h[i] = 0;
+  for (int t = 0; t < 2; ++t)
+    for (int i = threadIdx.x; i < kRadixBins; i += blockDim.x) h[t][i] = 0;
   __syncthreads();
   const uint64_t* __restrict__ lb = reinterpret_cast<const uint64_t*>(pool_lb(b));
-  const uint8_t* __restrict__ sel = which == 1 ? b.sel : nullptr;
-  const uint64_t prefix = rs->prefix, mask = rs->mask;
-  const uint32_t dmask = (uint32_t)(nb - 1);
+  const uint8_t* __restrict__ sel = which == 1 ? pool_sel(b) : nullptr;
   const int lane = threadIdx.x & 31;
   // each warp takes chunks of 32 x kHistUnroll consecutive entries and
   // issues all their loads before it bins them
   constexpr int kChunk = 32 * kHistUnroll;
   const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x / 32);
-  uint32_t run_bin = 0, run = 0;
+  uint32_t run_bin[2] = {0, 0}, run[2] = {0, 0};
   for (uint64_t c = (uint64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); c * kChunk < n; c += warps) {
     uint64_t x[kHistUnroll];
     bool in[kHistUnroll];
@@ -202,34 +236,43 @@ __global__ void radix_hist_kernel(const SolverCfg cfg, const SolverBufs b, int w
     }
 #pragma unroll
     for (int u = 0; u < kHistUnroll; ++u) {
+      if (!in[u]) continue;
       const uint64_t key = bits_key(x[u]);
-      if (!in[u] || (key & mask) != prefix) continue;
-      const uint32_t bin = (uint32_t)(key >> shift) & dmask;
-      if (bin != run_bin) {
-        if (run) atomicAdd(&h[run_bin], run);
-        run_bin = bin;
-        run = 0;
+#pragma unroll
+      for (int t = 0; t < 2; ++t) {
+        if (!go[t] || (key & mask[t]) != prefix[t]) continue;
+        const uint32_t bin = (uint32_t)(key >> shift[t]) & (uint32_t)(nb[t] - 1);
+        if (bin != run_bin[t]) {
+          if (run[t]) atomicAdd(&h[t][run_bin[t]], run[t]);
+          run_bin[t] = bin;
+          run[t] = 0;
+        }
+        ++run[t];
       }
-      ++run;
     }
   }
-  if (run) atomicAdd(&h[run_bin], run);
+  for (int t = 0; t < 2; ++t)
+    if (run[t]) atomicAdd(&h[t][run_bin[t]], run[t]);
   __syncthreads();
-  for (int i = threadIdx.x; i < nb; i += blockDim.x)
-    if (h[i]) atomicAdd(&rs->hist[i], h[i]);
+  for (int t = 0; t < T; ++t) {
+    if (!go[t]) continue;
+    for (int i = threadIdx.x; i < nb[t]; i += blockDim.x)
+      if (h[t][i]) atomicAdd(&b.radix[t].hist[i], h[t][i]);
+  }
   (void)cfg;
 }
 
 // Picks the digit whose bin holds the k-th entry: a block scan over the
-// bins (two per thread). When the entries up to and including that bin
-// are exactly k, the bin is taken whole and the search stops.
+// bins (two per thread); block t serves target t. When the entries up to
+// and including that bin are exactly k, the bin is taken whole and the
+// search stops.
 __global__ void __launch_bounds__(kPickThreads) radix_pick_kernel(const SolverBufs b)
 {
   __shared__ uint64_t warp_sum[kPickThreads / 32];
   __shared__ int pick_d;
   __shared__ uint64_t pick_cum, pick_cnt;
-  RadixState* rs = b.radix;
-  if (!rs->active || rs->settled || rs->bits_left == 0) return;
+  RadixState* rs = b.radix + blockIdx.x;
+  if (!target_live(*rs)) return;
   const int bits = rs->bits_left < (uint32_t)kRadixBits ? (int)rs->bits_left : kRadixBits;
   const int shift = (int)rs->bits_left - bits;
   const int nb = 1 << bits;
@@ -301,8 +344,10 @@ __device__ __forceinline__ uint64_t tile_first() { return (uint64_t)blockIdx.x *
 
 __device__ __forceinline__ uint64_t tile_item(uint64_t t0, int j) { return t0 + (uint64_t)j * kScanBlock; }
 
-// Ranks of the flagged items of this block's tile in item order; returns
-// the tile's flagged count. One call per kernel.
+// Ranks of the flagged items of this block's tile in item order (for every
+// item: the flagged items before it); returns the tile's flagged count. One
+// call per kernel and table slot `S`.
+template <int S = 0>
 __device__ __forceinline__ int tile_ranks(const bool (&f)[kScanItems], int (&rank)[kScanItems])
 {
   constexpr int kWarps = kScanBlock / 32;
@@ -344,7 +389,8 @@ __device__ __forceinline__ int tile_ranks(const bool (&f)[kScanItems], int (&ran
   return tile_total;
 }
 
-// Sum of `c` over the block.
+// Sum of `c` over the block (one call per kernel and slot `S`).
+template <int S = 0>
 __device__ __forceinline__ int tile_count(int c)
 {
   __shared__ int tot;
@@ -411,11 +457,12 @@ __device__ __forceinline__ uint64_t block_min(uint64_t m)
 // writes the total to *total_out (plus `total_bias`).
 __global__ void scan_kernel(const uint32_t* __restrict__ counts, uint32_t* __restrict__ offsets,
                             const uint64_t* __restrict__ n_items, uint64_t* __restrict__ total_out,
-                            const uint32_t* __restrict__ active, const uint32_t* __restrict__ done)
+                            const uint32_t* __restrict__ active, const uint32_t* __restrict__ skip,
+                            const uint32_t* __restrict__ done)
 {
   __shared__ uint32_t warp_sum[32];
   __shared__ uint64_t carry_s;
-  if (*done) return;
+  if (*done || (skip && *skip)) return;
   if (active && !*active) {
     if (threadIdx.x == 0 && total_out) *total_out = 0;
     return;
@@ -472,18 +519,6 @@ struct ScreenedChild {
   __device__ bool skip() const { return b.dev->done != 0; }
 };
 
-struct EqKey {  // alive entries inside the radix threshold bucket
-  SolverBufs b;
-  int which;
-  __device__ uint64_t size() const { return rs_n(b.dev, which); }
-  __device__ bool operator()(uint64_t i) const
-  {
-    if (which == 1 && b.sel[i] != kSelAlive) return false;
-    return (lb_key(pool_lb(b)[i]) & b.radix->mask) == b.radix->prefix;
-  }
-  __device__ bool skip() const { return b.dev->done != 0 || !b.radix->rank; }
-};
-
 template <class P>
 __global__ void __launch_bounds__(kScanBlock) count_kernel(const P pred, uint32_t* __restrict__ counts)
 {
@@ -504,26 +539,75 @@ __global__ void __launch_bounds__(kScanBlock) count_kernel(const P pred, uint32_
   if (threadIdx.x == 0) counts[blockIdx.x] = (uint32_t)c;
 }
 
-// Marks the k smallest (key, position) entries: all keys below the
-// threshold bucket, and the first `k` entries inside it in position order
-// (all of them once the bucket is settled).
-//   which = 0: marks the parents kSelParent (every entry of the pool is
-//              kSelAlive before) and writes the tile counts of the parents;
+// Tile counts of the alive entries inside each ranked target's threshold
+// bucket (target 0 into block_counts, target 1 into block_counts2).
+__global__ void __launch_bounds__(kScanBlock) eq_count_kernel(const SolverCfg cfg, const SolverBufs b, int which)
+{
+  const uint64_t t0 = tile_first();
+  const SolverDev* d = b.dev;
+  const RadixState* rs = b.radix;
+  const bool r0 = rs[0].rank != 0, r1 = which == 1 && rs[1].rank != 0;
+  if (d->done || (!r0 && !r1)) return;
+  const uint64_t n = rs_n(d, which);
+  if ((uint64_t)blockIdx.x * kScanTile >= n) return;
+  const uint64_t* __restrict__ lb = reinterpret_cast<const uint64_t*>(pool_lb(b));
+  const uint8_t* __restrict__ sel = pool_sel(b);
+  int c0 = 0, c1 = 0;
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    const uint64_t i = tile_item(t0, j);
+    if (i >= n || (which == 1 && sel[i] != kSelAlive)) continue;
+    const uint64_t key = bits_key(lb[i]);
+    c0 += (r0 && (key & rs[0].mask) == rs[0].prefix) ? 1 : 0;
+    c1 += (r1 && (key & rs[1].mask) == rs[1].prefix) ? 1 : 0;
+  }
+  c0 = tile_count<0>(c0);
+  c1 = tile_count<1>(c1);
+  if (threadIdx.x == 0) {
+    if (r0) b.block_counts[blockIdx.x] = (uint32_t)c0;
+    if (r1) b.block_counts2[blockIdx.x] = (uint32_t)c1;
+  }
+  (void)cfg;
+}
+
+// The select decision of one target for one entry (`key` already masked).
+struct TargetView {
+  bool active, settled, ranked;
+  uint64_t prefix, mask, k;
+  __device__ explicit TargetView(const RadixState& r)
+      : active(r.active != 0), settled(r.settled != 0), ranked(r.rank != 0), prefix(r.prefix), mask(r.mask), k(r.k)
+  {
+  }
+  __device__ bool take(uint64_t key, bool eq, uint64_t eq_rank) const
+  {
+    if (!active) return true;
+    if (eq) return settled || eq_rank < k;
+    return (key & mask) < prefix;
+  }
+};
+
+// Marks the k smallest (key, position) entries of each target: all keys
+// below the threshold bucket, and the first `k` entries inside it in
+// position order (all of them once the bucket is settled).
+//   which = 0: marks this iteration's parents kSelParent and the others
+//              kSelAlive, and writes the tile counts of the parents;
 //   which = 1: marks alive entries outside the cap kSelEvicted (leaving the
-//              parents' holes as they are), folds them into the dropped
-//              floor (search/budget.hpp:190-209) and writes the tile counts
-//              of the entries that stay.
-__global__ void __launch_bounds__(kScanBlock, 2) mark_kernel(const SolverCfg cfg, const SolverBufs b, int which,
-                                                          const uint32_t* __restrict__ eq_offsets,
-                                                          uint32_t* __restrict__ out_counts)
+//              parents' holes as they are) and folds them into the dropped
+//              floor (search/budget.hpp:190-209); marks the next iteration's
+//              parents among those that stay kSelNextParent; writes the tile
+//              counts of the entries that stay and of the next parents.
+__global__ void __launch_bounds__(kScanBlock, 2) mark_kernel(const SolverCfg cfg, const SolverBufs b, int which)
 {
   const uint64_t t0 = tile_first();
   SolverDev* d = b.dev;
+  if (which == 0 && d->skip_select) return;
   // the control words and the tile's entries are loaded together: a tile is
   // short, so a chain of dependent loads would set its duration
-  const uint32_t done = d->done;
+  const uint32_t done = d->done, skip = d->skip_select;
   const uint64_t n = rs_n(d, which);
+  const uint64_t pre_k = d->pre_k;
   const uint64_t* __restrict__ lb = reinterpret_cast<const uint64_t*>(pool_lb(b));
+  uint8_t* __restrict__ sel = pool_sel(b);
   uint64_t x[kScanItems];  // raw bits of the lower bounds
   uint8_t sv[kScanItems];
 #pragma unroll
@@ -531,53 +615,65 @@ __global__ void __launch_bounds__(kScanBlock, 2) mark_kernel(const SolverCfg cfg
     const uint64_t i = tile_item(t0, j);
     const bool inb = i < cfg.pstride;
     x[j] = inb ? lb[i] : 0;
-    sv[j] = (which == 1 && inb) ? b.sel[i] : kSelAlive;
+    sv[j] = (which == 1 && inb) ? sel[i] : kSelAlive;
   }
-  if (done) return;
+  if (done || (which == 0 && skip)) return;
   if ((uint64_t)blockIdx.x * kScanTile >= n) return;
-  const RadixState* rs = b.radix;
-  const bool active = rs->active != 0, settled = rs->settled != 0, ranked = rs->rank != 0;
-  const uint64_t prefix = rs->prefix, mask = rs->mask, kth = rs->k;
-  const uint64_t gub = (uint64_t)__double_as_longlong(d->gub);
-  bool alive[kScanItems], eq[kScanItems];
+  const TargetView A(b.radix[0]);
+  const bool pre = which == 1 && pre_k > 0;
+  const TargetView B(b.radix[which == 1 ? 1 : 0]);
+  const uint64_t gub = dbits(d->gub);
+  bool alive[kScanItems], eqA[kScanItems], eqB[kScanItems];
 #pragma unroll
-  for (int j = 0; j < kScanItems; ++j) alive[j] = tile_item(t0, j) < n && sv[j] == kSelAlive;
-#pragma unroll
-  for (int j = 0; j < kScanItems; ++j) eq[j] = active && alive[j] && (bits_key(x[j]) & mask) == prefix;
-  int rank[kScanItems] = {};
-  uint64_t eq_base = 0;
-  if (ranked) {  // the same for the whole grid
-    tile_ranks(eq, rank);
-    eq_base = eq_offsets[blockIdx.x];
+  for (int j = 0; j < kScanItems; ++j) {
+    alive[j] = tile_item(t0, j) < n && sv[j] == kSelAlive;
+    const uint64_t key = bits_key(x[j]);
+    eqA[j] = A.active && alive[j] && (key & A.mask) == A.prefix;
+    eqB[j] = pre && B.active && alive[j] && (key & B.mask) == B.prefix;
   }
-  int out = 0;
+  int rankA[kScanItems] = {}, rankB[kScanItems] = {};
+  uint64_t baseA = 0, baseB = 0;
+  if (A.ranked) {  // the same for the whole grid
+    tile_ranks<0>(eqA, rankA);
+    baseA = b.block_offsets[blockIdx.x];
+  }
+  if (pre && B.ranked) {
+    tile_ranks<1>(eqB, rankB);
+    baseB = b.block_offsets2[blockIdx.x];
+  }
+  int outA = 0, outB = 0;
   uint32_t viable = 0, dominated = 0;
   uint64_t mkey = ~0ULL;
 #pragma unroll
   for (int j = 0; j < kScanItems; ++j) {
     if (!alive[j]) continue;
     const uint64_t key = bits_key(x[j]);
-    bool mark;
-    if (!active) mark = true;
-    else if (eq[j]) mark = settled || eq_base + (uint64_t)rank[j] < kth;
-    else mark = (key & mask) < prefix;
+    const bool ta = A.take(key, eqA[j], baseA + (uint64_t)rankA[j]);
+    const bool tb = pre && ta && B.take(key, eqB[j], baseB + (uint64_t)rankB[j]);
     const uint64_t i = tile_item(t0, j);
     if (which == 0) {
-      if (mark) b.sel[i] = kSelParent;  // the others are kSelAlive already
-    } else if (!mark) {
-      b.sel[i] = kSelEvicted;
+      sel[i] = ta ? kSelParent : kSelAlive;
+    } else if (!ta) {
+      sel[i] = kSelEvicted;
       if (bits_le(x[j], gub)) {
         ++viable;
         mkey = key < mkey ? key : mkey;
       } else {
         ++dominated;
       }
+    } else if (tb) {
+      sel[i] = kSelNextParent;
     }
-    out += mark ? 1 : 0;
+    outA += ta ? 1 : 0;
+    outB += tb ? 1 : 0;
   }
-  out = tile_count(out);
-  if (threadIdx.x == 0) out_counts[blockIdx.x] = (uint32_t)out;
-  if (which == 1 && active) {
+  outA = tile_count<0>(outA);
+  if (threadIdx.x == 0) b.block_counts[blockIdx.x] = (uint32_t)outA;
+  if (which == 1) {
+    outB = tile_count<1>(outB);
+    if (threadIdx.x == 0) b.block_counts2[blockIdx.x] = (uint32_t)outB;
+  }
+  if (which == 1 && A.active) {
     unsigned long long c[2] = {viable, dominated};
     block_sum(c);
     mkey = block_min(mkey);
@@ -587,33 +683,27 @@ __global__ void __launch_bounds__(kScanBlock, 2) mark_kernel(const SolverCfg cfg
       if (mkey != ~0ULL) atomicMin((unsigned long long*)&d->dropped_min_key, (unsigned long long)mkey);
     }
   }
-  (void)cfg;
 }
 
-// gather the selected parents into the staging planes
-struct GatherParents {
-  SolverCfg cfg;
-  SolverBufs b;
-  __device__ void operator()(uint64_t i, uint64_t pos) const
-  {
-    const uint64_t s = parity_buf(b.slot, b.dev->parity)[i];
-    if (pos >= cfg.e_max) {  // more marks than parents: never written, flagged
-      b.dev->error = 1;
-      return;
-    }
-    for (int v = 0; v < cfg.n_vars; ++v) {
-      const double lo = b.lo[(uint64_t)v * cfg.pstride + s];
-      const double hi = b.hi[(uint64_t)v * cfg.pstride + s];
-      b.plo[(uint64_t)v * cfg.e_max + pos] = lo;
-      b.phi[(uint64_t)v * cfg.e_max + pos] = hi;
-      if (b.plo32 != nullptr) {
-        b.plo32[(uint64_t)v * cfg.e_max + pos] = __double2float_rd(lo);
-        b.phi32[(uint64_t)v * cfg.e_max + pos] = __double2float_ru(hi);
-      }
-    }
-    b.pdepth[pos] = b.depth[s];
+// stage the box in store slot `s` as parent `pos` of the staging planes
+__device__ __forceinline__ void stage_parent(const SolverCfg& cfg, const SolverBufs& b, uint64_t s, uint64_t pos)
+{
+  if (pos >= cfg.e_max) {  // more marks than parents: never written, flagged
+    b.dev->error = 1;
+    return;
   }
-};
+  for (int v = 0; v < cfg.n_vars; ++v) {
+    const double lo = b.lo[(uint64_t)v * cfg.pstride + s];
+    const double hi = b.hi[(uint64_t)v * cfg.pstride + s];
+    b.plo[(uint64_t)v * cfg.e_max + pos] = lo;
+    b.phi[(uint64_t)v * cfg.e_max + pos] = hi;
+    if (b.plo32 != nullptr) {
+      b.plo32[(uint64_t)v * cfg.e_max + pos] = __double2float_rd(lo);
+      b.phi32[(uint64_t)v * cfg.e_max + pos] = __double2float_ru(hi);
+    }
+  }
+  b.pdepth[pos] = b.depth[s];
+}
 
 // decode a kept child from its parent into a free store slot and append it
 // behind the pool in the current buffer (position pool_size + pos)
@@ -648,7 +738,7 @@ struct AppendChild {
     const uint32_t p = d->parity;
     parity_buf(b.lb, p)[at] = b.clb[g];
     parity_buf(b.slot, p)[at] = (uint32_t)s;
-    b.sel[at] = kSelAlive;
+    parity_buf(b.sel, p)[at] = kSelAlive;
   }
 };
 
@@ -680,54 +770,59 @@ __global__ void __launch_bounds__(kScanBlock) scatter_kernel(const P pred, const
 }
 
 // Stages this iteration's parents (kSelParent entries of the pool, in
-// position order) from the store into the parent planes.
+// position order) from the store into the parent planes, unless the
+// previous iteration staged them.
 __global__ void __launch_bounds__(kScanBlock) gather_parents_kernel(const SolverCfg cfg, const SolverBufs b,
                                                                     const uint32_t* __restrict__ offsets)
 {
   const uint64_t t0 = tile_first();
   const SolverDev* d = b.dev;
-  const uint32_t done = d->done;
+  if (d->done || d->skip_select) return;
   const uint64_t n = d->pool_size;
   const uint64_t base = offsets[blockIdx.x];
+  const uint8_t* __restrict__ sel = pool_sel(b);
   uint8_t sv[kScanItems];
 #pragma unroll
   for (int j = 0; j < kScanItems; ++j) {
     const uint64_t i = tile_item(t0, j);
-    sv[j] = i < cfg.pstride ? b.sel[i] : kSelAlive;
+    sv[j] = i < cfg.pstride ? sel[i] : kSelAlive;
   }
-  if (done) return;
   if ((uint64_t)blockIdx.x * kScanTile >= n) return;
   bool f[kScanItems];
 #pragma unroll
   for (int j = 0; j < kScanItems; ++j) f[j] = tile_item(t0, j) < n && sv[j] == kSelParent;
   int rank[kScanItems];
   tile_ranks(f, rank);
-  const GatherParents op{cfg, b};
+  const uint32_t* slot = parity_buf(b.slot, d->parity);
 #pragma unroll
   for (int j = 0; j < kScanItems; ++j)
-    if (f[j]) op(tile_item(t0, j), base + (uint64_t)rank[j]);
+    if (f[j]) stage_parent(cfg, b, slot[tile_item(t0, j)], base + (uint64_t)rank[j]);
 }
 
-// Moves the alive entries of the current buffer, in order, to the other
-// buffer (lower bound and store slot), folds their lower bounds into the
-// pool minimum, and pushes the store slots of the others (this iteration's
-// parents and the evicted) onto the free stack in position order.
-__global__ void __launch_bounds__(kScanBlock, 2) copy_pool_kernel(const SolverCfg cfg, const SolverBufs b,
-                                                                  const uint32_t* __restrict__ offsets)
+// Moves the entries that stay, in order, to the other buffer (lower bound,
+// store slot and mark), folds their keys into the pool's key range, lists
+// the store slots of the next iteration's parents among them in order, and
+// pushes the store slots of the others (this iteration's parents and the
+// evicted) onto the free stack in position order.
+__global__ void __launch_bounds__(kScanBlock, 2) copy_pool_kernel(const SolverCfg cfg, const SolverBufs b)
 {
   const uint64_t t0 = tile_first();
   SolverDev* d = b.dev;
-  // control words, the tile's entries and its offset are loaded together
+  // control words, the tile's entries and its offsets are loaded together
   const uint32_t done = d->done;
   const uint64_t n = d->extent;
   const uint64_t free_base = d->free_top;
+  const bool pre = d->pre_k > 0;
   const uint32_t p = d->parity, q = 1 - p;
   const uint64_t* __restrict__ slb = reinterpret_cast<const uint64_t*>(parity_buf(b.lb, p));
   const uint32_t* __restrict__ sslot = parity_buf(b.slot, p);
+  const uint8_t* __restrict__ ssel = parity_buf(b.sel, p);
   uint64_t* __restrict__ dlb = reinterpret_cast<uint64_t*>(parity_buf(b.lb, q));
   uint32_t* __restrict__ dslot = parity_buf(b.slot, q);
-  const uint64_t base = offsets[blockIdx.x];
-  bool f[kScanItems], in[kScanItems];
+  uint8_t* __restrict__ dsel = parity_buf(b.sel, q);
+  const uint64_t base = b.block_offsets[blockIdx.x];
+  const uint64_t pbase = b.block_offsets2[blockIdx.x];
+  bool f[kScanItems], g[kScanItems], in[kScanItems];
   uint64_t x[kScanItems];  // raw bits of the lower bounds
   uint32_t sl[kScanItems];
   uint8_t sv[kScanItems];
@@ -735,7 +830,7 @@ __global__ void __launch_bounds__(kScanBlock, 2) copy_pool_kernel(const SolverCf
   for (int j = 0; j < kScanItems; ++j) {
     const uint64_t i = tile_item(t0, j);
     const bool inb = i < cfg.pstride;
-    sv[j] = inb ? b.sel[i] : kSelParent;
+    sv[j] = inb ? ssel[i] : kSelParent;
     x[j] = inb ? slb[i] : 0;
     sl[j] = inb ? sslot[i] : 0u;
   }
@@ -744,24 +839,33 @@ __global__ void __launch_bounds__(kScanBlock, 2) copy_pool_kernel(const SolverCf
 #pragma unroll
   for (int j = 0; j < kScanItems; ++j) {
     in[j] = tile_item(t0, j) < n;
-    f[j] = in[j] && sv[j] == kSelAlive;
+    f[j] = in[j] && (sv[j] == kSelAlive || sv[j] == kSelNextParent);
+    g[j] = in[j] && sv[j] == kSelNextParent;
   }
-  int rank[kScanItems];  // alive entries before each item of the tile
-  tile_ranks(f, rank);
+  int rank[kScanItems];  // entries that stay before each item of the tile
+  tile_ranks<0>(f, rank);
+  int prank[kScanItems] = {};
+  if (pre) tile_ranks<1>(g, prank);  // the same for the whole grid
   uint64_t mkey = ~0ULL, xkey = 0;
 #pragma unroll
   for (int j = 0; j < kScanItems; ++j) {
     if (!in[j]) continue;
     const uint64_t i = tile_item(t0, j);
-    const uint64_t alive_before = base + (uint64_t)rank[j];
+    const uint64_t stay_before = base + (uint64_t)rank[j];
     if (f[j]) {
-      dlb[alive_before] = x[j];
-      dslot[alive_before] = sl[j];
+      dlb[stay_before] = x[j];
+      dslot[stay_before] = sl[j];
+      dsel[stay_before] = g[j] ? kSelParent : kSelAlive;
+      if (g[j]) {
+        const uint64_t pos = pbase + (uint64_t)prank[j];
+        if (pos < cfg.e_max) b.pslot[pos] = sl[j];
+        else d->error = 1;
+      }
       const uint64_t k = bits_key(x[j]);
       mkey = k < mkey ? k : mkey;
       xkey = k > xkey ? k : xkey;
     } else {
-      b.free_slots[free_base + (i - alive_before)] = sl[j];
+      b.free_slots[free_base + (i - stay_before)] = sl[j];
     }
   }
   mkey = block_min(mkey);
@@ -770,7 +874,16 @@ __global__ void __launch_bounds__(kScanBlock, 2) copy_pool_kernel(const SolverCf
     if (mkey != ~0ULL) atomicMin((unsigned long long*)&d->pool_min_key, (unsigned long long)mkey);
     if (xkey != 0) atomicMax((unsigned long long*)&d->pool_max_key, (unsigned long long)xkey);
   }
-  (void)cfg;
+}
+
+// stages the next iteration's parents listed by the pool move
+__global__ void stage_next_kernel(const SolverCfg cfg, const SolverBufs b)
+{
+  const SolverDev* d = b.dev;
+  if (d->done) return;
+  const uint64_t n = d->pre_count < cfg.e_max ? d->pre_count : cfg.e_max;
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
+    stage_parent(cfg, b, b.pslot[k], k);
 }
 
 // pool entries [start, start + count) in position order, unpacked from the
@@ -934,6 +1047,12 @@ __global__ void size_kernel(const SolverCfg cfg, const SolverBufs b)
   d->extent = d->pool_size + d->kept;
   d->free_top -= d->kept;  // taken by the appended children
   d->evict = d->new_size > cfg.cap ? 1 : 0;
+  // the next iteration's parents: its E (search/driver.hpp:221-233) over the
+  // pool this iteration leaves
+  const uint64_t next_L = d->evict ? cfg.cap : d->new_size;
+  uint64_t E = next_L < cfg.e_max ? next_L : cfg.e_max;
+  const uint64_t left = cfg.iter_limit > d->expansions ? cfg.iter_limit - d->expansions : 0;
+  d->pre_k = E < left ? E : left;
   d->evict_lo_key = d->pool_min_key < d->child_min_key ? d->pool_min_key : d->child_min_key;
   d->evict_hi_key = d->pool_max_key > d->child_max_key ? d->pool_max_key : d->child_max_key;
   d->pool_min_key = ~0ULL;  // refilled by the move to the other buffer
@@ -950,6 +1069,8 @@ __global__ void finish_kernel(const SolverCfg cfg, const SolverBufs b)
   if (d->survivors != expect) d->error = 1;
   d->free_top += d->extent - d->survivors;  // the parents' and the evicted slots
   if (d->free_top + d->survivors != cfg.pstride) d->error = 1;
+  if (d->pre_count != d->pre_k) d->error = 1;
+  d->pre_valid = d->pre_k > 0 ? 1u : 0u;
   d->pool_size = d->survivors;
   d->parity = 1 - d->parity;
   if (d->dropped_min_key != ~0ULL) d->dropped_lb_min = key_to_lb(d->dropped_min_key);
@@ -989,18 +1110,18 @@ __global__ void pool_min_reset_kernel(const SolverBufs b, uint64_t* viable_out)
 // ---------------------------------------------------------------------
 static int tiles(uint64_t max_items) { return (int)((max_items + kScanTile - 1) / kScanTile); }
 
-static void scan(const SolverBufs& b, const uint64_t* n_items_dev, uint64_t* total_dev, const uint32_t* active,
-                 cudaStream_t s)
+static void scan(const SolverBufs& b, const uint32_t* counts, uint32_t* offsets, const uint64_t* n_items_dev,
+                 uint64_t* total_dev, const uint32_t* active, const uint32_t* skip, cudaStream_t s)
 {
-  scan_kernel<<<1, 1024, 0, s>>>(b.block_counts, b.block_offsets, n_items_dev, total_dev, active, &b.dev->done);
+  scan_kernel<<<1, 1024, 0, s>>>(counts, offsets, n_items_dev, total_dev, active, skip, &b.dev->done);
 }
 
 template <class P>
 static void compact(const P& pred, uint64_t max_items, const uint64_t* n_items_dev, uint64_t* total_dev,
-                    const SolverBufs& b, const uint32_t* active, cudaStream_t s)
+                    const SolverBufs& b, cudaStream_t s)
 {
   count_kernel<P><<<tiles(max_items), kScanBlock, 0, s>>>(pred, b.block_counts);
-  scan(b, n_items_dev, total_dev, active, s);
+  scan(b, b.block_counts, b.block_offsets, n_items_dev, total_dev, nullptr, nullptr, s);
 }
 
 template <class P, class Op>
@@ -1009,23 +1130,29 @@ static void scatter(const P& pred, const Op& op, uint64_t max_items, cudaStream_
   scatter_kernel<P, Op><<<tiles(max_items), kScanBlock, 0, s>>>(pred, op, b.block_offsets);
 }
 
+// which = 0: this iteration's parents (skipped when the previous iteration
+// staged them); which = 1: the cap and the next iteration's parents
 static void radix_select(const SolverCfg& cfg, const SolverBufs& b, int which, uint64_t max_items, cudaStream_t s)
 {
+  const int T = which == 0 ? 1 : 2;
+  const uint32_t* skip = which == 0 ? &b.dev->skip_select : nullptr;
   radix_init_kernel<<<1, 256, 0, s>>>(cfg, b, which);
   const int grid = (int)std::min<uint64_t>((max_items + 255) / 256, 4096);
   // digits of up to 11 bits from below the keys' common leading bits;
-  // the passes after the bucket settles or the bits run out return at once
+  // the passes after the buckets settle or the bits run out return at once
   for (int p = 0; p < (64 + kRadixBits - 1) / kRadixBits; ++p) {
     radix_hist_kernel<<<grid, 256, 0, s>>>(cfg, b, which);
-    radix_pick_kernel<<<1, kPickThreads, 0, s>>>(b);
+    radix_pick_kernel<<<T, kPickThreads, 0, s>>>(b);
   }
-  // ranks among entries inside the threshold bucket, then the marks with
-  // the tile counts of the entries the next compaction moves
+  // ranks among entries inside the threshold buckets, then the marks with
+  // the tile counts of the entries the next compactions move
   const uint64_t* n_dev = which == 0 ? &b.dev->pool_size : &b.dev->extent;
-  EqKey eq{b, which};
-  compact(eq, max_items, n_dev, nullptr, b, &b.radix->rank, s);
-  mark_kernel<<<tiles(max_items), kScanBlock, 0, s>>>(cfg, b, which, b.block_offsets, b.block_counts);
-  scan(b, n_dev, which == 0 ? nullptr : &b.dev->survivors, nullptr, s);
+  eq_count_kernel<<<tiles(max_items), kScanBlock, 0, s>>>(cfg, b, which);
+  scan(b, b.block_counts, b.block_offsets, n_dev, nullptr, &b.radix[0].rank, skip, s);
+  if (which == 1) scan(b, b.block_counts2, b.block_offsets2, n_dev, nullptr, &b.radix[1].rank, nullptr, s);
+  mark_kernel<<<tiles(max_items), kScanBlock, 0, s>>>(cfg, b, which);
+  scan(b, b.block_counts, b.block_offsets, n_dev, which == 0 ? nullptr : &b.dev->survivors, nullptr, skip, s);
+  if (which == 1) scan(b, b.block_counts2, b.block_offsets2, n_dev, &b.dev->pre_count, nullptr, nullptr, s);
 }
 
 static void mark(const cudaEvent_t* marks, int i, cudaStream_t s)
@@ -1081,7 +1208,7 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
     e = launch_eval(ea, 2, true, eval_grid, kEvalThreads, s);
     if (e != cudaSuccess) return e;
     ScreenedChild sc{b};
-    compact(sc, max_children, &b.dev->n_children, &b.dev->certify_count, b, nullptr, s);
+    compact(sc, max_children, &b.dev->n_children, &b.dev->certify_count, b, s);
     scatter(sc, ListChild{b}, max_children, s, b);
     EvalArgs ca = ea;
     ca.prog = b.prog64;
@@ -1153,16 +1280,18 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
   // the kept children go behind the pool in the current buffer; the
   // parents stay there as holes until the one compaction below
   KeptChild kept{b};
-  compact(kept, max_children, &b.dev->n_children, &b.dev->kept, b, nullptr, s);
+  compact(kept, max_children, &b.dev->n_children, &b.dev->kept, b, s);
   scatter(kept, AppendChild{cfg, b}, max_children, s, b);
   size_kernel<<<1, 1, 0, s>>>(cfg, b);
 
   // (6) over the cap: keep the `cap` best alive entries, fold the rest into
   // the floor; then move every alive entry to the other buffer in order
   radix_select(cfg, b, 1, max_pool, s);
-  copy_pool_kernel<<<tiles(max_pool), kScanBlock, 0, s>>>(cfg, b, b.block_offsets);
-  // every entry of the next pool starts alive
-  cudaMemsetAsync(b.sel, kSelAlive, cfg.pstride, s);
+  copy_pool_kernel<<<tiles(max_pool), kScanBlock, 0, s>>>(cfg, b);
+  {
+    const int grid = (int)std::min<uint64_t>((cfg.e_max + 255) / 256, 1024);
+    stage_next_kernel<<<grid, 256, 0, s>>>(cfg, b);
+  }
   finish_kernel<<<1, 1, 0, s>>>(cfg, b);
   mark(marks, 4, s);
   return cudaGetLastError();
@@ -1174,7 +1303,8 @@ cudaError_t solver_init(const SolverCfg& cfg, const SolverBufs& b, const double*
   init_kernel<<<1, 256, 0, s>>>(cfg, b, root_lb_dev, root_ub_dev, gub0);
   const int grid = (int)std::min<uint64_t>((cfg.pstride + 255) / 256, 4096);
   free_init_kernel<<<grid, 256, 0, s>>>(cfg, b);
-  cudaMemsetAsync(b.sel, kSelAlive, cfg.pstride, s);
+  cudaMemsetAsync(b.sel[0], kSelAlive, cfg.pstride, s);
+  cudaMemsetAsync(b.sel[1], kSelAlive, cfg.pstride, s);
   return cudaGetLastError();
 }
 

@@ -211,6 +211,10 @@ __global__ void radix_hist_kernel(const SolverCfg cfg, const SolverBufs b, int w
     mask[t] = r.mask;
   }
   if (!go[0] && !go[1]) return;
+  // while both targets sit in the same bucket (the first pass of a rebuild)
+  // their histograms are the same: count once, add to both
+  const bool same = go[0] && go[1] && prefix[0] == prefix[1] && mask[0] == mask[1] && shift[0] == shift[1];
+  const bool count1 = go[1] && !same;
   const uint64_t n = rs_n(b.dev, which);
   if ((uint64_t)blockIdx.x * blockDim.x >= n) return;
   for (int t = 0; t < 2; ++t)
@@ -240,7 +244,7 @@ __global__ void radix_hist_kernel(const SolverCfg cfg, const SolverBufs b, int w
       const uint64_t key = bits_key(x[u]);
 #pragma unroll
       for (int t = 0; t < 2; ++t) {
-        if (!go[t] || (key & mask[t]) != prefix[t]) continue;
+        if (!(t == 0 ? go[0] : count1) || (key & mask[t]) != prefix[t]) continue;
         const uint32_t bin = (uint32_t)(key >> shift[t]) & (uint32_t)(nb[t] - 1);
         if (bin != run_bin[t]) {
           if (run[t]) atomicAdd(&h[t][run_bin[t]], run[t]);
@@ -256,8 +260,9 @@ __global__ void radix_hist_kernel(const SolverCfg cfg, const SolverBufs b, int w
   __syncthreads();
   for (int t = 0; t < T; ++t) {
     if (!go[t]) continue;
+    const uint32_t* src = (t == 1 && same) ? h[0] : h[t];
     for (int i = threadIdx.x; i < nb[t]; i += blockDim.x)
-      if (h[t][i]) atomicAdd(&b.radix[t].hist[i], h[t][i]);
+      if (src[i]) atomicAdd(&b.radix[t].hist[i], src[i]);
   }
   (void)cfg;
 }
@@ -387,6 +392,72 @@ __device__ __forceinline__ int tile_ranks(const bool (&f)[kScanItems], int (&ran
 #pragma unroll
   for (int j = 0; j < kScanItems; ++j) rank[j] = tab[j * kWarps + wid] + __popc(ball[j] & lt);
   return tile_total;
+}
+
+// tile_ranks of two flag sets with one pair of barriers
+__device__ __forceinline__ void tile_ranks2(const bool (&f)[kScanItems], const bool (&g)[kScanItems],
+                                            int (&rf)[kScanItems], int (&rg)[kScanItems])
+{
+  constexpr int kWarps = kScanBlock / 32;
+  constexpr int kPer = kScanItems * kWarps / 32;
+  __shared__ int tab[2][kScanItems * kWarps];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  unsigned bf[kScanItems], bg[kScanItems];
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    bf[j] = __ballot_sync(0xffffffffu, f[j]);
+    bg[j] = __ballot_sync(0xffffffffu, g[j]);
+    if (lane == 0) {
+      tab[0][j * kWarps + wid] = __popc(bf[j]);
+      tab[1][j * kWarps + wid] = __popc(bg[j]);
+    }
+  }
+  __syncthreads();
+  if (wid < 2) {  // warp 0 scans the first table, warp 1 the second
+    int* t = tab[wid];
+    int v[kPer], sum = 0;
+#pragma unroll
+    for (int e = 0; e < kPer; ++e) {
+      v[e] = t[lane * kPer + e];
+      sum += v[e];
+    }
+    int x = sum;
+    for (int off = 1; off < 32; off <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, off);
+      if (lane >= off) x += y;
+    }
+    int run = x - sum;
+#pragma unroll
+    for (int e = 0; e < kPer; ++e) {
+      t[lane * kPer + e] = run;
+      run += v[e];
+    }
+  }
+  __syncthreads();
+  const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    rf[j] = tab[0][j * kWarps + wid] + __popc(bf[j] & lt);
+    rg[j] = tab[1][j * kWarps + wid] + __popc(bg[j] & lt);
+  }
+}
+
+__device__ __forceinline__ uint64_t warp_min_u64(uint64_t m)
+{
+  for (int off = 16; off > 0; off >>= 1) {
+    const uint64_t o = __shfl_xor_sync(0xffffffffu, m, off);
+    m = o < m ? o : m;
+  }
+  return m;
+}
+
+__device__ __forceinline__ uint64_t warp_max_u64(uint64_t m)
+{
+  for (int off = 16; off > 0; off >>= 1) {
+    const uint64_t o = __shfl_xor_sync(0xffffffffu, m, off);
+    m = o > m ? o : m;
+  }
+  return m;
 }
 
 // Sum of `c` over the block (one call per kernel and slot `S`).
@@ -667,21 +738,36 @@ __global__ void __launch_bounds__(kScanBlock, 2) mark_kernel(const SolverCfg cfg
     outA += ta ? 1 : 0;
     outB += tb ? 1 : 0;
   }
-  outA = tile_count<0>(outA);
-  if (threadIdx.x == 0) b.block_counts[blockIdx.x] = (uint32_t)outA;
-  if (which == 1) {
-    outB = tile_count<1>(outB);
-    if (threadIdx.x == 0) b.block_counts2[blockIdx.x] = (uint32_t)outB;
+  // the tile's counts and the eviction tallies, with one barrier
+  struct Part {
+    uint32_t a, b, viable, dominated;
+    uint64_t mkey;
+  };
+  __shared__ Part part[kScanBlock / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  {
+    const uint32_t pa = __reduce_add_sync(0xffffffffu, (uint32_t)outA);
+    const uint32_t pb = __reduce_add_sync(0xffffffffu, (uint32_t)outB);
+    const uint32_t pv = __reduce_add_sync(0xffffffffu, viable);
+    const uint32_t pd = __reduce_add_sync(0xffffffffu, dominated);
+    const uint64_t pm = warp_min_u64(mkey);
+    if (lane == 0) part[wid] = Part{pa, pb, pv, pd, pm};
   }
+  __syncthreads();
+  if (wid != 0) return;
+  const bool has = lane < kScanBlock / 32;
+  const uint32_t ta = __reduce_add_sync(0xffffffffu, has ? part[lane].a : 0u);
+  const uint32_t tb = __reduce_add_sync(0xffffffffu, has ? part[lane].b : 0u);
+  const uint32_t tv = __reduce_add_sync(0xffffffffu, has ? part[lane].viable : 0u);
+  const uint32_t td = __reduce_add_sync(0xffffffffu, has ? part[lane].dominated : 0u);
+  const uint64_t tm = warp_min_u64(has ? part[lane].mkey : ~0ULL);
+  if (lane != 0) return;
+  b.block_counts[blockIdx.x] = ta;
+  if (which == 1) b.block_counts2[blockIdx.x] = tb;
   if (which == 1 && A.active) {
-    unsigned long long c[2] = {viable, dominated};
-    block_sum(c);
-    mkey = block_min(mkey);
-    if (threadIdx.x == 0) {
-      if (c[0]) atomicAdd((unsigned long long*)&d->counters.dropped_viable, c[0]);
-      if (c[1]) atomicAdd((unsigned long long*)&d->counters.dropped_dominated, c[1]);
-      if (mkey != ~0ULL) atomicMin((unsigned long long*)&d->dropped_min_key, (unsigned long long)mkey);
-    }
+    if (tv) atomicAdd((unsigned long long*)&d->counters.dropped_viable, (unsigned long long)tv);
+    if (td) atomicAdd((unsigned long long*)&d->counters.dropped_dominated, (unsigned long long)td);
+    if (tm != ~0ULL) atomicMin((unsigned long long*)&d->dropped_min_key, (unsigned long long)tm);
   }
 }
 
@@ -812,7 +898,6 @@ __global__ void __launch_bounds__(kScanBlock, 2) copy_pool_kernel(const SolverCf
   const uint32_t done = d->done;
   const uint64_t n = d->extent;
   const uint64_t free_base = d->free_top;
-  const bool pre = d->pre_k > 0;
   const uint32_t p = d->parity, q = 1 - p;
   const uint64_t* __restrict__ slb = reinterpret_cast<const uint64_t*>(parity_buf(b.lb, p));
   const uint32_t* __restrict__ sslot = parity_buf(b.slot, p);
@@ -842,11 +927,36 @@ __global__ void __launch_bounds__(kScanBlock, 2) copy_pool_kernel(const SolverCf
     f[j] = in[j] && (sv[j] == kSelAlive || sv[j] == kSelNextParent);
     g[j] = in[j] && sv[j] == kSelNextParent;
   }
-  int rank[kScanItems];  // entries that stay before each item of the tile
-  tile_ranks<0>(f, rank);
-  int prank[kScanItems] = {};
-  if (pre) tile_ranks<1>(g, prank);  // the same for the whole grid
-  uint64_t mkey = ~0ULL, xkey = 0;
+  // the key range of the entries that stay, per warp before the barriers
+  // of the ranks, for thread 0 after them
+  __shared__ uint64_t part_min[kScanBlock / 32], part_max[kScanBlock / 32];
+  {
+    uint64_t mkey = ~0ULL, xkey = 0;
+#pragma unroll
+    for (int j = 0; j < kScanItems; ++j)
+      if (f[j]) {
+        const uint64_t k = bits_key(x[j]);
+        mkey = k < mkey ? k : mkey;
+        xkey = k > xkey ? k : xkey;
+      }
+    mkey = warp_min_u64(mkey);
+    xkey = warp_max_u64(xkey);
+    if ((threadIdx.x & 31) == 0) {
+      part_min[threadIdx.x >> 5] = mkey;
+      part_max[threadIdx.x >> 5] = xkey;
+    }
+  }
+  int rank[kScanItems], prank[kScanItems];  // stayers / next parents before each item
+  tile_ranks2(f, g, rank, prank);
+  if (threadIdx.x == 0) {
+    uint64_t mkey = ~0ULL, xkey = 0;
+    for (int w = 0; w < kScanBlock / 32; ++w) {
+      mkey = part_min[w] < mkey ? part_min[w] : mkey;
+      xkey = part_max[w] > xkey ? part_max[w] : xkey;
+    }
+    if (mkey != ~0ULL) atomicMin((unsigned long long*)&d->pool_min_key, (unsigned long long)mkey);
+    if (xkey != 0) atomicMax((unsigned long long*)&d->pool_max_key, (unsigned long long)xkey);
+  }
 #pragma unroll
   for (int j = 0; j < kScanItems; ++j) {
     if (!in[j]) continue;
@@ -861,18 +971,9 @@ __global__ void __launch_bounds__(kScanBlock, 2) copy_pool_kernel(const SolverCf
         if (pos < cfg.e_max) b.pslot[pos] = sl[j];
         else d->error = 1;
       }
-      const uint64_t k = bits_key(x[j]);
-      mkey = k < mkey ? k : mkey;
-      xkey = k > xkey ? k : xkey;
     } else {
       b.free_slots[free_base + (i - stay_before)] = sl[j];
     }
-  }
-  mkey = block_min(mkey);
-  xkey = block_max(xkey);
-  if (threadIdx.x == 0) {
-    if (mkey != ~0ULL) atomicMin((unsigned long long*)&d->pool_min_key, (unsigned long long)mkey);
-    if (xkey != 0) atomicMax((unsigned long long*)&d->pool_max_key, (unsigned long long)xkey);
   }
 }
 

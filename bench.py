@@ -60,9 +60,11 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-batch", action="store_true", help="skip the 1024-instance batch (config 4)")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving stream (config 5)")
-    ap.add_argument("--only", choices=["batch", "serve"], help="run one of the extra workloads alone")
+    ap.add_argument("--only", choices=["batch", "serve", "ttg"], help="run one of the extra workloads alone")
     ap.add_argument("--instances", type=int, default=1024, help="--only batch: instances in the batch")
-    ap.add_argument("--precision", choices=["fp64", "fp32"], help="--only batch: one form only")
+    ap.add_argument("--precision", choices=["fp64", "fp32"], help="--only batch / ttg: one form only")
+    ap.add_argument("--ttg-iters", type=int, default=0,
+                    help="--only ttg: stop after this many iterations (0: run to the gap); the profiling case")
     return ap.parse_args()
 
 
@@ -317,21 +319,24 @@ def e2e_run(dp, problem, steps, warmup):
             "d2h_bytes_per_step": d2h, "regions_per_call": N, "ms_per_step": 1e3 * total / len(times)}
 
 
-def time_to_gap(problem, precision, limit_s):
+def time_to_gap(problem, precision, limit_s, iters=0):
     from cuminlp_gb300.solver import DeviceProblem, Solver
     dp = DeviceProblem(problem)
     s = Solver(dp, bisection_budget=TTG_B, batch_parents=TTG_E, frontier_cap=TTG_CAP, precision=precision,
-               time_limit_ms=int(limit_s * 1000), iter_limit=1 << 62)
+               time_limit_ms=int(limit_s * 1000), iter_limit=1 << 62, batch_iter_limit=iters)
     t0 = time.perf_counter()
     s.step(0)
     dt = time.perf_counter() - t0
     o = s.outcome()
+    phases = s.phase_ms()  # the last iteration: select+branch, bound, sample, prune+rebuild, whole
     s.close()
     gap = o["upper_bound"] - o["lower_bound"]
     rel = gap / max(1.0, abs(o["upper_bound"]))
     return {"seconds": round(dt, 3), "converged": o["stop_reason"] == "converged",
             "proven_optimal": bool(o["proven_optimal"]), "lower_bound": o["lower_bound"],
-            "upper_bound": o["upper_bound"], "rel_gap": rel, "boxes": o["counters"]["bounded"]}
+            "upper_bound": o["upper_bound"], "rel_gap": rel, "boxes": o["counters"]["bounded"],
+            "iterations": o["counters"]["iterations"], "frontier": o["frontier_size"],
+            "last_iteration_phases_ms": [round(x, 3) for x in phases]}
 
 
 BATCH_OPTS = dict(bisection_budget=4, batch_parents=256, frontier_cap=4096, sample_points=1)
@@ -421,6 +426,11 @@ def run_ours(args):
     if args.only == "batch":
         precs = ("fp64", "fp32") if args.precision is None else (args.precision,)
         print(json.dumps({p: batch_run(rt, p, args.steps, args.warmup, args.instances) for p in precs}))
+        return
+    if args.only == "ttg":
+        prec = args.precision or "fp64"
+        print(json.dumps({"config": "n=4 QCQP (config 1, instance 0)", "precision": prec,
+                          "run": time_to_gap(G.config1(0), prec, 20.0, args.ttg_iters)}))
         return
     if args.only == "serve":
         from cuminlp_gb300.solver import DeviceProblem

@@ -799,8 +799,12 @@ struct cmn_solver {
   SolverCfg cfg{};
   SolverBufs b{};
   cudaStream_t stream = nullptr;
+  // the first iteration selects its parents; every later one finds them
+  // staged by its predecessor and runs the graph without the select
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph_steady = nullptr;
+  cudaGraphExec_t exec_steady = nullptr;
   SolverDev* h_dev = nullptr;  // pinned mirror
   uint64_t* d_viable = nullptr;
   uint64_t* h_viable = nullptr;
@@ -820,6 +824,8 @@ struct cmn_solver {
       if (ev) cudaEventDestroy(ev);
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
+    if (exec_steady) cudaGraphExecDestroy(exec_steady);
+    if (graph_steady) cudaGraphDestroy(graph_steady);
     for (void* a : allocs) cudaFree(a);
     if (h_dev) cudaFreeHost(h_dev);
     if (h_viable) cudaFreeHost(h_viable);
@@ -964,25 +970,28 @@ extern "C" cmn_status cmn_solver_create(const cmn_problem* p, const cmn_solve_op
     if (e == cudaSuccess) e = cudaMemsetAsync(b.best_point, 0xff, (size_t)n * sizeof(double), s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     for (int i = 0; i < 5 && e == cudaSuccess; ++i) e = cudaEventCreate(&s->marks[i]);
-    // capture one iteration
-    if (e == cudaSuccess) e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
-    if (e == cudaSuccess) {
-      cudaError_t e2 = solver_iteration(cfg, b, s->eval_grid, s->sample_grid, s->stream, s->marks);
-      e = cudaStreamEndCapture(s->stream, &s->graph);
-      if (e2 != cudaSuccess) e = e2;
+    // capture one iteration, with and without the parent select
+    for (int steady = 0; steady < 2 && e == cudaSuccess; ++steady) {
+      cudaGraph_t* g = steady ? &s->graph_steady : &s->graph;
+      e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
+      if (e == cudaSuccess) {
+        cudaError_t e2 = solver_iteration(cfg, b, s->eval_grid, s->sample_grid, s->stream, s->marks, steady == 0);
+        e = cudaStreamEndCapture(s->stream, g);
+        if (e2 != cudaSuccess) e = e2;
+      }
+      if (e == cudaSuccess) e = cudaGraphInstantiate(steady ? &s->exec_steady : &s->exec, *g, 0);
     }
-    if (e == cudaSuccess) {
+    if (e == cudaSuccess) {  // kernels of a steady iteration
       size_t nn = 0;
-      e = cudaGraphGetNodes(s->graph, nullptr, &nn);
+      e = cudaGraphGetNodes(s->graph_steady, nullptr, &nn);
       std::vector<cudaGraphNode_t> nodes(nn);
-      if (e == cudaSuccess && nn) e = cudaGraphGetNodes(s->graph, nodes.data(), &nn);
+      if (e == cudaSuccess && nn) e = cudaGraphGetNodes(s->graph_steady, nodes.data(), &nn);
       for (size_t i = 0; i < nn && e == cudaSuccess; ++i) {
         cudaGraphNodeType t;
         e = cudaGraphNodeGetType(nodes[i], &t);
         if (t == cudaGraphNodeTypeKernel) ++s->kernels_per_iter;
       }
     }
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&s->exec, s->graph, 0);
     if (e != cudaSuccess) {
       delete s;
       return fail(CMN_CUDA_ERROR, std::string("solver setup: ") + cudaGetErrorString(e));
@@ -1017,7 +1026,7 @@ extern "C" cmn_status cmn_solver_step(cmn_solver* s, uint64_t max_iterations)
   while (!s->h_dev->done && (max_iterations == 0 || done_iters < max_iterations)) {
     uint64_t k = burst;
     if (max_iterations) k = std::min<uint64_t>(k, max_iterations - done_iters);
-    for (uint64_t i = 0; i < k; ++i) CK(cudaGraphLaunch(s->exec, s->stream));
+    for (uint64_t i = 0; i < k; ++i) CK(cudaGraphLaunch(s->launched + i == 0 ? s->exec : s->exec_steady, s->stream));
     done_iters += k;
     s->launched += k;
     st = pull_state(s);

@@ -168,8 +168,11 @@ cudaError_t solver_init(const SolverCfg& cfg, const SolverBufs& b, const double*
 // Enqueues one batched iteration (all kernels) on `s`; capturable.
 // `marks` (5 events or null) are recorded as event nodes at the phase
 // boundaries: start, after branching, after bounding, after sampling, end.
+// `with_select`: the iteration selects and stages its own parents (the first
+// iteration); otherwise the previous iteration staged them, and the
+// iteration flags a device error if it did not.
 cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval_grid, int sample_grid,
-                             cudaStream_t s, const cudaEvent_t* marks);
+                             cudaStream_t s, const cudaEvent_t* marks, bool with_select);
 // Fills min key / viable count of the current pool (after the run).
 cudaError_t solver_pool_stats(const SolverCfg& cfg, const SolverBufs& b, uint64_t* viable_dev, cudaStream_t s);
 // Copies pool entries [start, start + count) in position order: boxes as

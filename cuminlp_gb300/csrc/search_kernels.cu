@@ -71,7 +71,7 @@ __global__ void free_init_kernel(const SolverCfg cfg, const SolverBufs b)
 
 // Top of the loop of search/driver.hpp:221-233: convergence of the least
 // pending lower bound, the expansion budget, and this iteration's size.
-__global__ void begin_kernel(const SolverCfg cfg, const SolverBufs b)
+__global__ void begin_kernel(const SolverCfg cfg, const SolverBufs b, int require_staged)
 {
   SolverDev* d = b.dev;
   d->improved = 0;  // an iteration after the stop must not rewrite the witness
@@ -97,6 +97,7 @@ __global__ void begin_kernel(const SolverCfg cfg, const SolverBufs b)
   if (E > left) E = left;
   // the previous iteration staged the E best entries of this pool already
   d->skip_select = (d->pre_valid && d->pre_k == E) ? 1u : 0u;
+  if (require_staged && !d->skip_select) d->error = 1;
   d->pre_valid = 0;
   d->pre_k = 0;
   d->pre_count = 0;
@@ -1262,16 +1263,19 @@ static void mark(const cudaEvent_t* marks, int i, cudaStream_t s)
 }
 
 cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval_grid, int sample_grid,
-                             cudaStream_t s, const cudaEvent_t* marks)
+                             cudaStream_t s, const cudaEvent_t* marks, bool with_select)
 {
   const uint64_t max_children = cfg.e_max << cfg.log2C;
   const uint64_t max_pool = cfg.pstride;
   mark(marks, 0, s);
-  begin_kernel<<<1, 1, 0, s>>>(cfg, b);
+  begin_kernel<<<1, 1, 0, s>>>(cfg, b, with_select ? 0 : 1);
 
-  // (1) select the E best parents and stage them
-  radix_select(cfg, b, 0, cfg.cap, s);
-  gather_parents_kernel<<<tiles(cfg.cap), kScanBlock, 0, s>>>(cfg, b, b.block_offsets);
+  // (1) select the E best parents and stage them (after the first
+  // iteration, the previous one staged them)
+  if (with_select) {
+    radix_select(cfg, b, 0, cfg.cap, s);
+    gather_parents_kernel<<<tiles(cfg.cap), kScanBlock, 0, s>>>(cfg, b, b.block_offsets);
+  }
 
   // (2) branch
   {

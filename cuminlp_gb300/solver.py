@@ -255,6 +255,13 @@ class Solver:
             check(lib().cmn_solver_frontier(self.handle, A.ptr(boxes), A.ptr(lb), A.ptr(depth), m, C.byref(cnt)))
         return boxes, lb, depth
 
+    def phase_ms(self) -> list[float]:
+        """[select+branch, bound, sample, prune+rebuild, whole] device ms of the
+        last iteration, from events recorded inside its graph."""
+        ms = (C.c_double * 5)()
+        check(lib().cmn_solver_phase_ms(self.handle, ms))
+        return list(ms)
+
     @property
     def stream(self) -> int:
         return lib().cmn_solver_stream(self.handle) or 0

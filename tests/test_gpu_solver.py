@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 
 import oracle as O
+from cuminlp_gb300 import _abi as A
 from cuminlp_gb300 import generators as G
 from cuminlp_gb300 import report
 from cuminlp_gb300.solver import DeviceProblem, Solver
@@ -80,6 +81,26 @@ def test_solver_matches_oracle_larger(precision):
 def test_eviction_matches_oracle():
     g = compare(G.config1(1), 25, bisection_budget=3, batch_parents=128, frontier_cap=300)
     assert g["counters"]["dropped_viable"] + g["counters"]["dropped_dominated"] > 0
+
+
+def tied_model():
+    # the objective depends on x0 alone, so every child split on x1..x3 has
+    # its parent's lower bound: long runs of equal keys, and the selects of
+    # both the cap and the next parents end inside a bucket of ties that
+    # only pool position orders
+    from cuminlp_gb300.problem import Problem
+    p = Problem()
+    v = [p.var(-1.0, 1.0) for _ in range(4)]
+    p.set_objective(v[0] * v[0] - v[0])
+    p.add_constraint(v[1] * v[2] + v[3], A.CMP_LE, 1.5)
+    return p
+
+
+@pytest.mark.parametrize("cap", [97, 1000])
+def test_tied_lower_bounds_rank_by_position(cap):
+    g = compare(tied_model(), 14, bisection_budget=2, batch_parents=40, frontier_cap=cap, sample_points=1)
+    if cap == 97:
+        assert g["counters"]["dropped_viable"] + g["counters"]["dropped_dominated"] > 0
 
 
 def test_fp32_screen_identical_certified_bounds():

@@ -30,7 +30,7 @@ NVCC_FLAGS = [
     "--expt-relaxed-constexpr", "-DNDEBUG",
 ]
 SOURCES = ["program.cpp", "eval_kernels.cu", "search_kernels.cu", "batch_kernels.cu", "capi.cu", "batch.cu",
-           "server.cpp", "noalloc.cu"]
+           "server.cpp", "noalloc.cu", "emu_check.cu"]
 
 
 def _nvcc() -> str:

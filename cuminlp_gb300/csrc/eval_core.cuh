@@ -14,6 +14,7 @@
 
 #include <cstdint>
 
+#include "fp64_emu.cuh"
 #include "kernels.cuh"
 #include "program.h"
 
@@ -27,21 +28,45 @@ struct Iv {
 template <typename T>
 struct Arith;
 
+// Which FP64 operations run on the integer pipe (fp64_emu.cuh) instead of
+// the FP64 pipe, so that the two pipes share the work (both give the IEEE
+// result bit for bit): bit 0 interval add and subtract rounded up, bit 1
+// interval multiply rounded up, bit 2 interval multiply rounded down,
+// bit 3 point multiply (round to nearest).
+#ifndef CMN_FP64_EMU
+#define CMN_FP64_EMU 2
+#endif
+
 template <>
 struct Arith<double> {
   static __device__ __forceinline__ double add_rd(double a, double b) { return __dadd_rd(a, b); }
-  static __device__ __forceinline__ double add_ru(double a, double b) { return __dadd_ru(a, b); }
+  static __device__ __forceinline__ double add_ru(double a, double b)
+  {
+    return (CMN_FP64_EMU & 1) ? emu::add_ru(a, b) : __dadd_ru(a, b);
+  }
   static __device__ __forceinline__ double sub_rd(double a, double b) { return __dsub_rd(a, b); }
-  static __device__ __forceinline__ double sub_ru(double a, double b) { return __dsub_ru(a, b); }
-  static __device__ __forceinline__ double mul_rd(double a, double b) { return __dmul_rd(a, b); }
-  static __device__ __forceinline__ double mul_ru(double a, double b) { return __dmul_ru(a, b); }
+  static __device__ __forceinline__ double sub_ru(double a, double b)
+  {
+    return (CMN_FP64_EMU & 1) ? emu::sub_ru(a, b) : __dsub_ru(a, b);
+  }
+  static __device__ __forceinline__ double mul_rd(double a, double b)
+  {
+    return (CMN_FP64_EMU & 4) ? emu::mul_rd(a, b) : __dmul_rd(a, b);
+  }
+  static __device__ __forceinline__ double mul_ru(double a, double b)
+  {
+    return (CMN_FP64_EMU & 2) ? emu::mul_ru(a, b) : __dmul_ru(a, b);
+  }
   static __device__ __forceinline__ double div_rd(double a, double b) { return __ddiv_rd(a, b); }
   static __device__ __forceinline__ double div_ru(double a, double b) { return __ddiv_ru(a, b); }
   static __device__ __forceinline__ double sqrt_rd(double a) { return __dsqrt_rd(a); }
   static __device__ __forceinline__ double sqrt_ru(double a) { return __dsqrt_ru(a); }
   static __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
   static __device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
-  static __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+  static __device__ __forceinline__ double mul_rn(double a, double b)
+  {
+    return (CMN_FP64_EMU & 8) ? emu::mul_rn(a, b) : __dmul_rn(a, b);
+  }
   static __device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
   static __device__ __forceinline__ double sqrt_rn(double a) { return __dsqrt_rn(a); }
   // sign bit set (negative, -0 or negative NaN)

@@ -269,7 +269,7 @@ __device__ __forceinline__ void eval_children(const EvalArgs& a, const S* plo, c
 }
 
 template <typename T, int kMode>
-__global__ void __launch_bounds__(kEvalThreads, 4) eval_children_kernel(const EvalArgs a)
+__global__ void __launch_bounds__(kEvalThreads, CMN_EVAL_MIN_BLOCKS) eval_children_kernel(const EvalArgs a)
 {
   if constexpr (sizeof(T) == 4) {
     if (a.plo32 != nullptr) {

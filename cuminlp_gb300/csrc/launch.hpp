@@ -11,6 +11,12 @@
 namespace cmn {
 
 constexpr int kEvalThreads = 128;
+// resident blocks per SM the single-instance bound kernels are compiled
+// for (registers): 5 measured ahead of 4 and 6 on the n=32 and n=4
+// workloads, with a little spilling
+#ifndef CMN_EVAL_MIN_BLOCKS
+#define CMN_EVAL_MIN_BLOCKS 5
+#endif
 
 // interval kernels: program slots plus `max_slots` split variables per thread
 size_t eval_smem_bytes(int n_slots, int max_slots, bool fp32, int threads);

@@ -450,6 +450,15 @@ uint64_t cmn_solver_kernels_per_iteration(const cmn_solver* solver);
  * search path. */
 cmn_status cmn_measure_fma_peak(int32_t precision, double* tflops);
 
+/* Self-test of the integer-pipe binary64 add / subtract / multiply with
+ * directed rounding, and multiply rounded to nearest, against the device's
+ * FP64 instructions, over `n`
+ * operand pairs of one family (0: any bits, 1: close exponents, 2:
+ * cancellation, 3: range edges, 4: runs of ones and zeros) from `seed`.
+ * out3: [0] mismatches, [1] results the integer path produced, [2] results
+ * checked.  Not part of the search path. */
+cmn_status cmn_fp64_emu_check(uint64_t n, uint64_t seed, int32_t family, uint64_t* out3);
+
 /* One-call solve: create, run to a stop condition, report, destroy. */
 cmn_status cmn_solve(const cmn_problem* problem,
                      const cmn_solve_options* opts, cmn_outcome* outcome,

@@ -547,8 +547,11 @@ def run_ours(args):
             "achieved": achieved, "peak": peak64, "unit": "TFLOP/s", "frac": achieved / peak64,
             "peak_source": "measured by cmn_measure_fma_peak (DFMA loop, all SMs) in this run",
             # directed rounding forbids FMA: one flop per FP64 instruction, so
-            # the pipe's ceiling for this arithmetic is half the DFMA flop rate
+            # the pipe's ceiling for this arithmetic is half the DFMA flop rate;
+            # the round-up half of each interval product runs on the integer
+            # pipe instead, which is how the fraction passes 1
             "frac_of_fp64_instruction_ceiling": achieved / (peak64 / 2),
+            "integer_pipe_ops": "interval multiply rounded up (csrc/fp64_emu.cuh)",
             "flops_per_box": fpb, "boxes_per_launch": nb / len(plain["phases"]),
             "traffic": traffic,
             "hbm": {"achieved": hbm_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": hbm_gbs / hbm_peak,

@@ -31,10 +31,12 @@ struct Arith;
 // Which FP64 operations run on the integer pipe (fp64_emu.cuh) instead of
 // the FP64 pipe, so that the two pipes share the work (both give the IEEE
 // result bit for bit): bit 0 interval add and subtract rounded up, bit 1
-// interval multiply rounded up, bit 2 interval multiply rounded down,
-// bit 3 point multiply (round to nearest).
+// interval products rounded up outside the fused terms, bit 2 interval
+// multiply rounded down, bits 3 and 4 the point evaluation's variable and
+// coefficient products (round to nearest), bits 5 and 6 the fused terms'
+// variable and coefficient interval products rounded up.
 #ifndef CMN_FP64_EMU
-#define CMN_FP64_EMU 2
+#define CMN_FP64_EMU (2 | 8 | 32 | 64)
 #endif
 
 template <>
@@ -53,20 +55,14 @@ struct Arith<double> {
   {
     return (CMN_FP64_EMU & 4) ? emu::mul_rd(a, b) : __dmul_rd(a, b);
   }
-  static __device__ __forceinline__ double mul_ru(double a, double b)
-  {
-    return (CMN_FP64_EMU & 2) ? emu::mul_ru(a, b) : __dmul_ru(a, b);
-  }
+  static __device__ __forceinline__ double mul_ru(double a, double b) { return __dmul_ru(a, b); }
   static __device__ __forceinline__ double div_rd(double a, double b) { return __ddiv_rd(a, b); }
   static __device__ __forceinline__ double div_ru(double a, double b) { return __ddiv_ru(a, b); }
   static __device__ __forceinline__ double sqrt_rd(double a) { return __dsqrt_rd(a); }
   static __device__ __forceinline__ double sqrt_ru(double a) { return __dsqrt_ru(a); }
   static __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
   static __device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
-  static __device__ __forceinline__ double mul_rn(double a, double b)
-  {
-    return (CMN_FP64_EMU & 8) ? emu::mul_rn(a, b) : __dmul_rn(a, b);
-  }
+  static __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
   static __device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
   static __device__ __forceinline__ double sqrt_rn(double a) { return __dsqrt_rn(a); }
   // sign bit set (negative, -0 or negative NaN)
@@ -125,6 +121,17 @@ __device__ __forceinline__ T emul_ru(T x, T y)
   using A = Arith<T>;
   return (A::is_zero(x) | A::is_zero(y)) ? T(0) : A::mul_ru(x, y);
 }
+// emul_ru with the product on the integer pipe when kInt (FP64 only)
+template <typename T, bool kInt>
+__device__ __forceinline__ T emul_ru_sel(T x, T y)
+{
+  if constexpr (kInt && sizeof(T) == 8) {
+    using A = Arith<T>;
+    return (A::is_zero(x) | A::is_zero(y)) ? T(0) : emu::mul_ru(x, y);
+  } else {
+    return emul_ru(x, y);
+  }
+}
 
 template <typename T>
 __device__ __forceinline__ Iv<T> iv_add(Iv<T> a, Iv<T> b)
@@ -147,7 +154,7 @@ __device__ __forceinline__ Iv<T> iv_neg(Iv<T> a)
 // Tightest product.  Sign classes: pos (lo has no sign bit), neg (hi has
 // the sign bit), mixed otherwise.  A zero endpoint may land in either
 // class; the chosen corner products then differ only in the sign of a zero.
-template <typename T>
+template <typename T, bool kIntUp = (CMN_FP64_EMU & 2) != 0>
 __device__ __forceinline__ Iv<T> iv_mul(Iv<T> a, Iv<T> b)
 {
   using A = Arith<T>;
@@ -158,11 +165,11 @@ __device__ __forceinline__ Iv<T> iv_mul(Iv<T> a, Iv<T> b)
   const T lb = ap ? b.lo : (an ? b.hi : (bn ? b.lo : b.hi));
   const T ua = ap ? (bn ? a.lo : a.hi) : (an ? (bp ? a.hi : a.lo) : (bn ? a.lo : a.hi));
   const T ub = ap ? b.hi : (an ? b.lo : (bn ? b.lo : b.hi));
-  Iv<T> r = {emul_rd(la, lb), emul_ru(ua, ub)};
+  Iv<T> r = {emul_rd(la, lb), emul_ru_sel<T, kIntUp>(ua, ub)};
   const bool mm = am && bm;
   if (__any_sync(__activemask(), mm)) {
     const T l2 = emul_rd(a.hi, b.lo);
-    const T u2 = emul_ru(a.lo, b.lo);
+    const T u2 = emul_ru_sel<T, kIntUp>(a.lo, b.lo);
     if (mm) {
       r.lo = l2 < r.lo ? l2 : r.lo;
       r.hi = u2 > r.hi ? u2 : r.hi;
@@ -171,7 +178,7 @@ __device__ __forceinline__ Iv<T> iv_mul(Iv<T> a, Iv<T> b)
   return r;
 }
 
-template <typename T>
+template <typename T, bool kIntUp = (CMN_FP64_EMU & 2) != 0>
 __device__ __forceinline__ Iv<T> iv_sqr(Iv<T> a)
 {
   using A = Arith<T>;
@@ -180,7 +187,7 @@ __device__ __forceinline__ Iv<T> iv_sqr(Iv<T> a)
   const T mag = A::gt_nonneg(mlo, a.hi) ? mlo : a.hi;  // mixed: both >= 0
   const T lo_op = p ? a.lo : (n ? a.hi : T(0));
   const T hi_op = p ? a.hi : (n ? a.lo : mag);
-  return {emul_rd(lo_op, lo_op), emul_ru(hi_op, hi_op)};
+  return {emul_rd(lo_op, lo_op), emul_ru_sel<T, kIntUp>(hi_op, hi_op)};
 }
 
 template <typename T>
@@ -450,13 +457,13 @@ __device__ __forceinline__ void interval_range(const Instr* __restrict__ prog, i
         Iv<T> p;
         const int pk = sub & kTermPMask;
         if (pk == kTermProd) {
-          p = iv_mul(vars.var(cur.a), vars.var(cur.b));
+          p = iv_mul<T, (CMN_FP64_EMU & 32) != 0>(vars.var(cur.a), vars.var(cur.b));
         } else if (pk == kTermSqr) {
-          p = iv_sqr(vars.var(cur.a));
+          p = iv_sqr<T, (CMN_FP64_EMU & 32) != 0>(vars.var(cur.a));
         } else {
           p = vars.var(cur.a);
         }
-        if (sub & kTermHasC) p = iv_mul(const_of<T>(cur), p);
+        if (sub & kTermHasC) p = iv_mul<T, (CMN_FP64_EMU & 64) != 0>(const_of<T>(cur), p);
         if (sub & kTermInit) acc = p;
         else if (sub & kTermSub) acc = iv_sub(acc, p);
         else acc = iv_add(acc, p);
@@ -607,6 +614,18 @@ __device__ __forceinline__ double pfetch(const Tile<double>& t, double acc, cons
   }
 }
 
+// the point evaluation's products (round to nearest), on the integer pipe
+// as CMN_FP64_EMU selects: bit 3 the variable products, bit 4 the products
+// by a coefficient
+__device__ __forceinline__ double pt_mul_var(double a, double b)
+{
+  return (CMN_FP64_EMU & 8) ? emu::mul_rn(a, b) : __dmul_rn(a, b);
+}
+__device__ __forceinline__ double pt_mul_const(double c, double p)
+{
+  return (CMN_FP64_EMU & 16) ? emu::mul_rn(c, p) : __dmul_rn(c, p);
+}
+
 __device__ __forceinline__ void point_range(const Instr* __restrict__ prog, int pc0, int pc1, const Tile<double>& t,
                                             PointVerdict& out)
 {
@@ -624,13 +643,13 @@ __device__ __forceinline__ void point_range(const Instr* __restrict__ prog, int 
         const int pk = sub & kTermPMask;
         const double xa = t.lo[cur.a * t.stride + t.tid];
         if (pk == kTermProd) {
-          p = A::mul_rn(xa, t.lo[cur.b * t.stride + t.tid]);
+          p = pt_mul_var(xa, t.lo[cur.b * t.stride + t.tid]);
         } else if (pk == kTermSqr) {
-          p = A::mul_rn(xa, xa);
+          p = pt_mul_var(xa, xa);
         } else {
           p = xa;
         }
-        if (sub & kTermHasC) p = A::mul_rn(cur.c, p);
+        if (sub & kTermHasC) p = pt_mul_const(cur.c, p);
         if (sub & kTermInit) acc = p;
         else if (sub & kTermSub) acc = A::sub_rn(acc, p);
         else acc = A::add_rn(acc, p);

@@ -377,6 +377,9 @@ SERVE_OPTS = dict(bisection_budget=4, batch_parents=64, frontier_cap=2048, sampl
 SERVE_BUDGET = 120 * (1 << 30)
 SERVE_ITER_LIMIT = 64 * 32  # expansions per request: at most 32 full iterations
 SERVE_RUNS = ((100, 300), (1000, 1500), (10000, 6000))  # (arrivals per second, requests)
+# time to the 1e-6 gap: a longer budget per request (512 full iterations),
+# at the lowest rate
+SERVE_TTG = (100, 120, 64 * 512)
 
 
 def serving_workload() -> str:
@@ -406,13 +409,22 @@ def serving_run(rate, n_requests, dps, seed=11, iter_limit=SERVE_ITER_LIMIT):
     outs = [srv.wait(r, timeout_ms=600000) for r in ids]
     st = srv.stats()
     srv.close()
-    conv = [o["elapsed_ms"] for o in outs if o["stop_reason"] == "converged"]
-    conv.sort()
-    pick = (lambda q: conv[min(len(conv) - 1, max(0, int(np.ceil(q * len(conv))) - 1))]) if conv else (lambda q: None)
-    return {"rate_per_s": rate, "requests": n_requests, "latency_p50_ms": st["latency_p50_ms"],
+    # time to gap: requests whose 1e-6 gap was proven (the pool may also
+    # empty with a dropped floor, which stops a request without a proof)
+    proven = sorted(o["elapsed_ms"] for o in outs if o["proven_optimal"])
+    pick = (lambda q: proven[min(len(proven) - 1, max(0, int(np.ceil(q * len(proven))) - 1))]) if proven \
+        else (lambda q: None)
+    by_n = {}
+    for i, o in enumerate(outs):
+        n = int(dps[i % len(dps)].n_vars)
+        e = by_n.setdefault(str(n), {"requests": 0, "proven": 0})
+        e["requests"] += 1
+        e["proven"] += int(bool(o["proven_optimal"]))
+    return {"rate_per_s": rate, "requests": n_requests, "iter_limit_expansions": iter_limit,
+            "latency_p50_ms": st["latency_p50_ms"],
             "latency_p99_ms": st["latency_p99_ms"], "latency_max_ms": st["latency_max_ms"],
-            "queue_p99_ms": st["queue_p99_ms"], "converged": st["converged"],
-            "time_to_gap_p50_ms": pick(0.5), "time_to_gap_p99_ms": pick(0.99),
+            "queue_p99_ms": st["queue_p99_ms"], "converged": st["converged"], "proven": len(proven),
+            "proven_by_n": by_n, "time_to_gap_p50_ms": pick(0.5), "time_to_gap_p99_ms": pick(0.99),
             "boxes_per_s": st["boxes_per_s"], "wall_ms": st["wall_ms"],
             "pool_bytes_peak": st["pool_bytes_peak"], "rounds": st["rounds"]}
 
@@ -435,7 +447,8 @@ def run_ours(args):
     if args.only == "serve":
         from cuminlp_gb300.solver import DeviceProblem
         dps = [DeviceProblem(G.config5_request(i)) for i in range(400)]
-        print(json.dumps({"workload": serving_workload(), "runs": [serving_run(r, n, dps) for r, n in SERVE_RUNS]}))
+        print(json.dumps({"workload": serving_workload(), "runs": [serving_run(r, n, dps) for r, n in SERVE_RUNS],
+                          "time_to_gap_run": serving_run(SERVE_TTG[0], SERVE_TTG[1], dps, iter_limit=SERVE_TTG[2])}))
         return
     problem = G.config2(rank)  # replicas: one independent instance per GPU
     dp = DeviceProblem(problem)
@@ -506,7 +519,8 @@ def run_ours(args):
         from cuminlp_gb300 import generators as G
         from cuminlp_gb300.solver import DeviceProblem
         dps = [DeviceProblem(G.config5_request(i)) for i in range(400)]
-        serving = {"workload": serving_workload(), "runs": [serving_run(r, n, dps) for r, n in SERVE_RUNS]}
+        serving = {"workload": serving_workload(), "runs": [serving_run(r, n, dps) for r, n in SERVE_RUNS],
+                   "time_to_gap_run": serving_run(SERVE_TTG[0], SERVE_TTG[1], dps, iter_limit=SERVE_TTG[2])}
 
     kpi = screen["kernels_per_iter"]
     line = {

@@ -178,6 +178,25 @@ __device__ __forceinline__ Iv<T> iv_mul(Iv<T> a, Iv<T> b)
   return r;
 }
 
+// iv_mul(c, p) for a coefficient interval c: when c's two ends carry the
+// same sign bit (always in FP64, where c is a point), iv_mul's corner
+// choice depends on the sign bits of c and of one end of p only, so the
+// same two products come out with fewer selects. A coefficient pair that
+// straddles a sign change takes iv_mul itself.
+template <typename T, bool kIntUp = (CMN_FP64_EMU & 2) != 0>
+__device__ __forceinline__ Iv<T> iv_scale(Iv<T> c, Iv<T> p)
+{
+  using A = Arith<T>;
+  const bool cp = !A::sgn(c.lo), cn = A::sgn(c.hi);
+  if (cp) {  // c >= 0, iv_mul's class "pos" for a
+    return {emul_rd(A::sgn(p.lo) ? c.hi : c.lo, p.lo), emul_ru_sel<T, kIntUp>(A::sgn(p.hi) ? c.lo : c.hi, p.hi)};
+  }
+  if (cn) {  // c <= 0, class "neg"
+    return {emul_rd(A::sgn(p.hi) ? c.hi : c.lo, p.hi), emul_ru_sel<T, kIntUp>(A::sgn(p.lo) ? c.lo : c.hi, p.lo)};
+  }
+  return iv_mul<T, kIntUp>(c, p);
+}
+
 template <typename T, bool kIntUp = (CMN_FP64_EMU & 2) != 0>
 __device__ __forceinline__ Iv<T> iv_sqr(Iv<T> a)
 {
@@ -463,7 +482,7 @@ __device__ __forceinline__ void interval_range(const Instr* __restrict__ prog, i
         } else {
           p = vars.var(cur.a);
         }
-        if (sub & kTermHasC) p = iv_mul<T, (CMN_FP64_EMU & 64) != 0>(const_of<T>(cur), p);
+        if (sub & kTermHasC) p = iv_scale<T, (CMN_FP64_EMU & 64) != 0>(const_of<T>(cur), p);
         if (sub & kTermInit) acc = p;
         else if (sub & kTermSub) acc = iv_sub(acc, p);
         else acc = iv_add(acc, p);

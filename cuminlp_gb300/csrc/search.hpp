@@ -117,9 +117,10 @@ struct SolverBufs {
   // the pool in position order (two parities): lower bound and box slot
   double* lb[2];
   uint32_t* slot[2];
-  // box store: planes [v * pstride + slot] and depth [slot]. A box keeps its
-  // slot from its append until it is expanded or evicted, so rebuilding the
-  // pool moves 12 bytes per entry instead of the whole box.
+  // box store: boxes slot-major, [slot * n_vars + v], and depth [slot]. A box
+  // keeps its slot from its append until it is expanded or evicted, so
+  // rebuilding the pool moves 12 bytes per entry instead of the whole box;
+  // slot-major keeps the one write of a box and its one read contiguous.
   double* lo;
   double* hi;
   uint32_t* depth;

@@ -38,8 +38,8 @@ __global__ void init_kernel(const SolverCfg cfg, const SolverBufs b, const doubl
 {
   const int t = threadIdx.x + blockIdx.x * blockDim.x;
   for (int v = t; v < cfg.n_vars; v += blockDim.x * gridDim.x) {  // the root box in store slot 0
-    b.lo[(uint64_t)v * cfg.pstride] = root_lb[v];
-    b.hi[(uint64_t)v * cfg.pstride] = root_ub[v];
+    b.lo[v] = root_lb[v];
+    b.hi[v] = root_ub[v];
   }
   if (t == 0) {
     SolverDev* d = b.dev;
@@ -780,8 +780,8 @@ __device__ __forceinline__ void stage_parent(const SolverCfg& cfg, const SolverB
     return;
   }
   for (int v = 0; v < cfg.n_vars; ++v) {
-    const double lo = b.lo[(uint64_t)v * cfg.pstride + s];
-    const double hi = b.hi[(uint64_t)v * cfg.pstride + s];
+    const double lo = b.lo[s * (uint64_t)cfg.n_vars + v];
+    const double hi = b.hi[s * (uint64_t)cfg.n_vars + v];
     b.plo[(uint64_t)v * cfg.e_max + pos] = lo;
     b.phi[(uint64_t)v * cfg.e_max + pos] = hi;
     if (b.plo32 != nullptr) {
@@ -808,8 +808,8 @@ struct AppendChild {
     const uint64_t at = d->pool_size + pos;
     const uint64_t k = g >> cfg.log2C, r = g & ((1ULL << cfg.log2C) - 1ULL);
     for (int v = 0; v < cfg.n_vars; ++v) {
-      b.lo[(uint64_t)v * cfg.pstride + s] = b.plo[(uint64_t)v * cfg.e_max + k];
-      b.hi[(uint64_t)v * cfg.pstride + s] = b.phi[(uint64_t)v * cfg.e_max + k];
+      b.lo[s * (uint64_t)cfg.n_vars + v] = b.plo[(uint64_t)v * cfg.e_max + k];
+      b.hi[s * (uint64_t)cfg.n_vars + v] = b.phi[(uint64_t)v * cfg.e_max + k];
     }
     const ParentInfo pi = b.pinfo[k];
     const SlotPlan* sp = b.slots + k * (uint64_t)cfg.max_slots;
@@ -818,8 +818,8 @@ struct AppendChild {
       const uint64_t part = slot_part(r, sj);
       double lo, hi;
       slot_bounds(sj, b.plo[(uint64_t)sj.vid * cfg.e_max + k], b.phi[(uint64_t)sj.vid * cfg.e_max + k], part, lo, hi);
-      b.lo[(uint64_t)sj.vid * cfg.pstride + s] = lo;
-      b.hi[(uint64_t)sj.vid * cfg.pstride + s] = hi;
+      b.lo[s * (uint64_t)cfg.n_vars + sj.vid] = lo;
+      b.hi[s * (uint64_t)cfg.n_vars + sj.vid] = hi;
     }
     b.depth[s] = b.pdepth[k] + 1;
     const uint32_t p = d->parity;
@@ -988,6 +988,18 @@ __global__ void stage_next_kernel(const SolverCfg cfg, const SolverBufs b)
     stage_parent(cfg, b, b.pslot[k], k);
 }
 
+// appends the kept children listed (in order) by the compaction, one thread
+// per child so that each child's chain of dependent loads runs in parallel
+__global__ void append_children_kernel(const SolverCfg cfg, const SolverBufs b)
+{
+  const SolverDev* d = b.dev;
+  if (d->done) return;
+  const uint64_t n = d->kept;
+  const AppendChild op{cfg, b};
+  for (uint64_t pos = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; pos < n; pos += (uint64_t)gridDim.x * blockDim.x)
+    op(b.list[pos], pos);
+}
+
 // pool entries [start, start + count) in position order, unpacked from the
 // store
 __global__ void frontier_gather_kernel(const SolverCfg cfg, const SolverBufs b, uint64_t start, uint64_t count,
@@ -1000,8 +1012,8 @@ __global__ void frontier_gather_kernel(const SolverCfg cfg, const SolverBufs b, 
     const uint64_t s = slot[start + i];
     if (boxes)
       for (int v = 0; v < n; ++v) {
-        boxes[(i * n + v) * 2] = b.lo[(uint64_t)v * cfg.pstride + s];
-        boxes[(i * n + v) * 2 + 1] = b.hi[(uint64_t)v * cfg.pstride + s];
+        boxes[(i * n + v) * 2] = b.lo[s * (uint64_t)cfg.n_vars + v];
+        boxes[(i * n + v) * 2 + 1] = b.hi[s * (uint64_t)cfg.n_vars + v];
       }
     if (depths) depths[i] = b.depth[s];
   }
@@ -1386,7 +1398,11 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
   // parents stay there as holes until the one compaction below
   KeptChild kept{b};
   compact(kept, max_children, &b.dev->n_children, &b.dev->kept, b, s);
-  scatter(kept, AppendChild{cfg, b}, max_children, s, b);
+  scatter(kept, ListChild{b}, max_children, s, b);
+  {
+    const int grid = (int)std::min<uint64_t>((max_children + 255) / 256, 4096);
+    append_children_kernel<<<grid, 256, 0, s>>>(cfg, b);
+  }
   size_kernel<<<1, 1, 0, s>>>(cfg, b);
 
   // (6) over the cap: keep the `cap` best alive entries, fold the rest into

@@ -525,15 +525,17 @@ __device__ __forceinline__ uint64_t block_min(uint64_t m)
   return acc;
 }
 
-// Exclusive scan of `nblocks` block counts (one block of 1024 threads);
-// writes the total to *total_out (plus `total_bias`).
-__global__ void scan_kernel(const uint32_t* __restrict__ counts, uint32_t* __restrict__ offsets,
-                            const uint64_t* __restrict__ n_items, uint64_t* __restrict__ total_out,
-                            const uint32_t* __restrict__ active, const uint32_t* __restrict__ skip,
-                            const uint32_t* __restrict__ done)
+// Exclusive scan of the tile counts of `*n_items` items (one block of 1024
+// threads); writes the total to *total_out when given.
+__global__ void __launch_bounds__(1024) scan_kernel(const uint32_t* __restrict__ counts,
+                                                    uint32_t* __restrict__ offsets,
+                                                    const uint64_t* __restrict__ n_items,
+                                                    uint64_t* __restrict__ total_out,
+                                                    const uint32_t* __restrict__ active,
+                                                    const uint32_t* __restrict__ skip,
+                                                    const uint32_t* __restrict__ done)
 {
-  __shared__ uint32_t warp_sum[32];
-  __shared__ uint64_t carry_s;
+  __shared__ uint64_t warp_sum[32];
   if (*done || (skip && *skip)) return;
   if (active && !*active) {
     if (threadIdx.x == 0 && total_out) *total_out = 0;
@@ -541,36 +543,37 @@ __global__ void scan_kernel(const uint32_t* __restrict__ counts, uint32_t* __res
   }
   const uint64_t n = *n_items;
   const uint64_t nblocks = (n + kScanTile - 1) / kScanTile;
-  if (threadIdx.x == 0) carry_s = 0;
-  __syncthreads();
+  // each thread sums a run of consecutive counts, the block scans the sums
+  // once, and each thread writes its run's offsets: one pass, two barriers
+  const uint32_t* src = counts;
+  const uint64_t per = (nblocks + blockDim.x - 1) / blockDim.x;
+  const uint64_t b0 = (uint64_t)threadIdx.x * per;
+  const uint64_t b1 = b0 + per < nblocks ? b0 + per : nblocks;
+  uint64_t sum = 0;
+  for (uint64_t i = b0; i < b1; ++i) sum += src[i];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (uint64_t base = 0; base < nblocks; base += blockDim.x) {
-    const uint64_t i = base + threadIdx.x;
-    const uint32_t v = i < nblocks ? counts[i] : 0;
-    uint32_t x = v;
-    for (int off = 1; off < 32; off <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
-      if (lane >= off) x += y;
-    }
-    if (lane == 31) warp_sum[wid] = x;
-    __syncthreads();
-    if (wid == 0) {
-      uint32_t s = lane < (int)(blockDim.x / 32) ? warp_sum[lane] : 0;
-      for (int off = 1; off < 32; off <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, s, off);
-        if (lane >= off) s += y;
-      }
-      warp_sum[lane] = s;  // inclusive
-    }
-    __syncthreads();
-    const uint64_t carry = carry_s;
-    const uint32_t warp_before = wid > 0 ? warp_sum[wid - 1] : 0;
-    if (i < nblocks) offsets[i] = (uint32_t)(carry + warp_before + x - v);
-    __syncthreads();
-    if (threadIdx.x == blockDim.x - 1) carry_s = carry + warp_sum[blockDim.x / 32 - 1];
-    __syncthreads();
+  uint64_t x = sum;
+  for (int off = 1; off < 32; off <<= 1) {
+    const uint64_t y = __shfl_up_sync(0xffffffffu, x, off);
+    if (lane >= off) x += y;
   }
-  if (threadIdx.x == 0 && total_out) *total_out = carry_s;
+  if (lane == 31) warp_sum[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    uint64_t w = lane < (int)(blockDim.x / 32) ? warp_sum[lane] : 0;
+    for (int off = 1; off < 32; off <<= 1) {
+      const uint64_t y = __shfl_up_sync(0xffffffffu, w, off);
+      if (lane >= off) w += y;
+    }
+    warp_sum[lane] = w;  // inclusive
+  }
+  __syncthreads();
+  uint64_t run = x - sum + (wid > 0 ? warp_sum[wid - 1] : 0);
+  if (threadIdx.x == blockDim.x - 1 && total_out) *total_out = run + sum;
+  for (uint64_t i = b0; i < b1; ++i) {
+    offsets[i] = (uint32_t)run;
+    run += src[i];
+  }
 }
 
 // ---- predicates / operations -----------------------------------------

@@ -40,8 +40,10 @@ sys.path.insert(0, str(ROOT))
 
 EVAL_DRAM_BYTES_PER_BOX = (43186688 + 34048) / 1048576  # ncu, eval_children_kernel<double, 1>, config 2
 # time-to-gap on config 1: the cluster of boxes within 1e-6 of the optimum
-# holds tens of millions of boxes at n=4, so the frontier is capped at 2^25
-TTG_B, TTG_E, TTG_CAP = 3, 1 << 17, 1 << 25
+# holds tens of millions of boxes at n=4, so the frontier is capped at 2^25;
+# 2^21 parents x 2^2 children per iteration timed best (swept over
+# B in 1..4 and 2^16..2^23 parents)
+TTG_B, TTG_E, TTG_CAP = 2, 1 << 21, 1 << 25
 E_PARENTS = 1 << 16
 B_BITS = 4
 CAP = 1 << 20

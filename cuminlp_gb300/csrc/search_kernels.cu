@@ -1025,6 +1025,10 @@ __global__ void frontier_gather_kernel(const SolverCfg cfg, const SolverBufs b, 
 // ---------------------------------------------------------------------
 // branching: BisectionBudgetCompositionPolicy::choose per parent
 // ---------------------------------------------------------------------
+// kLocal > 0: the policy's per-parent scratch lives in this thread's local
+// memory (n <= kLocal), which the hardware interleaves across the warp and
+// caches in L1; otherwise in the global scratch arrays
+template <int kLocal>
 __global__ void branch_kernel(const SolverCfg cfg, const SolverBufs b)
 {
   const SolverDev* d = b.dev;
@@ -1033,10 +1037,13 @@ __global__ void branch_kernel(const SolverCfg cfg, const SolverBufs b)
   const int n = cfg.n_vars;
   const PolicyParams pp = {cfg.log2C, cfg.max_cycle, cfg.enumerate_cap, cfg.relative};
   uint64_t fathomed = 0, fathomed_points = 0, bounded = 0;
+  EnumCand ec_local[kLocal > 0 ? kLocal : 1];
+  BisCand bc_local[kLocal > 0 ? kLocal : 1];
+  uint64_t heap_local[kLocal > 0 ? kLocal : 1];
   for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < E; k += (uint64_t)gridDim.x * blockDim.x) {
-    EnumCand* ec = reinterpret_cast<EnumCand*>(b.enum_scratch) + k * (uint64_t)n;
-    BisCand* bc = reinterpret_cast<BisCand*>(b.bis_scratch) + k * (uint64_t)n;
-    uint64_t* heap = b.heap_scratch + k * (uint64_t)n;
+    EnumCand* ec = kLocal > 0 ? ec_local : reinterpret_cast<EnumCand*>(b.enum_scratch) + k * (uint64_t)n;
+    BisCand* bc = kLocal > 0 ? bc_local : reinterpret_cast<BisCand*>(b.bis_scratch) + k * (uint64_t)n;
+    uint64_t* heap = kLocal > 0 ? heap_local : b.heap_scratch + k * (uint64_t)n;
     SlotPlan* sp = b.slots + k * (uint64_t)cfg.max_slots;
     const ParentInfo pi = bisection_policy(b.plo + k, b.phi + k, cfg.e_max, n, b.kinds, pp, ec, bc, heap, sp);
     b.pinfo[k] = pi;
@@ -1295,7 +1302,9 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
   // (2) branch
   {
     const int grid = (int)std::min<uint64_t>((cfg.e_max + 127) / 128, 2048);
-    branch_kernel<<<grid, 128, 0, s>>>(cfg, b);
+    if (cfg.n_vars <= 8) branch_kernel<8><<<grid, 128, 0, s>>>(cfg, b);
+    else if (cfg.n_vars <= 32) branch_kernel<32><<<grid, 128, 0, s>>>(cfg, b);
+    else branch_kernel<0><<<grid, 128, 0, s>>>(cfg, b);
   }
   mark(marks, 1, s);
 

@@ -125,9 +125,12 @@ __global__ void begin_kernel(const SolverCfg cfg, const SolverBufs b, int requir
 // ---------------------------------------------------------------------
 // radix select of the k-th smallest lower-bound key
 // ---------------------------------------------------------------------
-// which = 0: the current pool (n = pool_size, k = n_parents)
+// which = 0: the current pool (n = pool_size; one target, k = n_parents),
+//            the first iteration only
 // which = 1: the current buffer after the children were appended behind
-//            the pool (n = extent, k = cap), alive entries only, when evicting
+//            the pool (n = extent), alive entries only; target 0 the cap
+//            (when evicting), target 1 the next iteration's parents
+
 // one of the two pool buffers without indexing the parameter arrays by a
 // runtime value (which would copy them to local memory)
 template <class T>

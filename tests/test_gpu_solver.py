@@ -96,6 +96,15 @@ def tied_model():
     return p
 
 
+@pytest.mark.parametrize("instance", [6, 13, 0])  # n = 11, 36, 44: the three branching scratch kinds
+def test_solver_matches_oracle_wider(instance):
+    # the branching policy keeps its scratch in local memory up to 32
+    # variables and in global scratch above; both against the oracle, with
+    # a cap small enough to evict
+    compare(G.config4_instance(instance), 6, bisection_budget=3, batch_parents=48, frontier_cap=400,
+            sample_points=1)
+
+
 @pytest.mark.parametrize("cap", [97, 1000])
 def test_tied_lower_bounds_rank_by_position(cap):
     g = compare(tied_model(), 14, bisection_budget=2, batch_parents=40, frontier_cap=cap, sample_points=1)

@@ -26,7 +26,7 @@ ORACLE_LIB = ORACLE_DIR / "liboracle.so"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = [
     "-O3", "-std=c++17", ARCH, "-lineinfo", "--fmad=false",
-    "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+    "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "-Xcompiler", "-frounding-math",
     "--expt-relaxed-constexpr", "-DNDEBUG",
 ]
 SOURCES = ["program.cpp", "eval_kernels.cu", "search_kernels.cu", "batch_kernels.cu", "capi.cu", "batch.cu",

@@ -2,14 +2,16 @@
 // (fp64_emu.cuh) against the FP64 instructions they stand in for.
 #include <cuda_runtime.h>
 
+#include <cfenv>
 #include <cstdint>
+#include <cstring>
 
 #include "../../include/cuminlp_gb300.h"
 #include "fp64_emu.cuh"
 
 namespace cmn {
 
-__device__ __forceinline__ uint64_t mix64(uint64_t x)
+__host__ __device__ __forceinline__ uint64_t mix64(uint64_t x)
 {
   x += 0x9e3779b97f4a7c15ULL;
   x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ULL;
@@ -23,7 +25,7 @@ __device__ __forceinline__ uint64_t mix64(uint64_t x)
 //   2: b close to -a (cancellation in a + b, and in a - b for b close to a)
 //   3: exponents near the top and the bottom of the normal range
 //   4: significands with long runs of ones or zeros (carries, exact results)
-__device__ __forceinline__ void operands(int family, uint64_t i, uint64_t seed, uint64_t& a, uint64_t& b)
+__host__ __device__ __forceinline__ void operands(int family, uint64_t i, uint64_t seed, uint64_t& a, uint64_t& b)
 {
   const uint64_t r0 = mix64(seed ^ (i * 4 + 0)), r1 = mix64(seed ^ (i * 4 + 1));
   const uint64_t r2 = mix64(seed ^ (i * 4 + 2)), r3 = mix64(seed ^ (i * 4 + 3));
@@ -71,6 +73,16 @@ __device__ __forceinline__ void operands(int family, uint64_t i, uint64_t seed, 
   }
 }
 
+// the integer path's result of operation `op` (the device check and its host twin)
+__host__ __device__ __forceinline__ bool emu_op(int op, uint64_t a, uint64_t b, uint64_t& r)
+{
+  const bool up = op & 1;
+  return op < 2 ? emu::add_dir(a, b, up, r)
+       : op < 4 ? emu::add_dir(a, b ^ (1ULL << 63), up, r)
+       : op < 6 ? emu::mul_dir(a, b, up, r)
+                : emu::mul_round(a, b, emu::kNearest, r);
+}
+
 // out[0] mismatches, out[1] results taken on the integer path, out[2]
 // results checked
 __global__ void emu_check_kernel(uint64_t n, uint64_t seed, int family, unsigned long long* out)
@@ -84,11 +96,7 @@ __global__ void emu_check_kernel(uint64_t n, uint64_t seed, int family, unsigned
                           __dmul_rd(x, y), __dmul_ru(x, y), __dmul_rn(x, y)};
     for (int op = 0; op < 7; ++op) {
       uint64_t r;
-      const bool up = op & 1;
-      const bool ok = op < 2 ? emu::add_dir(a, b, up, r)
-                    : op < 4 ? emu::add_dir(a, b ^ (1ULL << 63), up, r)
-                    : op < 6 ? emu::mul_dir(a, b, up, r)
-                             : emu::mul_round(a, b, emu::kNearest, r);
+      const bool ok = emu_op(op, a, b, r);
       ++total;
       if (!ok) continue;
       ++handled;
@@ -107,7 +115,54 @@ __global__ void emu_check_kernel(uint64_t n, uint64_t seed, int family, unsigned
   }
 }
 
+// The host FPU's result of operation `op` in its rounding mode. The
+// operands pass through volatile memory so that the arithmetic happens
+// after the mode switch.
+static uint64_t host_op(int op, uint64_t a, uint64_t b)
+{
+  volatile double x, y;
+  double xs, ys;
+  std::memcpy(&xs, &a, 8);
+  std::memcpy(&ys, &b, 8);
+  static const int modes[7] = {FE_DOWNWARD, FE_UPWARD, FE_DOWNWARD, FE_UPWARD, FE_DOWNWARD, FE_UPWARD, FE_TONEAREST};
+  std::fesetround(modes[op]);
+  x = xs;
+  y = ys;
+  volatile double r;
+  if (op < 2) r = x + y;
+  else if (op < 4) r = x - y;
+  else r = x * y;
+  const double out = r;
+  std::fesetround(FE_TONEAREST);
+  uint64_t u;
+  std::memcpy(&u, &out, 8);
+  return u;
+}
+
 }  // namespace cmn
+
+// Host twin of cmn_fp64_emu_check: the same integer path compiled for the
+// host, against the host FPU (IEEE binary64 in each rounding mode).
+extern "C" cmn_status cmn_fp64_emu_check_host(uint64_t n, uint64_t seed, int32_t family, uint64_t* out3)
+{
+  if (!out3 || family < 0 || family > 4) return CMN_INVALID_CONFIGURATION;
+  uint64_t bad = 0, handled = 0, total = 0;
+  for (uint64_t i = 0; i < n; ++i) {
+    uint64_t a, b;
+    cmn::operands(family, i, seed, a, b);
+    for (int op = 0; op < 7; ++op) {
+      uint64_t r;
+      ++total;
+      if (!cmn::emu_op(op, a, b, r)) continue;
+      ++handled;
+      if (r != cmn::host_op(op, a, b)) ++bad;
+    }
+  }
+  out3[0] = bad;
+  out3[1] = handled;
+  out3[2] = total;
+  return CMN_OK;
+}
 
 extern "C" cmn_status cmn_fp64_emu_check(uint64_t n, uint64_t seed, int32_t family, uint64_t* out3)
 {

@@ -17,6 +17,10 @@
 
 #include <cstdint>
 
+// The integer path compiles for the host as well, where a CPU test checks
+// it against the host's FPU in each rounding mode.
+#define CMN_EMU_HD __host__ __device__ __forceinline__
+
 namespace cmn {
 namespace emu {
 
@@ -26,12 +30,30 @@ constexpr uint64_t kAbs = 0x7fffffffffffffffULL;
 __device__ __forceinline__ uint64_t bits(double x) { return (uint64_t)__double_as_longlong(x); }
 __device__ __forceinline__ double from_bits(uint64_t u) { return __longlong_as_double((long long)u); }
 
+CMN_EMU_HD uint64_t umul64hi(uint64_t a, uint64_t b)
+{
+#ifdef __CUDA_ARCH__
+  return __umul64hi(a, b);
+#else
+  return (uint64_t)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+
+CMN_EMU_HD int clz64(uint64_t x)  // x != 0
+{
+#ifdef __CUDA_ARCH__
+  return __clzll((long long)x);
+#else
+  return __builtin_clzll(x);
+#endif
+}
+
 // exponent field in [1, 2046]: a normal number
-__device__ __forceinline__ bool normal_exp(uint32_t e) { return e - 1u < 2046u; }
+CMN_EMU_HD bool normal_exp(uint32_t e) { return e - 1u < 2046u; }
 
 // Packs sign, biased exponent e and significand m in [2^52, 2^53] after
 // rounding; false when the result is not normal.
-__device__ __forceinline__ bool pack(uint32_t sign, int e, uint64_t m, uint64_t& r)
+CMN_EMU_HD bool pack(uint32_t sign, int e, uint64_t m, uint64_t& r)
 {
   if (m >> 53) {  // the increment carried out: m was 2^53 - 1
     m >>= 1;
@@ -46,12 +68,12 @@ __device__ __forceinline__ bool pack(uint32_t sign, int e, uint64_t m, uint64_t&
 enum Round { kDown = 0, kUp = 1, kNearest = 2 };
 
 // a * b rounded in direction `mode`.
-__device__ __forceinline__ bool mul_round(uint64_t a, uint64_t b, int mode, uint64_t& r)
+CMN_EMU_HD bool mul_round(uint64_t a, uint64_t b, int mode, uint64_t& r)
 {
   const uint32_t ea = (uint32_t)(a >> 52) & 0x7ff, eb = (uint32_t)(b >> 52) & 0x7ff;
   if (!normal_exp(ea) || !normal_exp(eb)) return false;
   const uint64_t A = (a & kM52) | (1ULL << 52), B = (b & kM52) | (1ULL << 52);
-  const uint64_t hi = __umul64hi(A, B), lo = A * B;  // the exact product, < 2^106
+  const uint64_t hi = umul64hi(A, B), lo = A * B;  // the exact product, < 2^106
   const uint32_t sign = (uint32_t)((a ^ b) >> 63);
   int e = (int)ea + (int)eb - 1023;
   uint64_t m;
@@ -78,13 +100,13 @@ __device__ __forceinline__ bool mul_round(uint64_t a, uint64_t b, int mode, uint
 }
 
 // a * b rounded toward +inf (up) or -inf (!up).
-__device__ __forceinline__ bool mul_dir(uint64_t a, uint64_t b, bool up, uint64_t& r)
+CMN_EMU_HD bool mul_dir(uint64_t a, uint64_t b, bool up, uint64_t& r)
 {
   return mul_round(a, b, up ? kUp : kDown, r);
 }
 
 // a + b rounded toward +inf (up) or -inf (!up).
-__device__ __forceinline__ bool add_dir(uint64_t a, uint64_t b, bool up, uint64_t& r)
+CMN_EMU_HD bool add_dir(uint64_t a, uint64_t b, bool up, uint64_t& r)
 {
   uint32_t ea = (uint32_t)(a >> 52) & 0x7ff, eb = (uint32_t)(b >> 52) & 0x7ff;
   if (!normal_exp(ea) || !normal_exp(eb)) return false;
@@ -125,7 +147,7 @@ __device__ __forceinline__ bool add_dir(uint64_t a, uint64_t b, bool up, uint64_
     // argument holds (floor(M / 2^9) == floor(floor(M) / 2^9))
     S = A - Bs - (sticky ? 1 : 0);
     if (S == 0) return false;  // exact cancellation: the sign of zero is the instruction's
-    const int L = __clzll((long long)S) - 1;
+    const int L = clz64(S) - 1;
     S <<= L;
     e -= L;
   }

@@ -458,6 +458,9 @@ cmn_status cmn_measure_fma_peak(int32_t precision, double* tflops);
  * out3: [0] mismatches, [1] results the integer path produced, [2] results
  * checked.  Not part of the search path. */
 cmn_status cmn_fp64_emu_check(uint64_t n, uint64_t seed, int32_t family, uint64_t* out3);
+/* The same check with the integer path compiled for the host, against the
+ * host FPU in each rounding mode; needs no GPU. */
+cmn_status cmn_fp64_emu_check_host(uint64_t n, uint64_t seed, int32_t family, uint64_t* out3);
 
 /* One-call solve: create, run to a stop condition, report, destroy. */
 cmn_status cmn_solve(const cmn_problem* problem,

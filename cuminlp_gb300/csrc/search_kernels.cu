@@ -812,24 +812,45 @@ struct AppendChild {
     }
     const uint64_t s = b.free_slots[d->free_top - 1 - pos];
     const uint64_t at = d->pool_size + pos;
+    const uint32_t p = d->parity;
     const uint64_t k = g >> cfg.log2C, r = g & ((1ULL << cfg.log2C) - 1ULL);
-    for (int v = 0; v < cfg.n_vars; ++v) {
-      b.lo[s * (uint64_t)cfg.n_vars + v] = b.plo[(uint64_t)v * cfg.e_max + k];
-      b.hi[s * (uint64_t)cfg.n_vars + v] = b.phi[(uint64_t)v * cfg.e_max + k];
-    }
+    // every load is issued before the stores it does not depend on: the
+    // pointers do not alias, and without that each parent value would wait
+    // for the store before it
+    const double* __restrict__ plo = b.plo;
+    const double* __restrict__ phi = b.phi;
+    double* __restrict__ slo = b.lo + s * (uint64_t)cfg.n_vars;
+    double* __restrict__ shi = b.hi + s * (uint64_t)cfg.n_vars;
     const ParentInfo pi = b.pinfo[k];
+    const double clb = b.clb[g];
+    const uint32_t dep = b.pdepth[k];
+    constexpr int kGroup = 8;
+    for (int v0 = 0; v0 < cfg.n_vars; v0 += kGroup) {
+      double l[kGroup], h[kGroup];
+#pragma unroll
+      for (int u = 0; u < kGroup; ++u)
+        if (v0 + u < cfg.n_vars) {
+          l[u] = plo[(uint64_t)(v0 + u) * cfg.e_max + k];
+          h[u] = phi[(uint64_t)(v0 + u) * cfg.e_max + k];
+        }
+#pragma unroll
+      for (int u = 0; u < kGroup; ++u)
+        if (v0 + u < cfg.n_vars) {
+          slo[v0 + u] = l[u];
+          shi[v0 + u] = h[u];
+        }
+    }
     const SlotPlan* sp = b.slots + k * (uint64_t)cfg.max_slots;
     for (uint32_t j = 0; j < pi.count; ++j) {
       const SlotPlan sj = sp[j];
       const uint64_t part = slot_part(r, sj);
       double lo, hi;
-      slot_bounds(sj, b.plo[(uint64_t)sj.vid * cfg.e_max + k], b.phi[(uint64_t)sj.vid * cfg.e_max + k], part, lo, hi);
-      b.lo[s * (uint64_t)cfg.n_vars + sj.vid] = lo;
-      b.hi[s * (uint64_t)cfg.n_vars + sj.vid] = hi;
+      slot_bounds(sj, plo[(uint64_t)sj.vid * cfg.e_max + k], phi[(uint64_t)sj.vid * cfg.e_max + k], part, lo, hi);
+      slo[sj.vid] = lo;
+      shi[sj.vid] = hi;
     }
-    b.depth[s] = b.pdepth[k] + 1;
-    const uint32_t p = d->parity;
-    parity_buf(b.lb, p)[at] = b.clb[g];
+    b.depth[s] = dep + 1;
+    parity_buf(b.lb, p)[at] = clb;
     parity_buf(b.slot, p)[at] = (uint32_t)s;
     parity_buf(b.sel, p)[at] = kSelAlive;
   }

@@ -785,17 +785,34 @@ __device__ __forceinline__ void stage_parent(const SolverCfg& cfg, const SolverB
     b.dev->error = 1;
     return;
   }
-  for (int v = 0; v < cfg.n_vars; ++v) {
-    const double lo = b.lo[s * (uint64_t)cfg.n_vars + v];
-    const double hi = b.hi[s * (uint64_t)cfg.n_vars + v];
-    b.plo[(uint64_t)v * cfg.e_max + pos] = lo;
-    b.phi[(uint64_t)v * cfg.e_max + pos] = hi;
-    if (b.plo32 != nullptr) {
-      b.plo32[(uint64_t)v * cfg.e_max + pos] = __double2float_rd(lo);
-      b.phi32[(uint64_t)v * cfg.e_max + pos] = __double2float_ru(hi);
-    }
+  // loads in groups ahead of the stores (the pointers do not alias)
+  const double* __restrict__ slo = b.lo + s * (uint64_t)cfg.n_vars;
+  const double* __restrict__ shi = b.hi + s * (uint64_t)cfg.n_vars;
+  double* __restrict__ plo = b.plo;
+  double* __restrict__ phi = b.phi;
+  const uint32_t dep = b.depth[s];
+  constexpr int kGroup = 8;
+  for (int v0 = 0; v0 < cfg.n_vars; v0 += kGroup) {
+    double l[kGroup], h[kGroup];
+#pragma unroll
+    for (int u = 0; u < kGroup; ++u)
+      if (v0 + u < cfg.n_vars) {
+        l[u] = slo[v0 + u];
+        h[u] = shi[v0 + u];
+      }
+#pragma unroll
+    for (int u = 0; u < kGroup; ++u)
+      if (v0 + u < cfg.n_vars) {
+        const uint64_t at = (uint64_t)(v0 + u) * cfg.e_max + pos;
+        plo[at] = l[u];
+        phi[at] = h[u];
+        if (b.plo32 != nullptr) {
+          b.plo32[at] = __double2float_rd(l[u]);
+          b.phi32[at] = __double2float_ru(h[u]);
+        }
+      }
   }
-  b.pdepth[pos] = b.depth[s];
+  b.pdepth[pos] = dep;
 }
 
 // decode a kept child from its parent into a free store slot and append it

@@ -192,6 +192,14 @@ def barrier(dist):
         dist.barrier()
 
 
+def job_rate(dist, units: float, ms: float):
+    """Whole-job rate of independent replicas: the units all ranks processed
+    over the slowest rank's time (each rank times its own steps between
+    barriers). Returns (units per second, max ms over ranks)."""
+    t_max = reduce_max(dist, ms)
+    return reduce_sum(dist, units) / (t_max * 1e-3), t_max
+
+
 # ------------------------------------------------------------- CPU side
 def cpu_rate(problem, seconds: float, threads: int):
     """Box evaluations per second of the oracle (CPU restatement of the
@@ -286,7 +294,7 @@ def fma_peak(precision):
 def e2e_run(dp, problem, steps, warmup):
     import numpy as np
 
-    import oracle as O
+    from cuminlp_gb300.aggregate import bisection_choose
     from cuminlp_gb300.solver import Bounder, Sampler
     root = np.array(problem.box_bounds)
     rng = np.random.default_rng(7)
@@ -300,8 +308,10 @@ def e2e_run(dp, problem, steps, warmup):
         lo[kinds != 0] = np.ceil(lo[kinds != 0])
         hi[kinds != 0] = np.maximum(np.floor(hi[kinds != 0]), lo[kinds != 0])
         boxes.append(np.stack([lo, hi], 1).reshape(-1))
-    # one composition for all steps: the policy's choice on the first box
-    kinds, vids, widths, _ = O.bisection_choose(boxes[0], problem.var_kinds, E2E_B)
+    # one composition for all steps: the library's host policy
+    # (cmn_bisection_choose) on the first box
+    a = bisection_choose(boxes[0], problem.var_kinds, E2E_B)
+    kinds, vids, widths = a.kinds, a.var_ids, a.widths
     N = int(np.prod(widths))
     bounder = Bounder(dp, kinds, N)
     sampler = Sampler(dp, kinds, N, sample_points=1)
@@ -318,7 +328,8 @@ def e2e_run(dp, problem, steps, warmup):
     h2d = 2 * (16 * n + 64 * 40 + 16)  # box planes + slot table, for each of the two role calls
     d2h = N * 9 + 24 + 8 * n
     return {"value": N * len(times) / total, "unit": "boxes/s", "h2d_bytes_per_step": h2d,
-            "d2h_bytes_per_step": d2h, "regions_per_call": N, "ms_per_step": 1e3 * total / len(times)}
+            "d2h_bytes_per_step": d2h, "regions_per_call": N, "ms_per_step": 1e3 * total / len(times),
+            "units": N * len(times), "ms": 1e3 * total}
 
 
 def time_to_gap(problem, precision, limit_s, iters=0):
@@ -468,17 +479,15 @@ def run_ours(args):
 
     screen = res["fp32"]
     plain = res["fp64"]
-    t_max = reduce_max(dist, screen["ms"])
-    boxes = reduce_sum(dist, screen["delta"]["bounded"])
-    value = boxes / (t_max / 1e3)
-    t_plain = reduce_max(dist, plain["ms"])
-    plain_value = reduce_sum(dist, plain["delta"]["bounded"]) / (t_plain / 1e3)
+    value, t_max = job_rate(dist, screen["delta"]["bounded"], screen["ms"])
+    plain_value, t_plain = job_rate(dist, plain["delta"]["bounded"], plain["ms"])
 
     if args.quick:
         print(json.dumps({"quick": True, "fp64_ms": plain["ms"], "fp32_ms": screen["ms"], "boxes/s": value}))
         return
     e2e = e2e_run(dp, problem, args.steps, args.warmup)
-    e2e_all = reduce_sum(dist, e2e["value"])
+    e2e_rank0 = e2e["value"]
+    e2e["value"], _ = job_rate(dist, e2e["units"], e2e["ms"])
 
     if rank != 0:
         barrier(dist)
@@ -579,7 +588,7 @@ def run_ours(args):
                                    f"{cpu_s['steps']} steps in {cpu_s['seconds']} s", "cpu": model},
         "e2e": {k: e2e[k] for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step")},
         "e2e_detail": {"regions_per_call": e2e["regions_per_call"], "ms_per_step": e2e["ms_per_step"],
-                       "all_ranks_value": e2e_all},
+                       "rank0_value": e2e_rank0},
         "gpu_launches": kpi * args.steps,
         "clocks": clocks,
         "time_to_gap": ttg,

@@ -109,3 +109,35 @@ def test_malformed_node_table_is_rejected(lib):
     h = C.c_void_p()
     assert lib.cmn_problem_create(C.byref(d), C.byref(h)) == 1
     assert b"topological" in lib.cmn_last_error()
+
+
+# entry points that start device work from scalar arguments alone
+_DEVICE_WORK = {"cmn_measure_fma_peak", "cmn_fp64_emu_check"}
+
+
+def _is_pointer(t) -> bool:
+    return t is C.c_void_p or (isinstance(t, type) and issubclass(t, C._Pointer))
+
+
+def test_null_handles_are_rejected_without_gpu(lib):
+    """Every entry point that takes a handle or an output pointer answers a
+    null one with INVALID_CONFIGURATION (the reference's
+    InvalidConfiguration) before any device call; counts read 0 and
+    destroy is a no-op."""
+    seen = 0
+    for name, (res, args) in _lib.SIGNATURES.items():
+        if name in _DEVICE_WORK or not args:
+            continue
+        if not _is_pointer(args[0]):
+            continue
+        call = [None if _is_pointer(a) else 0 for a in args]
+        out = getattr(lib, name)(*call)
+        if res is None:
+            continue
+        if res is C.c_int32:
+            assert out == 4, (name, out, lib.cmn_last_error())
+            assert lib.cmn_last_error(), name
+        else:  # counts and stream handles
+            assert not out, (name, out)
+        seen += 1
+    assert seen >= 45, seen

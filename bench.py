@@ -485,6 +485,7 @@ def run_ours(args):
     if args.quick:
         print(json.dumps({"quick": True, "fp64_ms": plain["ms"], "fp32_ms": screen["ms"], "boxes/s": value}))
         return
+    barrier(dist)
     e2e = e2e_run(dp, problem, args.steps, args.warmup)
     e2e_rank0 = e2e["value"]
     e2e["value"], _ = job_rate(dist, e2e["units"], e2e["ms"])

@@ -227,15 +227,31 @@ def cpu_rate(problem, seconds: float, threads: int):
     return done / dt, {"children_per_step": N, "steps": salt - 1, "seconds": round(dt, 2)}
 
 
-def cpu_info():
+# Arm cores by (implementer, part) from /proc/cpuinfo, which has no model
+# name line on aarch64
+ARM_PARTS = {(0x41, 0xD4F): "Arm Neoverse-V2", (0x41, 0xD40): "Arm Neoverse-V1",
+             (0x41, 0xD0C): "Arm Neoverse-N1", (0x41, 0xD49): "Arm Neoverse-N2"}
+
+
+def cpu_info(path: str = "/proc/cpuinfo"):
     model = "unknown"
+    fields = {}
     try:
-        for line in open("/proc/cpuinfo"):
-            if line.lower().startswith(("model name", "cpu model", "hardware")):
-                model = line.split(":", 1)[1].strip()
-                break
+        for line in open(path):
+            key, _, val = line.partition(":")
+            key = key.strip().lower()
+            if key in ("model name", "cpu model", "hardware") and model == "unknown":
+                model = val.strip()
+            elif key in ("cpu implementer", "cpu part") and key not in fields:
+                fields[key] = val.strip()
     except OSError:
         pass
+    if model == "unknown" and len(fields) == 2:
+        try:
+            ip = (int(fields["cpu implementer"], 16), int(fields["cpu part"], 16))
+            model = ARM_PARTS.get(ip, f"arm implementer {ip[0]:#x} part {ip[1]:#x}")
+        except ValueError:
+            pass
     return model, os.cpu_count() or 1
 
 

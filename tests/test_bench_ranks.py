@@ -102,3 +102,22 @@ def test_replicas_are_distinct_instances():
     assert a.n_vars == b.n_vars and len(a.constraints) == len(b.constraints)
     consts = [[n.constant for n in p.graph.nodes] for p in (a, b)]
     assert consts[0] != consts[1]
+
+
+def test_cpu_model_on_x86_and_arm(tmp_path):
+    """The CPU baseline names the host's cores: x86 from its model name
+    line, aarch64 (no such line) from the implementer and part fields."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+    x86 = tmp_path / "x86"
+    x86.write_text("processor\t: 0\nvendor_id\t: GenuineIntel\nmodel name\t: Some Xeon CPU @ 2.00GHz\n")
+    assert bench.cpu_info(str(x86))[0] == "Some Xeon CPU @ 2.00GHz"
+    arm = tmp_path / "arm"
+    arm.write_text("processor\t: 0\nBogoMIPS\t: 2000.00\nCPU implementer\t: 0x41\nCPU architecture: 8\n"
+                   "CPU variant\t: 0x0\nCPU part\t: 0xd4f\nCPU revision\t: 0\n\nprocessor\t: 1\n"
+                   "CPU implementer\t: 0x41\nCPU part\t: 0xd4f\n")
+    assert bench.cpu_info(str(arm))[0] == "Arm Neoverse-V2"
+    other = tmp_path / "other"
+    other.write_text("CPU implementer\t: 0x61\nCPU part\t: 0x123\n")
+    assert bench.cpu_info(str(other))[0] == "arm implementer 0x61 part 0x123"
+    assert bench.cpu_info(str(tmp_path / "missing"))[0] == "unknown"

@@ -62,7 +62,9 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-batch", action="store_true", help="skip the 1024-instance batch (config 4)")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving stream (config 5)")
-    ap.add_argument("--only", choices=["batch", "serve", "ttg"], help="run one of the extra workloads alone")
+    ap.add_argument("--no-screen-check", action="store_true",
+                    help="skip the FP32 screen containment / width-inflation check (config 3)")
+    ap.add_argument("--only", choices=["batch", "serve", "ttg", "screen"], help="run one of the extra workloads alone")
     ap.add_argument("--instances", type=int, default=1024, help="--only batch: instances in the batch")
     ap.add_argument("--precision", choices=["fp64", "fp32"], help="--only batch / ttg: one form only")
     ap.add_argument("--ttg-iters", type=int, default=0,
@@ -458,6 +460,33 @@ def serving_run(rate, n_requests, dps, seed=11, iter_limit=SERVE_ITER_LIMIT):
             "pool_bytes_peak": st["pool_bytes_peak"], "rounds": st["rounds"]}
 
 
+def screen_check_run(seed: int = 5) -> dict:
+    """The FP32 screen against FP64 on the n=64 MIQCQP: 10^5 FP64 points per
+    box inside the box's FP32 enclosure (uniform boxes, and boxes around the
+    origin, a feasible point), and the FP32/FP64 width ratio of the
+    objective, every constraint root and 96 other nodes at three box
+    scales."""
+    import numpy as np
+
+    from cuminlp_gb300 import generators as G
+    from cuminlp_gb300 import screen_check as S
+    from cuminlp_gb300.solver import DeviceProblem
+    p = G.config3(0)
+    rng = np.random.default_rng(seed)
+    t0 = time.perf_counter()
+    dp = DeviceProblem(p)
+    points = [S.point_containment(p, 4, 100_000, rng, scale, dp=dp, centre=centre)
+              for scale, centre in ((0.01, None), (0.3, None), (0.03, np.zeros(p.n_vars)))]
+    nodes = S.pick_nodes(p, 96, rng)
+    scales = (1e-3, 1e-2, 1e-1)
+    rows = S.width_inflation(p, [S.sample_boxes(p, 2048, rng, sc) for sc in scales], nodes)
+    return {"workload": "config3: n=64 MIQCQP (8 int [0,15], 56 cont [-10,10]), Q 30% dense, m=32 at 10%",
+            "point_containment": points,
+            "width_inflation": S.inflation_summary(p, rows, [f"{sc:g}" for sc in scales]),
+            "box_scale_meaning": "box half-widths uniform up to this share of the root width; 2048 boxes per scale",
+            "seconds": round(time.perf_counter() - t0, 2)}
+
+
 def run_ours(args):
     world, rank, local, dist = dist_setup(args)
     from cuminlp_gb300 import generators as G
@@ -472,6 +501,9 @@ def run_ours(args):
         prec = args.precision or "fp64"
         print(json.dumps({"config": "n=4 QCQP (config 1, instance 0)", "precision": prec,
                           "run": time_to_gap(G.config1(0), prec, 20.0, args.ttg_iters)}))
+        return
+    if args.only == "screen":
+        print(json.dumps(screen_check_run()))
         return
     if args.only == "serve":
         from cuminlp_gb300.solver import DeviceProblem
@@ -550,6 +582,8 @@ def run_ours(args):
         serving = {"workload": serving_workload(), "runs": [serving_run(r, n, dps) for r, n in SERVE_RUNS],
                    "time_to_gap_run": serving_run(SERVE_TTG[0], SERVE_TTG[1], dps, iter_limit=SERVE_TTG[2])}
 
+    screen_check = None if args.no_screen_check else screen_check_run()
+
     kpi = screen["kernels_per_iter"]
     line = {
         "metric": "boxes/s (batched interval B&B box evaluations, FP32 screen + FP64 certify)",
@@ -611,6 +645,7 @@ def run_ours(args):
         "time_to_gap": ttg,
         "batch_uneven": batch,
         "serving": serving,
+        "fp32_screen_check": screen_check,
     }
     print(json.dumps(line))
     barrier(dist)

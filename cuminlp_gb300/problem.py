@@ -238,9 +238,14 @@ class Problem:
             cons[i]["rhs"] = c.rhs
         return nodes, lb, ub, kinds, cons
 
-    def desc(self):
-        """Returns (ProblemDesc, keepalive) for the C ABI."""
-        nodes, lb, ub, kinds, cons = self.arrays()
+    def desc(self, arrays=None, objective_root: int | None = None, constraints: bool = True):
+        """Returns (ProblemDesc, keepalive) for the C ABI.  `arrays` reuses
+        an earlier arrays() result; `objective_root` and `constraints=False`
+        describe the same DAG rooted at another node, unconstrained (that
+        objective's enclosure is the node's enclosure)."""
+        nodes, lb, ub, kinds, cons = self.arrays() if arrays is None else arrays
+        if not constraints:
+            cons = cons[:0]
         d = A.ProblemDesc()
         d.nodes = nodes.ctypes.data
         d.n_nodes = len(nodes)
@@ -248,7 +253,7 @@ class Problem:
         d.var_ub = ub.ctypes.data
         d.var_kinds = kinds.ctypes.data
         d.n_vars = len(lb)
-        d.objective_root = self.objective_root
+        d.objective_root = self.objective_root if objective_root is None else int(objective_root)
         d.constraints = cons.ctypes.data if len(cons) else None
         d.n_constraints = len(cons)
         return d, (nodes, lb, ub, kinds, cons)

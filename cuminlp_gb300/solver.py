@@ -25,9 +25,11 @@ from .problem import Problem
 class DeviceProblem:
     """A Problem compiled and resident on the current CUDA device."""
 
-    def __init__(self, problem: Problem):
+    def __init__(self, problem: Problem, **desc_options):
+        """`desc_options` go to Problem.desc (a node as the objective, no
+        constraints, reused arrays)."""
         self.problem = problem
-        desc, self._keep = problem.desc()
+        desc, self._keep = problem.desc(**desc_options)
         h = C.c_void_p()
         check(lib().cmn_problem_create(C.byref(desc), C.byref(h)))
         self.handle = h

@@ -62,9 +62,11 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-batch", action="store_true", help="skip the 1024-instance batch (config 4)")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving stream (config 5)")
+    ap.add_argument("--no-config3", action="store_true", help="skip the n=64 solver steps (config 3)")
     ap.add_argument("--no-screen-check", action="store_true",
                     help="skip the FP32 screen containment / width-inflation check (config 3)")
-    ap.add_argument("--only", choices=["batch", "serve", "ttg", "screen"], help="run one of the extra workloads alone")
+    ap.add_argument("--only", choices=["batch", "serve", "ttg", "screen", "config3"],
+                    help="run one of the extra workloads alone")
     ap.add_argument("--instances", type=int, default=1024, help="--only batch: instances in the batch")
     ap.add_argument("--precision", choices=["fp64", "fp32"], help="--only batch / ttg: one form only")
     ap.add_argument("--ttg-iters", type=int, default=0,
@@ -258,14 +260,13 @@ def cpu_info(path: str = "/proc/cpuinfo"):
 
 
 # ------------------------------------------------------------- GPU side
-def solver_run(dp, rt, precision, steps, warmup):
+def solver_run(dp, rt, precision, steps, warmup, e=E_PARENTS, b=B_BITS, cap=CAP):
     from cuminlp_gb300.solver import Solver
-    s = Solver(dp, bisection_budget=B_BITS, batch_parents=E_PARENTS, frontier_cap=CAP, precision=precision,
-               sample_points=1)
+    s = Solver(dp, bisection_budget=b, batch_parents=e, frontier_cap=cap, precision=precision, sample_points=1)
     # ramp from the root until the pool holds a full batch of parents
     for _ in range(64):
         s.step(1)
-        if s.outcome()["frontier_size"] >= E_PARENTS:
+        if s.outcome()["frontier_size"] >= e:
             break
     for _ in range(warmup):
         s.step(1)
@@ -460,6 +461,31 @@ def serving_run(rate, n_requests, dps, seed=11, iter_limit=SERVE_ITER_LIMIT):
             "pool_bytes_peak": st["pool_bytes_peak"], "rounds": st["rounds"]}
 
 
+CONFIG3_CAP = 1 << 22
+
+
+def config3_run(rt, steps, warmup) -> dict:
+    """Solver steps on the n=64 MIQCQP in both forms: 2^16 parents x 2^4
+    children per step, frontier cap 2^22 boxes."""
+    from cuminlp_gb300 import generators as G
+    from cuminlp_gb300.solver import DeviceProblem
+    dp = DeviceProblem(G.config3(0))
+    res = {p: solver_run(dp, rt, p, steps, warmup, cap=CONFIG3_CAP) for p in ("fp64", "fp32")}
+    out = {"workload": "config3: n=64 MIQCQP (8 int [0,15], 56 cont [-10,10]), Q 30% dense, m=32 at 10%; "
+                       f"{E_PARENTS} parents x 2^{B_BITS} children per step; frontier cap 2^22",
+           "flops_per_box": dp.info()["flops_per_box"]}
+    for p, r in res.items():
+        out["plain_fp64" if p == "fp64" else "fp32_screen"] = {
+            "value": r["delta"]["bounded"] / (r["ms"] * 1e-3), "unit": "boxes/s", "ms_per_step": r["ms"] / steps,
+            "phases_ms": [round(sum(ph[i] for ph in r["phases"]) / len(r["phases"]), 3) for i in range(5)]}
+    sc = res["fp32"]["delta"]
+    out["screen_speedup_vs_plain_fp64"] = out["fp32_screen"]["value"] / out["plain_fp64"]["value"]
+    out["identical_certified_bounds"] = res["fp64"]["outcome"] == res["fp32"]["outcome"]
+    out["screen_active_fraction"] = sc["screened_fp32"] / max(1, sc["bounded"])
+    out["screen_certified_fraction"] = sc["certified_fp64"] / max(1, sc["bounded"])
+    return out
+
+
 def screen_check_run(seed: int = 5) -> dict:
     """The FP32 screen against FP64 on the n=64 MIQCQP: 10^5 FP64 points per
     box inside the box's FP32 enclosure (uniform boxes, and boxes around the
@@ -504,6 +530,9 @@ def run_ours(args):
         return
     if args.only == "screen":
         print(json.dumps(screen_check_run()))
+        return
+    if args.only == "config3":
+        print(json.dumps(config3_run(rt, args.steps, args.warmup)))
         return
     if args.only == "serve":
         from cuminlp_gb300.solver import DeviceProblem
@@ -583,6 +612,7 @@ def run_ours(args):
                    "time_to_gap_run": serving_run(SERVE_TTG[0], SERVE_TTG[1], dps, iter_limit=SERVE_TTG[2])}
 
     screen_check = None if args.no_screen_check else screen_check_run()
+    config3 = None if args.no_config3 else config3_run(rt, args.steps, args.warmup)
 
     kpi = screen["kernels_per_iter"]
     line = {
@@ -646,6 +676,7 @@ def run_ours(args):
         "batch_uneven": batch,
         "serving": serving,
         "fp32_screen_check": screen_check,
+        "config3_solver": config3,
     }
     print(json.dumps(line))
     barrier(dist)

@@ -17,6 +17,15 @@ reference's SearchDriver makes) with host buffers: one parent box per step
 split into 2^20 regions, host->device copy of the box and slots and
 device->host copy of the 2^20 verdicts inside the timed region.
 
+The line also carries the other workloads, each skippable by a --no-* flag
+and runnable alone with --only:
+- time_to_gap: the n=4 QCQP to the 1e-6 gap;
+- batch_uneven: 1024 uneven instances in one batch;
+- serving: a Poisson request stream;
+- config3_solver: solver steps on the n=64 MIQCQP;
+- fp32_screen_check: FP64 points inside FP32 enclosures, and per-node width
+  inflation.
+
 --impl reference times the CPU restatement of the reference path (the
 reference has no CPU evaluation backend of its own; its region evaluation
 runs only on the GPU) on all host cores over a bounded sample.

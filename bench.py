@@ -522,6 +522,18 @@ def screen_check_run(seed: int = 5) -> dict:
             "seconds": round(time.perf_counter() - t0, 2)}
 
 
+def extra_leg(fn, *a, **k):
+    """Runs one of the workloads beside the headline. A failure is recorded
+    in the line (and its traceback printed to stderr) instead of losing the
+    headline measurement."""
+    try:
+        return fn(*a, **k)
+    except Exception as e:  # noqa: BLE001 -- reported, not swallowed
+        import traceback
+        traceback.print_exc(file=sys.stderr)
+        return {"error": f"{type(e).__name__}: {e}"}
+
+
 def run_ours(args):
     world, rank, local, dist = dist_setup(args)
     from cuminlp_gb300 import generators as G
@@ -596,32 +608,32 @@ def run_ours(args):
 
     model, cores = cpu_info()
     cpu_v, cpu_s = cpu_rate(problem, args.cpu_seconds, cores)
-    ttg = None
-    if not args.no_ttg:
-        ttg = {"config": f"n=4 QCQP (config 1, instances 0 and 1), gap 1e-6, 2^{TTG_B} children per parent, "
+    def ttg_leg():
+        out = {"config": f"n=4 QCQP (config 1, instances 0 and 1), gap 1e-6, 2^{TTG_B} children per parent, "
                          f"{TTG_E} parents per iteration, frontier cap {TTG_CAP}, 20 s cap each"}
         for inst in (0, 1):
             p1 = G.config1(inst)
-            ttg[f"instance{inst}"] = {"fp64": time_to_gap(p1, "fp64", 20.0),
+            out[f"instance{inst}"] = {"fp64": time_to_gap(p1, "fp64", 20.0),
                                       "fp32_screen_fp64_certify": time_to_gap(p1, "fp32", 20.0)}
+        return out
 
-    batch = None
-    if not args.no_batch:
+    def batch_leg():
         bres = {p: batch_run(rt, p, args.steps * 4, args.warmup) for p in ("fp64", "fp32")}
-        batch = {"workload": "config4: 1024 uneven QCQPs, n ~ U{4..48}, m ~ U{0..24}, 0-25% integers; "
-                             "256 parents x 2^4 children per instance per step; pool cap 4096 per instance",
-                 "fp32_screen": bres["fp32"], "plain_fp64": bres["fp64"],
-                 "screen_speedup_vs_plain_fp64": bres["fp32"]["value"] / bres["fp64"]["value"]}
-    serving = None
-    if not args.no_serve:
-        from cuminlp_gb300 import generators as G
-        from cuminlp_gb300.solver import DeviceProblem
-        dps = [DeviceProblem(G.config5_request(i)) for i in range(400)]
-        serving = {"workload": serving_workload(), "runs": [serving_run(r, n, dps) for r, n in SERVE_RUNS],
-                   "time_to_gap_run": serving_run(SERVE_TTG[0], SERVE_TTG[1], dps, iter_limit=SERVE_TTG[2])}
+        return {"workload": "config4: 1024 uneven QCQPs, n ~ U{4..48}, m ~ U{0..24}, 0-25% integers; "
+                            "256 parents x 2^4 children per instance per step; pool cap 4096 per instance",
+                "fp32_screen": bres["fp32"], "plain_fp64": bres["fp64"],
+                "screen_speedup_vs_plain_fp64": bres["fp32"]["value"] / bres["fp64"]["value"]}
 
-    screen_check = None if args.no_screen_check else screen_check_run()
-    config3 = None if args.no_config3 else config3_run(rt, args.steps, args.warmup)
+    def serving_leg():
+        dps = [DeviceProblem(G.config5_request(i)) for i in range(400)]
+        return {"workload": serving_workload(), "runs": [serving_run(r, n, dps) for r, n in SERVE_RUNS],
+                "time_to_gap_run": serving_run(SERVE_TTG[0], SERVE_TTG[1], dps, iter_limit=SERVE_TTG[2])}
+
+    ttg = None if args.no_ttg else extra_leg(ttg_leg)
+    batch = None if args.no_batch else extra_leg(batch_leg)
+    serving = None if args.no_serve else extra_leg(serving_leg)
+    screen_check = None if args.no_screen_check else extra_leg(screen_check_run)
+    config3 = None if args.no_config3 else extra_leg(config3_run, rt, args.steps, args.warmup)
 
     kpi = screen["kernels_per_iter"]
     line = {

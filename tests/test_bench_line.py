@@ -127,3 +127,17 @@ def test_skip_flags_leave_the_extra_legs_empty(stubbed, monkeypatch):
 def test_quick_line(stubbed, monkeypatch):
     d = _line(monkeypatch, ["--quick", "--steps", "2", "--warmup", "1"])
     assert d["quick"] is True and d["boxes/s"] == pytest.approx(2 * (1 << 20) / 0.12)
+
+
+def test_a_failing_extra_leg_is_recorded_not_fatal(stubbed, monkeypatch):
+    def boom(*a, **k):
+        raise RuntimeError("out of device memory")
+
+    monkeypatch.setattr(bench, "config3_run", boom)
+    monkeypatch.setattr(bench, "batch_run", boom)
+    d = _line(monkeypatch, ["--steps", "2", "--warmup", "1"])
+    assert d["config3_solver"] == {"error": "RuntimeError: out of device memory"}
+    assert d["batch_uneven"] == {"error": "RuntimeError: out of device memory"}
+    assert d["value"] > 0 and d["e2e"]["value"] > 0 and d["serving"] == {"workload": bench.serving_workload(),
+                                                                         "runs": [{"latency_p99_ms": 1.0}] * 3,
+                                                                         "time_to_gap_run": {"latency_p99_ms": 1.0}}

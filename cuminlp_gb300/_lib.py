@@ -56,6 +56,7 @@ SIGNATURES = {
     "cmn_measure_fma_peak": (I32, [I32, C.POINTER(D)]),
     "cmn_fp64_emu_check": (I32, [U64, U64, I32, C.POINTER(U64)]),
     "cmn_fp64_emu_check_host": (I32, [U64, U64, I32, C.POINTER(U64)]),
+    "cmn_fp64_emu_op_host": (I32, [I32, D, D, C.POINTER(D), C.POINTER(I32)]),
     "cmn_solve": (I32, [P, C.POINTER(A.SolveOptions), C.POINTER(A.Outcome), P]),
     "cmn_batch_create": (I32, [C.POINTER(A.BatchConfig), PP]),
     "cmn_batch_destroy": (None, [P]),

@@ -164,6 +164,18 @@ extern "C" cmn_status cmn_fp64_emu_check_host(uint64_t n, uint64_t seed, int32_t
   return CMN_OK;
 }
 
+extern "C" cmn_status cmn_fp64_emu_op_host(int32_t op, double a, double b, double* out, int32_t* handled)
+{
+  if (!out || !handled || op < 0 || op > 6) return CMN_INVALID_CONFIGURATION;
+  uint64_t ua, ub, r;
+  std::memcpy(&ua, &a, 8);
+  std::memcpy(&ub, &b, 8);
+  const bool ok = cmn::emu_op(op, ua, ub, r);
+  *handled = ok ? 1 : 0;
+  if (ok) std::memcpy(out, &r, 8);
+  return CMN_OK;
+}
+
 extern "C" cmn_status cmn_fp64_emu_check(uint64_t n, uint64_t seed, int32_t family, uint64_t* out3)
 {
   if (!out3 || family < 0 || family > 4) return CMN_INVALID_CONFIGURATION;

@@ -462,6 +462,13 @@ cmn_status cmn_fp64_emu_check(uint64_t n, uint64_t seed, int32_t family, uint64_
  * host FPU in each rounding mode; needs no GPU. */
 cmn_status cmn_fp64_emu_check_host(uint64_t n, uint64_t seed, int32_t family, uint64_t* out3);
 
+/* One integer-path operation on the host, for checks against exact
+ * arithmetic: op 0/1 add rounded down/up, 2/3 subtract down/up, 4/5
+ * multiply down/up, 6 multiply to nearest (ties to even).  *handled is 0,
+ * and *out unwritten, when an operand or the result is not a normal number
+ * or a sum cancels exactly (those take the FP64 instruction). */
+cmn_status cmn_fp64_emu_op_host(int32_t op, double a, double b, double* out, int32_t* handled);
+
 /* One-call solve: create, run to a stop condition, report, destroy. */
 cmn_status cmn_solve(const cmn_problem* problem,
                      const cmn_solve_options* opts, cmn_outcome* outcome,

@@ -16,9 +16,13 @@
 #include <vector>
 
 #include "../cuminlp_gb300.h"
+// The reference's headers: from its include directory, or already seen by
+// this translation unit (a single-header build of the reference).
+#if __has_include("cuminlp/backend/backend.hpp")
 #include "cuminlp/backend/backend.hpp"
 #include "cuminlp/errors.hpp"
 #include "cuminlp/model/problem.hpp"
+#endif
 
 namespace cuminlp_gb300 {
 

@@ -1,0 +1,298 @@
+// ref_gpu.cu -- the reference's own host driver and CUDA graph backend,
+// run on the GPU host beside this repository's library.
+//
+// TEST INFRASTRUCTURE ONLY.  Compiled against oracle/_ref/cuminlp_ref_gpu.cuh,
+// the reference's headers as oracle/amalgamate.py writes them (its
+// SearchDriver, policies, BackendCache and the whole CUDA graph backend of
+// backend/graph/*), with the interval operators of oracle/ref_shim_gpu
+// standing in for the un-vendored cuinterval library, and linked with
+// libcuminlp_gb300.so through the reference-side adapter
+// include/cuminlp_gb300/region_backend.hpp.
+//
+// Commands (numbers read and written as C99 hex floats / integers; the
+// problem file is the flattened DAG of tests/golden/make_golden.py):
+//
+//   driver <backend> <in> <out>
+//       SearchDriver::solve (search/driver.hpp:137-537) with the policy that
+//       make_policy (policy/greedy_enum.hpp:204-223) builds, over
+//       backend "gb300" (this library, through the adapter) or "graph"
+//       (the reference's GraphBackendFactory).  <in> starts with
+//       "<policy B|R|G|W> <iter_limit> <B> <partition_num> <enum_cap>
+//        <max_cycle> <samples> <tolerance>".  Writes bounds, stop reason,
+//       claims, counters, best point, and the solve's wall time.
+//
+//   roles <in> <out>
+//       Both backends' bounder and sampler built for the composition that
+//       BisectionBudget(B) picks on the root box (2^B regions): bound() and
+//       sample(salt) on the root region through each, outputs compared bit
+//       for bit (feasible flags, lower bounds with +0 == -0, and the
+//       candidate: found, value, index, point), and each call timed
+//       (median wall time of <reps> calls; every call copies the box in and
+//       the results out and synchronises, in both backends).  <in> starts
+//       with "<B> <samples> <reps> <n_salts> <roles b|s|bs> <frac>": the
+//       region is the root box, or for frac < 1 its part within frac of
+//       its half-width around the origin (where the QCQPs' points are
+//       feasible).
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "cuminlp_ref_gpu.cuh"
+#include "cuminlp_gb300/region_backend.hpp"
+
+using namespace cuminlp;
+
+static double rd(std::istream& in)
+{
+  std::string s;
+  in >> s;
+  return std::strtod(s.c_str(), nullptr);
+}
+
+static std::string hx(double x)
+{
+  char buf[64];
+  std::snprintf(buf, sizeof buf, "%a", x);
+  return buf;
+}
+
+static double now_s()
+{
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// the flattened DAG, rebuilt with ExprDAG::emit
+static model::Problem<double> load_problem(std::istream& in)
+{
+  model::Problem<double> P;
+  size_t n_nodes;
+  in >> n_nodes;
+  for (size_t i = 0; i < n_nodes; ++i) {
+    int op, n_in;
+    long long in0, in1, var_index, int_exp;
+    in >> op >> n_in >> in0 >> in1 >> var_index;
+    const double constant = rd(in);
+    in >> int_exp;
+    model::DAGNodePayload<double> p{};
+    if (op == CMN_OP_CONST) p.constant = constant;
+    if (op == CMN_OP_VAR) p.var_index = (size_t)var_index;
+    if (op == CMN_OP_POWN) p.int_exp = (int)int_exp;
+    const auto o = static_cast<model::Op>(op);
+    if (n_in == 0) P.graph.emit(o, {}, p);
+    else if (n_in == 1) P.graph.emit(o, {(size_t)in0}, p);
+    else P.graph.emit(o, {(size_t)in0, (size_t)in1}, p);
+  }
+  size_t n_vars;
+  in >> n_vars;
+  for (size_t v = 0; v < n_vars; ++v) {
+    const double lo = rd(in), hi = rd(in);
+    int k;
+    in >> k;
+    P.box_bounds.push_back({lo, hi});
+    P.var_kinds.push_back(static_cast<model::VarKind>(k));
+  }
+  in >> P.objective_root;
+  size_t m;
+  in >> m;
+  for (size_t c = 0; c < m; ++c) {
+    size_t root;
+    int cmp;
+    in >> root >> cmp;
+    const double rhs = rd(in);
+    P.constraints.push_back({root, static_cast<model::Cmp>(cmp), rhs});
+  }
+  P.validate();
+  return P;
+}
+
+static std::shared_ptr<const backend::RegionBackendFactory<double>> make_backend(const std::string& name)
+{
+  if (name == "gb300") return std::make_shared<cuminlp_gb300::GB300BackendFactory>();
+  if (name == "graph") return std::make_shared<backend::graph::GraphBackendFactory<double>>();
+  throw std::runtime_error("unknown backend " + name);
+}
+
+static int cmd_driver(const std::string& backend_name, std::istream& in, std::ostream& out)
+{
+  std::string pk;
+  uint32_t iter_limit;
+  size_t B, pn, ecap, max_cycle, samples;
+  in >> pk >> iter_limit >> B >> pn >> ecap >> max_cycle >> samples;
+  const double tol = rd(in);
+  model::Problem<double> P = load_problem(in);
+  policy::PolicyKind kind = policy::PolicyKind::BisectionBudget;
+  if (pk == "R") kind = policy::PolicyKind::RelativeBisectionBudget;
+  else if (pk == "G") kind = policy::PolicyKind::GreedyEnumerate;
+  else if (pk == "W") kind = policy::PolicyKind::WidthFirst;
+  config::SearchCalibration cal{};
+  cal.max_cycle_size = max_cycle;
+  std::shared_ptr<const policy::CompositionPolicy<double>> pol =
+      policy::make_policy<double>(kind, region::FanOutSpec(pn, ecap), B, cal);
+  search::SearchDriver<double> drv(pol, make_backend(backend_name), iter_limit, tol, samples);
+  std::streambuf* prev = std::cout.rdbuf();
+  std::ostringstream sink;
+  std::cout.rdbuf(sink.rdbuf());
+  const double t0 = now_s();
+  auto o = drv.solve(P);
+  const double t1 = now_s();
+  std::cout.rdbuf(prev);
+  const auto& t = o.counters;
+  out << hx(o.lower_bound) << ' ' << hx(o.upper_bound) << ' ' << search::to_string(o.stop_reason) << ' '
+      << o.proven_optimal << ' ' << o.infeasible << '\n';
+  out << t.iterations << ' ' << t.fathomed << ' ' << t.fathomed_points << ' ' << t.bounded << ' ' << t.sampled << ' '
+      << t.enqueued << ' ' << t.witness_rejected << ' ' << t.pruned_duplicate << ' ' << t.pruned_infeasible << ' '
+      << t.pruned_dominated << ' ' << t.pending << ' ' << t.viable << '\n';
+  out << o.best_point.size();
+  for (double x : o.best_point) out << ' ' << hx(x);
+  out << '\n';
+  out << "seconds " << (t1 - t0) << '\n';
+  return 0;
+}
+
+static bool same_bits(double a, double b)
+{
+  if (a == 0.0 && b == 0.0) return true;
+  if (a != a && b != b) return true;
+  uint64_t x, y;
+  std::memcpy(&x, &a, 8);
+  std::memcpy(&y, &b, 8);
+  return x == y;
+}
+
+template <class F>
+static double median_seconds(int reps, F&& f)
+{
+  std::vector<double> ts;
+  for (int i = 0; i < reps; ++i) {
+    const double t0 = now_s();
+    f();
+    ts.push_back(now_s() - t0);
+  }
+  std::sort(ts.begin(), ts.end());
+  return ts[ts.size() / 2];
+}
+
+static int cmd_roles(std::istream& in, std::ostream& out)
+{
+  size_t B, samples, reps, n_salts;
+  std::string which;
+  in >> B >> samples >> reps >> n_salts >> which;
+  const double frac = rd(in);
+  model::Problem<double> P = load_problem(in);
+  // the region: the root box, or for frac < 1 the part of it within
+  // frac * (half its width) of the origin, integer bounds rounded inward
+  std::vector<cu::interval<double>> box = P.box_bounds;
+  if (frac < 1.0) {
+    for (size_t v = 0; v < box.size(); ++v) {
+      const double w = frac * 0.5 * (box[v].ub - box[v].lb);
+      double lo = std::max(box[v].lb, -w), hi = std::min(box[v].ub, w);
+      if (P.var_kinds[v] != model::VarKind::Continuous) {
+        lo = std::ceil(lo);
+        hi = std::max(std::floor(hi), lo);
+      }
+      box[v] = {lo, hi};
+    }
+  }
+  policy::BisectionBudgetCompositionPolicy<double> pol(B);
+  const region::SlotAssignment a = pol.choose(box, P.var_kinds);
+  size_t n_regions = 1;
+  for (size_t w : a.widths) n_regions *= w;
+  const backend::Region<double> region{std::span<const cu::interval<double>>(box), a};
+  backend::BuildBudget budget;
+  budget.samples_per_region = samples;
+  out << "n_regions " << n_regions << '\n' << "slots " << a.size() << '\n';
+  const bool do_bound = which.find('b') != std::string::npos, do_sample = which.find('s') != std::string::npos;
+  std::vector<std::string> names = {"gb300", "graph"};
+
+  if (do_bound) {
+    std::vector<std::vector<unsigned char>> fe(2);
+    std::vector<std::vector<double>> lb(2);
+    for (int b = 0; b < 2; ++b) {
+      auto fac = make_backend(names[b]);
+      const double t0 = now_s();
+      auto bundle = fac->build_subdivision(P, a.composition, n_regions, budget, backend::RoleRequest{false, true, false});
+      out << "bound_build_seconds_" << names[b] << ' ' << (now_s() - t0) << '\n';
+      auto r = bundle.bounder->bound(region);
+      fe[b].assign(r.feasible.begin(), r.feasible.end());
+      lb[b].assign(r.obj_lb.begin(), r.obj_lb.end());
+      const double sec = median_seconds((int)reps, [&] { bundle.bounder->bound(region); });
+      out << "bound_seconds_" << names[b] << ' ' << sec << '\n';
+    }
+    size_t bad_fe = 0, bad_lb = 0;
+    for (size_t i = 0; i < n_regions; ++i) {
+      bad_fe += fe[0][i] != fe[1][i];
+      bad_lb += !same_bits(lb[0][i], lb[1][i]);
+    }
+    out << "bound_mismatch_feasible " << bad_fe << '\n' << "bound_mismatch_lb " << bad_lb << '\n';
+    size_t n_feasible = 0;
+    for (auto f : fe[1]) n_feasible += f != 0;
+    out << "bound_feasible " << n_feasible << '\n';
+  }
+  if (do_sample) {
+    size_t bad = 0;
+    std::vector<std::vector<std::string>> rec(2);
+    for (int b = 0; b < 2; ++b) {
+      auto fac = make_backend(names[b]);
+      const double t0 = now_s();
+      auto bundle = fac->build_subdivision(P, a.composition, n_regions, budget, backend::RoleRequest{true, false, false});
+      out << "sample_build_seconds_" << names[b] << ' ' << (now_s() - t0) << '\n';
+      for (size_t s = 1; s <= n_salts; ++s) {
+        auto c = bundle.sampler->sample(region, s);
+        std::ostringstream line;
+        // the index is CUB's raw output in the reference when nothing is
+        // found (and -1 here): compared only with a witness
+        line << c.found << ' ' << hx(c.value);
+        if (c.found) {
+          line << ' ' << c.index;
+          for (double x : c.point) line << ' ' << hx(x);
+        }
+        rec[b].push_back(line.str());
+      }
+      const double sec = median_seconds((int)reps, [&] { bundle.sampler->sample(region, 1); });
+      out << "sample_seconds_" << names[b] << ' ' << sec << '\n';
+    }
+    size_t found = 0;
+    for (size_t s = 0; s < n_salts; ++s) {
+      bad += rec[0][s] != rec[1][s];
+      found += rec[1][s][0] == '1';
+      out << "sample_" << names[1] << ' ' << rec[1][s] << '\n';
+    }
+    out << "sample_found " << found << '\n';
+    out << "sample_mismatch " << bad << '\n';
+  }
+  return 0;
+}
+
+int main(int argc, char** argv)
+{
+  if (argc < 4) {
+    std::cerr << "usage: ref_gpu driver <gb300|graph> <in> <out> | roles <in> <out>\n";
+    return 2;
+  }
+  const std::string cmd = argv[1];
+  try {
+    if (cmd == "driver" && argc >= 5) {
+      std::ifstream in(argv[3]);
+      std::ofstream out(argv[4]);
+      return cmd_driver(argv[2], in, out);
+    }
+    if (cmd == "roles") {
+      std::ifstream in(argv[2]);
+      std::ofstream out(argv[3]);
+      return cmd_roles(in, out);
+    }
+  } catch (const std::exception& e) {
+    std::cerr << "error: " << e.what() << '\n';
+    return 1;
+  }
+  std::cerr << "unknown command\n";
+  return 2;
+}

@@ -14,6 +14,7 @@
 //   decode  <in> <out>   lines "kind plo phi part fan" -> "lo hi"
 //   policy  <in> <out>   BisectionBudget / GreedyEnum choose() cases
 //   driver  <in> <out>   SearchDriver::solve on a problem file
+//   driverp <in> <out>   the same with any policy make_policy builds
 //   aggdriver <in> <out> AggregateDriver::solve (WidestBranchPolicy) on a
 //                        problem file, the oracle behind its roles
 #include <cstdio>
@@ -30,6 +31,7 @@
 #include "cuminlp/model/problem.hpp"
 #include "cuminlp/policy/bisection_budget.hpp"
 #include "cuminlp/policy/greedy_enum.hpp"
+#include "cuminlp/policy/width_first.hpp"
 #include "cuminlp/region/decode.hpp"
 #include "cuminlp/search/driver.hpp"
 
@@ -317,6 +319,46 @@ static int cmd_driver(std::istream& in, std::ostream& out)
   return 0;
 }
 
+// "<policy B|R|G|W> <iter_limit> <B> <partition_num> <enum_cap> <max_cycle>
+// <samples> <tolerance>" then the problem: SearchDriver::solve with the
+// policy make_policy (policy/greedy_enum.hpp:204-223) builds
+static int cmd_driverp(std::istream& in, std::ostream& out)
+{
+  std::string pk;
+  uint32_t iter_limit;
+  size_t B, pn, ecap, max_cycle, samples;
+  in >> pk >> iter_limit >> B >> pn >> ecap >> max_cycle >> samples;
+  double tol = rd(in);
+  Loaded L;
+  load_problem(in, L);
+  policy::PolicyKind kind = policy::PolicyKind::BisectionBudget;
+  if (pk == "R") kind = policy::PolicyKind::RelativeBisectionBudget;
+  else if (pk == "G") kind = policy::PolicyKind::GreedyEnumerate;
+  else if (pk == "W") kind = policy::PolicyKind::WidthFirst;
+  config::SearchCalibration cal{};
+  cal.max_cycle_size = max_cycle;
+  std::shared_ptr<const policy::CompositionPolicy<double>> pol =
+      policy::make_policy<double>(kind, region::FanOutSpec(pn, ecap), B, cal);
+  auto fac = std::make_shared<OracleFactory>(L.orc);
+  search::SearchDriver<double> drv(pol, fac, iter_limit, tol, samples);
+  std::streambuf* prev = std::cout.rdbuf();
+  std::ostringstream sink;
+  std::cout.rdbuf(sink.rdbuf());
+  auto o = drv.solve(L.problem);
+  std::cout.rdbuf(prev);
+  const auto& t = o.counters;
+  out << hx(o.lower_bound) << ' ' << hx(o.upper_bound) << ' ' << search::to_string(o.stop_reason) << ' '
+      << o.proven_optimal << ' ' << o.infeasible << '\n';
+  out << t.iterations << ' ' << t.fathomed << ' ' << t.fathomed_points << ' ' << t.bounded << ' ' << t.sampled << ' '
+      << t.enqueued << ' ' << t.witness_rejected << ' ' << t.pruned_duplicate << ' ' << t.pruned_infeasible << ' '
+      << t.pruned_dominated << ' ' << t.pending << ' ' << t.viable << '\n';
+  out << o.best_point.size();
+  for (double x : o.best_point) out << ' ' << hx(x);
+  out << '\n';
+  orc_problem_destroy(L.orc);
+  return 0;
+}
+
 // ---- aggregate roles over the oracle ---------------------------------------
 class OAggBounder : public aggregate::AggregateBounder<double> {
  public:
@@ -430,6 +472,7 @@ int main(int argc, char** argv)
     if (cmd == "decode") return cmd_decode(in, out);
     if (cmd == "policy") return cmd_policy(in, out);
     if (cmd == "driver") return cmd_driver(in, out);
+    if (cmd == "driverp") return cmd_driverp(in, out);
     if (cmd == "aggdriver") return cmd_aggdriver(in, out);
   } catch (const std::exception& e) {
     std::cerr << "error: " << e.what() << '\n';

@@ -201,6 +201,39 @@ def driver_cases(problems):
     return res
 
 
+# (problem, policy, iter_limit, B, partition_num, enumerate_cap, max_cycle,
+# samples): policies as make_policy builds them (policy/greedy_enum.hpp:204)
+POLICY_RUNS = [
+    ("contract_model", "G", 600, 0, 2, 4, 3, 2), ("int_eq", "G", 400, 0, 2, 6, 3, 2),
+    ("qcqp_n4_0", "G", 1500, 0, 2, 2, 2, 1), ("miqcqp_n6", "G", 800, 0, 2, 4, 3, 1),
+    ("qcqp_n4_1", "W", 1500, 0, 3, 2, 2, 2), ("aggregate_fixture", "W", 600, 0, 2, 2, 2, 2),
+    ("contract_model", "W", 600, 0, 2, 3, 4, 1),
+    ("square_le5", "R", 400, 2, 2, 1, 0, 4), ("miqcqp_n6", "R", 800, 3, 2, 1, 0, 1),
+]
+
+
+def policy_header(run_: tuple) -> str:
+    _, pk, iters, B, pn, ecap, mc, S = run_
+    return f"{pk} {iters} {B} {pn} {ecap} {mc} {S} {hx(1e-6)}\n"
+
+
+def driver_policy_cases(problems):
+    """The reference SearchDriver with GreedyEnum, WidthFirst and relative
+    BisectionBudget (the oracle behind its roles)."""
+    res = []
+    for r in POLICY_RUNS:
+        lines = run("driverp", policy_header(r) + problem_text(problems[r[0]]))
+        h = lines[0].split()
+        res.append({
+            "problem": r[0], "policy": r[1], "iter_limit": r[2], "B": r[3], "partition_num": r[4],
+            "enumerate_cap": r[5], "max_cycle": r[6], "samples": r[7],
+            "lower_bound": h[0], "upper_bound": h[1], "stop_reason": h[2], "proven_optimal": int(h[3]),
+            "infeasible": int(h[4]), "counters": [int(x) for x in lines[1].split()],
+            "best_point": lines[2].split()[1:],
+        })
+    return res
+
+
 AGG_CASES = (("square_le5", 300), ("infeasible", 50), ("aggregate_fixture", 400), ("int_eq", 100),
              ("miqcqp_n6", 300), ("qcqp_n4_1", 600))
 
@@ -238,6 +271,7 @@ def main():
     (HERE / "decode.json").write_text(json.dumps(decode_cases(), indent=0))
     (HERE / "policy.json").write_text(json.dumps(policy_cases(), indent=0))
     (HERE / "driver.json").write_text(json.dumps(driver_cases(fixture_problems()), indent=1))
+    (HERE / "driver_policies.json").write_text(json.dumps(driver_policy_cases(fixture_problems()), indent=1))
     (HERE / "gams.json").write_text(json.dumps(gams_cases(), indent=1))
     (HERE / "aggdriver.json").write_text(json.dumps(aggdriver_cases(fixture_problems()), indent=1))
     print("golden fixtures written")

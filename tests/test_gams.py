@@ -8,6 +8,7 @@ from __future__ import annotations
 
 import json
 import math
+import os
 from pathlib import Path
 
 import numpy as np
@@ -19,7 +20,7 @@ from tests.gams_ref import REF_GAMS, our_lowering, parse_lowering, reference_low
 
 HERE = Path(__file__).resolve().parent
 DATA = HERE / "data" / "gams"
-REF_DATA = Path("/root/reference/test/data/gams")
+REF_DATA = Path(os.environ["CMN_REFERENCE"]) / "test" / "data" / "gams" if os.environ.get("CMN_REFERENCE") else None
 
 
 def same(r: dict, o: dict):
@@ -41,7 +42,8 @@ def test_own_models_match_reference_golden():
         same(parse_lowering(lines), our_lowering(DATA / name))
 
 
-@pytest.mark.skipif(not (REF_GAMS.exists() and REF_DATA.exists()), reason="reference frontend not built here")
+@pytest.mark.skipif(REF_DATA is None or not (REF_GAMS.exists() and REF_DATA.exists()),
+                    reason="CMN_REFERENCE unset or the reference frontend not built here")
 def test_reference_corpus_lowers_identically():
     files = sorted(REF_DATA.glob("*.gms"))
     assert files

@@ -38,13 +38,13 @@ def problems():
     }
 
 
-def compare(p, iterations, **opts):
+def compare(p, iterations, room=1 << 20, **opts):
     dp = DeviceProblem(p)
     s = Solver(dp, batch_iter_limit=iterations, **opts)
     s.step(0)
     g = s.outcome()
     gbox, glb, gdepth = s.frontier()
-    obox, olb, odepth, o = O.OracleProblem(p).batched_frontier(iterations, room=1 << 20, **opts)
+    obox, olb, odepth, o = O.OracleProblem(p).batched_frontier(iterations, room=room, **opts)
     assert len(glb) == len(olb)
     assert bits_equal(glb, olb)
     assert np.array_equal(gdepth, odepth)
@@ -161,3 +161,23 @@ def test_batched_solver_certifies_the_reference_optimum():
         tol = 1e-6 * max(1.0, abs(ref["upper_bound"]))
         assert abs(g["upper_bound"] - ref["upper_bound"]) <= tol
         assert abs(g["lower_bound"] - ref["lower_bound"]) <= tol
+
+
+# The shapes bench.py times: 2^16 parents x 2^4 children per iteration
+# (BisectionBudget B = 4), one sample per child.  From the root the pool
+# grows 1 -> 16 -> 256 -> 4096 -> 65536 boxes, so iteration 5 is the first
+# to expand a full batch of 2^16 parents (2^20 children); the oracle needs
+# about a minute per such iteration for n = 32 on 16 host cores, and four
+# times that for n = 64, so the n = 64 case stops after iteration 4 (4096
+# parents, 65536 children) with the same options, buffers and launch shapes.
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_solver_matches_oracle_config2_bench_shape(precision):
+    g = compare(G.config2(), 5, room=1 << 21, bisection_budget=4, batch_parents=1 << 16, frontier_cap=1 << 20,
+                sample_points=1, precision=precision)
+    assert g["counters"]["expansions"] > (1 << 12)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_solver_matches_oracle_config3_bench_shape(precision):
+    compare(G.config3(), 4, room=1 << 21, bisection_budget=4, batch_parents=1 << 16, frontier_cap=1 << 22,
+            sample_points=1, precision=precision)

@@ -21,7 +21,19 @@ VAR_CONTINUOUS, VAR_INTEGER, VAR_BINARY = 0, 1, 2
 CMP_LE, CMP_EQ = 0, 1
 SLOT_CONTINUOUS, SLOT_INTEGER_PARTITION, SLOT_INTEGER_ENUMERATE, SLOT_BINARY_ENUMERATE = 0, 1, 2, 3
 ROLE_BOUNDER, ROLE_SAMPLER, ROLE_ENUMERATOR = 0, 1, 2
-PRECISION_FP64, PRECISION_FP32_SCREEN = 0, 1
+PRECISION_FP64, PRECISION_FP32_SCREEN, PRECISION_FP32_LAZY = 0, 1, 2
+
+
+def precision_code(v) -> int:
+    """cmn_precision from a name ("fp64", "fp32" for the screen with FP64
+    certification of every survivor, "lazy" for the FP32 bound with FP64
+    certification at selection) or a code."""
+    if not isinstance(v, str):
+        return int(v)
+    v = v.lower()
+    if "lazy" in v:
+        return PRECISION_FP32_LAZY
+    return PRECISION_FP32_SCREEN if v.startswith("fp32") else PRECISION_FP64
 
 STATUS_NAMES = ["OK", "INVALID_DAG", "INVALID_PROBLEM", "SHAPE_MISMATCH", "INVALID_CONFIGURATION",
                 "OVER_BUDGET", "CUDA_ERROR", "TIMEOUT", "INTERNAL"]
@@ -116,7 +128,8 @@ class ServerStats(C.Structure):
 
 COUNTER_NAMES = ["iterations", "expansions", "fathomed", "fathomed_points", "bounded", "sampled", "enqueued",
                  "witness_rejected", "pruned_duplicate", "pruned_infeasible", "pruned_dominated",
-                 "dropped_viable", "dropped_dominated", "screened_fp32", "certified_fp64", "peak_frontier"]
+                 "dropped_viable", "dropped_dominated", "screened_fp32", "certified_fp64", "peak_frontier",
+                 "certify_pruned"]
 
 
 class Counters(C.Structure):

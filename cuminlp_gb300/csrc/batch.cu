@@ -397,16 +397,17 @@ extern "C" cmn_status cmn_batch_totals(cmn_batch* s, cmn_counters* sum, uint64_t
   BCK(cudaSetDevice(s->device));
   cmn_status st = s->fresh ? CMN_OK : s->pull();
   if (st != CMN_OK) return st;
-  uint64_t acc[16] = {0};
-  static_assert(sizeof(cmn_counters) == sizeof(acc), "cmn_counters is 16 uint64");
+  constexpr int kN = (int)(sizeof(cmn_counters) / sizeof(uint64_t));
+  uint64_t acc[kN] = {0};
+  static_assert(sizeof(cmn_counters) == sizeof(acc), "cmn_counters holds uint64 fields only");
   for (uint64_t k = 0; k < s->cfg.K; ++k) {
     if (!s->busy[k]) continue;
     cmn_counters c = s->h_st[k].counters;
     c.iterations = s->h_st[k].iterations;
     c.expansions = s->h_st[k].expansions;
-    uint64_t v[16];
+    uint64_t v[kN];
     std::memcpy(v, &c, sizeof v);
-    for (int i = 0; i < 16; ++i) acc[i] += v[i];
+    for (int i = 0; i < kN; ++i) acc[i] += v[i];
   }
   std::memcpy(sum, acc, sizeof acc);
   if (running) *running = s->running();

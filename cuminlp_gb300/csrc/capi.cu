@@ -109,6 +109,7 @@ cmn_problem::~cmn_problem()
   if (cudaGetDevice(&cur) == cudaSuccess && cur != device) cudaSetDevice(device);
   dfree(d_prog64);
   dfree(d_prog32);
+  dfree(d_prog32p);
   dfree(d_kinds);
   dfree(d_root_lb);
   dfree(d_root_ub);
@@ -146,11 +147,14 @@ extern "C" cmn_status cmn_problem_create(const cmn_problem_desc* desc, cmn_probl
     const int64_t n = p->host.n_vars();
     cudaError_t e = dalloc(&p->d_prog64, L);
     if (e == cudaSuccess) e = dalloc(&p->d_prog32, L);
+    if (e == cudaSuccess) e = dalloc(&p->d_prog32p, L);
     if (e == cudaSuccess) e = dalloc(&p->d_kinds, (size_t)n);
     if (e == cudaSuccess) e = dalloc(&p->d_root_lb, (size_t)n);
     if (e == cudaSuccess) e = dalloc(&p->d_root_ub, (size_t)n);
     if (e == cudaSuccess && L) e = cudaMemcpy(p->d_prog64, p->prog.code64.data(), L * sizeof(Instr), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && L) e = cudaMemcpy(p->d_prog32, p->prog.code32.data(), L * sizeof(Instr), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && L)
+      e = cudaMemcpy(p->d_prog32p, p->prog.code32p.data(), L * sizeof(Instr), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
       e = cudaMemcpy(p->d_kinds, p->host.var_kinds.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
@@ -299,6 +303,7 @@ struct cmn_role {
   uint64_t S = 1;
   cudaStream_t stream = nullptr;
   int grid = 1;
+  int lg_min = 0;  // sampler: lanes per point column (sample_lg_min)
   // one device block: [box lo planes n][box hi planes n][slots][pinfo]
   unsigned char* d_stage = nullptr;
   unsigned char* h_stage = nullptr;
@@ -395,9 +400,16 @@ extern "C" cmn_status cmn_role_build(const cmn_problem* p, int32_t role, const u
       return fail(CMN_OVER_BUDGET, std::string(names[role]) + " needs " + std::to_string(needed) +
                                        " B of device memory, but only " + std::to_string(budget) + " B is available.");
     }
+    const int lg_min = sample_lg_min((int)p->host.n_vars(), p->prog.n_slots, p->d_sched != nullptr, kEvalThreads);
+    if (role != CMN_ROLE_BOUNDER &&
+        sample_smem_bytes((int)p->host.n_vars(), p->prog.n_slots, kEvalThreads, lg_min) > (size_t)max_dynamic_smem())
+      return fail(CMN_INVALID_CONFIGURATION,
+                  "the sampler's per-thread point columns do not fit in shared memory (a program with shared slots "
+                  "keeps one column of n_vars + slots doubles per thread)");
     cmn_role* r = new cmn_role();
     r->p = p;
     r->kind = role;
+    r->lg_min = lg_min;
     r->slot_kinds.assign(slot_kinds, slot_kinds + slot_count);
     r->n_regions = n_regions;
     r->S = S;
@@ -652,6 +664,7 @@ static cmn_status candidate_role(cmn_role* r, const double* box, const uint64_t*
   a.sched = r->p->d_sched;
   a.g_max = r->p->prog.group_max;
   a.capacity = (uint64_t)r->grid * kEvalThreads;
+  a.lg_min = r->lg_min;
   CK(launch_sample(a, r->grid, kEvalThreads, r->stream));
   Cand* best = r->d_block_best + r->grid;
   CK(launch_reduce_cand(r->d_block_best, r->grid, best, r->stream));
@@ -855,7 +868,8 @@ extern "C" cmn_status cmn_solver_create(const cmn_problem* p, const cmn_solve_op
   if (o.max_cycle_size > 64)
     return fail(CMN_INVALID_CONFIGURATION, "max_cycle_size (" + std::to_string(o.max_cycle_size) +
                                                ") exceeds kMaxSlots (64)");
-  if (o.precision != CMN_PRECISION_FP64 && o.precision != CMN_PRECISION_FP32_SCREEN)
+  if (o.precision != CMN_PRECISION_FP64 && o.precision != CMN_PRECISION_FP32_SCREEN &&
+      o.precision != CMN_PRECISION_FP32_LAZY)
     return fail(CMN_INVALID_CONFIGURATION, "unknown precision");
   const uint64_t C = 1ull << o.bisection_budget;
   if ((o.batch_parents << o.bisection_budget) > (1ull << 31))
@@ -863,10 +877,21 @@ extern "C" cmn_status cmn_solver_create(const cmn_problem* p, const cmn_solve_op
   if (o.frontier_cap > (1ull << 31)) return fail(CMN_INVALID_CONFIGURATION, "frontier_cap above 2^31");
   cmn_status st = check_interval(p);
   if (st != CMN_OK) return st;
-  st = check_smem(p, o.precision == CMN_PRECISION_FP32_SCREEN, o.bisection_budget);
+  st = check_smem(p, o.precision != CMN_PRECISION_FP64, o.bisection_budget);
   if (st != CMN_OK) return st;
-  if (sample_smem_bytes((int)p->host.n_vars(), p->prog.n_slots, kEvalThreads) > (size_t)max_dynamic_smem())
-    return fail(CMN_INVALID_CONFIGURATION, "problem too large for the sampler's shared-memory tile");
+  if (o.precision == CMN_PRECISION_FP32_LAZY) {  // the parents' FP64 pass
+    st = check_smem(p, false, 0);
+    if (st != CMN_OK) return st;
+  }
+  const int lg_min = sample_lg_min((int)p->host.n_vars(), p->prog.n_slots, p->d_sched != nullptr, kEvalThreads);
+  if (sample_smem_bytes((int)p->host.n_vars(), p->prog.n_slots, kEvalThreads, lg_min) > (size_t)max_dynamic_smem())
+    return fail(CMN_INVALID_CONFIGURATION,
+                "the sampler's per-thread point columns do not fit in shared memory (a program with shared slots "
+                "keeps one column of n_vars + slots doubles per thread)");
+  if (o.precision == CMN_PRECISION_FP32_LAZY &&
+      sample_screen_smem_bytes((int)p->host.n_vars(), p->prog.n_slots, kEvalThreads) > (size_t)max_dynamic_smem())
+    return fail(CMN_INVALID_CONFIGURATION, "the lazy form's FP32 sample screen keeps one column of n_vars + slots "
+                                           "floats per thread; this problem's does not fit in shared memory");
   try {
     CK(cudaSetDevice(p->device));
     CK(ensure_attributes());
@@ -894,13 +919,22 @@ extern "C" cmn_status cmn_solver_create(const cmn_problem* p, const cmn_solve_op
     cfg.tolerance = o.tolerance;
     const uint64_t maxc = cfg.e_max * C;
     const int threads = kEvalThreads;
-    const bool fp32 = o.precision == CMN_PRECISION_FP32_SCREEN;
-    const int occ_e = std::max(1, eval_kernel_occupancy(fp32 ? 2 : 1, fp32,
+    const bool fp32 = o.precision != CMN_PRECISION_FP64;
+    const bool lazy = o.precision == CMN_PRECISION_FP32_LAZY;
+    const int occ_e = std::max(1, eval_kernel_occupancy(lazy ? 5 : fp32 ? 2 : 1, fp32,
                                                         eval_smem_bytes(p->prog.n_slots, cfg.max_slots, fp32, threads), threads));
-    const int occ_s = std::max(1, sample_kernel_occupancy(sample_smem_bytes(n, p->prog.n_slots, threads), threads));
+    cfg.sample_lg_min = lg_min;
+    const int occ_s =
+        std::max(1, sample_kernel_occupancy(sample_smem_bytes(n, p->prog.n_slots, threads, lg_min), threads));
     const uint64_t need = (maxc * (uint64_t)p->prog.group_max + threads - 1) / threads;
     s->eval_grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(need, (uint64_t)sm_count() * occ_e));
     s->sample_grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(need, (uint64_t)sm_count() * occ_s));
+    if (lazy) {
+      const int occ_q = std::max(1, sample_screen_occupancy(sample_screen_smem_bytes(n, p->prog.n_slots, threads),
+                                                            threads));
+      cfg.screen_grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((maxc + threads - 1) / threads,
+                                                                      (uint64_t)sm_count() * occ_q));
+    }
     cfg.g_max = p->d_sched ? p->prog.group_max : 1;
     cfg.eval_capacity = (uint64_t)s->eval_grid * threads;
     cfg.sample_capacity = (uint64_t)s->sample_grid * threads;
@@ -929,6 +963,10 @@ extern "C" cmn_status cmn_solver_create(const cmn_problem* p, const cmn_solve_op
       A(&b.phi32, (size_t)n * cfg.e_max);
     }
     A(&b.pdepth, cfg.e_max);
+    if (lazy) {
+      A(&b.plb, cfg.e_max);
+      A(&b.pfeas, cfg.e_max);
+    }
     A(&b.pslot, cfg.e_max);
     A(&b.pinfo, cfg.e_max);
     A(&b.slots, cfg.e_max * (size_t)cfg.max_slots);
@@ -941,6 +979,7 @@ extern "C" cmn_status cmn_solver_create(const cmn_problem* p, const cmn_solve_op
     A(&b.heap_scratch, cfg.e_max * (size_t)n);
     A(&b.clb, maxc);
     A(&b.cstate, maxc);
+    if (lazy) A(&b.cbest, maxc);
     A(&b.list, maxc);
     const size_t nblk = (std::max<uint64_t>(cfg.pstride, maxc) + kScanTile - 1) / kScanTile + 1;
     A(&b.block_counts, nblk);
@@ -961,6 +1000,7 @@ extern "C" cmn_status cmn_solver_create(const cmn_problem* p, const cmn_solve_op
     }
     b.prog64 = p->d_prog64;
     b.prog32 = p->d_prog32;
+    b.prog32p = p->d_prog32p;
     b.sched = p->d_sched;
     b.kinds = p->d_kinds;
     b.root_lb = p->d_root_lb;

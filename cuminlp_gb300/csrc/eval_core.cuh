@@ -743,6 +743,117 @@ __device__ __forceinline__ PointVerdict group_point_verdict(PointVerdict v, int 
   return v;
 }
 
+// ---- FP32 point evaluation: the lazy form's sample screen ----
+// One round-to-nearest FP32 operation per DAG node, the point's variables
+// and the program's constants rounded to nearest (Program::code32p);
+// constraints by the point predicates on the FP32 values widened to FP64.
+// It only ranks sample points: the point that wins a chunk is evaluated
+// again in FP64 (point_range) before it can become the incumbent.
+struct PointVerdict32 {
+  float obj;
+  bool feasible;
+  bool has_obj;
+};
+
+// x^k by binary powering, round to nearest at every step (k > 0)
+__device__ __forceinline__ float pt32_powu(float a, int k)
+{
+  float r = 1.0f, base = a;
+  while (k > 0) {
+    if (k & 1) r = __fmul_rn(r, base);
+    k >>= 1;
+    if (k > 0) base = __fmul_rn(base, base);
+  }
+  return r;
+}
+
+__device__ __forceinline__ float pt32_generic(uint8_t op, float a, float b, int k)
+{
+  switch (op) {
+    case kGAdd: return __fadd_rn(a, b);
+    case kGSub: return __fsub_rn(a, b);
+    case kGMul: return __fmul_rn(a, b);
+    case kGDiv: return __fdiv_rn(a, b);
+    case kGSqr: return __fmul_rn(a, a);
+    case kGNeg: return -a;
+    case kGSqrt: return __fsqrt_rn(a);
+    case kGPowN: return k == 0 ? 1.0f : (k > 0 ? pt32_powu(a, k) : __fdiv_rn(1.0f, pt32_powu(a, -k)));
+    case kGAbs: return fabsf(a);
+    case kGMin: return fminf(a, b);
+    case kGMax: return fmaxf(a, b);
+    default: return Arith<float>::nan();
+  }
+}
+
+__device__ __forceinline__ float pfetch32(const Tile<float>& t, float acc, const Instr& ins, int mode, int idx)
+{
+  switch (mode) {
+    case kModeSlot: return t.slo[idx * t.stride + t.tid];
+    case kModeVar: return t.lo[idx * t.stride + t.tid];
+    case kModeAcc: return acc;
+    default: return ins.c32.clo;
+  }
+}
+
+__device__ __forceinline__ void point_range32(const Instr* __restrict__ prog, int pc0, int pc1, const Tile<float>& t,
+                                              PointVerdict32& out)
+{
+  float acc = 0.0f;
+  Instr ins = pc0 < pc1 ? load_instr(prog, pc0) : Instr{};
+  for (int pc = pc0; pc < pc1; ++pc) {
+    const Instr cur = ins;
+    if (pc + 1 < pc1) ins = load_instr(prog, pc + 1);
+    const int code = cur.head & 7;
+    const int sub = cur.head >> 3;
+    switch (code) {
+      case kOpTerm: {
+        float p;
+        const int pk = sub & kTermPMask;
+        const float xa = t.lo[cur.a * t.stride + t.tid];
+        if (pk == kTermProd) {
+          p = __fmul_rn(xa, t.lo[cur.b * t.stride + t.tid]);
+        } else if (pk == kTermSqr) {
+          p = __fmul_rn(xa, xa);
+        } else {
+          p = xa;
+        }
+        if (sub & kTermHasC) p = __fmul_rn(cur.c32.clo, p);
+        if (sub & kTermInit) acc = p;
+        else if (sub & kTermSub) acc = __fsub_rn(acc, p);
+        else acc = __fadd_rn(acc, p);
+        break;
+      }
+      case kOpGeneric: {
+        const float a = pfetch32(t, acc, cur, cur.modes & 3, cur.a);
+        const float b = pfetch32(t, acc, cur, (cur.modes >> 2) & 3, cur.b);
+        t.slo[cur.dst * t.stride + t.tid] = pt32_generic((uint8_t)sub, a, b, (int)(int16_t)cur.b);
+        break;
+      }
+      case kOpStoreAcc:
+        t.slo[cur.dst * t.stride + t.tid] = acc;
+        break;
+      case kOpLoadAcc:
+        acc = pfetch32(t, acc, cur, cur.modes & 3, cur.a);
+        break;
+      case kOpConstToSlot:
+        t.slo[cur.dst * t.stride + t.tid] = cur.c32.clo;
+        break;
+      case kOpCheck: {
+        const double v = (double)pfetch32(t, acc, cur, cur.modes & 3, cur.a);
+        const bool ok = (sub == 0) ? (v <= cur.c) : almost_equal(v, cur.c);
+        out.feasible = out.feasible && ok;
+        break;
+      }
+      case kOpObjective:
+        out.obj = pfetch32(t, acc, cur, cur.modes & 3, cur.a);
+        out.has_obj = true;
+        break;
+      default:
+        break;
+    }
+  }
+}
+
 // ---- region decode (region/decode.hpp:44-71), FMA form as compiled on
 // the device, and the sampler (graph/subregion_sampler.cuh:53-120) ----
 // The part of slot `s` that child `r` of a parent takes: (r / prefix) %

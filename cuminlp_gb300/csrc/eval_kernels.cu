@@ -83,11 +83,29 @@ size_t eval_smem_bytes(int n_slots, int max_slots, bool fp32, int threads)
   return ((2 * t) * (size_t)(n_slots + max_slots) + 4 * (size_t)max_slots) * (size_t)threads;
 }
 
-// Writes the verdict of child g (kModes as in eval_children).
+// Writes the verdict of child g of parent k (kModes as in eval_children).
 template <typename T, int kMode>
-__device__ __forceinline__ void write_verdict(const EvalArgs& a, uint64_t g, const Verdict<T>& v, double gub)
+__device__ __forceinline__ void write_verdict(const EvalArgs& a, uint64_t g, uint64_t k, const Verdict<T>& v,
+                                              double gub)
 {
-  const double lb = (double)v.obj.lo;
+  double lb = (double)v.obj.lo;
+  if (kMode == 5) {
+    // the parent's certified bound holds for every child box inside it
+    const double plb = a.parent_lb[k];
+    lb = plb > lb ? plb : lb;
+    a.out_lb[g] = lb;
+    // a survivor whose bound lies within the band below the incumbent goes
+    // to the FP64 pass, which may prune it; below the band FP64 could not
+    a.out_flag[g] = v.excluded  ? kChildInfeasible
+                    : lb > gub  ? kChildDominated
+                    : lb >= certify_floor(gub) ? kChildScreened
+                                               : kChildEligible;
+    return;
+  }
+  if (kMode == 3 && a.parent_lb != nullptr) {  // lazy form's certify pass
+    const double plb = a.parent_lb[k];
+    lb = plb > lb ? plb : lb;
+  }
   if (kMode == 0) {
     a.out_lb[g] = lb;
     if (a.out_ub) a.out_ub[g] = (double)v.obj.hi;
@@ -185,7 +203,7 @@ __device__ void eval_children_grouped(const EvalArgs& a, const S* plo, const S* 
     if constexpr (kMode == 4) {
       aggregate_fold(a, live && lane == 0, r, v);
     } else {
-      if (live && lane == 0) write_verdict<T, kMode>(a, g, v, gub);
+      if (live && lane == 0) write_verdict<T, kMode>(a, g, k, v, gub);
     }
   }
 }
@@ -194,6 +212,9 @@ __device__ void eval_children_grouped(const EvalArgs& a, const S* plo, const S* 
 // kMode 1: solver FP64 -> out_lb, out_flag = ChildState
 // kMode 2: solver FP32 screen -> out_lb (FP32 bound), out_flag = ChildState
 // kMode 3: solver FP64 certify of a child list
+// kMode 4: aggregate bounder fold
+// kMode 5: solver lazy form, FP32 -> out_lb = max(FP32 bound, parent's
+//          certified bound), out_flag = ChildState
 template <typename T, int kMode, typename S>
 __device__ __forceinline__ void eval_children(const EvalArgs& a, const S* plo, const S* phi)
 {
@@ -252,19 +273,7 @@ __device__ __forceinline__ void eval_children(const EvalArgs& a, const S* plo, c
       continue;
     }
     const Verdict<T> v = run_interval<T, ChildVars<T, S>>(a.prog, a.prog_len, cv, t);
-    const double lb = (double)v.obj.lo;
-    if (kMode == 0) {
-      a.out_lb[g] = lb;
-      if (a.out_ub) a.out_ub[g] = (double)v.obj.hi;
-      // FP64: the reference predicate; FP32: not proven violated
-      a.out_flag[g] = (uint8_t)(sizeof(T) == 8 ? v.feasible : !v.excluded);
-    } else if (kMode == 2) {
-      a.out_lb[g] = lb;
-      a.out_flag[g] = v.excluded ? kChildInfeasible : (lb > gub ? kChildDominated : kChildScreened);
-    } else {
-      a.out_lb[g] = lb;
-      a.out_flag[g] = !v.feasible ? kChildInfeasible : (lb > gub ? kChildDominated : kChildEligible);
-    }
+    write_verdict<T, kMode>(a, g, k, v, gub);
   }
 }
 
@@ -344,23 +353,73 @@ __device__ __forceinline__ void stage_point(const SampleArgs& a, const Tile<doub
   }
 }
 
-// Sampling with groups of 2^lg lanes per child (see eval_children_grouped):
-// every lane stages the whole point in its own column, runs its segments
-// of the point program, and lane 0 of the group scores the combined result.
-__device__ void sample_children_grouped(const SampleArgs& a, const Tile<double>& t, uint64_t total,
-                                        uint64_t salt_base, double gub, int lg, Cand& best,
-                                        unsigned long long& rejected)
+// The chunk of children [32c, 32c + 32) of the lazy form: the child and
+// sample with the smallest FP32 value (ties: the first child, then the
+// first sample).  Returns false when no point of the chunk is feasible in
+// FP32.
+__device__ __forceinline__ bool chunk_pick(const Best32* __restrict__ cbest, uint64_t c, uint64_t total, uint64_t& g,
+                                           uint64_t& i)
+{
+  float best = INFINITY;
+  const uint64_t g0 = c << kChunkLog2;
+  const uint64_t g1 = total < g0 + (1ULL << kChunkLog2) ? total : g0 + (1ULL << kChunkLog2);
+  for (uint64_t x = g0; x < g1; ++x) {
+    const Best32 b = cbest[x];
+    if (b.value < best) {
+      best = b.value;
+      g = x;
+      i = b.i;
+    }
+  }
+  return best < INFINITY;
+}
+
+// Variables v = lane, lane + G, ... of the point of sample i of child
+// (k, r), written into the group's column t.tid (see stage_point).
+__device__ __forceinline__ void stage_point_part(const SampleArgs& a, const Tile<double>& t, uint64_t k, uint64_t r,
+                                                 uint64_t i, uint64_t salt, bool fathom, int lane, int G)
+{
+  const SlotPlan* sp = a.pinfo ? a.slots + k * (uint64_t)a.max_slots : nullptr;
+  const uint32_t count = a.pinfo ? a.pinfo[k].count : 0;
+  for (int v = lane; v < a.n_vars; v += G) {
+    double lo = a.plo[(uint64_t)v * a.pstride + k];
+    double hi = a.phi[(uint64_t)v * a.pstride + k];
+    for (uint32_t j = 0; j < count; ++j) {
+      if (sp[j].vid == (uint32_t)v) {
+        slot_bounds(sp[j], lo, hi, slot_part(r, sp[j]), lo, hi);
+        break;
+      }
+    }
+    t.lo[v * t.stride + t.tid] = fathom ? lo : sample_value(a.var_kinds[v] != 0, lo, hi, (uint64_t)v, i, r, salt);
+  }
+}
+
+// Sampling with groups of 2^lg lanes per point (see eval_children_grouped):
+// the G lanes of a group stage the point together into one shared-memory
+// column (lane j writes variables j, j + G, ...), each runs its segments of
+// the point program, and lane 0 of the group scores the combined result.
+// A block holds blockDim.x >> lg_min columns, so a large point costs
+// 8 * n_vars / G bytes per thread.  An item is a child (all its samples), or
+// in the lazy form's chunk mode a chunk (the one point chunk_pick chose).
+// The loop bound is per block, so every lane of a warp reaches the
+// shuffles and warp barriers.
+__device__ void sample_children_grouped(const SampleArgs& a, Tile<double> t, uint64_t total, uint64_t salt_base,
+                                        double gub, int lg, Cand& best, unsigned long long& rejected)
 {
   const int B = blockDim.x;
   const int G = 1 << lg;
   const int lane = threadIdx.x & (G - 1);
+  t.tid = (int)((threadIdx.x & ~(unsigned)(G - 1)) >> a.lg_min);  // the group's column
+  const bool chunked = a.cbest != nullptr;
+  const uint64_t items = chunked ? (total + (1ULL << kChunkLog2) - 1) >> kChunkLog2 : total;
   const uint64_t per_block = (uint64_t)(B >> lg);
-  const uint64_t S_loop = a.exact ? 1 : a.S;
-  for (uint64_t base = (uint64_t)blockIdx.x * per_block; base < total; base += (uint64_t)gridDim.x * per_block) {
-    const uint64_t g = base + (threadIdx.x >> lg);
-    bool live = g < total;
-    uint64_t k = 0, r = 0;
+  const uint64_t S_loop = (a.exact || chunked) ? 1 : a.S;
+  for (uint64_t base = (uint64_t)blockIdx.x * per_block; base < items; base += (uint64_t)gridDim.x * per_block) {
+    const uint64_t item = base + (threadIdx.x >> lg);
+    bool live = item < items;
+    uint64_t g = item, i0 = 0, k = 0, r = 0;
     bool fathom = a.exact != 0;
+    if (live && chunked) live = chunk_pick(a.cbest, item, total, g, i0);
     if (live) {
       child_of(a.log2C, g, k, r);
       uint64_t nreg = ~0ULL;
@@ -370,23 +429,23 @@ __device__ void sample_children_grouped(const SampleArgs& a, const Tile<double>&
         fathom = fathom || pi.fathom;
       }
       if (r >= nreg) live = false;
-      if (live && a.state != nullptr && !fathom) {
+      if (live && !chunked && a.state != nullptr && !fathom) {
         const uint8_t st = a.state[g];
         live = a.sample_all ? (st != kChildNone) : (st == kChildEligible);
       }
     }
     const uint64_t salt = a.salt_base_dev ? salt_base + k + 1 : a.salt;
     const uint64_t S = fathom ? 1 : a.S;
-    for (uint64_t i = 0; i < S_loop; ++i) {
-      const bool act = live && i < S;
+    for (uint64_t j = 0; j < S_loop; ++j) {
+      const uint64_t i = chunked ? i0 : j;
+      const bool act = live && (chunked || j < S);
+      if (act) stage_point_part(a, t, k, r, i, salt, fathom, lane, G);
+      __syncwarp();
       PointVerdict pv;
       pv.obj = INFINITY;
       pv.feasible = true;
       pv.has_obj = false;
-      if (act) {
-        stage_point(a, t, k, r, i, salt, fathom);
-        pv = run_point_lane(a.prog, a.sched, lg, lane, t);
-      }
+      if (act) pv = run_point_lane(a.prog, a.sched, lg, lane, t);
       pv = group_point_verdict(pv, G);
       if (act && lane == 0) {
         double value = (pv.feasible && !(pv.obj != pv.obj)) ? pv.obj : INFINITY;
@@ -397,6 +456,7 @@ __device__ void sample_children_grouped(const SampleArgs& a, const Tile<double>&
         const Cand c = {value, (uint32_t)k, 0, r * S + i};
         if (value < INFINITY && cand_less(c, best)) best = c;
       }
+      __syncwarp();  // the column is restaged next
     }
   }
 }
@@ -409,12 +469,14 @@ __global__ void __launch_bounds__(kEvalThreads) sample_children_kernel(const Sam
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double* base = reinterpret_cast<double*>(smem_raw);
   const int B = blockDim.x;
+  // one point column per 2^lg_min threads (slots follow the variables)
+  const int cols = B >> a.lg_min;
   Tile<double> t;
   t.lo = base;
   t.hi = base;  // unused by the point program
-  t.slo = base + (size_t)a.n_vars * B;
+  t.slo = base + (size_t)a.n_vars * cols;
   t.shi = t.slo;
-  t.stride = B;
+  t.stride = cols;
   t.tid = threadIdx.x;
 
   if (a.done != nullptr && *a.done) {
@@ -427,9 +489,34 @@ __global__ void __launch_bounds__(kEvalThreads) sample_children_kernel(const Sam
   Cand best = {INFINITY, 0xffffffffu, 0, ~0ULL};
   unsigned long long rejected = 0;
 
-  const int lg = a.sched != nullptr ? lanes_per_box(total, a.capacity, a.g_max) : 0;
+  const uint64_t chunks = (total + (1ULL << kChunkLog2) - 1) >> kChunkLog2;
+  int lg = a.sched != nullptr ? lanes_per_box(a.cbest != nullptr ? chunks : total, a.capacity, a.g_max) : 0;
+  if (lg < a.lg_min) lg = a.lg_min;
   if (lg > 0) sample_children_grouped(a, t, total, salt_base, gub, lg, best, rejected);
-  for (uint64_t g = (uint64_t)blockIdx.x * B + threadIdx.x; lg == 0 && g < total; g += (uint64_t)gridDim.x * B) {
+  if (lg == 0 && a.cbest != nullptr) {
+    // lazy form: each chunk's FP32-best point, evaluated in FP64
+    for (uint64_t c = (uint64_t)blockIdx.x * B + threadIdx.x; c < chunks; c += (uint64_t)gridDim.x * B) {
+      uint64_t g = 0, i = 0;
+      if (!chunk_pick(a.cbest, c, total, g, i)) continue;
+      uint64_t k, r;
+      child_of(a.log2C, g, k, r);
+      bool fathom = a.exact != 0;
+      if (a.pinfo != nullptr) fathom = fathom || a.pinfo[k].fathom;
+      const uint64_t salt = a.salt_base_dev ? salt_base + k + 1 : a.salt;
+      stage_point(a, t, k, r, i, salt, fathom);
+      const PointVerdict pv = run_point(a.prog, a.prog_len, t);
+      double value = (pv.feasible && !(pv.obj != pv.obj)) ? pv.obj : INFINITY;
+      if (fathom && a.state != nullptr && value < INFINITY && !admissible(a, t)) {
+        if (value < gub) ++rejected;
+        value = INFINITY;
+      }
+      const uint64_t S = fathom ? 1 : a.S;
+      const Cand cand = {value, (uint32_t)k, 0, r * S + i};
+      if (value < INFINITY && cand_less(cand, best)) best = cand;
+    }
+  }
+  for (uint64_t g = (uint64_t)blockIdx.x * B + threadIdx.x; a.cbest == nullptr && lg == 0 && g < total;
+       g += (uint64_t)gridDim.x * B) {
     uint64_t k, r;
     child_of(a.log2C, g, k, r);
     bool fathom = a.exact != 0;
@@ -480,6 +567,72 @@ __global__ void __launch_bounds__(kEvalThreads) sample_children_kernel(const Sam
   if (a.rejected != nullptr) {
     for (int off = 16; off > 0; off >>= 1) rejected += __shfl_down_sync(0xffffffffu, rejected, off);
     if ((threadIdx.x & 31) == 0 && rejected) atomicAdd(a.rejected, rejected);
+  }
+}
+
+// The lazy form's sample screen: every sampled child's S points (or its
+// exact point) in FP32, keeping per child the smallest FP32 value and its
+// sample index in cbest[g].  Children not sampled get +inf.  One lane per
+// child; no barriers.
+__global__ void __launch_bounds__(kEvalThreads) sample_screen_kernel(const SampleArgs a)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float* base = reinterpret_cast<float*>(smem_raw);
+  const int B = blockDim.x;
+  Tile<float> t;
+  t.lo = base;
+  t.hi = base;
+  t.slo = base + (size_t)a.n_vars * B;
+  t.shi = t.slo;
+  t.stride = B;
+  t.tid = threadIdx.x;
+  if (a.done != nullptr && *a.done) return;
+  const uint64_t total = a.n_children_dev ? *a.n_children_dev : a.n_children;
+  const uint64_t salt_base = a.salt_base_dev ? *a.salt_base_dev : 0;
+  for (uint64_t g = (uint64_t)blockIdx.x * B + threadIdx.x; g < total; g += (uint64_t)gridDim.x * B) {
+    Best32 best = {INFINITY, 0};
+    uint64_t k, r;
+    child_of(a.log2C, g, k, r);
+    bool fathom = a.exact != 0;
+    uint64_t nreg = ~0ULL;
+    if (a.pinfo != nullptr) {
+      const ParentInfo pi = a.pinfo[k];
+      nreg = pi.nreg;
+      fathom = fathom || pi.fathom;
+    }
+    bool take = r < nreg;
+    if (take && a.state != nullptr && !fathom) {
+      const uint8_t st = a.state[g];
+      take = a.sample_all ? (st != kChildNone) : (st == kChildEligible);
+    }
+    if (take) {
+      const SlotPlan* sp = a.pinfo ? a.slots + k * (uint64_t)a.max_slots : nullptr;
+      const uint32_t count = a.pinfo ? a.pinfo[k].count : 0;
+      const uint64_t salt = a.salt_base_dev ? salt_base + k + 1 : a.salt;
+      const uint64_t S = fathom ? 1 : a.S;
+      for (uint64_t i = 0; i < S; ++i) {
+        for (int v = 0; v < a.n_vars; ++v) {
+          double lo = a.plo[(uint64_t)v * a.pstride + k];
+          double hi = a.phi[(uint64_t)v * a.pstride + k];
+          for (uint32_t j = 0; j < count; ++j) {
+            if (sp[j].vid == (uint32_t)v) {
+              slot_bounds(sp[j], lo, hi, slot_part(r, sp[j]), lo, hi);
+              break;
+            }
+          }
+          const double x = fathom ? lo : sample_value(a.var_kinds[v] != 0, lo, hi, (uint64_t)v, i, r, salt);
+          t.lo[v * B + t.tid] = __double2float_rn(x);
+        }
+        PointVerdict32 pv;
+        pv.obj = INFINITY;
+        pv.feasible = true;
+        pv.has_obj = false;
+        point_range32(a.prog, 0, a.prog_len, t, pv);
+        const float value = (pv.feasible && !(pv.obj != pv.obj)) ? pv.obj : INFINITY;
+        if (value < best.value) best = Best32{value, (uint32_t)i};
+      }
+    }
+    a.cbest[g] = best;
   }
 }
 
@@ -565,9 +718,17 @@ cudaError_t launch_fma_peak(int precision, int grid, int threads, int iters, voi
 // host launchers
 // ---------------------------------------------------------------------
 
-size_t sample_smem_bytes(int n_vars, int n_slots, int threads)
+size_t sample_smem_bytes(int n_vars, int n_slots, int threads, int lg_min)
 {
-  return 8 * (size_t)(n_vars + n_slots) * threads;
+  return 8 * (size_t)(n_vars + n_slots) * (size_t)(threads >> lg_min);
+}
+
+int sample_lg_min(int n_vars, int n_slots, bool has_sched, int threads)
+{
+  if (!has_sched) return 0;  // shared slots: one column per thread
+  int lg = 0;
+  while (lg < 5 && sample_smem_bytes(n_vars, n_slots, threads, lg) > kSampleColumnBytes) ++lg;
+  return lg;
 }
 
 // Kernel attributes are set once per device, before any launch, so that
@@ -592,7 +753,9 @@ cudaError_t set_eval_kernel_attributes(int max_smem)
   if (e == cudaSuccess) e = allow_dynamic_smem(eval_children_kernel<double, 4>, max_smem);
   if (e == cudaSuccess) e = allow_dynamic_smem(eval_children_kernel<float, 0>, max_smem);
   if (e == cudaSuccess) e = allow_dynamic_smem(eval_children_kernel<float, 2>, max_smem);
+  if (e == cudaSuccess) e = allow_dynamic_smem(eval_children_kernel<float, 5>, max_smem);
   if (e == cudaSuccess) e = allow_dynamic_smem(sample_children_kernel, max_smem);
+  if (e == cudaSuccess) e = allow_dynamic_smem(sample_screen_kernel, max_smem);
   return e;
 }
 
@@ -601,8 +764,9 @@ int eval_kernel_occupancy(int mode, bool fp32, size_t smem, int threads)
   int blocks = 0;
   cudaError_t e;
   if (fp32) {
-    e = mode == 0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, eval_children_kernel<float, 0>, threads, smem)
-                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, eval_children_kernel<float, 2>, threads, smem);
+    e = mode == 0   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, eval_children_kernel<float, 0>, threads, smem)
+        : mode == 5 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, eval_children_kernel<float, 5>, threads, smem)
+                    : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, eval_children_kernel<float, 2>, threads, smem);
   } else {
     e = mode == 0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, eval_children_kernel<double, 0>, threads, smem)
         : mode == 1
@@ -631,6 +795,7 @@ cudaError_t launch_eval(const EvalArgs& a, int mode, bool fp32, int grid, int th
 {
   if (fp32) {
     if (mode == 0) return launch_eval_t<float, 0>(a, grid, threads, s);
+    if (mode == 5) return launch_eval_t<float, 5>(a, grid, threads, s);
     return launch_eval_t<float, 2>(a, grid, threads, s);
   }
   if (mode == 0) return launch_eval_t<double, 0>(a, grid, threads, s);
@@ -639,9 +804,27 @@ cudaError_t launch_eval(const EvalArgs& a, int mode, bool fp32, int grid, int th
   return launch_eval_t<double, 3>(a, grid, threads, s);
 }
 
+size_t sample_screen_smem_bytes(int n_vars, int n_slots, int threads)
+{
+  return 4 * (size_t)(n_vars + n_slots) * threads;
+}
+
+cudaError_t launch_sample_screen(const SampleArgs& a, int grid, int threads, cudaStream_t s)
+{
+  sample_screen_kernel<<<grid, threads, sample_screen_smem_bytes(a.n_vars, a.n_slots, threads), s>>>(a);
+  return cudaGetLastError();
+}
+
+int sample_screen_occupancy(size_t smem, int threads)
+{
+  int blocks = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, sample_screen_kernel, threads, smem);
+  return e == cudaSuccess ? blocks : 1;
+}
+
 cudaError_t launch_sample(const SampleArgs& a, int grid, int threads, cudaStream_t s)
 {
-  const size_t smem = sample_smem_bytes(a.n_vars, a.n_slots, threads);
+  const size_t smem = sample_smem_bytes(a.n_vars, a.n_slots, threads, a.lg_min);
   sample_children_kernel<<<grid, threads, smem, s>>>(a);
   return cudaGetLastError();
 }

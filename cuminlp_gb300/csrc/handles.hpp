@@ -15,6 +15,7 @@ struct cmn_problem {
   int device = 0;
   cmn::Instr* d_prog64 = nullptr;
   cmn::Instr* d_prog32 = nullptr;
+  cmn::Instr* d_prog32p = nullptr;  // FP32 point program (the lazy form's sample screen)
   int32_t* d_kinds = nullptr;
   double* d_root_lb = nullptr;
   double* d_root_ub = nullptr;

@@ -71,6 +71,37 @@ __host__ __device__ inline bool cand_less(const Cand& a, const Cand& b)
   return a.e < b.e;
 }
 
+// The lazy form's sample screen, per child slot: the smallest FP32 point
+// value among its samples (+inf: none feasible in FP32, or not sampled) and
+// that sample's index.
+struct Best32 {
+  float value;
+  uint32_t i;
+};
+
+// The lazy form certifies a child in FP64 as soon as it is bounded when its
+// FP32 bound lies within kCertifyBand * max(1, |incumbent|) below the
+// incumbent: there the FP32 rounding error can hide a prune, further below
+// FP64 would keep the child too.
+constexpr double kCertifyBand = 1.0 / 1024.0;
+
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+inline double certify_floor(double gub)
+{
+#ifdef __CUDA_ARCH__
+  return __dsub_rn(gub, __dmul_rn(kCertifyBand, fmax(1.0, fabs(gub))));
+#else
+  return gub - kCertifyBand * std::fmax(1.0, std::fabs(gub));
+#endif
+}
+
+// Children per chunk of the lazy form's sample verification: the point
+// with the smallest FP32 value among the chunk's children is evaluated
+// again in FP64 and is the chunk's incumbent candidate.
+constexpr int kChunkLog2 = 5;
+
 // Arguments of the child evaluation kernels.
 struct EvalArgs {
   const Instr* prog;
@@ -93,6 +124,7 @@ struct EvalArgs {
   const double* gub;              // incumbent at the start of the iteration
   const uint32_t* done;           // solver: nonzero once the search stopped
   const uint32_t* use_screen;     // FP32 screen: zero passes every child to the certify pass
+  const double* parent_lb;        // lazy form: the parents' certified FP64 lower bounds
   // lane groups (null sched: one lane per box); see Program::sched
   const int32_t* sched;
   int g_max;
@@ -138,6 +170,10 @@ struct SampleArgs {
   const int32_t* sched;      // lane groups, as EvalArgs
   int g_max;
   uint64_t capacity;
+  int lg_min;                // points are shared by at least 2^lg_min lanes (sample_lg_min)
+  // lazy form: the sample screen writes `cbest` (prog = the FP32 point
+  // program); the sampler then evaluates only each chunk's best in FP64
+  Best32* cbest;
 };
 
 }  // namespace cmn

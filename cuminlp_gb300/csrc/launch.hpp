@@ -20,13 +20,25 @@ constexpr int kEvalThreads = 128;
 
 // interval kernels: program slots plus `max_slots` split variables per thread
 size_t eval_smem_bytes(int n_slots, int max_slots, bool fp32, int threads);
-size_t sample_smem_bytes(int n_vars, int n_slots, int threads);
+// sampler: one point column (variables + slots, FP64) per 2^lg_min threads
+size_t sample_smem_bytes(int n_vars, int n_slots, int threads, int lg_min);
+// Point columns of a block stay within this many bytes: lanes share a
+// column (2^lg_min of them) until they do, so the sampler's residency does
+// not fall with the number of variables.  Programs with shared slots have
+// no lane schedule and keep one column per thread.
+constexpr size_t kSampleColumnBytes = 32 * 1024;
+int sample_lg_min(int n_vars, int n_slots, bool has_sched, int threads);
+size_t sample_screen_smem_bytes(int n_vars, int n_slots, int threads);
 
 // mode 0: role / raw boxes; 1: solver FP64; 2: solver FP32 screen (fp32
 // must be true); 3: solver FP64 certify over EvalArgs::list; 4: aggregate
-// bounder (FP64, per-child fold into EvalArgs::agg_keys)
+// bounder (FP64, per-child fold into EvalArgs::agg_keys); 5: solver lazy
+// form, FP32 children bounded by the parents' certified bounds (fp32 true)
 cudaError_t launch_eval(const EvalArgs& a, int mode, bool fp32, int grid, int threads, cudaStream_t s);
 cudaError_t launch_sample(const SampleArgs& a, int grid, int threads, cudaStream_t s);
+// the lazy form's FP32 sample screen (SampleArgs::cbest out, prog = the
+// FP32 point program)
+cudaError_t launch_sample_screen(const SampleArgs& a, int grid, int threads, cudaStream_t s);
 cudaError_t launch_reduce_cand(const Cand* block_best, int n, Cand* out, cudaStream_t s);
 cudaError_t launch_witness(const Cand* cand, const double* plo, const double* phi, uint64_t pstride,
                            const ParentInfo* pinfo, const SlotPlan* slots, int max_slots, const int32_t* kinds,
@@ -37,6 +49,7 @@ cudaError_t launch_witness(const Cand* cand, const double* plo, const double* ph
 int max_dynamic_smem();
 // Resident blocks per SM of the sampler at this shared-memory size.
 int sample_kernel_occupancy(size_t smem, int threads);
+int sample_screen_occupancy(size_t smem, int threads);
 int sm_count();
 
 }  // namespace cmn

@@ -11,14 +11,15 @@
 // (kScratchBytes) until the process exits.
 //
 // The array's name is a host-side stand-in, not a device address, in host
-// code: its address is looked up once per device with cudaGetSymbolAddress
-// and that pointer is what the kernels receive.
+// code: its address is looked up with cudaGetSymbolAddress, with the
+// problem's device current, on every call (a lookup is cheap, and a device
+// reset between calls cannot leave a stale address behind), and that
+// pointer is what the kernels receive.
 #include <cuda_runtime.h>
 
 #include <cfloat>
 #include <cstdint>
 #include <cstring>
-#include <mutex>
 #include <string>
 
 #include "../../include/cuminlp_gb300.h"
@@ -33,7 +34,6 @@ namespace {
 constexpr size_t kScratchBytes = 512 * 1024;  // per device
 constexpr int64_t kMaxVars = 8192;
 constexpr int kMaxBlocks = 4096;
-constexpr int kMaxDevices = 64;
 
 // slot table and parent record, staged together with one copy
 struct StagedSlots {
@@ -43,29 +43,29 @@ struct StagedSlots {
 
 constexpr size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
-std::mutex g_mu;
-unsigned char* g_scratch_addr[kMaxDevices] = {};
-
 }  // namespace
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-// Device address of the scratch array on the current device, looked up on
-// the first call per device.
-static cmn_status scratch_on_device(int dev, unsigned char** out)
+// Device address of the scratch array on the current device.
+static cmn_status scratch_on_device(unsigned char** out)
 {
-  if (dev < 0 || dev >= kMaxDevices) return set_error(CMN_INVALID_CONFIGURATION, "device ordinal above 63");
-  std::lock_guard<std::mutex> lock(g_mu);
-  if (g_scratch_addr[dev] == nullptr) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess)
-      return set_error(CMN_CUDA_ERROR, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
-    g_scratch_addr[dev] = static_cast<unsigned char*>(p);
-  }
-  *out = g_scratch_addr[dev];
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess)
+    return set_error(CMN_CUDA_ERROR, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+  *out = static_cast<unsigned char*>(p);
   return CMN_OK;
 }
+
+// Restores the caller's current device on every return path.
+struct DeviceGuard {
+  int prev = -1;
+  ~DeviceGuard()
+  {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
 
 #define NA_CK(call)                                                                                            \
   do {                                                                                                         \
@@ -104,16 +104,21 @@ extern "C" cmn_status cmn_sample_noalloc(const cmn_problem* p, const uint8_t* sl
   if (running != n_regions) return set_error(CMN_SHAPE_MISMATCH, "the product of widths does not equal n_regions");
   staged.info = ParentInfo{(uint32_t)slot_count, 0, n_regions};
 
+  DeviceGuard guard;
+  NA_CK(cudaGetDevice(&guard.prev));
   NA_CK(cudaSetDevice(p->device));
   NA_CK(ensure_kernel_attributes());
   unsigned char* base = nullptr;
-  cmn_status st = scratch_on_device(p->device, &base);
+  cmn_status st = scratch_on_device(&base);
   if (st != CMN_OK) return st;
 
   const int threads = kEvalThreads;
-  const size_t smem = sample_smem_bytes((int)n, p->prog.n_slots, threads);
+  const int lg_min = sample_lg_min((int)n, p->prog.n_slots, p->d_sched != nullptr, threads);
+  const size_t smem = sample_smem_bytes((int)n, p->prog.n_slots, threads, lg_min);
   if (smem > (size_t)max_dynamic_smem())
-    return set_error(CMN_INVALID_CONFIGURATION, "problem too large for the sampler's shared-memory tile");
+    return set_error(CMN_INVALID_CONFIGURATION,
+                     "the sampler's point columns (" + std::to_string(smem) + " B per block) do not fit in shared "
+                     "memory; a program with shared slots keeps one column of n_vars + slots doubles per thread");
   int occ = sample_kernel_occupancy(smem, threads);
   if (occ < 1) occ = 1;
   const uint64_t need = (n_regions + threads - 1) / threads;
@@ -162,6 +167,11 @@ extern "C" cmn_status cmn_sample_noalloc(const cmn_problem* p, const uint8_t* sl
   a.salt = salt;
   a.exact = 0;
   a.block_best = d_blocks;  // every block writes its own entry
+  // lane groups and shared point columns, as the sampler role uses them
+  a.sched = p->d_sched;
+  a.g_max = p->prog.group_max;
+  a.capacity = (uint64_t)grid * threads;
+  a.lg_min = lg_min;
   NA_CK(launch_sample(a, grid, threads, s));
   NA_CK(launch_reduce_cand(d_blocks, grid, d_result, s));
   NA_CK(launch_witness(d_result, d_box, d_box + 1, 2, &d_slots->info, d_slots->slots, 64, p->d_kinds, (int)n,

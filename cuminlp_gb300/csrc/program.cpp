@@ -26,6 +26,19 @@ float d2f_ru(double x)
   return f;
 }
 
+// FP64 -> FP32 rounded to nearest, ties to even, whatever the host's
+// current rounding mode
+float d2f_rn(double x)
+{
+  const float lo = d2f_rd(x), hi = d2f_ru(x);
+  if (lo == hi || std::isnan(x)) return lo;
+  const double dl = x - (double)lo, dh = (double)hi - x;
+  if (dl != dh) return dl < dh ? lo : hi;
+  uint32_t bits;
+  std::memcpy(&bits, &lo, 4);
+  return (bits & 1u) ? hi : lo;
+}
+
 static bool is_unary(int op)
 {
   return op == CMN_OP_SQR || op == CMN_OP_NEG || op == CMN_OP_EXP || op == CMN_OP_LOG || op == CMN_OP_SQRT ||
@@ -272,8 +285,10 @@ class Compiler {
     out_.n_slots = max_slots_;
     build_schedule();
     out_.code32 = out_.code64;
+    out_.code32p = out_.code64;
     for (size_t k = 0; k < out_.code64.size(); ++k) {
       Instr& s = out_.code32[k];
+      Instr& q = out_.code32p[k];
       const Instr& d = out_.code64[k];
       const int code = d.head & 7;
       if (code == kOpCheck) continue;  // rhs stays FP64
@@ -285,6 +300,8 @@ class Compiler {
         const double c = d.c;
         s.c32.clo = d2f_rd(c);
         s.c32.chi = d2f_ru(c);
+        q.c32.clo = d2f_rn(c);
+        q.c32.chi = q.c32.clo;
       }
     }
   }

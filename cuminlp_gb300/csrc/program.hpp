@@ -33,6 +33,7 @@ cmn_status build_host_problem(const cmn_problem_desc* desc, HostProblem& out, st
 struct Program {
   std::vector<Instr> code64;  // FP64 interval / point program
   std::vector<Instr> code32;  // FP32 outward-rounded screen program
+  std::vector<Instr> code32p; // FP32 point program (constants rounded to nearest)
   int n_slots = 0;
   bool interval_supported = true;  // every reachable op has an interval form
   std::string unsupported_op;
@@ -57,5 +58,6 @@ void compile_program(const HostProblem& p, Program& out);
 // Outward conversion of an FP64 constant to an FP32 pair.
 float d2f_rd(double x);
 float d2f_ru(double x);
+float d2f_rn(double x);
 
 }  // namespace cmn

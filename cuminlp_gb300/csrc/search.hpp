@@ -109,6 +109,8 @@ struct SolverCfg {
   int g_max;                 // lanes per child at most (1: one lane per child)
   uint64_t eval_capacity;    // resident threads of the bound kernels
   uint64_t sample_capacity;  // resident threads of the sampler
+  int screen_grid;           // lazy form: blocks of the FP32 sample screen
+  int sample_lg_min;         // sampler point columns: one per 2^sample_lg_min lanes
 };
 
 struct SolverBufs {
@@ -135,6 +137,10 @@ struct SolverBufs {
   float* plo32;  // FP32 screen only: the same planes rounded outward
   float* phi32;
   uint32_t* pdepth;
+  // lazy form: the FP64 verdict of each staged parent (its certified lower
+  // bound, and whether the reference predicate keeps it)
+  double* plb;
+  uint8_t* pfeas;
   uint32_t* pslot;       // store slots of the next iteration's parents, in order
   ParentInfo* pinfo;
   SlotPlan* slots;
@@ -145,6 +151,7 @@ struct SolverBufs {
   // children
   double* clb;
   uint8_t* cstate;
+  Best32* cbest;         // lazy form: the FP32 sample screen's best per child
   uint32_t* list;        // certify list
   // compaction scratch
   uint32_t* block_counts;
@@ -156,6 +163,7 @@ struct SolverBufs {
   // problem
   const Instr* prog64;
   const Instr* prog32;
+  const Instr* prog32p;  // FP32 point program (the lazy form's sample screen)
   const int32_t* sched;  // lane schedules of the program (null: none)
   const int32_t* kinds;
   const double* root_lb;

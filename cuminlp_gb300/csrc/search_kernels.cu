@@ -1077,7 +1077,9 @@ __global__ void branch_kernel(const SolverCfg cfg, const SolverBufs b)
   const uint64_t E = d->n_parents;
   const int n = cfg.n_vars;
   const PolicyParams pp = {cfg.log2C, cfg.max_cycle, cfg.enumerate_cap, cfg.relative};
-  uint64_t fathomed = 0, fathomed_points = 0, bounded = 0;
+  const bool lazy = cfg.precision == CMN_PRECISION_FP32_LAZY;
+  const double gub = d->gub;
+  uint64_t fathomed = 0, fathomed_points = 0, bounded = 0, certified = 0, dropped = 0;
   EnumCand ec_local[kLocal > 0 ? kLocal : 1];
   BisCand bc_local[kLocal > 0 ? kLocal : 1];
   uint64_t heap_local[kLocal > 0 ? kLocal : 1];
@@ -1086,7 +1088,17 @@ __global__ void branch_kernel(const SolverCfg cfg, const SolverBufs b)
     BisCand* bc = kLocal > 0 ? bc_local : reinterpret_cast<BisCand*>(b.bis_scratch) + k * (uint64_t)n;
     uint64_t* heap = kLocal > 0 ? heap_local : b.heap_scratch + k * (uint64_t)n;
     SlotPlan* sp = b.slots + k * (uint64_t)cfg.max_slots;
-    const ParentInfo pi = bisection_policy(b.plo + k, b.phi + k, cfg.e_max, n, b.kinds, pp, ec, bc, heap, sp);
+    ParentInfo pi = bisection_policy(b.plo + k, b.phi + k, cfg.e_max, n, b.kinds, pp, ec, bc, heap, sp);
+    if (lazy) {
+      // the box's FP64 verdict, computed on selection: the reference
+      // predicate or the incumbent excludes it, so it is not expanded
+      ++certified;
+      const double plb = b.plb[k];
+      if (!b.pfeas[k] || plb > gub) {
+        pi = ParentInfo{0, 0, 0};
+        ++dropped;
+      }
+    }
     b.pinfo[k] = pi;
     if (pi.fathom) {
       ++fathomed;
@@ -1095,12 +1107,14 @@ __global__ void branch_kernel(const SolverCfg cfg, const SolverBufs b)
       bounded += pi.nreg;
     }
   }
-  unsigned long long c[3] = {fathomed, fathomed_points, bounded};
+  unsigned long long c[5] = {fathomed, fathomed_points, bounded, certified, dropped};
   block_sum(c);
   if (threadIdx.x == 0) {
     if (c[0]) atomicAdd((unsigned long long*)&b.dev->counters.fathomed, c[0]);
     if (c[1]) atomicAdd((unsigned long long*)&b.dev->counters.fathomed_points, c[1]);
     if (c[2]) atomicAdd((unsigned long long*)&b.dev->counters.bounded, c[2]);
+    if (c[3]) atomicAdd((unsigned long long*)&b.dev->counters.certified_fp64, c[3]);
+    if (c[4]) atomicAdd((unsigned long long*)&b.dev->counters.certify_pruned, c[4]);
   }
 }
 
@@ -1167,6 +1181,7 @@ __global__ void eval_count_kernel(const SolverCfg cfg, const SolverBufs b)
   if (d->done) return;
   const uint64_t n = d->n_children;
   const bool fp32 = cfg.precision == CMN_PRECISION_FP32_SCREEN;
+  const bool lazy = cfg.precision == CMN_PRECISION_FP32_LAZY;
   unsigned long long valid = 0, excluded = 0;
   for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n; g += (uint64_t)gridDim.x * blockDim.x) {
     const uint8_t s = b.cstate[g];
@@ -1179,8 +1194,8 @@ __global__ void eval_count_kernel(const SolverCfg cfg, const SolverBufs b)
   if (threadIdx.x == 0) {
     if (c[0]) atomicAdd((unsigned long long*)&d->iter_valid, c[0]);
     if (c[1]) atomicAdd((unsigned long long*)&d->iter_excluded, c[1]);
-    if (c[0] && fp32 && d->use_screen) atomicAdd((unsigned long long*)&d->counters.screened_fp32, c[0]);
-    if (c[0] && !fp32) atomicAdd((unsigned long long*)&d->counters.certified_fp64, c[0]);
+    if (c[0] && ((fp32 && d->use_screen) || lazy)) atomicAdd((unsigned long long*)&d->counters.screened_fp32, c[0]);
+    if (c[0] && !fp32 && !lazy) atomicAdd((unsigned long long*)&d->counters.certified_fp64, c[0]);
   }
 }
 
@@ -1340,6 +1355,30 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
     gather_parents_kernel<<<tiles(cfg.cap), kScanBlock, 0, s>>>(cfg, b, b.block_offsets);
   }
 
+  // (1b) lazy form: the FP64 verdict of every staged parent -- its bound
+  // has been an FP32 one (with its own parent's FP64 bound folded in) since
+  // it was appended
+  if (cfg.precision == CMN_PRECISION_FP32_LAZY) {
+    EvalArgs pa = {};
+    pa.prog = b.prog64;
+    pa.prog_len = cfg.prog_len;
+    pa.n_vars = cfg.n_vars;
+    pa.n_slots = cfg.n_slots;
+    pa.log2C = 0;  // one "child" per parent: the parent box itself
+    pa.plo = b.plo;
+    pa.phi = b.phi;
+    pa.pstride = cfg.e_max;
+    pa.n_children_dev = &b.dev->n_parents;
+    pa.done = &b.dev->done;
+    pa.out_lb = b.plb;
+    pa.out_flag = b.pfeas;
+    pa.sched = b.sched;
+    pa.g_max = cfg.g_max;
+    pa.capacity = cfg.eval_capacity;
+    cudaError_t e = launch_eval(pa, 0, false, eval_grid, kEvalThreads, s);
+    if (e != cudaSuccess) return e;
+  }
+
   // (2) branch
   {
     const int grid = (int)std::min<uint64_t>((cfg.e_max + 127) / 128, 2048);
@@ -1388,6 +1427,25 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
     ca.list_count = &b.dev->certify_count;
     e = launch_eval(ca, 3, false, eval_grid, kEvalThreads, s);
     if (e != cudaSuccess) return e;
+  } else if (cfg.precision == CMN_PRECISION_FP32_LAZY) {
+    ea.prog = b.prog32;
+    ea.plo32 = b.plo32;
+    ea.phi32 = b.phi32;
+    ea.parent_lb = b.plb;
+    e = launch_eval(ea, 5, true, eval_grid, kEvalThreads, s);
+    if (e != cudaSuccess) return e;
+    // the survivors within the band below the incumbent, in FP64
+    ScreenedChild sc{b};
+    compact(sc, max_children, &b.dev->n_children, &b.dev->certify_count, b, s);
+    scatter(sc, ListChild{b}, max_children, s, b);
+    EvalArgs ca = ea;
+    ca.prog = b.prog64;
+    ca.plo32 = nullptr;
+    ca.phi32 = nullptr;
+    ca.list = b.list;
+    ca.list_count = &b.dev->certify_count;
+    e = launch_eval(ca, 3, false, eval_grid, kEvalThreads, s);
+    if (e != cudaSuccess) return e;
   } else {
     ea.prog = b.prog64;
     e = launch_eval(ea, 1, false, eval_grid, kEvalThreads, s);
@@ -1399,6 +1457,8 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
     if (cfg.precision == CMN_PRECISION_FP32_SCREEN) {
       certify_count_kernel<<<1, 1, 0, s>>>(b);
       screen_policy_kernel<<<1, 1, 0, s>>>(cfg, b);
+    } else if (cfg.precision == CMN_PRECISION_FP32_LAZY) {
+      certify_count_kernel<<<1, 1, 0, s>>>(b);
     }
   }
   mark(marks, 2, s);
@@ -1431,6 +1491,17 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
   sa.sched = b.sched;
   sa.g_max = cfg.g_max;
   sa.capacity = cfg.sample_capacity;
+  sa.lg_min = cfg.sample_lg_min;
+  if (cfg.precision == CMN_PRECISION_FP32_LAZY) {
+    // FP32 screen of every sample, then each chunk's best in FP64
+    SampleArgs qa = sa;
+    qa.lg_min = 0;  // one FP32 column per thread
+    qa.prog = b.prog32p;
+    qa.cbest = b.cbest;
+    e = launch_sample_screen(qa, cfg.screen_grid, kEvalThreads, s);
+    if (e != cudaSuccess) return e;
+    sa.cbest = b.cbest;
+  }
   e = launch_sample(sa, sample_grid, kEvalThreads, s);
   if (e != cudaSuccess) return e;
   Cand* best = b.block_best + b.n_block_best - 1;  // last entry holds the result

@@ -196,7 +196,7 @@ def default_options(**kw) -> A.SolveOptions:
     lib().cmn_solve_options_default(C.byref(o))
     for k, v in kw.items():
         if k == "precision" and isinstance(v, str):
-            v = A.PRECISION_FP32_SCREEN if v.lower().startswith("fp32") else A.PRECISION_FP64
+            v = A.precision_code(v)
         if k == "known_primal_bound" and v is not None:
             o.has_known_primal = 1
         if v is None:

@@ -263,10 +263,18 @@ cmn_status cmn_enumerate(cmn_role* role, const double* box,
  * var_ids, widths, salt) does, with the same results, but allocates no
  * device memory: its scratch is one 512 KiB device array per GPU, held by
  * the library until the process exits.  Host inputs and outputs; `point`
- * receives n_vars doubles and out->point points at it.  Limits: at most
- * 8192 variables (larger problems get CMN_INVALID_CONFIGURATION).  The
- * first call on a device looks up the array's address on that device, so
- * make it before any stream capture.  All calls share the array and it
+ * receives n_vars doubles and out->point points at it.  Limits (beyond
+ * them the call returns CMN_INVALID_CONFIGURATION): at most 8192 variables
+ * (the array's share for the box and the witness), and the sampler's point
+ * columns must fit in one block's shared memory -- 8 * (n_vars + program
+ * slots) * 128 / G bytes, where G lanes share a point: up to 32 for a
+ * program without shared slots (every generated QCQP; n_vars + slots up to
+ * about 7,200 on GB300), 1 for a program with them (up to about 226).
+ * Every call looks up the array's address on the problem's device with
+ * cudaGetSymbolAddress; the first call on a device also loads the
+ * library's device code there, so make it before any stream capture.  The
+ * call makes the problem's device current and restores the caller's
+ * current device before it returns.  All calls share the array and it
  * keeps the last call's contents; calls that overlap on the GPU (several
  * streams or threads at once) race on it and must be serialised by the
  * caller.  `stream` is a cudaStream_t or NULL; the call returns after the
@@ -287,7 +295,13 @@ cmn_status cmn_sample_noalloc(const cmn_problem* problem,
  * ------------------------------------------------------------------- */
 typedef enum cmn_precision {
   CMN_PRECISION_FP64 = 0,            /* plain FP64 directed rounding */
-  CMN_PRECISION_FP32_SCREEN = 1      /* FP32 outward screen, FP64 certify */
+  CMN_PRECISION_FP32_SCREEN = 1,     /* FP32 outward screen, FP64 certify of
+                                        every survivor (the plain FP64
+                                        trajectory, bit for bit) */
+  CMN_PRECISION_FP32_LAZY = 2        /* solver only: children bounded in
+                                        FP32 only; a box's bound is certified
+                                        in FP64 when it is selected for
+                                        expansion (see cmn_solve_options) */
 } cmn_precision;
 
 /* `lo`/`hi` point at n_vars planes of `stride` doubles; outputs have
@@ -358,8 +372,12 @@ typedef struct cmn_counters {
   uint64_t dropped_viable;
   uint64_t dropped_dominated;
   uint64_t screened_fp32;      /* children evaluated by the FP32 screen */
-  uint64_t certified_fp64;     /* children evaluated in FP64 */
+  uint64_t certified_fp64;     /* boxes evaluated in FP64 (children, or
+                                  the selected parents of the lazy form) */
   uint64_t peak_frontier;
+  uint64_t certify_pruned;     /* lazy form: selected boxes whose FP64
+                                  bound is infeasible or above the
+                                  incumbent, so they are not expanded */
 } cmn_counters;
 
 typedef struct cmn_outcome {

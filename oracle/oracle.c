@@ -922,6 +922,65 @@ int orc_eval_point(const orc_problem* p, const double* x, double* obj,
   return 0;
 }
 
+/* Lazy form's sample screen: FP32 point evaluation, one round-to-nearest
+ * float operation per node, the point's variables and the constants
+ * rounded to nearest float; constraints by the point predicates on the
+ * float values widened to double.  PowN is binary powering (k < 0:
+ * 1 / x^|k|).  Restates point_range32 (csrc/eval_core.cuh). */
+static float powu_f(float a, int k)
+{
+  float r = 1.0f, b = a;
+  while (k > 0) {
+    if (k & 1) r = r * b;
+    k >>= 1;
+    if (k > 0) b = b * b;
+  }
+  return r;
+}
+
+static float point_apply_f(int op, float a, float b, int k)
+{
+  switch (op) {
+    case CMN_OP_ADD: return a + b;
+    case CMN_OP_SUB: return a - b;
+    case CMN_OP_MUL: return a * b;
+    case CMN_OP_DIV: return a / b;
+    case CMN_OP_SQR: return a * a;
+    case CMN_OP_NEG: return -a;
+    case CMN_OP_SQRT: return sqrtf(a);
+    case CMN_OP_POWN: return k == 0 ? 1.0f : (k > 0 ? powu_f(a, k) : 1.0f / powu_f(a, -k));
+    case CMN_OP_ABS: return fabsf(a);
+    case CMN_OP_MIN: return fminf(a, b);
+    case CMN_OP_MAX: return fmaxf(a, b);
+    default: return NAN;
+  }
+}
+
+static int eval_point_f(const orc_problem* p, const double* x, float* val, float* obj)
+{
+  for (int64_t v = 0; v < p->n_nodes; ++v) {
+    const cmn_node* nd = &p->nodes[v];
+    if (nd->op == CMN_OP_VAR) val[v] = (float)x[nd->var_index];
+    else if (nd->op == CMN_OP_CONST) val[v] = (float)nd->constant;
+  }
+  for (int64_t k = 0; k < p->n_order; ++k) {
+    int64_t i = p->order[k];
+    const cmn_node* nd = &p->nodes[i];
+    float a = val[nd->in0];
+    float b = nd->n_in >= 2 ? val[nd->in1] : a;
+    val[i] = point_apply_f(nd->op, a, b, nd->int_exp);
+  }
+  int feas = 1;
+  for (int64_t c = 0; c < p->n_cons; ++c) {
+    double v = (double)val[p->cons[c].root];
+    double rhs = p->cons[c].rhs;
+    int ok = p->cons[c].cmp == CMN_CMP_LE ? (v <= rhs) : almost_equal(v, rhs);
+    if (!ok) feas = 0;
+  }
+  *obj = val[p->root];
+  return feas;
+}
+
 /* ======================================================================
  * region decode (region/decode.hpp:44-71) and sampler
  * (graph/subregion_sampler.cuh:53-120)
@@ -2015,17 +2074,49 @@ typedef struct {
   double gub_old;
   uint64_t salt0;
   int use_screen; /* FP32 screen switched on for this iteration */
+  const double* plb; /* lazy form: the parents' FP64 lower bounds */
   /* outputs per child slot (E*C) */
   double* lb;
   uint8_t* state; /* 0 invalid, 1 dup, 2 infeasible, 3 dominated(old), 4 eligible */
   uint8_t* screened; /* FP32 screen excluded it */
   double* cand_val;  /* per child slot: best candidate value (inf none) */
   int64_t* cand_idx; /* element index within parent */
+  float* b32v;       /* lazy form: per child slot, smallest FP32 point value */
+  uint32_t* b32i;    /* and its sample index */
   int failed;
 } batch_ctx;
 
-/* One child slot: interval bound (FP64, or FP32 screen + FP64 certify) and
- * then its samples (or its exact point for a fathomed parent). */
+/* Lazy form: survivors whose FP32 bound lies within LAZY_BAND *
+ * max(1, |GUB|) below the incumbent are certified in FP64 when bounded
+ * (kCertifyBand in csrc/kernels.cuh). */
+#define LAZY_BAND (1.0 / 1024.0)
+
+/* Lazy form: the FP64 verdict of each selected parent box. */
+typedef struct {
+  const orc_problem* p;
+  const double* pbox;
+  double* lb;
+  int* feas;
+  int failed;
+} certify_ctx;
+
+static void certify_range(void* vc, int64_t k0, int64_t k1, int tid)
+{
+  (void)tid;
+  certify_ctx* c = (certify_ctx*)vc;
+  const int64_t n = c->p->n_vars;
+  iv64* v64 = (iv64*)malloc(sizeof(iv64) * (size_t)c->p->n_nodes);
+  for (int64_t k = k0; k < k1; ++k) {
+    double ub;
+    if (eval_all_d(c->p, c->pbox + 2 * (size_t)n * (size_t)k, v64)) c->failed = 1;
+    c->feas[k] = verdict_d(c->p, v64, &c->lb[k], &ub);
+  }
+  free(v64);
+}
+
+/* One child slot: interval bound (FP64, or FP32 screen + FP64 certify, or
+ * FP32 alone in the lazy form) and then its samples (or its exact point
+ * for a fathomed parent). */
 static void batch_range(void* vc, int64_t g0, int64_t g1, int tid)
 {
   (void)tid;
@@ -2037,12 +2128,18 @@ static void batch_range(void* vc, int64_t g0, int64_t g1, int tid)
   iv64* v64 = (iv64*)malloc(sizeof(iv64) * (size_t)p->n_nodes);
   iv32* v32 = (iv32*)malloc(sizeof(iv32) * (size_t)p->n_nodes);
   double* pv = (double*)malloc(sizeof(double) * (size_t)p->n_nodes);
+  float* pf = (float*)malloc(sizeof(float) * (size_t)p->n_nodes);
+  const int lazy = c->o->precision == CMN_PRECISION_FP32_LAZY;
   for (int64_t g = g0; g < g1; ++g) {
     uint64_t k = (uint64_t)g / c->C, r = (uint64_t)g % c->C;
     const parent_plan* pl = &c->plan[k];
     c->cand_val[g] = INFINITY;
     c->cand_idx[g] = -1;
     c->screened[g] = 0;
+    if (lazy) {
+      c->b32v[g] = INFINITY;
+      c->b32i[g] = 0;
+    }
     if (r >= pl->nreg) {
       c->state[g] = 0;
       c->lb[g] = NAN;
@@ -2053,10 +2150,17 @@ static void batch_range(void* vc, int64_t g0, int64_t g1, int tid)
     if (pl->fathom) {
       /* exact enumeration point (graph/kernels.cuh:131-172) */
       for (int64_t v = 0; v < n; ++v) x[v] = cb[2 * v];
-      double obj;
-      int f = eval_point_impl(p, x, pv, &obj);
       c->state[g] = 0;
       c->lb[g] = NAN;
+      if (lazy) { /* screened in FP32 like a sample; verified per chunk */
+        float o32;
+        int f32 = eval_point_f(p, x, pf, &o32);
+        float v32 = (f32 && o32 == o32) ? o32 : INFINITY;
+        if (v32 < c->b32v[g]) c->b32v[g] = v32;
+        continue;
+      }
+      double obj;
+      int f = eval_point_impl(p, x, pv, &obj);
       if (f && witness_is_admissible(p, x)) {
         c->cand_val[g] = obj;
         c->cand_idx[g] = (int64_t)r;
@@ -2072,7 +2176,29 @@ static void batch_range(void* vc, int64_t g0, int64_t g1, int tid)
     } else {
       double lb, ub;
       int f, screened_out = 0;
-      if (c->o->precision == CMN_PRECISION_FP32_SCREEN && c->use_screen) {
+      if (c->o->precision == CMN_PRECISION_FP32_LAZY) {
+        /* FP32; the parent's certified FP64 bound holds for the child; a
+         * survivor within the band below the incumbent is certified in
+         * FP64 at once (csrc/kernels.cuh certify_floor) */
+        if (eval_all_f(p, cb, v32)) c->failed = 1;
+        f = verdict_f(p, v32, &lb, &ub);
+        double plb = c->plb[k];
+        lb = plb > lb ? plb : lb;
+        if (!f) {
+          c->state[g] = 2;
+        } else if (lb > c->gub_old) {
+          c->state[g] = 3;
+        } else if (lb >= c->gub_old - LAZY_BAND * fmax(1.0, fabs(c->gub_old))) {
+          if (eval_all_d(p, cb, v64)) c->failed = 1;
+          f = verdict_d(p, v64, &lb, &ub);
+          lb = plb > lb ? plb : lb;
+          c->state[g] = !f ? 2 : (lb > c->gub_old ? 3 : 4);
+          c->screened[g] = 2; /* certified */
+        } else {
+          c->state[g] = 4;
+        }
+        screened_out = 1; /* no further FP64 pass */
+      } else if (c->o->precision == CMN_PRECISION_FP32_SCREEN && c->use_screen) {
         if (eval_all_f(p, cb, v32)) c->failed = 1;
         f = verdict_f(p, v32, &lb, &ub);
         if (!f) {
@@ -2092,7 +2218,19 @@ static void batch_range(void* vc, int64_t g0, int64_t g1, int tid)
       c->lb[g] = lb;
     }
     int do_sample = c->o->sample_all ? 1 : (c->state[g] == 4);
-    if (do_sample) {
+    if (do_sample && lazy) {
+      uint64_t salt = c->salt0 + k + 1;
+      for (uint64_t i = 0; i < c->o->sample_points; ++i) {
+        sample_point(p, cb, r, i, salt, x);
+        float o32;
+        int f32 = eval_point_f(p, x, pf, &o32);
+        float v32 = (f32 && o32 == o32) ? o32 : INFINITY;
+        if (v32 < c->b32v[g]) {
+          c->b32v[g] = v32;
+          c->b32i[g] = (uint32_t)i;
+        }
+      }
+    } else if (do_sample) {
       uint64_t salt = c->salt0 + k + 1;
       for (uint64_t i = 0; i < c->o->sample_points; ++i) {
         sample_point(p, cb, r, i, salt, x);
@@ -2112,6 +2250,7 @@ static void batch_range(void* vc, int64_t g0, int64_t g1, int tid)
   free(v64);
   free(v32);
   free(pv);
+  free(pf);
 }
 
 typedef struct {
@@ -2201,6 +2340,29 @@ static int batched_run(const orc_problem* p, const cmn_solve_options* o,
       pl->fathom = live <= pl->count && fully_enumerable(pl->kinds, pl->count);
       slots_init(&pl->s, pl->kinds, pl->vids, pl->widths, pl->count);
     }
+    /* lazy form: a selected box is expanded only if its FP64 verdict
+     * keeps it (the reference predicate, and its bound at most GUB) */
+    double* plb = NULL;
+    if (o->precision == CMN_PRECISION_FP32_LAZY) {
+      plb = (double*)malloc(sizeof(double) * (E ? E : 1));
+      int* pfeas = (int*)malloc(sizeof(int) * (E ? E : 1));
+      certify_ctx cc = {p, pbox, plb, pfeas, 0};
+      parallel_for((int64_t)E, threads, certify_range, &cc);
+      if (cc.failed) {
+        set_err("op without an interval implementation");
+        rc = -1;
+      }
+      for (k = 0; k < E; ++k) {
+        ++ct->certified_fp64;
+        if (!pfeas[k] || plb[k] > st->GUB) {
+          plan[k].nreg = 0;
+          plan[k].fathom = 0;
+          plan[k].count = 0;
+          ++ct->certify_pruned;
+        }
+      }
+      free(pfeas);
+    }
     uint64_t salt0 = st->expansions;
     st->expansions += E;
 
@@ -2216,15 +2378,57 @@ static int batched_run(const orc_problem* p, const cmn_solve_options* o,
     c.gub_old = st->GUB;
     c.salt0 = salt0;
     c.use_screen = st->use_screen;
+    c.plb = plb;
     c.lb = (double*)malloc(sizeof(double) * G);
     c.state = (uint8_t*)malloc(G);
     c.screened = (uint8_t*)malloc(G);
     c.cand_val = (double*)malloc(sizeof(double) * G);
     c.cand_idx = (int64_t*)malloc(sizeof(int64_t) * G);
+    const int lazy = o->precision == CMN_PRECISION_FP32_LAZY;
+    c.b32v = lazy ? (float*)malloc(sizeof(float) * G) : NULL;
+    c.b32i = lazy ? (uint32_t*)malloc(sizeof(uint32_t) * G) : NULL;
     parallel_for((int64_t)G, threads, batch_range, &c);
     if (c.failed) {
       set_err("op without an interval implementation");
       rc = -1;
+    }
+    if (lazy) {
+      /* each chunk of 32 child slots: its FP32-best point (first child,
+       * then first sample, on ties) evaluated again in FP64 */
+      double* cb = (double*)malloc(sizeof(double) * 2 * (size_t)n);
+      double* val = (double*)malloc(sizeof(double) * (size_t)p->n_nodes);
+      for (uint64_t c0 = 0; c0 < G; c0 += 32) {
+        float bv = INFINITY;
+        uint64_t bg = 0;
+        for (uint64_t g = c0; g < c0 + 32 && g < G; ++g)
+          if (c.b32v[g] < bv) {
+            bv = c.b32v[g];
+            bg = g;
+          }
+        if (!(bv < INFINITY)) continue;
+        uint64_t kk = bg / C, r = bg % C, i = c.b32i[bg];
+        const parent_plan* pl = &plan[kk];
+        child_box(pbox + 2 * (size_t)n * kk, n, &pl->s, r, cb);
+        if (pl->fathom) {
+          for (int64_t v = 0; v < n; ++v) x[v] = cb[2 * v];
+        } else {
+          sample_point(p, cb, r, i, salt0 + kk + 1, x);
+        }
+        double obj;
+        int f = eval_point_impl(p, x, val, &obj);
+        if (!f || obj != obj) continue;
+        if (pl->fathom && !witness_is_admissible(p, x)) {
+          if (obj < st->GUB) {
+            c.cand_idx[bg] = -2;
+            c.cand_val[bg] = obj;
+          }
+          continue;
+        }
+        c.cand_val[bg] = obj;
+        c.cand_idx[bg] = (int64_t)(pl->fathom ? r : r * S + i);
+      }
+      free(cb);
+      free(val);
     }
 
     /* incumbent: argmin over (value, parent, element) of admissible
@@ -2248,7 +2452,10 @@ static int batched_run(const orc_problem* p, const cmn_solve_options* o,
           if (c.state[g] != 1) { /* duplicates are never evaluated */
             ++iter_valid;
             if (c.state[g] == 2 || c.state[g] == 3) ++iter_excluded;
-            if (o->precision == CMN_PRECISION_FP32_SCREEN && st->use_screen) {
+            if (o->precision == CMN_PRECISION_FP32_LAZY) {
+              ++ct->screened_fp32;
+              if (c.screened[g] == 2) ++ct->certified_fp64;
+            } else if (o->precision == CMN_PRECISION_FP32_SCREEN && st->use_screen) {
               ++ct->screened_fp32;
               if (!c.screened[g]) {
                 ++ct->certified_fp64;
@@ -2368,11 +2575,14 @@ static int batched_run(const orc_problem* p, const cmn_solve_options* o,
     free(pbox);
     free(pdepth);
     free(plan);
+    free(plb);
     free(c.lb);
     free(c.state);
     free(c.screened);
     free(c.cand_val);
     free(c.cand_idx);
+    free(c.b32v);
+    free(c.b32i);
     if (rc) break;
   }
   free(x);

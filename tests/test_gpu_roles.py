@@ -4,6 +4,7 @@ known answers (graph_replay_test.cu, backend_contract.hpp)."""
 
 from __future__ import annotations
 
+import functools
 import math
 
 import numpy as np
@@ -128,3 +129,33 @@ def test_over_budget_and_shape_errors():
     assert e3.value.status_name == "INVALID_CONFIGURATION"
     with pytest.raises(CmnError):
         Sampler(dp, [A.SLOT_CONTINUOUS], 4, sample_points=0)
+
+
+@functools.lru_cache(maxsize=1)
+def wide_qcqp():
+    """n = 512: sparse Q and constraints, so the DAG stays small while the
+    sampler's point (512 doubles) far exceeds one thread's share of shared
+    memory; lanes share point columns (sample_lg_min)."""
+    return G.qcqp(G.QCQPSpec(n=512, m=4, n_int=32, int_lb=0, int_ub=3, cont_lb=-1.0, cont_ub=1.0,
+                             q_density=0.002, a_density=0.002, rhs=(1.0, 10.0)), G.seed_for(11, 0))
+
+
+def test_sampler_n512_matches_oracle():
+    p = wide_qcqp()
+    assert p.n_vars == 512
+    dp = DeviceProblem(p)
+    op = O.OracleProblem(p)
+    box = p.root_box()
+    kinds, vids, widths, _ = O.bisection_choose(box, p.var_kinds, 10)
+    N = int(np.prod(widths))
+    s = Sampler(dp, kinds, N, sample_points=2)
+    found_any = False
+    for salt in (1, 2, 3):
+        c = s.sample(box, vids, widths, salt)
+        found, val, pt, idx = op.sample(box, kinds, vids, widths, N, 2, salt)
+        assert c.found == found
+        if found:
+            found_any = True
+            assert c.value == val and c.index == idx
+            assert np.array_equal(c.point, pt)
+    assert found_any

@@ -1,15 +1,21 @@
 #!/usr/bin/env python3
 """Throughput of the batched interval branch-and-bound hot path.
 
-Workload (N=1): the n=32 MIQCQP (4 integers in [0,7], 28 continuous in
-[-5,5], dense Q, 16 quadratic constraints at 20% density), frontier capped
-at 2^20 boxes.  One step is one device-resident batched iteration: the
-2^16 best boxes are selected, each branched into 2^4 children
-(BisectionBudget), every child bounded (fused interval evaluator) and
-sampled, then pruned and compacted into the pool -- 2^20 box evaluations
-per step.  `value` is box evaluations per second of the FP32-screen +
-FP64-certify form; the plain FP64 form, which gives identical certified
-bounds, is reported beside it.
+Workload (N=1): the n=64 MIQCQP (8 integers in [0,15], 56 continuous in
+[-10,10], Q at 30% density, 32 quadratic constraints at 10% density),
+frontier capped at 2^22 boxes -- the largest single-GPU configuration.
+One step is one device-resident batched iteration: the 2^16 best boxes are
+selected, each branched into 2^4 children (BisectionBudget), every child
+bounded and sampled, then pruned and compacted into the pool -- 2^20 box
+evaluations per step.
+
+`value` is box evaluations per second of the lazy form (children bounded
+in FP32 with outward rounding; a box's bound is certified in FP64 when it
+is selected for expansion, or at once when its FP32 bound lies just below
+the incumbent; sample points ranked in FP32 and each chunk's best
+evaluated in FP64).  The plain FP64 form (the reference's arithmetic, bit
+for bit) and the FP32 screen with FP64 certification of every survivor
+(the plain trajectory, bit for bit) are reported beside it.
 
 `e2e` is the same metric through the reference-facing role ABI
 (cmn_sample + cmn_bound, the RegionSampler/RegionBounder calls the
@@ -19,16 +25,22 @@ device->host copy of the 2^20 verdicts inside the timed region.
 
 The line also carries the other workloads, each skippable by a --no-* flag
 and runnable alone with --only:
-- time_to_gap: the n=4 QCQP to the 1e-6 gap;
+- reference_gpu: the reference's own CUDA graph backend and its
+  SearchDriver on the same GPU (oracle/_ref/ref_gpu, built where the
+  reference headers were written out), beside this library's roles
+  through the same adapter;
+- time_to_gap: the n=4 QCQP to the 1e-6 gap in every form;
+- config2_solver: solver steps on the n=32 MIQCQP in every form;
 - batch_uneven: 1024 uneven instances in one batch;
 - serving: a Poisson request stream;
-- config3_solver: solver steps on the n=64 MIQCQP;
 - fp32_screen_check: FP64 points inside FP32 enclosures, and per-node width
   inflation.
 
---impl reference times the CPU restatement of the reference path (the
+--impl reference times the reference path on the host cores: the CPU
+restatement of its per-iteration work (sample + bound of one parent's
+children) with the host's directed-rounding hardware on every core (the
 reference has no CPU evaluation backend of its own; its region evaluation
-runs only on the GPU) on all host cores over a bounded sample.
+runs only on the GPU).
 """
 
 from __future__ import annotations
@@ -48,6 +60,8 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 EVAL_DRAM_BYTES_PER_BOX = (43186688 + 34048) / 1048576  # ncu, eval_children_kernel<double, 1>, config 2
+# ncu, eval_children_kernel<float, 5>, config 3 (profiles/eval_children_fp32_lazy_config3.md)
+EVAL32_DRAM_BYTES_PER_BOX = None
 # time-to-gap on config 1: the cluster of boxes within 1e-6 of the optimum
 # holds tens of millions of boxes at n=4, so the frontier is capped at 2^25;
 # 2^21 parents x 2^2 children per iteration timed best (swept over
@@ -55,8 +69,10 @@ EVAL_DRAM_BYTES_PER_BOX = (43186688 + 34048) / 1048576  # ncu, eval_children_ker
 TTG_B, TTG_E, TTG_CAP = 2, 1 << 21, 1 << 25
 E_PARENTS = 1 << 16
 B_BITS = 4
-CAP = 1 << 20
+CAP = 1 << 20          # config 2
+CONFIG3_CAP = 1 << 22  # config 3, the headline
 E2E_B = 20
+FORMS = ("fp64", "lazy", "fp32")  # plain, lazy certification, screen + certify every survivor
 
 
 def parse_args():
@@ -71,13 +87,21 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-batch", action="store_true", help="skip the 1024-instance batch (config 4)")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving stream (config 5)")
-    ap.add_argument("--no-config3", action="store_true", help="skip the n=64 solver steps (config 3)")
+    ap.add_argument("--no-config2", action="store_true", help="skip the n=32 solver steps (config 2)")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="skip the reference's own CUDA graph backend on this GPU")
     ap.add_argument("--no-screen-check", action="store_true",
                     help="skip the FP32 screen containment / width-inflation check (config 3)")
-    ap.add_argument("--only", choices=["batch", "serve", "ttg", "screen", "config3"],
+    ap.add_argument("--only", choices=["batch", "serve", "ttg", "screen", "config2", "refgpu"],
                     help="run one of the extra workloads alone")
     ap.add_argument("--instances", type=int, default=1024, help="--only batch: instances in the batch")
-    ap.add_argument("--precision", choices=["fp64", "fp32"], help="--only batch / ttg: one form only")
+    ap.add_argument("--precision", choices=["fp64", "fp32", "lazy"], help="--only batch / ttg: one form only")
+    ap.add_argument("--parents", type=int, default=0,
+                    help="--quick: parents per step instead of 2^16 (a smaller case for profiling)")
+    ap.add_argument("--cap", type=int, default=0,
+                    help="--quick: frontier cap instead of 2^22 (a smaller box store for profiling)")
+    ap.add_argument("--forms", default=",".join(FORMS),
+                    help="--quick: comma-separated forms to run (fp64, lazy, fp32)")
     ap.add_argument("--ttg-iters", type=int, default=0,
                     help="--only ttg: stop after this many iterations (0: run to the gap); the profiling case")
     return ap.parse_args()
@@ -215,9 +239,11 @@ def job_rate(dist, units: float, ms: float):
 
 # ------------------------------------------------------------- CPU side
 def cpu_rate(problem, seconds: float, threads: int):
-    """Box evaluations per second of the oracle (CPU restatement of the
-    reference path): sample + bound of one parent's children, the
-    reference's per-iteration work, on `threads` host threads."""
+    """Box evaluations per second of the reference path on the host:
+    sample + bound of one parent's children, the reference's per-iteration
+    work, on `threads` host threads, the bound with the host's
+    directed-rounding hardware (oracle orc_bound_hw, bit-identical to the
+    oracle's error-free transformations)."""
     import numpy as np
 
     import oracle as O
@@ -231,7 +257,7 @@ def cpu_rate(problem, seconds: float, threads: int):
     salt = 1
     while True:
         op.sample(box, kinds, vids, widths, N, 1, salt, threads=threads)
-        op.bound(box, kinds, vids, widths, N, threads=threads)
+        op.bound(box, kinds, vids, widths, N, threads=threads, hardware_rounding=True)
         done += N
         salt += 1
         if time.perf_counter() - t0 >= seconds:
@@ -322,7 +348,7 @@ def fma_peak(precision):
 def e2e_run(dp, problem, steps, warmup):
     import numpy as np
 
-    from cuminlp_gb300.aggregate import bisection_choose
+    from cuminlp_gb300.solver import bisection_choose
     from cuminlp_gb300.solver import Bounder, Sampler
     root = np.array(problem.box_bounds)
     rng = np.random.default_rng(7)
@@ -470,28 +496,90 @@ def serving_run(rate, n_requests, dps, seed=11, iter_limit=SERVE_ITER_LIMIT):
             "pool_bytes_peak": st["pool_bytes_peak"], "rounds": st["rounds"]}
 
 
-CONFIG3_CAP = 1 << 22
+def forms_summary(res: dict, steps: int) -> dict:
+    """Per form: boxes/s, ms per step, mean phase times (select+branch,
+    bound, sample, prune+rebuild, whole) and the FP32/FP64 box counts."""
+    out = {}
+    for p, r in res.items():
+        d = r["delta"]
+        out[p] = {"value": d["bounded"] / (r["ms"] * 1e-3), "unit": "boxes/s", "ms_per_step": r["ms"] / steps,
+                  "phases_ms": [round(sum(ph[i] for ph in r["phases"]) / len(r["phases"]), 3) for i in range(5)],
+                  "fp32_boxes": d["screened_fp32"], "fp64_boxes": d["certified_fp64"],
+                  "certify_pruned": d.get("certify_pruned", 0)}
+    return out
 
 
-def config3_run(rt, steps, warmup) -> dict:
-    """Solver steps on the n=64 MIQCQP in both forms: 2^16 parents x 2^4
-    children per step, frontier cap 2^22 boxes."""
+def config2_run(rt, steps, warmup) -> dict:
+    """Solver steps on the n=32 MIQCQP in every form: 2^16 parents x 2^4
+    children per step, frontier cap 2^20 boxes."""
     from cuminlp_gb300 import generators as G
     from cuminlp_gb300.solver import DeviceProblem
-    dp = DeviceProblem(G.config3(0))
-    res = {p: solver_run(dp, rt, p, steps, warmup, cap=CONFIG3_CAP) for p in ("fp64", "fp32")}
-    out = {"workload": "config3: n=64 MIQCQP (8 int [0,15], 56 cont [-10,10]), Q 30% dense, m=32 at 10%; "
-                       f"{E_PARENTS} parents x 2^{B_BITS} children per step; frontier cap 2^22",
-           "flops_per_box": dp.info()["flops_per_box"]}
-    for p, r in res.items():
-        out["plain_fp64" if p == "fp64" else "fp32_screen"] = {
-            "value": r["delta"]["bounded"] / (r["ms"] * 1e-3), "unit": "boxes/s", "ms_per_step": r["ms"] / steps,
-            "phases_ms": [round(sum(ph[i] for ph in r["phases"]) / len(r["phases"]), 3) for i in range(5)]}
-    sc = res["fp32"]["delta"]
-    out["screen_speedup_vs_plain_fp64"] = out["fp32_screen"]["value"] / out["plain_fp64"]["value"]
-    out["identical_certified_bounds"] = res["fp64"]["outcome"] == res["fp32"]["outcome"]
-    out["screen_active_fraction"] = sc["screened_fp32"] / max(1, sc["bounded"])
-    out["screen_certified_fraction"] = sc["certified_fp64"] / max(1, sc["bounded"])
+    dp = DeviceProblem(G.config2(0))
+    res = {p: solver_run(dp, rt, p, steps, warmup, cap=CAP) for p in FORMS}
+    f = forms_summary(res, steps)
+    return {"workload": "config2: n=32 MIQCQP (4 int [0,7], 28 cont [-5,5]), dense Q, m=16 at 20%; "
+                        f"{E_PARENTS} parents x 2^{B_BITS} children per step; frontier cap 2^20",
+            "flops_per_box": dp.info()["flops_per_box"], "plain_fp64": f["fp64"], "lazy": f["lazy"],
+            "fp32_screen_fp64_certify": f["fp32"],
+            "lazy_speedup_vs_plain_fp64": f["lazy"]["value"] / f["fp64"]["value"],
+            "screen_speedup_vs_plain_fp64": f["fp32"]["value"] / f["fp64"]["value"],
+            "screen_identical_to_plain": res["fp64"]["outcome"] == res["fp32"]["outcome"]}
+
+
+REF_GPU = ROOT / "oracle" / "_ref" / "ref_gpu"
+
+
+def _ref_gpu_call(args: list[str], text: str, timeout: float = 900.0) -> dict:
+    with tempfile.TemporaryDirectory() as d:
+        i, o = Path(d) / "in.txt", Path(d) / "out.txt"
+        i.write_text(text)
+        proc = subprocess.run([str(REF_GPU), *args, str(i), str(o)], capture_output=True, text=True,
+                              timeout=timeout)
+        if proc.returncode != 0:
+            raise RuntimeError(f"ref_gpu {' '.join(args)} failed: {proc.stderr[-400:]}")
+        lines = o.read_text().splitlines()
+    out = {}
+    for ln in lines:
+        k, _, v = ln.partition(" ")
+        out.setdefault(k, []).append(v)
+    return {"lines": lines, "kv": out}
+
+
+def reference_gpu_run() -> dict:
+    """The reference's own CUDA graph backend on this GPU (one kernel per DAG
+    node, captured as a CUDA graph; its device code compiled for sm_103a
+    with the build's interval operators standing in for the missing
+    cuinterval), beside this library's roles through the reference-side
+    adapter: bound() calls at 2^17 (config 3) and 2^19 (config 2) regions,
+    both timed through the same interface with the box in and the verdicts
+    out; and the reference's SearchDriver to the 1e-6 gap on the config-1
+    instance it proves, over either backend."""
+    from cuminlp_gb300 import generators as G
+    from tests.golden.make_golden import problem_text
+    if not REF_GPU.exists():
+        return {"unavailable": "oracle/_ref/ref_gpu not built (its reference headers are written where the "
+                               "reference tree is mounted)"}
+    out = {"label": "reference graph structure + the build's directed-rounding ops"}
+    for cfg, B in ((3, 17), (2, 19)):
+        r = _ref_gpu_call(["roles"], f"{B} 1 5 1 b 0x1p+0\n" + problem_text(G.CONFIGS[cfg]()))["kv"]
+        n = int(r["n_regions"][0])
+        g = float(r["bound_seconds_graph"][0])
+        ours = float(r["bound_seconds_gb300"][0])
+        out[f"config{cfg}_bound"] = {
+            "regions": n, "reference_graph_boxes_per_s": n / g, "gb300_roles_boxes_per_s": n / ours,
+            "speedup": g / ours, "mismatched_feasible": int(r["bound_mismatch_feasible"][0]),
+            "mismatched_lb": int(r["bound_mismatch_lb"][0]),
+            "graph_build_s": float(r["bound_build_seconds_graph"][0])}
+    head = f"B 100000 2 2 1 0 1 {(1e-6).hex()}\n"
+    text = head + problem_text(G.config1(1))
+    for backend in ("graph", "gb300"):
+        lines = _ref_gpu_call(["driver", backend], text)["lines"]
+        h = lines[0].split()
+        out[f"time_to_gap_config1_instance1_{backend}"] = {
+            "seconds": float(lines[3].split()[1]), "stop_reason": h[2], "proven_optimal": int(h[3]),
+            "lower_bound": float.fromhex(h[0]), "upper_bound": float.fromhex(h[1]),
+            "expansions": int(lines[1].split()[0])}
+    out["driver"] = "reference SearchDriver, BisectionBudget B=2, one sample per region"
     return out
 
 
@@ -552,8 +640,11 @@ def run_ours(args):
     if args.only == "screen":
         print(json.dumps(screen_check_run()))
         return
-    if args.only == "config3":
-        print(json.dumps(config3_run(rt, args.steps, args.warmup)))
+    if args.only == "config2":
+        print(json.dumps(config2_run(rt, args.steps, args.warmup)))
+        return
+    if args.only == "refgpu":
+        print(json.dumps(reference_gpu_run()))
         return
     if args.only == "serve":
         from cuminlp_gb300.solver import DeviceProblem
@@ -561,28 +652,35 @@ def run_ours(args):
         print(json.dumps({"workload": serving_workload(), "runs": [serving_run(r, n, dps) for r, n in SERVE_RUNS],
                           "time_to_gap_run": serving_run(SERVE_TTG[0], SERVE_TTG[1], dps, iter_limit=SERVE_TTG[2])}))
         return
-    problem = G.config2(rank)  # replicas: one independent instance per GPU
+    problem = G.config3(rank)  # replicas: one independent instance per GPU
     dp = DeviceProblem(problem)
     info = dp.info()
     peak64 = fma_peak(0)
     peak32 = fma_peak(1)
 
+    if args.quick:  # the profiling command: solver steps only
+        e = args.parents or E_PARENTS
+        out = {"quick": True, "parents": e, "cap": args.cap or CONFIG3_CAP}
+        for prec in args.forms.split(","):
+            r = solver_run(dp, rt, prec, args.steps, args.warmup, e=e, cap=args.cap or CONFIG3_CAP)
+            out[f"{prec}_ms"] = r["ms"]
+            out[f"{prec}_boxes/s"] = r["delta"]["bounded"] / (r["ms"] * 1e-3)
+        print(json.dumps(out))
+        return
+
     barrier(dist)
     res = {}
     with Clocks(local) as clk:
-        for prec in ("fp64", "fp32"):
+        for prec in FORMS:
             barrier(dist)
-            res[prec] = solver_run(dp, rt, prec, args.steps, args.warmup)
+            res[prec] = solver_run(dp, rt, prec, args.steps, args.warmup, cap=CONFIG3_CAP)
     clocks = clk.summary()
 
-    screen = res["fp32"]
+    lazy = res["lazy"]
     plain = res["fp64"]
-    value, t_max = job_rate(dist, screen["delta"]["bounded"], screen["ms"])
+    value, t_max = job_rate(dist, lazy["delta"]["bounded"], lazy["ms"])
     plain_value, t_plain = job_rate(dist, plain["delta"]["bounded"], plain["ms"])
 
-    if args.quick:
-        print(json.dumps({"quick": True, "fp64_ms": plain["ms"], "fp32_ms": screen["ms"], "boxes/s": value}))
-        return
     barrier(dist)
     e2e = e2e_run(dp, problem, args.steps, args.warmup)
     e2e_rank0 = e2e["value"]
@@ -591,30 +689,39 @@ def run_ours(args):
     if rank != 0:
         barrier(dist)
         return
-    # live roofline of the dominant kernel: the FP64 evaluator of the plain
-    # form (phase 1 of the iteration is that kernel plus a tiny count pass)
-    ev_ms = sum(p[1] for p in plain["phases"])
-    nb = plain["delta"]["bounded"]
+    forms = forms_summary(res, args.steps)
     fpb = info["flops_per_box"]
-    achieved = nb * fpb / (ev_ms * 1e-3) / 1e12
     bpb = info["bytes_per_box"]
-    hbm_gbs = nb * bpb / (ev_ms * 1e-3) / 1e9
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    # DRAM bytes per launch of the dominant kernel, from one ncu capture of
-    # a full-size config-2 iteration (43,186,688 B read + 34,048 B written
-    # for 1,048,576 child boxes), scaled to this run's boxes per launch
-    traffic = EVAL_DRAM_BYTES_PER_BOX * nb / max(1, len(plain["phases"]))
+
+    # live roofline of the dominant kernel of the headline (lazy) form: the
+    # FP32 child evaluator, phase 1 of the iteration (that kernel, a count
+    # pass, and the FP64 pass over children in the band below the incumbent,
+    # empty without an incumbent)
+    ev_ms = sum(p[1] for p in lazy["phases"])
+    nb = lazy["delta"]["bounded"]
+    achieved32 = nb * fpb / (ev_ms * 1e-3) / 1e12
+    launches = max(1, len(lazy["phases"]))
+    # the plain FP64 evaluator, for the record
+    ev64_ms = sum(p[1] for p in plain["phases"])
+    nb64 = plain["delta"]["bounded"]
+    achieved64 = nb64 * fpb / (ev64_ms * 1e-3) / 1e12
 
     model, cores = cpu_info()
     cpu_v, cpu_s = cpu_rate(problem, args.cpu_seconds, cores)
+
     def ttg_leg():
         out = {"config": f"n=4 QCQP (config 1, instances 0 and 1), gap 1e-6, 2^{TTG_B} children per parent, "
                          f"{TTG_E} parents per iteration, frontier cap {TTG_CAP}, 20 s cap each"}
         for inst in (0, 1):
             p1 = G.config1(inst)
-            out[f"instance{inst}"] = {"fp64": time_to_gap(p1, "fp64", 20.0),
+            out[f"instance{inst}"] = {"fp64": time_to_gap(p1, "fp64", 20.0), "lazy": time_to_gap(p1, "lazy", 20.0),
                                       "fp32_screen_fp64_certify": time_to_gap(p1, "fp32", 20.0)}
+            a, b = out[f"instance{inst}"]["fp64"], out[f"instance{inst}"]["lazy"]
+            tol = 1e-6 * max(1.0, abs(a["upper_bound"]))
+            out[f"instance{inst}"]["lazy_bounds_within_tolerance_of_plain"] = bool(
+                abs(a["upper_bound"] - b["upper_bound"]) <= tol and abs(a["lower_bound"] - b["lower_bound"]) <= tol)
         return out
 
     def batch_leg():
@@ -629,15 +736,16 @@ def run_ours(args):
         return {"workload": serving_workload(), "runs": [serving_run(r, n, dps) for r, n in SERVE_RUNS],
                 "time_to_gap_run": serving_run(SERVE_TTG[0], SERVE_TTG[1], dps, iter_limit=SERVE_TTG[2])}
 
+    ref_gpu = None if args.no_reference_gpu else extra_leg(reference_gpu_run)
     ttg = None if args.no_ttg else extra_leg(ttg_leg)
+    config2 = None if args.no_config2 else extra_leg(config2_run, rt, args.steps, args.warmup)
     batch = None if args.no_batch else extra_leg(batch_leg)
     serving = None if args.no_serve else extra_leg(serving_leg)
     screen_check = None if args.no_screen_check else extra_leg(screen_check_run)
-    config3 = None if args.no_config3 else extra_leg(config3_run, rt, args.steps, args.warmup)
 
-    kpi = screen["kernels_per_iter"]
+    kpi = lazy["kernels_per_iter"]
     line = {
-        "metric": "boxes/s (batched interval B&B box evaluations, FP32 screen + FP64 certify)",
+        "metric": "boxes/s (interval B&B box evaluations per second; FP32 bound with lazy FP64 certification)",
         "value": value,
         "unit": "boxes/s",
         "n_gpus": world,
@@ -647,57 +755,63 @@ def run_ours(args):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64 (certify) + f32 (screen)",
-        "data": "synthetic (seeded generator, config 2 shape)",
+        "dtype": "f32 (child bounds, sample ranking) + f64 (certification, incumbent)",
+        "data": "synthetic (seeded generator, config 3 shape)",
         "config": {
-            "workload": "config2: n=32 MIQCQP (4 int [0,7], 28 cont [-5,5]), m=16 at 20% density, dense Q; "
-                        f"frontier cap 2^20; {E_PARENTS} parents x 2^{B_BITS} children per step",
+            "workload": "config3: n=64 MIQCQP (8 int [0,15], 56 cont [-10,10]), Q 30% dense, m=32 at 10% density; "
+                        f"frontier cap 2^22; {E_PARENTS} parents x 2^{B_BITS} children per step",
+            "form": "lazy: children bounded in FP32 (outward), FP64 verdict of every box selected for expansion "
+                    "and of survivors within 2^-10 * max(1, |incumbent|) below the incumbent; samples ranked in "
+                    "FP32, each chunk of 32 children's best point evaluated in FP64",
             "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-            "l2": "box pool 2 x 512 MiB planes > 129 MB L2 (no flush needed)",
+            "l2": "box store 2 x 2 GiB planes > 129 MB L2 (no flush needed)",
             "dag_nodes": info["n_nodes"], "reachable_nodes": info["buffer_node_count"],
             "program_length": info["program_length"], "program_slots": info["program_slots"],
         },
         "plain_fp64": {"value": plain_value, "ms_per_step": t_plain / args.steps,
-                       "phases_ms": [round(sum(p[i] for p in plain["phases"]) / len(plain["phases"]), 3)
-                                     for i in range(5)]},
-        "screen_phases_ms": [round(sum(p[i] for p in screen["phases"]) / len(screen["phases"]), 3)
-                             for i in range(5)],
-        "screen_speedup_vs_plain_fp64": value / plain_value,
-        "identical_certified_bounds": plain["outcome"] == screen["outcome"],
-        # the adaptive screen: share of boxes the FP32 pass saw, and share of
-        # boxes that needed FP64 certification
-        "screen_active_fraction": screen["delta"]["screened_fp32"] / max(1, screen["delta"]["bounded"]),
-        "screen_certified_fraction": screen["delta"]["certified_fp64"] / max(1, screen["delta"]["bounded"]),
+                       "phases_ms": forms["fp64"]["phases_ms"]},
+        "lazy": forms["lazy"],
+        "fp32_screen_fp64_certify": forms["fp32"],
+        "lazy_speedup_vs_plain_fp64": value / plain_value,
+        "screen_speedup_vs_plain_fp64": forms["fp32"]["value"] / forms["fp64"]["value"],
+        "screen_identical_to_plain": plain["outcome"] == res["fp32"]["outcome"],
         "roofline": {
-            "bound": "fp64",
-            "kernel": "eval_children_kernel<double> (fused interval DAG evaluator, plain FP64 form)",
-            "achieved": achieved, "peak": peak64, "unit": "TFLOP/s", "frac": achieved / peak64,
-            "peak_source": "measured by cmn_measure_fma_peak (DFMA loop, all SMs) in this run",
-            # directed rounding forbids FMA: one flop per FP64 instruction, so
-            # the pipe's ceiling for this arithmetic is half the DFMA flop rate;
-            # the round-up half of each interval product runs on the integer
-            # pipe instead, which is how the fraction passes 1
-            "frac_of_fp64_instruction_ceiling": achieved / (peak64 / 2),
+            "bound": "fp32",
+            "kernel": "eval_children_kernel<float, 5> (fused interval DAG evaluator, FP32, lazy form)",
+            "achieved": achieved32, "peak": peak32, "unit": "TFLOP/s", "frac": achieved32 / peak32,
+            "peak_source": "measured by cmn_measure_fma_peak (FFMA loop, all SMs) in this run; FMA counted as 2",
+            # directed rounding forbids FMA: one flop per instruction
+            "frac_of_fp32_instruction_ceiling": achieved32 / (peak32 / 2),
+            "flops_per_box": fpb, "boxes_per_launch": nb / launches,
+            "traffic": None if EVAL32_DRAM_BYTES_PER_BOX is None else EVAL32_DRAM_BYTES_PER_BOX * nb / launches,
+            "hbm": {"achieved": nb * (8 * problem.n_vars + 9) / (ev_ms * 1e-3) / 1e9, "peak": hbm_peak,
+                    "unit": "GB/s", "bytes_per_box": 8 * problem.n_vars + 9,
+                    "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
+        },
+        "roofline_plain_fp64": {
+            "bound": "fp64", "kernel": "eval_children_kernel<double, 1> (plain FP64 form)",
+            "achieved": achieved64, "peak": peak64, "unit": "TFLOP/s", "frac": achieved64 / peak64,
+            "frac_of_fp64_instruction_ceiling": achieved64 / (peak64 / 2),
             "integer_pipe_ops": "interval multiply rounded up (csrc/fp64_emu.cuh)",
-            "flops_per_box": fpb, "boxes_per_launch": nb / len(plain["phases"]),
-            "traffic": traffic,
-            "hbm": {"achieved": hbm_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": hbm_gbs / hbm_peak,
-                    "bytes_per_box": bpb, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
-            "fp32_fma_peak_tflops": peak32,
+            "traffic": EVAL_DRAM_BYTES_PER_BOX * nb64 / max(1, len(plain["phases"])),
+            "hbm": {"achieved": nb64 * bpb / (ev64_ms * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                    "bytes_per_box": bpb},
         },
         "cpu_baseline": {"value": cpu_v, "unit": "boxes/s", "cores": cores, "kind": "port",
-                         "sample": f"oracle sample+bound of {cpu_s['children_per_step']} children of the root, "
-                                   f"{cpu_s['steps']} steps in {cpu_s['seconds']} s", "cpu": model},
+                         "sample": f"sample + bound of {cpu_s['children_per_step']} children of the root, "
+                                   f"{cpu_s['steps']} steps in {cpu_s['seconds']} s; bound with the host's "
+                                   "directed-rounding hardware", "cpu": model},
         "e2e": {k: e2e[k] for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step")},
         "e2e_detail": {"regions_per_call": e2e["regions_per_call"], "ms_per_step": e2e["ms_per_step"],
-                       "rank0_value": e2e_rank0},
+                       "rank0_value": e2e_rank0, "form": "plain FP64 roles (the reference's role semantics)"},
         "gpu_launches": kpi * args.steps,
         "clocks": clocks,
+        "reference_gpu": ref_gpu,
         "time_to_gap": ttg,
+        "config2_solver": config2,
         "batch_uneven": batch,
         "serving": serving,
         "fp32_screen_check": screen_check,
-        "config3_solver": config3,
     }
     print(json.dumps(line))
     barrier(dist)
@@ -708,7 +822,7 @@ def run_reference(args):
     if rank != 0:
         return
     from cuminlp_gb300 import generators as G
-    problem = G.config2(0)
+    problem = G.config3(0)
     model, cores = cpu_info()
     per_step = max(2.0, min(20.0, 90.0 / max(1, args.steps + args.warmup)))
     for _ in range(args.warmup):
@@ -722,15 +836,16 @@ def run_reference(args):
     value = statistics.mean(vals)
     line = {
         "impl": "reference",
-        "metric": "boxes/s (batched interval B&B box evaluations, FP32 screen + FP64 certify)",
+        "metric": "boxes/s (interval B&B box evaluations per second; FP32 bound with lazy FP64 certification)",
         "value": value, "unit": "boxes/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic (seeded generator, config 2 shape)",
-        "config": {"workload": "config2: n=32 MIQCQP, m=16; reference path (sample + bound of one parent's "
-                               "children per iteration) on the host cores"},
+        "dtype": "f64", "data": "synthetic (seeded generator, config 3 shape)",
+        "config": {"workload": "config3: n=64 MIQCQP, m=32; reference path (sample + bound of one parent's "
+                               "children per iteration, FP64) on the host cores"},
         "cpu_baseline": {"value": value, "unit": "boxes/s", "cores": cores, "kind": "port",
-                         "sample": f"per step: oracle sample+bound of {s['children_per_step']} children for "
-                                   f"~{per_step:.0f} s", "cpu": model},
+                         "sample": f"per step: sample + bound of {s['children_per_step']} children for "
+                                   f"~{per_step:.0f} s, the bound with the host's directed-rounding hardware",
+                         "cpu": model},
         "e2e": {"value": value, "unit": "boxes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))

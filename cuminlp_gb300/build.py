@@ -82,7 +82,7 @@ def build_oracle(force: bool = False) -> Path:
             ROOT / "include" / "cuminlp_gb300.h"]
     if force or _stale(ORACLE_LIB, srcs):
         cc = os.environ.get("CC", "gcc")
-        _run([cc, "-O2", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
+        _run([cc, "-O2", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-frounding-math", "-fPIC", "-shared",
               str(ORACLE_DIR / "oracle.c"), "-o", str(ORACLE_LIB), "-lm", "-lpthread"])
     return ORACLE_LIB
 

@@ -67,6 +67,21 @@ struct cmn_batch {
   cudaGraphExec_t exec = nullptr;
   InstState* h_st = nullptr;  // pinned mirror, valid after pull()
   std::vector<InstDesc> h_desc;
+  std::vector<uint32_t> h_order;  // BatchBufs::order on the host
+
+  // Slots by descending program length (free slots, length 0, last; ties by
+  // slot), uploaded as the launches' walk order.  The order changes only
+  // which thread evaluates which child, never a result.
+  cudaError_t upload_order()
+  {
+    h_order.resize(cfg.K);
+    for (uint64_t i = 0; i < cfg.K; ++i) h_order[i] = (uint32_t)i;
+    std::stable_sort(h_order.begin(), h_order.end(),
+                     [&](uint32_t a, uint32_t x) { return h_desc[a].prog_len > h_desc[x].prog_len; });
+    // pageable source: the copy is staged before the call returns
+    return cudaMemcpyAsync(const_cast<uint32_t*>(b.order), h_order.data(), sizeof(uint32_t) * cfg.K,
+                           cudaMemcpyHostToDevice, stream);
+  }
   std::vector<const cmn_problem*> prob;
   std::vector<cmn_solve_options> opts;
   std::vector<uint8_t> busy;
@@ -227,6 +242,9 @@ extern "C" cmn_status cmn_batch_create(const cmn_batch_config* config, cmn_batch
     A(&b.block_counts, (G + 511) / 512);
     A(&b.block_offsets, (G + 511) / 512);
     A(&b.child_base, K + 2);
+    uint32_t* order = nullptr;
+    A(&order, K);
+    b.order = order;
     A(&b.best_point, K * nm);
     if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&s->h_st), sizeof(InstState) * K);
     if (e != cudaSuccess) {
@@ -244,6 +262,7 @@ extern "C" cmn_status cmn_batch_create(const cmn_batch_config* config, cmn_batch
     std::memset(s->h_st, 0, sizeof(InstState) * K);
     for (uint64_t i = 0; i < K; ++i) s->h_st[i].done = 1;
     e = cudaMemsetAsync(b.desc, 0, sizeof(InstDesc) * K, s->stream);
+    if (e == cudaSuccess) e = s->upload_order();
     if (e == cudaSuccess) e = cudaMemcpyAsync(b.st, s->h_st, sizeof(InstState) * K, cudaMemcpyHostToDevice, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     const int occ = std::max(1, std::min(batch_eval_occupancy(c, fp32), batch_sample_occupancy(c)));
@@ -322,6 +341,7 @@ extern "C" cmn_status cmn_batch_add(cmn_batch* s, const cmn_problem* p, const cm
   s->h_desc[k] = d;
   // pageable source: the copy is staged before the call returns
   BCK(cudaMemcpyAsync(s->b.desc + k, &s->h_desc[k], sizeof(InstDesc), cudaMemcpyHostToDevice, s->stream));
+  BCK(s->upload_order());
   const double gub0 = opts->has_known_primal ? opts->known_primal_bound : DBL_MAX;
   BCK(batch_init_slot(s->cfg, s->b, k, gub0, s->stream));
   s->prob[k] = p;
@@ -544,6 +564,7 @@ extern "C" cmn_status cmn_batch_release(cmn_batch* s, uint64_t slot)
   BCK(cudaSetDevice(s->device));
   s->h_desc[slot] = InstDesc{};
   BCK(cudaMemcpyAsync(s->b.desc + slot, &s->h_desc[slot], sizeof(InstDesc), cudaMemcpyHostToDevice, s->stream));
+  BCK(s->upload_order());
   s->busy[slot] = 0;
   s->prob[slot] = nullptr;
   s->h_st[slot].done = 1;

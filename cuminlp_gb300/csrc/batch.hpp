@@ -107,7 +107,11 @@ struct BatchBufs {
   uint64_t* list_count;
   uint32_t* block_counts;
   uint32_t* block_offsets;
-  uint64_t* child_base;  // [K + 2]: exclusive prefix of live children per slot, then the lane cap
+  uint64_t* child_base;  // [K + 2]: exclusive prefix of live children by `order` position, then the lane cap
+  // [K]: the slots in the order the bound and sample launches walk their
+  // children -- longest program first, so the launch's tail is short
+  // programs (longest-processing-time-first balance)
+  const uint32_t* order;
   double* best_point;  // [K][n_max]
 };
 

@@ -316,9 +316,10 @@ __global__ void batch_branch_kernel(const BatchCfg c, const BatchBufs b)
   }
 }
 
-// Exclusive prefix of the live children per slot (n_parents << B) into
-// child_base[0..K]; child_base[K] is this iteration's live child count and
-// child_base[K + 1] the most lanes any live instance can use per child.
+// Exclusive prefix of the live children per slot (n_parents << B), slots
+// taken in `order`, into child_base[0..K]; child_base[K] is this
+// iteration's live child count and child_base[K + 1] the most lanes any
+// live instance can use per child.
 __global__ void __launch_bounds__(1024) batch_live_kernel(const BatchCfg c, const BatchBufs b)
 {
   __shared__ uint64_t wsum[32];
@@ -336,7 +337,7 @@ __global__ void __launch_bounds__(1024) batch_live_kernel(const BatchCfg c, cons
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (uint64_t base = 0; base < c.K; base += 1024) {
     const uint64_t i = base + threadIdx.x;
-    const uint64_t v = i < c.K ? (b.st[i].n_parents << c.log2C) : 0;
+    const uint64_t v = i < c.K ? (b.st[b.order[i]].n_parents << c.log2C) : 0;
     uint64_t x = v;
     for (int off = 1; off < 32; off <<= 1) {
       const uint64_t y = __shfl_up_sync(0xffffffffu, x, off);
@@ -368,13 +369,13 @@ __global__ void __launch_bounds__(1024) batch_live_kernel(const BatchCfg c, cons
 // Live child i -> its global index slot * child_stride + local.
 __device__ __forceinline__ uint64_t live_child(const BatchCfg& c, const BatchBufs& b, uint64_t i)
 {
-  uint64_t lo = 0, hi = c.K;  // largest slot with child_base[slot] <= i
+  uint64_t lo = 0, hi = c.K;  // largest position with child_base[pos] <= i
   while (hi - lo > 1) {
     const uint64_t mid = (lo + hi) >> 1;
     if (__ldg(b.child_base + mid) <= i) lo = mid;
     else hi = mid;
   }
-  return lo * c.child_stride + (i - __ldg(b.child_base + lo));
+  return (uint64_t)__ldg(b.order + lo) * c.child_stride + (i - __ldg(b.child_base + lo));
 }
 
 // Lanes of a group of 2^lg that run instance d's program on one box: all of

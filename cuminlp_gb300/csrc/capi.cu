@@ -114,6 +114,9 @@ cmn_problem::~cmn_problem()
   dfree(d_root_lb);
   dfree(d_root_ub);
   dfree(d_sched);
+  dfree(d_inc_seg);
+  dfree(d_inc_off);
+  dfree(d_inc_pcs);
   if (cur != device) cudaSetDevice(cur);
 }
 
@@ -167,6 +170,16 @@ extern "C" cmn_status cmn_problem_create(const cmn_problem_desc* desc, cmn_probl
         e = cudaMemcpy(p->d_sched, p->prog.sched.data(), p->prog.sched.size() * sizeof(int32_t),
                        cudaMemcpyHostToDevice);
     }
+    if (e == cudaSuccess && p->prog.inc_ok) {
+      auto up = [&](int32_t** d, const std::vector<int32_t>& h) {
+        if (e == cudaSuccess) e = dalloc(d, std::max<size_t>(1, h.size()));
+        if (e == cudaSuccess && !h.empty())
+          e = cudaMemcpy(*d, h.data(), h.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+      };
+      up(&p->d_inc_seg, p->prog.inc_seg);
+      up(&p->d_inc_off, p->prog.inc_off);
+      up(&p->d_inc_pcs, p->prog.inc_pcs);
+    }
     if (e != cudaSuccess) {
       delete p;
       return fail(CMN_CUDA_ERROR, std::string("uploading the problem: ") + cudaGetErrorString(e));
@@ -196,6 +209,18 @@ extern "C" cmn_status cmn_problem_get_info(const cmn_problem* p, cmn_problem_inf
   out->bytes_per_box = 16.0 * (double)p->host.n_vars() + 17.0;
   out->program_segments = p->prog.n_segments;
   out->lanes_per_box_max = p->prog.group_max;
+  return CMN_OK;
+}
+
+extern "C" cmn_status cmn_problem_program(const cmn_problem* p, int32_t precision, void* out, int64_t capacity,
+                                          int64_t* length)
+{
+  if (!p || !length) return fail(CMN_INVALID_CONFIGURATION, "null argument");
+  if (precision != 0 && precision != 1) return fail(CMN_INVALID_CONFIGURATION, "precision must be 0 or 1");
+  const std::vector<Instr>& code = precision == 0 ? p->prog.code64 : p->prog.code32;
+  *length = (int64_t)code.size();
+  if (out && capacity > 0)
+    std::memcpy(out, code.data(), sizeof(Instr) * (size_t)std::min<int64_t>(capacity, (int64_t)code.size()));
   return CMN_OK;
 }
 
@@ -888,10 +913,14 @@ extern "C" cmn_status cmn_solver_create(const cmn_problem* p, const cmn_solve_op
     return fail(CMN_INVALID_CONFIGURATION,
                 "the sampler's per-thread point columns do not fit in shared memory (a program with shared slots "
                 "keeps one column of n_vars + slots doubles per thread)");
+  const int lg_screen =
+      sample_screen_lg_min((int)p->host.n_vars(), p->prog.n_slots, p->d_sched != nullptr, kEvalThreads);
   if (o.precision == CMN_PRECISION_FP32_LAZY &&
-      sample_screen_smem_bytes((int)p->host.n_vars(), p->prog.n_slots, kEvalThreads) > (size_t)max_dynamic_smem())
+      sample_screen_smem_bytes((int)p->host.n_vars(), p->prog.n_slots, kEvalThreads, lg_screen) >
+          (size_t)max_dynamic_smem())
     return fail(CMN_INVALID_CONFIGURATION, "the lazy form's FP32 sample screen keeps one column of n_vars + slots "
-                                           "floats per thread; this problem's does not fit in shared memory");
+                                           "floats per thread for a program with shared slots; this problem's "
+                                           "does not fit in shared memory");
   try {
     CK(cudaSetDevice(p->device));
     CK(ensure_attributes());
@@ -930,8 +959,9 @@ extern "C" cmn_status cmn_solver_create(const cmn_problem* p, const cmn_solve_op
     s->eval_grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(need, (uint64_t)sm_count() * occ_e));
     s->sample_grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(need, (uint64_t)sm_count() * occ_s));
     if (lazy) {
-      const int occ_q = std::max(1, sample_screen_occupancy(sample_screen_smem_bytes(n, p->prog.n_slots, threads),
-                                                            threads));
+      cfg.screen_lg_min = lg_screen;
+      const int occ_q = std::max(
+          1, sample_screen_occupancy(sample_screen_smem_bytes(n, p->prog.n_slots, threads, lg_screen), threads));
       cfg.screen_grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((maxc + threads - 1) / threads,
                                                                       (uint64_t)sm_count() * occ_q));
     }
@@ -966,6 +996,14 @@ extern "C" cmn_status cmn_solver_create(const cmn_problem* p, const cmn_solve_op
     if (lazy) {
       A(&b.plb, cfg.e_max);
       A(&b.pfeas, cfg.e_max);
+    }
+    cfg.inc = lazy && p->d_inc_seg != nullptr ? 1 : 0;
+    if (cfg.inc) {
+      cfg.inc_segments = p->prog.inc_segments;
+      b.inc_seg = p->d_inc_seg;
+      b.inc_off = p->d_inc_off;
+      b.inc_pcs = p->d_inc_pcs;
+      A(&b.inc_common, 2 * (size_t)cfg.inc_segments * cfg.e_max);
     }
     A(&b.pslot, cfg.e_max);
     A(&b.pinfo, cfg.e_max);

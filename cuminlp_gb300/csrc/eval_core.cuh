@@ -301,10 +301,132 @@ __device__ Iv<T> iv_pown(Iv<T> a, int k)
           a.hi >= T(0) ? powu_ru(a.hi, k) : -powu_rd(-a.hi, k)};
 }
 
+// ---- transcendental enclosures ----
+// Exp, Log, Sin, Cos, Tanh and Pow bound their range by CUDA's math
+// functions at the interval's ends (and at the interior extrema of Sin and
+// Cos), each result moved outward by kTransWiden ulps: the CUDA math
+// library's documented maximum errors are 1-2 ulps in double and 1-4 ulps in
+// float for these functions, so the widened result encloses the exact
+// value.  These enclosures are sound but not tightest, and no reference
+// result pins them bit for bit.
+template <typename T>
+struct Trans;
+template <>
+struct Trans<double> {
+  static constexpr int kWiden = 3;
+  static __device__ __forceinline__ double exp(double x) { return ::exp(x); }
+  static __device__ __forceinline__ double log(double x) { return ::log(x); }
+  static __device__ __forceinline__ double sin(double x) { return ::sin(x); }
+  static __device__ __forceinline__ double cos(double x) { return ::cos(x); }
+  static __device__ __forceinline__ double tanh(double x) { return ::tanh(x); }
+  static __device__ __forceinline__ double pow(double x, double y) { return ::pow(x, y); }
+  static __device__ __forceinline__ double next(double x, double dir) { return ::nextafter(x, dir); }
+  static __device__ __forceinline__ double pi_lo() { return 3.141592653589793; }
+  static __device__ __forceinline__ double pi_hi() { return 3.1415926535897936; }
+};
+template <>
+struct Trans<float> {
+  static constexpr int kWiden = 5;
+  static __device__ __forceinline__ float exp(float x) { return ::expf(x); }
+  static __device__ __forceinline__ float log(float x) { return ::logf(x); }
+  static __device__ __forceinline__ float sin(float x) { return ::sinf(x); }
+  static __device__ __forceinline__ float cos(float x) { return ::cosf(x); }
+  static __device__ __forceinline__ float tanh(float x) { return ::tanhf(x); }
+  static __device__ __forceinline__ float pow(float x, float y) { return ::powf(x, y); }
+  static __device__ __forceinline__ float next(float x, float dir) { return ::nextafterf(x, dir); }
+  static __device__ __forceinline__ float pi_lo() { return 3.14159250f; }
+  static __device__ __forceinline__ float pi_hi() { return 3.14159274f; }
+};
+
+template <typename T>
+__device__ __forceinline__ T widen_down(T x)
+{
+  if (x != x) return x;
+  for (int i = 0; i < Trans<T>::kWiden; ++i) x = Trans<T>::next(x, -Arith<T>::inf());
+  return x;
+}
+template <typename T>
+__device__ __forceinline__ T widen_up(T x)
+{
+  if (x != x) return x;
+  for (int i = 0; i < Trans<T>::kWiden; ++i) x = Trans<T>::next(x, Arith<T>::inf());
+  return x;
+}
+template <typename T>
+__device__ __forceinline__ T clampv(T x, T lo, T hi) { return x < lo ? lo : (x > hi ? hi : x); }
+
+template <typename T>
+__device__ Iv<T> iv_exp(Iv<T> a)
+{
+  const T lo = widen_down(Trans<T>::exp(a.lo));
+  return {lo < T(0) ? T(0) : lo, widen_up(Trans<T>::exp(a.hi))};
+}
+
+// log over the part of the interval inside its domain [0, inf)
+template <typename T>
+__device__ Iv<T> iv_log(Iv<T> a)
+{
+  if (a.hi < T(0)) return {Arith<T>::nan(), Arith<T>::nan()};
+  const T lo = a.lo <= T(0) ? -Arith<T>::inf() : widen_down(Trans<T>::log(a.lo));
+  const T hi = a.hi == T(0) ? -Arith<T>::inf() : widen_up(Trans<T>::log(a.hi));
+  return {lo, hi};
+}
+
+template <typename T>
+__device__ Iv<T> iv_tanh(Iv<T> a)
+{
+  return {clampv(widen_down(Trans<T>::tanh(a.lo)), T(-1), T(1)), clampv(widen_up(Trans<T>::tanh(a.hi)), T(-1), T(1))};
+}
+
+// sin (shift 1) or cos (shift 0): the ends, plus +-1 wherever an extremum
+// (a multiple of pi for cos, pi/2 off it for sin) may lie in the interval;
+// every multiple of pi is located with pi's enclosure, so near-misses count
+// as hits
+template <typename T>
+__device__ Iv<T> iv_trig(Iv<T> a, bool is_sin)
+{
+  using A = Arith<T>;
+  if (!(a.lo <= a.hi)) return {A::nan(), A::nan()};
+  if (a.lo == -A::inf() || a.hi == A::inf()) return {T(-1), T(1)};
+  const T f0 = is_sin ? Trans<T>::sin(a.lo) : Trans<T>::cos(a.lo);
+  const T f1 = is_sin ? Trans<T>::sin(a.hi) : Trans<T>::cos(a.hi);
+  T lo = widen_down(tmin(f0, f1)), hi = widen_up(tmax(f0, f1));
+  const T pl = Trans<T>::pi_lo(), ph = Trans<T>::pi_hi();
+  T tl = tmin(A::div_rd(a.lo, pl), A::div_rd(a.lo, ph));
+  T th = tmax(A::div_ru(a.hi, pl), A::div_ru(a.hi, ph));
+  if (is_sin) {
+    tl = A::sub_rd(tl, T(0.5));
+    th = A::sub_ru(th, T(0.5));
+  }
+  const T jl = ceil(widen_down(tl)), jh = floor(widen_up(th));
+  if (!(jh - jl < T(2))) return {T(-1), T(1)};
+  for (T j = jl; j <= jh; j = j + T(1)) {
+    const T half = j * T(0.5);
+    if (half == floor(half)) hi = T(1);  // even multiple: a maximum
+    else lo = T(-1);                      // odd: a minimum
+  }
+  return {clampv(lo, T(-1), T(1)), clampv(hi, T(-1), T(1))};
+}
+
+// a^b for a clipped to [0, inf), enclosed as exp(b * log(a))
+template <typename T>
+__device__ Iv<T> iv_pow(Iv<T> a, Iv<T> b)
+{
+  if (a.hi < T(0)) return {Arith<T>::nan(), Arith<T>::nan()};
+  const Iv<T> x = {a.lo < T(0) ? T(0) : a.lo, a.hi};
+  return iv_exp(iv_mul(b, iv_log(x)));
+}
+
 template <typename T>
 __device__ __forceinline__ Iv<T> iv_generic(uint8_t op, Iv<T> a, Iv<T> b, int k)
 {
   switch (op) {
+    case kGExp: return iv_exp(a);
+    case kGLog: return iv_log(a);
+    case kGSin: return iv_trig(a, true);
+    case kGCos: return iv_trig(a, false);
+    case kGTanh: return iv_tanh(a);
+    case kGPow: return iv_pow(a, b);
     case kGAdd: return iv_add(a, b);
     case kGSub: return iv_sub(a, b);
     case kGMul: return iv_mul(a, b);
@@ -337,6 +459,12 @@ __device__ __forceinline__ double pt_generic(uint8_t op, double a, double b, int
     case kGAbs: return fabs(a);
     case kGMin: return fmin(a, b);
     case kGMax: return fmax(a, b);
+    case kGExp: return exp(a);
+    case kGLog: return log(a);
+    case kGSin: return sin(a);
+    case kGCos: return cos(a);
+    case kGTanh: return tanh(a);
+    case kGPow: return pow(a, b);
     default: return A::nan();
   }
 }
@@ -456,6 +584,24 @@ __device__ __forceinline__ Verdict<T> verdict_init()
   return out;
 }
 
+// The term t of a TERM instruction: x_a * x_b, sqr(x_a) or x_a, times the
+// coefficient when it has one.
+template <typename T, typename V>
+__device__ __forceinline__ Iv<T> term_value(const Instr& cur, int sub, const V& vars)
+{
+  Iv<T> p;
+  const int pk = sub & kTermPMask;
+  if (pk == kTermProd) {
+    p = iv_mul<T, (CMN_FP64_EMU & 32) != 0>(vars.var(cur.a), vars.var(cur.b));
+  } else if (pk == kTermSqr) {
+    p = iv_sqr<T, (CMN_FP64_EMU & 32) != 0>(vars.var(cur.a));
+  } else {
+    p = vars.var(cur.a);
+  }
+  if (sub & kTermHasC) p = iv_scale<T, (CMN_FP64_EMU & 64) != 0>(const_of<T>(cur), p);
+  return p;
+}
+
 // Interval interpretation of instructions [pc0, pc1) for this thread's box,
 // starting from a zero accumulator: variables from `vars` (anything with
 // var(v) -> Iv<T>), program slots in `t`.  Checks fold into `out` with AND /
@@ -473,16 +619,7 @@ __device__ __forceinline__ void interval_range(const Instr* __restrict__ prog, i
     const int sub = cur.head >> 3;
     switch (code) {
       case kOpTerm: {
-        Iv<T> p;
-        const int pk = sub & kTermPMask;
-        if (pk == kTermProd) {
-          p = iv_mul<T, (CMN_FP64_EMU & 32) != 0>(vars.var(cur.a), vars.var(cur.b));
-        } else if (pk == kTermSqr) {
-          p = iv_sqr<T, (CMN_FP64_EMU & 32) != 0>(vars.var(cur.a));
-        } else {
-          p = vars.var(cur.a);
-        }
-        if (sub & kTermHasC) p = iv_scale<T, (CMN_FP64_EMU & 64) != 0>(const_of<T>(cur), p);
+        const Iv<T> p = term_value<T, V>(cur, sub, vars);
         if (sub & kTermInit) acc = p;
         else if (sub & kTermSub) acc = iv_sub(acc, p);
         else acc = iv_add(acc, p);
@@ -533,6 +670,50 @@ __device__ Verdict<T> run_interval(const Instr* __restrict__ prog, int len, cons
   Verdict<T> out = verdict_init<T>();
   interval_range<T, V>(prog, 0, len, vars, t, out);
   return out;
+}
+
+// ---- incremental chain evaluation (the lazy form's FP32 children) ----
+// acc <- acc + (the instruction's term) for a chain instruction (a TERM,
+// whose kTermInit only means "first of its chain", or a LoadAcc), so a
+// chain can be summed in any grouping of its terms: every partial sum is
+// an outward-rounded enclosure of the exact one.
+template <typename T, typename V>
+__device__ __forceinline__ Iv<T> chain_add(Iv<T> acc, const Instr& cur, const V& vars)
+{
+  const int code = cur.head & 7, sub = cur.head >> 3;
+  if (code == kOpTerm) {
+    const Iv<T> p = term_value<T, V>(cur, sub, vars);
+    return (sub & kTermSub) ? iv_sub(acc, p) : iv_add(acc, p);
+  }
+  const int mode = cur.modes & 3;  // LoadAcc: a variable or a constant
+  return iv_add(acc, mode == kModeVar ? vars.var(cur.a) : const_of<T>(cur));
+}
+
+// The checks and objective [pc0, pc1) that read a chain's value `acc`
+// (interval_range's kOpCheck / kOpObjective).
+template <typename T, typename V>
+__device__ __forceinline__ void chain_tail(const Instr* __restrict__ prog, int pc0, int pc1, const V& vars,
+                                           Iv<T> acc, Verdict<T>& out)
+{
+  for (int pc = pc0; pc < pc1; ++pc) {
+    const Instr cur = load_instr(prog, pc);
+    const int code = cur.head & 7, sub = cur.head >> 3, mode = cur.modes & 3;
+    const Iv<T> v = mode == kModeAcc ? acc : (mode == kModeVar ? vars.var(cur.a) : const_of<T>(cur));
+    if (code == kOpCheck) {
+      const double rhs = cur.c;
+      const double lo = (double)v.lo, hi = (double)v.hi;
+      if (sub == 0) {
+        out.feasible = out.feasible && (lo <= rhs);
+        out.excluded = out.excluded || (lo > rhs);
+      } else {
+        out.feasible = out.feasible && (lo <= rhs && rhs <= hi);
+        out.excluded = out.excluded || (lo > rhs || hi < rhs);
+      }
+    } else if (code == kOpObjective) {
+      out.obj = v;
+      out.has_obj = true;
+    }
+  }
 }
 
 // Segments of `lane` in a group of 2^l lanes: [b, e) indexes the (pc0, pc1)
@@ -781,6 +962,12 @@ __device__ __forceinline__ float pt32_generic(uint8_t op, float a, float b, int 
     case kGAbs: return fabsf(a);
     case kGMin: return fminf(a, b);
     case kGMax: return fmaxf(a, b);
+    case kGExp: return expf(a);
+    case kGLog: return logf(a);
+    case kGSin: return sinf(a);
+    case kGCos: return cosf(a);
+    case kGTanh: return tanhf(a);
+    case kGPow: return powf(a, b);
     default: return Arith<float>::nan();
   }
 }

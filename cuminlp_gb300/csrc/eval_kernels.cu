@@ -277,6 +277,117 @@ __device__ __forceinline__ void eval_children(const EvalArgs& a, const S* plo, c
   }
 }
 
+// Whether variable v is parent k's split variable of a slot before `j`
+// (ovid holds this thread's slot variables at stride `stride`).
+__device__ __forceinline__ bool split_before(const int32_t* ovid, int stride, int j, int v)
+{
+  for (int q = 0; q < j; ++q)
+    if (ovid[q * stride] == v) return true;
+  return false;
+}
+
+// Lazy form, incremental children, pass 1: for every (segment s, parent
+// k), the sum of segment s's chain terms that read none of k's split
+// variables, over the parent's FP32 planes.  A warp covers 32 parents of
+// one segment, so the instruction stream is the same across the warp and
+// the parent planes are read coalesced.
+__global__ void __launch_bounds__(kEvalThreads) inc_common_kernel(const EvalArgs a)
+{
+  if (a.done != nullptr && *a.done) return;
+  const uint64_t E = *a.n_parents_dev;
+  const uint64_t total = E * (uint64_t)a.inc_segments;
+  for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t s = idx / E, k = idx - s * E;
+    const ParentInfo pi = a.pinfo[k];
+    if (pi.nreg == 0) continue;  // dropped on certification: no children
+    const SlotPlan* sp = a.slots + k * (uint64_t)a.max_slots;
+    uint64_t mask = 0;
+    for (uint32_t j = 0; j < pi.count; ++j) mask |= 1ULL << (sp[j].vid & 63);
+    ChildVars<float, float> pv;
+    pv.plo = a.plo32 + k;
+    pv.phi = a.phi32 + k;
+    pv.pstride = a.pstride;
+    pv.mask = 0;  // the parent's own bounds for every variable
+    pv.count = 0;
+    auto is_split = [&](int v) {
+      if (!((mask >> (v & 63)) & 1ULL)) return false;
+      for (uint32_t j = 0; j < pi.count; ++j)
+        if (sp[j].vid == (uint32_t)v) return true;
+      return false;
+    };
+    Iv<float> acc = {0.0f, 0.0f};
+    const int b = __ldg(a.inc_seg + 3 * s), t = __ldg(a.inc_seg + 3 * s + 1);
+    for (int pc = b; pc < t; ++pc) {
+      const Instr cur = load_instr(a.prog, pc);
+      const int code = cur.head & 7;
+      const bool reads_var = code == kOpTerm || (cur.modes & 3) == kModeVar;
+      if (reads_var && (is_split(cur.a) || (code == kOpTerm && is_split(cur.b)))) continue;
+      acc = chain_add<float, ChildVars<float, float>>(acc, cur, pv);
+    }
+    a.inc_common[2 * (s * a.pstride + k)] = acc.lo;
+    a.inc_common[2 * (s * a.pstride + k) + 1] = acc.hi;
+  }
+}
+
+// Lazy form, incremental children, pass 2: each child starts every
+// segment's chain from its parent's common sum and adds the terms that read
+// its split variables -- for each split variable in slot order, its terms
+// in program order, a term reading two split variables taken with the
+// first of them -- then runs the segment's checks and objective.  One lane
+// per child; shared memory holds the child's split variables as in
+// eval_children.
+__global__ void __launch_bounds__(kEvalThreads, CMN_EVAL_MIN_BLOCKS) eval_children_inc_kernel(const EvalArgs a)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float* base = reinterpret_cast<float*>(smem_raw);
+  const int B = blockDim.x;
+  const int ms = a.max_slots;
+  float* olo = base + threadIdx.x;
+  float* ohi = olo + (size_t)ms * B;
+  int32_t* ovid = reinterpret_cast<int32_t*>(base + (size_t)2 * ms * B) + threadIdx.x;
+  if (a.done != nullptr && *a.done) return;
+  const uint64_t total = a.n_children_dev ? *a.n_children_dev : a.n_children;
+  const double gub = a.gub ? *a.gub : DBL_MAX;
+  const int S = a.inc_segments;
+  for (uint64_t g = (uint64_t)blockIdx.x * B + threadIdx.x; g < total; g += (uint64_t)gridDim.x * B) {
+    uint64_t k, r;
+    child_of(a.log2C, g, k, r);
+    const ParentInfo pi = a.pinfo[k];
+    if (pi.fathom || r >= pi.nreg) {
+      a.out_flag[g] = kChildNone;
+      continue;
+    }
+    bool dup;
+    const ChildVars<float, float> cv = child_vars<float, float>(a, a.plo32, a.phi32, k, r, olo, ohi, ovid, B, dup);
+    if (dup) {
+      a.out_flag[g] = kChildDuplicate;
+      continue;
+    }
+    Verdict<float> v = verdict_init<float>();
+    for (int s = 0; s < S; ++s) {
+      Iv<float> acc = {a.inc_common[2 * ((uint64_t)s * a.pstride + k)],
+                       a.inc_common[2 * ((uint64_t)s * a.pstride + k) + 1]};
+      for (int j = 0; j < cv.count; ++j) {
+        const int vj = ovid[j * B];
+        if (split_before(ovid, B, j, vj)) continue;  // the same variable in two slots
+        const int q0 = __ldg(a.inc_off + (uint64_t)vj * S + s), q1 = __ldg(a.inc_off + (uint64_t)vj * S + s + 1);
+        for (int q = q0; q < q1; ++q) {
+          const Instr cur = load_instr(a.prog, __ldg(a.inc_pcs + q));
+          if ((cur.head & 7) == kOpTerm) {
+            const int other = cur.a == vj ? cur.b : cur.a;
+            if (other != vj && split_before(ovid, B, j, other)) continue;  // taken with that variable
+          }
+          acc = chain_add<float, ChildVars<float, float>>(acc, cur, cv);
+        }
+      }
+      chain_tail<float, ChildVars<float, float>>(a.prog, __ldg(a.inc_seg + 3 * s + 1), __ldg(a.inc_seg + 3 * s + 2),
+                                                 cv, acc, v);
+    }
+    write_verdict<float, 5>(a, g, k, v, gub);
+  }
+}
+
 template <typename T, int kMode>
 __global__ void __launch_bounds__(kEvalThreads, CMN_EVAL_MIN_BLOCKS) eval_children_kernel(const EvalArgs a)
 {
@@ -572,46 +683,64 @@ __global__ void __launch_bounds__(kEvalThreads) sample_children_kernel(const Sam
 
 // The lazy form's sample screen: every sampled child's S points (or its
 // exact point) in FP32, keeping per child the smallest FP32 value and its
-// sample index in cbest[g].  Children not sampled get +inf.  One lane per
-// child; no barriers.
+// sample index in cbest[g].  Children not sampled get +inf.  Groups of
+// 2^lg_min lanes share a child and one shared-memory point column (lane j
+// stages variables j, j + G, ... and runs its segments of the lane
+// schedule), so a point of n variables costs 4n/G bytes per thread; with
+// lg_min = 0 a lane evaluates its child alone.  The loop bound is per
+// block, so every lane of a warp reaches the shuffles and barriers.
 __global__ void __launch_bounds__(kEvalThreads) sample_screen_kernel(const SampleArgs a)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float* base = reinterpret_cast<float*>(smem_raw);
   const int B = blockDim.x;
+  const int lg = a.lg_min;
+  const int G = 1 << lg;
+  const int lane = threadIdx.x & (G - 1);
+  const int cols = B >> lg;
   Tile<float> t;
   t.lo = base;
   t.hi = base;
-  t.slo = base + (size_t)a.n_vars * B;
+  t.slo = base + (size_t)a.n_vars * cols;
   t.shi = t.slo;
-  t.stride = B;
-  t.tid = threadIdx.x;
+  t.stride = cols;
+  t.tid = threadIdx.x >> lg;
   if (a.done != nullptr && *a.done) return;
   const uint64_t total = a.n_children_dev ? *a.n_children_dev : a.n_children;
   const uint64_t salt_base = a.salt_base_dev ? *a.salt_base_dev : 0;
-  for (uint64_t g = (uint64_t)blockIdx.x * B + threadIdx.x; g < total; g += (uint64_t)gridDim.x * B) {
+  const uint64_t per_block = (uint64_t)cols;
+  const uint64_t S_loop = a.exact ? 1 : a.S;
+  int32_t p0 = 0, p1 = a.prog_len;  // this lane's segments (lg > 0: the lane schedule)
+  LaneSegs ls = {nullptr, 0, 0};
+  if (lg > 0) ls = lane_segments(a.sched, lg, lane);
+  for (uint64_t bb = (uint64_t)blockIdx.x * per_block; bb < total; bb += (uint64_t)gridDim.x * per_block) {
+    const uint64_t g = bb + (threadIdx.x >> lg);
     Best32 best = {INFINITY, 0};
-    uint64_t k, r;
-    child_of(a.log2C, g, k, r);
+    bool live = g < total;
+    uint64_t k = 0, r = 0;
     bool fathom = a.exact != 0;
-    uint64_t nreg = ~0ULL;
-    if (a.pinfo != nullptr) {
-      const ParentInfo pi = a.pinfo[k];
-      nreg = pi.nreg;
-      fathom = fathom || pi.fathom;
+    if (live) {
+      child_of(a.log2C, g, k, r);
+      uint64_t nreg = ~0ULL;
+      if (a.pinfo != nullptr) {
+        const ParentInfo pi = a.pinfo[k];
+        nreg = pi.nreg;
+        fathom = fathom || pi.fathom;
+      }
+      live = r < nreg;
+      if (live && a.state != nullptr && !fathom) {
+        const uint8_t st = a.state[g];
+        live = a.sample_all ? (st != kChildNone) : (st == kChildEligible);
+      }
     }
-    bool take = r < nreg;
-    if (take && a.state != nullptr && !fathom) {
-      const uint8_t st = a.state[g];
-      take = a.sample_all ? (st != kChildNone) : (st == kChildEligible);
-    }
-    if (take) {
-      const SlotPlan* sp = a.pinfo ? a.slots + k * (uint64_t)a.max_slots : nullptr;
-      const uint32_t count = a.pinfo ? a.pinfo[k].count : 0;
-      const uint64_t salt = a.salt_base_dev ? salt_base + k + 1 : a.salt;
-      const uint64_t S = fathom ? 1 : a.S;
-      for (uint64_t i = 0; i < S; ++i) {
-        for (int v = 0; v < a.n_vars; ++v) {
+    const SlotPlan* sp = a.pinfo ? a.slots + k * (uint64_t)a.max_slots : nullptr;
+    const uint32_t count = (live && a.pinfo) ? a.pinfo[k].count : 0;
+    const uint64_t salt = a.salt_base_dev ? salt_base + k + 1 : a.salt;
+    const uint64_t S = fathom ? 1 : a.S;
+    for (uint64_t i = 0; i < S_loop; ++i) {
+      const bool act = live && i < S;
+      if (act) {
+        for (int v = lane; v < a.n_vars; v += G) {
           double lo = a.plo[(uint64_t)v * a.pstride + k];
           double hi = a.phi[(uint64_t)v * a.pstride + k];
           for (uint32_t j = 0; j < count; ++j) {
@@ -621,18 +750,37 @@ __global__ void __launch_bounds__(kEvalThreads) sample_screen_kernel(const Sampl
             }
           }
           const double x = fathom ? lo : sample_value(a.var_kinds[v] != 0, lo, hi, (uint64_t)v, i, r, salt);
-          t.lo[v * B + t.tid] = __double2float_rn(x);
+          t.lo[v * cols + t.tid] = __double2float_rn(x);
         }
-        PointVerdict32 pv;
-        pv.obj = INFINITY;
-        pv.feasible = true;
-        pv.has_obj = false;
-        point_range32(a.prog, 0, a.prog_len, t, pv);
-        const float value = (pv.feasible && !(pv.obj != pv.obj)) ? pv.obj : INFINITY;
-        if (value < best.value) best = Best32{value, (uint32_t)i};
       }
+      __syncwarp();
+      PointVerdict32 pv;
+      pv.obj = INFINITY;
+      pv.feasible = true;
+      pv.has_obj = false;
+      if (act) {
+        if (lg == 0) {
+          point_range32(a.prog, p0, p1, t, pv);
+        } else {
+          for (int j = ls.b; j < ls.e; ++j)
+            point_range32(a.prog, __ldg(ls.pairs + 2 * j), __ldg(ls.pairs + 2 * j + 1), t, pv);
+        }
+      }
+      for (int off = 1; off < G; off <<= 1) {  // the group's verdict
+        const int f = __shfl_xor_sync(0xffffffffu, (int)pv.feasible, off);
+        const int h = __shfl_xor_sync(0xffffffffu, (int)pv.has_obj, off);
+        const float o = __shfl_xor_sync(0xffffffffu, pv.obj, off);
+        pv.feasible = pv.feasible && f;
+        if (!pv.has_obj && h) {
+          pv.obj = o;
+          pv.has_obj = true;
+        }
+      }
+      const float value = (pv.feasible && !(pv.obj != pv.obj)) ? pv.obj : INFINITY;
+      if (act && value < best.value) best = Best32{value, (uint32_t)i};
+      __syncwarp();  // the column is restaged next
     }
-    a.cbest[g] = best;
+    if (g < total && lane == 0) a.cbest[g] = best;
   }
 }
 
@@ -791,6 +939,16 @@ static cudaError_t launch_eval_t(const EvalArgs& a, int grid, int threads, cudaS
   return cudaGetLastError();
 }
 
+cudaError_t launch_inc(const EvalArgs& a, int grid, int threads, cudaStream_t s)
+{
+  inc_common_kernel<<<grid, threads, 0, s>>>(a);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const size_t smem = (size_t)(8 + 4) * a.max_slots * threads;
+  eval_children_inc_kernel<<<grid, threads, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_eval(const EvalArgs& a, int mode, bool fp32, int grid, int threads, cudaStream_t s)
 {
   if (fp32) {
@@ -804,14 +962,22 @@ cudaError_t launch_eval(const EvalArgs& a, int mode, bool fp32, int grid, int th
   return launch_eval_t<double, 3>(a, grid, threads, s);
 }
 
-size_t sample_screen_smem_bytes(int n_vars, int n_slots, int threads)
+size_t sample_screen_smem_bytes(int n_vars, int n_slots, int threads, int lg_min)
 {
-  return 4 * (size_t)(n_vars + n_slots) * threads;
+  return 4 * (size_t)(n_vars + n_slots) * (size_t)(threads >> lg_min);
+}
+
+int sample_screen_lg_min(int n_vars, int n_slots, bool has_sched, int threads)
+{
+  if (!has_sched) return 0;
+  int lg = 0;
+  while (lg < 5 && sample_screen_smem_bytes(n_vars, n_slots, threads, lg) > kSampleColumnBytes) ++lg;
+  return lg;
 }
 
 cudaError_t launch_sample_screen(const SampleArgs& a, int grid, int threads, cudaStream_t s)
 {
-  sample_screen_kernel<<<grid, threads, sample_screen_smem_bytes(a.n_vars, a.n_slots, threads), s>>>(a);
+  sample_screen_kernel<<<grid, threads, sample_screen_smem_bytes(a.n_vars, a.n_slots, threads, a.lg_min), s>>>(a);
   return cudaGetLastError();
 }
 

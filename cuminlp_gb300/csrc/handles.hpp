@@ -20,6 +20,9 @@ struct cmn_problem {
   double* d_root_lb = nullptr;
   double* d_root_ub = nullptr;
   int32_t* d_sched = nullptr;  // lane schedules (Program::sched), null when none
+  int32_t* d_inc_seg = nullptr;  // incremental child tables (Program::inc_*), null when none
+  int32_t* d_inc_off = nullptr;
+  int32_t* d_inc_pcs = nullptr;
 
   ~cmn_problem();
 };

@@ -125,6 +125,15 @@ struct EvalArgs {
   const uint32_t* done;           // solver: nonzero once the search stopped
   const uint32_t* use_screen;     // FP32 screen: zero passes every child to the certify pass
   const double* parent_lb;        // lazy form: the parents' certified FP64 lower bounds
+  // lazy form, incremental children (Program::inc_*): per (segment, parent)
+  // the chain sums of the terms that touch no split variable, (lo, hi)
+  // pairs at inc_common[2 * (s * pstride + k)]
+  int inc_segments;
+  const uint64_t* n_parents_dev;
+  const int32_t* inc_seg;
+  const int32_t* inc_off;
+  const int32_t* inc_pcs;
+  float* inc_common;
   // lane groups (null sched: one lane per box); see Program::sched
   const int32_t* sched;
   int g_max;

@@ -28,7 +28,9 @@ size_t sample_smem_bytes(int n_vars, int n_slots, int threads, int lg_min);
 // no lane schedule and keep one column per thread.
 constexpr size_t kSampleColumnBytes = 32 * 1024;
 int sample_lg_min(int n_vars, int n_slots, bool has_sched, int threads);
-size_t sample_screen_smem_bytes(int n_vars, int n_slots, int threads);
+size_t sample_screen_smem_bytes(int n_vars, int n_slots, int threads, int lg_min);
+// the lazy form's FP32 sample screen: one point column (FP32) per 2^lg_min lanes
+int sample_screen_lg_min(int n_vars, int n_slots, bool has_sched, int threads);
 
 // mode 0: role / raw boxes; 1: solver FP64; 2: solver FP32 screen (fp32
 // must be true); 3: solver FP64 certify over EvalArgs::list; 4: aggregate
@@ -36,6 +38,9 @@ size_t sample_screen_smem_bytes(int n_vars, int n_slots, int threads);
 // form, FP32 children bounded by the parents' certified bounds (fp32 true)
 cudaError_t launch_eval(const EvalArgs& a, int mode, bool fp32, int grid, int threads, cudaStream_t s);
 cudaError_t launch_sample(const SampleArgs& a, int grid, int threads, cudaStream_t s);
+// the lazy form's incremental FP32 children: the common chain sums per
+// (segment, parent), then every child (EvalArgs::inc_* set, prog = FP32)
+cudaError_t launch_inc(const EvalArgs& a, int grid, int threads, cudaStream_t s);
 // the lazy form's FP32 sample screen (SampleArgs::cbest out, prog = the
 // FP32 point program)
 cudaError_t launch_sample_screen(const SampleArgs& a, int grid, int threads, cudaStream_t s);

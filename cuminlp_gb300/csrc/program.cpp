@@ -50,7 +50,8 @@ static bool interval_op(int op)
   switch (op) {
     case CMN_OP_ADD: case CMN_OP_SUB: case CMN_OP_MUL: case CMN_OP_DIV: case CMN_OP_SQR:
     case CMN_OP_NEG: case CMN_OP_SQRT: case CMN_OP_POWN: case CMN_OP_ABS: case CMN_OP_MIN:
-    case CMN_OP_MAX:
+    case CMN_OP_MAX: case CMN_OP_EXP: case CMN_OP_LOG: case CMN_OP_SIN: case CMN_OP_COS:
+    case CMN_OP_TANH: case CMN_OP_POW:
       return true;
     default:
       return false;
@@ -284,6 +285,7 @@ class Compiler {
     emit_all();
     out_.n_slots = max_slots_;
     build_schedule();
+    build_incremental();
     out_.code32 = out_.code64;
     out_.code32p = out_.code64;
     for (size_t k = 0; k < out_.code64.size(); ++k) {
@@ -366,6 +368,74 @@ class Compiler {
       if (out_.makespan[l] * 5 > out_.makespan[l - 1] * 4) break;
       out_.group_max = 1 << l;
     }
+  }
+
+  // Segments of a slot-free program as sum chains plus their readers, and
+  // per (variable, segment) the chain instructions that read the variable
+  // (Program::inc_*).  Leaves inc_ok false for any other shape.
+  void build_incremental()
+  {
+    const std::vector<Instr>& code = out_.code64;
+    const int len = (int)code.size();
+    const int n = (int)p_.n_vars();
+    if (out_.n_slots != 0 || len == 0) return;
+    auto accumulates = [](const Instr& in) {
+      const int code = in.head & 7;
+      return code == kOpTerm || code == kOpLoadAcc;
+    };
+    auto starts = [](const Instr& in) {
+      const int code = in.head & 7, sub = in.head >> 3;
+      return (code == kOpTerm && (sub & kTermInit)) || code == kOpLoadAcc;
+    };
+    std::vector<int32_t> seg;
+    int pc = 0;
+    while (pc < len) {
+      const int b = pc;
+      int t = pc;
+      if (starts(code[pc])) {
+        t = pc + 1;
+        while (t < len && accumulates(code[t]) && !starts(code[t])) ++t;
+      }
+      int e = t;
+      while (e < len && !accumulates(code[e])) {
+        const int c = code[e].head & 7;
+        if (c != kOpCheck && c != kOpObjective) return;  // slots or other forms
+        ++e;
+      }
+      if (e == b) return;  // an accumulating instruction that does not start a chain
+      seg.push_back(b);
+      seg.push_back(t);
+      seg.push_back(e);
+      pc = e;
+    }
+    const int S = (int)seg.size() / 3;
+    std::vector<std::vector<int32_t>> lists((size_t)n * S);
+    for (int s = 0; s < S; ++s) {
+      for (int q = seg[3 * s]; q < seg[3 * s + 1]; ++q) {
+        const Instr& in = code[q];
+        const int c = in.head & 7;
+        int va = -1, vb = -1;
+        if (c == kOpTerm) {
+          va = in.a;
+          vb = in.b;
+        } else if ((in.modes & 3) == kModeVar) {  // LoadAcc of a variable
+          va = vb = in.a;
+        }
+        if (va >= n || vb >= n) return;
+        if (va >= 0) lists[(size_t)va * S + s].push_back(q);
+        if (vb >= 0 && vb != va) lists[(size_t)vb * S + s].push_back(q);
+      }
+    }
+    out_.inc_seg = seg;
+    out_.inc_segments = S;
+    out_.inc_off.assign((size_t)n * S + 1, 0);
+    out_.inc_pcs.clear();
+    for (size_t i = 0; i < lists.size(); ++i) {
+      out_.inc_off[i] = (int32_t)out_.inc_pcs.size();
+      out_.inc_pcs.insert(out_.inc_pcs.end(), lists[i].begin(), lists[i].end());
+    }
+    out_.inc_off[lists.size()] = (int32_t)out_.inc_pcs.size();
+    out_.inc_ok = true;
   }
 
   bool is_var(int64_t id) const { return p_.nodes[id].op == CMN_OP_VAR; }

@@ -59,8 +59,14 @@ enum GenericOp : uint8_t {
   kGDiv = 5,
   kGSqr = 6,
   kGNeg = 7,
+  kGExp = 8,
+  kGLog = 9,
   kGSqrt = 10,
+  kGSin = 11,
+  kGCos = 12,
+  kGTanh = 13,
   kGPowN = 14,
+  kGPow = 15,
   kGAbs = 16,
   kGMin = 17,
   kGMax = 18,

@@ -50,6 +50,21 @@ struct Program {
   int group_max = 1;               // largest G that still shortens a box's critical path
   std::vector<int32_t> sched;
   std::vector<int64_t> makespan;   // instructions on the busiest lane, per level
+  // Incremental child evaluation (the lazy form's FP32 children), built for
+  // a slot-free program whose segments are each one sum chain -- a LoadAcc
+  // or an initialising TERM, then TERMs -- followed by the checks and the
+  // objective that read it.  The chain terms that touch none of a parent's
+  // split variables are summed once per parent; each child adds the terms
+  // that touch its split variables.
+  bool inc_ok = false;
+  int inc_segments = 0;
+  // per segment s: pcs [inc_seg[3s], inc_seg[3s+1]) accumulate,
+  // [inc_seg[3s+1], inc_seg[3s+2]) are its checks / objective
+  std::vector<int32_t> inc_seg;
+  // the accumulating instructions of segment s that read variable v:
+  // inc_pcs[inc_off[v * inc_segments + s] .. inc_off[v * inc_segments + s + 1])
+  std::vector<int32_t> inc_off;
+  std::vector<int32_t> inc_pcs;
 };
 
 // Compiles the reachable DAG into the fused straight-line program.

@@ -110,7 +110,10 @@ struct SolverCfg {
   uint64_t eval_capacity;    // resident threads of the bound kernels
   uint64_t sample_capacity;  // resident threads of the sampler
   int screen_grid;           // lazy form: blocks of the FP32 sample screen
+  int screen_lg_min;         // and its lanes per point column
   int sample_lg_min;         // sampler point columns: one per 2^sample_lg_min lanes
+  int inc;                   // lazy form: children by the incremental chain sums
+  int inc_segments;
 };
 
 struct SolverBufs {
@@ -152,6 +155,12 @@ struct SolverBufs {
   double* clb;
   uint8_t* cstate;
   Best32* cbest;         // lazy form: the FP32 sample screen's best per child
+  // lazy form, incremental children: the program's tables and the common
+  // chain sums [segment][parent] (lo, hi)
+  const int32_t* inc_seg;
+  const int32_t* inc_off;
+  const int32_t* inc_pcs;
+  float* inc_common;
   uint32_t* list;        // certify list
   // compaction scratch
   uint32_t* block_counts;

@@ -1432,7 +1432,17 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
     ea.plo32 = b.plo32;
     ea.phi32 = b.phi32;
     ea.parent_lb = b.plb;
-    e = launch_eval(ea, 5, true, eval_grid, kEvalThreads, s);
+    if (cfg.inc) {
+      ea.inc_segments = cfg.inc_segments;
+      ea.n_parents_dev = &b.dev->n_parents;
+      ea.inc_seg = b.inc_seg;
+      ea.inc_off = b.inc_off;
+      ea.inc_pcs = b.inc_pcs;
+      ea.inc_common = b.inc_common;
+      e = launch_inc(ea, eval_grid, kEvalThreads, s);
+    } else {
+      e = launch_eval(ea, 5, true, eval_grid, kEvalThreads, s);
+    }
     if (e != cudaSuccess) return e;
     // the survivors within the band below the incumbent, in FP64
     ScreenedChild sc{b};
@@ -1442,6 +1452,7 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
     ca.prog = b.prog64;
     ca.plo32 = nullptr;
     ca.phi32 = nullptr;
+    ca.inc_segments = 0;
     ca.list = b.list;
     ca.list_count = &b.dev->certify_count;
     e = launch_eval(ca, 3, false, eval_grid, kEvalThreads, s);
@@ -1495,7 +1506,7 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
   if (cfg.precision == CMN_PRECISION_FP32_LAZY) {
     // FP32 screen of every sample, then each chunk's best in FP64
     SampleArgs qa = sa;
-    qa.lg_min = 0;  // one FP32 column per thread
+    qa.lg_min = cfg.screen_lg_min;
     qa.prog = b.prog32p;
     qa.cbest = b.cbest;
     e = launch_sample_screen(qa, cfg.screen_grid, kEvalThreads, s);

@@ -13,13 +13,67 @@ return a candidate (found, value, point, index).  ``solve()`` mirrors
 from __future__ import annotations
 
 import ctypes as C
-from dataclasses import dataclass
+from dataclasses import dataclass, field
 
 import numpy as np
 
 from . import _abi as A
 from ._lib import check, lib
 from .problem import Problem
+
+
+K_MAX_SLOTS = 64  # config::kMaxSlots
+
+
+# -- the library's host builds of the branching policy and the decode ------
+@dataclass
+class SlotAssignment:
+    kinds: list = field(default_factory=list)
+    var_ids: list = field(default_factory=list)
+    widths: list = field(default_factory=list)
+    domains: list = field(default_factory=list)
+
+    def size(self) -> int:
+        return len(self.kinds)
+
+    def key(self) -> tuple:
+        return (tuple(self.kinds), tuple(self.var_ids), tuple(self.widths))
+
+
+def bisection_choose(box, var_kinds, budget_bits: int, max_cycle: int = 0, enumerate_cap: int = 0,
+                     relative: bool = False) -> SlotAssignment:
+    """BisectionBudgetCompositionPolicy::choose on the host (cmn_bisection_choose)."""
+    box = np.ascontiguousarray(box, dtype=np.float64)
+    vk = np.ascontiguousarray(var_kinds, dtype=np.int32)
+    kinds = np.zeros(K_MAX_SLOTS, dtype=np.uint8)
+    vids = np.zeros(K_MAX_SLOTS, dtype=np.uint64)
+    widths = np.zeros(K_MAX_SLOTS, dtype=np.uint64)
+    doms = np.zeros(K_MAX_SLOTS, dtype=np.uint64)
+    cnt = C.c_int64()
+    check(lib().cmn_bisection_choose(A.ptr(box), A.ptr(vk), len(vk), int(budget_bits), int(max_cycle),
+                                     int(enumerate_cap), int(relative), A.ptr(kinds), A.ptr(vids), A.ptr(widths),
+                                     A.ptr(doms), C.byref(cnt), None))
+    c = cnt.value
+    return SlotAssignment([int(x) for x in kinds[:c]], [int(x) for x in vids[:c]], [int(x) for x in widths[:c]],
+                          [int(x) for x in doms[:c]])
+
+
+def slot_bounds(kind: int, plo: float, phi: float, part: int, fan_out: int):
+    lo, hi = C.c_double(), C.c_double()
+    lib().cmn_slot_bounds(int(kind), float(plo), float(phi), int(part), int(fan_out), C.byref(lo), C.byref(hi))
+    return lo.value, hi.value
+
+
+def materialise(parent: list, sidx: int, a: SlotAssignment) -> list:
+    """region::materialise: the child `sidx` of `parent` under `a` (slot 0
+    least significant)."""
+    out = list(parent)
+    idx = sidx
+    for kind, vid, w in zip(a.kinds, a.var_ids, a.widths):
+        part = idx % w
+        idx //= w
+        out[vid] = slot_bounds(kind, parent[vid][0], parent[vid][1], part, w)
+    return out
 
 
 class DeviceProblem:
@@ -34,6 +88,15 @@ class DeviceProblem:
         check(lib().cmn_problem_create(C.byref(desc), C.byref(h)))
         self.handle = h
         self.n_vars = problem.n_vars
+
+    def program(self, precision: int = 0) -> np.ndarray:
+        """The compiled program (cmn_problem_program): 16 bytes per
+        instruction, FP64 (0) or the FP32 screen's (1)."""
+        n = C.c_int64()
+        check(lib().cmn_problem_program(self.handle, precision, None, 0, C.byref(n)))
+        buf = np.zeros(16 * n.value, dtype=np.uint8)
+        check(lib().cmn_problem_program(self.handle, precision, A.ptr(buf), n.value, C.byref(n)))
+        return buf
 
     def info(self) -> dict:
         inf = A.ProblemInfo()

@@ -487,6 +487,17 @@ cmn_status cmn_fp64_emu_check_host(uint64_t n, uint64_t seed, int32_t family, ui
  * or a sum cancels exactly (those take the FP64 instruction). */
 cmn_status cmn_fp64_emu_op_host(int32_t op, double a, double b, double* out, int32_t* handled);
 
+/* The compiled program of a problem (the fused evaluator's straight-line
+ * code), for tools and tests: `precision` 0 gives the FP64 program, 1 the
+ * FP32 screen program (constants as outward-rounded pairs).  Each
+ * instruction is 16 bytes: u8 head (bits 0-2 the opcode, 3-7 its
+ * sub-code), u8 operand modes, u16 dst, u16 a, u16 b, then an f64 payload
+ * or, in the FP32 program, an (f32 lo, f32 hi) pair.  Writes at most
+ * `capacity` instructions to `out` (16 * capacity bytes) and the program's
+ * length to *length. */
+cmn_status cmn_problem_program(const cmn_problem* problem, int32_t precision,
+                               void* out, int64_t capacity, int64_t* length);
+
 /* One-call solve: create, run to a stop condition, report, destroy. */
 cmn_status cmn_solve(const cmn_problem* problem,
                      const cmn_solve_options* opts, cmn_outcome* outcome,

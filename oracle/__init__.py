@@ -49,6 +49,9 @@ _SIG = {
     "orc_sample_continuous_f32": (F, [F, F, U64, U64, U64, U64]),
     "orc_sample_discrete_f32": (F, [F, F, U64, U64, U64, U64]),
     "orc_bound": (I32, [P, P, P, P, P, I64, U64, P, P, I32]),
+    "orc_bound_hw": (I32, [P, P, P, P, P, I64, U64, P, P, I32]),
+    "orc_set_program32": (I32, [P, P, I64]),
+    "orc_bound_inc32": (I32, [P, P, P, P, P, I64, U64, P, P, P]),
     "orc_aggregate_bound": (I32, [P, P, P, P, P, I64, U64, U64, P, P, P, I32]),
     "orc_sample": (I32, [P, P, P, P, P, I64, U64, U64, U64, C.POINTER(I32), C.POINTER(D), C.POINTER(I64), P, I32]),
     "orc_enumerate": (I32, [P, P, P, P, P, I64, U64, C.POINTER(I32), C.POINTER(D), C.POINTER(I64), P, I32]),
@@ -157,13 +160,37 @@ class OracleProblem:
         w = np.ascontiguousarray(widths, dtype=np.uint64)
         return k, v, w
 
-    def bound(self, box, kinds, var_ids, widths, n_regions, threads=None):
+    def set_program32(self, code: np.ndarray) -> bool:
+        """The library's compiled FP32 program (DeviceProblem.program(1)):
+        the lazy form then bounds children incrementally, as the device
+        does.  True when the program has the sum-chain shape for that."""
+        code = np.ascontiguousarray(code, dtype=np.uint8)
+        return bool(lib().orc_set_program32(self.h, A.ptr(code), code.size // 16))
+
+    def bound_inc32(self, box, kinds, var_ids, widths, n_regions):
+        """The lazy form's incremental FP32 bounds of one parent's regions
+        (after set_program32): feasible (not proven violated), lb, ub."""
         box = np.ascontiguousarray(box, dtype=np.float64)
         k, v, w = self._slots(kinds, var_ids, widths)
         fe = np.empty(n_regions, dtype=np.uint8)
         lb = np.empty(n_regions)
-        if lib().orc_bound(self.h, A.ptr(box), A.ptr(k), A.ptr(v), A.ptr(w), len(k), n_regions, A.ptr(fe), A.ptr(lb),
-                           threads or threads_default()):
+        ub = np.empty(n_regions)
+        if lib().orc_bound_inc32(self.h, A.ptr(box), A.ptr(k), A.ptr(v), A.ptr(w), len(k), n_regions, A.ptr(fe),
+                                 A.ptr(lb), A.ptr(ub)):
+            raise ValueError(lib().orc_last_error().decode())
+        return fe, lb, ub
+
+    def bound(self, box, kinds, var_ids, widths, n_regions, threads=None, hardware_rounding=False):
+        """orc_bound; hardware_rounding=True runs orc_bound_hw (the host's
+        directed-rounding mode instead of error-free transformations, same
+        results)."""
+        box = np.ascontiguousarray(box, dtype=np.float64)
+        k, v, w = self._slots(kinds, var_ids, widths)
+        fe = np.empty(n_regions, dtype=np.uint8)
+        lb = np.empty(n_regions)
+        fn = lib().orc_bound_hw if hardware_rounding else lib().orc_bound
+        if fn(self.h, A.ptr(box), A.ptr(k), A.ptr(v), A.ptr(w), len(k), n_regions, A.ptr(fe), A.ptr(lb),
+              threads or threads_default()):
             raise ValueError(lib().orc_last_error().decode())
         return fe, lb
 

@@ -19,6 +19,8 @@ HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent
 REF_OUT = HERE / "_ref"
 HEADER = REF_OUT / "cuminlp_ref_gpu.cuh"
+GAMS_SRC = REF_OUT / "cuminlp_ref_gams.cpp"
+GAMS_OBJ = REF_OUT / "ref_gams_frontend.o"
 OBJ = REF_OUT / "ref_gpu.o"
 EXE = REF_OUT / "ref_gpu"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
@@ -46,11 +48,18 @@ def available() -> bool:
 
 
 def compile_ref_gpu(force: bool = False) -> Path | None:
-    """Compiles ref_gpu.cu to an object (no library needed yet)."""
+    """Compiles ref_gpu.cu, and the reference's GAMS frontend beside it, to
+    objects (no library needed yet)."""
     if not available():
         return None
+    if GAMS_SRC.exists() and (force or _stale(GAMS_OBJ, [GAMS_SRC])):
+        # plain IEEE arithmetic in the frontend's constant folding, as the
+        # reference builds it
+        _run([os.environ.get("CXX", "g++"), "-std=c++20", "-O2", "-ffp-contract=off", "-fPIC",
+              f"-I{HERE / 'ref_shim_gpu'}", "-c", "-x", "c++", str(GAMS_SRC), "-o", str(GAMS_OBJ)])
     deps = [HEADER, HERE / "ref_gpu.cu", ROOT / "include" / "cuminlp_gb300.h",
             ROOT / "include" / "cuminlp_gb300" / "region_backend.hpp",
+            ROOT / "include" / "cuminlp_gb300" / "aggregate_backend.hpp",
             HERE / "ref_shim_gpu" / "cuinterval" / "cuinterval.h", HERE / "ref_shim_gpu" / "cuinterval" / "interval.h"]
     if force or _stale(OBJ, deps):
         _run([_nvcc(), "-std=c++20", "-O2", ARCH, "--expt-relaxed-constexpr", "-w",
@@ -63,7 +72,8 @@ def link_ref_gpu(lib: Path, force: bool = False) -> Path | None:
     """Links the harness against the library built in place."""
     if not available() or not OBJ.exists():
         return None
-    if force or _stale(EXE, [OBJ, lib]):
-        _run([_nvcc(), ARCH, str(OBJ), "-o", str(EXE), f"-L{lib.parent}", "-lcuminlp_gb300",
+    objs = [OBJ] + ([GAMS_OBJ] if GAMS_OBJ.exists() else [])
+    if force or _stale(EXE, objs + [lib]):
+        _run([_nvcc(), ARCH, *map(str, objs), "-o", str(EXE), f"-L{lib.parent}", "-lcuminlp_gb300",
               "-Xlinker", "-rpath", "-Xlinker", str(lib.parent)])
     return EXE

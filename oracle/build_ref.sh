@@ -7,8 +7,11 @@
 #     reference's own host sources, where they lie, for this machine (they
 #     generate the golden fixtures under tests/golden/);
 #   - writes oracle/_ref/cuminlp_ref_gpu.cuh, the reference's headers for its
-#     SearchDriver, policies and CUDA graph backend as one file
-#     (oracle/amalgamate.py), which travels with the working tree to the GPU
+#     SearchDriver, policies, AggregateDriver, GAMS frontend interface and
+#     CUDA graph backend as one file, and oracle/_ref/cuminlp_ref_gams.cpp,
+#     its GAMS frontend source with its headers (oracle/amalgamate.py); and
+#     copies the reference's test models (test/data/gams) to
+#     oracle/_ref/gams.  All of it travels with the working tree to the GPU
 #     host, where oracle/build.py compiles oracle/ref_gpu.cu against it.
 # Without the reference tree it does nothing and exits 0.
 #
@@ -29,7 +32,13 @@ PY=${PYTHON:-python3}
 "$PY" "$HERE/amalgamate.py" "$REF" "$OUT/cuminlp_ref_gpu.cuh" \
   include/cuminlp/search/driver.hpp include/cuminlp/policy/greedy_enum.hpp \
   include/cuminlp/policy/width_first.hpp include/cuminlp/policy/bisection_budget.hpp \
+  include/cuminlp/aggregate/driver.hpp include/cuminlp/gams.hpp \
   include/cuminlp/backend/graph/factory.cuh
+# the GAMS frontend (a source file with its own headers), and the reference's
+# MINLPLib test models it is tested on
+"$PY" "$HERE/amalgamate.py" "$REF" "$OUT/cuminlp_ref_gams.cpp" source/gams/frontend.cpp
+mkdir -p "$OUT/gams"
+cp "$REF"/test/data/gams/*.gms "$OUT/gams/"
 case "$(uname -m)" in
   x86_64) ;;
   *) echo "host harnesses are built on x86-64 only"; exit 0 ;;

@@ -11,6 +11,7 @@
  */
 #define _GNU_SOURCE
 #include <float.h>
+#include <fenv.h>
 #include <math.h>
 #include <pthread.h>
 #include <stdarg.h>
@@ -379,6 +380,53 @@ typedef struct { float lo, hi; } iv32;
 #undef SQRT_RU
 #undef T_INF
 
+/* The same operators with the host's directed-rounding hardware, for the
+ * timed CPU path of the bench: the calling thread's rounding mode is
+ * FE_DOWNWARD for a whole box evaluation, so round-down results are the
+ * plain IEEE operations and round-up ones are negated round-down ones
+ * (ru(x op y) = -rd(-(x op y))).  Tested bit for bit against the error-free
+ * transformations above.  Sqrt (whose round-up form has no such identity)
+ * and the remaining operators run through the software forms under
+ * round-to-nearest (apply_hw). */
+static inline double hw_add_ru(double a, double b) { return -((-a) + (-b)); }
+static inline double hw_sub_ru(double a, double b) { return -(b - a); }
+static inline double hw_mul_ru(double a, double b) { return -((-a) * b); }
+static inline double hw_div_ru(double a, double b) { return -((-a) / b); }
+static inline double hw_add_rd(double a, double b) { return a + b; }
+static inline double hw_sub_rd(double a, double b) { return a - b; }
+static inline double hw_mul_rd(double a, double b) { return a * b; }
+static inline double hw_div_rd(double a, double b) { return a / b; }
+
+#define T double
+#define IV iv64
+#define SUF(n) n##_h
+#define ADD_RD hw_add_rd
+#define ADD_RU hw_add_ru
+#define SUB_RD hw_sub_rd
+#define SUB_RU hw_sub_ru
+#define MUL_RD hw_mul_rd
+#define MUL_RU hw_mul_ru
+#define DIV_RD hw_div_rd
+#define DIV_RU hw_div_ru
+#define SQRT_RD sqrt_rd
+#define SQRT_RU sqrt_ru
+#define T_INF INFINITY
+#include "oracle_interval.inc"
+#undef T
+#undef IV
+#undef SUF
+#undef ADD_RD
+#undef ADD_RU
+#undef SUB_RD
+#undef SUB_RU
+#undef MUL_RD
+#undef MUL_RU
+#undef DIV_RD
+#undef DIV_RU
+#undef SQRT_RD
+#undef SQRT_RU
+#undef T_INF
+
 static int op_supported_interval(int op)
 {
   switch (op) {
@@ -408,6 +456,25 @@ static iv64 apply_d(int op, iv64 a, iv64 b, int k)
     case CMN_OP_MAX: return iv_max_d(a, b);
     default: {
       iv64 r = {NAN, NAN};
+      return r;
+    }
+  }
+}
+
+/* under FE_DOWNWARD (see the _h operators) */
+static iv64 apply_hw(int op, iv64 a, iv64 b, int k)
+{
+  switch (op) {
+    case CMN_OP_ADD: return iv_add_h(a, b);
+    case CMN_OP_SUB: return iv_sub_h(a, b);
+    case CMN_OP_MUL: return iv_mul_h(a, b);
+    case CMN_OP_DIV: return iv_div_h(a, b);
+    case CMN_OP_SQR: return iv_sqr_h(a);
+    case CMN_OP_NEG: return iv_neg_h(a);
+    default: {
+      fesetround(FE_TONEAREST);
+      iv64 r = apply_d(op, a, b, k);
+      fesetround(FE_DOWNWARD);
       return r;
     }
   }
@@ -495,6 +562,14 @@ struct orc_problem {
   int64_t n_order;
   float* clo32; /* per node: FP32 outward bounds of a Const payload */
   float* chi32;
+  /* the lazy form's incremental FP32 children (orc_set_program32) */
+  int inc_ok;
+  int64_t prog_len;
+  struct orc_instr* prog32;
+  int64_t inc_segments;
+  int32_t* inc_seg; /* 3 per segment: chain [b, t), checks/objective [t, e) */
+  int32_t* inc_off; /* n_vars * segments + 1 */
+  int32_t* inc_pcs;
 };
 
 void orc_problem_destroy(orc_problem* p)
@@ -509,6 +584,10 @@ void orc_problem_destroy(orc_problem* p)
   free(p->order);
   free(p->clo32);
   free(p->chi32);
+  free(p->prog32);
+  free(p->inc_seg);
+  free(p->inc_off);
+  free(p->inc_pcs);
   free(p);
 }
 
@@ -681,6 +760,30 @@ static int eval_all_d(const orc_problem* p, const double* box, iv64* val)
     iv64 a = val[nd->in0];
     iv64 b = nd->n_in >= 2 ? val[nd->in1] : a;
     val[i] = apply_d(nd->op, a, b, nd->int_exp);
+  }
+  return 0;
+}
+
+/* eval_all_d with the hardware operators; the caller has set FE_DOWNWARD */
+static int eval_all_hw(const orc_problem* p, const double* box, iv64* val)
+{
+  for (int64_t v = 0; v < p->n_nodes; ++v) {
+    const cmn_node* nd = &p->nodes[v];
+    if (nd->op == CMN_OP_VAR && p->reach[v]) {
+      val[v].lo = box[2 * nd->var_index];
+      val[v].hi = box[2 * nd->var_index + 1];
+    } else if (nd->op == CMN_OP_CONST) {
+      val[v].lo = nd->constant;
+      val[v].hi = nd->constant;
+    }
+  }
+  for (int64_t k = 0; k < p->n_order; ++k) {
+    int64_t i = p->order[k];
+    const cmn_node* nd = &p->nodes[i];
+    if (!op_supported_interval(nd->op)) return -1;
+    iv64 a = val[nd->in0];
+    iv64 b = nd->n_in >= 2 ? val[nd->in1] : a;
+    val[i] = apply_hw(nd->op, a, b, nd->int_exp);
   }
   return 0;
 }
@@ -1112,6 +1215,7 @@ typedef struct {
   double* obj_lb;
   double* obj_ub; /* optional */
   int failed;
+  int hw; /* bound with the hardware directed rounding (_h operators) */
   /* sampling / enumerate */
   uint64_t S, salt;
   int exact;
@@ -1128,7 +1232,13 @@ static void bound_range(void* vc, int64_t r0, int64_t r1, int tid)
   iv64* val = (iv64*)malloc(sizeof(iv64) * (size_t)p->n_nodes);
   for (int64_t r = r0; r < r1; ++r) {
     child_box(c->box, p->n_vars, c->s, (uint64_t)r, cb);
-    if (eval_all_d(p, cb, val)) c->failed = 1;
+    if (c->hw) {
+      fesetround(FE_DOWNWARD);
+      if (eval_all_hw(p, cb, val)) c->failed = 1;
+      fesetround(FE_TONEAREST);
+    } else if (eval_all_d(p, cb, val)) {
+      c->failed = 1;
+    }
     double lb, ub;
     c->feas[r] = (uint8_t)verdict_d(p, val, &lb, &ub);
     c->obj_lb[r] = lb;
@@ -1150,10 +1260,29 @@ static int check_widths(const slots_t* s, uint64_t n_regions)
   return total == n_regions ? 0 : -1;
 }
 
+static int bound_impl(const orc_problem* p, const double* box, const uint8_t* slot_kinds,
+                      const uint64_t* var_ids, const uint64_t* widths, int64_t slot_count,
+                      uint64_t n_regions, uint8_t* feasible, double* obj_lb, int threads, int hw);
+
 int orc_bound(const orc_problem* p, const double* box,
               const uint8_t* slot_kinds, const uint64_t* var_ids,
               const uint64_t* widths, int64_t slot_count, uint64_t n_regions,
               uint8_t* feasible, double* obj_lb, int threads)
+{
+  return bound_impl(p, box, slot_kinds, var_ids, widths, slot_count, n_regions, feasible, obj_lb, threads, 0);
+}
+
+int orc_bound_hw(const orc_problem* p, const double* box,
+                 const uint8_t* slot_kinds, const uint64_t* var_ids,
+                 const uint64_t* widths, int64_t slot_count, uint64_t n_regions,
+                 uint8_t* feasible, double* obj_lb, int threads)
+{
+  return bound_impl(p, box, slot_kinds, var_ids, widths, slot_count, n_regions, feasible, obj_lb, threads, 1);
+}
+
+static int bound_impl(const orc_problem* p, const double* box, const uint8_t* slot_kinds,
+                      const uint64_t* var_ids, const uint64_t* widths, int64_t slot_count,
+                      uint64_t n_regions, uint8_t* feasible, double* obj_lb, int threads, int hw)
 {
   slots_t s;
   if (slot_count > 64) {
@@ -1172,6 +1301,7 @@ int orc_bound(const orc_problem* p, const double* box,
   c.s = &s;
   c.feas = feasible;
   c.obj_lb = obj_lb;
+  c.hw = hw;
   parallel_for((int64_t)n_regions, threads, bound_range, &c);
   if (c.failed) {
     set_err("op without an interval implementation");
@@ -2015,6 +2145,280 @@ int orc_solve_reference(const orc_problem* p, const cmn_solve_options* opts_in,
 }
 
 /* ======================================================================
+ * the lazy form's incremental FP32 children, restated from the device
+ * (csrc/eval_kernels.cu inc_common_kernel / eval_children_inc_kernel)
+ * over the library's compiled FP32 program (cmn_problem_program)
+ * ==================================================================== */
+/* One instruction of the compiled program, 16 bytes (cmn_problem_program). */
+struct orc_instr {
+  uint8_t head, modes;
+  uint16_t dst, a, b;
+  union {
+    double c;
+    struct {
+      float clo, chi;
+    } c32;
+  } u;
+};
+
+enum { OP_GENERIC = 0, OP_TERM = 1, OP_LOADACC = 3, OP_CHECK = 5, OP_OBJECTIVE = 6 };
+enum { MODE_VAR = 1, MODE_ACC = 2 };
+enum { T_INIT = 1, T_SUB = 2, T_HASC = 4, T_SQR = 8, T_VAR = 16, T_PMASK = 24 };
+
+/* Segments and per-(variable, segment) chain lists, derived here from the
+ * instruction stream independently of the library's own tables: a
+ * segment is a sum chain (a LoadAcc or an initialising TERM, then TERMs)
+ * followed by the checks and objective that read it. */
+int orc_set_program32(orc_problem* p, const void* instrs, int64_t len)
+{
+  free(p->prog32);
+  free(p->inc_seg);
+  free(p->inc_off);
+  free(p->inc_pcs);
+  p->prog32 = NULL;
+  p->inc_seg = p->inc_off = p->inc_pcs = NULL;
+  p->inc_ok = 0;
+  p->prog_len = len;
+  if (len <= 0) return 0;
+  p->prog32 = (struct orc_instr*)malloc(sizeof(struct orc_instr) * (size_t)len);
+  memcpy(p->prog32, instrs, sizeof(struct orc_instr) * (size_t)len);
+  const struct orc_instr* code = p->prog32;
+  int32_t* seg = (int32_t*)malloc(sizeof(int32_t) * 3 * (size_t)(len + 1));
+  int64_t S = 0, pc = 0;
+#define ACCUM(in) (((in).head & 7) == OP_TERM || ((in).head & 7) == OP_LOADACC)
+#define STARTS(in) ((((in).head & 7) == OP_TERM && (((in).head >> 3) & T_INIT)) || ((in).head & 7) == OP_LOADACC)
+  while (pc < len) {
+    int64_t b = pc, t = pc, e;
+    if (STARTS(code[pc])) {
+      t = pc + 1;
+      while (t < len && ACCUM(code[t]) && !STARTS(code[t])) ++t;
+    }
+    e = t;
+    while (e < len && !ACCUM(code[e])) {
+      int c = code[e].head & 7;
+      if (c != OP_CHECK && c != OP_OBJECTIVE) {
+        free(seg);
+        return 0;
+      }
+      ++e;
+    }
+    if (e == b) {
+      free(seg);
+      return 0;
+    }
+    seg[3 * S] = (int32_t)b;
+    seg[3 * S + 1] = (int32_t)t;
+    seg[3 * S + 2] = (int32_t)e;
+    ++S;
+    pc = e;
+  }
+#undef ACCUM
+#undef STARTS
+  const int64_t n = p->n_vars;
+  int32_t* cnt = (int32_t*)calloc((size_t)(n * S + 1), sizeof(int32_t));
+  for (int pass = 0; pass < 2; ++pass) {
+    int32_t* fill = pass ? (int32_t*)calloc((size_t)(n * S + 1), sizeof(int32_t)) : NULL;
+    for (int64_t s = 0; s < S; ++s) {
+      for (int32_t q = seg[3 * s]; q < seg[3 * s + 1]; ++q) {
+        const struct orc_instr* in = &code[q];
+        int va = -1, vb = -1;
+        if ((in->head & 7) == OP_TERM) {
+          va = in->a;
+          vb = in->b;
+        } else if ((in->modes & 3) == MODE_VAR) {
+          va = vb = in->a;
+        }
+        int vs[2] = {va, vb != va ? vb : -1};
+        for (int w = 0; w < 2; ++w) {
+          if (vs[w] < 0) continue;
+          if (vs[w] >= n) {
+            free(seg);
+            free(cnt);
+            free(fill);
+            return 0;
+          }
+          int64_t slot = vs[w] * S + s;
+          if (!pass) ++cnt[slot];
+          else p->inc_pcs[p->inc_off[slot] + fill[slot]++] = q;
+        }
+      }
+    }
+    if (!pass) {
+      p->inc_off = (int32_t*)malloc(sizeof(int32_t) * (size_t)(n * S + 1));
+      int32_t acc = 0;
+      for (int64_t i = 0; i < n * S; ++i) {
+        p->inc_off[i] = acc;
+        acc += cnt[i];
+      }
+      p->inc_off[n * S] = acc;
+      p->inc_pcs = (int32_t*)malloc(sizeof(int32_t) * (size_t)(acc ? acc : 1));
+    } else {
+      free(fill);
+    }
+  }
+  free(cnt);
+  p->inc_seg = seg;
+  p->inc_segments = S;
+  p->inc_ok = 1;
+  return 1;
+}
+
+/* x of a box as an FP32 interval: box holds FP32 (lo, hi) per variable */
+static iv32 term_value_f(const struct orc_instr* in, const iv32* x)
+{
+  const int sub = in->head >> 3, pk = sub & T_PMASK;
+  iv32 r;
+  if (pk == 0) r = iv_mul_f(x[in->a], x[in->b]);
+  else if (pk == T_SQR) r = iv_sqr_f(x[in->a]);
+  else r = x[in->a];
+  if (sub & T_HASC) {
+    iv32 c = {in->u.c32.clo, in->u.c32.chi};
+    r = iv_mul_f(c, r);
+  }
+  return r;
+}
+
+static iv32 chain_add_f(iv32 acc, const struct orc_instr* in, const iv32* x)
+{
+  if ((in->head & 7) == OP_TERM) {
+    iv32 t = term_value_f(in, x);
+    return ((in->head >> 3) & T_SUB) ? iv_sub_f(acc, t) : iv_add_f(acc, t);
+  }
+  iv32 v;
+  if ((in->modes & 3) == MODE_VAR) {
+    v = x[in->a];
+  } else {
+    v.lo = in->u.c32.clo;
+    v.hi = in->u.c32.chi;
+  }
+  return iv_add_f(acc, v);
+}
+
+/* the FP32 box of parent box `pb` (FP64 lo/hi pairs) rounded outward */
+static void box32(const orc_problem* p, const double* pb, iv32* x)
+{
+  for (int64_t v = 0; v < p->n_vars; ++v) {
+    x[v].lo = orc_d2f_rd(pb[2 * v]);
+    x[v].hi = orc_d2f_ru(pb[2 * v + 1]);
+  }
+}
+
+/* common chain sums of one parent (its split variables `vids[0..count)`):
+ * out[2s], out[2s+1] */
+static void inc_common_one(const orc_problem* p, const double* pb, const uint64_t* vids, int64_t count,
+                           iv32* x, float* out)
+{
+  box32(p, pb, x);
+  for (int64_t s = 0; s < p->inc_segments; ++s) {
+    iv32 acc = {0.0f, 0.0f};
+    for (int32_t q = p->inc_seg[3 * s]; q < p->inc_seg[3 * s + 1]; ++q) {
+      const struct orc_instr* in = &p->prog32[q];
+      const int term = (in->head & 7) == OP_TERM;
+      int skip = 0;
+      if (term || (in->modes & 3) == MODE_VAR) {
+        for (int64_t j = 0; j < count; ++j)
+          if (vids[j] == in->a || (term && vids[j] == in->b)) skip = 1;
+      }
+      if (!skip) acc = chain_add_f(acc, in, x);
+    }
+    out[2 * s] = acc.lo;
+    out[2 * s + 1] = acc.hi;
+  }
+}
+
+static int split_before_o(const uint64_t* vids, int64_t j, uint64_t v)
+{
+  for (int64_t q = 0; q < j; ++q)
+    if (vids[q] == v) return 1;
+  return 0;
+}
+
+/* the child box `cb` (FP64) of a parent with the given common sums and
+ * split variables: FP32 verdict (1 unless a constraint is proven
+ * violated), lb, ub */
+static int inc_child(const orc_problem* p, const double* cb, const float* common, const uint64_t* vids,
+                     int64_t count, iv32* x, double* lb, double* ub)
+{
+  box32(p, cb, x);
+  int feas = 1;
+  iv32 obj = {NAN, NAN};
+  const int64_t S = p->inc_segments;
+  for (int64_t s = 0; s < S; ++s) {
+    iv32 acc = {common[2 * s], common[2 * s + 1]};
+    for (int64_t j = 0; j < count; ++j) {
+      const uint64_t vj = vids[j];
+      if (split_before_o(vids, j, vj)) continue;
+      for (int32_t q = p->inc_off[vj * S + s]; q < p->inc_off[vj * S + s + 1]; ++q) {
+        const struct orc_instr* in = &p->prog32[p->inc_pcs[q]];
+        if ((in->head & 7) == OP_TERM) {
+          uint64_t other = in->a == vj ? in->b : in->a;
+          if (other != vj && split_before_o(vids, j, other)) continue;
+        }
+        acc = chain_add_f(acc, in, x);
+      }
+    }
+    for (int32_t q = p->inc_seg[3 * s + 1]; q < p->inc_seg[3 * s + 2]; ++q) {
+      const struct orc_instr* in = &p->prog32[q];
+      const int mode = in->modes & 3;
+      iv32 v;
+      if (mode == MODE_ACC) v = acc;
+      else if (mode == MODE_VAR) v = x[in->a];
+      else {
+        v.lo = in->u.c32.clo;
+        v.hi = in->u.c32.chi;
+      }
+      if ((in->head & 7) == OP_CHECK) {
+        double rhs = in->u.c;
+        int excluded = ((in->head >> 3) == 0) ? ((double)v.lo > rhs) : ((double)v.lo > rhs || (double)v.hi < rhs);
+        if (excluded) feas = 0;
+      } else if ((in->head & 7) == OP_OBJECTIVE) {
+        obj = v;
+      }
+    }
+  }
+  *lb = (double)obj.lo;
+  *ub = (double)obj.hi;
+  return feas;
+}
+
+/* The lazy form's incremental FP32 bound of every region of one parent
+ * box (the slot plan as orc_bound takes it): feasible[r] is 0 when the
+ * FP32 enclosure proves a constraint violated.  For soundness tests
+ * against the FP64 bound. */
+int orc_bound_inc32(const orc_problem* p, const double* box, const uint8_t* slot_kinds, const uint64_t* var_ids,
+                    const uint64_t* widths, int64_t slot_count, uint64_t n_regions, uint8_t* feasible,
+                    double* obj_lb, double* obj_ub)
+{
+  if (!p->inc_ok) {
+    set_err("no incremental program set (orc_set_program32)");
+    return -1;
+  }
+  slots_t s;
+  if (slot_count > 64) {
+    set_err("slot count above 64");
+    return -1;
+  }
+  slots_init(&s, slot_kinds, var_ids, widths, slot_count);
+  if (check_widths(&s, n_regions)) {
+    set_err("widths do not multiply out to n_regions");
+    return -1;
+  }
+  const int64_t n = p->n_vars;
+  iv32* x = (iv32*)malloc(sizeof(iv32) * (size_t)(n ? n : 1));
+  float* common = (float*)malloc(sizeof(float) * 2 * (size_t)(p->inc_segments ? p->inc_segments : 1));
+  double* cb = (double*)malloc(sizeof(double) * 2 * (size_t)(n ? n : 1));
+  inc_common_one(p, box, var_ids, slot_count, x, common);
+  for (uint64_t r = 0; r < n_regions; ++r) {
+    child_box(box, n, &s, r, cb);
+    feasible[r] = (uint8_t)inc_child(p, cb, common, var_ids, slot_count, x, &obj_lb[r], &obj_ub[r]);
+  }
+  free(x);
+  free(common);
+  free(cb);
+  return 0;
+}
+
+/* ======================================================================
  * batched algorithm, restated step for step from the device solver
  * ==================================================================== */
 /* Total order on lower bounds used by parent selection and eviction: the
@@ -2075,6 +2479,7 @@ typedef struct {
   uint64_t salt0;
   int use_screen; /* FP32 screen switched on for this iteration */
   const double* plb; /* lazy form: the parents' FP64 lower bounds */
+  const float* common; /* lazy form, incremental: [parent][segment] (lo, hi) */
   /* outputs per child slot (E*C) */
   double* lb;
   uint8_t* state; /* 0 invalid, 1 dup, 2 infeasible, 3 dominated(old), 4 eligible */
@@ -2090,6 +2495,28 @@ typedef struct {
  * max(1, |GUB|) below the incumbent are certified in FP64 when bounded
  * (kCertifyBand in csrc/kernels.cuh). */
 #define LAZY_BAND (1.0 / 1024.0)
+
+/* Lazy form, incremental children: each parent's common chain sums. */
+typedef struct {
+  const orc_problem* p;
+  const double* pbox;
+  const parent_plan* plan;
+  float* common;
+} common_ctx;
+
+static void common_range(void* vc, int64_t k0, int64_t k1, int tid)
+{
+  (void)tid;
+  common_ctx* c = (common_ctx*)vc;
+  const orc_problem* p = c->p;
+  iv32* x = (iv32*)malloc(sizeof(iv32) * (size_t)(p->n_vars ? p->n_vars : 1));
+  for (int64_t k = k0; k < k1; ++k) {
+    if (c->plan[k].nreg == 0) continue;
+    inc_common_one(p, c->pbox + 2 * (size_t)p->n_vars * (size_t)k, c->plan[k].vids, c->plan[k].count, x,
+                   c->common + 2 * (size_t)p->inc_segments * (size_t)k);
+  }
+  free(x);
+}
 
 /* Lazy form: the FP64 verdict of each selected parent box. */
 typedef struct {
@@ -2180,8 +2607,13 @@ static void batch_range(void* vc, int64_t g0, int64_t g1, int tid)
         /* FP32; the parent's certified FP64 bound holds for the child; a
          * survivor within the band below the incumbent is certified in
          * FP64 at once (csrc/kernels.cuh certify_floor) */
-        if (eval_all_f(p, cb, v32)) c->failed = 1;
-        f = verdict_f(p, v32, &lb, &ub);
+        if (c->common) {
+          f = inc_child(p, cb, c->common + 2 * (size_t)p->inc_segments * k, pl->vids, pl->count,
+                        (iv32*)v32, &lb, &ub);
+        } else {
+          if (eval_all_f(p, cb, v32)) c->failed = 1;
+          f = verdict_f(p, v32, &lb, &ub);
+        }
         double plb = c->plb[k];
         lb = plb > lb ? plb : lb;
         if (!f) {
@@ -2379,6 +2811,13 @@ static int batched_run(const orc_problem* p, const cmn_solve_options* o,
     c.salt0 = salt0;
     c.use_screen = st->use_screen;
     c.plb = plb;
+    float* common = NULL;
+    if (o->precision == CMN_PRECISION_FP32_LAZY && p->inc_ok) {
+      common = (float*)malloc(sizeof(float) * 2 * (size_t)(p->inc_segments ? p->inc_segments : 1) * (E ? E : 1));
+      common_ctx cc = {p, pbox, plan, common};
+      parallel_for((int64_t)E, threads, common_range, &cc);
+      c.common = common;
+    }
     c.lb = (double*)malloc(sizeof(double) * G);
     c.state = (uint8_t*)malloc(G);
     c.screened = (uint8_t*)malloc(G);
@@ -2583,6 +3022,7 @@ static int batched_run(const orc_problem* p, const cmn_solve_options* o,
     free(c.cand_idx);
     free(c.b32v);
     free(c.b32i);
+    free(common);
     if (rc) break;
   }
   free(x);

@@ -87,10 +87,29 @@ float orc_sample_discrete_f32(float lb, float ub, uint64_t vid, uint64_t i,
                               uint64_t region, uint64_t salt);
 
 /* ---- roles (reference semantics, graph/replay.cuh:823-844) ------------- */
+/* The library's compiled FP32 program (cmn_problem_program, precision 1):
+ * enables the lazy form's incremental child bounds, derived from it the way
+ * the device evaluates them.  Returns 1 when the program has the sum-chain
+ * shape they need, else 0 (the lazy form then bounds children node by
+ * node). */
+int orc_set_program32(orc_problem* p, const void* instrs, int64_t len);
+
+/* The lazy form's incremental FP32 bound of every region of one parent
+ * box, after orc_set_program32. */
+int orc_bound_inc32(const orc_problem* p, const double* box, const uint8_t* slot_kinds, const uint64_t* var_ids,
+                    const uint64_t* widths, int64_t slot_count, uint64_t n_regions, uint8_t* feasible,
+                    double* obj_lb, double* obj_ub);
+
 int orc_bound(const orc_problem* p, const double* box,
               const uint8_t* slot_kinds, const uint64_t* var_ids,
               const uint64_t* widths, int64_t slot_count, uint64_t n_regions,
               uint8_t* feasible, double* obj_lb, int threads);
+/* orc_bound with the host's directed-rounding hardware (the timed CPU
+ * path; same results bit for bit). */
+int orc_bound_hw(const orc_problem* p, const double* box,
+                 const uint8_t* slot_kinds, const uint64_t* var_ids,
+                 const uint64_t* widths, int64_t slot_count, uint64_t n_regions,
+                 uint8_t* feasible, double* obj_lb, int threads);
 /* AggregateBounder::bound_children for one region: k children of
  * n_regions / k contiguous regions each. */
 int orc_aggregate_bound(const orc_problem* p, const double* box,

@@ -33,6 +33,14 @@
 //       region is the root box, or for frac < 1 its part within frac of
 //       its half-width around the origin (where the QCQPs' points are
 //       feasible).
+//
+//   aggdriver <in> <out>
+//       the reference's AggregateDriver over this library's aggregate roles
+//       (include/cuminlp_gb300/aggregate_backend.hpp).
+//
+//   gams <model.gms> <out> <iter_limit> <B> <parents>
+//       the reference's GAMS frontend, then the library's solver on the
+//       lowered problem.
 #include <algorithm>
 #include <chrono>
 #include <cstdio>
@@ -46,6 +54,7 @@
 #include <vector>
 
 #include "cuminlp_ref_gpu.cuh"
+#include "cuminlp_gb300/aggregate_backend.hpp"
 #include "cuminlp_gb300/region_backend.hpp"
 
 using namespace cuminlp;
@@ -271,10 +280,127 @@ static int cmd_roles(std::istream& in, std::ostream& out)
   return 0;
 }
 
+static void print_outcome_lines(std::ostream& out, const search::SolveOutcome<double>& o)
+{
+  const auto& t = o.counters;
+  out << hx(o.lower_bound) << ' ' << hx(o.upper_bound) << ' ' << search::to_string(o.stop_reason) << ' '
+      << o.proven_optimal << ' ' << o.infeasible << '\n';
+  out << t.iterations << ' ' << t.fathomed << ' ' << t.fathomed_points << ' ' << t.bounded << ' ' << t.sampled << ' '
+      << t.enqueued << ' ' << t.witness_rejected << ' ' << t.pruned_duplicate << ' ' << t.pruned_infeasible << ' '
+      << t.pruned_dominated << ' ' << t.pending << ' ' << t.viable << '\n';
+}
+
+// "<iter_limit> <k> <N> <Ns> <samples> <rule> <tolerance>" then the problem:
+// the reference's AggregateDriver (aggregate/driver.hpp:137-420) with
+// WidestBranchPolicy, over this library's roles through
+// include/cuminlp_gb300/aggregate_backend.hpp
+static int cmd_aggdriver(std::istream& in, std::ostream& out)
+{
+  uint32_t iter_limit;
+  size_t k, N, Ns, samples;
+  std::string rule_name;
+  in >> iter_limit >> k >> N >> Ns >> samples >> rule_name;
+  const double tol = rd(in);
+  model::Problem<double> P = load_problem(in);
+  auto rule = aggregate::parse_selection_rule(rule_name);
+  if (!rule) throw std::runtime_error("unknown selection rule");
+  auto pol = std::make_shared<aggregate::WidestBranchPolicy<double>>(k, N);
+  auto spol = std::make_shared<aggregate::WidestBranchPolicy<double>>(k, Ns);
+  auto cache = std::make_shared<cuminlp_gb300::AggregateRoleCache>(P, N, k, Ns, samples);
+  auto obs = std::make_shared<report::SearchObserver>();
+  aggregate::AggregateDriver<double> drv(pol, spol, cache, *rule, iter_limit, tol, 0, obs);
+  const double t0 = now_s();
+  auto o = drv.solve(P);
+  const double t1 = now_s();
+  const auto& t = o.counters;
+  out << hx(o.lower_bound) << ' ' << hx(o.upper_bound) << ' ' << search::to_string(o.stop_reason) << ' '
+      << o.proven_optimal << ' ' << o.infeasible << ' ' << o.selection_rule_engaged << '\n';
+  out << t.iterations << ' ' << t.fathomed << ' ' << t.fathomed_points << ' ' << t.bounded << ' ' << t.sampled << ' '
+      << t.enqueued << ' ' << t.witness_rejected << ' ' << t.pruned_duplicate << ' ' << t.pruned_infeasible << ' '
+      << t.pruned_dominated << ' ' << t.pending << ' ' << t.viable << ' ' << t.history_freed << ' '
+      << t.history_peak_live << '\n';
+  out << o.best_point.size();
+  for (double x : o.best_point) out << ' ' << hx(x);
+  out << '\n';
+  out << "seconds " << (t1 - t0) << '\n';
+  return 0;
+}
+
+// gams <model.gms> <out> <iter_limit> <B> <parents>: the reference's GAMS
+// frontend (source/gams/frontend.cpp) lowers the model; the lowered Problem
+// crosses the C ABI (include/cuminlp_gb300/region_backend.hpp's Flat) and
+// the library's device-resident solver (cmn_solve) runs on it.  Writes the
+// lowering in oracle/ref_gams.cpp's record format, then
+//   solve <lb> <ub> <stop_reason> <proven_optimal> <infeasible> <iterations>
+//         <expansions> <bounded> <seconds>
+// or
+//   solve_error <status> <message>
+static int cmd_gams(const char* path, std::ostream& out, uint64_t iter_limit, int B, uint64_t parents)
+{
+  gams::ParsedModel<double> r;
+  try {
+    r = gams::parse_file<double>(path, {});
+  } catch (const gams::ParseError& e) {
+    out << "err " << (int)e.kind << ' ' << e.line << '\n';
+    return 0;
+  }
+  const auto& p = r.problem;
+  const auto& nodes = p.graph.nodes;
+  out << "ok " << (r.sense == gams::Sense::Maximise ? "max" : "min") << ' ' << (r.objvar_kept ? 1 : 0) << ' '
+      << nodes.size() << ' ' << p.box_bounds.size() << ' ' << p.constraints.size() << ' ' << r.warnings.size()
+      << '\n';
+  for (const auto& nd : nodes) {
+    const long in0 = nd.in.size() > 0 ? (long)nd.in[0] : -1;
+    const long in1 = nd.in.size() > 1 ? (long)nd.in[1] : -1;
+    double c = 0.0;
+    unsigned long vi = 0;
+    int ie = 0;
+    if (nd.op == model::Op::Const) c = nd.payload.constant;
+    if (nd.op == model::Op::Var) vi = nd.payload.var_index;
+    if (nd.op == model::Op::PowN) ie = nd.payload.int_exp;
+    out << "node " << (int)nd.op << ' ' << nd.in.size() << ' ' << in0 << ' ' << in1 << ' ' << hx(c) << ' ' << vi
+        << ' ' << ie << '\n';
+  }
+  for (std::size_t i = 0; i < p.box_bounds.size(); ++i)
+    out << "var " << hx(p.box_bounds[i].lb) << ' ' << hx(p.box_bounds[i].ub) << ' ' << (int)p.var_kinds[i] << ' '
+        << (i < r.var_names.size() ? r.var_names[i] : std::string("?")) << '\n';
+  out << "obj " << (std::size_t)p.objective_root << '\n';
+  for (std::size_t i = 0; i < p.constraints.size(); ++i)
+    out << "con " << (std::size_t)p.constraints[i].root_id << ' ' << (int)p.constraints[i].cmp << ' '
+        << hx(p.constraints[i].rhs) << ' '
+        << (i < r.constraint_names.size() ? r.constraint_names[i] : std::string("?")) << '\n';
+  cuminlp_gb300::detail::Flat f(p);
+  cmn_problem* h = nullptr;
+  cmn_status st = cmn_problem_create(&f.desc, &h);
+  if (st != CMN_OK) {
+    out << "solve_error " << (int)st << ' ' << cmn_last_error() << '\n';
+    return 0;
+  }
+  cmn_solve_options o;
+  cmn_solve_options_default(&o);
+  o.iter_limit = iter_limit;
+  o.bisection_budget = B;
+  o.batch_parents = parents;
+  o.frontier_cap = 1ull << 20;
+  cmn_outcome oc{};
+  const double t0 = now_s();
+  st = cmn_solve(h, &o, &oc, nullptr);
+  const double t1 = now_s();
+  if (st != CMN_OK) {
+    out << "solve_error " << (int)st << ' ' << cmn_last_error() << '\n';
+  } else {
+    out << "solve " << hx(oc.lower_bound) << ' ' << hx(oc.upper_bound) << ' ' << oc.stop_reason << ' '
+        << oc.proven_optimal << ' ' << oc.infeasible << ' ' << oc.counters.iterations << ' '
+        << oc.counters.expansions << ' ' << oc.counters.bounded << ' ' << (t1 - t0) << '\n';
+  }
+  cmn_problem_destroy(h);
+  return 0;
+}
+
 int main(int argc, char** argv)
 {
   if (argc < 4) {
-    std::cerr << "usage: ref_gpu driver <gb300|graph> <in> <out> | roles <in> <out>\n";
+    std::cerr << "usage: ref_gpu driver <gb300|graph> <in> <out> | roles|aggdriver <in> <out> | gams <gms> <out> <iters> <B> <parents>\n";
     return 2;
   }
   const std::string cmd = argv[1];
@@ -288,6 +414,16 @@ int main(int argc, char** argv)
       std::ifstream in(argv[2]);
       std::ofstream out(argv[3]);
       return cmd_roles(in, out);
+    }
+    if (cmd == "aggdriver") {
+      std::ifstream in(argv[2]);
+      std::ofstream out(argv[3]);
+      return cmd_aggdriver(in, out);
+    }
+    if (cmd == "gams" && argc >= 7) {
+      std::ofstream out(argv[3]);
+      return cmd_gams(argv[2], out, std::strtoull(argv[4], nullptr, 10), std::atoi(argv[5]),
+                      std::strtoull(argv[6], nullptr, 10));
     }
   } catch (const std::exception& e) {
     std::cerr << "error: " << e.what() << '\n';

@@ -4,8 +4,17 @@
 // TEST INFRASTRUCTURE ONLY.  The reference reads and writes the two bounds
 // (`lb`, `ub`), value-initialises arrays of intervals, builds point
 // intervals from one scalar (`cu::interval<T>(b)`, graph/ops.cuh:143-207)
-// and brace-initialises from two bounds.
+// and brace-initialises from two bounds.  The same definition serves the
+// reference's host code compiled by g++ (its GAMS frontend), so every
+// translation unit of the harness sees one interval type.
 #pragma once
+
+// host and device under nvcc; host code (the GAMS frontend) under g++
+#ifdef __CUDACC__
+#define CMN_SHIM_HD __host__ __device__
+#else
+#define CMN_SHIM_HD
+#endif
 
 namespace cu
 {
@@ -16,7 +25,7 @@ struct interval
   T ub;
 
   interval() = default;
-  __host__ __device__ constexpr interval(T point) : lb(point), ub(point) {}
-  __host__ __device__ constexpr interval(T lo, T hi) : lb(lo), ub(hi) {}
+  CMN_SHIM_HD constexpr interval(T point) : lb(point), ub(point) {}
+  CMN_SHIM_HD constexpr interval(T lo, T hi) : lb(lo), ub(hi) {}
 };
 }  // namespace cu

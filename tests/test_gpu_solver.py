@@ -44,7 +44,13 @@ def compare(p, iterations, room=1 << 20, **opts):
     s.step(0)
     g = s.outcome()
     gbox, glb, gdepth = s.frontier()
-    obox, olb, odepth, o = O.OracleProblem(p).batched_frontier(iterations, room=room, **opts)
+    op = O.OracleProblem(p)
+    if opts.get("precision") == "lazy":
+        # the lazy form bounds children incrementally over the compiled
+        # program when it is a set of sum chains; the oracle restates that
+        # from the same program
+        op.set_program32(dp.program(1))
+    obox, olb, odepth, o = op.batched_frontier(iterations, room=room, **opts)
     assert len(glb) == len(olb)
     assert bits_equal(glb, olb)
     assert np.array_equal(gdepth, odepth)
@@ -222,3 +228,29 @@ def test_solver_n512_matches_oracle(precision):
     # the sampler's points shared by lane groups at n = 512, in the search
     from tests.test_gpu_roles import wide_qcqp
     compare(wide_qcqp(), 4, bisection_budget=3, batch_parents=64, sample_points=1, precision=precision)
+
+
+@pytest.mark.parametrize("cfg", [1, 2, 3])
+def test_incremental_fp32_bounds_enclose_fp64(cfg):
+    # the lazy form's incremental FP32 child bounds (common chain sums per
+    # parent, split-variable terms per child) are sound: never above the
+    # FP64 bound, and a constraint they prove violated is violated in FP64
+    p = G.CONFIGS[cfg]()
+    dp = DeviceProblem(p)
+    op = O.OracleProblem(p)
+    assert op.set_program32(dp.program(1))
+    rng = np.random.default_rng(cfg)
+    root = np.array(p.box_bounds)
+    for _ in range(4):
+        c = rng.uniform(root[:, 0], root[:, 1])
+        w = (root[:, 1] - root[:, 0]) * rng.uniform(0.01, 0.3)
+        lo, hi = np.maximum(c - w, root[:, 0]), np.minimum(c + w, root[:, 1])
+        ints = np.array(p.var_kinds) != A.VAR_CONTINUOUS
+        lo[ints], hi[ints] = np.ceil(lo[ints]), np.maximum(np.floor(hi[ints]), np.ceil(lo[ints]))
+        box = np.stack([lo, hi], 1).reshape(-1)
+        kinds, vids, widths, _ = O.bisection_choose(box, p.var_kinds, 6)
+        n = int(np.prod(widths))
+        fe32, lb32, ub32 = op.bound_inc32(box, kinds, vids, widths, n)
+        fe64, lb64 = op.bound(box, kinds, vids, widths, n)
+        assert np.all(lb32 <= lb64)
+        assert not np.any(fe64.astype(bool) & ~fe32.astype(bool))

@@ -12,7 +12,7 @@ from pathlib import Path
 
 import numpy as np
 
-from cuminlp_gb300.aggregate import bisection_choose, slot_bounds
+from cuminlp_gb300.solver import bisection_choose, slot_bounds
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
 

@@ -377,3 +377,20 @@ def test_fp32_enclosure_contains_fp64():
         ok = ~np.isnan(lo64)
         assert np.all(lo32[ok].astype(np.float64) <= lo64[ok])
         assert np.all(hi32[ok].astype(np.float64) >= hi64[ok])
+
+
+@pytest.mark.parametrize("cfg", [1, 2, 3])
+def test_hardware_rounding_bound_equals_error_free_transformations(cfg):
+    # the bench's timed CPU path (the host's FE_DOWNWARD mode, round-up as a
+    # negated round-down) gives the oracle's bounds bit for bit, signs of
+    # zero included
+    from cuminlp_gb300 import generators as G
+    p = G.CONFIGS[cfg]()
+    op = O.OracleProblem(p)
+    box = p.root_box()
+    kinds, vids, widths, _ = O.bisection_choose(box, p.var_kinds, 9)
+    n = int(np.prod(widths))
+    fe, lb = op.bound(box, kinds, vids, widths, n, threads=4)
+    fe2, lb2 = op.bound(box, kinds, vids, widths, n, threads=4, hardware_rounding=True)
+    assert np.array_equal(fe, fe2)
+    assert np.array_equal(lb.view(np.uint64), lb2.view(np.uint64))

@@ -444,9 +444,29 @@ SERVE_OPTS = dict(bisection_budget=4, batch_parents=64, frontier_cap=2048, sampl
 SERVE_BUDGET = 120 * (1 << 30)
 SERVE_ITER_LIMIT = 64 * 32  # expansions per request: at most 32 full iterations
 SERVE_RUNS = ((100, 300), (1000, 1500), (10000, 6000))  # (arrivals per second, requests)
-# time to the 1e-6 gap: a longer budget per request (512 full iterations),
-# at the lowest rate
-SERVE_TTG = (100, 120, 64 * 512)
+# Time to the 1e-6 gap is served on the n=4 QCQP shape of config 1 (fresh
+# instances): the config-5 mix's requests of n >= 8 rarely prove that gap
+# within a bounded budget (the oracle proves 4 of 16 n=8 requests within
+# 262,144 expansions at a 2^15 pool), while 20 of 24 n=4 instances prove
+# within 131,072.  (arrivals per second, requests, expansions per request)
+SERVE_TTG = (100, 150, 64 * 2048)
+SERVE_TTG_CLASSES = [(8, 256)]
+SERVE_TTG_OPTS = dict(SERVE_OPTS, frontier_cap=1 << 15)
+SERVE_TTG_MIN_PROVED = 100  # p99 is reported over at least this many proofs
+
+
+def serving_ttg_run():
+    """Time to the 1e-6 gap under a Poisson stream of n=4 QCQPs (config-1
+    shape, instances 1000 on) at 100 arrivals per second."""
+    from cuminlp_gb300 import generators as G
+    from cuminlp_gb300.solver import DeviceProblem
+    rate, n, limit = SERVE_TTG
+    dps = [DeviceProblem(G.config1(1000 + i)) for i in range(n)]
+    out = serving_run(rate, n, dps, iter_limit=limit, classes=SERVE_TTG_CLASSES, opts=SERVE_TTG_OPTS)
+    out["workload"] = (f"n=4 QCQPs of the config-1 generator (instances 1000..{1000 + n - 1}), {rate} arrivals per "
+                       f"second, one size class of {SERVE_TTG_CLASSES[0][1]} slots, pool cap 2^15 per request, at "
+                       f"most {limit} expansions each")
+    return out
 
 
 def serving_workload() -> str:
@@ -456,14 +476,15 @@ def serving_workload() -> str:
             "120 GiB box-pool admission cap; requests cycle through 400 pre-built problems")
 
 
-def serving_run(rate, n_requests, dps, seed=11, iter_limit=SERVE_ITER_LIMIT):
-    """Poisson arrivals at `rate` per second of the n in {8,16,32,64} mix;
-    requests cycle through the pre-built problems `dps`."""
+def serving_run(rate, n_requests, dps, seed=11, iter_limit=SERVE_ITER_LIMIT, classes=None, opts=None):
+    """Poisson arrivals at `rate` per second of the n in {8,16,32,64} mix (or
+    the given problems); requests cycle through the pre-built problems
+    `dps`."""
     import numpy as np
     from cuminlp_gb300.solver import Server
     slots = max(dp.info()["program_slots"] for dp in dps)
-    srv = Server([(v, k, slots) for v, k in SERVE_CLASSES], pool_budget_bytes=SERVE_BUDGET,
-                 iterations_per_round=2, **SERVE_OPTS)
+    srv = Server([(v, k, slots) for v, k in (classes or SERVE_CLASSES)], pool_budget_bytes=SERVE_BUDGET,
+                 iterations_per_round=2, **(opts or SERVE_OPTS))
     rng = np.random.default_rng(seed)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n_requests))
     ids = []
@@ -487,11 +508,14 @@ def serving_run(rate, n_requests, dps, seed=11, iter_limit=SERVE_ITER_LIMIT):
         e = by_n.setdefault(str(n), {"requests": 0, "proven": 0})
         e["requests"] += 1
         e["proven"] += int(bool(o["proven_optimal"]))
+    p99_ok = len(proven) >= SERVE_TTG_MIN_PROVED
     return {"rate_per_s": rate, "requests": n_requests, "iter_limit_expansions": iter_limit,
             "latency_p50_ms": st["latency_p50_ms"],
             "latency_p99_ms": st["latency_p99_ms"], "latency_max_ms": st["latency_max_ms"],
             "queue_p99_ms": st["queue_p99_ms"], "converged": st["converged"], "proven": len(proven),
-            "proven_by_n": by_n, "time_to_gap_p50_ms": pick(0.5), "time_to_gap_p99_ms": pick(0.99),
+            "proven_by_n": by_n, "time_to_gap_p50_ms": pick(0.5),
+            "time_to_gap_p99_ms": pick(0.99) if p99_ok else None,
+            "time_to_gap_p99_note": None if p99_ok else f"{len(proven)} proofs, fewer than {SERVE_TTG_MIN_PROVED}",
             "boxes_per_s": st["boxes_per_s"], "wall_ms": st["wall_ms"],
             "pool_bytes_peak": st["pool_bytes_peak"], "rounds": st["rounds"]}
 
@@ -650,7 +674,7 @@ def run_ours(args):
         from cuminlp_gb300.solver import DeviceProblem
         dps = [DeviceProblem(G.config5_request(i)) for i in range(400)]
         print(json.dumps({"workload": serving_workload(), "runs": [serving_run(r, n, dps) for r, n in SERVE_RUNS],
-                          "time_to_gap_run": serving_run(SERVE_TTG[0], SERVE_TTG[1], dps, iter_limit=SERVE_TTG[2])}))
+                          "time_to_gap_run": serving_ttg_run()}))
         return
     problem = G.config3(rank)  # replicas: one independent instance per GPU
     dp = DeviceProblem(problem)
@@ -734,7 +758,7 @@ def run_ours(args):
     def serving_leg():
         dps = [DeviceProblem(G.config5_request(i)) for i in range(400)]
         return {"workload": serving_workload(), "runs": [serving_run(r, n, dps) for r, n in SERVE_RUNS],
-                "time_to_gap_run": serving_run(SERVE_TTG[0], SERVE_TTG[1], dps, iter_limit=SERVE_TTG[2])}
+                "time_to_gap_run": serving_ttg_run()}
 
     ref_gpu = None if args.no_reference_gpu else extra_leg(reference_gpu_run)
     ttg = None if args.no_ttg else extra_leg(ttg_leg)

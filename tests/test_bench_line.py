@@ -143,6 +143,7 @@ def test_a_failing_extra_leg_is_recorded_not_fatal(stubbed, monkeypatch):
     d = _line(monkeypatch, ["--steps", "2", "--warmup", "1"])
     assert d["config2_solver"] == {"error": "RuntimeError: out of device memory"}
     assert d["batch_uneven"] == {"error": "RuntimeError: out of device memory"}
-    assert d["value"] > 0 and d["e2e"]["value"] > 0 and d["serving"] == {"workload": bench.serving_workload(),
-                                                                         "runs": [{"latency_p99_ms": 1.0}] * 3,
-                                                                         "time_to_gap_run": {"latency_p99_ms": 1.0}}
+    assert d["value"] > 0 and d["e2e"]["value"] > 0
+    sv = d["serving"]
+    assert sv["workload"] == bench.serving_workload() and sv["runs"] == [{"latency_p99_ms": 1.0}] * 3
+    assert sv["time_to_gap_run"]["latency_p99_ms"] == 1.0 and "n=4" in sv["time_to_gap_run"]["workload"]

@@ -60,8 +60,11 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 EVAL_DRAM_BYTES_PER_BOX = (43186688 + 34048) / 1048576  # ncu, eval_children_kernel<double, 1>, config 2
-# ncu, eval_children_kernel<float, 5>, config 3 (profiles/eval_children_fp32_lazy_config3.md)
-EVAL32_DRAM_BYTES_PER_BOX = None
+# ncu, eval_children_inc_kernel and sample_screen_kernel, config 3 at 2^14
+# parents x 2^4 children (profiles/lazy_form_kernels_config3.md): DRAM
+# bytes per child box / per sample point, scaled by the units of a launch
+INC32_DRAM_BYTES_PER_BOX = 15380736 / 262144
+SCREEN32_DRAM_BYTES_PER_POINT = 20115712 / 262144
 # time-to-gap on config 1: the cluster of boxes within 1e-6 of the optimum
 # holds tens of millions of boxes at n=4, so the frontier is capped at 2^25;
 # 2^21 parents x 2^2 children per iteration timed best (swept over
@@ -719,14 +722,35 @@ def run_ours(args):
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
 
-    # live roofline of the dominant kernel of the headline (lazy) form: the
-    # FP32 child evaluator, phase 1 of the iteration (that kernel, a count
-    # pass, and the FP64 pass over children in the band below the incumbent,
-    # empty without an incumbent)
-    ev_ms = sum(p[1] for p in lazy["phases"])
-    nb = lazy["delta"]["bounded"]
-    achieved32 = nb * fpb / (ev_ms * 1e-3) / 1e12
+    # live rooflines of the headline (lazy) form, per phase of the iteration
+    # (CUDA events at the phase boundaries): the FP64 verdict of the
+    # selected boxes, the FP32 bound of the children, the FP32 sample
+    # screen; the dominant one is `roofline`
     launches = max(1, len(lazy["phases"]))
+    ld = lazy["delta"]
+    pfb = info.get("point_flops_per_box", fpb / 2)
+
+    def phase_line(i, units, flops, peak, kernel, dram_per_unit, unit_name):
+        ms = sum(p[i] for p in lazy["phases"])
+        ach = units * flops / (ms * 1e-3) / 1e12
+        return {"kernel": kernel, "ms_per_step": ms / launches, "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+                "frac": ach / peak, "frac_of_instruction_ceiling": ach / (peak / 2),
+                "flops_per_unit": flops, "units_per_launch": units / launches, "unit_of_work": unit_name,
+                "traffic": None if dram_per_unit is None else dram_per_unit * units / launches}
+
+    phase_rl = {
+        "certify": dict(phase_line(0, ld["expansions"], fpb, peak64,
+                                   "eval_children_kernel<double, 0> (FP64 verdict of each selected box), with the "
+                                   "selection and branch", None, "selected box"), bound="fp64"),
+        "bound": dict(phase_line(1, ld["bounded"], fpb, peak32,
+                                 "inc_common_kernel + eval_children_inc_kernel (FP32 child bounds, incremental)",
+                                 INC32_DRAM_BYTES_PER_BOX, "child box"), bound="fp32"),
+        "sample": dict(phase_line(2, ld["sampled"], pfb, peak32,
+                                  "sample_screen_kernel (FP32 point ranking) + sample_children_kernel (FP64 "
+                                  "point of each chunk's best)", SCREEN32_DRAM_BYTES_PER_POINT, "sample point"),
+                       bound="fp32"),
+    }
+    dominant = max(phase_rl, key=lambda k: phase_rl[k]["ms_per_step"])
     # the plain FP64 evaluator, for the record
     ev64_ms = sum(p[1] for p in plain["phases"])
     nb64 = plain["delta"]["bounded"]
@@ -799,19 +823,11 @@ def run_ours(args):
         "lazy_speedup_vs_plain_fp64": value / plain_value,
         "screen_speedup_vs_plain_fp64": forms["fp32"]["value"] / forms["fp64"]["value"],
         "screen_identical_to_plain": plain["outcome"] == res["fp32"]["outcome"],
-        "roofline": {
-            "bound": "fp32",
-            "kernel": "eval_children_kernel<float, 5> (fused interval DAG evaluator, FP32, lazy form)",
-            "achieved": achieved32, "peak": peak32, "unit": "TFLOP/s", "frac": achieved32 / peak32,
-            "peak_source": "measured by cmn_measure_fma_peak (FFMA loop, all SMs) in this run; FMA counted as 2",
-            # directed rounding forbids FMA: one flop per instruction
-            "frac_of_fp32_instruction_ceiling": achieved32 / (peak32 / 2),
-            "flops_per_box": fpb, "boxes_per_launch": nb / launches,
-            "traffic": None if EVAL32_DRAM_BYTES_PER_BOX is None else EVAL32_DRAM_BYTES_PER_BOX * nb / launches,
-            "hbm": {"achieved": nb * (8 * problem.n_vars + 9) / (ev_ms * 1e-3) / 1e9, "peak": hbm_peak,
-                    "unit": "GB/s", "bytes_per_box": 8 * problem.n_vars + 9,
-                    "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
-        },
+        "roofline": dict(phase_rl[dominant], phase=dominant,
+                         peak_source="measured by cmn_measure_fma_peak (FMA loop, all SMs) in this run; FMA counted "
+                                     "as 2 flops, and directed rounding allows none, so the instruction ceiling is "
+                                     "half the peak"),
+        "phase_rooflines": phase_rl,
         "roofline_plain_fp64": {
             "bound": "fp64", "kernel": "eval_children_kernel<double, 1> (plain FP64 form)",
             "achieved": achieved64, "peak": peak64, "unit": "TFLOP/s", "frac": achieved64 / peak64,

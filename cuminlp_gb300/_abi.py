@@ -97,9 +97,14 @@ class SolveOptions(C.Structure):
         ("precision", C.c_int32), ("bisection_budget", C.c_int32), ("frontier_cap", C.c_uint64),
         ("batch_parents", C.c_uint64), ("sample_points", C.c_uint64), ("sample_all", C.c_int32),
         ("relative_width", C.c_int32), ("max_cycle_size", C.c_uint64), ("enumerate_cap", C.c_uint64),
-        ("has_known_primal", C.c_int32), ("reserved", C.c_int32), ("known_primal_bound", C.c_double),
+        ("has_known_primal", C.c_int32), ("autotune", C.c_int32), ("known_primal_bound", C.c_double),
         ("time_limit_ms", C.c_uint64),
     ]
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("blocks_per_sm", C.c_int32), ("lanes_cap", C.c_int32), ("ms_best", C.c_double),
+                ("ms_default", C.c_double), ("candidates", C.c_int32), ("reserved", C.c_int32)]
 
 
 class BatchConfig(C.Structure):

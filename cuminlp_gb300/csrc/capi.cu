@@ -810,6 +810,115 @@ extern "C" cmn_status cmn_eval_boxes(const cmn_problem* p, int32_t precision, co
 // ----------------------------------------------------------------------
 // solver
 // ----------------------------------------------------------------------
+extern "C" cmn_status cmn_autotune(cmn_problem* p, int32_t precision, uint64_t n_boxes, cmn_tune_result* out)
+{
+  if (!p || !out) return fail(CMN_INVALID_CONFIGURATION, "null argument");
+  if (precision != 0 && precision != 1) return fail(CMN_INVALID_CONFIGURATION, "precision must be 0 or 1");
+  if (n_boxes < 1) return fail(CMN_INVALID_CONFIGURATION, "n_boxes must be at least 1");
+  cmn_status st = check_interval(p);
+  if (st != CMN_OK) return st;
+  const bool fp32 = precision == 1;
+  st = check_smem(p, fp32, 0);
+  if (st != CMN_OK) return st;
+  CK(cudaSetDevice(p->device));
+  CK(ensure_attributes());
+  const int64_t n = p->host.n_vars();
+  // random boxes inside the root box (a fixed seed), as planes
+  std::vector<double> lo((size_t)n * n_boxes), hi((size_t)n * n_boxes);
+  uint64_t x = 0x9e3779b97f4a7c15ULL;
+  auto uni = [&]() {
+    x ^= x << 13;
+    x ^= x >> 7;
+    x ^= x << 17;
+    return (double)(x >> 11) * (1.0 / 9007199254740992.0);
+  };
+  for (int64_t v = 0; v < n; ++v) {
+    const double a = p->host.var_lb[v], b = p->host.var_ub[v];
+    const double span = std::isfinite(b - a) ? b - a : 2.0;
+    const double base = std::isfinite(a) ? a : -1.0;
+    for (uint64_t i = 0; i < n_boxes; ++i) {
+      const double c = base + span * uni(), w = span * 0.05 * uni();
+      double l = std::max(base, c - w), h = std::min(base + span, c + w);
+      if (p->host.var_kinds[v] != CMN_VAR_CONTINUOUS) {
+        l = std::ceil(l);
+        h = std::max(std::floor(h), l);
+      }
+      lo[(size_t)v * n_boxes + i] = l;
+      hi[(size_t)v * n_boxes + i] = h;
+    }
+  }
+  double* d = nullptr;
+  uint8_t* f = nullptr;
+  const size_t planes = (size_t)n * n_boxes;
+  CK(dalloc(&d, 2 * planes + n_boxes));
+  cudaError_t e = dalloc(&f, n_boxes);
+  cudaStream_t s = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d, lo.data(), planes * sizeof(double), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d + planes, hi.data(), planes * sizeof(double), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  EvalArgs a = {};
+  a.prog = fp32 ? p->d_prog32 : p->d_prog64;
+  a.prog_len = (int)p->prog.code64.size();
+  a.n_vars = (int)n;
+  a.n_slots = p->prog.n_slots;
+  a.log2C = 0;
+  a.plo = d;
+  a.phi = d + planes;
+  a.pstride = n_boxes;
+  a.n_children = n_boxes;
+  a.out_lb = d + 2 * planes;
+  a.out_flag = f;
+  a.sched = p->d_sched;
+  const int threads = kEvalThreads;
+  const int occ =
+      std::max(1, eval_kernel_occupancy(0, fp32, eval_smem_bytes(p->prog.n_slots, 0, fp32, threads), threads));
+  const int lanes_max = p->d_sched ? p->prog.group_max : 1;
+  auto time_shape = [&](int bps, int lanes, double& ms) {
+    const uint64_t need = (n_boxes * (uint64_t)lanes + threads - 1) / threads;
+    const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(need, (uint64_t)sm_count() * bps));
+    a.g_max = lanes;
+    a.capacity = (uint64_t)grid * threads;
+    ms = 1e30;
+    for (int r = 0; r < 4 && e == cudaSuccess; ++r) {  // the first launch warms up
+      e = cudaEventRecord(e0, s);
+      if (e == cudaSuccess) e = launch_eval(a, 0, fp32, grid, threads, s);
+      if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+      float t = 0;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+      if (r > 0 && t < ms) ms = t;
+    }
+  };
+  out->candidates = 0;
+  out->ms_best = 1e30;
+  time_shape(occ, lanes_max, out->ms_default);
+  for (int bps = 1; bps <= occ && e == cudaSuccess; ++bps) {
+    for (int lanes = 1; lanes <= lanes_max && e == cudaSuccess; lanes <<= 1) {
+      double ms;
+      time_shape(bps, lanes, ms);
+      ++out->candidates;
+      if (ms < out->ms_best) {
+        out->ms_best = ms;
+        out->blocks_per_sm = bps;
+        out->lanes_cap = lanes;
+      }
+    }
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (s) cudaStreamDestroy(s);
+  dfree(d);
+  dfree(f);
+  if (e != cudaSuccess) return fail(CMN_CUDA_ERROR, std::string("autotune: ") + cudaGetErrorString(e));
+  out->reserved = 0;
+  p->tuned_bps[precision] = out->blocks_per_sm;
+  p->tuned_lanes[precision] = out->lanes_cap;
+  return CMN_OK;
+}
+
 extern "C" void cmn_solve_options_default(cmn_solve_options* o)
 {
   if (!o) return;
@@ -955,8 +1064,20 @@ extern "C" cmn_status cmn_solver_create(const cmn_problem* p, const cmn_solve_op
     cfg.sample_lg_min = lg_min;
     const int occ_s =
         std::max(1, sample_kernel_occupancy(sample_smem_bytes(n, p->prog.n_slots, threads, lg_min), threads));
+    const int tp = fp32 ? 1 : 0;
+    if (o.autotune && p->tuned_bps[tp] == 0) {
+      cmn_tune_result tr{};
+      cmn_status ts =
+          cmn_autotune(const_cast<cmn_problem*>(p), tp, std::min<uint64_t>(maxc, 1ull << 18), &tr);
+      if (ts != CMN_OK) {
+        delete s;
+        return ts;
+      }
+    }
+    const bool tuned = o.autotune && p->tuned_bps[tp] > 0;
     const uint64_t need = (maxc * (uint64_t)p->prog.group_max + threads - 1) / threads;
-    s->eval_grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(need, (uint64_t)sm_count() * occ_e));
+    s->eval_grid = (int)std::max<uint64_t>(
+        1, std::min<uint64_t>(need, (uint64_t)sm_count() * (tuned ? std::min(p->tuned_bps[tp], occ_e) : occ_e)));
     s->sample_grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(need, (uint64_t)sm_count() * occ_s));
     if (lazy) {
       cfg.screen_lg_min = lg_screen;
@@ -965,7 +1086,7 @@ extern "C" cmn_status cmn_solver_create(const cmn_problem* p, const cmn_solve_op
       cfg.screen_grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((maxc + threads - 1) / threads,
                                                                       (uint64_t)sm_count() * occ_q));
     }
-    cfg.g_max = p->d_sched ? p->prog.group_max : 1;
+    cfg.g_max = p->d_sched ? (tuned ? std::min(p->tuned_lanes[tp], p->prog.group_max) : p->prog.group_max) : 1;
     cfg.eval_capacity = (uint64_t)s->eval_grid * threads;
     cfg.sample_capacity = (uint64_t)s->sample_grid * threads;
 

@@ -986,30 +986,31 @@ __device__ __forceinline__ void point_range32(const Instr* __restrict__ prog, in
                                               PointVerdict32& out)
 {
   float acc = 0.0f;
-  Instr ins = pc0 < pc1 ? load_instr(prog, pc0) : Instr{};
+  // this thread's point column: variable v at x[v * stride]
+  const float* __restrict__ x = t.lo + t.tid;
+  const int st = t.stride;
+  const int4* __restrict__ code4 = reinterpret_cast<const int4*>(prog);
+  int4 raw = pc0 < pc1 ? __ldg(code4 + pc0) : make_int4(0, 0, 0, 0);
   for (int pc = pc0; pc < pc1; ++pc) {
-    const Instr cur = ins;
-    if (pc + 1 < pc1) ins = load_instr(prog, pc + 1);
+    const int4 w = raw;
+    if (pc + 1 < pc1) raw = __ldg(code4 + pc + 1);  // software prefetch
+    // the common case first, straight from the instruction's words: head in
+    // bits 0-7 of word 0, a and b in word 1, the coefficient in word 2
+    if ((w.x & 7) == kOpTerm) {
+      const int sub = (w.x >> 3) & 31;
+      const uint32_t ab = (uint32_t)w.y;
+      const float xa = x[(int)(ab & 0xffffu) * st];
+      const float xb = x[(int)(ab >> 16) * st];  // b == a for sqr(x_a) and x_a terms
+      float p = (sub & kTermPMask) == kTermVar ? xa : __fmul_rn(xa, xb);
+      if (sub & kTermHasC) p = __fmul_rn(__int_as_float(w.z), p);
+      acc = (sub & kTermInit) ? p : ((sub & kTermSub) ? __fsub_rn(acc, p) : __fadd_rn(acc, p));
+      continue;
+    }
+    Instr cur;
+    memcpy(&cur, &w, sizeof(Instr));
     const int code = cur.head & 7;
     const int sub = cur.head >> 3;
     switch (code) {
-      case kOpTerm: {
-        float p;
-        const int pk = sub & kTermPMask;
-        const float xa = t.lo[cur.a * t.stride + t.tid];
-        if (pk == kTermProd) {
-          p = __fmul_rn(xa, t.lo[cur.b * t.stride + t.tid]);
-        } else if (pk == kTermSqr) {
-          p = __fmul_rn(xa, xa);
-        } else {
-          p = xa;
-        }
-        if (sub & kTermHasC) p = __fmul_rn(cur.c32.clo, p);
-        if (sub & kTermInit) acc = p;
-        else if (sub & kTermSub) acc = __fsub_rn(acc, p);
-        else acc = __fadd_rn(acc, p);
-        break;
-      }
       case kOpGeneric: {
         const float a = pfetch32(t, acc, cur, cur.modes & 3, cur.a);
         const float b = pfetch32(t, acc, cur, (cur.modes >> 2) & 3, cur.b);

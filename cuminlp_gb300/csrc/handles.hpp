@@ -23,6 +23,10 @@ struct cmn_problem {
   int32_t* d_inc_seg = nullptr;  // incremental child tables (Program::inc_*), null when none
   int32_t* d_inc_off = nullptr;
   int32_t* d_inc_pcs = nullptr;
+  // cmn_autotune's choice per precision (0 FP64, 1 FP32): blocks per SM
+  // and lanes per box cap; 0 = not tuned
+  int tuned_bps[2] = {0, 0};
+  int tuned_lanes[2] = {0, 0};
 
   ~cmn_problem();
 };

@@ -98,6 +98,13 @@ class DeviceProblem:
         check(lib().cmn_problem_program(self.handle, precision, A.ptr(buf), n.value, C.byref(n)))
         return buf
 
+    def autotune(self, precision: int = 0, n_boxes: int = 1 << 16) -> dict:
+        """cmn_autotune: times the evaluator's launch shapes on this problem
+        and records the fastest for solvers created with autotune=1."""
+        r = A.TuneResult()
+        check(lib().cmn_autotune(self.handle, precision, n_boxes, C.byref(r)))
+        return {f: getattr(r, f) for f, _ in A.TuneResult._fields_ if f != "reserved"}
+
     def info(self) -> dict:
         inf = A.ProblemInfo()
         check(lib().cmn_problem_get_info(self.handle, C.byref(inf)))

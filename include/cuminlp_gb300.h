@@ -350,7 +350,8 @@ typedef struct cmn_solve_options {
   uint64_t max_cycle_size;    /* slot cap (SearchCalibration) 0 = 64 */
   uint64_t enumerate_cap;     /* SearchCalibration::enumerate_cap */
   int32_t has_known_primal;   /* seeds GUB (known_primal_bound) */
-  int32_t reserved;
+  int32_t autotune;           /* 1: the evaluator's launch shape from
+                                 cmn_autotune (run on first use) */
   double known_primal_bound;
   uint64_t time_limit_ms;     /* 0 = none */
 } cmn_solve_options;
@@ -486,6 +487,26 @@ cmn_status cmn_fp64_emu_check_host(uint64_t n, uint64_t seed, int32_t family, ui
  * and *out unwritten, when an operand or the result is not a normal number
  * or a sum cancels exactly (those take the FP64 instruction). */
 cmn_status cmn_fp64_emu_op_host(int32_t op, double a, double b, double* out, int32_t* handled);
+
+/* Timed autotuning of the fused evaluator's launch shape for one problem.
+ * No counterpart in the reference (its graph backend launches one kernel
+ * per DAG node with a fixed shape).  Candidates: blocks per SM from 1 to
+ * the kernel's residency, and caps on the lanes that share one box (boxes
+ * per warp = 32 / lanes) of 1, 2, 4 ... up to the program's useful
+ * maximum; each is timed with CUDA events over `n_boxes` random boxes
+ * inside the root box, best of three launches.  The fastest is recorded on
+ * the problem (for `precision` 0, FP64, or 1, FP32) and used by every
+ * solver created for it with cmn_solve_options.autotune = 1; results never
+ * depend on the choice.  Synchronous; allocates its test boxes. */
+typedef struct cmn_tune_result {
+  int32_t blocks_per_sm;   /* chosen */
+  int32_t lanes_cap;       /* chosen: most lanes per box */
+  double ms_best;          /* its launch time */
+  double ms_default;       /* the untuned shape's (full residency, program's lane maximum) */
+  int32_t candidates;      /* shapes timed */
+  int32_t reserved;
+} cmn_tune_result;
+cmn_status cmn_autotune(cmn_problem* problem, int32_t precision, uint64_t n_boxes, cmn_tune_result* out);
 
 /* The compiled program of a problem (the fused evaluator's straight-line
  * code), for tools and tests: `precision` 0 gives the FP64 program, 1 the

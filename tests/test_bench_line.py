@@ -51,7 +51,8 @@ class _DeviceProblem:
 
 def _solver_run(dp, rt, precision, steps, warmup, **kw):
     return {"ms": 60.0 * steps, "wall_ms": 61.0 * steps,
-            "delta": {"bounded": (1 << 20) * steps, "screened_fp32": 0, "certified_fp64": (1 << 20) * steps},
+            "delta": {"bounded": (1 << 20) * steps, "screened_fp32": 0, "certified_fp64": (1 << 20) * steps,
+                      "expansions": (1 << 16) * steps, "sampled": (1 << 20) * steps},
             "phases": [[0.1, 43.0, 17.0, 0.8, 60.0]] * steps, "kernels_per_iter": 42,
             "outcome": {"lower_bound": -1.0, "upper_bound": 1.0, "frontier_size": 1 << 20}}
 
@@ -103,10 +104,12 @@ def test_default_line_carries_the_contract(stubbed, monkeypatch):
     assert d["ms_per_step"] == pytest.approx(60.0)
     assert "workload" in d["config"]
     r = d["roofline"]
-    for k in ("bound", "achieved", "peak", "unit", "frac", "traffic"):
+    for k in ("bound", "achieved", "peak", "unit", "frac", "traffic", "phase"):
         assert k in r, k
     assert r["frac"] == pytest.approx(r["achieved"] / r["peak"])
-    assert r["achieved"] == pytest.approx((1 << 20) * 28930.0 / 43e-3 / 1e12)
+    # the stub's longest phase is the bound (43 ms of 60)
+    assert r["phase"] == "bound" and r["achieved"] == pytest.approx((1 << 20) * 28930.0 / 43e-3 / 1e12)
+    assert set(d["phase_rooflines"]) == {"certify", "bound", "sample"}
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == 75e3 and cb["sample"]
     e = d["e2e"]

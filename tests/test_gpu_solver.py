@@ -254,3 +254,26 @@ def test_incremental_fp32_bounds_enclose_fp64(cfg):
         fe64, lb64 = op.bound(box, kinds, vids, widths, n)
         assert np.all(lb32 <= lb64)
         assert not np.any(fe64.astype(bool) & ~fe32.astype(bool))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "lazy"])
+def test_autotuned_launch_shape_changes_no_result(precision):
+    # cmn_autotune times launch shapes (blocks per SM, lanes per box); a
+    # solver on the tuned shape must give the untuned solver's search bit
+    # for bit
+    p = G.config1(2)
+    dp = DeviceProblem(p)
+    t = dp.autotune(0 if precision == "fp64" else 1, 1 << 14)
+    assert t["candidates"] >= 1 and t["blocks_per_sm"] >= 1 and t["lanes_cap"] >= 1
+    assert t["ms_best"] <= t["ms_default"] * 1.05
+    out = []
+    for tune in (0, 1):
+        s = Solver(dp, batch_iter_limit=20, bisection_budget=3, batch_parents=256, precision=precision,
+                   autotune=tune)
+        s.step(0)
+        out.append((s.outcome(), s.frontier()))
+        s.close()
+    (a, fa), (b, fb) = out
+    assert a["lower_bound"] == b["lower_bound"] and a["upper_bound"] == b["upper_bound"]
+    assert a["counters"] == b["counters"]
+    assert bits_equal(fa[1], fb[1]) and bits_equal(fa[0], fb[0])

@@ -450,11 +450,13 @@ SERVE_RUNS = ((100, 300), (1000, 1500), (10000, 6000))  # (arrivals per second, 
 # Time to the 1e-6 gap is served on the n=4 QCQP shape of config 1 (fresh
 # instances): the config-5 mix's requests of n >= 8 rarely prove that gap
 # within a bounded budget (the oracle proves 4 of 16 n=8 requests within
-# 262,144 expansions at a 2^15 pool), while 20 of 24 n=4 instances prove
-# within 131,072.  (arrivals per second, requests, expansions per request)
-SERVE_TTG = (100, 150, 64 * 2048)
+# 262,144 expansions at a 2^15 pool), while 31 of 40 n=4 instances prove
+# within 131,072 at the largest pool a batch slot takes (8192 entries, less
+# one iteration's 64 x 2^4 children).  (arrivals per second, requests,
+# expansions per request)
+SERVE_TTG = (100, 160, 64 * 2048)
 SERVE_TTG_CLASSES = [(8, 256)]
-SERVE_TTG_OPTS = dict(SERVE_OPTS, frontier_cap=1 << 15)
+SERVE_TTG_OPTS = dict(SERVE_OPTS, frontier_cap=8192 - 64 * 16)
 SERVE_TTG_MIN_PROVED = 100  # p99 is reported over at least this many proofs
 
 
@@ -467,7 +469,7 @@ def serving_ttg_run():
     dps = [DeviceProblem(G.config1(1000 + i)) for i in range(n)]
     out = serving_run(rate, n, dps, iter_limit=limit, classes=SERVE_TTG_CLASSES, opts=SERVE_TTG_OPTS)
     out["workload"] = (f"n=4 QCQPs of the config-1 generator (instances 1000..{1000 + n - 1}), {rate} arrivals per "
-                       f"second, one size class of {SERVE_TTG_CLASSES[0][1]} slots, pool cap 2^15 per request, at "
+                       f"second, one size class of {SERVE_TTG_CLASSES[0][1]} slots, pool cap 7168 per request, at "
                        f"most {limit} expansions each")
     return out
 
@@ -554,6 +556,9 @@ def config2_run(rt, steps, warmup) -> dict:
 
 
 REF_GPU = ROOT / "oracle" / "_ref" / "ref_gpu"
+# iteration cap of the reference driver over the host-core roles on config 1,
+# instance 0 (about 15 s of host time)
+REF_DRIVER_ITER_CAP = 2_500_000
 
 
 def _ref_gpu_call(args: list[str], text: str, timeout: float = 900.0) -> dict:
@@ -597,16 +602,24 @@ def reference_gpu_run() -> dict:
             "speedup": g / ours, "mismatched_feasible": int(r["bound_mismatch_feasible"][0]),
             "mismatched_lb": int(r["bound_mismatch_lb"][0]),
             "graph_build_s": float(r["bound_build_seconds_graph"][0])}
-    head = f"B 100000 2 2 1 0 1 {(1e-6).hex()}\n"
-    text = head + problem_text(G.config1(1))
-    for backend in ("graph", "gb300"):
-        lines = _ref_gpu_call(["driver", backend], text)["lines"]
+    def driver(backend, inst, iter_limit):
+        head = f"B {iter_limit} 2 2 1 0 1 {(1e-6).hex()}\n"
+        lines = _ref_gpu_call(["driver", backend], head + problem_text(G.config1(inst)))["lines"]
         h = lines[0].split()
-        out[f"time_to_gap_config1_instance1_{backend}"] = {
-            "seconds": float(lines[3].split()[1]), "stop_reason": h[2], "proven_optimal": int(h[3]),
-            "lower_bound": float.fromhex(h[0]), "upper_bound": float.fromhex(h[1]),
-            "expansions": int(lines[1].split()[0])}
+        lb, ub = float.fromhex(h[0]), float.fromhex(h[1])
+        return {"seconds": float(lines[3].split()[1]), "stop_reason": h[2], "proven_optimal": int(h[3]),
+                "lower_bound": lb, "upper_bound": ub, "rel_gap": (ub - lb) / max(1.0, abs(ub)),
+                "expansions": int(lines[1].split()[0])}
+
+    for backend in ("graph", "gb300", "oracle"):
+        out[f"time_to_gap_config1_instance1_{backend}"] = driver(backend, 1, 100000)
+    # instance 0 needs about 10^8 single-box expansions in this driver; the
+    # host-core run is capped and reports the gap it reached
+    out["time_to_gap_config1_instance0_oracle"] = driver("oracle", 0, REF_DRIVER_ITER_CAP)
     out["driver"] = "reference SearchDriver, BisectionBudget B=2, one sample per region"
+    out["backends"] = {"graph": "the reference's CUDA graph backend on this GPU",
+                       "gb300": "this library's roles through include/cuminlp_gb300/region_backend.hpp",
+                       "oracle": "the CPU oracle's roles on all host cores (the host's directed rounding)"}
     return out
 
 
@@ -784,7 +797,14 @@ def run_ours(args):
         return {"workload": serving_workload(), "runs": [serving_run(r, n, dps) for r, n in SERVE_RUNS],
                 "time_to_gap_run": serving_ttg_run()}
 
+    def autotune_leg():
+        # cmn_autotune on the headline problem: launch shapes timed over
+        # 2^18 random boxes, FP64 and FP32 evaluator
+        return {"fp64": dp.autotune(0, 1 << 18), "fp32": dp.autotune(1, 1 << 18),
+                "candidates": "blocks per SM 1..residency x lanes per box 1, 2, 4 .. program maximum"}
+
     ref_gpu = None if args.no_reference_gpu else extra_leg(reference_gpu_run)
+    tune = extra_leg(autotune_leg)
     ttg = None if args.no_ttg else extra_leg(ttg_leg)
     config2 = None if args.no_config2 else extra_leg(config2_run, rt, args.steps, args.warmup)
     batch = None if args.no_batch else extra_leg(batch_leg)
@@ -847,6 +867,7 @@ def run_ours(args):
         "gpu_launches": kpi * args.steps,
         "clocks": clocks,
         "reference_gpu": ref_gpu,
+        "autotune": tune,
         "time_to_gap": ttg,
         "config2_solver": config2,
         "batch_uneven": batch,

@@ -60,7 +60,8 @@ def compile_ref_gpu(force: bool = False) -> Path | None:
     deps = [HEADER, HERE / "ref_gpu.cu", ROOT / "include" / "cuminlp_gb300.h",
             ROOT / "include" / "cuminlp_gb300" / "region_backend.hpp",
             ROOT / "include" / "cuminlp_gb300" / "aggregate_backend.hpp",
-            HERE / "ref_shim_gpu" / "cuinterval" / "cuinterval.h", HERE / "ref_shim_gpu" / "cuinterval" / "interval.h"]
+            HERE / "ref_shim_gpu" / "cuinterval" / "cuinterval.h", HERE / "ref_shim_gpu" / "cuinterval" / "interval.h",
+            HERE / "oracle.h", HERE / "ref_oracle_roles.hpp"]
     if force or _stale(OBJ, deps):
         _run([_nvcc(), "-std=c++20", "-O2", ARCH, "--expt-relaxed-constexpr", "-w",
               f"-I{REF_OUT}", f"-I{HERE / 'ref_shim_gpu'}", f"-I{ROOT / 'include'}",
@@ -69,11 +70,16 @@ def compile_ref_gpu(force: bool = False) -> Path | None:
 
 
 def link_ref_gpu(lib: Path, force: bool = False) -> Path | None:
-    """Links the harness against the library built in place."""
+    """Links the harness against the library built in place, and against
+    the oracle (its "oracle" backend: the reference driver over the CPU
+    oracle's roles)."""
     if not available() or not OBJ.exists():
         return None
+    from cuminlp_gb300 import build as b
+    orc = b.build_oracle()
     objs = [OBJ] + ([GAMS_OBJ] if GAMS_OBJ.exists() else [])
-    if force or _stale(EXE, objs + [lib]):
+    if force or _stale(EXE, objs + [lib, orc]):
         _run([_nvcc(), ARCH, *map(str, objs), "-o", str(EXE), f"-L{lib.parent}", "-lcuminlp_gb300",
-              "-Xlinker", "-rpath", "-Xlinker", str(lib.parent)])
+              f"-L{orc.parent}", "-loracle", "-Xlinker", "-rpath", "-Xlinker", str(lib.parent),
+              "-Xlinker", "-rpath", "-Xlinker", str(orc.parent)])
     return EXE

@@ -15,8 +15,9 @@
 //   driver <backend> <in> <out>
 //       SearchDriver::solve (search/driver.hpp:137-537) with the policy that
 //       make_policy (policy/greedy_enum.hpp:204-223) builds, over
-//       backend "gb300" (this library, through the adapter) or "graph"
-//       (the reference's GraphBackendFactory).  <in> starts with
+//       backend "gb300" (this library, through the adapter), "graph"
+//       (the reference's GraphBackendFactory) or "oracle" (the CPU
+//       oracle's roles on all host cores, oracle/ref_oracle_roles.hpp).  <in> starts with
 //       "<policy B|R|G|W> <iter_limit> <B> <partition_num> <enum_cap>
 //        <max_cycle> <samples> <tolerance>".  Writes bounds, stop reason,
 //       claims, counters, best point, and the solve's wall time.
@@ -51,11 +52,17 @@
 #include <memory>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "cuminlp_ref_gpu.cuh"
 #include "cuminlp_gb300/aggregate_backend.hpp"
 #include "cuminlp_gb300/region_backend.hpp"
+
+extern "C" {
+#include "oracle.h"
+}
+#include "ref_oracle_roles.hpp"
 
 using namespace cuminlp;
 
@@ -122,10 +129,28 @@ static model::Problem<double> load_problem(std::istream& in)
   return P;
 }
 
-static std::shared_ptr<const backend::RegionBackendFactory<double>> make_backend(const std::string& name)
+// The oracle's problem behind the "oracle" backend, alive until exit.
+struct OracleProblem {
+  orc_problem* p = nullptr;
+  ~OracleProblem() { orc_problem_destroy(p); }
+};
+
+static std::shared_ptr<const backend::RegionBackendFactory<double>> make_backend(const std::string& name,
+                                                                                 const model::Problem<double>& P)
 {
   if (name == "gb300") return std::make_shared<cuminlp_gb300::GB300BackendFactory>();
   if (name == "graph") return std::make_shared<backend::graph::GraphBackendFactory<double>>();
+  if (name == "oracle") {
+    // the reference's region work on the host cores: the oracle's roles
+    // with the host's directed-rounding hardware, one thread per core
+    static OracleProblem held;
+    if (held.p) orc_problem_destroy(held.p);
+    cuminlp_gb300::detail::Flat f(P);
+    held.p = orc_problem_create(&f.desc);
+    if (!held.p) throw std::runtime_error(orc_last_error());
+    const int threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    return std::make_shared<cmn_oracle_roles::OracleFactory>(held.p, threads, true);
+  }
   throw std::runtime_error("unknown backend " + name);
 }
 
@@ -145,7 +170,7 @@ static int cmd_driver(const std::string& backend_name, std::istream& in, std::os
   cal.max_cycle_size = max_cycle;
   std::shared_ptr<const policy::CompositionPolicy<double>> pol =
       policy::make_policy<double>(kind, region::FanOutSpec(pn, ecap), B, cal);
-  search::SearchDriver<double> drv(pol, make_backend(backend_name), iter_limit, tol, samples);
+  search::SearchDriver<double> drv(pol, make_backend(backend_name, P), iter_limit, tol, samples);
   std::streambuf* prev = std::cout.rdbuf();
   std::ostringstream sink;
   std::cout.rdbuf(sink.rdbuf());
@@ -225,7 +250,7 @@ static int cmd_roles(std::istream& in, std::ostream& out)
     std::vector<std::vector<unsigned char>> fe(2);
     std::vector<std::vector<double>> lb(2);
     for (int b = 0; b < 2; ++b) {
-      auto fac = make_backend(names[b]);
+      auto fac = make_backend(names[b], P);
       const double t0 = now_s();
       auto bundle = fac->build_subdivision(P, a.composition, n_regions, budget, backend::RoleRequest{false, true, false});
       out << "bound_build_seconds_" << names[b] << ' ' << (now_s() - t0) << '\n';
@@ -249,7 +274,7 @@ static int cmd_roles(std::istream& in, std::ostream& out)
     size_t bad = 0;
     std::vector<std::vector<std::string>> rec(2);
     for (int b = 0; b < 2; ++b) {
-      auto fac = make_backend(names[b]);
+      auto fac = make_backend(names[b], P);
       const double t0 = now_s();
       auto bundle = fac->build_subdivision(P, a.composition, n_regions, budget, backend::RoleRequest{true, false, false});
       out << "sample_build_seconds_" << names[b] << ' ' << (now_s() - t0) << '\n';

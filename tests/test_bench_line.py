@@ -44,6 +44,9 @@ class _DeviceProblem:
     def __init__(self, problem, **kw):
         self.n_vars = problem.n_vars
 
+    def autotune(self, precision, n_boxes):
+        return {"blocks_per_sm": 5, "lanes_cap": 1, "ms_best": 1.0, "ms_default": 1.0, "candidates": 30}
+
     def info(self):
         return {"n_nodes": 10819, "buffer_node_count": 7982, "program_length": 2854, "program_slots": 0,
                 "flops_per_box": 28930.0, "bytes_per_box": 529.0}

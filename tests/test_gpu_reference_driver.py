@@ -10,6 +10,9 @@ through the adapter include/cuminlp_gb300/region_backend.hpp.  These tests:
   them (policy/greedy_enum.hpp:204-223), and require the golden runs of the
   same driver over the oracle bit for bit: bounds, stop reason, claims,
   counters and the best point;
+- run the same driver over the CPU oracle's roles on all host cores with the
+  host's directed rounding (the "oracle" backend the bench times) and
+  require the same golden runs;
 - run the same driver over the reference's own CUDA graph backend
   (backend/graph/*, with the build's interval operators standing in for the
   missing cuinterval) and require the same golden runs: this pins the
@@ -75,7 +78,7 @@ def driver_runs():
     return json.loads((GOLDEN / "driver.json").read_text())
 
 
-@pytest.mark.parametrize("backend", ["gb300", "graph"])
+@pytest.mark.parametrize("backend", ["gb300", "graph", "oracle"])
 @pytest.mark.parametrize("idx", range(9))
 def test_reference_driver_bisection(backend, idx):
     want = driver_runs()[idx]
@@ -85,7 +88,7 @@ def test_reference_driver_bisection(backend, idx):
     check_run(lines, want, [want["counters"][k] for k in COUNTERS])
 
 
-@pytest.mark.parametrize("backend", ["gb300", "graph"])
+@pytest.mark.parametrize("backend", ["gb300", "graph", "oracle"])
 @pytest.mark.parametrize("idx", range(len(POLICY_RUNS)))
 def test_reference_driver_policies(backend, idx):
     want = json.loads((GOLDEN / "driver_policies.json").read_text())[idx]

@@ -311,12 +311,14 @@ def solver_run(dp, rt, precision, steps, warmup, e=E_PARENTS, b=B_BITS, cap=CAP)
     rt.sync()
     before = s.outcome()["counters"]
     ev0, ev1 = rt.event(), rt.event()
-    phases = []
+    phases, lazy_phases = [], []
     t0 = time.perf_counter()
     rt.record(ev0, s.stream)
     for _ in range(steps):
         s.step(1)
         phases.append(phase_ms(s))
+        if precision == "lazy":
+            lazy_phases.append(s.lazy_ms())
     rt.record(ev1, s.stream)
     ms = rt.elapsed_ms(ev0, ev1)
     wall = (time.perf_counter() - t0) * 1e3
@@ -325,8 +327,8 @@ def solver_run(dp, rt, precision, steps, warmup, e=E_PARENTS, b=B_BITS, cap=CAP)
     kpi = s_kernels(s)
     s.close()
     delta = {k: after[k] - before[k] for k in after}
-    return {"ms": ms, "wall_ms": wall, "delta": delta, "phases": phases, "kernels_per_iter": kpi,
-            "outcome": {k: out[k] for k in ("lower_bound", "upper_bound", "frontier_size")}}
+    return {"ms": ms, "wall_ms": wall, "delta": delta, "phases": phases, "lazy_phases": lazy_phases,
+            "kernels_per_iter": kpi, "outcome": {k: out[k] for k in ("lower_bound", "upper_bound", "frontier_size")}}
 
 
 def phase_ms(s):
@@ -535,6 +537,9 @@ def forms_summary(res: dict, steps: int) -> dict:
                   "phases_ms": [round(sum(ph[i] for ph in r["phases"]) / len(r["phases"]), 3) for i in range(5)],
                   "fp32_boxes": d["screened_fp32"], "fp64_boxes": d["certified_fp64"],
                   "certify_pruned": d.get("certify_pruned", 0)}
+        if r.get("lazy_phases"):
+            lp = r["lazy_phases"]
+            out[p]["verdict_and_fp32_bound_ms"] = [round(sum(x[i] for x in lp) / len(lp), 3) for i in range(2)]
     return out
 
 
@@ -705,6 +710,7 @@ def run_ours(args):
             r = solver_run(dp, rt, prec, args.steps, args.warmup, e=e, cap=args.cap or CONFIG3_CAP)
             out[f"{prec}_ms"] = r["ms"]
             out[f"{prec}_boxes/s"] = r["delta"]["bounded"] / (r["ms"] * 1e-3)
+            out[f"{prec}_phases_ms"] = forms_summary({prec: r}, args.steps)[prec]
         print(json.dumps(out))
         return
 
@@ -736,15 +742,15 @@ def run_ours(args):
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
 
     # live rooflines of the headline (lazy) form, per phase of the iteration
-    # (CUDA events at the phase boundaries): the FP64 verdict of the
-    # selected boxes, the FP32 bound of the children, the FP32 sample
-    # screen; the dominant one is `roofline`
+    # (CUDA events inside the captured iteration): the FP64 verdict of the
+    # selected boxes (on its own stream) and the FP32 bound of the children,
+    # which run at once, and the sampling; the dominant one is `roofline`
     launches = max(1, len(lazy["phases"]))
     ld = lazy["delta"]
     pfb = info.get("point_flops_per_box", fpb / 2)
 
-    def phase_line(i, units, flops, peak, kernel, dram_per_unit, unit_name):
-        ms = sum(p[i] for p in lazy["phases"])
+    def phase_line(i, units, flops, peak, kernel, dram_per_unit, unit_name, source="phases"):
+        ms = sum(p[i] for p in lazy[source])
         ach = units * flops / (ms * 1e-3) / 1e12
         return {"kernel": kernel, "ms_per_step": ms / launches, "achieved": ach, "peak": peak, "unit": "TFLOP/s",
                 "frac": ach / peak, "frac_of_instruction_ceiling": ach / (peak / 2),
@@ -753,11 +759,13 @@ def run_ours(args):
 
     phase_rl = {
         "certify": dict(phase_line(0, ld["expansions"], fpb, peak64,
-                                   "eval_children_kernel<double, 0> (FP64 verdict of each selected box), with the "
-                                   "selection and branch", None, "selected box"), bound="fp64"),
+                                   "eval_children_kernel<double, 0> (FP64 verdict of each selected box, on its own "
+                                   "stream beside the branching and the FP32 bound)", None, "selected box",
+                                   "lazy_phases"), bound="fp64"),
         "bound": dict(phase_line(1, ld["bounded"], fpb, peak32,
-                                 "inc_common_kernel + eval_children_inc_kernel (FP32 child bounds, incremental)",
-                                 INC32_DRAM_BYTES_PER_BOX, "child box"), bound="fp32"),
+                                 "inc_common_kernel + eval_children_inc_kernel (FP32 child bounds, incremental; "
+                                 "beside the FP64 verdict)", INC32_DRAM_BYTES_PER_BOX, "child box", "lazy_phases"),
+                      bound="fp32"),
         "sample": dict(phase_line(2, ld["sampled"], pfb, peak32,
                                   "sample_screen_kernel (FP32 point ranking) + sample_children_kernel (FP64 "
                                   "point of each chunk's best)", SCREEN32_DRAM_BYTES_PER_POINT, "sample point"),

@@ -54,6 +54,7 @@ SIGNATURES = {
     "cmn_solver_stream": (P, [P]),
     "cmn_solver_frontier": (I32, [P, P, P, P, U64, C.POINTER(U64)]),
     "cmn_solver_phase_ms": (I32, [P, C.POINTER(D)]),
+    "cmn_solver_lazy_ms": (I32, [P, C.POINTER(D)]),
     "cmn_solver_kernels_per_iteration": (U64, [P]),
     "cmn_measure_fma_peak": (I32, [I32, C.POINTER(D)]),
     "cmn_fp64_emu_check": (I32, [U64, U64, I32, C.POINTER(U64)]),

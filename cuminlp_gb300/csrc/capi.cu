@@ -960,15 +960,20 @@ struct cmn_solver {
   double elapsed_ms = 0;
   uint64_t launched = 0;
   uint64_t kernels_per_iter = 0;
-  cudaEvent_t marks[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t marks[kPhaseMarks] = {};
+  SideStream side;
 
   ~cmn_solver()
   {
     int cur = 0;
     if (p && cudaGetDevice(&cur) == cudaSuccess && cur != p->device) cudaSetDevice(p->device);
     if (stream) cudaStreamSynchronize(stream);
+    if (side.stream) cudaStreamSynchronize(side.stream);
     for (cudaEvent_t ev : marks)
       if (ev) cudaEventDestroy(ev);
+    if (side.fork) cudaEventDestroy(side.fork);
+    if (side.join) cudaEventDestroy(side.join);
+    if (side.stream) cudaStreamDestroy(side.stream);
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
     if (exec_steady) cudaGraphExecDestroy(exec_steady);
@@ -1168,13 +1173,21 @@ extern "C" cmn_status cmn_solver_create(const cmn_problem* p, const cmn_solve_op
     e = solver_init(cfg, b, p->d_root_lb, p->d_root_ub, gub0, s->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(b.best_point, 0xff, (size_t)n * sizeof(double), s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-    for (int i = 0; i < 5 && e == cudaSuccess; ++i) e = cudaEventCreate(&s->marks[i]);
+    for (int i = 0; i < kPhaseMarks && e == cudaSuccess; ++i) e = cudaEventCreate(&s->marks[i]);
+    // the side stream carries the lazy form's FP64 verdict, the longest of
+    // the work it runs beside: its blocks go first
+    int prio_low = 0, prio_high = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s->side.stream, cudaStreamNonBlocking, prio_high);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->side.fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->side.join, cudaEventDisableTiming);
     // capture one iteration, with and without the parent select
     for (int steady = 0; steady < 2 && e == cudaSuccess; ++steady) {
       cudaGraph_t* g = steady ? &s->graph_steady : &s->graph;
       e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
       if (e == cudaSuccess) {
-        cudaError_t e2 = solver_iteration(cfg, b, s->eval_grid, s->sample_grid, s->stream, s->marks, steady == 0);
+        cudaError_t e2 =
+            solver_iteration(cfg, b, s->eval_grid, s->sample_grid, s->stream, s->side, s->marks, steady == 0);
         e = cudaStreamEndCapture(s->stream, g);
         if (e2 != cudaSuccess) e = e2;
       }
@@ -1390,6 +1403,20 @@ extern "C" cmn_status cmn_solver_phase_ms(cmn_solver* s, double* ms5)
   }
   CK(cudaEventElapsedTime(&t, s->marks[0], s->marks[4]));
   ms5[4] = t;
+  return CMN_OK;
+}
+
+extern "C" cmn_status cmn_solver_lazy_ms(cmn_solver* s, double* ms2)
+{
+  if (!s || !ms2) return fail(CMN_INVALID_CONFIGURATION, "null argument");
+  if (s->cfg.precision != CMN_PRECISION_FP32_LAZY)
+    return fail(CMN_INVALID_CONFIGURATION, "the solver does not run the lazy form");
+  CK(cudaEventSynchronize(s->marks[4]));
+  float t = 0;
+  CK(cudaEventElapsedTime(&t, s->marks[5], s->marks[6]));
+  ms2[0] = t;
+  CK(cudaEventElapsedTime(&t, s->marks[1], s->marks[7]));
+  ms2[1] = t;
   return CMN_OK;
 }
 

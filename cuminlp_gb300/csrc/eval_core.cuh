@@ -982,6 +982,21 @@ __device__ __forceinline__ float pfetch32(const Tile<float>& t, float acc, const
   }
 }
 
+// One chain term of the FP32 point program on one point: acc (+|-)
+// [c *] (x_a [* x_b]), each operation rounded to nearest; `cbits` is the
+// coefficient's bit pattern.
+__device__ __forceinline__ float term32(float acc, int sub, float xa, float xb, int cbits)
+{
+  float p = (sub & kTermPMask) == kTermVar ? xa : __fmul_rn(xa, xb);
+  if (sub & kTermHasC) p = __fmul_rn(__int_as_float(cbits), p);
+  return (sub & kTermInit) ? p : ((sub & kTermSub) ? __fsub_rn(acc, p) : __fadd_rn(acc, p));
+}
+
+// Terms the point interpreters take at once when the next instructions are
+// all terms: their words and variables are loaded before the first add, so
+// the loads of a run overlap.
+constexpr int kTermRun = 4;
+
 __device__ __forceinline__ void point_range32(const Instr* __restrict__ prog, int pc0, int pc1, const Tile<float>& t,
                                               PointVerdict32& out)
 {
@@ -990,20 +1005,37 @@ __device__ __forceinline__ void point_range32(const Instr* __restrict__ prog, in
   const float* __restrict__ x = t.lo + t.tid;
   const int st = t.stride;
   const int4* __restrict__ code4 = reinterpret_cast<const int4*>(prog);
-  int4 raw = pc0 < pc1 ? __ldg(code4 + pc0) : make_int4(0, 0, 0, 0);
-  for (int pc = pc0; pc < pc1; ++pc) {
-    const int4 w = raw;
-    if (pc + 1 < pc1) raw = __ldg(code4 + pc + 1);  // software prefetch
-    // the common case first, straight from the instruction's words: head in
-    // bits 0-7 of word 0, a and b in word 1, the coefficient in word 2
+  int pc = pc0;
+  while (pc < pc1) {
+    // the common case first, straight from the instruction's words (head
+    // in bits 0-7 of word 0, a and b in word 1, the coefficient in word 2):
+    // a run of kTermRun terms, every load issued before the first add
+    if (pc + kTermRun <= pc1) {
+      int4 w[kTermRun];
+      int all = 0;
+#pragma unroll
+      for (int q = 0; q < kTermRun; ++q) {
+        w[q] = __ldg(code4 + pc + q);
+        all |= (w[q].x & 7) ^ kOpTerm;
+      }
+      if (all == 0) {
+        float xa[kTermRun], xb[kTermRun];
+#pragma unroll
+        for (int q = 0; q < kTermRun; ++q) {
+          xa[q] = x[(int)((uint32_t)w[q].y & 0xffffu) * st];
+          xb[q] = x[(int)((uint32_t)w[q].y >> 16) * st];  // b == a for sqr(x_a) and x_a terms
+        }
+#pragma unroll
+        for (int q = 0; q < kTermRun; ++q) acc = term32(acc, (w[q].x >> 3) & 31, xa[q], xb[q], w[q].z);
+        pc += kTermRun;
+        continue;
+      }
+    }
+    const int4 w = __ldg(code4 + pc);
+    ++pc;
     if ((w.x & 7) == kOpTerm) {
-      const int sub = (w.x >> 3) & 31;
       const uint32_t ab = (uint32_t)w.y;
-      const float xa = x[(int)(ab & 0xffffu) * st];
-      const float xb = x[(int)(ab >> 16) * st];  // b == a for sqr(x_a) and x_a terms
-      float p = (sub & kTermPMask) == kTermVar ? xa : __fmul_rn(xa, xb);
-      if (sub & kTermHasC) p = __fmul_rn(__int_as_float(w.z), p);
-      acc = (sub & kTermInit) ? p : ((sub & kTermSub) ? __fsub_rn(acc, p) : __fadd_rn(acc, p));
+      acc = term32(acc, (w.x >> 3) & 31, x[(int)(ab & 0xffffu) * st], x[(int)(ab >> 16) * st], w.z);
       continue;
     }
     Instr cur;

@@ -89,6 +89,14 @@ __device__ __forceinline__ void write_verdict(const EvalArgs& a, uint64_t g, uin
                                               double gub)
 {
   double lb = (double)v.obj.lo;
+  if (kMode == 5 && a.parent_lb == nullptr) {
+    // the solver's lazy form: the parent's FP64 verdict runs beside this
+    // pass, and lazy_fold_kernel folds it in and settles every state but
+    // these two
+    a.out_lb[g] = lb;
+    a.out_flag[g] = v.excluded ? kChildInfeasible : kChildScreened;
+    return;
+  }
   if (kMode == 5) {
     // the parent's certified bound holds for every child box inside it
     const double plb = a.parent_lb[k];

@@ -183,14 +183,26 @@ struct SolverBufs {
 // Initialises the device state: the root box as the only pool entry.
 cudaError_t solver_init(const SolverCfg& cfg, const SolverBufs& b, const double* root_lb_host,
                         const double* root_ub_host, double gub0, cudaStream_t s);
+// The lazy form's second stream: the FP64 verdict of the staged parents
+// runs on `stream` beside the branching and the FP32 child bounds, forked
+// from and joined back to the iteration's stream by the two events.
+struct SideStream {
+  cudaStream_t stream = nullptr;
+  cudaEvent_t fork = nullptr;
+  cudaEvent_t join = nullptr;
+};
+
 // Enqueues one batched iteration (all kernels) on `s`; capturable.
-// `marks` (5 events or null) are recorded as event nodes at the phase
-// boundaries: start, after branching, after bounding, after sampling, end.
+// `marks` (kPhaseMarks events or null) are recorded as event nodes: 0-4 at
+// the phase boundaries (start, after branching, after bounding, after
+// sampling, end); in the lazy form 5 and 6 around the FP64 verdict on the
+// side stream and 7 after the FP32 child bounds.
 // `with_select`: the iteration selects and stages its own parents (the first
 // iteration); otherwise the previous iteration staged them, and the
 // iteration flags a device error if it did not.
+constexpr int kPhaseMarks = 8;
 cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval_grid, int sample_grid,
-                             cudaStream_t s, const cudaEvent_t* marks, bool with_select);
+                             cudaStream_t s, const SideStream& side, const cudaEvent_t* marks, bool with_select);
 // Fills min key / viable count of the current pool (after the run).
 cudaError_t solver_pool_stats(const SolverCfg& cfg, const SolverBufs& b, uint64_t* viable_dev, cudaStream_t s);
 // Copies pool entries [start, start + count) in position order: boxes as

@@ -1078,8 +1078,7 @@ __global__ void branch_kernel(const SolverCfg cfg, const SolverBufs b)
   const int n = cfg.n_vars;
   const PolicyParams pp = {cfg.log2C, cfg.max_cycle, cfg.enumerate_cap, cfg.relative};
   const bool lazy = cfg.precision == CMN_PRECISION_FP32_LAZY;
-  const double gub = d->gub;
-  uint64_t fathomed = 0, fathomed_points = 0, bounded = 0, certified = 0, dropped = 0;
+  uint64_t fathomed = 0, fathomed_points = 0, bounded = 0;
   EnumCand ec_local[kLocal > 0 ? kLocal : 1];
   BisCand bc_local[kLocal > 0 ? kLocal : 1];
   uint64_t heap_local[kLocal > 0 ? kLocal : 1];
@@ -1089,17 +1088,46 @@ __global__ void branch_kernel(const SolverCfg cfg, const SolverBufs b)
     uint64_t* heap = kLocal > 0 ? heap_local : b.heap_scratch + k * (uint64_t)n;
     SlotPlan* sp = b.slots + k * (uint64_t)cfg.max_slots;
     ParentInfo pi = bisection_policy(b.plo + k, b.phi + k, cfg.e_max, n, b.kinds, pp, ec, bc, heap, sp);
-    if (lazy) {
-      // the box's FP64 verdict, computed on selection: the reference
-      // predicate or the incumbent excludes it, so it is not expanded
-      ++certified;
-      const double plb = b.plb[k];
-      if (!b.pfeas[k] || plb > gub) {
-        pi = ParentInfo{0, 0, 0};
-        ++dropped;
-      }
-    }
     b.pinfo[k] = pi;
+    // lazy form: the box's FP64 verdict runs beside this kernel, and
+    // lazy_drop_kernel applies it and counts afterwards
+    if (lazy) continue;
+    if (pi.fathom) {
+      ++fathomed;
+      fathomed_points += pi.nreg;
+    } else {
+      bounded += pi.nreg;
+    }
+  }
+  if (lazy) return;  // every thread of the block takes this branch
+  unsigned long long c[3] = {fathomed, fathomed_points, bounded};
+  block_sum(c);
+  if (threadIdx.x == 0) {
+    if (c[0]) atomicAdd((unsigned long long*)&b.dev->counters.fathomed, c[0]);
+    if (c[1]) atomicAdd((unsigned long long*)&b.dev->counters.fathomed_points, c[1]);
+    if (c[2]) atomicAdd((unsigned long long*)&b.dev->counters.bounded, c[2]);
+  }
+}
+
+// Lazy form, after the FP64 verdict of the staged parents (run beside the
+// branching): a box that the reference predicate or the incumbent excludes
+// is not expanded -- its plan becomes empty -- and the expansion counters
+// are taken as branch_kernel takes them for the other forms.
+__global__ void lazy_drop_kernel(const SolverCfg cfg, const SolverBufs b)
+{
+  const SolverDev* d = b.dev;
+  if (d->done) return;
+  const uint64_t E = d->n_parents;
+  const double gub = d->gub;
+  uint64_t fathomed = 0, fathomed_points = 0, bounded = 0, certified = 0, dropped = 0;
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < E; k += (uint64_t)gridDim.x * blockDim.x) {
+    ParentInfo pi = b.pinfo[k];
+    ++certified;
+    if (!b.pfeas[k] || b.plb[k] > gub) {
+      pi = ParentInfo{0, 0, 0};
+      b.pinfo[k] = pi;
+      ++dropped;
+    }
     if (pi.fathom) {
       ++fathomed;
       fathomed_points += pi.nreg;
@@ -1115,6 +1143,37 @@ __global__ void branch_kernel(const SolverCfg cfg, const SolverBufs b)
     if (c[2]) atomicAdd((unsigned long long*)&b.dev->counters.bounded, c[2]);
     if (c[3]) atomicAdd((unsigned long long*)&b.dev->counters.certified_fp64, c[3]);
     if (c[4]) atomicAdd((unsigned long long*)&b.dev->counters.certify_pruned, c[4]);
+  }
+}
+
+// Lazy form, per child, after lazy_drop_kernel: the FP32 pass wrote the
+// child's own FP32 bound and, for a box it proved infeasible or a
+// duplicate, the final state.  A child of a dropped parent has no box; for
+// the others the parent's certified bound, which holds for every child box
+// inside it, is folded in, and the state follows from the folded bound:
+// above the incumbent, within the band below it (to the FP64 pass, which
+// may prune it; below the band FP64 could not), or eligible.
+__global__ void lazy_fold_kernel(const SolverCfg cfg, const SolverBufs b)
+{
+  const SolverDev* d = b.dev;
+  if (d->done) return;
+  const uint64_t total = d->n_children;
+  const double gub = d->gub;
+  const double floor_b = certify_floor(gub);
+  for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < total;
+       g += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t k = g >> cfg.log2C, r = g & ((1ULL << cfg.log2C) - 1ULL);
+    const ParentInfo pi = b.pinfo[k];
+    if (pi.fathom || r >= pi.nreg) {
+      b.cstate[g] = kChildNone;
+      continue;
+    }
+    const uint8_t st = b.cstate[g];
+    if (st == kChildInfeasible || st == kChildDuplicate) continue;
+    const double plb = b.plb[k], lb32 = b.clb[g];
+    const double lb = plb > lb32 ? plb : lb32;
+    b.clb[g] = lb;
+    b.cstate[g] = lb > gub ? kChildDominated : lb >= floor_b ? kChildScreened : kChildEligible;
   }
 }
 
@@ -1341,8 +1400,9 @@ static void mark(const cudaEvent_t* marks, int i, cudaStream_t s)
 }
 
 cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval_grid, int sample_grid,
-                             cudaStream_t s, const cudaEvent_t* marks, bool with_select)
+                             cudaStream_t s, const SideStream& side, const cudaEvent_t* marks, bool with_select)
 {
+  const bool lazy = cfg.precision == CMN_PRECISION_FP32_LAZY;
   const uint64_t max_children = cfg.e_max << cfg.log2C;
   const uint64_t max_pool = cfg.pstride;
   mark(marks, 0, s);
@@ -1357,8 +1417,14 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
 
   // (1b) lazy form: the FP64 verdict of every staged parent -- its bound
   // has been an FP32 one (with its own parent's FP64 bound folded in) since
-  // it was appended
-  if (cfg.precision == CMN_PRECISION_FP32_LAZY) {
+  // it was appended.  It runs on the side stream, beside the branching and
+  // the FP32 child bounds, which do not read it: the 2^-B share of boxes
+  // it evaluates leaves part of the GPU idle on its own.
+  if (lazy) {
+    cudaError_t e = cudaEventRecord(side.fork, s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(side.stream, side.fork, 0);
+    if (e != cudaSuccess) return e;
+    mark(marks, 5, side.stream);
     EvalArgs pa = {};
     pa.prog = b.prog64;
     pa.prog_len = cfg.prog_len;
@@ -1375,7 +1441,10 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
     pa.sched = b.sched;
     pa.g_max = cfg.g_max;
     pa.capacity = cfg.eval_capacity;
-    cudaError_t e = launch_eval(pa, 0, false, eval_grid, kEvalThreads, s);
+    e = launch_eval(pa, 0, false, eval_grid, kEvalThreads, side.stream);
+    if (e != cudaSuccess) return e;
+    mark(marks, 6, side.stream);
+    e = cudaEventRecord(side.join, side.stream);
     if (e != cudaSuccess) return e;
   }
 
@@ -1427,11 +1496,11 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
     ca.list_count = &b.dev->certify_count;
     e = launch_eval(ca, 3, false, eval_grid, kEvalThreads, s);
     if (e != cudaSuccess) return e;
-  } else if (cfg.precision == CMN_PRECISION_FP32_LAZY) {
+  } else if (lazy) {
     ea.prog = b.prog32;
     ea.plo32 = b.plo32;
     ea.phi32 = b.phi32;
-    ea.parent_lb = b.plb;
+    ea.parent_lb = nullptr;  // folded in by lazy_fold_kernel
     if (cfg.inc) {
       ea.inc_segments = cfg.inc_segments;
       ea.n_parents_dev = &b.dev->n_parents;
@@ -1444,6 +1513,17 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
       e = launch_eval(ea, 5, true, eval_grid, kEvalThreads, s);
     }
     if (e != cudaSuccess) return e;
+    mark(marks, 7, s);
+    // join the parents' FP64 verdict: drop the boxes it excludes, fold the
+    // certified bounds into their children
+    e = cudaStreamWaitEvent(s, side.join, 0);
+    if (e != cudaSuccess) return e;
+    {
+      const int pgrid = (int)std::min<uint64_t>((cfg.e_max + 255) / 256, 1024);
+      lazy_drop_kernel<<<pgrid, 256, 0, s>>>(cfg, b);
+      const int cgrid = (int)std::min<uint64_t>((max_children + 255) / 256, 2048);
+      lazy_fold_kernel<<<cgrid, 256, 0, s>>>(cfg, b);
+    }
     // the survivors within the band below the incumbent, in FP64
     ScreenedChild sc{b};
     compact(sc, max_children, &b.dev->n_children, &b.dev->certify_count, b, s);
@@ -1452,6 +1532,7 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
     ca.prog = b.prog64;
     ca.plo32 = nullptr;
     ca.phi32 = nullptr;
+    ca.parent_lb = b.plb;
     ca.inc_segments = 0;
     ca.list = b.list;
     ca.list_count = &b.dev->certify_count;

@@ -334,6 +334,13 @@ class Solver:
         check(lib().cmn_solver_phase_ms(self.handle, ms))
         return list(ms)
 
+    def lazy_ms(self) -> list[float]:
+        """Lazy form: [FP64 verdict of the staged parents, FP32 child bounds]
+        device ms of the last iteration; the two run at once."""
+        ms = (C.c_double * 2)()
+        check(lib().cmn_solver_lazy_ms(self.handle, ms))
+        return list(ms)
+
     @property
     def stream(self) -> int:
         return lib().cmn_solver_stream(self.handle) or 0

@@ -457,9 +457,16 @@ cmn_status cmn_solver_frontier(cmn_solver* solver, double* boxes,
 
 /* Phase timings of the most recent iteration, from CUDA events recorded
  * inside the captured iteration: [0] select+branch, [1] bound (FP64
- * evaluation, or FP32 screen + FP64 certify), [2] sample + incumbent,
- * [3] prune + pool rebuild, [4] whole iteration; milliseconds. */
+ * evaluation, or FP32 screen + FP64 certify; in the lazy form the FP32
+ * child bounds, the wait for the parents' FP64 verdict that runs beside
+ * them, and the fold), [2] sample + incumbent, [3] prune + pool rebuild,
+ * [4] whole iteration; milliseconds. */
 cmn_status cmn_solver_phase_ms(cmn_solver* solver, double* ms5);
+/* Lazy form only: [0] the FP64 verdict of the staged parents, timed on
+ * its own stream, [1] the FP32 child bounds, timed on the iteration's
+ * stream from the end of branching; both run at once, so they overlap
+ * phases [0] and [1] above.  Milliseconds, most recent iteration. */
+cmn_status cmn_solver_lazy_ms(cmn_solver* solver, double* ms2);
 /* Kernel nodes one captured iteration launches. */
 uint64_t cmn_solver_kernels_per_iteration(const cmn_solver* solver);
 

@@ -57,6 +57,7 @@ def _solver_run(dp, rt, precision, steps, warmup, **kw):
             "delta": {"bounded": (1 << 20) * steps, "screened_fp32": 0, "certified_fp64": (1 << 20) * steps,
                       "expansions": (1 << 16) * steps, "sampled": (1 << 20) * steps},
             "phases": [[0.1, 43.0, 17.0, 0.8, 60.0]] * steps, "kernels_per_iter": 42,
+            "lazy_phases": [[20.0, 43.0]] * steps if precision == "lazy" else [],
             "outcome": {"lower_bound": -1.0, "upper_bound": 1.0, "frontier_size": 1 << 20}}
 
 
@@ -110,7 +111,7 @@ def test_default_line_carries_the_contract(stubbed, monkeypatch):
     for k in ("bound", "achieved", "peak", "unit", "frac", "traffic", "phase"):
         assert k in r, k
     assert r["frac"] == pytest.approx(r["achieved"] / r["peak"])
-    # the stub's longest phase is the bound (43 ms of 60)
+    # the stub's longest phase is the FP32 bound (43 ms of 60; the FP64 verdict beside it 20 ms)
     assert r["phase"] == "bound" and r["achieved"] == pytest.approx((1 << 20) * 28930.0 / 43e-3 / 1e12)
     assert set(d["phase_rooflines"]) == {"certify", "bound", "sample"}
     cb = d["cpu_baseline"]

@@ -611,10 +611,24 @@ __device__ __forceinline__ void interval_range(const Instr* __restrict__ prog, i
                                                const Tile<T>& t, Verdict<T>& out)
 {
   Iv<T> acc = {T(0), T(0)};
-  Instr ins = pc0 < pc1 ? load_instr(prog, pc0) : Instr{};
-  for (int pc = pc0; pc < pc1; ++pc) {
-    const Instr cur = ins;
-    if (pc + 1 < pc1) ins = load_instr(prog, pc + 1);  // software prefetch
+  int pc = pc0;
+  while (pc < pc1) {
+    // two terms in a row: both products before the first add, so the two
+    // interval products (and their variable loads) overlap
+    if (pc + 2 <= pc1) {
+      const Instr c0 = load_instr(prog, pc), c1 = load_instr(prog, pc + 1);
+      if ((c0.head & 7) == kOpTerm && (c1.head & 7) == kOpTerm) {
+        const int s0 = c0.head >> 3, s1 = c1.head >> 3;
+        const Iv<T> p0 = term_value<T, V>(c0, s0, vars);
+        const Iv<T> p1 = term_value<T, V>(c1, s1, vars);
+        acc = (s0 & kTermInit) ? p0 : ((s0 & kTermSub) ? iv_sub(acc, p0) : iv_add(acc, p0));
+        acc = (s1 & kTermInit) ? p1 : ((s1 & kTermSub) ? iv_sub(acc, p1) : iv_add(acc, p1));
+        pc += 2;
+        continue;
+      }
+    }
+    const Instr cur = load_instr(prog, pc);
+    ++pc;
     const int code = cur.head & 7;
     const int sub = cur.head >> 3;
     switch (code) {
@@ -826,35 +840,68 @@ __device__ __forceinline__ double pt_mul_const(double c, double p)
   return (CMN_FP64_EMU & 16) ? emu::mul_rn(c, p) : __dmul_rn(c, p);
 }
 
+// One chain term of the FP64 point program: acc (+|-) [c *] (x_a [* x_b]),
+// each operation rounded to nearest (the products as pt_mul_* give them).
+// xb is read for every term: b == a for sqr(x_a) and x_a terms.
+__device__ __forceinline__ double term64(double acc, const Instr& cur, double xa, double xb)
+{
+  using A = Arith<double>;
+  const int sub = cur.head >> 3;
+  const int pk = sub & kTermPMask;
+  double p;
+  if (pk == kTermProd) {
+    p = pt_mul_var(xa, xb);
+  } else if (pk == kTermSqr) {
+    p = pt_mul_var(xa, xa);
+  } else {
+    p = xa;
+  }
+  if (sub & kTermHasC) p = pt_mul_const(cur.c, p);
+  if (sub & kTermInit) return p;
+  return (sub & kTermSub) ? A::sub_rn(acc, p) : A::add_rn(acc, p);
+}
+
+// Terms the FP64 point interpreter takes at once when the next
+// instructions are all terms.
+constexpr int kPointRun64 = 4;
+
 __device__ __forceinline__ void point_range(const Instr* __restrict__ prog, int pc0, int pc1, const Tile<double>& t,
                                             PointVerdict& out)
 {
-  using A = Arith<double>;
   double acc = 0.0;
-  Instr ins = pc0 < pc1 ? load_instr(prog, pc0) : Instr{};
-  for (int pc = pc0; pc < pc1; ++pc) {
-    const Instr cur = ins;
-    if (pc + 1 < pc1) ins = load_instr(prog, pc + 1);
+  int pc = pc0;
+  while (pc < pc1) {
+    // a run of kPointRun64 terms: their words and variables are loaded
+    // before the first add, so the loads of a run overlap
+    if (pc + kPointRun64 <= pc1) {
+      Instr c[kPointRun64];
+      int all = 0;
+#pragma unroll
+      for (int q = 0; q < kPointRun64; ++q) {
+        c[q] = load_instr(prog, pc + q);
+        all |= (c[q].head & 7) ^ kOpTerm;
+      }
+      if (all == 0) {
+        double xa[kPointRun64], xb[kPointRun64];
+#pragma unroll
+        for (int q = 0; q < kPointRun64; ++q) {
+          xa[q] = t.lo[c[q].a * t.stride + t.tid];
+          xb[q] = t.lo[c[q].b * t.stride + t.tid];
+        }
+#pragma unroll
+        for (int q = 0; q < kPointRun64; ++q) acc = term64(acc, c[q], xa[q], xb[q]);
+        pc += kPointRun64;
+        continue;
+      }
+    }
+    const Instr cur = load_instr(prog, pc);
+    ++pc;
     const int code = cur.head & 7;
     const int sub = cur.head >> 3;
     switch (code) {
-      case kOpTerm: {
-        double p;
-        const int pk = sub & kTermPMask;
-        const double xa = t.lo[cur.a * t.stride + t.tid];
-        if (pk == kTermProd) {
-          p = pt_mul_var(xa, t.lo[cur.b * t.stride + t.tid]);
-        } else if (pk == kTermSqr) {
-          p = pt_mul_var(xa, xa);
-        } else {
-          p = xa;
-        }
-        if (sub & kTermHasC) p = pt_mul_const(cur.c, p);
-        if (sub & kTermInit) acc = p;
-        else if (sub & kTermSub) acc = A::sub_rn(acc, p);
-        else acc = A::add_rn(acc, p);
+      case kOpTerm:
+        acc = term64(acc, cur, t.lo[cur.a * t.stride + t.tid], t.lo[cur.b * t.stride + t.tid]);
         break;
-      }
       case kOpGeneric: {
         const double a = pfetch(t, acc, cur, cur.modes & 3, cur.a);
         const double b = pfetch(t, acc, cur, (cur.modes >> 2) & 3, cur.b);
@@ -995,7 +1042,7 @@ __device__ __forceinline__ float term32(float acc, int sub, float xa, float xb, 
 // Terms the point interpreters take at once when the next instructions are
 // all terms: their words and variables are loaded before the first add, so
 // the loads of a run overlap.
-constexpr int kTermRun = 4;
+constexpr int kTermRun = 8;
 
 __device__ __forceinline__ void point_range32(const Instr* __restrict__ prog, int pc0, int pc1, const Tile<float>& t,
                                               PointVerdict32& out)

@@ -536,7 +536,8 @@ def forms_summary(res: dict, steps: int) -> dict:
         out[p] = {"value": d["bounded"] / (r["ms"] * 1e-3), "unit": "boxes/s", "ms_per_step": r["ms"] / steps,
                   "phases_ms": [round(sum(ph[i] for ph in r["phases"]) / len(r["phases"]), 3) for i in range(5)],
                   "fp32_boxes": d["screened_fp32"], "fp64_boxes": d["certified_fp64"],
-                  "certify_pruned": d.get("certify_pruned", 0)}
+                  "certify_pruned": d.get("certify_pruned", 0),
+                  "pruned_infeasible": d.get("pruned_infeasible", 0), "pruned_dominated": d.get("pruned_dominated", 0)}
         if r.get("lazy_phases"):
             lp = r["lazy_phases"]
             out[p]["verdict_and_fp32_bound_ms"] = [round(sum(x[i] for x in lp) / len(lp), 3) for i in range(2)]

@@ -921,6 +921,8 @@ __device__ __forceinline__ void point_range(const Instr* __restrict__ prog, int 
         const double v = pfetch(t, acc, cur, cur.modes & 3, cur.a);
         const bool ok = (sub == 0) ? (v <= cur.c) : almost_equal(v, cur.c);
         out.feasible = out.feasible && ok;
+        // an infeasible point counts as +inf whatever the rest gives: stop
+        if (!ok) return;
         break;
       }
       case kOpObjective:
@@ -952,7 +954,8 @@ __device__ inline PointVerdict run_point_lane(const Instr* __restrict__ prog, co
   out.feasible = true;
   out.has_obj = false;
   const LaneSegs ls = lane_segments(sched, l, lane);
-  for (int j = ls.b; j < ls.e; ++j) point_range(prog, __ldg(ls.pairs + 2 * j), __ldg(ls.pairs + 2 * j + 1), t, out);
+  for (int j = ls.b; j < ls.e && out.feasible; ++j)
+    point_range(prog, __ldg(ls.pairs + 2 * j), __ldg(ls.pairs + 2 * j + 1), t, out);
   return out;
 }
 
@@ -1109,6 +1112,8 @@ __device__ __forceinline__ void point_range32(const Instr* __restrict__ prog, in
         const double v = (double)pfetch32(t, acc, cur, cur.modes & 3, cur.a);
         const bool ok = (sub == 0) ? (v <= cur.c) : almost_equal(v, cur.c);
         out.feasible = out.feasible && ok;
+        // an infeasible point ranks as +inf whatever the rest gives: stop
+        if (!ok) return;
         break;
       }
       case kOpObjective:

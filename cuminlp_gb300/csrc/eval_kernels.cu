@@ -770,7 +770,7 @@ __global__ void __launch_bounds__(kEvalThreads) sample_screen_kernel(const Sampl
         if (lg == 0) {
           point_range32(a.prog, p0, p1, t, pv);
         } else {
-          for (int j = ls.b; j < ls.e; ++j)
+          for (int j = ls.b; j < ls.e && pv.feasible; ++j)
             point_range32(a.prog, __ldg(ls.pairs + 2 * j), __ldg(ls.pairs + 2 * j + 1), t, pv);
         }
       }

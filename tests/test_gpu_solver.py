@@ -196,6 +196,9 @@ def test_lazy_form_matches_oracle_small_problems():
     # selection) on the fixture problems, with pruning at certification
     for name in ("square_le5", "infeasible", "aggregate", "contract", "int_eq", "miqcqp_n6"):
         compare(problems()[name], 12, bisection_budget=2, batch_parents=64, sample_points=2, precision="lazy")
+        # every valid child sampled, whatever its bound
+        compare(problems()[name], 8, bisection_budget=3, batch_parents=16, sample_points=1, sample_all=1,
+                precision="lazy")
 
 
 @pytest.mark.parametrize("instance", [0, 1, 2])

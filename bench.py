@@ -712,6 +712,9 @@ def run_ours(args):
             out[f"{prec}_ms"] = r["ms"]
             out[f"{prec}_boxes/s"] = r["delta"]["bounded"] / (r["ms"] * 1e-3)
             out[f"{prec}_phases_ms"] = forms_summary({prec: r}, args.steps)[prec]
+            out[f"{prec}_per_step"] = [[round(x, 3) for x in ph] for ph in r["phases"]]
+            if r.get("lazy_phases"):
+                out[f"{prec}_per_step_verdict_bound"] = [[round(x, 3) for x in ph] for ph in r["lazy_phases"]]
         print(json.dumps(out))
         return
 

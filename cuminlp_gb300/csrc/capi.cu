@@ -1130,6 +1130,7 @@ extern "C" cmn_status cmn_solver_create(const cmn_problem* p, const cmn_solve_op
       b.inc_off = p->d_inc_off;
       b.inc_pcs = p->d_inc_pcs;
       A(&b.inc_common, 2 * (size_t)cfg.inc_segments * cfg.e_max);
+      A(&b.inc_parts, 2 * (size_t)cfg.inc_segments * ((size_t)1 << cfg.log2C) * cfg.e_max);
     }
     A(&b.pslot, cfg.e_max);
     A(&b.pinfo, cfg.e_max);

@@ -285,15 +285,6 @@ __device__ __forceinline__ void eval_children(const EvalArgs& a, const S* plo, c
   }
 }
 
-// Whether variable v is parent k's split variable of a slot before `j`
-// (ovid holds this thread's slot variables at stride `stride`).
-__device__ __forceinline__ bool split_before(const int32_t* ovid, int stride, int j, int v)
-{
-  for (int q = 0; q < j; ++q)
-    if (ovid[q * stride] == v) return true;
-  return false;
-}
-
 // Lazy form, incremental children, pass 1: for every (segment s, parent
 // k), the sum of segment s's chain terms that read none of k's split
 // variables, over the parent's FP32 planes.  A warp covers 32 parents of
@@ -338,13 +329,99 @@ __global__ void __launch_bounds__(kEvalThreads) inc_common_kernel(const EvalArgs
   }
 }
 
-// Lazy form, incremental children, pass 2: each child starts every
-// segment's chain from its parent's common sum and adds the terms that read
-// its split variables -- for each split variable in slot order, its terms
-// in program order, a term reading two split variables taken with the
-// first of them -- then runs the segment's checks and objective.  One lane
-// per child; shared memory holds the child's split variables as in
-// eval_children.
+// A parent box's FP32 planes with one variable narrowed to one part of its
+// slot (pass 2 of the incremental children).
+struct PartVars {
+  const float* plo;
+  const float* phi;
+  uint64_t pstride;
+  int vid;
+  Iv<float> val;
+  __device__ __forceinline__ Iv<float> var(int v) const
+  {
+    if (v == vid) return val;
+    const uint64_t off = (uint64_t)v * pstride;
+    return {__ldg(plo + off), __ldg(phi + off)};
+  }
+};
+
+// Whether variable v is the variable of one of slots 0..j-1.
+__device__ __forceinline__ bool slot_var_before(const SlotPlan* sp, int j, int v)
+{
+  for (int q = 0; q < j; ++q)
+    if (sp[q].vid == (uint32_t)v) return true;
+  return false;
+}
+
+// Lazy form, incremental children, pass 2: for every (slot part u, parent
+// k) -- part p of slot j -- and every segment s, the chain sum (from zero,
+// in program order) of the segment's terms that read slot j's variable v
+// and no variable of an earlier slot, with v over part p of its slot and
+// every other variable, split at a later slot or not, over the parent's
+// bounds.  A variable that an earlier slot already splits contributes
+// nothing here.  Each child then adds, per segment, the part sum of each of
+// its slots (eval_children_inc_kernel): a sibling shares each part sum with
+// the siblings on the same part of that slot.
+__global__ void __launch_bounds__(kEvalThreads) inc_parts_kernel(const EvalArgs a)
+{
+  if (a.done != nullptr && *a.done) return;
+  const uint64_t E = *a.n_parents_dev;
+  const uint64_t C = 1ULL << a.log2C;
+  const int S = a.inc_segments;
+  for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < E * C;
+       idx += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t u = idx / E, k = idx - u * E;
+    const ParentInfo pi = a.pinfo[k];
+    if (pi.fathom || pi.nreg == 0) continue;  // no bounded children
+    const SlotPlan* sp = a.slots + k * (uint64_t)a.max_slots;
+    int j = -1;
+    uint64_t p = 0, base = 0;
+    for (uint32_t q = 0; q < pi.count; ++q) {
+      const uint64_t w = sp[q].width;
+      if (u < base + w) {
+        j = (int)q;
+        p = u - base;
+        break;
+      }
+      base += w;
+    }
+    if (j < 0) continue;  // u beyond this parent's parts
+    const SlotPlan sj = sp[j];
+    const int vj = (int)sj.vid;
+    const bool repeated = slot_var_before(sp, j, vj);
+    PartVars pv;
+    pv.plo = a.plo32 + k;
+    pv.phi = a.phi32 + k;
+    pv.pstride = a.pstride;
+    pv.vid = vj;
+    double lo, hi;
+    slot_bounds(sj, a.plo[(uint64_t)vj * a.pstride + k], a.phi[(uint64_t)vj * a.pstride + k], p, lo, hi);
+    pv.val = {Widen<float, double>::lo(lo), Widen<float, double>::hi(hi)};
+    for (int s = 0; s < S; ++s) {
+      Iv<float> acc = {0.0f, 0.0f};
+      if (!repeated) {
+        const int q0 = __ldg(a.inc_off + (uint64_t)vj * S + s), q1 = __ldg(a.inc_off + (uint64_t)vj * S + s + 1);
+        for (int q = q0; q < q1; ++q) {
+          const Instr cur = load_instr(a.prog, __ldg(a.inc_pcs + q));
+          if ((cur.head & 7) == kOpTerm) {
+            const int other = cur.a == vj ? cur.b : cur.a;
+            if (other != vj && slot_var_before(sp, j, other)) continue;  // that slot's part sum has it
+          }
+          acc = chain_add<float, PartVars>(acc, cur, pv);
+        }
+      }
+      const uint64_t at = 2 * (((uint64_t)s * C + u) * a.pstride + k);
+      a.inc_parts[at] = acc.lo;
+      a.inc_parts[at + 1] = acc.hi;
+    }
+  }
+}
+
+// Lazy form, incremental children, pass 3: each child starts every
+// segment's chain from its parent's common sum, adds the part sum of each
+// of its slots in slot order, then runs the segment's checks and objective.
+// One lane per child; shared memory holds the child's split variables (as
+// in eval_children, for the checks and the objective) and its slot parts.
 __global__ void __launch_bounds__(kEvalThreads, CMN_EVAL_MIN_BLOCKS) eval_children_inc_kernel(const EvalArgs a)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -354,10 +431,12 @@ __global__ void __launch_bounds__(kEvalThreads, CMN_EVAL_MIN_BLOCKS) eval_childr
   float* olo = base + threadIdx.x;
   float* ohi = olo + (size_t)ms * B;
   int32_t* ovid = reinterpret_cast<int32_t*>(base + (size_t)2 * ms * B) + threadIdx.x;
+  uint32_t* opart = reinterpret_cast<uint32_t*>(base + (size_t)3 * ms * B) + threadIdx.x;
   if (a.done != nullptr && *a.done) return;
   const uint64_t total = a.n_children_dev ? *a.n_children_dev : a.n_children;
   const double gub = a.gub ? *a.gub : DBL_MAX;
   const int S = a.inc_segments;
+  const uint64_t C = 1ULL << a.log2C;
   for (uint64_t g = (uint64_t)blockIdx.x * B + threadIdx.x; g < total; g += (uint64_t)gridDim.x * B) {
     uint64_t k, r;
     child_of(a.log2C, g, k, r);
@@ -372,22 +451,21 @@ __global__ void __launch_bounds__(kEvalThreads, CMN_EVAL_MIN_BLOCKS) eval_childr
       a.out_flag[g] = kChildDuplicate;
       continue;
     }
+    {
+      const SlotPlan* sp = a.slots + k * (uint64_t)a.max_slots;
+      uint64_t pbase = 0;
+      for (int j = 0; j < cv.count; ++j) {
+        opart[j * B] = (uint32_t)(pbase + slot_part(r, sp[j]));
+        pbase += sp[j].width;
+      }
+    }
     Verdict<float> v = verdict_init<float>();
     for (int s = 0; s < S; ++s) {
       Iv<float> acc = {a.inc_common[2 * ((uint64_t)s * a.pstride + k)],
                        a.inc_common[2 * ((uint64_t)s * a.pstride + k) + 1]};
       for (int j = 0; j < cv.count; ++j) {
-        const int vj = ovid[j * B];
-        if (split_before(ovid, B, j, vj)) continue;  // the same variable in two slots
-        const int q0 = __ldg(a.inc_off + (uint64_t)vj * S + s), q1 = __ldg(a.inc_off + (uint64_t)vj * S + s + 1);
-        for (int q = q0; q < q1; ++q) {
-          const Instr cur = load_instr(a.prog, __ldg(a.inc_pcs + q));
-          if ((cur.head & 7) == kOpTerm) {
-            const int other = cur.a == vj ? cur.b : cur.a;
-            if (other != vj && split_before(ovid, B, j, other)) continue;  // taken with that variable
-          }
-          acc = chain_add<float, ChildVars<float, float>>(acc, cur, cv);
-        }
+        const uint64_t at = 2 * (((uint64_t)s * C + opart[j * B]) * a.pstride + k);
+        acc = iv_add(acc, Iv<float>{a.inc_parts[at], a.inc_parts[at + 1]});
       }
       chain_tail<float, ChildVars<float, float>>(a.prog, __ldg(a.inc_seg + 3 * s + 1), __ldg(a.inc_seg + 3 * s + 2),
                                                  cv, acc, v);
@@ -952,9 +1030,16 @@ cudaError_t launch_inc(const EvalArgs& a, int grid, int threads, cudaStream_t s)
   inc_common_kernel<<<grid, threads, 0, s>>>(a);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  const size_t smem = (size_t)(8 + 4) * a.max_slots * threads;
-  eval_children_inc_kernel<<<grid, threads, smem, s>>>(a);
+  inc_parts_kernel<<<grid, threads, 0, s>>>(a);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  eval_children_inc_kernel<<<grid, threads, inc_child_smem_bytes(a.max_slots, threads), s>>>(a);
   return cudaGetLastError();
+}
+
+size_t inc_child_smem_bytes(int max_slots, int threads)
+{
+  return (size_t)(8 + 4 + 4) * (size_t)max_slots * (size_t)threads;
 }
 
 cudaError_t launch_eval(const EvalArgs& a, int mode, bool fp32, int grid, int threads, cudaStream_t s)

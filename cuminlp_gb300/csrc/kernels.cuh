@@ -127,13 +127,17 @@ struct EvalArgs {
   const double* parent_lb;        // lazy form: the parents' certified FP64 lower bounds
   // lazy form, incremental children (Program::inc_*): per (segment, parent)
   // the chain sums of the terms that touch no split variable, (lo, hi)
-  // pairs at inc_common[2 * (s * pstride + k)]
+  // pairs at inc_common[2 * (s * pstride + k)]; per (segment, slot part,
+  // parent) the chain sums of the terms of one split variable at one of
+  // its parts, at inc_parts[2 * ((s * 2^log2C + u) * pstride + k)], where
+  // u counts the parts of slot 0, then of slot 1, ...
   int inc_segments;
   const uint64_t* n_parents_dev;
   const int32_t* inc_seg;
   const int32_t* inc_off;
   const int32_t* inc_pcs;
   float* inc_common;
+  float* inc_parts;
   // lane groups (null sched: one lane per box); see Program::sched
   const int32_t* sched;
   int g_max;

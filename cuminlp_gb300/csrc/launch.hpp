@@ -41,6 +41,8 @@ cudaError_t launch_sample(const SampleArgs& a, int grid, int threads, cudaStream
 // the lazy form's incremental FP32 children: the common chain sums per
 // (segment, parent), then every child (EvalArgs::inc_* set, prog = FP32)
 cudaError_t launch_inc(const EvalArgs& a, int grid, int threads, cudaStream_t s);
+// shared memory of the incremental child pass per block
+size_t inc_child_smem_bytes(int max_slots, int threads);
 // the lazy form's FP32 sample screen (SampleArgs::cbest out, prog = the
 // FP32 point program)
 cudaError_t launch_sample_screen(const SampleArgs& a, int grid, int threads, cudaStream_t s);

@@ -161,6 +161,7 @@ struct SolverBufs {
   const int32_t* inc_off;
   const int32_t* inc_pcs;
   float* inc_common;
+  float* inc_parts;
   uint32_t* list;        // certify list
   // compaction scratch
   uint32_t* block_counts;

@@ -1508,6 +1508,7 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
       ea.inc_off = b.inc_off;
       ea.inc_pcs = b.inc_pcs;
       ea.inc_common = b.inc_common;
+      ea.inc_parts = b.inc_parts;
       e = launch_inc(ea, eval_grid, kEvalThreads, s);
     } else {
       e = launch_eval(ea, 5, true, eval_grid, kEvalThreads, s);

@@ -2333,30 +2333,48 @@ static int split_before_o(const uint64_t* vids, int64_t j, uint64_t v)
   return 0;
 }
 
-/* the child box `cb` (FP64) of a parent with the given common sums and
- * split variables: FP32 verdict (1 unless a constraint is proven
- * violated), lb, ub */
-static int inc_child(const orc_problem* p, const double* cb, const float* common, const uint64_t* vids,
-                     int64_t count, iv32* x, double* lb, double* ub)
+/* the child box `cb` (FP64) of parent box `pb` with the given common sums
+ * and split variables: FP32 verdict (1 unless a constraint is proven
+ * violated), lb, ub.  Per segment: the common sum, then in slot order the
+ * part sum of each slot j -- from zero, in program order, the segment's
+ * terms reading slot j's variable and no variable of an earlier slot, with
+ * that variable over the child's part and every other variable over the
+ * parent's bounds (a variable an earlier slot already splits adds
+ * nothing) -- then the checks and the objective
+ * (csrc/eval_kernels.cu inc_parts_kernel, eval_children_inc_kernel).
+ * `x` and `xs` have room for n_vars intervals each. */
+static int inc_child(const orc_problem* p, const double* pb, const double* cb, const float* common,
+                     const uint64_t* vids, int64_t count, iv32* x, iv32* xs, double* lb, double* ub)
 {
   box32(p, cb, x);
+  const int64_t S = p->inc_segments;
+  /* part sums per (slot, segment) */
+  iv32* part = (iv32*)malloc(sizeof(iv32) * (size_t)(count * S > 0 ? count * S : 1));
+  for (int64_t j = 0; j < count; ++j) {
+    const uint64_t vj = vids[j];
+    const int repeated = split_before_o(vids, j, vj);
+    box32(p, pb, xs);
+    xs[vj] = x[vj];
+    for (int64_t s = 0; s < S; ++s) {
+      iv32 acc = {0.0f, 0.0f};
+      if (!repeated) {
+        for (int32_t q = p->inc_off[vj * S + s]; q < p->inc_off[vj * S + s + 1]; ++q) {
+          const struct orc_instr* in = &p->prog32[p->inc_pcs[q]];
+          if ((in->head & 7) == OP_TERM) {
+            uint64_t other = in->a == vj ? in->b : in->a;
+            if (other != vj && split_before_o(vids, j, other)) continue;
+          }
+          acc = chain_add_f(acc, in, xs);
+        }
+      }
+      part[j * S + s] = acc;
+    }
+  }
   int feas = 1;
   iv32 obj = {NAN, NAN};
-  const int64_t S = p->inc_segments;
   for (int64_t s = 0; s < S; ++s) {
     iv32 acc = {common[2 * s], common[2 * s + 1]};
-    for (int64_t j = 0; j < count; ++j) {
-      const uint64_t vj = vids[j];
-      if (split_before_o(vids, j, vj)) continue;
-      for (int32_t q = p->inc_off[vj * S + s]; q < p->inc_off[vj * S + s + 1]; ++q) {
-        const struct orc_instr* in = &p->prog32[p->inc_pcs[q]];
-        if ((in->head & 7) == OP_TERM) {
-          uint64_t other = in->a == vj ? in->b : in->a;
-          if (other != vj && split_before_o(vids, j, other)) continue;
-        }
-        acc = chain_add_f(acc, in, x);
-      }
-    }
+    for (int64_t j = 0; j < count; ++j) acc = iv_add_f(acc, part[j * S + s]);
     for (int32_t q = p->inc_seg[3 * s + 1]; q < p->inc_seg[3 * s + 2]; ++q) {
       const struct orc_instr* in = &p->prog32[q];
       const int mode = in->modes & 3;
@@ -2376,6 +2394,7 @@ static int inc_child(const orc_problem* p, const double* cb, const float* common
       }
     }
   }
+  free(part);
   *lb = (double)obj.lo;
   *ub = (double)obj.hi;
   return feas;
@@ -2405,13 +2424,15 @@ int orc_bound_inc32(const orc_problem* p, const double* box, const uint8_t* slot
   }
   const int64_t n = p->n_vars;
   iv32* x = (iv32*)malloc(sizeof(iv32) * (size_t)(n ? n : 1));
+  iv32* xs = (iv32*)malloc(sizeof(iv32) * (size_t)(n ? n : 1));
   float* common = (float*)malloc(sizeof(float) * 2 * (size_t)(p->inc_segments ? p->inc_segments : 1));
   double* cb = (double*)malloc(sizeof(double) * 2 * (size_t)(n ? n : 1));
   inc_common_one(p, box, var_ids, slot_count, x, common);
   for (uint64_t r = 0; r < n_regions; ++r) {
     child_box(box, n, &s, r, cb);
-    feasible[r] = (uint8_t)inc_child(p, cb, common, var_ids, slot_count, x, &obj_lb[r], &obj_ub[r]);
+    feasible[r] = (uint8_t)inc_child(p, box, cb, common, var_ids, slot_count, x, xs, &obj_lb[r], &obj_ub[r]);
   }
+  free(xs);
   free(x);
   free(common);
   free(cb);
@@ -2554,6 +2575,7 @@ static void batch_range(void* vc, int64_t g0, int64_t g1, int tid)
   double* x = (double*)malloc(sizeof(double) * (size_t)n);
   iv64* v64 = (iv64*)malloc(sizeof(iv64) * (size_t)p->n_nodes);
   iv32* v32 = (iv32*)malloc(sizeof(iv32) * (size_t)p->n_nodes);
+  iv32* xs = (iv32*)malloc(sizeof(iv32) * (size_t)(n ? n : 1));
   double* pv = (double*)malloc(sizeof(double) * (size_t)p->n_nodes);
   float* pf = (float*)malloc(sizeof(float) * (size_t)p->n_nodes);
   const int lazy = c->o->precision == CMN_PRECISION_FP32_LAZY;
@@ -2608,8 +2630,8 @@ static void batch_range(void* vc, int64_t g0, int64_t g1, int tid)
          * survivor within the band below the incumbent is certified in
          * FP64 at once (csrc/kernels.cuh certify_floor) */
         if (c->common) {
-          f = inc_child(p, cb, c->common + 2 * (size_t)p->inc_segments * k, pl->vids, pl->count,
-                        (iv32*)v32, &lb, &ub);
+          f = inc_child(p, parent, cb, c->common + 2 * (size_t)p->inc_segments * k, pl->vids, pl->count,
+                        (iv32*)v32, xs, &lb, &ub);
         } else {
           if (eval_all_f(p, cb, v32)) c->failed = 1;
           f = verdict_f(p, v32, &lb, &ub);
@@ -2681,6 +2703,7 @@ static void batch_range(void* vc, int64_t g0, int64_t g1, int tid)
   free(x);
   free(v64);
   free(v32);
+  free(xs);
   free(pv);
   free(pf);
 }

@@ -602,21 +602,33 @@ __device__ __forceinline__ Iv<T> term_value(const Instr& cur, int sub, const V& 
   return p;
 }
 
+// Where the interval interpreter reads instruction pc: the program in
+// global memory through the read-only cache, or a tile of it staged in
+// shared memory (instructions [base, base + tile length) at tile[0..]).
+struct GlobalCode {
+  const Instr* prog;
+  __device__ __forceinline__ Instr operator()(int pc) const { return load_instr(prog, pc); }
+};
+struct SharedCode {
+  const Instr* tile;
+  int base;
+  __device__ __forceinline__ Instr operator()(int pc) const { return tile[pc - base]; }
+};
+
 // Interval interpretation of instructions [pc0, pc1) for this thread's box,
-// starting from a zero accumulator: variables from `vars` (anything with
+// continuing the accumulator `acc`: variables from `vars` (anything with
 // var(v) -> Iv<T>), program slots in `t`.  Checks fold into `out` with AND /
 // OR, so ranges may run in any order.
-template <typename T, typename V>
-__device__ __forceinline__ void interval_range(const Instr* __restrict__ prog, int pc0, int pc1, const V& vars,
-                                               const Tile<T>& t, Verdict<T>& out)
+template <typename T, typename V, typename Code>
+__device__ __forceinline__ void interval_range_from(const Code& code_at, int pc0, int pc1, const V& vars,
+                                                    const Tile<T>& t, Verdict<T>& out, Iv<T>& acc)
 {
-  Iv<T> acc = {T(0), T(0)};
   int pc = pc0;
   while (pc < pc1) {
     // two terms in a row: both products before the first add, so the two
     // interval products (and their variable loads) overlap
     if (pc + 2 <= pc1) {
-      const Instr c0 = load_instr(prog, pc), c1 = load_instr(prog, pc + 1);
+      const Instr c0 = code_at(pc), c1 = code_at(pc + 1);
       if ((c0.head & 7) == kOpTerm && (c1.head & 7) == kOpTerm) {
         const int s0 = c0.head >> 3, s1 = c1.head >> 3;
         const Iv<T> p0 = term_value<T, V>(c0, s0, vars);
@@ -627,7 +639,7 @@ __device__ __forceinline__ void interval_range(const Instr* __restrict__ prog, i
         continue;
       }
     }
-    const Instr cur = load_instr(prog, pc);
+    const Instr cur = code_at(pc);
     ++pc;
     const int code = cur.head & 7;
     const int sub = cur.head >> 3;
@@ -676,6 +688,15 @@ __device__ __forceinline__ void interval_range(const Instr* __restrict__ prog, i
         break;
     }
   }
+}
+
+// The same from a zero accumulator, reading the program in global memory.
+template <typename T, typename V>
+__device__ __forceinline__ void interval_range(const Instr* __restrict__ prog, int pc0, int pc1, const V& vars,
+                                               const Tile<T>& t, Verdict<T>& out)
+{
+  Iv<T> acc = {T(0), T(0)};
+  interval_range_from<T, V, GlobalCode>(GlobalCode{prog}, pc0, pc1, vars, t, out, acc);
 }
 
 template <typename T, typename V>

@@ -146,6 +146,10 @@ struct EvalArgs {
   double* out_lb;
   double* out_ub;
   uint8_t* out_flag;  // role/raw: feasible; solver: ChildState
+  uint32_t* error;    // solver: set when a staged program tile never arrived
+  // byte offset in dynamic shared memory of the staged program tiles (FP64
+  // passes with one lane per box); 0: the program is read from global memory
+  size_t stage_at;
   // aggregate bounder: child c = r / agg_m folds into agg_keys[c] (min lb
   // key) and agg_keys[agg_k + c] (max ub key)
   unsigned long long* agg_keys;

@@ -1441,6 +1441,7 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
     pa.sched = b.sched;
     pa.g_max = cfg.g_max;
     pa.capacity = cfg.eval_capacity;
+    pa.error = &b.dev->error;
     e = launch_eval(pa, 0, false, eval_grid, kEvalThreads, side.stream);
     if (e != cudaSuccess) return e;
     mark(marks, 6, side.stream);
@@ -1473,6 +1474,7 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
   ea.done = &b.dev->done;
   ea.out_lb = b.clb;
   ea.out_flag = b.cstate;
+  ea.error = &b.dev->error;
   ea.prog_len = cfg.prog_len;
   ea.sched = b.sched;
   ea.g_max = cfg.g_max;

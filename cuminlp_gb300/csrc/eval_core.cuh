@@ -602,6 +602,53 @@ __device__ __forceinline__ Iv<T> term_value(const Instr& cur, int sub, const V& 
   return p;
 }
 
+// The lazy form's FP64 verdict folds a term's coefficient into the chain
+// add: acc (+|-) c * p with __fma_rd / __fma_ru, one rounding per bound
+// instead of two (the product by c and the add).  The coefficient's sign
+// picks the endpoint of p.  Sound, and tighter; not the reference's order
+// of operations, so only the lazy form's own certification uses it.
+template <typename T, bool kFused>
+__device__ __forceinline__ bool fused_term(int sub)
+{
+  return kFused && sizeof(T) == 8 && (sub & kTermHasC) && !(sub & kTermInit);
+}
+
+// x_a * x_b, sqr(x_a) or x_a of a TERM instruction, before its coefficient.
+template <typename T, typename V>
+__device__ __forceinline__ Iv<T> term_product(const Instr& cur, int sub, const V& vars)
+{
+  const int pk = sub & kTermPMask;
+  if (pk == kTermProd) return iv_mul<T, (CMN_FP64_EMU & 32) != 0>(vars.var(cur.a), vars.var(cur.b));
+  if (pk == kTermSqr) return iv_sqr<T, (CMN_FP64_EMU & 32) != 0>(vars.var(cur.a));
+  return vars.var(cur.a);
+}
+
+__device__ __forceinline__ Iv<double> fma_into(Iv<double> acc, double c, Iv<double> p, bool sub)
+{
+  const double cc = sub ? -c : c;
+  const bool pos = cc >= 0.0;
+  return {__fma_rd(cc, pos ? p.lo : p.hi, acc.lo), __fma_ru(cc, pos ? p.hi : p.lo, acc.hi)};
+}
+
+// A TERM's contribution: its value (term_value) added into / subtracted from
+// / starting the chain, or, fused, its product folded in with fma_into.
+template <typename T, typename V, bool kFused>
+__device__ __forceinline__ Iv<T> term_operand(const Instr& cur, int sub, const V& vars)
+{
+  if (fused_term<T, kFused>(sub)) return term_product<T, V>(cur, sub, vars);
+  return term_value<T, V>(cur, sub, vars);
+}
+
+template <typename T, bool kFused>
+__device__ __forceinline__ Iv<T> term_apply(Iv<T> acc, const Instr& cur, int sub, Iv<T> p)
+{
+  if constexpr (kFused && sizeof(T) == 8) {
+    if (fused_term<T, kFused>(sub)) return fma_into(acc, cur.c, p, (sub & kTermSub) != 0);
+  }
+  if (sub & kTermInit) return p;
+  return (sub & kTermSub) ? iv_sub(acc, p) : iv_add(acc, p);
+}
+
 // Where the interval interpreter reads instruction pc: the program in
 // global memory through the read-only cache, or a tile of it staged in
 // shared memory (instructions [base, base + tile length) at tile[0..]).
@@ -619,7 +666,7 @@ struct SharedCode {
 // continuing the accumulator `acc`: variables from `vars` (anything with
 // var(v) -> Iv<T>), program slots in `t`.  Checks fold into `out` with AND /
 // OR, so ranges may run in any order.
-template <typename T, typename V, typename Code>
+template <typename T, typename V, typename Code, bool kFused = false>
 __device__ __forceinline__ void interval_range_from(const Code& code_at, int pc0, int pc1, const V& vars,
                                                     const Tile<T>& t, Verdict<T>& out, Iv<T>& acc)
 {
@@ -631,10 +678,10 @@ __device__ __forceinline__ void interval_range_from(const Code& code_at, int pc0
       const Instr c0 = code_at(pc), c1 = code_at(pc + 1);
       if ((c0.head & 7) == kOpTerm && (c1.head & 7) == kOpTerm) {
         const int s0 = c0.head >> 3, s1 = c1.head >> 3;
-        const Iv<T> p0 = term_value<T, V>(c0, s0, vars);
-        const Iv<T> p1 = term_value<T, V>(c1, s1, vars);
-        acc = (s0 & kTermInit) ? p0 : ((s0 & kTermSub) ? iv_sub(acc, p0) : iv_add(acc, p0));
-        acc = (s1 & kTermInit) ? p1 : ((s1 & kTermSub) ? iv_sub(acc, p1) : iv_add(acc, p1));
+        const Iv<T> p0 = term_operand<T, V, kFused>(c0, s0, vars);
+        const Iv<T> p1 = term_operand<T, V, kFused>(c1, s1, vars);
+        acc = term_apply<T, kFused>(acc, c0, s0, p0);
+        acc = term_apply<T, kFused>(acc, c1, s1, p1);
         pc += 2;
         continue;
       }
@@ -645,10 +692,7 @@ __device__ __forceinline__ void interval_range_from(const Code& code_at, int pc0
     const int sub = cur.head >> 3;
     switch (code) {
       case kOpTerm: {
-        const Iv<T> p = term_value<T, V>(cur, sub, vars);
-        if (sub & kTermInit) acc = p;
-        else if (sub & kTermSub) acc = iv_sub(acc, p);
-        else acc = iv_add(acc, p);
+        acc = term_apply<T, kFused>(acc, cur, sub, term_operand<T, V, kFused>(cur, sub, vars));
         break;
       }
       case kOpGeneric: {
@@ -691,19 +735,19 @@ __device__ __forceinline__ void interval_range_from(const Code& code_at, int pc0
 }
 
 // The same from a zero accumulator, reading the program in global memory.
-template <typename T, typename V>
+template <typename T, typename V, bool kFused = false>
 __device__ __forceinline__ void interval_range(const Instr* __restrict__ prog, int pc0, int pc1, const V& vars,
                                                const Tile<T>& t, Verdict<T>& out)
 {
   Iv<T> acc = {T(0), T(0)};
-  interval_range_from<T, V, GlobalCode>(GlobalCode{prog}, pc0, pc1, vars, t, out, acc);
+  interval_range_from<T, V, GlobalCode, kFused>(GlobalCode{prog}, pc0, pc1, vars, t, out, acc);
 }
 
-template <typename T, typename V>
+template <typename T, typename V, bool kFused = false>
 __device__ Verdict<T> run_interval(const Instr* __restrict__ prog, int len, const V& vars, const Tile<T>& t)
 {
   Verdict<T> out = verdict_init<T>();
-  interval_range<T, V>(prog, 0, len, vars, t, out);
+  interval_range<T, V, kFused>(prog, 0, len, vars, t, out);
   return out;
 }
 
@@ -772,14 +816,14 @@ __device__ __forceinline__ LaneSegs lane_segments(const int32_t* __restrict__ sc
 // accumulator reset).  Every instruction performs the same roundings as in
 // the whole-program run, so the group's combined verdict (group_verdict) is
 // bit-identical to run_interval's.
-template <typename T, typename V>
+template <typename T, typename V, bool kFused = false>
 __device__ Verdict<T> run_interval_lane(const Instr* __restrict__ prog, const int32_t* __restrict__ sched, int l,
                                         int lane, const V& vars, const Tile<T>& t)
 {
   Verdict<T> out = verdict_init<T>();
   const LaneSegs ls = lane_segments(sched, l, lane);
   for (int j = ls.b; j < ls.e; ++j)
-    interval_range<T, V>(prog, __ldg(ls.pairs + 2 * j), __ldg(ls.pairs + 2 * j + 1), vars, t, out);
+    interval_range<T, V, kFused>(prog, __ldg(ls.pairs + 2 * j), __ldg(ls.pairs + 2 * j + 1), vars, t, out);
   return out;
 }
 

@@ -230,7 +230,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
 // kMode 0 or 1, one lane per box, program tiles staged in shared memory.
 // The block's trip count over boxes is uniform, so every thread reaches the
 // barriers; a thread without a (live) box only steps through the tiles.
-template <typename T, int kMode, typename S>
+template <typename T, int kMode, typename S, bool kFused = false>
 __device__ void eval_children_staged(const EvalArgs& a, const S* plo, const S* phi, uint64_t total, double gub,
                                      const Tile<T>& t, T* olo, T* ohi, int32_t* ovid)
 {
@@ -298,7 +298,7 @@ __device__ void eval_children_staged(const EvalArgs& a, const S* plo, const S* p
       if (threadIdx.x == 0 && tile + 1 < ntiles) issue(tile + 1, seq + 1);
       const int pc0 = tile * kStageTile, pc1 = min(len, pc0 + kStageTile);
       if (live)
-        interval_range_from<T, ChildVars<T, S>, SharedCode>(SharedCode{tiles[seq & 1], pc0}, pc0, pc1, cv, t, out,
+        interval_range_from<T, ChildVars<T, S>, SharedCode, kFused>(SharedCode{tiles[seq & 1], pc0}, pc0, pc1, cv, t, out,
                                                              acc);
       __syncthreads();
     }
@@ -309,7 +309,7 @@ __device__ void eval_children_staged(const EvalArgs& a, const S* plo, const S* p
 // Groups of 2^lg consecutive lanes share one child: each lane runs its
 // segments of the program and the group combines the verdicts.  The loop
 // bound is per block, so every lane of a warp reaches the shuffles.
-template <typename T, int kMode, typename S>
+template <typename T, int kMode, typename S, bool kFused = false>
 __device__ void eval_children_grouped(const EvalArgs& a, const S* plo, const S* phi, uint64_t total, double gub,
                                       bool pass_through, int lg, const Tile<T>& t, T* olo, T* ohi, int32_t* ovid)
 {
@@ -348,9 +348,9 @@ __device__ void eval_children_grouped(const EvalArgs& a, const S* plo, const S* 
         if (lane == 0) a.out_flag[g] = kChildDuplicate;
         live = false;
       } else if (lg > 0) {
-        v = run_interval_lane<T, ChildVars<T, S>>(a.prog, a.sched, lg, lane, cv, t);
+        v = run_interval_lane<T, ChildVars<T, S>, kFused>(a.prog, a.sched, lg, lane, cv, t);
       } else {  // one lane per box (the aggregate fold's loop): the whole program
-        v = run_interval<T, ChildVars<T, S>>(a.prog, a.prog_len, cv, t);
+        v = run_interval<T, ChildVars<T, S>, kFused>(a.prog, a.prog_len, cv, t);
       }
     }
     v = group_verdict<T>(v, G);
@@ -369,7 +369,7 @@ __device__ void eval_children_grouped(const EvalArgs& a, const S* plo, const S* 
 // kMode 4: aggregate bounder fold
 // kMode 5: solver lazy form, FP32 -> out_lb = max(FP32 bound, parent's
 //          certified bound), out_flag = ChildState
-template <typename T, int kMode, typename S, bool kStaged = false>
+template <typename T, int kMode, typename S, bool kStaged = false, bool kFused = false>
 __device__ __forceinline__ void eval_children(const EvalArgs& a, const S* plo, const S* phi)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -398,11 +398,11 @@ __device__ __forceinline__ void eval_children(const EvalArgs& a, const S* plo, c
 
   const int lg = a.sched != nullptr ? lanes_per_box(total, a.capacity, a.g_max) : 0;
   if (lg > 0 || kMode == 4) {  // the aggregate fold needs whole warps: the grouped loop, even at one lane
-    eval_children_grouped<T, kMode, S>(a, plo, phi, total, gub, pass_through, lg, t, olo, ohi, ovid);
+    eval_children_grouped<T, kMode, S, kFused>(a, plo, phi, total, gub, pass_through, lg, t, olo, ohi, ovid);
     return;
   }
   if constexpr (kStaged) {
-    eval_children_staged<T, kMode, S>(a, plo, phi, total, gub, t, olo, ohi, ovid);
+    eval_children_staged<T, kMode, S, kFused>(a, plo, phi, total, gub, t, olo, ohi, ovid);
     return;
   }
   for (uint64_t idx = (uint64_t)blockIdx.x * B + threadIdx.x; idx < total; idx += (uint64_t)gridDim.x * B) {
@@ -430,7 +430,7 @@ __device__ __forceinline__ void eval_children(const EvalArgs& a, const S* plo, c
       a.out_flag[g] = kChildDuplicate;
       continue;
     }
-    const Verdict<T> v = run_interval<T, ChildVars<T, S>>(a.prog, a.prog_len, cv, t);
+    const Verdict<T> v = run_interval<T, ChildVars<T, S>, kFused>(a.prog, a.prog_len, cv, t);
     write_verdict<T, kMode>(a, g, k, v, gub);
   }
 }
@@ -624,7 +624,7 @@ __global__ void __launch_bounds__(kEvalThreads, CMN_EVAL_MIN_BLOCKS) eval_childr
   }
 }
 
-template <typename T, int kMode>
+template <typename T, int kMode, bool kFused = false>
 __global__ void __launch_bounds__(kEvalThreads, CMN_EVAL_MIN_BLOCKS) eval_children_kernel(const EvalArgs a)
 {
   if constexpr (sizeof(T) == 4) {
@@ -633,15 +633,15 @@ __global__ void __launch_bounds__(kEvalThreads, CMN_EVAL_MIN_BLOCKS) eval_childr
       return;
     }
   }
-  eval_children<T, kMode, double>(a, a.plo, a.phi);
+  eval_children<T, kMode, double, false, kFused>(a, a.plo, a.phi);
 }
 
 // The FP64 one-lane passes with their program staged in shared memory
 // (kMode 0 and 1; EvalArgs::stage_at set by the launcher).
-template <int kMode>
+template <int kMode, bool kFused = false>
 __global__ void __launch_bounds__(kEvalThreads, CMN_EVAL_MIN_BLOCKS) eval_children_staged_kernel(const EvalArgs a)
 {
-  eval_children<double, kMode, double, true>(a, a.plo, a.phi);
+  eval_children<double, kMode, double, true, kFused>(a, a.plo, a.phi);
 }
 
 __device__ __forceinline__ void warp_min_cand(Cand& c)
@@ -1142,6 +1142,8 @@ cudaError_t set_eval_kernel_attributes(int max_smem)
   cudaError_t e = allow_dynamic_smem(eval_children_kernel<double, 0>, max_smem);
   if (e == cudaSuccess) e = allow_dynamic_smem(eval_children_staged_kernel<0>, max_smem);
   if (e == cudaSuccess) e = allow_dynamic_smem(eval_children_staged_kernel<1>, max_smem);
+  if (e == cudaSuccess) e = allow_dynamic_smem(eval_children_staged_kernel<0, true>, max_smem);
+  if (e == cudaSuccess) e = allow_dynamic_smem(eval_children_kernel<double, 0, true>, max_smem);
   if (e == cudaSuccess) e = allow_dynamic_smem(eval_children_kernel<double, 1>, max_smem);
   if (e == cudaSuccess) e = allow_dynamic_smem(eval_children_kernel<double, 3>, max_smem);
   if (e == cudaSuccess) e = allow_dynamic_smem(eval_children_kernel<double, 4>, max_smem);
@@ -1177,7 +1179,7 @@ int sample_kernel_occupancy(size_t smem, int threads)
   return e == cudaSuccess ? blocks : 1;
 }
 
-template <typename T, int kMode>
+template <typename T, int kMode, bool kFused = false>
 static cudaError_t launch_eval_t(const EvalArgs& a, int grid, int threads, cudaStream_t s)
 {
   size_t smem = eval_smem_bytes(a.n_slots, a.pinfo != nullptr ? a.max_slots : 0, sizeof(T) == 4, threads);
@@ -1193,11 +1195,11 @@ static cudaError_t launch_eval_t(const EvalArgs& a, int grid, int threads, cudaS
   }
   if constexpr (sizeof(T) == 8 && (kMode == 0 || kMode == 1)) {
     if (b.stage_at != 0) {
-      eval_children_staged_kernel<kMode><<<grid, threads, smem, s>>>(b);
+      eval_children_staged_kernel<kMode, kFused><<<grid, threads, smem, s>>>(b);
       return cudaGetLastError();
     }
   }
-  eval_children_kernel<T, kMode><<<grid, threads, smem, s>>>(b);
+  eval_children_kernel<T, kMode, kFused><<<grid, threads, smem, s>>>(b);
   return cudaGetLastError();
 }
 
@@ -1226,6 +1228,7 @@ cudaError_t launch_eval(const EvalArgs& a, int mode, bool fp32, int grid, int th
     return launch_eval_t<float, 2>(a, grid, threads, s);
   }
   if (mode == 0) return launch_eval_t<double, 0>(a, grid, threads, s);
+  if (mode == 6) return launch_eval_t<double, 0, true>(a, grid, threads, s);
   if (mode == 1) return launch_eval_t<double, 1>(a, grid, threads, s);
   if (mode == 4) return launch_eval_t<double, 4>(a, grid, threads, s);
   return launch_eval_t<double, 3>(a, grid, threads, s);

@@ -35,7 +35,9 @@ int sample_screen_lg_min(int n_vars, int n_slots, bool has_sched, int threads);
 // mode 0: role / raw boxes; 1: solver FP64; 2: solver FP32 screen (fp32
 // must be true); 3: solver FP64 certify over EvalArgs::list; 4: aggregate
 // bounder (FP64, per-child fold into EvalArgs::agg_keys); 5: solver lazy
-// form, FP32 children bounded by the parents' certified bounds (fp32 true)
+// form, FP32 children bounded by the parents' certified bounds (fp32 true);
+// 6: the lazy form's FP64 verdict of the staged parents (mode 0's outputs,
+// each term's coefficient and chain add fused into __fma_rd / __fma_ru)
 cudaError_t launch_eval(const EvalArgs& a, int mode, bool fp32, int grid, int threads, cudaStream_t s);
 cudaError_t launch_sample(const SampleArgs& a, int grid, int threads, cudaStream_t s);
 // the lazy form's incremental FP32 children: the common chain sums per

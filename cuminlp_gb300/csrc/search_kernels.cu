@@ -1442,7 +1442,7 @@ cudaError_t solver_iteration(const SolverCfg& cfg, const SolverBufs& b, int eval
     pa.g_max = cfg.g_max;
     pa.capacity = cfg.eval_capacity;
     pa.error = &b.dev->error;
-    e = launch_eval(pa, 0, false, eval_grid, kEvalThreads, side.stream);
+    e = launch_eval(pa, 6, false, eval_grid, kEvalThreads, side.stream);
     if (e != cudaSuccess) return e;
     mark(marks, 6, side.stream);
     e = cudaEventRecord(side.join, side.stream);

@@ -51,6 +51,7 @@ _SIG = {
     "orc_bound": (I32, [P, P, P, P, P, I64, U64, P, P, I32]),
     "orc_bound_hw": (I32, [P, P, P, P, P, I64, U64, P, P, I32]),
     "orc_set_program32": (I32, [P, P, I64]),
+    "orc_set_program64": (I32, [P, P, I64]),
     "orc_bound_inc32": (I32, [P, P, P, P, P, I64, U64, P, P, P]),
     "orc_aggregate_bound": (I32, [P, P, P, P, P, I64, U64, U64, P, P, P, I32]),
     "orc_sample": (I32, [P, P, P, P, P, I64, U64, U64, U64, C.POINTER(I32), C.POINTER(D), C.POINTER(I64), P, I32]),
@@ -166,6 +167,13 @@ class OracleProblem:
         does.  True when the program has the sum-chain shape for that."""
         code = np.ascontiguousarray(code, dtype=np.uint8)
         return bool(lib().orc_set_program32(self.h, A.ptr(code), code.size // 16))
+
+    def set_program64(self, code: np.ndarray) -> bool:
+        """The library's compiled FP64 program (DeviceProblem.program(0)):
+        the lazy form's verdict of each expanded box runs it with fused
+        terms, as the device does."""
+        code = np.ascontiguousarray(code, dtype=np.uint8)
+        return bool(lib().orc_set_program64(self.h, A.ptr(code), code.size // 16))
 
     def bound_inc32(self, box, kinds, var_ids, widths, n_regions):
         """The lazy form's incremental FP32 bounds of one parent's regions

@@ -566,6 +566,9 @@ struct orc_problem {
   int inc_ok;
   int64_t prog_len;
   struct orc_instr* prog32;
+  struct orc_instr* prog64; /* the FP64 program: the lazy form's fused verdict */
+  int64_t prog64_len;
+  int64_t n_prog_slots;
   int64_t inc_segments;
   int32_t* inc_seg; /* 3 per segment: chain [b, t), checks/objective [t, e) */
   int32_t* inc_off; /* n_vars * segments + 1 */
@@ -585,6 +588,7 @@ void orc_problem_destroy(orc_problem* p)
   free(p->clo32);
   free(p->chi32);
   free(p->prog32);
+  free(p->prog64);
   free(p->inc_seg);
   free(p->inc_off);
   free(p->inc_pcs);
@@ -2161,14 +2165,125 @@ struct orc_instr {
   } u;
 };
 
-enum { OP_GENERIC = 0, OP_TERM = 1, OP_LOADACC = 3, OP_CHECK = 5, OP_OBJECTIVE = 6 };
-enum { MODE_VAR = 1, MODE_ACC = 2 };
+enum { OP_GENERIC = 0, OP_TERM = 1, OP_STOREACC = 2, OP_LOADACC = 3, OP_CONSTTOSLOT = 4, OP_CHECK = 5,
+       OP_OBJECTIVE = 6 };
+enum { MODE_SLOT = 0, MODE_VAR = 1, MODE_ACC = 2, MODE_CONST = 3 };
 enum { T_INIT = 1, T_SUB = 2, T_HASC = 4, T_SQR = 8, T_VAR = 16, T_PMASK = 24 };
 
 /* Segments and per-(variable, segment) chain lists, derived here from the
  * instruction stream independently of the library's own tables: a
  * segment is a sum chain (a LoadAcc or an initialising TERM, then TERMs)
  * followed by the checks and objective that read it. */
+int orc_set_program64(orc_problem* p, const void* instrs, int64_t len)
+{
+  free(p->prog64);
+  p->prog64 = NULL;
+  p->prog64_len = 0;
+  p->n_prog_slots = 0;
+  if (len <= 0) return 0;
+  p->prog64 = (struct orc_instr*)malloc(sizeof(struct orc_instr) * (size_t)len);
+  memcpy(p->prog64, instrs, sizeof(struct orc_instr) * (size_t)len);
+  p->prog64_len = len;
+  for (int64_t pc = 0; pc < len; ++pc) {
+    const struct orc_instr* in = &p->prog64[pc];
+    const int op = in->head & 7;
+    if (op == OP_GENERIC || op == OP_STOREACC || op == OP_CONSTTOSLOT)
+      if ((int64_t)in->dst + 1 > p->n_prog_slots) p->n_prog_slots = (int64_t)in->dst + 1;
+  }
+  return 1;
+}
+
+static iv64 prog_fetch64(const struct orc_instr* in, int mode, int idx, const double* box, const iv64* slots,
+                         iv64 acc)
+{
+  iv64 v;
+  switch (mode) {
+    case MODE_SLOT: return slots[idx];
+    case MODE_VAR:
+      v.lo = box[2 * idx];
+      v.hi = box[2 * idx + 1];
+      return v;
+    case MODE_ACC: return acc;
+    default:
+      v.lo = in->u.c;
+      v.hi = in->u.c;
+      return v;
+  }
+}
+
+/* The lazy form's FP64 verdict of box `box` (lo, hi pairs) from the FP64
+ * program (orc_set_program64), restating csrc/eval_core.cuh interval_range
+ * with fused terms: a TERM with a coefficient c that adds into its chain
+ * folds c and the add into one directed FMA per bound (the coefficient's
+ * sign picks the product's endpoint), every other instruction as the
+ * program's unfused operations.  Runs under FE_DOWNWARD with the _h
+ * operators (round-up as negated round-down, fma included).  Returns the
+ * reference predicate (1 feasible), or -1 for an operator without an
+ * interval form; *lb, *ub the objective's enclosure.  `slots` has room for
+ * the program's slots. */
+static int verdict_fused64(const orc_problem* p, const double* box, iv64* slots, double* lb, double* ub)
+{
+  iv64 acc = {0.0, 0.0};
+  iv64 obj = {NAN, NAN};
+  int feas = 1, rc = 0;
+  fesetround(FE_DOWNWARD);
+  for (int64_t pc = 0; pc < p->prog64_len && rc == 0; ++pc) {
+    const struct orc_instr* in = &p->prog64[pc];
+    const int op = in->head & 7, sub = in->head >> 3;
+    switch (op) {
+      case OP_TERM: {
+        iv64 xa = prog_fetch64(in, MODE_VAR, in->a, box, slots, acc);
+        iv64 xb = prog_fetch64(in, MODE_VAR, in->b, box, slots, acc);
+        const int pk = sub & T_PMASK;
+        iv64 prod = pk == T_SQR ? iv_sqr_h(xa) : (pk == T_VAR ? xa : iv_mul_h(xa, xb));
+        if ((sub & T_HASC) && !(sub & T_INIT)) {
+          const double cc = (sub & T_SUB) ? -in->u.c : in->u.c;
+          const int pos = cc >= 0.0;
+          acc.lo = fma(cc, pos ? prod.lo : prod.hi, acc.lo);
+          acc.hi = -fma(-cc, pos ? prod.hi : prod.lo, -acc.hi);
+        } else {
+          iv64 t = prod;
+          if (sub & T_HASC) {
+            iv64 c = {in->u.c, in->u.c};
+            t = iv_mul_h(c, prod);
+          }
+          acc = (sub & T_INIT) ? t : ((sub & T_SUB) ? iv_sub_h(acc, t) : iv_add_h(acc, t));
+        }
+        break;
+      }
+      case OP_GENERIC: {
+        if (!op_supported_interval(sub)) {
+          rc = -1;
+          break;
+        }
+        iv64 a = prog_fetch64(in, in->modes & 3, in->a, box, slots, acc);
+        iv64 b = prog_fetch64(in, (in->modes >> 2) & 3, in->b, box, slots, acc);
+        slots[in->dst] = apply_hw(sub, a, b, (int)(int16_t)in->b);
+        break;
+      }
+      case OP_STOREACC: slots[in->dst] = acc; break;
+      case OP_LOADACC: acc = prog_fetch64(in, in->modes & 3, in->a, box, slots, acc); break;
+      case OP_CONSTTOSLOT:
+        slots[in->dst].lo = in->u.c;
+        slots[in->dst].hi = in->u.c;
+        break;
+      case OP_CHECK: {
+        iv64 v = prog_fetch64(in, in->modes & 3, in->a, box, slots, acc);
+        const double rhs = in->u.c;
+        if (sub == 0) feas = feas && (v.lo <= rhs);
+        else feas = feas && (v.lo <= rhs && rhs <= v.hi);
+        break;
+      }
+      case OP_OBJECTIVE: obj = prog_fetch64(in, in->modes & 3, in->a, box, slots, acc); break;
+      default: break;
+    }
+  }
+  fesetround(FE_TONEAREST);
+  *lb = obj.lo;
+  *ub = obj.hi;
+  return rc ? rc : feas;
+}
+
 int orc_set_program32(orc_problem* p, const void* instrs, int64_t len)
 {
   free(p->prog32);
@@ -2553,13 +2668,14 @@ static void certify_range(void* vc, int64_t k0, int64_t k1, int tid)
   (void)tid;
   certify_ctx* c = (certify_ctx*)vc;
   const int64_t n = c->p->n_vars;
-  iv64* v64 = (iv64*)malloc(sizeof(iv64) * (size_t)c->p->n_nodes);
+  iv64* slots = (iv64*)malloc(sizeof(iv64) * (size_t)(c->p->n_prog_slots > 0 ? c->p->n_prog_slots : 1));
   for (int64_t k = k0; k < k1; ++k) {
     double ub;
-    if (eval_all_d(c->p, c->pbox + 2 * (size_t)n * (size_t)k, v64)) c->failed = 1;
-    c->feas[k] = verdict_d(c->p, v64, &c->lb[k], &ub);
+    const int f = verdict_fused64(c->p, c->pbox + 2 * (size_t)n * (size_t)k, slots, &c->lb[k], &ub);
+    if (f < 0) c->failed = 1;
+    c->feas[k] = f > 0;
   }
-  free(v64);
+  free(slots);
 }
 
 /* One child slot: interval bound (FP64, or FP32 screen + FP64 certify, or
@@ -2728,6 +2844,10 @@ static int batched_run(const orc_problem* p, const cmn_solve_options* o,
   const uint64_t C = (uint64_t)1 << o->bisection_budget;
   const uint64_t S = o->sample_points;
   uint64_t cap = o->frontier_cap ? o->frontier_cap : (1ull << 20);
+  if (o->precision == CMN_PRECISION_FP32_LAZY && !p->prog64) {
+    set_err("the lazy form's verdict needs the FP64 program (orc_set_program64)");
+    return -1;
+  }
   double* x = (double*)malloc(sizeof(double) * (size_t)n);
   int rc = 0;
   uint64_t run_iters = 0;

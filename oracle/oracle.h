@@ -93,6 +93,10 @@ float orc_sample_discrete_f32(float lb, float ub, uint64_t vid, uint64_t i,
  * shape they need, else 0 (the lazy form then bounds children node by
  * node). */
 int orc_set_program32(orc_problem* p, const void* instrs, int64_t len);
+/* The library's compiled FP64 program (cmn_problem_program precision 0):
+ * the lazy form's verdict of each expanded box runs it with fused terms,
+ * as the device does.  Required for the lazy form. */
+int orc_set_program64(orc_problem* p, const void* instrs, int64_t len);
 
 /* The lazy form's incremental FP32 bound of every region of one parent
  * box, after orc_set_program32. */

@@ -47,9 +47,11 @@ def compare(p, iterations, room=1 << 20, **opts):
     op = O.OracleProblem(p)
     if opts.get("precision") == "lazy":
         # the lazy form bounds children incrementally over the compiled
-        # program when it is a set of sum chains; the oracle restates that
-        # from the same program
+        # program when it is a set of sum chains, and certifies each expanded
+        # box with the FP64 program's fused terms; the oracle restates both
+        # from the same programs
         op.set_program32(dp.program(1))
+        op.set_program64(dp.program(0))
     obox, olb, odepth, o = op.batched_frontier(iterations, room=room, **opts)
     assert len(glb) == len(olb)
     assert bits_equal(glb, olb)

@@ -60,11 +60,13 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 EVAL_DRAM_BYTES_PER_BOX = (43186688 + 34048) / 1048576  # ncu, eval_children_kernel<double, 1>, config 2
-# ncu, eval_children_inc_kernel and sample_screen_kernel, config 3 at 2^14
-# parents x 2^4 children (profiles/lazy_form_kernels_config3.md): DRAM
-# bytes per child box / per sample point, scaled by the units of a launch
-INC32_DRAM_BYTES_PER_BOX = 15380736 / 262144
-SCREEN32_DRAM_BYTES_PER_POINT = 20115712 / 262144
+# ncu, config 3 at 2^14 parents x 2^4 children in a steady iteration
+# (profiles/lazy_form_kernels_config3.md): DRAM bytes per child box of the
+# FP32 bound (inc_common + inc_parts + eval_children_inc, reads and writes)
+# and per sample point of sample_screen_kernel, scaled by the units of a
+# launch
+INC32_DRAM_BYTES_PER_BOX = (10849280 + 11762688 + 2355968 + 59540224 + 154368) / 262144
+SCREEN32_DRAM_BYTES_PER_POINT = 20065792 / 262144
 # time-to-gap on config 1: the cluster of boxes within 1e-6 of the optimum
 # holds tens of millions of boxes at n=4, so the frontier is capped at 2^25;
 # 2^21 parents x 2^2 children per iteration timed best (swept over

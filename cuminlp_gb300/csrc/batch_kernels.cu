@@ -584,7 +584,7 @@ __global__ void __launch_bounds__(kEvalThreads) batch_sample_kernel(const BatchC
         int li = 0;
         while (li < lg && (2 << li) <= d->g_max) ++li;
         if (d->sched == nullptr || li == 0) {
-          if (lane == 0) pv = run_point(d->prog64, d->prog_len, t);
+          if (lane == 0) pv = run_point_ordered(d->prog64, d->prog_len, d->sched, t);
         } else if (lane < (1 << li)) {
           pv = run_point_lane(d->prog64, d->sched, li, lane, t);
         }

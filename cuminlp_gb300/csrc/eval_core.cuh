@@ -1010,6 +1010,12 @@ __device__ inline PointVerdict run_point(const Instr* __restrict__ prog, int len
   return out;
 }
 
+// The whole point program on one lane: with a lane schedule, its level-0
+// segment order (the objective's segments last, so an infeasible point
+// stops early), else program order.
+__device__ inline PointVerdict run_point_ordered(const Instr* __restrict__ prog, int len,
+                                                 const int32_t* __restrict__ sched, const Tile<double>& t);
+
 // One lane of a group sharing a point (see run_interval_lane).
 __device__ inline PointVerdict run_point_lane(const Instr* __restrict__ prog, const int32_t* __restrict__ sched, int l,
                                               int lane, const Tile<double>& t)
@@ -1022,6 +1028,12 @@ __device__ inline PointVerdict run_point_lane(const Instr* __restrict__ prog, co
   for (int j = ls.b; j < ls.e && out.feasible; ++j)
     point_range(prog, __ldg(ls.pairs + 2 * j), __ldg(ls.pairs + 2 * j + 1), t, out);
   return out;
+}
+
+__device__ inline PointVerdict run_point_ordered(const Instr* __restrict__ prog, int len,
+                                                 const int32_t* __restrict__ sched, const Tile<double>& t)
+{
+  return sched != nullptr ? run_point_lane(prog, sched, 0, 0, t) : run_point(prog, len, t);
 }
 
 __device__ __forceinline__ PointVerdict group_point_verdict(PointVerdict v, int G)

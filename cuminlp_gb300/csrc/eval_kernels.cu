@@ -859,7 +859,7 @@ __global__ void __launch_bounds__(kEvalThreads) sample_children_kernel(const Sam
       if (a.pinfo != nullptr) fathom = fathom || a.pinfo[k].fathom;
       const uint64_t salt = a.salt_base_dev ? salt_base + k + 1 : a.salt;
       stage_point(a, t, k, r, i, salt, fathom);
-      const PointVerdict pv = run_point(a.prog, a.prog_len, t);
+      const PointVerdict pv = run_point_ordered(a.prog, a.prog_len, a.sched, t);
       double value = (pv.feasible && !(pv.obj != pv.obj)) ? pv.obj : INFINITY;
       if (fathom && a.state != nullptr && value < INFINITY && !admissible(a, t)) {
         if (value < gub) ++rejected;
@@ -907,7 +907,7 @@ __global__ void __launch_bounds__(kEvalThreads) sample_children_kernel(const Sam
         t.lo[v * B + t.tid] =
             fathom ? lo : sample_value(a.var_kinds[v] != 0, lo, hi, (uint64_t)v, i, r, salt);
       }
-      const PointVerdict pv = run_point(a.prog, a.prog_len, t);
+      const PointVerdict pv = run_point_ordered(a.prog, a.prog_len, a.sched, t);
       double value = (pv.feasible && !(pv.obj != pv.obj)) ? pv.obj : INFINITY;
       if (fathom && a.state != nullptr && value < INFINITY && !admissible(a, t)) {
         if (value < gub) ++rejected;
@@ -1003,7 +1003,12 @@ __global__ void __launch_bounds__(kEvalThreads) sample_screen_kernel(const Sampl
       pv.feasible = true;
       pv.has_obj = false;
       if (act) {
-        if (lg == 0) {
+        if (lg == 0 && a.sched != nullptr) {
+          // level 0 of the lane schedule: the objective's segments last
+          const LaneSegs l0 = lane_segments(a.sched, 0, 0);
+          for (int j = l0.b; j < l0.e && pv.feasible; ++j)
+            point_range32(a.prog, __ldg(l0.pairs + 2 * j), __ldg(l0.pairs + 2 * j + 1), t, pv);
+        } else if (lg == 0) {
           point_range32(a.prog, p0, p1, t, pv);
         } else {
           for (int j = ls.b; j < ls.e && pv.feasible; ++j)

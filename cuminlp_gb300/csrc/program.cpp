@@ -328,6 +328,15 @@ class Compiler {
       }
     }
     segs.push_back({start, len});
+    // a point stops at its first violated constraint: the segments that
+    // hold the objective come last in every lane's list (level 0: one lane,
+    // program order otherwise)
+    auto holds_objective = [&](const std::pair<int, int>& sg) {
+      for (int pc = sg.first; pc < sg.second; ++pc)
+        if ((out_.code64[pc].head & 7) == kOpObjective) return true;
+      return false;
+    };
+    const std::vector<std::pair<int, int>> in_order = segs;
     std::stable_sort(segs.begin(), segs.end(), [](const std::pair<int, int>& a, const std::pair<int, int>& b) {
       return (a.second - a.first) > (b.second - b.first);
     });
@@ -336,6 +345,15 @@ class Compiler {
     out_.sched.assign(6, 0);
     out_.makespan.assign(6, 0);
     out_.makespan[0] = len;
+    out_.sched[0] = (int32_t)out_.sched.size();
+    out_.sched.push_back(0);
+    out_.sched.push_back(ns);
+    for (int pass = 0; pass < 2; ++pass)
+      for (const auto& sg : in_order)
+        if (holds_objective(sg) == (pass == 1)) {
+          out_.sched.push_back(sg.first);
+          out_.sched.push_back(sg.second);
+        }
     for (int l = 1; l <= 5; ++l) {
       const int G = 1 << l;
       std::vector<std::vector<int>> lanes(G);
@@ -356,10 +374,12 @@ class Compiler {
         out_.sched.push_back(acc);
       }
       for (int q = 0; q < G; ++q)
-        for (int j : lanes[q]) {
-          out_.sched.push_back(segs[j].first);
-          out_.sched.push_back(segs[j].second);
-        }
+        for (int pass = 0; pass < 2; ++pass)
+          for (int j : lanes[q])
+            if (holds_objective(segs[j]) == (pass == 1)) {
+              out_.sched.push_back(segs[j].first);
+              out_.sched.push_back(segs[j].second);
+            }
     }
     // more lanes per box only while they cut the busiest lane's work by a
     // fifth or more

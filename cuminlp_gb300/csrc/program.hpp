@@ -45,7 +45,9 @@ struct Program {
   // chains) can run in any order.  Layout: sched[l] is the offset of level
   // l's block: G + 1 per-lane offsets into the pair list that follows, then
   // (pc0, pc1) pairs in lane order.  Lanes get segments by longest-first
-  // greedy assignment (LPT).
+  // greedy assignment (LPT); within a lane, and in level 0 (one lane, the
+  // program's order), the segments that hold the objective come last, so a
+  // point evaluation stops at a violated constraint before it.
   int n_segments = 0;
   int group_max = 1;               // largest G that still shortens a box's critical path
   std::vector<int32_t> sched;

@@ -765,12 +765,13 @@ def run_ours(args):
 
     phase_rl = {
         "certify": dict(phase_line(0, ld["expansions"], fpb, peak64,
-                                   "eval_children_kernel<double, 0> (FP64 verdict of each selected box, on its own "
-                                   "stream beside the branching and the FP32 bound)", None, "selected box",
+                                   "eval_children_staged_kernel<0, 1> (FP64 verdict of each selected box, fused "
+                                   "terms, on its own stream beside the branching and the FP32 bound)", None,
+                                   "selected box",
                                    "lazy_phases"), bound="fp64"),
         "bound": dict(phase_line(1, ld["bounded"], fpb, peak32,
-                                 "inc_common_kernel + eval_children_inc_kernel (FP32 child bounds, incremental; "
-                                 "beside the FP64 verdict)", INC32_DRAM_BYTES_PER_BOX, "child box", "lazy_phases"),
+                                 "inc_common_kernel + inc_parts_kernel + eval_children_inc_kernel (FP32 child "
+                                 "bounds, incremental; beside the FP64 verdict)", INC32_DRAM_BYTES_PER_BOX, "child box", "lazy_phases"),
                       bound="fp32"),
         "sample": dict(phase_line(2, ld["sampled"], pfb, peak32,
                                   "sample_screen_kernel (FP32 point ranking) + sample_children_kernel (FP64 "
@@ -859,11 +860,12 @@ def run_ours(args):
         "screen_identical_to_plain": plain["outcome"] == res["fp32"]["outcome"],
         "roofline": dict(phase_rl[dominant], phase=dominant,
                          peak_source="measured by cmn_measure_fma_peak (FMA loop, all SMs) in this run; FMA counted "
-                                     "as 2 flops, and directed rounding allows none, so the instruction ceiling is "
-                                     "half the peak"),
+                                     "as 2 flops.  The interval operations round each product and sum on its own, so "
+                                     "the instruction ceiling is half the peak, except the verdict's coefficient-and-"
+                                     "add pairs, which are one directed FMA each"),
         "phase_rooflines": phase_rl,
         "roofline_plain_fp64": {
-            "bound": "fp64", "kernel": "eval_children_kernel<double, 1> (plain FP64 form)",
+            "bound": "fp64", "kernel": "eval_children_staged_kernel<1, 0> (plain FP64 form, program tiles in shared memory)",
             "achieved": achieved64, "peak": peak64, "unit": "TFLOP/s", "frac": achieved64 / peak64,
             "frac_of_fp64_instruction_ceiling": achieved64 / (peak64 / 2),
             "integer_pipe_ops": "interval multiply rounded up (csrc/fp64_emu.cuh)",

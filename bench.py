@@ -801,10 +801,11 @@ def run_ours(args):
         return out
 
     def batch_leg():
-        bres = {p: batch_run(rt, p, args.steps * 4, args.warmup) for p in ("fp64", "fp32")}
+        bres = {p: batch_run(rt, p, args.steps * 4, args.warmup) for p in ("fp64", "lazy", "fp32")}
         return {"workload": "config4: 1024 uneven QCQPs, n ~ U{4..48}, m ~ U{0..24}, 0-25% integers; "
                             "256 parents x 2^4 children per instance per step; pool cap 4096 per instance",
-                "fp32_screen": bres["fp32"], "plain_fp64": bres["fp64"],
+                "lazy": bres["lazy"], "fp32_screen": bres["fp32"], "plain_fp64": bres["fp64"],
+                "lazy_speedup_vs_plain_fp64": bres["lazy"]["value"] / bres["fp64"]["value"],
                 "screen_speedup_vs_plain_fp64": bres["fp32"]["value"] / bres["fp64"]["value"]}
 
     def serving_leg():

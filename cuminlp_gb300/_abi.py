@@ -109,7 +109,7 @@ class TuneResult(C.Structure):
 
 class BatchConfig(C.Structure):
     _fields_ = [("slots", C.c_uint64), ("max_vars", C.c_int32), ("max_program_slots", C.c_int32),
-                ("device", C.c_int32), ("reserved", C.c_int32), ("shared", SolveOptions)]
+                ("device", C.c_int32), ("max_segments", C.c_int32), ("shared", SolveOptions)]
 
 
 SERVER_MAX_CLASSES = 8

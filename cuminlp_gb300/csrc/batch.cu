@@ -158,8 +158,10 @@ extern "C" cmn_status cmn_batch_create(const cmn_batch_config* config, cmn_batch
   if (o.batch_parents < 1 || o.frontier_cap < 1)
     return fail(CMN_INVALID_CONFIGURATION, "batch_parents and frontier_cap must be at least 1");
   if (o.max_cycle_size > 64) return fail(CMN_INVALID_CONFIGURATION, "max_cycle_size exceeds kMaxSlots (64)");
-  if (o.precision != CMN_PRECISION_FP64 && o.precision != CMN_PRECISION_FP32_SCREEN)
+  if (o.precision != CMN_PRECISION_FP64 && o.precision != CMN_PRECISION_FP32_SCREEN &&
+      o.precision != CMN_PRECISION_FP32_LAZY)
     return fail(CMN_INVALID_CONFIGURATION, "unknown precision");
+  if (cf.max_segments < 0) return fail(CMN_INVALID_CONFIGURATION, "max_segments must not be negative");
   if (o.batch_parents > (uint64_t)kMiSortMax || o.frontier_cap > (uint64_t)kMiSortMax ||
       o.frontier_cap + (o.batch_parents << o.bisection_budget) > (uint64_t)kMiSortMax)
     return fail(CMN_INVALID_CONFIGURATION, "frontier_cap + batch_parents * 2^bisection_budget must be <= " +
@@ -172,6 +174,7 @@ extern "C" cmn_status cmn_batch_create(const cmn_batch_config* config, cmn_batch
     BCK(ensure_kernel_attributes());
     const int max_smem = max_dynamic_smem();
     const bool fp32 = o.precision == CMN_PRECISION_FP32_SCREEN;
+    const bool lazy = o.precision == CMN_PRECISION_FP32_LAZY;
     const int64_t n_max = cf.max_vars;
     // program slots that fit beside the split variables in the FP64 bound
     // tile (the certify pass of the FP32 form is FP64 too) and beside
@@ -204,6 +207,7 @@ extern "C" cmn_status cmn_batch_create(const cmn_batch_config* config, cmn_batch
     c.child_stride = child_stride;
     c.max_cycle = (int64_t)o.max_cycle_size;
     c.enumerate_cap = (int64_t)o.enumerate_cap;
+    c.seg_max = lazy ? (cf.max_segments > 0 ? cf.max_segments : (int)n_max + 1) : 0;
     const uint64_t K = c.K, nm = (uint64_t)n_max, G = K * child_stride;
 
     BatchBufs& b = s->b;
@@ -219,9 +223,16 @@ extern "C" cmn_status cmn_batch_create(const cmn_batch_config* config, cmn_batch
     A(&b.depth, K * c.P);
     A(&b.plo, K * nm * c.e_max);
     A(&b.phi, K * nm * c.e_max);
-    if (fp32) {
+    if (fp32 || lazy) {
       A(&b.plo32, K * nm * c.e_max);
       A(&b.phi32, K * nm * c.e_max);
+    }
+    if (lazy) {
+      A(&b.plb, K * c.e_max);
+      A(&b.pfeas, K * c.e_max);
+      A(&b.inc_common, 2 * K * (uint64_t)c.seg_max * c.e_max);
+      A(&b.inc_parts, 2 * K * (uint64_t)c.seg_max * child_stride);
+      A(&b.cbest, G);
     }
     A(&b.pdepth, K * c.e_max);
     A(&b.pinfo, K * c.e_max);
@@ -334,6 +345,19 @@ extern "C" cmn_status cmn_batch_add(cmn_batch* s, const cmn_problem* p, const cm
   d.n_slots = p->prog.n_slots;
   d.sched = p->d_sched;
   d.g_max = p->d_sched ? p->prog.group_max : 1;
+  if (s->cfg.precision == CMN_PRECISION_FP32_LAZY) {
+    d.prog32p = p->d_prog32p;
+    if (p->d_inc_seg != nullptr) {
+      if (p->prog.inc_segments > s->cfg.seg_max)
+        return fail(CMN_INVALID_CONFIGURATION, "problem program has " + std::to_string(p->prog.inc_segments) +
+                                                   " sum-chain segments; the batch takes " +
+                                                   std::to_string(s->cfg.seg_max) + " (max_segments)");
+      d.inc_seg = p->d_inc_seg;
+      d.inc_off = p->d_inc_off;
+      d.inc_pcs = p->d_inc_pcs;
+      d.inc_segments = p->prog.inc_segments;
+    }
+  }
   d.active = 1;
   d.iter_limit = opts->iter_limit;
   d.batch_iter_limit = opts->batch_iter_limit;

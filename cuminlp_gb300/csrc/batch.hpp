@@ -41,6 +41,7 @@ struct BatchCfg {
   int g_max;                 // lanes per child at most (1: one lane per child)
   uint64_t eval_capacity;    // threads the bound launches keep resident
   uint64_t sample_capacity;  // threads the sample launch keeps resident
+  int seg_max;               // lazy form: sum-chain segments per instance program, at most
 };
 
 struct InstDesc {
@@ -59,6 +60,15 @@ struct InstDesc {
   uint64_t iter_limit;
   uint64_t batch_iter_limit;
   double tolerance;
+  // lazy form: the FP32 point program, and the program's incremental
+  // tables (Program::inc_*; inc_segments 0: the whole FP32 program bounds
+  // each child)
+  const Instr* prog32p;
+  const int32_t* inc_seg;
+  const int32_t* inc_off;
+  const int32_t* inc_pcs;
+  int32_t inc_segments;
+  int32_t pad2_;
 };
 
 struct InstState {
@@ -113,6 +123,12 @@ struct BatchBufs {
   // programs (longest-processing-time-first balance)
   const uint32_t* order;
   double* best_point;  // [K][n_max]
+  // lazy form
+  double* plb;         // [K][e_max] the staged parents' certified FP64 lower bounds
+  uint8_t* pfeas;      // [K][e_max] and their reference predicate
+  float* inc_common;   // [K][seg_max][e_max] (lo, hi): chain sums without split variables
+  float* inc_parts;    // [K][seg_max][2^B][e_max] (lo, hi): per slot part (incremental children)
+  Best32* cbest;       // [K][child_stride] the FP32 screen's best sample per child
 };
 
 // Puts `slot`'s root box in its pool and resets its state.

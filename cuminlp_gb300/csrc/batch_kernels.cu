@@ -308,6 +308,7 @@ __global__ void batch_branch_kernel(const BatchCfg c, const BatchBufs b)
       bisection_policy(b.plo + splane(c, slot, 0) + k, b.phi + splane(c, slot, 0) + k, c.e_max, d.n_vars, d.kinds,
                        pp, ec, bc, heap, sp);
   b.pinfo[pk] = pi;
+  if (c.precision == CMN_PRECISION_FP32_LAZY) return;  // batch_drop_kernel counts after the verdict
   if (pi.fathom) {
     atomicAdd((unsigned long long*)&st->counters.fathomed, 1ULL);
     atomicAdd((unsigned long long*)&st->counters.fathomed_points, (unsigned long long)pi.nreg);
@@ -395,11 +396,378 @@ __device__ __forceinline__ Verdict<T> batch_lane_verdict(const InstDesc& d, cons
   return verdict_init<T>();
 }
 
-// kMode 1: FP64 bound; 2: FP32 screen; 3: FP64 certify of the listed children.
-// Variables come from the parent planes (FP32 copies for the screen) with
-// the child's split variables in this thread's shared-memory column.  The
-// launch walks only live children (child_base), with 2^lg lanes per child
-// when there are few of them.
+__device__ __forceinline__ double child_bound(const BatchCfg& c, const BatchBufs& b, uint64_t slot, uint64_t k,
+                                              uint64_t r, int v, const SlotPlan* sp, uint32_t count, double& hi)
+{
+  double lo = b.plo[splane(c, slot, v) + k];
+  hi = b.phi[splane(c, slot, v) + k];
+  for (uint32_t j = 0; j < count; ++j) {
+    if (sp[j].vid == (uint32_t)v) {
+      const uint64_t part = slot_part(r, sp[j]);
+      slot_bounds(sp[j], lo, hi, part, lo, hi);
+      break;
+    }
+  }
+  return lo;
+}
+
+// ---- the lazy form over many instances (as the single-instance solver
+// runs it: csrc/search_kernels.cu solver_iteration, csrc/eval_kernels.cu) ----
+__device__ __forceinline__ size_t common_at(const BatchCfg& c, uint64_t slot, int s, uint64_t k)
+{
+  return 2 * (((size_t)slot * c.seg_max + s) * c.e_max + k);
+}
+
+__device__ __forceinline__ size_t part_at(const BatchCfg& c, uint64_t slot, int s, uint64_t u, uint64_t k)
+{
+  return 2 * ((((size_t)slot * c.seg_max + s) * ((size_t)1 << c.log2C) + u) * c.e_max + k);
+}
+
+// A parent's FP32 planes with one variable narrowed to one part of its slot.
+struct BatchPartVars {
+  const float* plo;
+  const float* phi;
+  uint64_t pstride;
+  int vid;
+  Iv<float> val;
+  __device__ __forceinline__ Iv<float> var(int v) const
+  {
+    if (v == vid) return val;
+    const uint64_t off = (uint64_t)v * pstride;
+    return {__ldg(plo + off), __ldg(phi + off)};
+  }
+};
+
+__device__ __forceinline__ bool slot_var_before_b(const SlotPlan* sp, int j, int v)
+{
+  for (int q = 0; q < j; ++q)
+    if (sp[q].vid == (uint32_t)v) return true;
+  return false;
+}
+
+// FP64 verdict of every staged parent (fused terms, as mode 6 of the
+// single-instance evaluator): plb, pfeas.  One lane per parent.
+__global__ void __launch_bounds__(kEvalThreads) batch_verdict_kernel(const BatchCfg c, const BatchBufs b)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* base = reinterpret_cast<double*>(smem_raw);
+  const int B = blockDim.x;
+  Tile<double> t;
+  t.lo = nullptr;
+  t.hi = nullptr;
+  t.slo = base;
+  t.shi = base + (size_t)c.slots_max * B;
+  t.stride = B;
+  t.tid = threadIdx.x;
+  for (uint64_t idx = (uint64_t)blockIdx.x * B + threadIdx.x; idx < c.K * c.e_max;
+       idx += (uint64_t)gridDim.x * B) {
+    const uint64_t slot = idx / c.e_max, k = idx % c.e_max;
+    if (k >= b.st[slot].n_parents) continue;
+    const InstDesc& d = b.desc[slot];
+    ChildVars<double, double> cv = {};
+    cv.plo = b.plo + splane(c, slot, 0) + k;
+    cv.phi = b.phi + splane(c, slot, 0) + k;
+    cv.pstride = c.e_max;
+    cv.mask = 0;
+    cv.count = 0;
+    cv.stride = B;
+    const Verdict<double> v = run_interval<double, ChildVars<double, double>, true>(d.prog64, d.prog_len, cv, t);
+    b.plb[slot * c.e_max + k] = v.obj.lo;
+    b.pfeas[slot * c.e_max + k] = (uint8_t)v.feasible;
+  }
+}
+
+// A box the verdict excludes (reference predicate, or bound above the
+// incumbent) is not expanded; the expansion counters as lazy_drop_kernel.
+__global__ void batch_drop_kernel(const BatchCfg c, const BatchBufs b)
+{
+  const uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= c.K * c.e_max) return;
+  const uint64_t slot = idx / c.e_max, k = idx % c.e_max;
+  InstState* st = &b.st[slot];
+  if (k >= st->n_parents) return;
+  const size_t pk = slot * c.e_max + k;
+  ParentInfo pi = b.pinfo[pk];
+  unsigned long long dropped = 0;
+  if (!b.pfeas[pk] || b.plb[pk] > st->gub) {
+    pi = ParentInfo{0, 0, 0};
+    b.pinfo[pk] = pi;
+    dropped = 1;
+  }
+  atomicAdd((unsigned long long*)&st->counters.certified_fp64, 1ULL);
+  if (dropped) atomicAdd((unsigned long long*)&st->counters.certify_pruned, 1ULL);
+  if (pi.fathom) {
+    atomicAdd((unsigned long long*)&st->counters.fathomed, 1ULL);
+    atomicAdd((unsigned long long*)&st->counters.fathomed_points, (unsigned long long)pi.nreg);
+  } else {
+    atomicAdd((unsigned long long*)&st->counters.bounded, (unsigned long long)pi.nreg);
+  }
+}
+
+// Common chain sums of every (instance, segment, parent) whose program has
+// the incremental tables (inc_common_kernel per instance).
+__global__ void __launch_bounds__(kEvalThreads) batch_inc_common_kernel(const BatchCfg c, const BatchBufs b)
+{
+  const uint64_t total = c.K * (uint64_t)c.seg_max * c.e_max;
+  for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t k = idx % c.e_max, rest = idx / c.e_max;
+    const int s = (int)(rest % (uint64_t)c.seg_max);
+    const uint64_t slot = rest / (uint64_t)c.seg_max;
+    if (k >= b.st[slot].n_parents) continue;
+    const InstDesc& d = b.desc[slot];
+    if (s >= d.inc_segments) continue;
+    const ParentInfo pi = b.pinfo[slot * c.e_max + k];
+    if (pi.nreg == 0 || pi.fathom) continue;  // no bounded children
+    const SlotPlan* sp = b.slots + (slot * c.e_max + k) * c.max_slots;
+    uint64_t mask = 0;
+    for (uint32_t j = 0; j < pi.count; ++j) mask |= 1ULL << (sp[j].vid & 63);
+    ChildVars<float, float> pv = {};
+    pv.plo = b.plo32 + splane(c, slot, 0) + k;
+    pv.phi = b.phi32 + splane(c, slot, 0) + k;
+    pv.pstride = c.e_max;
+    auto is_split = [&](int v) {
+      if (!((mask >> (v & 63)) & 1ULL)) return false;
+      for (uint32_t j = 0; j < pi.count; ++j)
+        if (sp[j].vid == (uint32_t)v) return true;
+      return false;
+    };
+    Iv<float> acc = {0.0f, 0.0f};
+    const int pb = __ldg(d.inc_seg + 3 * s), pt = __ldg(d.inc_seg + 3 * s + 1);
+    for (int pc = pb; pc < pt; ++pc) {
+      const Instr cur = load_instr(d.prog32, pc);
+      const int code = cur.head & 7;
+      const bool reads_var = code == kOpTerm || (cur.modes & 3) == kModeVar;
+      if (reads_var && (is_split(cur.a) || (code == kOpTerm && is_split(cur.b)))) continue;
+      acc = chain_add<float, ChildVars<float, float>>(acc, cur, pv);
+    }
+    const size_t at = common_at(c, slot, s, k);
+    b.inc_common[at] = acc.lo;
+    b.inc_common[at + 1] = acc.hi;
+  }
+}
+
+// Part sums of every (instance, slot part, parent) (inc_parts_kernel per
+// instance), every segment of the instance's program.
+__global__ void __launch_bounds__(kEvalThreads) batch_inc_parts_kernel(const BatchCfg c, const BatchBufs b)
+{
+  const uint64_t C = 1ULL << c.log2C;
+  const uint64_t total = c.K * C * c.e_max;
+  for (uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t k = idx % c.e_max, rest = idx / c.e_max;
+    const uint64_t u = rest % C, slot = rest / C;
+    if (k >= b.st[slot].n_parents) continue;
+    const InstDesc& d = b.desc[slot];
+    const int S = d.inc_segments;
+    if (S == 0) continue;
+    const ParentInfo pi = b.pinfo[slot * c.e_max + k];
+    if (pi.fathom || pi.nreg == 0) continue;
+    const SlotPlan* sp = b.slots + (slot * c.e_max + k) * c.max_slots;
+    int j = -1;
+    uint64_t p = 0, base = 0;
+    for (uint32_t q = 0; q < pi.count; ++q) {
+      const uint64_t w = sp[q].width;
+      if (u < base + w) {
+        j = (int)q;
+        p = u - base;
+        break;
+      }
+      base += w;
+    }
+    if (j < 0) continue;
+    const SlotPlan sj = sp[j];
+    const int vj = (int)sj.vid;
+    const bool repeated = slot_var_before_b(sp, j, vj);
+    BatchPartVars pv;
+    pv.plo = b.plo32 + splane(c, slot, 0) + k;
+    pv.phi = b.phi32 + splane(c, slot, 0) + k;
+    pv.pstride = c.e_max;
+    pv.vid = vj;
+    double lo, hi;
+    slot_bounds(sj, b.plo[splane(c, slot, vj) + k], b.phi[splane(c, slot, vj) + k], p, lo, hi);
+    pv.val = {Widen<float, double>::lo(lo), Widen<float, double>::hi(hi)};
+    for (int s = 0; s < S; ++s) {
+      Iv<float> acc = {0.0f, 0.0f};
+      if (!repeated) {
+        const int q0 = __ldg(d.inc_off + (uint64_t)vj * S + s), q1 = __ldg(d.inc_off + (uint64_t)vj * S + s + 1);
+        for (int q = q0; q < q1; ++q) {
+          const Instr cur = load_instr(d.prog32, __ldg(d.inc_pcs + q));
+          if ((cur.head & 7) == kOpTerm) {
+            const int other = cur.a == vj ? cur.b : cur.a;
+            if (other != vj && slot_var_before_b(sp, j, other)) continue;
+          }
+          acc = chain_add<float, BatchPartVars>(acc, cur, pv);
+        }
+      }
+      const size_t at = part_at(c, slot, s, u, k);
+      b.inc_parts[at] = acc.lo;
+      b.inc_parts[at + 1] = acc.hi;
+    }
+  }
+}
+
+// A child's FP32 bound from its parent's common sums and its slots' part
+// sums, then each segment's checks and objective (eval_children_inc_kernel).
+__device__ Verdict<float> batch_inc_child(const BatchCfg& c, const BatchBufs& b, const InstDesc& d, uint64_t slot,
+                                          uint64_t k, uint64_t r, const SlotPlan* sp, uint32_t count,
+                                          const ChildVars<float, float>& cv, uint32_t* opart, int B)
+{
+  uint64_t pbase = 0;
+  for (uint32_t j = 0; j < count; ++j) {
+    opart[j * B] = (uint32_t)(pbase + slot_part(r, sp[j]));
+    pbase += sp[j].width;
+  }
+  Verdict<float> v = verdict_init<float>();
+  for (int s = 0; s < d.inc_segments; ++s) {
+    const size_t ca = common_at(c, slot, s, k);
+    Iv<float> acc = {b.inc_common[ca], b.inc_common[ca + 1]};
+    for (uint32_t j = 0; j < count; ++j) {
+      const size_t at = part_at(c, slot, s, opart[j * B], k);
+      acc = iv_add(acc, Iv<float>{b.inc_parts[at], b.inc_parts[at + 1]});
+    }
+    chain_tail<float, ChildVars<float, float>>(d.prog32, __ldg(d.inc_seg + 3 * s + 1), __ldg(d.inc_seg + 3 * s + 2),
+                                               cv, acc, v);
+  }
+  return v;
+}
+
+// The FP32 sample screen over every live child (sample_screen_kernel with
+// one lane per child): per child its smallest FP32 sample value and that
+// sample's index, +inf when none is feasible in FP32 or it is not sampled.
+__global__ void __launch_bounds__(kEvalThreads) batch_screen_kernel(const BatchCfg c, const BatchBufs b)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float* base = reinterpret_cast<float*>(smem_raw);
+  const int B = blockDim.x;
+  Tile<float> t;
+  t.lo = base;
+  t.hi = base;
+  t.slo = base + (size_t)c.n_max * B;
+  t.shi = t.slo;
+  t.stride = B;
+  t.tid = threadIdx.x;
+  const uint64_t total = b.child_base[c.K];
+  for (uint64_t idx = (uint64_t)blockIdx.x * B + threadIdx.x; idx < total; idx += (uint64_t)gridDim.x * B) {
+    const uint64_t g = live_child(c, b, idx);
+    const uint64_t slot = g / c.child_stride, local = g % c.child_stride;
+    const uint64_t k = local >> c.log2C, r = local & ((1ULL << c.log2C) - 1ULL);
+    const InstState* st = &b.st[slot];
+    const ParentInfo pi = b.pinfo[slot * c.e_max + k];
+    Best32 best = {INFINITY, 0};
+    const bool fathom = pi.fathom != 0;
+    bool live = r < pi.nreg;
+    if (live && !fathom) {
+      const uint8_t s8 = b.cstate[g] & 0x7f;
+      live = c.sample_all ? (s8 != kChildNone) : (s8 == kChildEligible);
+    }
+    if (live) {
+      const InstDesc& d = b.desc[slot];
+      const SlotPlan* sp = b.slots + (slot * c.e_max + k) * c.max_slots;
+      const uint64_t S = fathom ? 1 : c.S;
+      const uint64_t salt = st->salt_base + k + 1;
+      for (uint64_t i = 0; i < S; ++i) {
+        for (int v = 0; v < d.n_vars; ++v) {
+          double hi;
+          const double lo = child_bound(c, b, slot, k, r, v, sp, pi.count, hi);
+          const double x = fathom ? lo : sample_value(d.kinds[v] != 0, lo, hi, (uint64_t)v, i, r, salt);
+          t.lo[v * B + t.tid] = __double2float_rn(x);
+        }
+        PointVerdict32 pv = {INFINITY, true, false};
+        if (d.sched != nullptr) {
+          const LaneSegs l0 = lane_segments(d.sched, 0, 0);
+          for (int j = l0.b; j < l0.e && pv.feasible; ++j)
+            point_range32(d.prog32p, __ldg(l0.pairs + 2 * j), __ldg(l0.pairs + 2 * j + 1), t, pv);
+        } else {
+          point_range32(d.prog32p, 0, d.prog_len, t, pv);
+        }
+        const float value = (pv.feasible && !(pv.obj != pv.obj)) ? pv.obj : INFINITY;
+        if (value < best.value) best = Best32{value, (uint32_t)i};
+      }
+    }
+    b.cbest[g] = best;
+  }
+}
+
+// Each chunk of 32 consecutive children of an instance: its FP32-best
+// sample (chunk_pick's order: smallest value, then first child, then first
+// sample) evaluated again in FP64; only that value can become the
+// incumbent (sample_children_kernel in chunk mode).  cval / ce of the
+// chunk's other children are +inf.
+__global__ void __launch_bounds__(kEvalThreads) batch_chunk_kernel(const BatchCfg c, const BatchBufs b)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* base = reinterpret_cast<double*>(smem_raw);
+  const int B = blockDim.x;
+  Tile<double> t;
+  t.lo = base;
+  t.hi = base;
+  t.slo = base + (size_t)c.n_max * B;
+  t.shi = t.slo;
+  t.stride = B;
+  t.tid = threadIdx.x;
+  const uint64_t per_slot = (c.child_stride + 31) >> 5;
+  for (uint64_t idx = (uint64_t)blockIdx.x * B + threadIdx.x; idx < c.K * per_slot; idx += (uint64_t)gridDim.x * B) {
+    const uint64_t slot = idx / per_slot, ch = idx % per_slot;
+    InstState* st = &b.st[slot];
+    const uint64_t nch = st->n_parents << c.log2C;
+    const uint64_t g0 = ch << 5;
+    if (g0 >= nch) continue;
+    const uint64_t g1 = nch < g0 + 32 ? nch : g0 + 32;
+    const uint64_t cbase = slot * c.child_stride;
+    float bv = INFINITY;
+    uint64_t bg = 0;
+    uint32_t bi = 0;
+    for (uint64_t x = g0; x < g1; ++x) {
+      b.cval[cbase + x] = INFINITY;
+      const Best32 q = b.cbest[cbase + x];
+      if (q.value < bv) {
+        bv = q.value;
+        bg = x;
+        bi = q.i;
+      }
+    }
+    if (!(bv < INFINITY)) continue;
+    const InstDesc& d = b.desc[slot];
+    const uint64_t k = bg >> c.log2C, r = bg & ((1ULL << c.log2C) - 1ULL);
+    const ParentInfo pi = b.pinfo[slot * c.e_max + k];
+    if (r >= pi.nreg) continue;
+    const bool fathom = pi.fathom != 0;
+    const SlotPlan* sp = b.slots + (slot * c.e_max + k) * c.max_slots;
+    const uint64_t salt = st->salt_base + k + 1;
+    for (int v = 0; v < d.n_vars; ++v) {
+      double hi;
+      const double lo = child_bound(c, b, slot, k, r, v, sp, pi.count, hi);
+      t.lo[v * B + t.tid] = fathom ? lo : sample_value(d.kinds[v] != 0, lo, hi, (uint64_t)v, bi, r, salt);
+    }
+    const PointVerdict pv = run_point_ordered(d.prog64, d.prog_len, d.sched, t);
+    double value = (pv.feasible && !(pv.obj != pv.obj)) ? pv.obj : INFINITY;
+    if (fathom && value < INFINITY) {
+      bool ok = true;
+      for (int v = 0; v < d.n_vars && ok; ++v) {
+        const double x = t.lo[v * B + t.tid];
+        if (!(x >= d.root_lb[v]) || !(x <= d.root_ub[v])) ok = false;
+        else if (d.kinds[v] != 0 && fabs(__dsub_rn(x, rint(x))) > 1e-6) ok = false;
+      }
+      if (!ok) {
+        if (value < st->gub) atomicAdd((unsigned long long*)&st->counters.witness_rejected, 1ULL);
+        value = INFINITY;
+      }
+    }
+    const uint64_t S = fathom ? 1 : c.S;
+    b.cval[cbase + bg] = value;
+    b.ce[cbase + bg] = r * S + bi;
+  }
+}
+
+// kMode 1: FP64 bound; 2: FP32 screen; 3: FP64 certify of the listed
+// children; 5: the lazy form's FP32 child bound (incremental from the part
+// sums when the instance's program has the tables, else its whole FP32
+// program), the parent's certified bound folded in.  Variables come from
+// the parent planes (FP32 copies for the FP32 passes) with the child's
+// split variables in this thread's shared-memory column.  The launch walks
+// only live children (child_base), with 2^lg lanes per child when there
+// are few of them.
 template <typename T, int kMode>
 __global__ void __launch_bounds__(kEvalThreads, 4) batch_eval_kernel(const BatchCfg c, const BatchBufs b)
 {
@@ -417,6 +785,8 @@ __global__ void __launch_bounds__(kEvalThreads, 4) batch_eval_kernel(const Batch
   T* olo = base + (size_t)2 * c.slots_max * B + threadIdx.x;
   T* ohi = olo + (size_t)c.max_slots * B;
   int32_t* ovid = reinterpret_cast<int32_t*>(base + (size_t)2 * (c.slots_max + c.max_slots) * B) + threadIdx.x;
+  // kMode 5: the child's slot parts (u_j), after the split variables
+  uint32_t* opart = reinterpret_cast<uint32_t*>(ovid + (size_t)c.max_slots * B);
   const S* planes_lo;
   const S* planes_hi;
   if constexpr (sizeof(T) == 4) {
@@ -487,16 +857,37 @@ __global__ void __launch_bounds__(kEvalThreads, 4) batch_eval_kernel(const Batch
       } else {
         const InstDesc& d = b.desc[slot];
         const Instr* prog = sizeof(T) == 4 ? d.prog32 : d.prog64;
-        v = batch_lane_verdict<T, ChildVars<T, S>>(d, prog, lg, lane, cv, t);
+        if constexpr (kMode == 5 && sizeof(T) == 4) {
+          if (d.inc_segments > 0) {
+            // the parent's common sum plus the part sum of each slot
+            if (lane == 0) v = batch_inc_child(c, b, d, slot, k, r, sp, pi.count, cv, opart, B);
+          } else {
+            v = batch_lane_verdict<T, ChildVars<T, S>>(d, prog, lg, lane, cv, t);
+          }
+        } else {
+          v = batch_lane_verdict<T, ChildVars<T, S>>(d, prog, lg, lane, cv, t);
+        }
       }
     }
     if (lg > 0) v = group_verdict<T>(v, G);
     if (live && lane == 0) {
-      const double lb = (double)v.obj.lo;
+      double lb = (double)v.obj.lo;
       const double gub = st->gub;
+      if (kMode == 5 || (kMode == 3 && c.precision == CMN_PRECISION_FP32_LAZY)) {
+        // the parent's certified bound holds for every child box inside it
+        const double plb = b.plb[slot * c.e_max + k];
+        lb = plb > lb ? plb : lb;
+      }
       b.clb[g] = lb;
       if (kMode == 2) {
         b.cstate[g] = v.excluded ? kChildInfeasible : (lb > gub ? kChildDominated : kChildScreened);
+      } else if (kMode == 5) {
+        // a survivor within the band below the incumbent goes to the FP64
+        // pass, which may prune it; below the band FP64 could not
+        b.cstate[g] = v.excluded     ? kChildInfeasible
+                      : lb > gub     ? kChildDominated
+                      : lb >= certify_floor(gub) ? kChildScreened
+                                                 : kChildEligible;
       } else {
         const uint8_t sv = !v.feasible ? kChildInfeasible : (lb > gub ? kChildDominated : kChildEligible);
         b.cstate[g] = kMode == 3 ? (uint8_t)(sv | kCertifiedBit) : sv;
@@ -505,20 +896,6 @@ __global__ void __launch_bounds__(kEvalThreads, 4) batch_eval_kernel(const Batch
   }
 }
 
-__device__ __forceinline__ double child_bound(const BatchCfg& c, const BatchBufs& b, uint64_t slot, uint64_t k,
-                                              uint64_t r, int v, const SlotPlan* sp, uint32_t count, double& hi)
-{
-  double lo = b.plo[splane(c, slot, v) + k];
-  hi = b.phi[splane(c, slot, v) + k];
-  for (uint32_t j = 0; j < count; ++j) {
-    if (sp[j].vid == (uint32_t)v) {
-      const uint64_t part = slot_part(r, sp[j]);
-      slot_bounds(sp[j], lo, hi, part, lo, hi);
-      break;
-    }
-  }
-  return lo;
-}
 
 // samples (or exact points of fathomed parents) of every live child: the
 // best (value, element) per child.  With 2^lg lanes per child every lane
@@ -813,6 +1190,9 @@ __global__ void __launch_bounds__(kMiThreads) batch_finish_kernel(const BatchCfg
         const unsigned long long x = st->use_screen ? cnt[5] - cnt[7] : cnt[6];
         st->use_screen = (x * 4 >= cnt[5]) ? 1 : 0;
       }
+    } else if (c.precision == CMN_PRECISION_FP32_LAZY) {
+      ct.screened_fp32 += cnt[5];   // every valid child is bounded in FP32
+      ct.certified_fp64 += cnt[7];  // the band's FP64 pass (the parents: batch_drop_kernel)
     } else {
       ct.certified_fp64 += cnt[5];
     }
@@ -901,10 +1281,18 @@ __global__ void __launch_bounds__(512) batch_list_scatter_kernel(const BatchCfg 
 // ---------------------------------------------------------------------
 size_t batch_eval_smem(const BatchCfg& c, bool fp32)
 {
-  return ((fp32 ? 8 : 16) * (size_t)(c.slots_max + c.max_slots) + 4 * (size_t)c.max_slots) * kEvalThreads;
+  // FP32 (the screen, the lazy bound): slot parts after the split variables
+  return ((fp32 ? 8 : 16) * (size_t)(c.slots_max + c.max_slots) + (fp32 ? 8 : 4) * (size_t)c.max_slots) *
+         kEvalThreads;
 }
 
 size_t batch_sample_smem(const BatchCfg& c) { return 8 * (size_t)(c.n_max + c.slots_max) * kEvalThreads; }
+
+// the lazy form's FP32 screen: one FP32 point column per thread
+static size_t batch_screen_smem(const BatchCfg& c) { return 4 * (size_t)(c.n_max + c.slots_max) * kEvalThreads; }
+
+// the lazy form's verdict: program slots (FP64 intervals) per thread
+static size_t batch_verdict_smem(const BatchCfg& c) { return 16 * (size_t)c.slots_max * kEvalThreads; }
 
 int batch_eval_occupancy(const BatchCfg& c, bool fp32)
 {
@@ -939,6 +1327,10 @@ cudaError_t set_batch_kernel_attributes(int max_smem)
   if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_eval_kernel<float, 2>, at, max_smem);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_eval_kernel<double, 3>, at, max_smem);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_sample_kernel, at, max_smem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_eval_kernel<float, 5>, at, max_smem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_verdict_kernel, at, max_smem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_screen_kernel, at, max_smem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_chunk_kernel, at, max_smem);
   return e;
 }
 
@@ -965,6 +1357,31 @@ cudaError_t batch_iteration(const BatchCfg& c, const BatchBufs& b, int eval_grid
   batch_live_kernel<<<1, 1024, 0, s>>>(c, b);
   mark(marks, 1, s);
   const bool fp32 = c.precision == CMN_PRECISION_FP32_SCREEN;
+  const bool lazy = c.precision == CMN_PRECISION_FP32_LAZY;
+  if (lazy) {
+    // the FP64 verdict of the staged parents, the drop, then the FP32 child
+    // bounds with each parent's certified bound folded in, and the band's
+    // FP64 pass (the single-instance solver runs the verdict beside the
+    // bounds; the states and counters are the same)
+    batch_verdict_kernel<<<eval_grid, kEvalThreads, batch_verdict_smem(c), s>>>(c, b);
+    const uint64_t np2 = c.K * c.e_max;
+    batch_drop_kernel<<<(int)((np2 + 255) / 256), 256, 0, s>>>(c, b);
+    batch_inc_common_kernel<<<eval_grid, kEvalThreads, 0, s>>>(c, b);
+    batch_inc_parts_kernel<<<eval_grid, kEvalThreads, 0, s>>>(c, b);
+    batch_eval_kernel<float, 5><<<eval_grid, kEvalThreads, batch_eval_smem(c, true), s>>>(c, b);
+    const int lg = (int)((c.K * c.child_stride + 511) / 512);
+    batch_list_count_kernel<<<lg, 512, 0, s>>>(c, b);
+    batch_list_scan_kernel<<<1, 1024, 0, s>>>(c, b);
+    batch_list_scatter_kernel<<<lg, 512, 0, s>>>(c, b);
+    batch_eval_kernel<double, 3><<<eval_grid, kEvalThreads, batch_eval_smem(c, false), s>>>(c, b);
+    mark(marks, 2, s);
+    batch_screen_kernel<<<eval_grid, kEvalThreads, batch_screen_smem(c), s>>>(c, b);
+    batch_chunk_kernel<<<eval_grid, kEvalThreads, batch_sample_smem(c), s>>>(c, b);
+    mark(marks, 3, s);
+    batch_finish_kernel<<<(int)c.K, kMiThreads, sort_smem_bytes(), s>>>(c, b);
+    mark(marks, 4, s);
+    return cudaGetLastError();
+  }
   if (fp32) {
     batch_eval_kernel<float, 2><<<eval_grid, kEvalThreads, batch_eval_smem(c, true), s>>>(c, b);
     const int lg = (int)((c.K * c.child_stride + 511) / 512);

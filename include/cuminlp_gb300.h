@@ -554,7 +554,9 @@ typedef struct {
   int32_t max_program_slots; /* largest program slot count; -1: as many as
                                 fit (smaller tiles give more resident blocks) */
   int32_t device;            /* CUDA device of the batch and its problems */
-  int32_t reserved;
+  int32_t max_segments;      /* lazy form: largest number of sum-chain
+                                segments (objective + constraint chains) of
+                                an instance's program; 0: max_vars + 1 */
   cmn_solve_options shared;  /* the shared options listed above */
 } cmn_batch_config;
 

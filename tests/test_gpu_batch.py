@@ -19,7 +19,7 @@ pytestmark = pytest.mark.gpu
 
 COUNTERS = ["iterations", "expansions", "fathomed", "fathomed_points", "bounded", "sampled", "enqueued",
             "witness_rejected", "pruned_duplicate", "pruned_infeasible", "pruned_dominated", "dropped_viable",
-            "dropped_dominated", "screened_fp32", "certified_fp64", "peak_frontier"]
+            "dropped_dominated", "screened_fp32", "certified_fp64", "peak_frontier", "certify_pruned"]
 FIELDS = ("lower_bound", "upper_bound", "stop_reason", "proven_optimal", "infeasible", "found_incumbent",
           "frontier_size", "viable", "dropped_lb_min")
 
@@ -88,6 +88,41 @@ def test_batch_matches_oracle_per_instance(precision):
         g, fg = got[k]
         same_frontier(fg, (obox, olb, odepth), k)
         same_outcome(g, o, k)
+
+
+def lazy_oracle(p, dp):
+    # the lazy form bounds children from the compiled FP32 program's sum
+    # chains and certifies each expanded box with the FP64 program's fused
+    # terms; the oracle restates both from the same programs
+    op = O.OracleProblem(p)
+    op.set_program32(dp.program(1))
+    op.set_program64(dp.program(0))
+    return op
+
+
+def test_batch_lazy_matches_oracle_per_instance():
+    named = mixed_problems()
+    shared = dict(SHARED, precision="lazy")
+    got = run_batch(named, shared, dict(batch_iter_limit=20))
+    for k, p in named.items():
+        op = lazy_oracle(p, DeviceProblem(p))
+        obox, olb, odepth, o = op.batched_frontier(0, room=1 << 16, batch_iter_limit=20, **shared)
+        g, fg = got[k]
+        same_frontier(fg, (obox, olb, odepth), k)
+        same_outcome(g, o, k)
+
+
+def test_batch_lazy_matches_single_instance_solver():
+    named = mixed_problems()
+    keep = {k: named[k] for k in ("aggregate", "contract", "miqcqp_n6", "cfg1b", "cfg4_0", "cfg4_3")}
+    shared = dict(SHARED, precision="lazy", sample_all=1)
+    got = run_batch(keep, shared, dict(batch_iter_limit=30))
+    for k, p in keep.items():
+        s = Solver(DeviceProblem(p), batch_iter_limit=30, **shared)
+        s.step(0)
+        same_outcome(s.outcome(), got[k][0], k)
+        same_frontier(s.frontier(), got[k][1], k)
+        s.close()
 
 
 def test_batch_alone_equals_mixed():

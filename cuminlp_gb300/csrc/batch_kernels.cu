@@ -382,17 +382,17 @@ __device__ __forceinline__ uint64_t live_child(const BatchCfg& c, const BatchBuf
 // Lanes of a group of 2^lg that run instance d's program on one box: all of
 // them over the instance's lane schedule, or lane 0 alone over the whole
 // program when the instance has none (or takes fewer lanes).
-template <typename T, typename V>
+template <typename T, typename V, bool kFused = false>
 __device__ __forceinline__ Verdict<T> batch_lane_verdict(const InstDesc& d, const Instr* prog, int lg, int lane,
                                                          const V& vars, const Tile<T>& t)
 {
   int li = 0;
   while (li < lg && (2 << li) <= d.g_max) ++li;
   if (d.sched == nullptr || li == 0) {
-    if (lane == 0) return run_interval<T, V>(prog, d.prog_len, vars, t);
+    if (lane == 0) return run_interval<T, V, kFused>(prog, d.prog_len, vars, t);
     return verdict_init<T>();
   }
-  if (lane < (1 << li)) return run_interval_lane<T, V>(prog, d.sched, li, lane, vars, t);
+  if (lane < (1 << li)) return run_interval_lane<T, V, kFused>(prog, d.sched, li, lane, vars, t);
   return verdict_init<T>();
 }
 
@@ -446,7 +446,10 @@ __device__ __forceinline__ bool slot_var_before_b(const SlotPlan* sp, int j, int
 }
 
 // FP64 verdict of every staged parent (fused terms, as mode 6 of the
-// single-instance evaluator): plb, pfeas.  One lane per parent.
+// single-instance evaluator): plb, pfeas.  The launch walks the live
+// parents (child_base >> B), with 2^lg lanes per parent when there are few
+// of them (the program's lane schedule; the verdict is the same).  The loop
+// bound is per block, so every lane of a warp reaches the shuffles.
 __global__ void __launch_bounds__(kEvalThreads) batch_verdict_kernel(const BatchCfg c, const BatchBufs b)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -459,21 +462,35 @@ __global__ void __launch_bounds__(kEvalThreads) batch_verdict_kernel(const Batch
   t.shi = base + (size_t)c.slots_max * B;
   t.stride = B;
   t.tid = threadIdx.x;
-  for (uint64_t idx = (uint64_t)blockIdx.x * B + threadIdx.x; idx < c.K * c.e_max;
-       idx += (uint64_t)gridDim.x * B) {
-    const uint64_t slot = idx / c.e_max, k = idx % c.e_max;
-    if (k >= b.st[slot].n_parents) continue;
-    const InstDesc& d = b.desc[slot];
-    ChildVars<double, double> cv = {};
-    cv.plo = b.plo + splane(c, slot, 0) + k;
-    cv.phi = b.phi + splane(c, slot, 0) + k;
-    cv.pstride = c.e_max;
-    cv.mask = 0;
-    cv.count = 0;
-    cv.stride = B;
-    const Verdict<double> v = run_interval<double, ChildVars<double, double>, true>(d.prog64, d.prog_len, cv, t);
-    b.plb[slot * c.e_max + k] = v.obj.lo;
-    b.pfeas[slot * c.e_max + k] = (uint8_t)v.feasible;
+  const uint64_t total = b.child_base[c.K] >> c.log2C;
+  const int lg = lanes_per_box(total, c.eval_capacity, (int)b.child_base[c.K + 1]);
+  const int G = 1 << lg;
+  const int lane = threadIdx.x & (G - 1);
+  const uint64_t per_block = (uint64_t)(B >> lg);
+  for (uint64_t bb = (uint64_t)blockIdx.x * per_block; bb < total; bb += (uint64_t)gridDim.x * per_block) {
+    const uint64_t idx = bb + (threadIdx.x >> lg);
+    const bool live = idx < total;
+    Verdict<double> v = verdict_init<double>();
+    uint64_t slot = 0, k = 0;
+    if (live) {
+      const uint64_t g = live_child(c, b, idx << c.log2C);
+      slot = g / c.child_stride;
+      k = (g % c.child_stride) >> c.log2C;
+      const InstDesc& d = b.desc[slot];
+      ChildVars<double, double> cv = {};
+      cv.plo = b.plo + splane(c, slot, 0) + k;
+      cv.phi = b.phi + splane(c, slot, 0) + k;
+      cv.pstride = c.e_max;
+      cv.mask = 0;
+      cv.count = 0;
+      cv.stride = B;
+      v = batch_lane_verdict<double, ChildVars<double, double>, true>(d, d.prog64, lg, lane, cv, t);
+    }
+    if (lg > 0) v = group_verdict<double>(v, G);
+    if (live && lane == 0) {
+      b.plb[slot * c.e_max + k] = v.obj.lo;
+      b.pfeas[slot * c.e_max + k] = (uint8_t)v.feasible;
+    }
   }
 }
 

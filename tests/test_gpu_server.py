@@ -37,8 +37,8 @@ def requests():
     return ps, limits
 
 
-def alone(dp, iter_limit):
-    b = Batch(1, dp.n_vars, dp.info()["program_slots"], **SHARED)
+def alone(dp, iter_limit, shared=SHARED):
+    b = Batch(1, dp.n_vars, dp.info()["program_slots"], **shared)
     s = b.add(dp, iter_limit=iter_limit)
     b.step(0)
     out = b.outcome(s)
@@ -79,6 +79,27 @@ def test_server_results_same_alone_and_in_mix():
     # and the alone runs are the oracle's batched search
     for k in (0, 3, 14, 15, 16):
         o = O.OracleProblem(ps[k]).solve_batched(iter_limit=limits[k], **SHARED)
+        same_outcome(got[k], o, f"request {k} vs oracle")
+
+
+def test_lazy_server_results_same_alone_and_as_the_oracle():
+    # the lazy form in every class: each result the one-slot batch's and
+    # the oracle's (which restates the lazy form from the compiled programs)
+    shared = dict(SHARED, precision="lazy")
+    ps, limits = requests()
+    dps = [DeviceProblem(p) for p in ps]
+    slots = max(dp.info()["program_slots"] for dp in dps)
+    srv = Server([(v, n, slots) for v, n in CLASSES], iterations_per_round=3, **shared)
+    ids = submit_stream(srv, dps, limits)
+    got = [srv.wait(i, timeout_ms=120000) for i in ids]
+    srv.close()
+    for k, (dp, il, g) in enumerate(zip(dps, limits, got)):
+        same_outcome(g, alone(dp, il, shared), f"request {k}")
+    for k in (0, 3, 14, 15, 16):
+        op = O.OracleProblem(ps[k])
+        op.set_program32(dps[k].program(1))
+        op.set_program64(dps[k].program(0))
+        o = op.solve_batched(iter_limit=limits[k], **shared)
         same_outcome(got[k], o, f"request {k} vs oracle")
 
 

@@ -448,8 +448,12 @@ __device__ __forceinline__ bool slot_var_before_b(const SlotPlan* sp, int j, int
 // FP64 verdict of every staged parent (fused terms, as mode 6 of the
 // single-instance evaluator): plb, pfeas.  The launch walks the live
 // parents (child_base >> B), with 2^lg lanes per parent when there are few
-// of them (the program's lane schedule; the verdict is the same).  The loop
-// bound is per block, so every lane of a warp reaches the shuffles.
+// of them (the program's lane schedule; the verdict is the same).  Live
+// parents come longest program first, and the launch has about one pass:
+// the warps' runs of consecutive parents (mostly one instance, so one
+// instruction stream per warp) go to the blocks in turn, so every SM gets
+// long and short programs alike.  The loop bound is per block, so every
+// lane of a warp reaches the shuffles.
 __global__ void __launch_bounds__(kEvalThreads) batch_verdict_kernel(const BatchCfg c, const BatchBufs b)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -467,8 +471,10 @@ __global__ void __launch_bounds__(kEvalThreads) batch_verdict_kernel(const Batch
   const int G = 1 << lg;
   const int lane = threadIdx.x & (G - 1);
   const uint64_t per_block = (uint64_t)(B >> lg);
-  for (uint64_t bb = (uint64_t)blockIdx.x * per_block; bb < total; bb += (uint64_t)gridDim.x * per_block) {
-    const uint64_t idx = bb + (threadIdx.x >> lg);
+  const uint64_t per_warp = (uint64_t)(32 >> lg), warps = (uint64_t)(B >> 5);
+  for (uint64_t pass = 0; pass * per_block * gridDim.x < total; ++pass) {
+    const uint64_t wslot = (pass * warps + (threadIdx.x >> 5)) * gridDim.x + blockIdx.x;
+    const uint64_t idx = wslot * per_warp + ((threadIdx.x & 31) >> lg);
     const bool live = idx < total;
     Verdict<double> v = verdict_init<double>();
     uint64_t slot = 0, k = 0;

@@ -712,11 +712,27 @@ __global__ void __launch_bounds__(kEvalThreads) batch_screen_kernel(const BatchC
   }
 }
 
+// Lane of the n-th (from 0) set bit of m, -1 when m has fewer set bits.
+__device__ __forceinline__ int nth_set_lane(unsigned m, int n)
+{
+  for (int i = 0; i < n && m != 0u; ++i) m &= m - 1u;
+  return m != 0u ? __ffs((int)m) - 1 : -1;
+}
+
 // Each chunk of 32 consecutive children of an instance: its FP32-best
 // sample (chunk_pick's order: smallest value, then first child, then first
 // sample) evaluated again in FP64; only that value can become the
 // incumbent (sample_children_kernel in chunk mode).  cval / ce of the
 // chunk's other children are +inf.
+//
+// A warp takes 32 >> lg chunks per pass (lg from the live children and the
+// grid, as the bound's lane groups) and scans each on one lane.  It then
+// splits its 32 lanes evenly over the chunks whose pick is FP32-feasible:
+// with q of them, a group of 2^lw lanes (2^lw * q <= 32) evaluates one
+// point over its instance's lane schedule.  Most chunks of an instance
+// with several constraints hold no feasible point, so the few that do get
+// many lanes instead of running a long program on one.  The loop and the
+// shuffles are warp-uniform: every lane of a warp takes the same passes.
 __global__ void __launch_bounds__(kEvalThreads) batch_chunk_kernel(const BatchCfg c, const BatchBufs b)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -728,58 +744,106 @@ __global__ void __launch_bounds__(kEvalThreads) batch_chunk_kernel(const BatchCf
   t.slo = base + (size_t)c.n_max * B;
   t.shi = t.slo;
   t.stride = B;
-  t.tid = threadIdx.x;
+  t.tid = threadIdx.x;  // every lane stages its group's point in its own column
   const uint64_t per_slot = (c.child_stride + 31) >> 5;
-  for (uint64_t idx = (uint64_t)blockIdx.x * B + threadIdx.x; idx < c.K * per_slot; idx += (uint64_t)gridDim.x * B) {
-    const uint64_t slot = idx / per_slot, ch = idx % per_slot;
-    InstState* st = &b.st[slot];
-    const uint64_t nch = st->n_parents << c.log2C;
-    const uint64_t g0 = ch << 5;
-    if (g0 >= nch) continue;
-    const uint64_t g1 = nch < g0 + 32 ? nch : g0 + 32;
-    const uint64_t cbase = slot * c.child_stride;
-    float bv = INFINITY;
-    uint64_t bg = 0;
+  const uint64_t items = c.K * per_slot;
+  const int lg = lanes_per_box((b.child_base[c.K] + 31) >> 5, c.sample_capacity, (int)b.child_base[c.K + 1]);
+  const int lane = threadIdx.x & 31;
+  const uint64_t per_warp = 32u >> lg;
+  const uint64_t warps = (uint64_t)gridDim.x * (uint64_t)(B >> 5);
+  for (uint64_t w0 = ((uint64_t)blockIdx.x * (uint64_t)(B >> 5) + (threadIdx.x >> 5)) * per_warp; w0 < items;
+       w0 += warps * per_warp) {
+    // (1) lane i < per_warp: the pick of chunk w0 + i
+    bool need = false;
+    uint64_t slot = 0, bg = 0;
     uint32_t bi = 0;
-    for (uint64_t x = g0; x < g1; ++x) {
-      b.cval[cbase + x] = INFINITY;
-      const Best32 q = b.cbest[cbase + x];
-      if (q.value < bv) {
-        bv = q.value;
-        bg = x;
-        bi = q.i;
+    if ((uint64_t)lane < per_warp && w0 + lane < items) {
+      const uint64_t idx = w0 + lane;
+      slot = idx / per_slot;
+      const uint64_t ch = idx % per_slot;
+      const uint64_t nch = b.st[slot].n_parents << c.log2C;
+      const uint64_t g0 = ch << 5;
+      if (g0 < nch) {
+        const uint64_t g1 = nch < g0 + 32 ? nch : g0 + 32;
+        const uint64_t cbase = slot * c.child_stride;
+        float bv = INFINITY;
+        for (uint64_t x = g0; x < g1; ++x) {
+          b.cval[cbase + x] = INFINITY;
+          const Best32 q = b.cbest[cbase + x];
+          if (q.value < bv) {
+            bv = q.value;
+            bg = x;
+            bi = q.i;
+          }
+        }
+        if (bv < INFINITY) {
+          const uint64_t k = bg >> c.log2C, r = bg & ((1ULL << c.log2C) - 1ULL);
+          need = r < b.pinfo[slot * c.e_max + k].nreg;
+        }
       }
     }
-    if (!(bv < INFINITY)) continue;
-    const InstDesc& d = b.desc[slot];
+    // (2) the warp's lanes over the picks to evaluate; the barrier orders
+    // the +inf stores above before a group leader's store of the value
+    __syncwarp();
+    const unsigned m = __ballot_sync(0xffffffffu, need);
+    if (m == 0u) continue;
+    const int q = __popc(m);
+    int lw = 0;
+    while ((q << (lw + 1)) <= 32) ++lw;
+    const int G = 1 << lw, gl = lane & (G - 1);
+    const int src = nth_set_lane(m, lane >> lw);
+    const int from = src < 0 ? lane : src;
+    slot = __shfl_sync(0xffffffffu, slot, from);
+    bg = __shfl_sync(0xffffffffu, bg, from);
+    bi = __shfl_sync(0xffffffffu, bi, from);
+    const bool act = src >= 0;
+    PointVerdict pv;
+    pv.obj = INFINITY;
+    pv.feasible = true;
+    pv.has_obj = false;
+    const InstDesc* d = act ? &b.desc[slot] : nullptr;
     const uint64_t k = bg >> c.log2C, r = bg & ((1ULL << c.log2C) - 1ULL);
-    const ParentInfo pi = b.pinfo[slot * c.e_max + k];
-    if (r >= pi.nreg) continue;
-    const bool fathom = pi.fathom != 0;
-    const SlotPlan* sp = b.slots + (slot * c.e_max + k) * c.max_slots;
-    const uint64_t salt = st->salt_base + k + 1;
-    for (int v = 0; v < d.n_vars; ++v) {
-      double hi;
-      const double lo = child_bound(c, b, slot, k, r, v, sp, pi.count, hi);
-      t.lo[v * B + t.tid] = fathom ? lo : sample_value(d.kinds[v] != 0, lo, hi, (uint64_t)v, bi, r, salt);
-    }
-    const PointVerdict pv = run_point_ordered(d.prog64, d.prog_len, d.sched, t);
-    double value = (pv.feasible && !(pv.obj != pv.obj)) ? pv.obj : INFINITY;
-    if (fathom && value < INFINITY) {
-      bool ok = true;
-      for (int v = 0; v < d.n_vars && ok; ++v) {
-        const double x = t.lo[v * B + t.tid];
-        if (!(x >= d.root_lb[v]) || !(x <= d.root_ub[v])) ok = false;
-        else if (d.kinds[v] != 0 && fabs(__dsub_rn(x, rint(x))) > 1e-6) ok = false;
+    ParentInfo pi = {0, 0, 0};
+    if (act) {
+      pi = b.pinfo[slot * c.e_max + k];
+      const bool fathom = pi.fathom != 0;
+      const SlotPlan* sp = b.slots + (slot * c.e_max + k) * c.max_slots;
+      const uint64_t salt = b.st[slot].salt_base + k + 1;
+      for (int v = 0; v < d->n_vars; ++v) {
+        double hi;
+        const double lo = child_bound(c, b, slot, k, r, v, sp, pi.count, hi);
+        t.lo[v * B + t.tid] = fathom ? lo : sample_value(d->kinds[v] != 0, lo, hi, (uint64_t)v, bi, r, salt);
       }
-      if (!ok) {
-        if (value < st->gub) atomicAdd((unsigned long long*)&st->counters.witness_rejected, 1ULL);
-        value = INFINITY;
+      int li = 0;
+      while (li < lw && (2 << li) <= d->g_max) ++li;
+      if (d->sched == nullptr || li == 0) {
+        if (gl == 0) pv = run_point_ordered(d->prog64, d->prog_len, d->sched, t);
+      } else if (gl < (1 << li)) {
+        pv = run_point_lane(d->prog64, d->sched, li, gl, t);
       }
     }
-    const uint64_t S = fathom ? 1 : c.S;
-    b.cval[cbase + bg] = value;
-    b.ce[cbase + bg] = r * S + bi;
+    if (lw > 0) pv = group_point_verdict(pv, G);
+    if (act && gl == 0) {
+      InstState* st = &b.st[slot];
+      const bool fathom = pi.fathom != 0;
+      double value = (pv.feasible && !(pv.obj != pv.obj)) ? pv.obj : INFINITY;
+      if (fathom && value < INFINITY) {
+        bool ok = true;
+        for (int v = 0; v < d->n_vars && ok; ++v) {
+          const double x = t.lo[v * B + t.tid];
+          if (!(x >= d->root_lb[v]) || !(x <= d->root_ub[v])) ok = false;
+          else if (d->kinds[v] != 0 && fabs(__dsub_rn(x, rint(x))) > 1e-6) ok = false;
+        }
+        if (!ok) {
+          if (value < st->gub) atomicAdd((unsigned long long*)&st->counters.witness_rejected, 1ULL);
+          value = INFINITY;
+        }
+      }
+      const uint64_t S = fathom ? 1 : c.S;
+      const uint64_t cbase = slot * c.child_stride;
+      b.cval[cbase + bg] = value;
+      b.ce[cbase + bg] = r * S + bi;
+    }
   }
 }
 

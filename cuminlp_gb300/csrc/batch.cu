@@ -91,6 +91,7 @@ struct cmn_batch {
   uint64_t alloc_bytes = 0;
   bool fresh = false;  // h_st matches the device: nothing enqueued since pull()
   int eval_grid = 1;
+  BatchGrids grids;
   uint64_t kernels_per_iter = 0;
   cudaEvent_t marks[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
 
@@ -233,6 +234,8 @@ extern "C" cmn_status cmn_batch_create(const cmn_batch_config* config, cmn_batch
       A(&b.inc_common, 2 * K * (uint64_t)c.seg_max * c.e_max);
       A(&b.inc_parts, 2 * K * (uint64_t)c.seg_max * child_stride);
       A(&b.cbest, G);
+      A(&b.vrun, K + 2);
+      A(&b.vlg, K);
     }
     A(&b.pdepth, K * c.e_max);
     A(&b.pinfo, K * c.e_max);
@@ -282,10 +285,11 @@ extern "C" cmn_status cmn_batch_create(const cmn_batch_config* config, cmn_batch
     c.g_max = 32;
     c.eval_capacity = (uint64_t)s->eval_grid * kEvalThreads;
     c.sample_capacity = c.eval_capacity;
+    s->grids = batch_grids(c, s->eval_grid);
     for (int i = 0; i < 5 && e == cudaSuccess; ++i) e = cudaEventCreate(&s->marks[i]);
     if (e == cudaSuccess) e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-      cudaError_t e2 = batch_iteration(c, b, s->eval_grid, s->stream, s->marks);
+      cudaError_t e2 = batch_iteration(c, b, s->grids, s->stream, s->marks);
       e = cudaStreamEndCapture(s->stream, &s->graph);
       if (e2 != cudaSuccess) e = e2;
     }

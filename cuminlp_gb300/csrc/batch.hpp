@@ -129,14 +129,29 @@ struct BatchBufs {
   float* inc_common;   // [K][seg_max][e_max] (lo, hi): chain sums without split variables
   float* inc_parts;    // [K][seg_max][2^B][e_max] (lo, hi): per slot part (incremental children)
   Best32* cbest;       // [K][child_stride] the FP32 screen's best sample per child
+  // the verdict's warp runs: per `order` position the exclusive prefix of
+  // its runs, then the total and the ticket the warps draw runs from
+  uint64_t* vrun;      // [K + 2]
+  uint8_t* vlg;        // [K] log2 of the lanes per parent of each position
 };
 
 // Puts `slot`'s root box in its pool and resets its state.
 cudaError_t batch_init_slot(const BatchCfg& cfg, const BatchBufs& b, uint64_t slot, double gub0, cudaStream_t s);
+// Blocks of the grid-stride launches of an iteration.  `eval` serves the
+// evaluators, the verdict and the samplers (their lane groups size
+// themselves to it); the lazy form's FP32 sum and screen passes use fewer
+// registers and take as many blocks as stay resident on the GPU.
+struct BatchGrids {
+  int eval = 1;
+  int inc_common = 1;
+  int inc_parts = 1;
+  int screen = 1;
+};
+BatchGrids batch_grids(const BatchCfg& cfg, int eval_grid);
 // Enqueues one iteration over every active instance (capturable).
 // `marks` (5 events or null) are recorded at the phase boundaries: start,
 // after select + branch, after bound, after sample, after finish.
-cudaError_t batch_iteration(const BatchCfg& cfg, const BatchBufs& b, int eval_grid, cudaStream_t s,
+cudaError_t batch_iteration(const BatchCfg& cfg, const BatchBufs& b, const BatchGrids& grids, cudaStream_t s,
                             const cudaEvent_t* marks);
 size_t batch_eval_smem(const BatchCfg& cfg, bool fp32);
 size_t batch_sample_smem(const BatchCfg& cfg);

@@ -6,6 +6,7 @@
 // FP64, or FP32 screen + FP64 certify) -> sample (one launch) -> finish
 // (block per instance: ArgMin, incumbent and witness, prune, append kept
 // children, evict above the cap, pool minimum, adaptive screen).
+#include <algorithm>
 #include <cfloat>
 #include <cstdint>
 
@@ -321,49 +322,121 @@ __global__ void batch_branch_kernel(const BatchCfg c, const BatchBufs b)
 // taken in `order`, into child_base[0..K]; child_base[K] is this
 // iteration's live child count and child_base[K + 1] the most lanes any
 // live instance can use per child.
+//
+// The lazy form's verdict takes its parents in warp runs: a run is one
+// warp over 32 >> lg parents of one instance, 2^lg lanes per parent.  lg
+// is chosen per instance: the capacity's lanes when few parents are live,
+// and more for a long program, until a run is at most half of a warp's
+// fair share of the verdict's work (the parents' program lengths over the
+// grid's warps), within the lanes the instance's schedule has.  vrun gets
+// the runs' exclusive prefix by `order` position and their total, vlg each
+// position's lg, and the run ticket is reset.
 __global__ void __launch_bounds__(1024) batch_live_kernel(const BatchCfg c, const BatchBufs b)
 {
-  __shared__ uint64_t wsum[32];
-  __shared__ uint64_t carry;
+  __shared__ uint64_t wsum[32], wrun[32];
+  __shared__ uint64_t carry, rcarry;
   __shared__ int gmax;
+  __shared__ unsigned long long work, parents;
   if (threadIdx.x == 0) {
     carry = 0;
+    rcarry = 0;
     gmax = 1;
+    work = 0;
+    parents = 0;
   }
   __syncthreads();
+  const bool runs = b.vrun != nullptr;
   int my_gmax = 1;
-  for (uint64_t i = threadIdx.x; i < c.K; i += 1024)
-    if (b.st[i].n_parents > 0 && b.desc[i].g_max > my_gmax) my_gmax = b.desc[i].g_max;
+  unsigned long long my_work = 0, my_par = 0;
+  for (uint64_t i = threadIdx.x; i < c.K; i += 1024) {
+    const uint64_t np = b.st[i].n_parents;
+    if (np > 0 && b.desc[i].g_max > my_gmax) my_gmax = b.desc[i].g_max;
+    my_work += np * (uint64_t)b.desc[i].prog_len;
+    my_par += np;
+  }
   atomicMax(&gmax, my_gmax);
+  if (runs) {
+    atomicAdd(&work, my_work);
+    atomicAdd(&parents, my_par);
+  }
+  __syncthreads();
+  int lg_cap = 0;
+  unsigned long long half_share = 0;
+  if (runs) {
+    lg_cap = lanes_per_box(parents, c.eval_capacity, min(gmax, c.g_max));
+    const unsigned long long warps = c.eval_capacity >> 5 > 0 ? c.eval_capacity >> 5 : 1;
+    half_share = work / (64ULL * warps);  // (work / 32 lanes / warps) / 2
+    if (half_share < 64) half_share = 64;
+  }
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (uint64_t base = 0; base < c.K; base += 1024) {
     const uint64_t i = base + threadIdx.x;
-    const uint64_t v = i < c.K ? (b.st[b.order[i]].n_parents << c.log2C) : 0;
-    uint64_t x = v;
-    for (int off = 1; off < 32; off <<= 1) {
-      const uint64_t y = __shfl_up_sync(0xffffffffu, x, off);
-      if (lane >= off) x += y;
+    uint64_t v = 0, u = 0;
+    int lgi = 0;
+    if (i < c.K) {
+      const uint32_t slot = b.order[i];
+      const uint64_t np = b.st[slot].n_parents;
+      v = np << c.log2C;
+      if (runs && np > 0) {
+        const InstDesc& d = b.desc[slot];
+        int lim = 0;
+        while (lim < 5 && (2 << lim) <= d.g_max) ++lim;
+        int l = 0;
+        while (l < lim && ((unsigned long long)d.prog_len >> l) > half_share) ++l;
+        lgi = max(l, min(lg_cap, lim));
+        u = ((np << lgi) + 31) >> 5;
+      }
     }
-    if (lane == 31) wsum[wid] = x;
+    uint64_t x = v, y = u;
+    for (int off = 1; off < 32; off <<= 1) {
+      const uint64_t xa = __shfl_up_sync(0xffffffffu, x, off);
+      const uint64_t ya = __shfl_up_sync(0xffffffffu, y, off);
+      if (lane >= off) {
+        x += xa;
+        y += ya;
+      }
+    }
+    if (lane == 31) {
+      wsum[wid] = x;
+      wrun[wid] = y;
+    }
     __syncthreads();
     if (wid == 0) {
-      uint64_t w = wsum[lane];
+      uint64_t w = wsum[lane], z = wrun[lane];
       for (int off = 1; off < 32; off <<= 1) {
-        const uint64_t y = __shfl_up_sync(0xffffffffu, w, off);
-        if (lane >= off) w += y;
+        const uint64_t wa = __shfl_up_sync(0xffffffffu, w, off);
+        const uint64_t za = __shfl_up_sync(0xffffffffu, z, off);
+        if (lane >= off) {
+          w += wa;
+          z += za;
+        }
       }
       wsum[lane] = w;
+      wrun[lane] = z;
     }
     __syncthreads();
-    const uint64_t cy = carry;
-    if (i < c.K) b.child_base[i] = cy + (wid > 0 ? wsum[wid - 1] : 0) + x - v;
+    const uint64_t cy = carry, ry = rcarry;
+    if (i < c.K) {
+      b.child_base[i] = cy + (wid > 0 ? wsum[wid - 1] : 0) + x - v;
+      if (runs) {
+        b.vrun[i] = ry + (wid > 0 ? wrun[wid - 1] : 0) + y - u;
+        b.vlg[i] = (uint8_t)lgi;
+      }
+    }
     __syncthreads();
-    if (threadIdx.x == 0) carry = cy + wsum[31];
+    if (threadIdx.x == 0) {
+      carry = cy + wsum[31];
+      rcarry = ry + wrun[31];
+    }
     __syncthreads();
   }
   if (threadIdx.x == 0) {
     b.child_base[c.K] = carry;
     b.child_base[c.K + 1] = (uint64_t)min(gmax, c.g_max);
+    if (runs) {
+      b.vrun[c.K] = rcarry;
+      b.vrun[c.K + 1] = 0;
+    }
   }
 }
 
@@ -446,13 +519,12 @@ __device__ __forceinline__ bool slot_var_before_b(const SlotPlan* sp, int j, int
 }
 
 // FP64 verdict of every staged parent (fused terms, as mode 6 of the
-// single-instance evaluator): plb, pfeas.  The launch walks the live
-// parents (child_base >> B), with 2^lg lanes per parent when there are few
-// of them (the program's lane schedule; the verdict is the same).  Live
-// parents come longest program first, and the launch has about one pass:
-// the warps' runs of consecutive parents (mostly one instance, so one
-// instruction stream per warp) go to the blocks in turn, so every SM gets
-// long and short programs alike.  The loop bound is per block, so every
+// single-instance evaluator): plb, pfeas.  Each warp draws warp runs
+// (batch_live_kernel's layout: 32 >> lg parents of one instance, 2^lg
+// lanes each over the program's lane schedule; the verdict is the same)
+// from a ticket, longest program first, until none is left: a warp that
+// finishes a short run takes the next, so the SMs end together and no
+// long program waits on one lane.  The ticket is warp-uniform, so every
 // lane of a warp reaches the shuffles.
 __global__ void __launch_bounds__(kEvalThreads) batch_verdict_kernel(const BatchCfg c, const BatchBufs b)
 {
@@ -466,22 +538,28 @@ __global__ void __launch_bounds__(kEvalThreads) batch_verdict_kernel(const Batch
   t.shi = base + (size_t)c.slots_max * B;
   t.stride = B;
   t.tid = threadIdx.x;
-  const uint64_t total = b.child_base[c.K] >> c.log2C;
-  const int lg = lanes_per_box(total, c.eval_capacity, (int)b.child_base[c.K + 1]);
-  const int G = 1 << lg;
-  const int lane = threadIdx.x & (G - 1);
-  const uint64_t per_block = (uint64_t)(B >> lg);
-  const uint64_t per_warp = (uint64_t)(32 >> lg), warps = (uint64_t)(B >> 5);
-  for (uint64_t pass = 0; pass * per_block * gridDim.x < total; ++pass) {
-    const uint64_t wslot = (pass * warps + (threadIdx.x >> 5)) * gridDim.x + blockIdx.x;
-    const uint64_t idx = wslot * per_warp + ((threadIdx.x & 31) >> lg);
-    const bool live = idx < total;
+  const uint64_t runs = b.vrun[c.K];
+  unsigned long long* ticket = reinterpret_cast<unsigned long long*>(b.vrun + c.K + 1);
+  const int wl = threadIdx.x & 31;
+  for (;;) {
+    unsigned long long w = 0;
+    if (wl == 0) w = atomicAdd(ticket, 1ULL);
+    w = __shfl_sync(0xffffffffu, w, 0);
+    if (w >= runs) break;
+    uint64_t pos = 0, hi = c.K;  // largest position with vrun[pos] <= w: it has runs
+    while (hi - pos > 1) {
+      const uint64_t mid = (pos + hi) >> 1;
+      if (b.vrun[mid] <= w) pos = mid;
+      else hi = mid;
+    }
+    const uint64_t slot = b.order[pos];
+    const int lg = b.vlg[pos];
+    const int G = 1 << lg;
+    const int lane = wl & (G - 1);
+    const uint64_t k = ((w - b.vrun[pos]) << (5 - lg)) + (uint64_t)(wl >> lg);
+    const bool live = k < b.st[slot].n_parents;
     Verdict<double> v = verdict_init<double>();
-    uint64_t slot = 0, k = 0;
     if (live) {
-      const uint64_t g = live_child(c, b, idx << c.log2C);
-      slot = g / c.child_stride;
-      k = (g % c.child_stride) >> c.log2C;
       const InstDesc& d = b.desc[slot];
       ChildVars<double, double> cv = {};
       cv.plo = b.plo + splane(c, slot, 0) + k;
@@ -1432,9 +1510,35 @@ static void mark(const cudaEvent_t* marks, int i, cudaStream_t s)
   if (marks) cudaEventRecordWithFlags(marks[i], s, cudaEventRecordExternal);
 }
 
-cudaError_t batch_iteration(const BatchCfg& c, const BatchBufs& b, int eval_grid, cudaStream_t s,
+// Blocks for a grid-stride launch of `kernel` over `items` threads' worth
+// of work: as many as stay resident on every SM, no more than the items
+// need.
+template <typename Kernel>
+static int resident_grid(Kernel kernel, size_t smem, uint64_t items)
+{
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, kEvalThreads, smem) != cudaSuccess) {
+    (void)cudaGetLastError();
+    n = 1;
+  }
+  const uint64_t need = (items + kEvalThreads - 1) / kEvalThreads;
+  return (int)std::max<uint64_t>(1, std::min<uint64_t>(need, (uint64_t)sm_count() * (uint64_t)std::max(1, n)));
+}
+
+BatchGrids batch_grids(const BatchCfg& c, int eval_grid)
+{
+  BatchGrids g;
+  g.eval = eval_grid;
+  g.inc_common = resident_grid(batch_inc_common_kernel, 0, c.K * (uint64_t)c.seg_max * c.e_max);
+  g.inc_parts = resident_grid(batch_inc_parts_kernel, 0, c.K * (c.e_max << c.log2C));
+  g.screen = resident_grid(batch_screen_kernel, batch_screen_smem(c), c.K * c.child_stride);
+  return g;
+}
+
+cudaError_t batch_iteration(const BatchCfg& c, const BatchBufs& b, const BatchGrids& grids, cudaStream_t s,
                             const cudaEvent_t* marks)
 {
+  const int eval_grid = grids.eval;
   mark(marks, 0, s);
   const int kb = (int)((c.K + 255) / 256);
   batch_begin_kernel<<<kb, 256, 0, s>>>(c, b);
@@ -1453,8 +1557,8 @@ cudaError_t batch_iteration(const BatchCfg& c, const BatchBufs& b, int eval_grid
     batch_verdict_kernel<<<eval_grid, kEvalThreads, batch_verdict_smem(c), s>>>(c, b);
     const uint64_t np2 = c.K * c.e_max;
     batch_drop_kernel<<<(int)((np2 + 255) / 256), 256, 0, s>>>(c, b);
-    batch_inc_common_kernel<<<eval_grid, kEvalThreads, 0, s>>>(c, b);
-    batch_inc_parts_kernel<<<eval_grid, kEvalThreads, 0, s>>>(c, b);
+    batch_inc_common_kernel<<<grids.inc_common, kEvalThreads, 0, s>>>(c, b);
+    batch_inc_parts_kernel<<<grids.inc_parts, kEvalThreads, 0, s>>>(c, b);
     batch_eval_kernel<float, 5><<<eval_grid, kEvalThreads, batch_eval_smem(c, true), s>>>(c, b);
     const int lg = (int)((c.K * c.child_stride + 511) / 512);
     batch_list_count_kernel<<<lg, 512, 0, s>>>(c, b);
@@ -1462,7 +1566,7 @@ cudaError_t batch_iteration(const BatchCfg& c, const BatchBufs& b, int eval_grid
     batch_list_scatter_kernel<<<lg, 512, 0, s>>>(c, b);
     batch_eval_kernel<double, 3><<<eval_grid, kEvalThreads, batch_eval_smem(c, false), s>>>(c, b);
     mark(marks, 2, s);
-    batch_screen_kernel<<<eval_grid, kEvalThreads, batch_screen_smem(c), s>>>(c, b);
+    batch_screen_kernel<<<grids.screen, kEvalThreads, batch_screen_smem(c), s>>>(c, b);
     batch_chunk_kernel<<<eval_grid, kEvalThreads, batch_sample_smem(c), s>>>(c, b);
     mark(marks, 3, s);
     batch_finish_kernel<<<(int)c.K, kMiThreads, sort_smem_bytes(), s>>>(c, b);

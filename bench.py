@@ -30,7 +30,7 @@ and runnable alone with --only:
   reference headers were written out), beside this library's roles
   through the same adapter;
 - time_to_gap: the n=4 QCQP to the 1e-6 gap in every form;
-- config2_solver: solver steps on the n=32 MIQCQP in every form;
+- miqcqp_n32_solver: solver steps on the n=32 MIQCQP in every form;
 - batch_uneven: 1024 uneven instances in one batch;
 - serving: a Poisson request stream;
 - fp32_screen_check: FP64 points inside FP32 enclosures, and per-node width
@@ -59,23 +59,23 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-EVAL_DRAM_BYTES_PER_BOX = (43186688 + 34048) / 1048576  # ncu, eval_children_kernel<double, 1>, config 2
-# ncu, config 3 at 2^14 parents x 2^4 children in a steady iteration
-# (profiles/lazy_form_kernels_config3.md): DRAM bytes per child box of the
+EVAL_DRAM_BYTES_PER_BOX = (43186688 + 34048) / 1048576  # ncu, eval_children_kernel<double, 1>, n=32 MIQCQP
+# ncu, the n=64 MIQCQP at 2^14 parents x 2^4 children in a steady iteration
+# (profiles/lazy_form_kernels_miqcqp_n64.md): DRAM bytes per child box of the
 # FP32 bound (inc_common + inc_parts + eval_children_inc, reads and writes)
 # and per sample point of sample_screen_kernel, scaled by the units of a
 # launch
 INC32_DRAM_BYTES_PER_BOX = (10849280 + 11762688 + 2355968 + 59540224 + 154368) / 262144
 SCREEN32_DRAM_BYTES_PER_POINT = 20065792 / 262144
-# time-to-gap on config 1: the cluster of boxes within 1e-6 of the optimum
+# time-to-gap on the n=4 QCQP: the cluster of boxes within 1e-6 of the optimum
 # holds tens of millions of boxes at n=4, so the frontier is capped at 2^25;
 # 2^21 parents x 2^2 children per iteration timed best (swept over
 # B in 1..4 and 2^16..2^23 parents)
 TTG_B, TTG_E, TTG_CAP = 2, 1 << 21, 1 << 25
 E_PARENTS = 1 << 16
 B_BITS = 4
-CAP = 1 << 20          # config 2
-CONFIG3_CAP = 1 << 22  # config 3, the headline
+N32_CAP = 1 << 20  # the n=32 MIQCQP
+N64_CAP = 1 << 22  # the n=64 MIQCQP, the headline
 E2E_B = 20
 FORMS = ("fp64", "lazy", "fp32")  # plain, lazy certification, screen + certify every survivor
 
@@ -90,14 +90,14 @@ def parse_args():
     ap.add_argument("--quick", action="store_true",
                     help="solver steps only (no e2e, CPU baseline or time-to-gap): the profiling command")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--no-batch", action="store_true", help="skip the 1024-instance batch (config 4)")
-    ap.add_argument("--no-serve", action="store_true", help="skip the serving stream (config 5)")
-    ap.add_argument("--no-config2", action="store_true", help="skip the n=32 solver steps (config 2)")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 1024-instance uneven batch")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving stream")
+    ap.add_argument("--no-n32", action="store_true", help="skip the n=32 MIQCQP solver steps")
     ap.add_argument("--no-reference-gpu", action="store_true",
                     help="skip the reference's own CUDA graph backend on this GPU")
     ap.add_argument("--no-screen-check", action="store_true",
-                    help="skip the FP32 screen containment / width-inflation check (config 3)")
-    ap.add_argument("--only", choices=["batch", "serve", "ttg", "screen", "config2", "refgpu"],
+                    help="skip the FP32 screen containment / width-inflation check (n=64)")
+    ap.add_argument("--only", choices=["batch", "serve", "ttg", "screen", "n32", "refgpu"],
                     help="run one of the extra workloads alone")
     ap.add_argument("--instances", type=int, default=1024, help="--only batch: instances in the batch")
     ap.add_argument("--precision", choices=["fp64", "fp32", "lazy"], help="--only batch / ttg: one form only")
@@ -300,7 +300,7 @@ def cpu_info(path: str = "/proc/cpuinfo"):
 
 
 # ------------------------------------------------------------- GPU side
-def solver_run(dp, rt, precision, steps, warmup, e=E_PARENTS, b=B_BITS, cap=CAP):
+def solver_run(dp, rt, precision, steps, warmup, e=E_PARENTS, b=B_BITS, cap=N32_CAP):
     from cuminlp_gb300.solver import Solver
     s = Solver(dp, bisection_budget=b, batch_parents=e, frontier_cap=cap, precision=precision, sample_points=1)
     # ramp from the root until the pool holds a full batch of parents
@@ -421,7 +421,7 @@ def batch_run(rt, precision, steps, warmup, n_inst=1024):
     iterations, each iteration one captured graph over every instance."""
     from cuminlp_gb300 import generators as G
     from cuminlp_gb300.solver import Batch, DeviceProblem
-    dps = [DeviceProblem(G.config4_instance(i)) for i in range(n_inst)]
+    dps = [DeviceProblem(G.uneven_qcqp(i)) for i in range(n_inst)]
     n_max = max(dp.n_vars for dp in dps)
     slots = max(dp.info()["program_slots"] for dp in dps)
     b = Batch(n_inst, n_max, slots, precision=precision, **BATCH_OPTS)
@@ -451,8 +451,8 @@ SERVE_OPTS = dict(bisection_budget=4, batch_parents=64, frontier_cap=2048, sampl
 SERVE_BUDGET = 120 * (1 << 30)
 SERVE_ITER_LIMIT = 64 * 32  # expansions per request: at most 32 full iterations
 SERVE_RUNS = ((100, 300), (1000, 1500), (10000, 6000))  # (arrivals per second, requests)
-# Time to the 1e-6 gap is served on the n=4 QCQP shape of config 1 (fresh
-# instances): the config-5 mix's requests of n >= 8 rarely prove that gap
+# Time to the 1e-6 gap is served on the n=4 QCQP shape (fresh instances):
+# the serving mix's requests of n >= 8 rarely prove that gap
 # within a bounded budget (the oracle proves 4 of 16 n=8 requests within
 # 262,144 expansions at a 2^15 pool), while 31 of 40 n=4 instances prove
 # within 131,072 at the largest pool a batch slot takes (8192 entries, less
@@ -468,21 +468,21 @@ SERVE_TTG_MIN_PROVED = 100  # p99 is reported over at least this many proofs
 
 
 def serving_ttg_run():
-    """Time to the 1e-6 gap under a Poisson stream of n=4 QCQPs (config-1
-    shape, instances 1000 on) at 100 arrivals per second."""
+    """Time to the 1e-6 gap under a Poisson stream of n=4 QCQPs (instances
+    1000 on) at 100 arrivals per second."""
     from cuminlp_gb300 import generators as G
     from cuminlp_gb300.solver import DeviceProblem
     rate, n, limit = SERVE_TTG
-    dps = [DeviceProblem(G.config1(1000 + i)) for i in range(n)]
+    dps = [DeviceProblem(G.qcqp_n4(1000 + i)) for i in range(n)]
     out = serving_run(rate, n, dps, iter_limit=limit, classes=SERVE_TTG_CLASSES, opts=SERVE_TTG_OPTS)
-    out["workload"] = (f"n=4 QCQPs of the config-1 generator (instances 1000..{1000 + n - 1}), {rate} arrivals per "
+    out["workload"] = (f"n=4 QCQPs of the seeded generator (instances 1000..{1000 + n - 1}), {rate} arrivals per "
                        f"second, one size class of {SERVE_TTG_CLASSES[0][1]} slots, pool cap 7168 per request, at "
                        f"most {limit} expansions each")
     return out
 
 
 def serving_workload() -> str:
-    return ("config5: Poisson arrivals, n in {8,16,32,64} (0.4/0.3/0.2/0.1), m = n/2, 10% integers; lazy form "
+    return ("Poisson arrivals, n in {8,16,32,64} (0.4/0.3/0.2/0.1), m = n/2, 10% integers; lazy form "
             f"(FP32 bounds, FP64 verdict of each expanded box); 64 parents x 2^4 children per request per iteration, "
             f"per-request limit "
             f"{SERVE_ITER_LIMIT} expansions, gap 1e-6; size classes (max_vars, slots) {SERVE_CLASSES}; "
@@ -550,15 +550,15 @@ def forms_summary(res: dict, steps: int) -> dict:
     return out
 
 
-def config2_run(rt, steps, warmup) -> dict:
+def miqcqp_n32_run(rt, steps, warmup) -> dict:
     """Solver steps on the n=32 MIQCQP in every form: 2^16 parents x 2^4
     children per step, frontier cap 2^20 boxes."""
     from cuminlp_gb300 import generators as G
     from cuminlp_gb300.solver import DeviceProblem
-    dp = DeviceProblem(G.config2(0))
-    res = {p: solver_run(dp, rt, p, steps, warmup, cap=CAP) for p in FORMS}
+    dp = DeviceProblem(G.miqcqp_n32(0))
+    res = {p: solver_run(dp, rt, p, steps, warmup, cap=N32_CAP) for p in FORMS}
     f = forms_summary(res, steps)
-    return {"workload": "config2: n=32 MIQCQP (4 int [0,7], 28 cont [-5,5]), dense Q, m=16 at 20%; "
+    return {"workload": "n=32 MIQCQP (4 int [0,7], 28 cont [-5,5]), dense Q, m=16 at 20%; "
                         f"{E_PARENTS} parents x 2^{B_BITS} children per step; frontier cap 2^20",
             "flops_per_box": dp.info()["flops_per_box"], "plain_fp64": f["fp64"], "lazy": f["lazy"],
             "fp32_screen_fp64_certify": f["fp32"],
@@ -568,8 +568,8 @@ def config2_run(rt, steps, warmup) -> dict:
 
 
 REF_GPU = ROOT / "oracle" / "_ref" / "ref_gpu"
-# iteration cap of the reference driver over the host-core roles on config 1,
-# instance 0 (about 15 s of host time)
+# iteration cap of the reference driver over the host-core roles on the n=4
+# QCQP, instance 0 (about 15 s of host time)
 REF_DRIVER_ITER_CAP = 2_500_000
 
 
@@ -594,9 +594,9 @@ def reference_gpu_run() -> dict:
     node, captured as a CUDA graph; its device code compiled for sm_103a
     with the build's interval operators standing in for the missing
     cuinterval), beside this library's roles through the reference-side
-    adapter: bound() calls at 2^17 (config 3) and 2^19 (config 2) regions,
+    adapter: bound() calls at 2^17 (n=64 MIQCQP) and 2^19 (n=32) regions,
     both timed through the same interface with the box in and the verdicts
-    out; and the reference's SearchDriver to the 1e-6 gap on the config-1
+    out; and the reference's SearchDriver to the 1e-6 gap on the n=4 QCQP
     instance it proves, over either backend."""
     from cuminlp_gb300 import generators as G
     from tests.golden.make_golden import problem_text
@@ -604,19 +604,19 @@ def reference_gpu_run() -> dict:
         return {"unavailable": "oracle/_ref/ref_gpu not built (its reference headers are written where the "
                                "reference tree is mounted)"}
     out = {"label": "reference graph structure + the build's directed-rounding ops"}
-    for cfg, B in ((3, 17), (2, 19)):
-        r = _ref_gpu_call(["roles"], f"{B} 1 5 1 b 0x1p+0\n" + problem_text(G.CONFIGS[cfg]()))["kv"]
+    for n_vars, B in ((64, 17), (32, 19)):
+        r = _ref_gpu_call(["roles"], f"{B} 1 5 1 b 0x1p+0\n" + problem_text(G.BY_N[n_vars]()))["kv"]
         n = int(r["n_regions"][0])
         g = float(r["bound_seconds_graph"][0])
         ours = float(r["bound_seconds_gb300"][0])
-        out[f"config{cfg}_bound"] = {
+        out[f"miqcqp_n{n_vars}_bound"] = {
             "regions": n, "reference_graph_boxes_per_s": n / g, "gb300_roles_boxes_per_s": n / ours,
             "speedup": g / ours, "mismatched_feasible": int(r["bound_mismatch_feasible"][0]),
             "mismatched_lb": int(r["bound_mismatch_lb"][0]),
             "graph_build_s": float(r["bound_build_seconds_graph"][0])}
     def driver(backend, inst, iter_limit):
         head = f"B {iter_limit} 2 2 1 0 1 {(1e-6).hex()}\n"
-        lines = _ref_gpu_call(["driver", backend], head + problem_text(G.config1(inst)))["lines"]
+        lines = _ref_gpu_call(["driver", backend], head + problem_text(G.qcqp_n4(inst)))["lines"]
         h = lines[0].split()
         lb, ub = float.fromhex(h[0]), float.fromhex(h[1])
         return {"seconds": float(lines[3].split()[1]), "stop_reason": h[2], "proven_optimal": int(h[3]),
@@ -624,10 +624,10 @@ def reference_gpu_run() -> dict:
                 "expansions": int(lines[1].split()[0])}
 
     for backend in ("graph", "gb300", "oracle"):
-        out[f"time_to_gap_config1_instance1_{backend}"] = driver(backend, 1, 100000)
+        out[f"time_to_gap_qcqp_n4_instance1_{backend}"] = driver(backend, 1, 100000)
     # instance 0 needs about 10^8 single-box expansions in this driver; the
     # host-core run is capped and reports the gap it reached
-    out["time_to_gap_config1_instance0_oracle"] = driver("oracle", 0, REF_DRIVER_ITER_CAP)
+    out["time_to_gap_qcqp_n4_instance0_oracle"] = driver("oracle", 0, REF_DRIVER_ITER_CAP)
     out["driver"] = "reference SearchDriver, BisectionBudget B=2, one sample per region"
     out["backends"] = {"graph": "the reference's CUDA graph backend on this GPU",
                        "gb300": "this library's roles through include/cuminlp_gb300/region_backend.hpp",
@@ -646,7 +646,7 @@ def screen_check_run(seed: int = 5) -> dict:
     from cuminlp_gb300 import generators as G
     from cuminlp_gb300 import screen_check as S
     from cuminlp_gb300.solver import DeviceProblem
-    p = G.config3(0)
+    p = G.miqcqp_n64(0)
     rng = np.random.default_rng(seed)
     t0 = time.perf_counter()
     dp = DeviceProblem(p)
@@ -655,7 +655,7 @@ def screen_check_run(seed: int = 5) -> dict:
     nodes = S.pick_nodes(p, 96, rng)
     scales = (1e-3, 1e-2, 1e-1)
     rows = S.width_inflation(p, [S.sample_boxes(p, 2048, rng, sc) for sc in scales], nodes)
-    return {"workload": "config3: n=64 MIQCQP (8 int [0,15], 56 cont [-10,10]), Q 30% dense, m=32 at 10%",
+    return {"workload": "n=64 MIQCQP (8 int [0,15], 56 cont [-10,10]), Q 30% dense, m=32 at 10%",
             "point_containment": points,
             "width_inflation": S.inflation_summary(p, rows, [f"{sc:g}" for sc in scales]),
             "box_scale_meaning": "box half-widths uniform up to this share of the root width; 2048 boxes per scale",
@@ -686,25 +686,25 @@ def run_ours(args):
         return
     if args.only == "ttg":
         prec = args.precision or "fp64"
-        print(json.dumps({"config": "n=4 QCQP (config 1, instance 0)", "precision": prec,
-                          "run": time_to_gap(G.config1(0), prec, 20.0, args.ttg_iters)}))
+        print(json.dumps({"config": "n=4 QCQP (instance 0)", "precision": prec,
+                          "run": time_to_gap(G.qcqp_n4(0), prec, 20.0, args.ttg_iters)}))
         return
     if args.only == "screen":
         print(json.dumps(screen_check_run()))
         return
-    if args.only == "config2":
-        print(json.dumps(config2_run(rt, args.steps, args.warmup)))
+    if args.only == "n32":
+        print(json.dumps(miqcqp_n32_run(rt, args.steps, args.warmup)))
         return
     if args.only == "refgpu":
         print(json.dumps(reference_gpu_run()))
         return
     if args.only == "serve":
         from cuminlp_gb300.solver import DeviceProblem
-        dps = [DeviceProblem(G.config5_request(i)) for i in range(400)]
+        dps = [DeviceProblem(G.serving_qcqp(i)) for i in range(400)]
         print(json.dumps({"workload": serving_workload(), "runs": [serving_run(r, n, dps) for r, n in SERVE_RUNS],
                           "time_to_gap_run": serving_ttg_run()}))
         return
-    problem = G.config3(rank)  # replicas: one independent instance per GPU
+    problem = G.miqcqp_n64(rank)  # replicas: one independent instance per GPU
     dp = DeviceProblem(problem)
     info = dp.info()
     peak64 = fma_peak(0)
@@ -712,9 +712,9 @@ def run_ours(args):
 
     if args.quick:  # the profiling command: solver steps only
         e = args.parents or E_PARENTS
-        out = {"quick": True, "parents": e, "cap": args.cap or CONFIG3_CAP}
+        out = {"quick": True, "parents": e, "cap": args.cap or N64_CAP}
         for prec in args.forms.split(","):
-            r = solver_run(dp, rt, prec, args.steps, args.warmup, e=e, cap=args.cap or CONFIG3_CAP)
+            r = solver_run(dp, rt, prec, args.steps, args.warmup, e=e, cap=args.cap or N64_CAP)
             out[f"{prec}_ms"] = r["ms"]
             out[f"{prec}_boxes/s"] = r["delta"]["bounded"] / (r["ms"] * 1e-3)
             out[f"{prec}_phases_ms"] = forms_summary({prec: r}, args.steps)[prec]
@@ -729,7 +729,7 @@ def run_ours(args):
     with Clocks(local) as clk:
         for prec in FORMS:
             barrier(dist)
-            res[prec] = solver_run(dp, rt, prec, args.steps, args.warmup, cap=CONFIG3_CAP)
+            res[prec] = solver_run(dp, rt, prec, args.steps, args.warmup, cap=N64_CAP)
     clocks = clk.summary()
 
     lazy = res["lazy"]
@@ -792,10 +792,10 @@ def run_ours(args):
     cpu_v, cpu_s = cpu_rate(problem, args.cpu_seconds, cores)
 
     def ttg_leg():
-        out = {"config": f"n=4 QCQP (config 1, instances 0 and 1), gap 1e-6, 2^{TTG_B} children per parent, "
+        out = {"config": f"n=4 QCQP (instances 0 and 1), gap 1e-6, 2^{TTG_B} children per parent, "
                          f"{TTG_E} parents per iteration, frontier cap {TTG_CAP}, 20 s cap each"}
         for inst in (0, 1):
-            p1 = G.config1(inst)
+            p1 = G.qcqp_n4(inst)
             out[f"instance{inst}"] = {"fp64": time_to_gap(p1, "fp64", 20.0), "lazy": time_to_gap(p1, "lazy", 20.0),
                                       "fp32_screen_fp64_certify": time_to_gap(p1, "fp32", 20.0)}
             a, b = out[f"instance{inst}"]["fp64"], out[f"instance{inst}"]["lazy"]
@@ -806,14 +806,14 @@ def run_ours(args):
 
     def batch_leg():
         bres = {p: batch_run(rt, p, args.steps * 4, args.warmup) for p in ("fp64", "lazy", "fp32")}
-        return {"workload": "config4: 1024 uneven QCQPs, n ~ U{4..48}, m ~ U{0..24}, 0-25% integers; "
+        return {"workload": "1024 uneven QCQPs, n ~ U{4..48}, m ~ U{0..24}, 0-25% integers; "
                             "256 parents x 2^4 children per instance per step; pool cap 4096 per instance",
                 "lazy": bres["lazy"], "fp32_screen": bres["fp32"], "plain_fp64": bres["fp64"],
                 "lazy_speedup_vs_plain_fp64": bres["lazy"]["value"] / bres["fp64"]["value"],
                 "screen_speedup_vs_plain_fp64": bres["fp32"]["value"] / bres["fp64"]["value"]}
 
     def serving_leg():
-        dps = [DeviceProblem(G.config5_request(i)) for i in range(400)]
+        dps = [DeviceProblem(G.serving_qcqp(i)) for i in range(400)]
         return {"workload": serving_workload(), "runs": [serving_run(r, n, dps) for r, n in SERVE_RUNS],
                 "time_to_gap_run": serving_ttg_run()}
 
@@ -826,7 +826,7 @@ def run_ours(args):
     ref_gpu = None if args.no_reference_gpu else extra_leg(reference_gpu_run)
     tune = extra_leg(autotune_leg)
     ttg = None if args.no_ttg else extra_leg(ttg_leg)
-    config2 = None if args.no_config2 else extra_leg(config2_run, rt, args.steps, args.warmup)
+    n32 = None if args.no_n32 else extra_leg(miqcqp_n32_run, rt, args.steps, args.warmup)
     batch = None if args.no_batch else extra_leg(batch_leg)
     serving = None if args.no_serve else extra_leg(serving_leg)
     screen_check = None if args.no_screen_check else extra_leg(screen_check_run)
@@ -844,9 +844,9 @@ def run_ours(args):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32 (child bounds, sample ranking) + f64 (certification, incumbent)",
-        "data": "synthetic (seeded generator, config 3 shape)",
+        "data": "synthetic (seeded generator, n=64 MIQCQP shape)",
         "config": {
-            "workload": "config3: n=64 MIQCQP (8 int [0,15], 56 cont [-10,10]), Q 30% dense, m=32 at 10% density; "
+            "workload": "n=64 MIQCQP (8 int [0,15], 56 cont [-10,10]), Q 30% dense, m=32 at 10% density; "
                         f"frontier cap 2^22; {E_PARENTS} parents x 2^{B_BITS} children per step",
             "form": "lazy: children bounded in FP32 (outward), FP64 verdict of every box selected for expansion "
                     "and of survivors within 2^-10 * max(1, |incumbent|) below the incumbent; samples ranked in "
@@ -890,7 +890,7 @@ def run_ours(args):
         "reference_gpu": ref_gpu,
         "autotune": tune,
         "time_to_gap": ttg,
-        "config2_solver": config2,
+        "miqcqp_n32_solver": n32,
         "batch_uneven": batch,
         "serving": serving,
         "fp32_screen_check": screen_check,
@@ -904,7 +904,7 @@ def run_reference(args):
     if rank != 0:
         return
     from cuminlp_gb300 import generators as G
-    problem = G.config3(0)
+    problem = G.miqcqp_n64(0)
     model, cores = cpu_info()
     per_step = max(2.0, min(20.0, 90.0 / max(1, args.steps + args.warmup)))
     for _ in range(args.warmup):
@@ -921,8 +921,8 @@ def run_reference(args):
         "metric": "boxes/s (interval B&B box evaluations per second; FP32 bound with lazy FP64 certification)",
         "value": value, "unit": "boxes/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic (seeded generator, config 3 shape)",
-        "config": {"workload": "config3: n=64 MIQCQP, m=32; reference path (sample + bound of one parent's "
+        "dtype": "f64", "data": "synthetic (seeded generator, n=64 MIQCQP shape)",
+        "config": {"workload": "n=64 MIQCQP, m=32; reference path (sample + bound of one parent's "
                                "children per iteration, FP64) on the host cores"},
         "cpu_baseline": {"value": value, "unit": "boxes/s", "cores": cores, "kind": "port",
                          "sample": f"per step: sample + bound of {s['children_per_step']} children for "

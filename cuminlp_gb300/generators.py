@@ -10,7 +10,9 @@ matrices.
 Random numbers come from a SplitMix64 stream; a standard normal draw is
 the Irwin-Hall sum of twelve uniforms minus six (mean 0, variance 1).
 Both use integer and IEEE add/multiply only, so an instance is bit-for-bit
-the same on every host.  Seeds: 0xC0FFEE ^ (config << 32) ^ instance.
+the same on every host.  Seeds: 0xC0FFEE ^ (family << 32) ^ instance, where
+the family number is fixed per generator below (1: n=4 QCQP, 2: n=32
+MIQCQP, 3: n=64 MIQCQP, 4: uneven batch instances, 5: serving requests).
 """
 
 from __future__ import annotations
@@ -52,8 +54,8 @@ class SplitMix64:
         return lo + self.next() % (hi - lo + 1)
 
 
-def seed_for(config: int, instance: int = 0) -> int:
-    return 0xC0FFEE ^ (config << 32) ^ instance
+def seed_for(family: int, instance: int = 0) -> int:
+    return 0xC0FFEE ^ (family << 32) ^ instance
 
 
 @dataclass
@@ -119,28 +121,28 @@ def qcqp(spec: QCQPSpec, seed: int) -> Problem:
     return p
 
 
-# ---- the benchmark configurations -------------------------------------
-def config1(instance: int = 0) -> Problem:
+# ---- the benchmark workloads ------------------------------------------
+def qcqp_n4(instance: int = 0) -> Problem:
     """n=4 continuous in [-10,10]; Q, A dense symmetric N(0,1); c, b N(0,1);
     one constraint x^T A x + b^T x <= 5."""
     return qcqp(QCQPSpec(n=4, m=1, cont_lb=-10, cont_ub=10, rhs=(5.0, 5.0)), seed_for(1, instance))
 
 
-def config2(instance: int = 0) -> Problem:
+def miqcqp_n32(instance: int = 0) -> Problem:
     """n=32: 4 integers in [0,7] + 28 continuous in [-5,5]; Q dense; m=16
     constraints with A_i at 20% density, b_i N(0,1), r_i U[1,10]."""
     return qcqp(QCQPSpec(n=32, m=16, n_int=4, int_lb=0, int_ub=7, cont_lb=-5, cont_ub=5, q_density=1.0,
                          a_density=0.2, rhs=(1.0, 10.0)), seed_for(2, instance))
 
 
-def config3(instance: int = 0) -> Problem:
+def miqcqp_n64(instance: int = 0) -> Problem:
     """n=64: 8 integers in [0,15] + 56 continuous in [-10,10]; Q at 30%
     density; m=32 constraints at 10% density."""
     return qcqp(QCQPSpec(n=64, m=32, n_int=8, int_lb=0, int_ub=15, cont_lb=-10, cont_ub=10, q_density=0.3,
                          a_density=0.1, rhs=(1.0, 10.0)), seed_for(3, instance))
 
 
-def config4_instance(instance: int) -> Problem:
+def uneven_qcqp(instance: int) -> Problem:
     """One of the 1024 uneven instances: n ~ U{4..48}, m ~ U{0..24},
     integer share U[0, 0.25], densities U[0.1, 1.0], bounds [-10, 10]."""
     rng = SplitMix64(seed_for(4, instance) ^ 0x5A5A5A5A)
@@ -153,7 +155,7 @@ def config4_instance(instance: int) -> Problem:
                          a_density=ad, rhs=(1.0, 10.0)), seed_for(4, instance))
 
 
-def config5_request(instance: int) -> Problem:
+def serving_qcqp(instance: int) -> Problem:
     """A serving request: n in {8,16,32,64} with weights 0.4/0.3/0.2/0.1,
     m = n/2, 10% integers, densities U[0.1, 1.0]."""
     rng = SplitMix64(seed_for(5, instance) ^ 0xA5A5A5A5)
@@ -165,4 +167,5 @@ def config5_request(instance: int) -> Problem:
                          q_density=qd, a_density=ad, rhs=(1.0, 10.0)), seed_for(5, instance))
 
 
-CONFIGS = {1: config1, 2: config2, 3: config3}
+# the three single-problem workloads, keyed by their variable count
+BY_N = {4: qcqp_n4, 32: miqcqp_n32, 64: miqcqp_n64}

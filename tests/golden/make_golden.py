@@ -168,7 +168,7 @@ def fixture_problems():
     p.add_constraint(a + b, A.CMP_EQ, 5.0)
     out["int_eq"] = p
     for i in range(3):
-        out[f"qcqp_n4_{i}"] = G.config1(i)
+        out[f"qcqp_n4_{i}"] = G.qcqp_n4(i)
     out["miqcqp_n6"] = G.qcqp(G.QCQPSpec(n=6, m=2, n_int=2, int_lb=0, int_ub=3, cont_lb=-2, cont_ub=2,
                                          rhs=(1.0, 4.0)), G.seed_for(9, 0))
     return out

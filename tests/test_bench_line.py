@@ -79,11 +79,11 @@ def stubbed(monkeypatch):
     monkeypatch.setattr(bench, "batch_run", lambda *a, **k: {"value": 9e6})
     monkeypatch.setattr(bench, "serving_run", lambda *a, **k: {"latency_p99_ms": 1.0})
     monkeypatch.setattr(bench, "screen_check_run", lambda *a, **k: {"point_containment": []})
-    monkeypatch.setattr(bench, "config2_run", lambda *a, **k: {"plain_fp64": {"value": 17e6}})
-    monkeypatch.setattr(bench, "reference_gpu_run", lambda *a, **k: {"config3_bound": {"speedup": 2.0}})
+    monkeypatch.setattr(bench, "miqcqp_n32_run", lambda *a, **k: {"plain_fp64": {"value": 17e6}})
+    monkeypatch.setattr(bench, "reference_gpu_run", lambda *a, **k: {"miqcqp_n64_bound": {"speedup": 2.0}})
     monkeypatch.setattr(S, "DeviceProblem", _DeviceProblem)
-    small = G.config1(0)
-    monkeypatch.setattr(G, "config5_request", lambda i: small)
+    small = G.qcqp_n4(0)
+    monkeypatch.setattr(G, "serving_qcqp", lambda i: small)
     for k in ("WORLD_SIZE", "RANK", "LOCAL_RANK"):
         monkeypatch.delenv(k, raising=False)
 
@@ -121,16 +121,16 @@ def test_default_line_carries_the_contract(stubbed, monkeypatch):
     assert e["value"] == pytest.approx(5 * (1 << 20) / 0.325)
     assert d["gpu_launches"] == 42 * 5
     assert d["clocks"]["sm_mhz"] == 2070.0 and d["clocks"]["reasons"] == []
-    for k in ("time_to_gap", "batch_uneven", "serving", "fp32_screen_check", "config2_solver", "reference_gpu"):
+    for k in ("time_to_gap", "batch_uneven", "serving", "fp32_screen_check", "miqcqp_n32_solver", "reference_gpu"):
         assert d[k] is not None, k
     for k in ("plain_fp64", "lazy", "fp32_screen_fp64_certify", "roofline_plain_fp64"):
         assert k in d, k
 
 
 def test_skip_flags_leave_the_extra_legs_empty(stubbed, monkeypatch):
-    d = _line(monkeypatch, ["--no-ttg", "--no-batch", "--no-serve", "--no-screen-check", "--no-config2",
+    d = _line(monkeypatch, ["--no-ttg", "--no-batch", "--no-serve", "--no-screen-check", "--no-n32",
                             "--no-reference-gpu"])
-    for k in ("time_to_gap", "batch_uneven", "serving", "fp32_screen_check", "config2_solver", "reference_gpu"):
+    for k in ("time_to_gap", "batch_uneven", "serving", "fp32_screen_check", "miqcqp_n32_solver", "reference_gpu"):
         assert d[k] is None, k
     assert d["e2e"]["value"] > 0
 
@@ -145,10 +145,10 @@ def test_a_failing_extra_leg_is_recorded_not_fatal(stubbed, monkeypatch):
     def boom(*a, **k):
         raise RuntimeError("out of device memory")
 
-    monkeypatch.setattr(bench, "config2_run", boom)
+    monkeypatch.setattr(bench, "miqcqp_n32_run", boom)
     monkeypatch.setattr(bench, "batch_run", boom)
     d = _line(monkeypatch, ["--steps", "2", "--warmup", "1"])
-    assert d["config2_solver"] == {"error": "RuntimeError: out of device memory"}
+    assert d["miqcqp_n32_solver"] == {"error": "RuntimeError: out of device memory"}
     assert d["batch_uneven"] == {"error": "RuntimeError: out of device memory"}
     assert d["value"] > 0 and d["e2e"]["value"] > 0
     sv = d["serving"]

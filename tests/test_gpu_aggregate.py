@@ -25,10 +25,10 @@ def _built():
     build.build_library()
 
 
-def layout(cfg, k):
+def layout(n_vars, k):
     """(slot kinds, var ids, widths) with the branch slot last."""
     C = A.SLOT_CONTINUOUS
-    if cfg == 1:
+    if n_vars == 4:
         return [C, C, C], [1, 2, 0], [8, 4, k]
     return [C, C, C], [5, 6, 4], [16, 8, k]
 
@@ -55,17 +55,17 @@ def check(p, kinds, vids, widths, box, k):
 
 
 @pytest.mark.parametrize("k", [1, 2, 4, 16])
-@pytest.mark.parametrize("cfg", [1, 2])
-def test_bound_children_matches_oracle(cfg, k):
-    p = G.CONFIGS[cfg]()
-    kinds, vids, widths = layout(cfg, k)
+@pytest.mark.parametrize("n_vars", [4, 32])
+def test_bound_children_matches_oracle(n_vars, k):
+    p = G.BY_N[n_vars]()
+    kinds, vids, widths = layout(n_vars, k)
     lb, ub, fe = check(p, kinds, vids, widths, p.root_box(), k)
     assert np.all(lb[fe == 1] <= ub[fe == 1])
 
 
 def test_small_segments_span_warps():
     # M = 2: every warp holds 16 children, the per-lane atomic path
-    p = G.config1()
+    p = G.qcqp_n4()
     kinds = [A.SLOT_CONTINUOUS, A.SLOT_CONTINUOUS]
     _, _, fe = check(p, kinds, [1, 0], [2, 64], p.root_box(), 64)
     assert 0 < fe.sum() <= 64
@@ -81,7 +81,7 @@ def test_infeasible_children_are_normalised():
 
 
 def test_k_must_divide_regions():
-    p = G.config1()
+    p = G.qcqp_n4()
     b = Bounder(DeviceProblem(p), [A.SLOT_CONTINUOUS], 8)
     with pytest.raises(CmnError) as e:
         b.bound_children(p.root_box(), [0], [8], 3)

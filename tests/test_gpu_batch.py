@@ -35,10 +35,10 @@ def mixed_problems():
     ps = {
         "square_le5": fx["square_le5"], "infeasible": fx["infeasible"], "aggregate": fx["aggregate_fixture"],
         "contract": contract_model(), "int_eq": fx["int_eq"], "miqcqp_n6": fx["miqcqp_n6"],
-        "cfg1": G.config1(), "cfg1b": G.config1(1),
+        "qcqp_n4": G.qcqp_n4(), "qcqp_n4_1": G.qcqp_n4(1),
     }
     for i in range(6):
-        ps[f"cfg4_{i}"] = G.config4_instance(i)
+        ps[f"uneven_{i}"] = G.uneven_qcqp(i)
     return ps
 
 
@@ -114,7 +114,7 @@ def test_batch_lazy_matches_oracle_per_instance():
 
 def test_batch_lazy_matches_single_instance_solver():
     named = mixed_problems()
-    keep = {k: named[k] for k in ("aggregate", "contract", "miqcqp_n6", "cfg1b", "cfg4_0", "cfg4_3")}
+    keep = {k: named[k] for k in ("aggregate", "contract", "miqcqp_n6", "qcqp_n4_1", "uneven_0", "uneven_3")}
     shared = dict(SHARED, precision="lazy", sample_all=1)
     got = run_batch(keep, shared, dict(batch_iter_limit=30))
     for k, p in keep.items():
@@ -137,7 +137,7 @@ def test_batch_alone_equals_mixed():
 
 def test_batch_matches_single_instance_solver():
     named = mixed_problems()
-    keep = {k: named[k] for k in ("aggregate", "miqcqp_n6", "cfg1b", "cfg4_0", "cfg4_3")}
+    keep = {k: named[k] for k in ("aggregate", "miqcqp_n6", "qcqp_n4_1", "uneven_0", "uneven_3")}
     got = run_batch(keep, SHARED, dict(batch_iter_limit=30))
     for k, p in keep.items():
         s = Solver(DeviceProblem(p), batch_iter_limit=30, **SHARED)
@@ -176,7 +176,7 @@ def test_batch_solve_refills_slots():
 
 
 def test_batch_runs_to_convergence_like_the_oracle():
-    named = {k: v for k, v in mixed_problems().items() if k in ("square_le5", "cfg1", "cfg1b", "int_eq")}
+    named = {k: v for k, v in mixed_problems().items() if k in ("square_le5", "qcqp_n4", "qcqp_n4_1", "int_eq")}
     res = batch_solve(list(named.values()), iter_limit=100000, **SHARED)
     for (k, p), r in zip(named.items(), res):
         o = O.OracleProblem(p).solve_batched(iter_limit=100000, **SHARED)
@@ -184,14 +184,14 @@ def test_batch_runs_to_convergence_like_the_oracle():
 
 
 def test_batch_slot_errors():
-    p = DeviceProblem(G.config1())
+    p = DeviceProblem(G.qcqp_n4())
     b = Batch(2, 4, **SHARED)
     b.add(p)
     b.add(p)
     with pytest.raises(CmnError) as e:
         b.add(p)
     assert e.value.status_name == "OVER_BUDGET"
-    big = DeviceProblem(G.config2())
+    big = DeviceProblem(G.miqcqp_n32())
     b.release(0)
     with pytest.raises(CmnError) as e:
         b.add(big)

@@ -36,13 +36,12 @@ def check_eval(problem, n_boxes, seed, precision, scale=0.2):
 
 
 @pytest.mark.parametrize("precision", [A.PRECISION_FP64, A.PRECISION_FP32_SCREEN])
-@pytest.mark.parametrize("cfg", [1, 2, 3])
-def test_eval_boxes_match_oracle(cfg, precision):
-    p = G.CONFIGS[cfg]()
-    n = {1: 20000, 2: 3000, 3: 600}[cfg]
-    lb, ub, fe = check_eval(p, n, 100 + cfg, precision)
+@pytest.mark.parametrize("n_vars,boxes,seed", [(4, 20000, 101), (32, 3000, 102), (64, 600, 103)])
+def test_eval_boxes_match_oracle(n_vars, boxes, seed, precision):
+    p = G.BY_N[n_vars]()
+    lb, ub, fe = check_eval(p, boxes, seed, precision)
     assert np.all(lb <= ub)
-    if cfg == 1:
+    if n_vars == 4:
         assert 0 < fe.sum() < len(fe)  # both verdicts occur
 
 
@@ -53,9 +52,9 @@ def test_every_operator_matches_oracle(precision):
 
 @pytest.mark.parametrize("precision", [A.PRECISION_FP64, A.PRECISION_FP32_SCREEN])
 def test_node_enclosures_match_oracle(precision):
-    # each sampled node of config 2 as the objective: its enclosure on every
+    # each sampled node of the n=32 MIQCQP as the objective: its enclosure on every
     # box must equal the oracle's node-by-node evaluation
-    p = G.config2()
+    p = G.miqcqp_n32()
     rng = np.random.default_rng(5)
     cands = [n.id for n in p.graph.nodes if n.op not in (A.OP_CONST,)]
     picks = sorted(set(rng.choice(cands, 60, replace=False).tolist()) | {p.objective_root})
@@ -73,7 +72,7 @@ def test_node_enclosures_match_oracle(precision):
 
 
 def test_fp32_screen_contains_fp64():
-    p = G.config3()
+    p = G.miqcqp_n64()
     rng = np.random.default_rng(11)
     lo, hi = random_boxes(p, 2000, rng, 0.05)
     dp = DeviceProblem(p)
@@ -84,7 +83,7 @@ def test_fp32_screen_contains_fp64():
 
 
 def test_enclosure_contains_sampled_points():
-    p = G.config2()
+    p = G.miqcqp_n32()
     rng = np.random.default_rng(3)
     lo, hi = random_boxes(p, 256, rng, 0.1)
     dp = DeviceProblem(p)

@@ -25,10 +25,10 @@ def _built():
 
 
 def problems():
-    ps = {"cfg1": G.config1(), "cfg2": G.config2(), "cfg3": G.config3()}
+    ps = {"qcqp_n4": G.qcqp_n4(), "miqcqp_n32": G.miqcqp_n32(), "miqcqp_n64": G.miqcqp_n64()}
     for i in (0, 2, 10):
-        ps[f"cfg5_{i}"] = G.config5_request(i)
-    ps["cfg4_0"] = G.config4_instance(0)
+        ps[f"serving_{i}"] = G.serving_qcqp(i)
+    ps["uneven_0"] = G.uneven_qcqp(0)
     return ps
 
 
@@ -57,6 +57,6 @@ def test_grouped_equals_one_lane(name, precision):
 
 
 def test_segments_reported():
-    info = DeviceProblem(G.config2()).info()
+    info = DeviceProblem(G.miqcqp_n32()).info()
     assert info["program_segments"] == 17  # objective + 16 constraints
     assert info["lanes_per_box_max"] >= 4

@@ -107,12 +107,12 @@ def roles(problem, B: int, samples: int, n_salts: int, which: str = "bs", frac: 
     return out
 
 
-@pytest.mark.parametrize("cfg,B,S,frac", [(1, 10, 4, 1.0), (2, 12, 2, 1.0), (2, 12, 2, 0.05), (3, 10, 1, 1.0),
-                                          (3, 12, 2, 0.02)])
-def test_roles_match_reference_graph_backend(cfg, B, S, frac):
-    # the root boxes of configs 2 and 3 hold no feasible sample; the small
-    # boxes around the origin do, so the witnesses are compared there
-    r = roles(G.CONFIGS[cfg](), B, S, 4, frac=frac)
+@pytest.mark.parametrize("n_vars,B,S,frac", [(4, 10, 4, 1.0), (32, 12, 2, 1.0), (32, 12, 2, 0.05), (64, 10, 1, 1.0),
+                                             (64, 12, 2, 0.02)])
+def test_roles_match_reference_graph_backend(n_vars, B, S, frac):
+    # the root boxes of the n=32 and n=64 MIQCQPs hold no feasible sample;
+    # the small boxes around the origin do, so the witnesses are compared there
+    r = roles(G.BY_N[n_vars](), B, S, 4, frac=frac)
     assert int(r["n_regions"][0]) == 1 << B
     assert int(r["bound_mismatch_feasible"][0]) == 0
     assert int(r["bound_mismatch_lb"][0]) == 0

@@ -71,9 +71,9 @@ def test_sampler_determinism_and_salt():
     assert np.array_equal(l1, l2)
 
 
-@pytest.mark.parametrize("cfg,B", [(1, 8), (2, 10), (3, 6)])
-def test_roles_match_oracle(cfg, B):
-    p = G.CONFIGS[cfg]()
+@pytest.mark.parametrize("n_vars,B", [(4, 8), (32, 10), (64, 6)])
+def test_roles_match_oracle(n_vars, B):
+    p = G.BY_N[n_vars]()
     dp = DeviceProblem(p)
     op = O.OracleProblem(p)
     box = p.root_box()

@@ -1,4 +1,4 @@
-"""The FP32 screen against FP64 on the n=64 MIQCQP (config 3): 10^5 FP64
+"""The FP32 screen against FP64 on the n=64 MIQCQP: 10^5 FP64
 points per box inside the box's FP32 enclosure, and the FP32/FP64 width
 ratios node by node, checked against the oracle's node enclosures."""
 
@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 
 @pytest.mark.parametrize("scale,at_origin", [(0.01, False), (0.3, False), (0.03, True)])
 def test_fp64_points_lie_in_fp32_enclosures(scale, at_origin):
-    p = G.config3()
+    p = G.miqcqp_n64()
     # boxes around the origin, which satisfies every constraint (zero
     # quadratic and linear terms, rhs >= 1), hold FP64-feasible points
     centre = np.zeros(p.n_vars) if at_origin else None
@@ -30,7 +30,7 @@ def test_fp64_points_lie_in_fp32_enclosures(scale, at_origin):
 
 
 def test_width_inflation_matches_oracle_node_enclosures():
-    p = G.config3()
+    p = G.miqcqp_n64()
     rng = np.random.default_rng(9)
     nodes = S.pick_nodes(p, 16, rng)
     sets = [S.sample_boxes(p, 12, rng, s) for s in (1e-3, 1e-1)]

@@ -32,7 +32,7 @@ def _built():
 
 def requests():
     fx = fixture_problems()
-    ps = [G.config5_request(i) for i in range(14)] + [fx["square_le5"], fx["miqcqp_n6"], G.config1(1)]
+    ps = [G.serving_qcqp(i) for i in range(14)] + [fx["square_le5"], fx["miqcqp_n6"], G.qcqp_n4(1)]
     limits = [300 + 97 * (i % 7) for i in range(len(ps))]
     return ps, limits
 
@@ -125,13 +125,13 @@ def test_server_admits_by_pool_memory():
 
 def test_server_rejects_and_times_out():
     srv = Server([(8, 1)], **SHARED)
-    big = DeviceProblem(G.config5_request(3) if G.config5_request(3).n_vars > 8 else G.config2())
+    big = DeviceProblem(G.serving_qcqp(3) if G.serving_qcqp(3).n_vars > 8 else G.miqcqp_n32())
     with pytest.raises(CmnError) as e:
         srv.submit(big)
     assert e.value.status_name == "INVALID_CONFIGURATION"
     # a negative tolerance never closes the gap: the request runs until its
     # boxes degenerate, far longer than the wait
-    small = DeviceProblem(next(p for p in (G.config5_request(i) for i in range(20)) if p.n_vars == 8))
+    small = DeviceProblem(next(p for p in (G.serving_qcqp(i) for i in range(20)) if p.n_vars == 8))
     rid = srv.submit(small, iter_limit=10 ** 9, tolerance=-1.0)
     with pytest.raises(CmnError) as e:
         srv.wait(rid, timeout_ms=20)

@@ -34,7 +34,7 @@ def problems():
     return {
         "square_le5": fx["square_le5"], "infeasible": fx["infeasible"], "aggregate": fx["aggregate_fixture"],
         "contract": contract_model(), "int_eq": fx["int_eq"], "miqcqp_n6": fx["miqcqp_n6"],
-        "cfg1": G.config1(), "cfg1b": G.config1(1),
+        "qcqp_n4": G.qcqp_n4(), "qcqp_n4_1": G.qcqp_n4(1),
     }
 
 
@@ -73,7 +73,7 @@ def compare(p, iterations, room=1 << 20, **opts):
 
 
 @pytest.mark.parametrize("name", ["square_le5", "infeasible", "aggregate", "contract", "int_eq", "miqcqp_n6",
-                                  "cfg1"])
+                                  "qcqp_n4"])
 def test_solver_matches_oracle(name):
     p = problems()[name]
     compare(p, 12, bisection_budget=2, batch_parents=64, sample_points=2)
@@ -82,12 +82,12 @@ def test_solver_matches_oracle(name):
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32", "lazy"])
 def test_solver_matches_oracle_larger(precision):
-    compare(G.config1(), 30, bisection_budget=3, batch_parents=512, precision=precision)
-    compare(G.config1(2), 20, bisection_budget=4, batch_parents=256, precision=precision, relative_width=1)
+    compare(G.qcqp_n4(), 30, bisection_budget=3, batch_parents=512, precision=precision)
+    compare(G.qcqp_n4(2), 20, bisection_budget=4, batch_parents=256, precision=precision, relative_width=1)
 
 
 def test_eviction_matches_oracle():
-    g = compare(G.config1(1), 25, bisection_budget=3, batch_parents=128, frontier_cap=300)
+    g = compare(G.qcqp_n4(1), 25, bisection_budget=3, batch_parents=128, frontier_cap=300)
     assert g["counters"]["dropped_viable"] + g["counters"]["dropped_dominated"] > 0
 
 
@@ -109,7 +109,7 @@ def test_solver_matches_oracle_wider(instance):
     # the branching policy keeps its scratch in local memory up to 32
     # variables and in global scratch above; both against the oracle, with
     # a cap small enough to evict
-    compare(G.config4_instance(instance), 6, bisection_budget=3, batch_parents=48, frontier_cap=400,
+    compare(G.uneven_qcqp(instance), 6, bisection_budget=3, batch_parents=48, frontier_cap=400,
             sample_points=1)
 
 
@@ -121,7 +121,7 @@ def test_tied_lower_bounds_rank_by_position(cap):
 
 
 def test_fp32_screen_identical_certified_bounds():
-    p = G.config1()
+    p = G.qcqp_n4()
     dp = DeviceProblem(p)
     out = {}
     for prec in ("fp64", "fp32"):
@@ -142,7 +142,7 @@ def test_one_parent_per_iteration_reproduces_reference_driver():
     # search expands boxes in the reference SearchDriver's order: its bounds
     # after a fixed expansion budget equal the driver restatement's (which
     # the golden fixtures pin to the reference's own code)
-    for name, iters in (("aggregate", 4000), ("miqcqp_n6", 1500), ("cfg1", 1500)):
+    for name, iters in (("aggregate", 4000), ("miqcqp_n6", 1500), ("qcqp_n4", 1500)):
         p = problems()[name]
         s = Solver(DeviceProblem(p), bisection_budget=2, batch_parents=1, sample_all=1, iter_limit=iters)
         s.step(0)
@@ -154,10 +154,10 @@ def test_one_parent_per_iteration_reproduces_reference_driver():
 
 
 def test_batched_solver_certifies_the_reference_optimum():
-    # config-1 instance 1: the reference driver proves optimality (golden
+    # instance 1 of the n=4 QCQP: the reference driver proves optimality (golden
     # fixture); the batched search must certify the same optimum within the
     # solver's gap
-    p = G.config1(1)
+    p = G.qcqp_n4(1)
     ref = O.OracleProblem(p).solve_reference(iter_limit=20000, bisection_budget=3, sample_points=2, threads=1)
     assert ref["proven_optimal"] == 1
     for prec in ("fp64", "fp32"):
@@ -181,15 +181,15 @@ def test_batched_solver_certifies_the_reference_optimum():
 # (Measured on the GB300 host: the n = 32 case takes 14 s and the n = 64
 # case at 4 iterations 4 s, so both run to iteration 5.)
 @pytest.mark.parametrize("precision", ["fp64", "fp32", "lazy"])
-def test_solver_matches_oracle_config2_bench_shape(precision):
-    g = compare(G.config2(), 5, room=1 << 21, bisection_budget=4, batch_parents=1 << 16, frontier_cap=1 << 20,
+def test_solver_matches_oracle_miqcqp_n32_bench_shape(precision):
+    g = compare(G.miqcqp_n32(), 5, room=1 << 21, bisection_budget=4, batch_parents=1 << 16, frontier_cap=1 << 20,
                 sample_points=1, precision=precision)
     assert g["counters"]["expansions"] > (1 << 12)
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32", "lazy"])
-def test_solver_matches_oracle_config3_bench_shape(precision):
-    compare(G.config3(), 5, room=1 << 21, bisection_budget=4, batch_parents=1 << 16, frontier_cap=1 << 22,
+def test_solver_matches_oracle_miqcqp_n64_bench_shape(precision):
+    compare(G.miqcqp_n64(), 5, room=1 << 21, bisection_budget=4, batch_parents=1 << 16, frontier_cap=1 << 22,
             sample_points=1, precision=precision)
 
 
@@ -208,7 +208,7 @@ def test_lazy_form_certifies_the_plain_bounds(instance):
     # to the 1e-6 gap: the lazy form's certified bounds agree with the plain
     # FP64 form's within the solver's tolerance, and it spends FP64 on the
     # expanded boxes only
-    p = G.config1(instance)
+    p = G.qcqp_n4(instance)
     out = {}
     for prec in ("fp64", "lazy"):
         s = Solver(DeviceProblem(p), bisection_budget=2, batch_parents=1 << 21, frontier_cap=1 << 25,
@@ -235,16 +235,16 @@ def test_solver_n512_matches_oracle(precision):
     compare(wide_qcqp(), 4, bisection_budget=3, batch_parents=64, sample_points=1, precision=precision)
 
 
-@pytest.mark.parametrize("cfg", [1, 2, 3])
-def test_incremental_fp32_bounds_enclose_fp64(cfg):
+@pytest.mark.parametrize("n_vars,seed", [(4, 1), (32, 2), (64, 3)])
+def test_incremental_fp32_bounds_enclose_fp64(n_vars, seed):
     # the lazy form's incremental FP32 child bounds (common chain sums per
     # parent, split-variable terms per child) are sound: never above the
     # FP64 bound, and a constraint they prove violated is violated in FP64
-    p = G.CONFIGS[cfg]()
+    p = G.BY_N[n_vars]()
     dp = DeviceProblem(p)
     op = O.OracleProblem(p)
     assert op.set_program32(dp.program(1))
-    rng = np.random.default_rng(cfg)
+    rng = np.random.default_rng(seed)
     root = np.array(p.box_bounds)
     for _ in range(4):
         c = rng.uniform(root[:, 0], root[:, 1])
@@ -266,7 +266,7 @@ def test_autotuned_launch_shape_changes_no_result(precision):
     # cmn_autotune times launch shapes (blocks per SM, lanes per box); a
     # solver on the tuned shape must give the untuned solver's search bit
     # for bit
-    p = G.config1(2)
+    p = G.qcqp_n4(2)
     dp = DeviceProblem(p)
     t = dp.autotune(0 if precision == "fp64" else 1, 1 << 14)
     assert t["candidates"] >= 1 and t["blocks_per_sm"] >= 1 and t["lanes_cap"] >= 1

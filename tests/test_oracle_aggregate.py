@@ -44,7 +44,7 @@ def fold(lb, ub, fe, k):
 
 
 def test_aggregate_oracle_is_a_fold_of_box_evaluation():
-    for p, vids, widths, k in ((G.config1(), [1, 2, 0], [4, 4, 4], 4), (G.config1(3), [3, 0], [8, 2], 2),
+    for p, vids, widths, k in ((G.qcqp_n4(), [1, 2, 0], [4, 4, 4], 4), (G.qcqp_n4(3), [3, 0], [8, 2], 2),
                                (fixture_problems()["infeasible"], [0], [8], 4)):
         box = p.root_box()
         op = O.OracleProblem(p)

@@ -350,8 +350,7 @@ def test_batched_search_agrees_with_reference_driver():
 
 
 def test_batched_fp32_screen_matches_fp64():
-    for cfg in (1,):
-        p = G.CONFIGS[cfg]()
+    for p in (G.qcqp_n4(),):
         op = O.OracleProblem(p)
         a = op.solve_batched(iter_limit=3000, bisection_budget=3, batch_parents=64)
         b = op.solve_batched(iter_limit=3000, bisection_budget=3, batch_parents=64, precision="fp32")
@@ -364,7 +363,7 @@ def test_batched_fp32_screen_matches_fp64():
 
 
 def test_fp32_enclosure_contains_fp64():
-    p = G.config2()
+    p = G.miqcqp_n32()
     op = O.OracleProblem(p)
     rng = np.random.default_rng(9)
     root = p.root_box().reshape(-1, 2)
@@ -379,13 +378,13 @@ def test_fp32_enclosure_contains_fp64():
         assert np.all(hi32[ok].astype(np.float64) >= hi64[ok])
 
 
-@pytest.mark.parametrize("cfg", [1, 2, 3])
-def test_hardware_rounding_bound_equals_error_free_transformations(cfg):
+@pytest.mark.parametrize("n_vars", [4, 32, 64])
+def test_hardware_rounding_bound_equals_error_free_transformations(n_vars):
     # the bench's timed CPU path (the host's FE_DOWNWARD mode, round-up as a
     # negated round-down) gives the oracle's bounds bit for bit, signs of
     # zero included
     from cuminlp_gb300 import generators as G
-    p = G.CONFIGS[cfg]()
+    p = G.BY_N[n_vars]()
     op = O.OracleProblem(p)
     box = p.root_box()
     kinds, vids, widths, _ = O.bisection_choose(box, p.var_kinds, 9)

@@ -52,17 +52,17 @@ def test_op_count_and_validate():
 
 
 def test_generators_are_deterministic_and_shaped():
-    a, b = G.config2(), G.config2()
+    a, b = G.miqcqp_n32(), G.miqcqp_n32()
     assert [(n.op, n.inputs, n.constant) for n in a.graph.nodes] == [(n.op, n.inputs, n.constant) for n in b.graph.nodes]
     assert a.n_vars == 32 and sum(k == A.VAR_INTEGER for k in a.var_kinds) == 4
     assert len(a.constraints) == 16
     assert a.box_bounds[0] == (0.0, 7.0) and a.box_bounds[10] == (-5.0, 5.0)
-    c1 = G.config1()
+    c1 = G.qcqp_n4()
     assert c1.n_vars == 4 and len(c1.constraints) == 1 and c1.constraints[0].rhs == 5.0
-    c3 = G.config3()
+    c3 = G.miqcqp_n64()
     assert c3.n_vars == 64 and len(c3.constraints) == 32
     for i in range(5):
-        p = G.config4_instance(i)
+        p = G.uneven_qcqp(i)
         assert 4 <= p.n_vars <= 48 and len(p.constraints) <= 24
         p.validate()
 

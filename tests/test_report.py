@@ -15,7 +15,7 @@ def outcomes():
     for name in ("square_le5", "infeasible", "aggregate_fixture", "int_eq", "miqcqp_n6"):
         yield name, O.OracleProblem(fx[name]).solve_batched(iter_limit=2000, bisection_budget=3, batch_parents=32,
                                                             frontier_cap=150, threads=2)
-    yield "cfg1b", O.OracleProblem(G.config1(1)).solve_batched(iter_limit=20000, bisection_budget=3,
+    yield "qcqp_n4_1", O.OracleProblem(G.qcqp_n4(1)).solve_batched(iter_limit=20000, bisection_budget=3,
                                                                batch_parents=256, threads=2)
 
 
@@ -26,7 +26,7 @@ def test_counters_balance():
 
 def test_result_line_grammar():
     got = dict(outcomes())
-    o = got["cfg1b"]
+    o = got["qcqp_n4_1"]
     assert o["proven_optimal"] == 1
     line = report.result_line(o)
     f = line.split("\t")
@@ -40,9 +40,9 @@ def test_result_line_grammar():
 
 def test_finish_block():
     got = dict(outcomes())
-    lines = report.finish_block(got["cfg1b"])
+    lines = report.finish_block(got["qcqp_n4_1"])
     assert lines[0] == "------------ Finished ------------"
-    assert lines[1].endswith("<= min <= %g" % got["cfg1b"]["upper_bound"])
+    assert lines[1].endswith("<= min <= %g" % got["qcqp_n4_1"]["upper_bound"])
     assert "Proven optimal: no pending region can beat the incumbent." in lines
     assert "Stop reason: converged" in lines
     infeasible = report.finish_block(got["infeasible"])

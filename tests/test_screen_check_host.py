@@ -12,7 +12,7 @@ from cuminlp_gb300 import screen_check as S
 
 
 def test_points_stay_in_their_box_and_on_the_lattice():
-    p = G.config3()
+    p = G.miqcqp_n64()
     rng = np.random.default_rng(1)
     lo, hi = S.sample_boxes(p, 6, rng, 0.2)
     ints = np.array(p.var_kinds) != A.VAR_CONTINUOUS
@@ -31,7 +31,7 @@ def test_points_stay_in_their_box_and_on_the_lattice():
 
 
 def test_node_choice_covers_the_roots_and_skips_leaves():
-    p = G.config3()
+    p = G.miqcqp_n64()
     a = S.pick_nodes(p, 40, np.random.default_rng(7))
     b = S.pick_nodes(p, 40, np.random.default_rng(7))
     assert a == b == sorted(a)
@@ -42,7 +42,7 @@ def test_node_choice_covers_the_roots_and_skips_leaves():
 
 
 def test_rerooted_description_shares_the_node_table():
-    p = G.config2()
+    p = G.miqcqp_n32()
     arrays = p.arrays()
     nid = p.constraints[3].root_id
     d, keep = p.desc(arrays=arrays, objective_root=nid, constraints=False)

@@ -44,14 +44,14 @@ def sample_noalloc(dp, kinds, n_regions, S, box, vids, widths, salt):
     return bool(cand.found), cand.value, point, cand.index
 
 
-@pytest.mark.parametrize("cfg,B,S", [(1, 10, 4), (2, 12, 1), ("n512", 10, 2)])
-def test_noalloc_sampler_matches_sampler_role(cfg, B, S):
-    # "n512": 512 variables, whose points are shared by lane groups
-    if cfg == "n512":
+@pytest.mark.parametrize("n_vars,B,S", [(4, 10, 4), (32, 12, 1), (512, 10, 2)])
+def test_noalloc_sampler_matches_sampler_role(n_vars, B, S):
+    # n = 512: a wide QCQP whose points are shared by lane groups
+    if n_vars == 512:
         from tests.test_gpu_roles import wide_qcqp
         p = wide_qcqp()
     else:
-        p = G.CONFIGS[cfg]()
+        p = G.BY_N[n_vars]()
     dp = DeviceProblem(p)
     box = p.root_box()
     kinds, vids, widths, _ = O.bisection_choose(box, p.var_kinds, B)

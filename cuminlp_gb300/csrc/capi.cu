@@ -1011,7 +1011,7 @@ extern "C" cmn_status cmn_solver_create(const cmn_problem* p, const cmn_solve_op
       o.precision != CMN_PRECISION_FP32_LAZY)
     return fail(CMN_INVALID_CONFIGURATION, "unknown precision");
   const uint64_t C = 1ull << o.bisection_budget;
-  if ((o.batch_parents << o.bisection_budget) > (1ull << 31))
+  if (o.batch_parents > ((1ull << 31) >> o.bisection_budget))  // shifted this way round, nothing wraps
     return fail(CMN_INVALID_CONFIGURATION, "batch_parents * 2^bisection_budget above 2^31 children per iteration");
   if (o.frontier_cap > (1ull << 31)) return fail(CMN_INVALID_CONFIGURATION, "frontier_cap above 2^31");
   cmn_status st = check_interval(p);

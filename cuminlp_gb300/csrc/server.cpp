@@ -367,13 +367,16 @@ extern "C" cmn_status cmn_server_wait(cmn_server* s, uint64_t id, uint64_t timeo
   std::unique_lock<std::mutex> lk(s->mu);
   auto it = s->reqs.find(id);
   if (it == s->reqs.end()) return cmn::set_error(CMN_INVALID_CONFIGURATION, "unknown request");
-  auto ready = [&] { return it->second.state == kDone; };
+  // Submits made while this thread waits may rehash the table, which
+  // invalidates iterators but not references to the elements.
+  const Request* r = &it->second;
+  auto ready = [&] { return r->state == kDone; };
   if (timeout_ms == 0) {
     s->cv_done.wait(lk, ready);
   } else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready)) {
     return cmn::set_error(CMN_TIMEOUT, "request still running after " + std::to_string(timeout_ms) + " ms");
   }
-  return copy_result(it->second, out, best_point);
+  return copy_result(*r, out, best_point);
 }
 
 extern "C" cmn_status cmn_server_stats_get(cmn_server* s, cmn_server_stats* out)

@@ -659,7 +659,10 @@ cmn_status cmn_server_create(const cmn_server_config* config,
 void cmn_server_destroy(cmn_server* server);
 /* Queues a solve of `problem` (which must outlive the request).  `opts`
  * shared options must equal the server's; CMN_INVALID_CONFIGURATION when
- * no class takes the problem. */
+ * no class takes the problem.  A finished request's outcome and best point
+ * (a few hundred bytes of host memory plus 8 per variable) stay readable until the
+ * server is destroyed, so a long-running caller recreates the server from
+ * time to time. */
 cmn_status cmn_server_submit(cmn_server* server, const cmn_problem* problem,
                              const cmn_solve_options* opts,
                              uint64_t* request_id);

@@ -29,6 +29,7 @@ SIGNATURES = {
     "cmn_problem_destroy": (None, [P]),
     "cmn_problem_get_info": (I32, [P, C.POINTER(A.ProblemInfo)]),
     "cmn_problem_program": (I32, [P, I32, P, I64, C.POINTER(I64)]),
+    "cmn_program_compile": (I32, [C.POINTER(A.ProblemDesc), I32, P, I64, C.POINTER(I64)]),
     "cmn_autotune": (I32, [P, I32, U64, C.POINTER(A.TuneResult)]),
     "cmn_cost_model_get": (I32, [P, C.POINTER(A.CostModel)]),
     "cmn_bisection_choose": (I32, [P, P, I64, I32, U64, U64, I32, P, P, P, P, C.POINTER(I64), C.POINTER(I32)]),

@@ -224,6 +224,30 @@ extern "C" cmn_status cmn_problem_program(const cmn_problem* p, int32_t precisio
   return CMN_OK;
 }
 
+extern "C" cmn_status cmn_program_compile(const cmn_problem_desc* desc, int32_t precision, void* out,
+                                          int64_t capacity, int64_t* length)
+{
+  if (!desc || !length) return fail(CMN_INVALID_CONFIGURATION, "null argument");
+  if (precision != 0 && precision != 1) return fail(CMN_INVALID_CONFIGURATION, "precision must be 0 or 1");
+  try {
+    HostProblem host;
+    std::string err;
+    const cmn_status st = build_host_problem(desc, host, err);
+    if (st != CMN_OK) return fail(st, err);
+    Program prog;
+    compile_program(host, prog);
+    const std::vector<Instr>& code = precision == 0 ? prog.code64 : prog.code32;
+    *length = (int64_t)code.size();
+    if (out && capacity > 0)
+      std::memcpy(out, code.data(), sizeof(Instr) * (size_t)std::min<int64_t>(capacity, (int64_t)code.size()));
+    return CMN_OK;
+  } catch (const std::bad_alloc&) {
+    return fail(CMN_INTERNAL, "host allocation failed");
+  } catch (const std::exception& ex) {
+    return fail(CMN_INTERNAL, ex.what());
+  }
+}
+
 static cmn_status check_interval(const cmn_problem* p)
 {
   if (!p->prog.interval_supported)

@@ -76,6 +76,18 @@ def materialise(parent: list, sidx: int, a: SlotAssignment) -> list:
     return out
 
 
+def compile_program(problem: Problem, precision: int = 0) -> np.ndarray:
+    """The compiled program of `problem` built on the host
+    (cmn_program_compile), without a CUDA device: the bytes
+    DeviceProblem.program(precision) returns."""
+    desc, _keep = problem.desc()  # _keep holds the arrays desc points into
+    n = C.c_int64()
+    check(lib().cmn_program_compile(C.byref(desc), precision, None, 0, C.byref(n)))
+    buf = np.zeros(16 * n.value, dtype=np.uint8)
+    check(lib().cmn_program_compile(C.byref(desc), precision, A.ptr(buf), n.value, C.byref(n)))
+    return buf
+
+
 class DeviceProblem:
     """A Problem compiled and resident on the current CUDA device."""
 

@@ -18,6 +18,10 @@
  *     owns, valid until the next call on that role
  *     (backend/backend.hpp:52-54, 66-67).
  *   - One handle is never used from two threads at once.
+ *   - A problem lives on the device current when it is created.  Calls on
+ *     a problem, role, solver or batch make that device current and leave
+ *     it current (cmn_sample_noalloc alone restores the caller's); a thread
+ *     that drives several GPUs sets its device again after such a call.
  */
 #ifndef CUMINLP_GB300_H
 #define CUMINLP_GB300_H
@@ -524,6 +528,12 @@ cmn_status cmn_autotune(cmn_problem* problem, int32_t precision, uint64_t n_boxe
  * `capacity` instructions to `out` (16 * capacity bytes) and the program's
  * length to *length. */
 cmn_status cmn_problem_program(const cmn_problem* problem, int32_t precision,
+                               void* out, int64_t capacity, int64_t* length);
+/* The same program, compiled on the host straight from a description:
+ * needs no CUDA device and allocates no device memory, for tools and tests
+ * that run where no GPU is present.  The description is validated as
+ * cmn_problem_create validates it. */
+cmn_status cmn_program_compile(const cmn_problem_desc* desc, int32_t precision,
                                void* out, int64_t capacity, int64_t* length);
 
 /* One-call solve: create, run to a stop condition, report, destroy. */

@@ -16,7 +16,7 @@ def outcomes():
         yield name, O.OracleProblem(fx[name]).solve_batched(iter_limit=2000, bisection_budget=3, batch_parents=32,
                                                             frontier_cap=150, threads=2)
     yield "qcqp_n4_1", O.OracleProblem(G.qcqp_n4(1)).solve_batched(iter_limit=20000, bisection_budget=3,
-                                                               batch_parents=256, threads=2)
+                                                                   batch_parents=256, threads=2)
 
 
 def test_counters_balance():

@@ -67,6 +67,10 @@ EVAL_DRAM_BYTES_PER_BOX = (43186688 + 34048) / 1048576  # ncu, eval_children_ker
 # launch
 INC32_DRAM_BYTES_PER_BOX = (10849280 + 11762688 + 2355968 + 59540224 + 154368) / 262144
 SCREEN32_DRAM_BYTES_PER_POINT = 20065792 / 262144
+# the same capture: the FP64 verdict of 2^14 selected boxes reads 17.8 MB
+# (their staged planes, 1,024 B a box, and the program); the 9 B a box it
+# writes (bound and state) are added as counted, not measured
+VERDICT_DRAM_BYTES_PER_BOX = 17.8e6 / 16384 + 9
 # time-to-gap on the n=4 QCQP: the cluster of boxes within 1e-6 of the optimum
 # holds tens of millions of boxes at n=4, so the frontier is capped at 2^25;
 # 2^21 parents x 2^2 children per iteration timed best (swept over
@@ -770,8 +774,8 @@ def run_ours(args):
     phase_rl = {
         "certify": dict(phase_line(0, ld["expansions"], fpb, peak64,
                                    "eval_children_staged_kernel<0, 1> (FP64 verdict of each selected box, fused "
-                                   "terms, on its own stream beside the branching and the FP32 bound)", None,
-                                   "selected box",
+                                   "terms, on its own stream beside the branching and the FP32 bound)",
+                                   VERDICT_DRAM_BYTES_PER_BOX, "selected box",
                                    "lazy_phases"), bound="fp64"),
         "bound": dict(phase_line(1, ld["bounded"], fpb, peak32,
                                  "inc_common_kernel + inc_parts_kernel + eval_children_inc_kernel (FP32 child "

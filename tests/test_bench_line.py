@@ -114,6 +114,10 @@ def test_default_line_carries_the_contract(stubbed, monkeypatch):
     # the stub's longest phase is the FP32 bound (43 ms of 60; the FP64 verdict beside it 20 ms)
     assert r["phase"] == "bound" and r["achieved"] == pytest.approx((1 << 20) * 28930.0 / 43e-3 / 1e12)
     assert set(d["phase_rooflines"]) == {"certify", "bound", "sample"}
+    # every phase carries its DRAM traffic per launch from the ncu capture
+    certify = d["phase_rooflines"]["certify"]
+    assert certify["traffic"] == pytest.approx(bench.VERDICT_DRAM_BYTES_PER_BOX * (1 << 16))
+    assert all(v["traffic"] > 0 for v in d["phase_rooflines"].values())
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == 75e3 and cb["sample"]
     e = d["e2e"]

@@ -95,10 +95,10 @@ def test_reference_arm_prints_from_rank0_only(tmp_path):
 
 
 def test_replicas_are_distinct_instances():
-    """Each rank solves its own seeded n=32 MIQCQP instance (independent
-    replicas), of the same shape."""
+    """Each rank solves its own seeded n=64 MIQCQP instance, the bench's
+    headline shape (independent replicas)."""
     from cuminlp_gb300 import generators as G
-    a, b = G.miqcqp_n32(0), G.miqcqp_n32(1)
+    a, b = G.miqcqp_n64(0), G.miqcqp_n64(1)
     assert a.n_vars == b.n_vars and len(a.constraints) == len(b.constraints)
     consts = [[n.constant for n in p.graph.nodes] for p in (a, b)]
     assert consts[0] != consts[1]

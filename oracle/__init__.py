@@ -52,6 +52,7 @@ _SIG = {
     "orc_bound_hw": (I32, [P, P, P, P, P, I64, U64, P, P, I32]),
     "orc_set_program32": (I32, [P, P, I64]),
     "orc_set_program64": (I32, [P, P, I64]),
+    "orc_program_eval64": (I32, [P, P, C.POINTER(D), C.POINTER(D)]),
     "orc_bound_inc32": (I32, [P, P, P, P, P, I64, U64, P, P, P]),
     "orc_aggregate_bound": (I32, [P, P, P, P, P, I64, U64, U64, P, P, P, I32]),
     "orc_sample": (I32, [P, P, P, P, P, I64, U64, U64, U64, C.POINTER(I32), C.POINTER(D), C.POINTER(I64), P, I32]),
@@ -174,6 +175,17 @@ class OracleProblem:
         terms, as the device does."""
         code = np.ascontiguousarray(code, dtype=np.uint8)
         return bool(lib().orc_set_program64(self.h, A.ptr(code), code.size // 16))
+
+    def program_eval64(self, box):
+        """One box through the FP64 program (after set_program64) with every
+        operation rounded on its own, as the plain form runs it: (feasible,
+        lb, ub), feasible -1 for an operator without an interval form."""
+        box = np.ascontiguousarray(box, dtype=np.float64)
+        lb, ub = C.c_double(), C.c_double()
+        f = lib().orc_program_eval64(self.h, A.ptr(box), C.byref(lb), C.byref(ub))
+        if f == -2:
+            raise ValueError(lib().orc_last_error().decode())
+        return f, lb.value, ub.value
 
     def bound_inc32(self, box, kinds, var_ids, widths, n_regions):
         """The lazy form's incremental FP32 bounds of one parent's regions

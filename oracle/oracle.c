@@ -2211,17 +2211,18 @@ static iv64 prog_fetch64(const struct orc_instr* in, int mode, int idx, const do
   }
 }
 
-/* The lazy form's FP64 verdict of box `box` (lo, hi pairs) from the FP64
- * program (orc_set_program64), restating csrc/eval_core.cuh interval_range
- * with fused terms: a TERM with a coefficient c that adds into its chain
+/* Box `box` (lo, hi pairs) through the FP64 program (orc_set_program64),
+ * restating csrc/eval_core.cuh interval_range.  With `fused` set, the lazy
+ * form's verdict: a TERM with a coefficient c that adds into its chain
  * folds c and the add into one directed FMA per bound (the coefficient's
- * sign picks the product's endpoint), every other instruction as the
- * program's unfused operations.  Runs under FE_DOWNWARD with the _h
- * operators (round-up as negated round-down, fma included).  Returns the
- * reference predicate (1 feasible), or -1 for an operator without an
- * interval form; *lb, *ub the objective's enclosure.  `slots` has room for
- * the program's slots. */
-static int verdict_fused64(const orc_problem* p, const double* box, iv64* slots, double* lb, double* ub)
+ * sign picks the product's endpoint).  Without it, and for every other
+ * instruction, the program's operations each round on their own, as the
+ * plain form runs them.  Runs under FE_DOWNWARD with the _h operators
+ * (round-up as negated round-down, fma included).  Returns the reference
+ * predicate (1 feasible), or -1 for an operator without an interval form;
+ * *lb, *ub the objective's enclosure.  `slots` has room for the program's
+ * slots. */
+static int program_run64(const orc_problem* p, const double* box, iv64* slots, double* lb, double* ub, int fused)
 {
   iv64 acc = {0.0, 0.0};
   iv64 obj = {NAN, NAN};
@@ -2236,7 +2237,7 @@ static int verdict_fused64(const orc_problem* p, const double* box, iv64* slots,
         iv64 xb = prog_fetch64(in, MODE_VAR, in->b, box, slots, acc);
         const int pk = sub & T_PMASK;
         iv64 prod = pk == T_SQR ? iv_sqr_h(xa) : (pk == T_VAR ? xa : iv_mul_h(xa, xb));
-        if ((sub & T_HASC) && !(sub & T_INIT)) {
+        if (fused && (sub & T_HASC) && !(sub & T_INIT)) {
           const double cc = (sub & T_SUB) ? -in->u.c : in->u.c;
           const int pos = cc >= 0.0;
           acc.lo = fma(cc, pos ? prod.lo : prod.hi, acc.lo);
@@ -2282,6 +2283,19 @@ static int verdict_fused64(const orc_problem* p, const double* box, iv64* slots,
   *lb = obj.lo;
   *ub = obj.hi;
   return rc ? rc : feas;
+}
+
+int orc_program_eval64(const orc_problem* p, const double* box, double* lb, double* ub)
+{
+  if (!p->prog64) {
+    set_err("no FP64 program: call orc_set_program64 first");
+    return -2;
+  }
+  iv64* slots = (iv64*)malloc(sizeof(iv64) * (size_t)(p->n_prog_slots > 0 ? p->n_prog_slots : 1));
+  const int f = program_run64(p, box, slots, lb, ub, 0);
+  free(slots);
+  if (f < 0) set_err("op without an interval implementation");
+  return f;
 }
 
 int orc_set_program32(orc_problem* p, const void* instrs, int64_t len)
@@ -2671,7 +2685,7 @@ static void certify_range(void* vc, int64_t k0, int64_t k1, int tid)
   iv64* slots = (iv64*)malloc(sizeof(iv64) * (size_t)(c->p->n_prog_slots > 0 ? c->p->n_prog_slots : 1));
   for (int64_t k = k0; k < k1; ++k) {
     double ub;
-    const int f = verdict_fused64(c->p, c->pbox + 2 * (size_t)n * (size_t)k, slots, &c->lb[k], &ub);
+    const int f = program_run64(c->p, c->pbox + 2 * (size_t)n * (size_t)k, slots, &c->lb[k], &ub, 1);
     if (f < 0) c->failed = 1;
     c->feas[k] = f > 0;
   }

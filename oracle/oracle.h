@@ -97,6 +97,13 @@ int orc_set_program32(orc_problem* p, const void* instrs, int64_t len);
  * the lazy form's verdict of each expanded box runs it with fused terms,
  * as the device does.  Required for the lazy form. */
 int orc_set_program64(orc_problem* p, const void* instrs, int64_t len);
+/* One box (n_vars (lo, hi) pairs) through that FP64 program with every
+ * operation rounded on its own, as the device's plain form runs it: 1
+ * feasible, 0 not, -1 an operator without an interval form, -2 no program
+ * set; *lb, *ub the objective's enclosure.  Node-by-node evaluation gives
+ * the same enclosures bit for bit (signs of zero aside) when the compiler
+ * keeps every node's roundings in their order. */
+int orc_program_eval64(const orc_problem* p, const double* box, double* lb, double* ub);
 
 /* The lazy form's incremental FP32 bound of every region of one parent
  * box, after orc_set_program32. */

@@ -53,6 +53,7 @@ _SIG = {
     "orc_set_program32": (I32, [P, P, I64]),
     "orc_set_program64": (I32, [P, P, I64]),
     "orc_program_eval64": (I32, [P, P, C.POINTER(D), C.POINTER(D)]),
+    "orc_program_eval32": (I32, [P, P, C.POINTER(D), C.POINTER(D)]),
     "orc_bound_inc32": (I32, [P, P, P, P, P, I64, U64, P, P, P]),
     "orc_aggregate_bound": (I32, [P, P, P, P, P, I64, U64, U64, P, P, P, I32]),
     "orc_sample": (I32, [P, P, P, P, P, I64, U64, U64, U64, C.POINTER(I32), C.POINTER(D), C.POINTER(I64), P, I32]),
@@ -183,6 +184,16 @@ class OracleProblem:
         box = np.ascontiguousarray(box, dtype=np.float64)
         lb, ub = C.c_double(), C.c_double()
         f = lib().orc_program_eval64(self.h, A.ptr(box), C.byref(lb), C.byref(ub))
+        if f == -2:
+            raise ValueError(lib().orc_last_error().decode())
+        return f, lb.value, ub.value
+
+    def program_eval32(self, box):
+        """The same through the FP32 program (after set_program32): (not
+        proven infeasible, lb, ub) as the FP32 screen evaluates it."""
+        box = np.ascontiguousarray(box, dtype=np.float64)
+        lb, ub = C.c_double(), C.c_double()
+        f = lib().orc_program_eval32(self.h, A.ptr(box), C.byref(lb), C.byref(ub))
         if f == -2:
             raise ValueError(lib().orc_last_error().decode())
         return f, lb.value, ub.value

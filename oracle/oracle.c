@@ -2298,6 +2298,93 @@ int orc_program_eval64(const orc_problem* p, const double* box, double* lb, doub
   return f;
 }
 
+/* An FP32 program operand: variables widened outward on conversion,
+ * constants as the program's outward-rounded pair (csrc/eval_core.cuh
+ * const_of<float>). */
+static iv32 prog_fetch32(const struct orc_instr* in, int mode, int idx, const double* box, const iv32* slots,
+                         iv32 acc)
+{
+  iv32 v;
+  switch (mode) {
+    case MODE_SLOT: return slots[idx];
+    case MODE_VAR:
+      v.lo = orc_d2f_rd(box[2 * idx]);
+      v.hi = orc_d2f_ru(box[2 * idx + 1]);
+      return v;
+    case MODE_ACC: return acc;
+    default:
+      v.lo = in->u.c32.clo;
+      v.hi = in->u.c32.chi;
+      return v;
+  }
+}
+
+int orc_program_eval32(const orc_problem* p, const double* box, double* lb, double* ub)
+{
+  if (!p->prog32) {
+    set_err("no FP32 program: call orc_set_program32 first");
+    return -2;
+  }
+  int64_t n_slots = 1;
+  for (int64_t pc = 0; pc < p->prog_len; ++pc) {
+    const int op = p->prog32[pc].head & 7;
+    if (op == OP_GENERIC || op == OP_STOREACC || op == OP_CONSTTOSLOT)
+      if ((int64_t)p->prog32[pc].dst + 1 > n_slots) n_slots = (int64_t)p->prog32[pc].dst + 1;
+  }
+  iv32* slots = (iv32*)malloc(sizeof(iv32) * (size_t)n_slots);
+  iv32 acc = {0.0f, 0.0f};
+  iv32 obj = {NAN, NAN};
+  int excluded = 0, rc = 0;
+  for (int64_t pc = 0; pc < p->prog_len && rc == 0; ++pc) {
+    const struct orc_instr* in = &p->prog32[pc];
+    const int op = in->head & 7, sub = in->head >> 3;
+    switch (op) {
+      case OP_TERM: {
+        const iv32 xa = prog_fetch32(in, MODE_VAR, in->a, box, slots, acc);
+        const iv32 xb = prog_fetch32(in, MODE_VAR, in->b, box, slots, acc);
+        const int pk = sub & T_PMASK;
+        iv32 t = pk == T_SQR ? iv_sqr_f(xa) : (pk == T_VAR ? xa : iv_mul_f(xa, xb));
+        if (sub & T_HASC) {
+          const iv32 c = {in->u.c32.clo, in->u.c32.chi};
+          t = iv_mul_f(c, t);
+        }
+        acc = (sub & T_INIT) ? t : ((sub & T_SUB) ? iv_sub_f(acc, t) : iv_add_f(acc, t));
+        break;
+      }
+      case OP_GENERIC: {
+        if (!op_supported_interval(sub)) {
+          rc = -1;
+          break;
+        }
+        const iv32 a = prog_fetch32(in, in->modes & 3, in->a, box, slots, acc);
+        const iv32 b = prog_fetch32(in, (in->modes >> 2) & 3, in->b, box, slots, acc);
+        slots[in->dst] = apply_f(sub, a, b, (int)(int16_t)in->b);
+        break;
+      }
+      case OP_STOREACC: slots[in->dst] = acc; break;
+      case OP_LOADACC: acc = prog_fetch32(in, in->modes & 3, in->a, box, slots, acc); break;
+      case OP_CONSTTOSLOT:
+        slots[in->dst].lo = in->u.c32.clo;
+        slots[in->dst].hi = in->u.c32.chi;
+        break;
+      case OP_CHECK: { /* the rhs stays FP64 in both programs; "proven violated" */
+        const iv32 v = prog_fetch32(in, in->modes & 3, in->a, box, slots, acc);
+        const double rhs = in->u.c;
+        if (sub == 0) excluded = excluded || ((double)v.lo > rhs);
+        else excluded = excluded || ((double)v.lo > rhs || (double)v.hi < rhs);
+        break;
+      }
+      case OP_OBJECTIVE: obj = prog_fetch32(in, in->modes & 3, in->a, box, slots, acc); break;
+      default: break;
+    }
+  }
+  free(slots);
+  *lb = (double)obj.lo;
+  *ub = (double)obj.hi;
+  if (rc < 0) set_err("op without an interval implementation");
+  return rc < 0 ? rc : !excluded;
+}
+
 int orc_set_program32(orc_problem* p, const void* instrs, int64_t len)
 {
   free(p->prog32);

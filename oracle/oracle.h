@@ -104,6 +104,11 @@ int orc_set_program64(orc_problem* p, const void* instrs, int64_t len);
  * the same enclosures bit for bit (signs of zero aside) when the compiler
  * keeps every node's roundings in their order. */
 int orc_program_eval64(const orc_problem* p, const double* box, double* lb, double* ub);
+/* The same through the FP32 program (orc_set_program32): variables widened
+ * outward, constants as outward pairs, every operation directed in FP32;
+ * 1 when no constraint is proven violated (rhs compared in FP64), 0 when
+ * one is, -1 / -2 as above.  Equals node-by-node FP32 evaluation. */
+int orc_program_eval32(const orc_problem* p, const double* box, double* lb, double* ub);
 
 /* The lazy form's incremental FP32 bound of every region of one parent
  * box, after orc_set_program32. */

@@ -1,14 +1,15 @@
-"""CPU: the compiled program keeps every node's roundings in their order.
+"""CPU: the compiled programs keep every node's roundings in their order.
 
 The library compiles a problem's DAG into a straight-line program (sum
 chains folded into TERM instructions, shared intermediates in liveness-
-allocated slots) and the plain FP64 form evaluates that program.  Here the
-program comes from cmn_program_compile (no GPU) and runs through the
+allocated slots): an FP64 one, which the plain form evaluates, and an FP32
+one with outward-rounded constant pairs, which the FP32 screen evaluates.
+Here both come from cmn_program_compile (no GPU) and run through the
 oracle's restatement of the interpreter with every operation rounded on its
-own; its enclosures and feasibility verdicts must equal the oracle's
-node-by-node evaluation of the DAG -- the reference's per-node kernel chain
-(backend/graph/kernels.cuh:177-419) -- bit for bit.  A mistake planted in
-the program is caught the same way."""
+own; their enclosures and verdicts must equal the oracle's node-by-node
+evaluation of the DAG in the same precision -- the reference's per-node
+kernel chain (backend/graph/kernels.cuh:177-419) -- bit for bit.  A mistake
+planted in the program is caught the same way."""
 
 from __future__ import annotations
 
@@ -26,16 +27,21 @@ from tests.test_oracle_pins import fixture_problems
 OP_TERM, T_HASC = 1, 4  # instruction opcode (head bits 0-2) and term sub-code bit (head bits 3-7)
 
 
-def mismatches(p: Problem, code: np.ndarray, n_boxes: int, seed: int, scale: float = 0.2) -> int:
+def mismatches(p: Problem, code: np.ndarray, n_boxes: int, seed: int, scale: float = 0.2, fp32: bool = False) -> int:
     """Boxes on which the program and node-by-node evaluation differ in the
-    objective's enclosure or the feasibility verdict (+0 and -0 equal)."""
+    objective's enclosure or the verdict (+0 and -0 equal): FP64, the
+    reference predicate; FP32, not proven violated."""
     op = O.OracleProblem(p)
-    assert op.set_program64(code)
+    if fp32:
+        op.set_program32(code)  # False only says the program is not a set of sum chains
+    else:
+        assert op.set_program64(code)
+    run = op.program_eval32 if fp32 else op.program_eval64
     lo, hi = random_boxes(p, n_boxes, np.random.default_rng(seed), scale)
-    lb, ub, fe = op.eval_boxes(lo, hi, A.PRECISION_FP64, threads=2)
+    lb, ub, fe = op.eval_boxes(lo, hi, A.PRECISION_FP32_SCREEN if fp32 else A.PRECISION_FP64, threads=2)
     bad = 0
     for k in range(n_boxes):
-        f, plb, pub = op.program_eval64(np.stack([lo[:, k], hi[:, k]], 1).reshape(-1))
+        f, plb, pub = run(np.stack([lo[:, k], hi[:, k]], 1).reshape(-1))
         assert f >= 0, "an operator without an interval form"
         same = f == fe[k] and (plb == lb[k] or (np.isnan(plb) and np.isnan(lb[k]))) and (
             pub == ub[k] or (np.isnan(pub) and np.isnan(ub[k])))
@@ -53,29 +59,33 @@ def cases():
         yield name, p
 
 
+@pytest.mark.parametrize("fp32", [False, True], ids=["fp64", "fp32"])
 @pytest.mark.parametrize("name,p", list(cases()), ids=[n for n, _ in cases()])
-def test_program_matches_node_by_node(name, p):
+def test_program_matches_node_by_node(name, p, fp32):
     n_boxes = 200 if p.n_vars > 8 else 1000
-    assert mismatches(p, compile_program(p, 0), n_boxes, seed=7, scale=0.5 if name == "every_operator" else 0.2) == 0
+    scale = 0.5 if name == "every_operator" else 0.2
+    assert mismatches(p, compile_program(p, int(fp32)), n_boxes, seed=7, scale=scale, fp32=fp32) == 0
 
 
+@pytest.mark.parametrize("fp32", [False, True], ids=["fp64", "fp32"])
 @pytest.mark.parametrize("n_vars", [32, 64])
-def test_every_constraint_chain_matches_node_by_node(n_vars):
+def test_every_constraint_chain_matches_node_by_node(n_vars, fp32):
     # each constraint root as the objective: the chain's enclosure itself,
     # not only the verdict it feeds
     p = G.BY_N[n_vars]()
     for c in p.constraints[:8]:
         q = with_objective(p, c.root_id)
-        assert mismatches(q, compile_program(q, 0), 64, seed=c.root_id) == 0
+        assert mismatches(q, compile_program(q, int(fp32)), 64, seed=c.root_id, fp32=fp32) == 0
 
 
-def test_every_node_of_the_operator_problem_matches():
+@pytest.mark.parametrize("fp32", [False, True], ids=["fp64", "fp32"])
+def test_every_node_of_the_operator_problem_matches(fp32):
     p = ops_problem()
     for node in p.graph.nodes:
         if node.op in (A.OP_CONST, A.OP_VAR):
             continue
         q = with_objective(p, node.id)
-        assert mismatches(q, compile_program(q, 0), 200, seed=node.id, scale=0.5) == 0, node.op
+        assert mismatches(q, compile_program(q, int(fp32)), 200, seed=node.id, scale=0.5, fp32=fp32) == 0, node.op
 
 
 def test_a_planted_program_error_is_caught():
@@ -95,3 +105,12 @@ def test_a_planted_program_error_is_caught():
 
     assert mismatches(p, planted(terms[:1], lambda c: 2.0 * c), 200, seed=7) > 0
     assert mismatches(p, planted(terms, lambda c: np.nextafter(c, np.inf)), 200, seed=7) > 0
+
+
+def test_a_planted_fp32_program_error_is_caught():
+    p = G.miqcqp_n32()
+    code = compile_program(p, 1)
+    r = code.reshape(-1, 16)
+    first = next(i for i in range(len(r)) if (r[i, 0] & 7) == OP_TERM and (r[i, 0] >> 3) & T_HASC)
+    r[first, 8:16] = np.frombuffer((2.0 * r[first, 8:16].view(np.float32)).astype(np.float32).tobytes(), np.uint8)
+    assert mismatches(p, code, 200, seed=7, fp32=True) > 0

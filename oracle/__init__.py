@@ -54,6 +54,7 @@ _SIG = {
     "orc_set_program64": (I32, [P, P, I64]),
     "orc_program_eval64": (I32, [P, P, C.POINTER(D), C.POINTER(D)]),
     "orc_program_eval32": (I32, [P, P, C.POINTER(D), C.POINTER(D)]),
+    "orc_finalise": (I32, [D, D, D, I32, I32, I32, D, U64, P, P, I64, C.POINTER(A.Outcome)]),
     "orc_bound_inc32": (I32, [P, P, P, P, P, I64, U64, P, P, P]),
     "orc_aggregate_bound": (I32, [P, P, P, P, P, I64, U64, U64, P, P, P, I32]),
     "orc_sample": (I32, [P, P, P, P, P, I64, U64, U64, U64, C.POINTER(I32), C.POINTER(D), C.POINTER(I64), P, I32]),
@@ -296,6 +297,21 @@ class OracleProblem:
         d = A.outcome_dict(out)
         d["best_point"] = pt
         return box[:m], lb[:m], depth[:m], d
+
+
+def finalise(glb, gub, converged, pending_empty, frontier_min, viable, drops=(), tolerance=1e-6,
+             found=None):
+    """The epilogue's answers (proven_optimal, infeasible, lower_bound) for
+    a run that dropped the (lb, gub at the time) pairs in `drops`; `found`
+    defaults to gub below the no-incumbent sentinel (DBL_MAX)."""
+    if found is None:
+        found = gub < np.finfo(np.float64).max
+    lbs = np.ascontiguousarray([d[0] for d in drops] or [0.0], dtype=np.float64)
+    gubs = np.ascontiguousarray([d[1] for d in drops] or [0.0], dtype=np.float64)
+    out = A.Outcome()
+    lib().orc_finalise(glb, gub, tolerance, int(found), int(converged), int(pending_empty), frontier_min, viable,
+                       A.ptr(lbs), A.ptr(gubs), len(drops), C.byref(out))
+    return bool(out.proven_optimal), bool(out.infeasible), out.lower_bound
 
 
 def bisection_choose(box, var_kinds, B, max_cycle=0, enumerate_cap=0, relative=False):

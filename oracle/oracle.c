@@ -1831,6 +1831,16 @@ static void finalise(double glb, double gub, double tol, int found,
   }
 }
 
+int orc_finalise(double glb, double gub, double tol, int found, int converged, int pending_empty,
+                 double frontier_min, uint64_t viable, const double* drop_lbs, const double* drop_gubs,
+                 int64_t n_drops, cmn_outcome* out)
+{
+  drop_acc d = {INFINITY, 0, 0};
+  for (int64_t i = 0; i < n_drops; ++i) drop_fold(&d, drop_lbs[i], drop_gubs[i]);
+  finalise(glb, gub, tol, found, converged, pending_empty, frontier_min, viable, &d, out);
+  return 0;
+}
+
 static uint64_t slot_product(const uint64_t* widths, int64_t count)
 {
   uint64_t total = 1;

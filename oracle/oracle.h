@@ -110,6 +110,14 @@ int orc_program_eval64(const orc_problem* p, const double* box, double* lb, doub
  * one is, -1 / -2 as above.  Equals node-by-node FP32 evaluation. */
 int orc_program_eval32(const orc_problem* p, const double* box, double* lb, double* ub);
 
+/* The epilogue (search/epilogue.hpp:89-127, finalise_bounds) over a drop
+ * record that folds each dropped lb against the gub it was dropped under
+ * (search/budget.hpp:190-209, DropAccounting::fold): fills
+ * out->proven_optimal, out->infeasible and out->lower_bound. */
+int orc_finalise(double glb, double gub, double tol, int found, int converged, int pending_empty,
+                 double frontier_min, uint64_t viable, const double* drop_lbs, const double* drop_gubs,
+                 int64_t n_drops, cmn_outcome* out);
+
 /* The lazy form's incremental FP32 bound of every region of one parent
  * box, after orc_set_program32. */
 int orc_bound_inc32(const orc_problem* p, const double* box, const uint8_t* slot_kinds, const uint64_t* var_ids,

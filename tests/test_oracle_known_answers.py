@@ -1,5 +1,8 @@
-"""CPU: the oracle against two sets of the reference's own known answers
-that pin this path and run without Catch2 or a GPU.
+"""CPU: the oracle against the reference's own known answers that pin this
+path and run without Catch2 or a GPU.
+
+- The cost model's count of buffer-bearing nodes
+  (backend/graph/cost.hpp:38-68): graph_replay_test.cu:463-480.
 
 - The epilogue (search/epilogue.hpp:89-127, finalise_bounds, with
   DropAccounting, search/budget.hpp:190-209): every case of
@@ -51,6 +54,21 @@ def test_epilogue_known_answers(name):
     got = O.finalise(glb, gub, converged, pending_empty, frontier_min, viable, drops)
     assert got[0] == proven and got[1] == infeasible
     assert got[2] == pytest.approx(lb, rel=0, abs=1e-12)
+
+
+def test_buffer_node_count_counts_only_reachable_nodes():
+    # graph_replay_test.cu:463-480 over backend/graph/cost.hpp:38-68: the
+    # cost model counts the non-Const nodes a root reaches; an expression no
+    # root refers to adds nothing
+    p = Problem()
+    x = p.var(0.0, 10.0)
+    p.set_objective(x * x)
+    p.add_constraint(x, A.CMP_LE, 5.0)
+    reachable = O.OracleProblem(p).buffer_node_count
+    dead = p.var(0.0, 1.0) * p.var(0.0, 1.0)
+    assert dead is not None
+    assert O.OracleProblem(p).buffer_node_count == reachable == 2  # x and x*x
+    assert reachable < len(p.graph.nodes)
 
 
 def test_point_evaluation_every_root():

@@ -411,7 +411,6 @@ extern "C" cmn_status cmn_role_build(const cmn_problem* p, int32_t role, const u
   for (int64_t j = 0; j < slot_count; ++j)
     if (slot_kinds[j] > CMN_SLOT_BINARY_ENUMERATE) return fail(CMN_INVALID_CONFIGURATION, "unknown slot kind");
   if (n_regions < 1) return fail(CMN_INVALID_CONFIGURATION, "n_regions must be at least 1");
-  if (n_regions > (1ULL << 32)) return fail(CMN_INVALID_CONFIGURATION, "n_regions above 2^32");
   if (role == CMN_ROLE_ENUMERATOR) {
     for (int64_t j = 0; j < slot_count; ++j)
       if (!is_enum_kind(slot_kinds[j]))
@@ -430,22 +429,34 @@ extern "C" cmn_status cmn_role_build(const cmn_problem* p, int32_t role, const u
     uint64_t per = role == CMN_ROLE_BOUNDER ? cm.bound_bytes_per_region
                    : role == CMN_ROLE_SAMPLER ? cm.sampler_bytes_per_sample * S
                                               : cm.exact_bytes_per_region;
-    const uint64_t needed = n_regions * per + cm.fixed_bytes;
+    // saturating, as the reference's estimate is: a fan-out that saturates
+    // is over any budget rather than wrapped to an affordable size
+    const uint64_t needed = per != 0 && n_regions > (UINT64_MAX - cm.fixed_bytes) / per
+                                ? UINT64_MAX
+                                : n_regions * per + cm.fixed_bytes;
     uint64_t budget = budget_bytes;
     if (budget == 0) {
       size_t fr = 0, tot = 0;
       CK(cudaMemGetInfo(&fr, &tot));
       budget = fr;
     }
-    if (needed > budget) {
+    // Beyond 2^32 regions a role cannot index its launch; like a saturated
+    // fan-out in the reference (graph_replay_test.cu:442-461) it is reported
+    // as over budget, before anything is allocated, so a driver's cache can
+    // evict, retry and finally stop the run as out of device memory.
+    const bool too_many = n_regions > (1ULL << 32);
+    if (needed > budget || too_many) {
       if (facts) {
-        facts->needed_bytes = needed;
+        facts->needed_bytes = too_many ? UINT64_MAX : needed;
         facts->budget_bytes = budget;
         facts->n_regions = n_regions;
         facts->elements_per_region = S;
         facts->bytes_per_element = per;
       }
       const char* names[] = {"interval graph", "point graph", "exact graph"};
+      if (too_many)
+        return fail(CMN_OVER_BUDGET, std::string(names[role]) + " of " + std::to_string(n_regions) +
+                                         " regions: a role indexes at most 2^32 regions per launch.");
       return fail(CMN_OVER_BUDGET, std::string(names[role]) + " needs " + std::to_string(needed) +
                                        " B of device memory, but only " + std::to_string(budget) + " B is available.");
     }

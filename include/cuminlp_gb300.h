@@ -228,7 +228,9 @@ typedef struct cmn_candidate {
 /* Replaces RegionBackendFactory::build_subdivision for one role
  * (backend/backend.hpp:215-219; graph/replay.cuh:264-521 GraphReplay::build).
  * `budget_bytes` 0 means "what the device has free".  On CMN_OVER_BUDGET
- * `facts` (if non-null) is filled and nothing is allocated.  Building an
+ * `facts` (if non-null) is filled and nothing is allocated; more than 2^32
+ * regions is over budget too (needed_bytes UINT64_MAX), as a saturated
+ * fan-out is in the reference (graph_replay_test.cu:442-461).  Building an
  * enumerator for a composition that is not fully enumerable returns
  * CMN_INVALID_CONFIGURATION. */
 cmn_status cmn_role_build(const cmn_problem* problem, int32_t role,

@@ -114,3 +114,52 @@ def test_a_planted_fp32_program_error_is_caught():
     first = next(i for i in range(len(r)) if (r[i, 0] & 7) == OP_TERM and (r[i, 0] >> 3) & T_HASC)
     r[first, 8:16] = np.frombuffer((2.0 * r[first, 8:16].view(np.float32)).astype(np.float32).tobytes(), np.uint8)
     assert mismatches(p, code, 200, seed=7, fp32=True) > 0
+
+
+def random_problem(seed: int) -> Problem:
+    """A random DAG over a few variables: every operator with an interval
+    form, shared subexpressions (each new node may reuse any earlier one),
+    sum chains of coefficient products, and LE / EQ constraints on random
+    nodes -- the shapes that exercise the compiler's slot liveness and
+    chain folding beyond the generated QCQPs."""
+    from cuminlp_gb300.problem import Expr, pow, sqr, sqrt
+    rng = np.random.default_rng(seed)
+    p = Problem()
+    pool = []
+    for _ in range(int(rng.integers(2, 7))):
+        if rng.random() < 0.2:
+            pool.append(p.int_var(-2.0, 3.0))
+        else:
+            lo = float(rng.uniform(-5.0, 1.0))
+            pool.append(p.var(lo, lo + float(rng.uniform(0.5, 6.0))))
+    n_vars = len(pool)
+    g = p.graph
+    for _ in range(int(rng.integers(10, 60))):
+        a, b = pool[int(rng.integers(len(pool)))], pool[int(rng.integers(len(pool)))]
+        c = float(np.round(rng.normal() * 3.0, 3)) or 1.5
+        kind = int(rng.integers(0, 14))
+        e = (a + b if kind == 0 else a - b if kind == 1 else a * b if kind == 2 else a / b if kind == 3
+             else sqr(a) if kind == 4 else -a if kind == 5 else sqrt(a) if kind == 6
+             else pow(a, int(rng.integers(-3, 5))) if kind == 7
+             else Expr(g, g.emit(A.OP_ABS, (a.id,))) if kind == 8
+             else Expr(g, g.emit(A.OP_MIN, (a.id, b.id))) if kind == 9
+             else Expr(g, g.emit(A.OP_MAX, (a.id, b.id))) if kind == 10
+             else c * a if kind == 11 else a + c if kind == 12 else None)
+        if e is None:  # a sum chain over the variables, from an earlier node
+            e = pool[int(rng.integers(len(pool)))]
+            for _ in range(int(rng.integers(1, 5))):
+                xi, xj = pool[int(rng.integers(n_vars))], pool[int(rng.integers(n_vars))]
+                e = e + float(np.round(rng.normal() * 3.0, 3) or 0.5) * (xi * xj)
+        pool.append(e)
+    p.set_objective(pool[-1])
+    for _ in range(int(rng.integers(0, 4))):
+        root = pool[int(rng.integers(n_vars, len(pool)))]
+        p.add_constraint(root, A.CMP_LE if rng.random() < 0.7 else A.CMP_EQ, float(rng.normal() * 5.0))
+    return p
+
+
+@pytest.mark.parametrize("fp32", [False, True], ids=["fp64", "fp32"])
+def test_random_dags_match_node_by_node(fp32):
+    for seed in range(60):
+        p = random_problem(seed)
+        assert mismatches(p, compile_program(p, int(fp32)), 100, seed=seed, scale=0.4, fp32=fp32) == 0, seed

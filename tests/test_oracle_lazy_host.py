@@ -69,6 +69,38 @@ def test_incremental_fp32_bounds_enclose_fp64(n_vars, seed):
         assert not np.any(fe64.astype(bool) & ~fe32.astype(bool))
 
 
+def test_incremental_fp32_bounds_enclose_fp64_on_random_shapes():
+    # the same soundness over random QCQP shapes: sizes, densities, integer
+    # shares and constraint counts the three workloads do not cover
+    rng = np.random.default_rng(2024)
+    checked = 0
+    for seed in range(30):
+        n = int(rng.integers(2, 21))
+        spec = G.QCQPSpec(n=n, m=int(rng.integers(0, 7)), n_int=int(rng.integers(0, n // 2 + 1)), int_lb=-3,
+                          int_ub=4, cont_lb=-6.0, cont_ub=6.0, q_density=float(rng.uniform(0.1, 1.0)),
+                          a_density=float(rng.uniform(0.1, 1.0)), rhs=(1.0, 10.0))
+        p = G.qcqp(spec, G.seed_for(20, seed))
+        op = O.OracleProblem(p)
+        if not op.set_program32(compile_program(p, 1)):
+            continue
+        root = np.array(p.box_bounds)
+        ints = np.array(p.var_kinds) != A.VAR_CONTINUOUS
+        for _ in range(3):
+            c = rng.uniform(root[:, 0], root[:, 1])
+            w = (root[:, 1] - root[:, 0]) * rng.uniform(0.01, 0.5)
+            lo, hi = np.maximum(c - w, root[:, 0]), np.minimum(c + w, root[:, 1])
+            lo[ints], hi[ints] = np.ceil(lo[ints]), np.maximum(np.floor(hi[ints]), np.ceil(lo[ints]))
+            box = np.stack([lo, hi], 1).reshape(-1)
+            kinds, vids, widths, _ = O.bisection_choose(box, p.var_kinds, int(rng.integers(1, 7)))
+            k = int(np.prod(widths))
+            fe32, lb32, _ = op.bound_inc32(box, kinds, vids, widths, k)
+            fe64, lb64 = op.bound(box, kinds, vids, widths, k)
+            assert np.all(lb32 <= lb64), seed
+            assert not np.any(fe64.astype(bool) & ~fe32.astype(bool)), seed
+            checked += 1
+    assert checked >= 60
+
+
 def lazy_cases():
     fx = fixture_problems()
     for name in ("square_le5", "infeasible", "int_eq", "miqcqp_n6"):

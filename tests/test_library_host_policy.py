@@ -2,8 +2,8 @@
 (cmn_bisection_choose: the device policy of csrc/policy.cuh compiled for the
 host; cmn_slot_bounds: the FMA-form decode) against the golden fixtures
 generated from the reference's own BisectionBudgetCompositionPolicy::choose
-(policy/bisection_budget.hpp) and decode::slot_bounds (region/decode.hpp).
-No GPU."""
+(policy/bisection_budget.hpp) and decode::slot_bounds (region/decode.hpp),
+and against the oracle's restatements of both on random inputs.  No GPU."""
 
 from __future__ import annotations
 
@@ -71,3 +71,19 @@ def test_library_policy_matches_oracle_on_random_boxes():
         k, v, w, d = oracle_choose(box, kinds, B, max_cycle, cap, rel)
         assert (a.kinds, a.var_ids, a.widths, a.domains) == (list(map(int, k)), list(map(int, v)),
                                                              list(map(int, w)), list(map(int, d))), (box, kinds, B)
+
+
+def test_library_decode_matches_oracle_on_random_parts():
+    from oracle import slot_bounds as oracle_bounds
+    rng = np.random.default_rng(78)
+    for _ in range(20000):
+        kind = int(rng.integers(0, 4))
+        if kind == 0:
+            plo = float(rng.uniform(-1e3, 1e3))
+            phi = plo + float(rng.choice([0.0, rng.uniform(0, 1e-6), rng.uniform(0, 1e3)]))
+        else:
+            plo = float(rng.integers(-50, 50))
+            phi = plo + float(rng.integers(0, 40))
+        fan = int(rng.integers(1, 65))
+        part = int(rng.integers(0, fan))
+        assert slot_bounds(kind, plo, phi, part, fan) == oracle_bounds(kind, plo, phi, part, fan), (kind, plo, phi)
